@@ -1,0 +1,376 @@
+/*
+ * wf_api.h — C ABI of the GB300 wavefront path tracer (libwfgpu.so).
+ *
+ * This is the drop-in boundary for the per-bounce loop of the CPU renderer
+ * fhidargue/wavefront-renderer.  Every entry point below names the reference
+ * interface it replaces (file:line in that project).  The reference has no
+ * FFI of its own: its loop is a set of C++ types and member functions
+ * (WavefrontRenderer, RayQueue, ShadingQueue, EmbreeAccelerator) compiled into
+ * one executable.  The C++17 mirror in `wf/wavefront.hpp` presents those types
+ * again on top of this ABI.
+ *
+ * Conventions
+ *  - Every function returns an int status: WF_OK (0) or a negative WF_ERR_*.
+ *    No C++ exception crosses the ABI.  wf_last_error() gives the message of
+ *    the last failure on a context (the reference reported errors through
+ *    exceptions caught in main, src/main.cpp:218-222).
+ *  - The library owns device memory behind opaque handles; the caller owns
+ *    every host buffer it passes.  Calls on one context are externally
+ *    serialised (one host thread per context); each context owns one CUDA
+ *    stream.
+ *  - Host arrays are plain pointers plus element counts.  Float columns are
+ *    IEEE binary32, index columns int32, exactly as the reference's
+ *    std::vector<float>/std::vector<int> columns.
+ */
+#ifndef WF_API_H
+#define WF_API_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define WF_API_VERSION 1
+
+/* ---- status codes ------------------------------------------------------ */
+#define WF_OK 0
+#define WF_ERR_INVALID_ARGUMENT (-1) /* null pointer, size out of range      */
+#define WF_ERR_CUDA (-2)             /* a CUDA runtime call failed            */
+#define WF_ERR_OUT_OF_MEMORY (-3)    /* device allocation or HBM budget       */
+#define WF_ERR_STATE (-4)            /* e.g. stage called before scene upload */
+#define WF_ERR_DEVICE_CHECK (-5)     /* a kernel's own bounds check tripped   */
+#define WF_ERR_NO_DEVICE (-6)        /* no CUDA device visible                */
+#define WF_ERR_CAPACITY (-7)         /* queue or static buffer too small      */
+
+/* ---- enums mirroring the reference ------------------------------------- */
+/* MaterialType, reference include/shading/Material.h:9-17 (same order). */
+enum {
+    WF_MATERIAL_DIFFUSE = 0,
+    WF_MATERIAL_METAL = 1,
+    WF_MATERIAL_EMISSIVE = 2,
+    WF_MATERIAL_SPOTLIGHT = 3,
+    WF_MATERIAL_GLASS = 4,
+    WF_MATERIAL_PLASTIC = 5
+};
+
+/* SchedulingPolicy, reference include/scheduling/ShadingQueue.h:18-24. */
+enum {
+    WF_POLICY_NONE = 0,
+    WF_POLICY_MATERIAL_AWARE = 1,
+    WF_POLICY_TEXTURE_AWARE = 2,
+    WF_POLICY_COST_BENEFIT_AWARE = 3
+};
+
+/* Texel formats.  RGB32F is the reference's Texture::pixels (linear float
+ * RGB, include/shading/Texture.h:19).  RGBA8_SRGB is an 8-bit source that the
+ * reference's Texture::load decodes with srgbToLinear (src/shading/Texture.cpp
+ * :20-27,47-53); the device keeps the bytes and decodes through a 256-entry
+ * table built on the host with that same formula, so sampled values agree bit
+ * for bit with the decoded float texture. */
+enum { WF_TEXEL_RGB32F = 0, WF_TEXEL_RGBA8_SRGB = 1 };
+
+/* ---- scene description --------------------------------------------------- */
+
+/* Material, reference include/shading/Material.h:19-41 without the uuid
+ * string.  48 bytes, the device layout as well. */
+typedef struct wf_material {
+    int32_t type;               /* WF_MATERIAL_*                          */
+    float albedo[3];            /* Material::albedo                       */
+    float roughness;            /* Material::roughness                    */
+    float emission;             /* Material::emission (strength)          */
+    int32_t texture_id;         /* Material::textureID, -1 = none         */
+    float ior;                  /* Material::indexOfRefraction            */
+    float spot_outer_deg;       /* Material::spotOuterAngle               */
+    float spot_falloff_deg;     /* Material::spotFalloffAngle             */
+    int32_t use_spatial_checker;/* Material::useSpatialChecker            */
+    float checker_cell_size;    /* Material::spatialCheckerCellSize       */
+} wf_material;
+
+/* Texture, reference include/shading/Texture.h:15-55. */
+typedef struct wf_texture {
+    int32_t width;
+    int32_t height;
+    int32_t format;   /* WF_TEXEL_*                                        */
+    const void* data; /* width*height texels, row-major (y*width + x)      */
+} wf_texture;
+
+/* EnvironmentMap, reference include/core/EnvironmentMap.h:7-24: equirect
+ * float RGB, nearest texel; width == 0 means "not loaded" and the miss path
+ * uses the gradient sky of WavefrontRenderer::getSkyColor (.cpp:879-888). */
+typedef struct wf_environment {
+    int32_t width;
+    int32_t height;
+    const float* rgb;        /* width*height*3 floats                     */
+    float intensity_scale;   /* EnvironmentMap::intensityScale            */
+    float tint[3];           /* EnvironmentMap::tint                      */
+} wf_environment;
+
+/* DirectionalLight, reference include/core/Scene.h:57-62. */
+typedef struct wf_directional_light {
+    float direction[3];
+    float color[3];
+    float intensity; /* 0 disables directional NEE (WavefrontRenderer.cpp:713) */
+} wf_directional_light;
+
+/* Scene, reference include/core/Scene.h:14-46 (SceneGeometry flat arrays)
+ * plus materials/textures/lights.  Mesh i owns indices
+ * [mesh_index_offsets[i], mesh_index_offsets[i] + mesh_index_counts[i]);
+ * its triangles are geomID i, primID 0.. in that order (the reference gives
+ * each Mesh its own Embree geometry, src/accelerator/Embree.cpp:77-113). */
+typedef struct wf_scene_desc {
+    int32_t num_vertices;
+    const float* positions_x;      /* SceneGeometry::allPositionsX        */
+    const float* positions_y;
+    const float* positions_z;
+    int32_t num_indices;           /* 3 per triangle                       */
+    const int32_t* indices;        /* SceneGeometry::allIndices (global)  */
+    int32_t num_meshes;
+    const int32_t* mesh_index_offsets; /* SceneGeometry::meshIndexOffsets */
+    const int32_t* mesh_index_counts;  /* SceneGeometry::meshIndexCounts  */
+    const int32_t* mesh_material_ids;  /* SceneGeometry::meshMaterialIDs  */
+    /* Mesh::triangleUVsU/V (include/geometry/Mesh.h:11-12), one value per
+     * triangle corner, aligned with indices[].  NULL when no mesh has UVs. */
+    const float* corner_u;
+    const float* corner_v;
+    const uint8_t* mesh_has_uv;    /* per mesh; NULL = none has UVs        */
+    int32_t num_materials;
+    const wf_material* materials;
+    int32_t num_textures;
+    const wf_texture* textures;
+    wf_environment environment;
+    wf_directional_light directional;
+} wf_scene_desc;
+
+/* Camera, reference include/core/Camera.h:6-41 (its four public fields). */
+typedef struct wf_camera {
+    float origin[3];
+    float top_left[3];
+    float horizontal[3];
+    float vertical[3];
+} wf_camera;
+
+/* ---- render parameters ---------------------------------------------------- */
+
+/* The public fields of WavefrontRenderer (include/render/WavefrontRenderer.h
+ * :19-34) that change the image, plus device-only batching fields. */
+typedef struct wf_render_params {
+    int32_t width;
+    int32_t height;
+    int32_t samples_per_pixel;     /* samplesPerPixel                       */
+    int32_t max_depth;             /* maxDepth                              */
+    int32_t rr_min_depth;          /* rrMinDepth (the reference fixes 3)    */
+    int32_t policy;                /* WF_POLICY_*                           */
+    int32_t enable_ray_sort;       /* enableRaySort                         */
+    int32_t enable_cost_aware_rr;  /* enableCostAwareRR (frozen costs)      */
+    float firefly_threshold;       /* fireflyThreshold (10)                 */
+    uint32_t seed_lo;              /* counter-based RNG key                 */
+    uint32_t seed_hi;
+    int32_t first_sample;          /* samples [first, first+spp) are drawn  */
+    int32_t spp_per_wave;          /* samples per wavefront; 0 = automatic  */
+    /* CostTracker::relativeCost per material / texture, frozen for the
+     * render (include/render/CostTracker.h:42-55).  NULL = 1.0 for all. */
+    const double* rel_cost_material;
+    const double* rel_cost_texture;
+    wf_camera camera;
+} wf_render_params;
+
+/* Counters of one render, mirroring the stat blocks of renderScene
+ * (WavefrontRenderer.cpp:317-389) plus ray counts. */
+typedef struct wf_render_stats {
+    uint64_t closest_rays;      /* closest-hit rays traced (all bounces)  */
+    uint64_t shadow_rays;       /* shadow (any-hit) rays traced           */
+    uint64_t shaded_hits;       /* total shaded hits                      */
+    uint64_t misses;            /* rays that left the scene               */
+    uint64_t sorted_elements;   /* keys sorted (ray sort + shade sort)    */
+    double ms_total;            /* device time of the render              */
+    double ms_ray_sort;         /* "Total ray sort time (ms)"             */
+    double ms_intersect;        /* "Total intersect time (ms)"            */
+    double ms_shade;            /* "Total shade time (ms)" incl. shadows  */
+    double ms_schedule;         /* ShadingQueue schedule + materialize    */
+    int32_t waves;              /* wavefronts launched                    */
+    int32_t bounces;            /* bounce iterations over all waves       */
+    int64_t kernel_launches;    /* kernels this library launched          */
+} wf_render_stats;
+
+/* ---- library / context ------------------------------------------------------- */
+
+typedef struct wf_ctx wf_ctx;
+
+typedef struct wf_config {
+    int32_t device;              /* CUDA ordinal                            */
+    int64_t max_paths_per_wave;  /* queue capacity; 0 = automatic           */
+} wf_config;
+
+/* Library version (WF_API_VERSION). */
+int wf_version(void);
+
+/* Creates a context on a device: stream, events, scratch.  Replaces the
+ * construction of WavefrontRenderer (include/render/WavefrontRenderer.h:36-39)
+ * and EmbreeAccelerator (src/accelerator/Embree.cpp:9-14). */
+int wf_create(const wf_config* config, wf_ctx** out_ctx);
+int wf_destroy(wf_ctx* ctx);
+/* Message of the last failing call on ctx ("" when none). */
+const char* wf_last_error(const wf_ctx* ctx);
+
+/* Camera::Camera(lookFrom, lookAt, up, vfov, w, h), include/core/Camera.h
+ * :13-33.  Host arithmetic only (no context needed). */
+int wf_camera_make(const float look_from[3], const float look_at[3], const float up[3],
+                   float vfov_degrees, int32_t image_width, int32_t image_height,
+                   wf_camera* out_camera);
+
+/* Uploads the scene and builds the device BVH (Morton/LBVH).  Replaces
+ * Scene::buildAccelerator (src/core/Scene.cpp:79-113) with
+ * EmbreeAccelerator::build (src/accelerator/Embree.cpp:66-119).  Bounds and
+ * the emissive-mesh list are derived exactly as the reference does. */
+int wf_scene_upload(wf_ctx* ctx, const wf_scene_desc* scene);
+
+/* Scene facts after upload: bounds (Scene::computeBounds, Scene.cpp:59-77),
+ * total emissive area (Scene::totalEmissiveArea, Scene.cpp:162-190), BVH
+ * node count and build time (EmbreeAccelerator::m_buildTimeMs). */
+typedef struct wf_scene_info {
+    float bounds_min[3];
+    float bounds_max[3];
+    float total_emissive_area;
+    int32_t num_triangles;
+    int32_t num_meshes;
+    int32_t num_emissive_meshes;
+    int32_t bvh_nodes;
+    double bvh_build_ms;
+    int64_t device_bytes;
+} wf_scene_info;
+int wf_scene_get_info(wf_ctx* ctx, wf_scene_info* out_info);
+
+/* ---- ray batches (host buffers) --------------------------------------------- */
+
+/* Closest hit of n rays, t in [tmin, tmax].  Replaces
+ * EmbreeAccelerator::intersect4 / intersect (src/accelerator/Embree.cpp
+ * :122-256) and the HitRecord they fill (include/core/HitRecord.h:6-22).
+ * Output columns (all length n, any may be NULL): geom_id (-1 on miss),
+ * prim_id (HitRecord::triangleIndex), distance, bary_u/bary_v (raw
+ * barycentrics), point xyz, normal xyz (face-forwarded), front_face, u/v
+ * (Mesh::interpolateUV), material_id, texture_id. */
+typedef struct wf_hit_columns {
+    int32_t* geom_id;
+    int32_t* prim_id;
+    float* distance;
+    float* bary_u;
+    float* bary_v;
+    float* point_x;
+    float* point_y;
+    float* point_z;
+    float* normal_x;
+    float* normal_y;
+    float* normal_z;
+    uint8_t* front_face;
+    float* u;
+    float* v;
+    int32_t* material_id;
+    int32_t* texture_id;
+} wf_hit_columns;
+int wf_trace_closest_host(wf_ctx* ctx, int64_t n, const float* origins_x,
+                          const float* origins_y, const float* origins_z, const float* dirs_x,
+                          const float* dirs_y, const float* dirs_z, float tmin, float tmax,
+                          wf_hit_columns* out);
+
+/* Any hit with t in [0.001, max_distance - 0.001].  Replaces
+ * EmbreeAccelerator::occluded (src/accelerator/Embree.cpp:258-280).
+ * out_occluded[i] = 1 when ray i is blocked. */
+int wf_trace_occluded_host(wf_ctx* ctx, int64_t n, const float* origins_x,
+                           const float* origins_y, const float* origins_z, const float* dirs_x,
+                           const float* dirs_y, const float* dirs_z, const float* max_distance,
+                           uint8_t* out_occluded);
+
+/* Camera rays of WavefrontRenderer::generatePrimaryRays (.cpp:401-457) for
+ * samples [first_sample, first_sample + nspp) of every pixel, jittered by the
+ * counter-based RNG keyed (seed, pixel, sample).  Output order: sample-major,
+ * then pixel (y*width + x).  Columns of length width*height*nspp. */
+int wf_generate_primary_host(wf_ctx* ctx, const wf_camera* camera, int32_t width,
+                             int32_t height, uint32_t seed_lo, uint32_t seed_hi,
+                             int32_t first_sample, int32_t nspp, float* origins_x,
+                             float* origins_y, float* origins_z, float* dirs_x, float* dirs_y,
+                             float* dirs_z, int32_t* pixel_indices, int32_t* sample_indices);
+
+/* ---- scheduling (host buffers) ---------------------------------------------- */
+
+/* RayQueue::sortKey + RayQueue::schedule (include/scheduling/RayQueue.h
+ * :135-179): key = octant << 30 | morton3(origin quantised to the scene
+ * bounds).  Writes the sort permutation (sortedIndices) and, if not NULL,
+ * the keys.  The permutation is that of a stable sort of the keys. */
+int wf_ray_schedule_host(wf_ctx* ctx, int64_t n, const float* origins_x,
+                         const float* origins_y, const float* origins_z, const float* dirs_x,
+                         const float* dirs_y, const float* dirs_z, const float bounds_min[3],
+                         const float bounds_max[3], int32_t* out_sorted_indices,
+                         uint64_t* out_keys);
+
+/* ShadingQueue::schedule (include/scheduling/ShadingQueue.h:90-141,277-329,
+ * 437-550) for one queue.  Inputs are the queue columns the policies read;
+ * texture_bytes[t] is Texture::memoryBytes() of texture t.  rel_cost_* are
+ * frozen CostTracker::relativeCost values (NULL = no tracker, i.e. 1.0 for
+ * materials and 0 texture cost, as the reference does with a null tracker).
+ * Writes sortedIndices: the permutation of a stable sort under the policy's
+ * comparator. */
+int wf_shading_schedule_host(wf_ctx* ctx, int32_t policy, int64_t n,
+                             const int32_t* material_ids, const int32_t* texture_ids,
+                             const float* throughputs_r, const float* throughputs_g,
+                             const float* throughputs_b, const float* hit_points_x,
+                             const float* hit_points_y, const float* hit_points_z,
+                             int32_t num_materials, const wf_material* materials,
+                             int32_t num_textures, const int64_t* texture_bytes,
+                             const double* rel_cost_material, const double* rel_cost_texture,
+                             int32_t* out_sorted_indices);
+
+/* ---- full render -------------------------------------------------------------- */
+
+/* WavefrontRenderer::renderScene (src/render/WavefrontRenderer.cpp:94-399)
+ * with adaptive sampling off: renders samples_per_pixel samples of every
+ * pixel and writes the averaged image (accumulator / spp, the reference's
+ * writeAveragedImage) to image_rgb (width*height*3 floats, host memory).
+ * The scene must have been uploaded.  stats may be NULL. */
+int wf_render(wf_ctx* ctx, const wf_render_params* params, float* image_rgb,
+              wf_render_stats* stats);
+
+/* Same loop, but leaves the per-pixel sums (not divided by spp) on the
+ * device and returns them in accum_rgb (host) — the form used to merge
+ * batches of samples. */
+int wf_render_accumulate(wf_ctx* ctx, const wf_render_params* params, float* accum_rgb,
+                         wf_render_stats* stats);
+
+/* Same loop; the averaged image stays in a context-owned device buffer
+ * (no host copy) until wf_image_download.  The form a resident render
+ * service uses between progressive frames. */
+int wf_render_device(wf_ctx* ctx, const wf_render_params* params, wf_render_stats* stats);
+/* Copies the image of the last wf_render_device (width*height*3 floats). */
+int wf_image_download(wf_ctx* ctx, float* image_rgb, int64_t num_floats);
+
+/* The context's CUDA stream (a cudaStream_t), so a caller can record its own
+ * events around library calls. */
+int wf_get_stream(wf_ctx* ctx, void** out_stream);
+
+/* CUDA-event timer on the context's stream: wf_timer_begin records the start
+ * event, wf_timer_end records the stop event, waits for it and returns the
+ * elapsed device time in milliseconds. */
+int wf_timer_begin(wf_ctx* ctx);
+int wf_timer_end(wf_ctx* ctx, double* out_ms);
+
+/* ---- procedural scenes (host only) ------------------------------------------- */
+
+/* The synthetic workloads that stand in for the reference's stress scenes:
+ *   0  Cornell box, 0.55 m, 36 triangles in 18 meshes (one per quad, as the
+ *      reference's CornellBox::addQuad/addRotatedBox build it)
+ *   1  config-0 room plus a displaced icosphere (subdivision 8, 1,310,720
+ *      triangles) split into Lambert / metal / glass regions
+ * The scene owns its arrays until wf_host_scene_free. */
+typedef struct wf_host_scene wf_host_scene;
+int wf_host_scene_generate(int32_t config, uint64_t seed, wf_host_scene** out_scene);
+int wf_host_scene_describe(const wf_host_scene* scene, wf_scene_desc* out_desc);
+/* The camera the workload is rendered with at the given image size. */
+int wf_host_scene_camera(const wf_host_scene* scene, int32_t width, int32_t height,
+                         wf_camera* out_camera);
+int wf_host_scene_free(wf_host_scene* scene);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* WF_API_H */

@@ -1,0 +1,320 @@
+"""Parity of the CUDA path (through the C ABI) with the CPU oracle.
+
+Integer and index results are compared bit for bit; float results of basic
+IEEE arithmetic (camera rays, Moller-Trumbore t, hit points, Morton keys) are
+compared bit for bit as well, because the device build uses no fused
+multiply-add (-fmad=false).  Rendered images use the same random streams on
+both sides, so they agree pixel by pixel except where a transcendental
+(cosf, sinf, powf: CUDA's and glibc's differ in the last ulp) nudges a path;
+the tolerance for that is written in each test.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import rays_in_box
+
+pytestmark = pytest.mark.gpu
+
+HIT_KEYS_EXACT = ["prim_id", "material_id", "texture_id", "front_face", "distance", "point_x", "point_y",
+                  "point_z", "normal_x", "normal_y", "normal_z", "u", "v"]
+
+
+def _od(cols):
+    o = np.stack([cols["ox"], cols["oy"], cols["oz"]], 1)
+    d = np.stack([cols["dx"], cols["dy"], cols["dz"]], 1)
+    return o, d
+
+
+def test_camera_rays_bit_exact(wf, orc, ctx, scene0):
+    """generatePrimaryRays + Camera::getRay, same Philox jitter: all columns equal."""
+    W, H = 256, 256
+    cam = scene0.camera(W, H)
+    g = ctx.generate_primary(cam, W, H, seed=0x1234_5678_9ABC, first_sample=5, nspp=2)
+    c = orc.generate_primary(cam, W, H, 0x1234_5678_9ABC, 5, 2)
+    for k in ("ox", "oy", "oz", "dx", "dy", "dz", "pixel", "sample"):
+        assert np.array_equal(g[k], c[k]), k
+
+
+@pytest.mark.parametrize("which", ["c0", "small"])
+def test_trace_closest_matches_oracle(wf, orc, ctx, scene0, scene_small, which):
+    scene = scene0 if which == "c0" else scene_small
+    ctx.upload(scene.desc)
+    port = orc.Port(scene.desc)
+    rng = np.random.default_rng(11)
+    cam = scene.camera(128, 128)
+    prim = orc.generate_primary(cam, 128, 128, 3, 0, 1)
+    o1, d1 = _od(prim)
+    o2, d2 = rays_in_box(rng, 50000, [-0.27, 0.01, -0.54], [0.27, 0.54, -0.01])
+    o = np.concatenate([o1, o2])
+    d = np.concatenate([d1, d2])
+    g = ctx.trace_closest(o, d)
+    c = port.trace_closest(o, d)
+    hit = c["prim_id"] >= 0
+    assert hit.mean() > 0.5
+    # geomID: the GPU reports it; the oracle's geom id is the mesh index too
+    assert np.array_equal(g["geom_id"], c["geom_id"])
+    for k in HIT_KEYS_EXACT:
+        assert np.array_equal(g[k][hit], c[k][hit]), k
+    assert np.array_equal(g["prim_id"] < 0, ~hit)
+
+
+def test_trace_closest_equals_brute_force(wf, orc, ctx, scene0):
+    """The BVH result equals the reference's brute-force Scene::hit order."""
+    ctx.upload(scene0.desc)
+    port = orc.Port(scene0.desc)
+    rng = np.random.default_rng(5)
+    o, d = rays_in_box(rng, 20000, [-0.27, 0.01, -0.54], [0.27, 0.54, -0.01])
+    g = ctx.trace_closest(o, d)
+    b = port.trace_closest(o, d, brute=True)
+    assert np.array_equal(g["prim_id"], b["prim_id"])
+    assert np.array_equal(g["geom_id"], b["geom_id"])
+    assert np.array_equal(g["distance"], b["distance"])
+
+
+def test_trace_closest_t_range(wf, orc, ctx, scene0):
+    """tmin / tmax cut-offs (EmbreeTest HitBeyondMaxDistanceReturnsFalse)."""
+    ctx.upload(scene0.desc)
+    port = orc.Port(scene0.desc)
+    rng = np.random.default_rng(8)
+    o, d = rays_in_box(rng, 4000, [-0.27, 0.01, -0.54], [0.27, 0.54, -0.01])
+    for tmin, tmax in [(0.001, 0.05), (0.1, 0.3), (0.0, 1e9)]:
+        g = ctx.trace_closest(o, d, tmin, tmax)
+        c = port.trace_closest(o, d, tmin, tmax)
+        assert np.array_equal(g["prim_id"], c["prim_id"])
+        assert np.array_equal(g["distance"], c["distance"])
+
+
+def test_trace_occluded_matches_oracle(wf, orc, ctx, scene_small):
+    ctx.upload(scene_small.desc)
+    port = orc.Port(scene_small.desc)
+    rng = np.random.default_rng(2)
+    o, d = rays_in_box(rng, 40000, [-0.27, 0.01, -0.54], [0.27, 0.54, -0.01])
+    maxd = rng.uniform(0.002, 0.8, size=40000).astype(np.float32)
+    g = ctx.trace_occluded(o, d, maxd)
+    c = port.trace_occluded(o, d, maxd)
+    assert np.array_equal(g, c)
+    assert 0.05 < g.mean() < 0.95
+
+
+def test_embree_known_answers_on_gpu(wf, ctx):
+    """tests/accelerator/EmbreeTest.cpp cases, run through the GPU."""
+    def quad_scene(verts, mats):
+        pass
+
+    # single quad at z = -1 (EmbreeTest buildSingleQuadScene)
+    px = np.array([-1, 1, 1, -1], np.float32)
+    py = np.array([-1, -1, 1, 1], np.float32)
+    pz = np.array([-1, -1, -1, -1], np.float32)
+    idx = np.array([0, 1, 2, 0, 2, 3], np.int32)
+    desc, keep = _desc(wf, [(px, py, pz, idx, 0)], [wf.WfMaterial(type=0, albedo=(0.8, 0.8, 0.8), texture_id=-1)])
+    ctx.upload(desc)
+    o = np.array([[0, 0, 0], [0, 0, 0], [5, 5, 0]], np.float32)
+    d = np.array([[0, 0, -1], [0, 0, 1], [0, 0, -1]], np.float32)
+    h = ctx.trace_closest(o, d)
+    assert h["prim_id"][0] >= 0 and abs(h["distance"][0] - 1.0) < 1e-3
+    assert h["material_id"][0] == 0 and h["normal_z"][0] > 0 and h["front_face"][0] == 1
+    assert h["prim_id"][1] == -1 and h["prim_id"][2] == -1
+    h = ctx.trace_closest(o[:1], d[:1], 0.001, 0.5)
+    assert h["prim_id"][0] == -1
+    # nearest of two meshes (MultiMeshSceneHitsCorrectMaterial)
+    tri = np.array([0, 1, 2], np.int32)
+    A = (np.array([-1, 1, 0], np.float32), np.array([-1, -1, 1], np.float32), np.full(3, -2, np.float32), tri, 0)
+    B = (np.array([-1, 1, 0], np.float32), np.array([-1, -1, 1], np.float32), np.full(3, -1, np.float32), tri, 1)
+    mats = [wf.WfMaterial(type=0, albedo=(1, 0, 0), texture_id=-1), wf.WfMaterial(type=0, albedo=(0, 1, 0), texture_id=-1)]
+    desc, keep = _desc(wf, [A, B], mats)
+    ctx.upload(desc)
+    h = ctx.trace_closest(o[:1], d[:1])
+    assert h["material_id"][0] == 1 and abs(h["distance"][0] - 1.0) < 1e-2
+    # empty scene (EmptySceneReturnsNoHit)
+    desc, keep = _desc(wf, [], mats)
+    ctx.upload(desc)
+    assert ctx.trace_closest(o[:1], d[:1])["prim_id"][0] == -1
+    assert ctx.trace_occluded(o[:1], d[:1], np.array([10.0], np.float32))[0] == 0
+
+
+def _desc(wf, meshes, materials):
+    """Flat scene description from (px, py, pz, local indices, material) meshes."""
+    px, py, pz, idx, off, cnt, mat = [], [], [], [], [], [], []
+    base = 0
+    for (x, y, z, i, m) in meshes:
+        off.append(sum(len(a) for a in idx))
+        cnt.append(len(i))
+        idx.append(np.asarray(i, np.int32) + base)
+        px.append(x); py.append(y); pz.append(z)
+        mat.append(m)
+        base += len(x)
+    cat = lambda L, t: np.ascontiguousarray(np.concatenate(L) if L else np.zeros(0, t), dtype=t)
+    arrs = dict(px=cat(px, np.float32), py=cat(py, np.float32), pz=cat(pz, np.float32),
+                idx=cat(idx, np.int32), off=np.array(off, np.int32), cnt=np.array(cnt, np.int32),
+                mat=np.array(mat, np.int32))
+    marr = (wf.WfMaterial * len(materials))(*materials)
+    import ctypes as C
+    d = wf.WfSceneDesc()
+    d.num_vertices = len(arrs["px"])
+    d.positions_x, d.positions_y, d.positions_z = wf.ptr(arrs["px"]), wf.ptr(arrs["py"]), wf.ptr(arrs["pz"])
+    d.num_indices = len(arrs["idx"])
+    d.indices = wf.ptr(arrs["idx"], C.c_int32)
+    d.num_meshes = len(meshes)
+    d.mesh_index_offsets = wf.ptr(arrs["off"], C.c_int32)
+    d.mesh_index_counts = wf.ptr(arrs["cnt"], C.c_int32)
+    d.mesh_material_ids = wf.ptr(arrs["mat"], C.c_int32)
+    d.num_materials = len(materials)
+    d.materials = marr
+    d.environment.intensity_scale = 1.0
+    return d, (arrs, marr)
+
+
+def test_ray_schedule_matches_oracle(wf, orc, ctx):
+    rng = np.random.default_rng(21)
+    n = 100_000
+    o = rng.uniform(-12, 12, size=(n, 3)).astype(np.float32)  # some outside the bounds (clamped)
+    d = rng.normal(size=(n, 3)).astype(np.float32)
+    d[:500, 0] = 0.0  # +0 direction components go to the positive octant
+    o[1000:1500] = o[1000]  # identical keys: the stable order must hold
+    bmin, bmax = np.array([-10, -10, -10], np.float32), np.array([10, 10, 10], np.float32)
+    perm, keys = ctx.ray_schedule(o, d, bmin, bmax)
+    assert np.array_equal(keys, orc.ray_sort_keys(o, d, bmin, bmax))
+    assert np.array_equal(perm, orc.ray_schedule(o, d, bmin, bmax))
+    # flat scene: zero extent on an axis (SceneTest RayQueueScheduleDoesNotDivideByZeroOnFlatScene)
+    bmin2, bmax2 = np.array([-1, -1, 0], np.float32), np.array([1, 1, 0], np.float32)
+    perm2, _ = ctx.ray_schedule(o[:1000], d[:1000], bmin2, bmax2)
+    assert np.array_equal(perm2, orc.ray_schedule(o[:1000], d[:1000], bmin2, bmax2))
+
+
+def test_ray_schedule_known_answers(wf, ctx):
+    """tests/scheduling/RayQueueTest.cpp:132-171 through the GPU."""
+    bmin, bmax = np.array([-10, -10, -10], np.float32), np.array([10, 10, 10], np.float32)
+    o = np.zeros((4, 3), np.float32)
+    d = np.array([[1, 1, 1], [-1, -1, -1], [1, 1, 1], [-1, -1, -1]], np.float32)
+    perm, _ = ctx.ray_schedule(o, d, bmin, bmax)
+    pix = np.array([10, 20, 11, 21])[perm]
+    assert sorted(pix[:2]) in ([10, 11], [20, 21]) and sorted(pix[2:]) in ([10, 11], [20, 21])
+    o = np.array([[5, 0, 0], [-5, 0, 0], [0, 0, 0]], np.float32)
+    d = np.tile(np.array([[0, 0, 1]], np.float32), (3, 1))
+    perm, _ = ctx.ray_schedule(o, d, bmin, bmax)
+    assert list(np.array([100, 200, 300])[perm]) == [200, 300, 100]
+
+
+def _materials(wf):
+    mk = wf.WfMaterial
+    return [mk(type=0, albedo=(1, 1, 1), roughness=1, texture_id=-1),
+            mk(type=1, albedo=(1, 1, 1), roughness=0.5, texture_id=-1),
+            mk(type=2, albedo=(1, 1, 1), emission=1, texture_id=-1),
+            mk(type=3, albedo=(1, 1, 1), emission=1, spot_outer_deg=45, spot_falloff_deg=30, texture_id=-1),
+            mk(type=4, albedo=(1, 1, 1), ior=1.5, texture_id=-1),
+            mk(type=5, albedo=(1, 1, 1), roughness=0.5, texture_id=-1)]
+
+
+def test_shading_schedule_known_answers(wf, ctx):
+    """tests/scheduling/ShadingQueueTest.cpp:73-200 through the GPU."""
+    mats = _materials(wf)
+    tb = np.array([12, 48, 192], np.int64)  # Texture(1,1), (2,2), (4,4) memoryBytes
+    def run(policy, mids, tids=None):
+        n = len(mids)
+        tids = np.zeros(n, np.int32) if tids is None else np.asarray(tids, np.int32)
+        return ctx.shading_schedule(policy, np.asarray(mids, np.int32), tids, np.ones((n, 3), np.float32),
+                                    np.zeros((n, 3), np.float32), mats, tb)
+    m = np.array([2, 0, 1])
+    assert list(m[run(0, m)]) == [2, 0, 1]          # none keeps arrival order
+    assert list(m[run(1, m)]) == [2, 1, 0]          # material: ties -> higher type first
+    m = np.array([1, 0, 1, 0, 1])
+    assert list(m[run(1, m)]) == [1, 1, 1, 0, 0]    # grouping by count
+    t = np.array([0, 2, 1])
+    assert list(t[run(2, [0, 1, 0], t)]) == [2, 1, 0]  # texture bytes descending
+    assert list(run(1, [5])) == [0]
+    assert list(np.array([42, 99])[run(1, [1, 0])]) == [42, 99]
+
+
+@pytest.mark.parametrize("policy", [0, 1, 2, 3])
+def test_shading_schedule_matches_oracle(wf, orc, ctx, policy):
+    rng = np.random.default_rng(100 + policy)
+    mk = wf.WfMaterial
+    types = [0, 1, 4, 5, 0, 1, 4, 2, 0, 5, 1, 3]
+    mats = [mk(type=t, albedo=(0.5, 0.5, 0.5), roughness=0.3, emission=1.0, ior=1.5,
+               texture_id=(i % 5 if i % 3 else -1)) for i, t in enumerate(types)]
+    tex_bytes = np.array([12 * 512 * 512, 12 * 256 * 256, 12 * 512 * 512, 12 * 64 * 64, 0], np.int64)
+    n = 30000
+    mids = rng.integers(0, len(mats), n).astype(np.int32)
+    tids = np.array([mats[m].texture_id for m in mids], np.int32)
+    tids[rng.random(n) < 0.1] = -1  # queue texture ids need not match the material
+    thr = rng.uniform(0, 1, size=(n, 3)).astype(np.float32)
+    thr[rng.random(n) < 0.2] = 1.0
+    pts = rng.uniform(-3, 3, size=(n, 3)).astype(np.float32)
+    ids = rng.integers(0, len(mats), 4000)
+    rc_mat = orc.cost_tracker_relative(len(mats), ids, rng.uniform(10, 50, 4000))
+    rc_tex = orc.cost_tracker_relative(5, rng.integers(0, 5, 600), rng.uniform(5, 9, 600))
+    g = ctx.shading_schedule(policy, mids, tids, thr, pts, mats, tex_bytes, rc_mat, rc_tex)
+    c = orc.shading_schedule(policy, mids, tids, thr, pts, mats, tex_bytes, rc_mat, rc_tex)
+    assert np.array_equal(g, c)
+    assert sorted(g) == list(range(n))
+
+
+def _mean_close(a, b, rel):
+    ma, mb = a.mean(axis=(0, 1)), b.mean(axis=(0, 1))
+    return np.all(np.abs(ma - mb) <= rel * np.abs(mb))
+
+
+@pytest.mark.parametrize("which", ["c0", "small"])
+def test_render_matches_oracle_paths(wf, orc, ctx, scene0, scene_small, which):
+    """Same seed, same random streams: pixels agree except where a
+    transcendental's last ulp moves a path.  Tolerance: 98% of pixels within
+    1e-3 relative + 1e-4 absolute, channel means within 1%."""
+    scene = scene0 if which == "c0" else scene_small
+    ctx.upload(scene.desc)
+    port = orc.Port(scene.desc)
+    W = H = 64
+    spp = 8
+    cam = scene.camera(W, H)
+    p = wf.render_params(W, H, spp, 8 if which == "c0" else 12, cam, seed=99)
+    img, st = ctx.render(p)
+    acc, cnt = port.render_window(p, 0, 0, W, H)
+    ref = acc / spp
+    agree = np.isclose(img, ref, rtol=1e-3, atol=1e-4).all(axis=2).mean()
+    assert agree >= 0.98, agree
+    assert _mean_close(img, ref, 0.01)
+    assert st["closest_rays"] == cnt["closest_rays"] or abs(st["closest_rays"] - cnt["closest_rays"]) < 0.01 * cnt["closest_rays"]
+
+
+def test_render_is_order_independent(wf, ctx, scene_small):
+    """Ray sort, policies and wave size change only the order of work: with
+    path-keyed random streams the image is the same up to float-add order
+    (atomic accumulation); tolerance 1e-4 relative on 99.9% of pixels."""
+    ctx.upload(scene_small.desc)
+    W = H = 48
+    cam = scene_small.camera(W, H)
+    base, _ = ctx.render(wf.render_params(W, H, 8, 12, cam, seed=5))
+    for kw in [dict(ray_sort=True), dict(policy=1), dict(policy=2), dict(policy=3), dict(spp_per_wave=3)]:
+        img, _ = ctx.render(wf.render_params(W, H, 8, 12, cam, seed=5, **kw))
+        agree = np.isclose(img, base, rtol=1e-4, atol=1e-6).all(axis=2).mean()
+        assert agree >= 0.999, (kw, agree)
+
+
+def test_render_accumulate_and_device_paths(wf, ctx, scene0):
+    ctx.upload(scene0.desc)
+    W = H = 32
+    cam = scene0.camera(W, H)
+    p = wf.render_params(W, H, 4, 8, cam, seed=3)
+    img, _ = ctx.render(p)
+    acc, _ = ctx.render(p, accumulate=True)
+    assert np.allclose(acc / 4.0, img, rtol=1e-6, atol=1e-7)
+    st = ctx.render_device(p)
+    img2 = ctx.image_download(W, H)
+    assert np.allclose(img2, img, rtol=1e-5, atol=1e-6)
+    assert st["kernel_launches"] > 0
+
+
+def test_errors_are_reported(wf, ctx, scene0):
+    ctx.upload(scene0.desc)
+    cam = scene0.camera(8, 8)
+    with pytest.raises(wf.WfError):
+        ctx.render(wf.render_params(1, 8, 1, 8, cam))
+    with pytest.raises(wf.WfError):
+        ctx.render(wf.render_params(8, 8, 0, 8, cam))
+    with pytest.raises(wf.WfError):
+        ctx.render(wf.render_params(8, 8, 1, 8, cam, policy=7))
+    c2 = wf.Context(0)
+    with pytest.raises(wf.WfError, match="STATE"):
+        c2.render(wf.render_params(8, 8, 1, 8, cam))
+    c2.close()

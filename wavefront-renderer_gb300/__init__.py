@@ -1,0 +1,412 @@
+"""Python bindings of libwfgpu.so (the C ABI in include/wf_api.h).
+
+The GB300 wavefront path tracer is a C ABI shared library; this module only
+loads it with ctypes and wraps the entry points with numpy-friendly calls.
+There is no Python or CPU fallback: if the library is missing or no CUDA
+device is visible, the calls raise.
+
+Import it by path (the directory name is not a Python identifier):
+
+    import importlib.util, pathlib
+    spec = importlib.util.spec_from_file_location(
+        "wavefront_gb300", pathlib.Path("wavefront-renderer_gb300/__init__.py"))
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+PKG_DIR = Path(__file__).resolve().parent
+LIB_PATH = PKG_DIR / "lib" / "libwfgpu.so"
+HEADER = PKG_DIR.parent / "include" / "wf_api.h"
+
+WF_OK = 0
+ERRORS = {
+    -1: "WF_ERR_INVALID_ARGUMENT",
+    -2: "WF_ERR_CUDA",
+    -3: "WF_ERR_OUT_OF_MEMORY",
+    -4: "WF_ERR_STATE",
+    -5: "WF_ERR_DEVICE_CHECK",
+    -6: "WF_ERR_NO_DEVICE",
+    -7: "WF_ERR_CAPACITY",
+}
+
+MATERIAL_DIFFUSE, MATERIAL_METAL, MATERIAL_EMISSIVE, MATERIAL_SPOTLIGHT, MATERIAL_GLASS, MATERIAL_PLASTIC = range(6)
+POLICY_NONE, POLICY_MATERIAL, POLICY_TEXTURE, POLICY_COST_BENEFIT = range(4)
+POLICIES = {"none": 0, "material": 1, "texture": 2, "costBenefit": 3}
+TEXEL_RGB32F, TEXEL_RGBA8_SRGB = 0, 1
+
+f32p = C.POINTER(C.c_float)
+i32p = C.POINTER(C.c_int32)
+u8p = C.POINTER(C.c_uint8)
+f64p = C.POINTER(C.c_double)
+i64p = C.POINTER(C.c_int64)
+u64p = C.POINTER(C.c_uint64)
+
+
+class WfMaterial(C.Structure):
+    _fields_ = [("type", C.c_int32), ("albedo", C.c_float * 3), ("roughness", C.c_float),
+                ("emission", C.c_float), ("texture_id", C.c_int32), ("ior", C.c_float),
+                ("spot_outer_deg", C.c_float), ("spot_falloff_deg", C.c_float),
+                ("use_spatial_checker", C.c_int32), ("checker_cell_size", C.c_float)]
+
+
+class WfTexture(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("format", C.c_int32), ("data", C.c_void_p)]
+
+
+class WfEnvironment(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("rgb", f32p),
+                ("intensity_scale", C.c_float), ("tint", C.c_float * 3)]
+
+
+class WfDirectional(C.Structure):
+    _fields_ = [("direction", C.c_float * 3), ("color", C.c_float * 3), ("intensity", C.c_float)]
+
+
+class WfSceneDesc(C.Structure):
+    _fields_ = [("num_vertices", C.c_int32), ("positions_x", f32p), ("positions_y", f32p),
+                ("positions_z", f32p), ("num_indices", C.c_int32), ("indices", i32p),
+                ("num_meshes", C.c_int32), ("mesh_index_offsets", i32p), ("mesh_index_counts", i32p),
+                ("mesh_material_ids", i32p), ("corner_u", f32p), ("corner_v", f32p),
+                ("mesh_has_uv", u8p), ("num_materials", C.c_int32), ("materials", C.POINTER(WfMaterial)),
+                ("num_textures", C.c_int32), ("textures", C.POINTER(WfTexture)),
+                ("environment", WfEnvironment), ("directional", WfDirectional)]
+
+
+class WfCamera(C.Structure):
+    _fields_ = [("origin", C.c_float * 3), ("top_left", C.c_float * 3), ("horizontal", C.c_float * 3),
+                ("vertical", C.c_float * 3)]
+
+    def as_array(self) -> np.ndarray:
+        return np.array([*self.origin, *self.top_left, *self.horizontal, *self.vertical], dtype=np.float32)
+
+
+class WfRenderParams(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("samples_per_pixel", C.c_int32),
+                ("max_depth", C.c_int32), ("rr_min_depth", C.c_int32), ("policy", C.c_int32),
+                ("enable_ray_sort", C.c_int32), ("enable_cost_aware_rr", C.c_int32),
+                ("firefly_threshold", C.c_float), ("seed_lo", C.c_uint32), ("seed_hi", C.c_uint32),
+                ("first_sample", C.c_int32), ("spp_per_wave", C.c_int32),
+                ("rel_cost_material", f64p), ("rel_cost_texture", f64p), ("camera", WfCamera)]
+
+
+class WfRenderStats(C.Structure):
+    _fields_ = [("closest_rays", C.c_uint64), ("shadow_rays", C.c_uint64), ("shaded_hits", C.c_uint64),
+                ("misses", C.c_uint64), ("sorted_elements", C.c_uint64), ("ms_total", C.c_double),
+                ("ms_ray_sort", C.c_double), ("ms_intersect", C.c_double), ("ms_shade", C.c_double),
+                ("ms_schedule", C.c_double), ("waves", C.c_int32), ("bounces", C.c_int32),
+                ("kernel_launches", C.c_int64)]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+class WfConfig(C.Structure):
+    _fields_ = [("device", C.c_int32), ("max_paths_per_wave", C.c_int64)]
+
+
+class WfSceneInfo(C.Structure):
+    _fields_ = [("bounds_min", C.c_float * 3), ("bounds_max", C.c_float * 3),
+                ("total_emissive_area", C.c_float), ("num_triangles", C.c_int32),
+                ("num_meshes", C.c_int32), ("num_emissive_meshes", C.c_int32), ("bvh_nodes", C.c_int32),
+                ("bvh_build_ms", C.c_double), ("device_bytes", C.c_int64)]
+
+
+class WfHitColumns(C.Structure):
+    _fields_ = [("geom_id", i32p), ("prim_id", i32p), ("distance", f32p), ("bary_u", f32p),
+                ("bary_v", f32p), ("point_x", f32p), ("point_y", f32p), ("point_z", f32p),
+                ("normal_x", f32p), ("normal_y", f32p), ("normal_z", f32p), ("front_face", u8p),
+                ("u", f32p), ("v", f32p), ("material_id", i32p), ("texture_id", i32p)]
+
+
+HIT_FIELDS = {"geom_id": np.int32, "prim_id": np.int32, "distance": np.float32, "bary_u": np.float32,
+              "bary_v": np.float32, "point_x": np.float32, "point_y": np.float32, "point_z": np.float32,
+              "normal_x": np.float32, "normal_y": np.float32, "normal_z": np.float32,
+              "front_face": np.uint8, "u": np.float32, "v": np.float32, "material_id": np.int32,
+              "texture_id": np.int32}
+
+
+def ptr(a: np.ndarray | None, ctype=C.c_float):
+    if a is None:
+        return None
+    assert a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(C.POINTER(ctype))
+
+
+def make_hit_columns(n: int):
+    cols = {k: np.zeros(n, dtype=t) for k, t in HIT_FIELDS.items()}
+    ct = {np.int32: C.c_int32, np.float32: C.c_float, np.uint8: C.c_uint8}
+    hc = WfHitColumns(**{k: ptr(v, ct[HIT_FIELDS[k]]) for k, v in cols.items()})
+    return cols, hc
+
+
+_lib = None
+
+
+def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
+    """Loads libwfgpu.so; raises if it has not been built."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise RuntimeError(f"{p} not built: run __graft_entry__.build() (nvcc, sm_103a)")
+    lib = C.CDLL(str(p))
+    _declare(lib)
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def _declare(lib: C.CDLL) -> None:
+    V = C.c_void_p
+    sig = {
+        "wf_version": ([], C.c_int),
+        "wf_create": ([C.POINTER(WfConfig), C.POINTER(V)], C.c_int),
+        "wf_destroy": ([V], C.c_int),
+        "wf_last_error": ([V], C.c_char_p),
+        "wf_camera_make": ([f32p, f32p, f32p, C.c_float, C.c_int32, C.c_int32, C.POINTER(WfCamera)], C.c_int),
+        "wf_scene_upload": ([V, C.POINTER(WfSceneDesc)], C.c_int),
+        "wf_scene_get_info": ([V, C.POINTER(WfSceneInfo)], C.c_int),
+        "wf_trace_closest_host": ([V, C.c_int64] + [f32p] * 6 + [C.c_float, C.c_float, C.POINTER(WfHitColumns)], C.c_int),
+        "wf_trace_occluded_host": ([V, C.c_int64] + [f32p] * 7 + [u8p], C.c_int),
+        "wf_generate_primary_host": ([V, C.POINTER(WfCamera), C.c_int32, C.c_int32, C.c_uint32, C.c_uint32,
+                                      C.c_int32, C.c_int32] + [f32p] * 6 + [i32p, i32p], C.c_int),
+        "wf_ray_schedule_host": ([V, C.c_int64] + [f32p] * 6 + [f32p, f32p, i32p, u64p], C.c_int),
+        "wf_shading_schedule_host": ([V, C.c_int32, C.c_int64, i32p, i32p] + [f32p] * 6 +
+                                     [C.c_int32, C.POINTER(WfMaterial), C.c_int32, i64p, f64p, f64p, i32p], C.c_int),
+        "wf_render": ([V, C.POINTER(WfRenderParams), f32p, C.POINTER(WfRenderStats)], C.c_int),
+        "wf_render_accumulate": ([V, C.POINTER(WfRenderParams), f32p, C.POINTER(WfRenderStats)], C.c_int),
+        "wf_render_device": ([V, C.POINTER(WfRenderParams), C.POINTER(WfRenderStats)], C.c_int),
+        "wf_image_download": ([V, f32p, C.c_int64], C.c_int),
+        "wf_get_stream": ([V, C.POINTER(V)], C.c_int),
+        "wf_timer_begin": ([V], C.c_int),
+        "wf_timer_end": ([V, f64p], C.c_int),
+        "wf_host_scene_generate": ([C.c_int32, C.c_uint64, C.POINTER(V)], C.c_int),
+        "wf_host_scene_describe": ([V, C.POINTER(WfSceneDesc)], C.c_int),
+        "wf_host_scene_camera": ([V, C.c_int32, C.c_int32, C.POINTER(WfCamera)], C.c_int),
+        "wf_host_scene_free": ([V], C.c_int),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+
+
+def header_symbols() -> list[str]:
+    """Every function the C header declares."""
+    import re
+    text = HEADER.read_text()
+    return sorted(set(re.findall(r"^(?:int|const char\*|void)\s+(wf_\w+)\s*\(", text, re.M)))
+
+
+class WfError(RuntimeError):
+    pass
+
+
+def _check(rc: int, what: str, ctx=None) -> None:
+    if rc != WF_OK:
+        msg = ""
+        if ctx is not None and ctx._h:
+            msg = (load_library().wf_last_error(ctx._h) or b"").decode()
+        raise WfError(f"{what} failed: {ERRORS.get(rc, rc)} {msg}")
+
+
+class HostScene:
+    """A procedural workload (wf_host_scene_*): 0 Cornell box, 1 icosphere
+    scene (1.31 M triangles), 100 the icosphere scene at subdivision 4."""
+
+    def __init__(self, config: int, seed: int = 1):
+        lib = load_library()
+        self._h = C.c_void_p()
+        _check(lib.wf_host_scene_generate(config, seed, C.byref(self._h)), "wf_host_scene_generate")
+        self.desc = WfSceneDesc()
+        _check(lib.wf_host_scene_describe(self._h, C.byref(self.desc)), "wf_host_scene_describe")
+        self.config = config
+
+    def camera(self, width: int, height: int) -> WfCamera:
+        cam = WfCamera()
+        _check(load_library().wf_host_scene_camera(self._h, width, height, C.byref(cam)), "camera")
+        return cam
+
+    def arrays(self) -> dict:
+        d = self.desc
+        nv, ni, nm = d.num_vertices, d.num_indices, d.num_meshes
+        return {
+            "px": np.ctypeslib.as_array(d.positions_x, (nv,)).copy(),
+            "py": np.ctypeslib.as_array(d.positions_y, (nv,)).copy(),
+            "pz": np.ctypeslib.as_array(d.positions_z, (nv,)).copy(),
+            "indices": np.ctypeslib.as_array(d.indices, (ni,)).copy(),
+            "mesh_offsets": np.ctypeslib.as_array(d.mesh_index_offsets, (nm,)).copy(),
+            "mesh_counts": np.ctypeslib.as_array(d.mesh_index_counts, (nm,)).copy(),
+            "mesh_materials": np.ctypeslib.as_array(d.mesh_material_ids, (nm,)).copy(),
+            "materials": [d.materials[i] for i in range(d.num_materials)],
+        }
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.wf_host_scene_free(self._h)
+            self._h = None
+
+
+def camera_make(look_from, look_at, up, vfov, width, height) -> WfCamera:
+    cam = WfCamera()
+    a = [np.asarray(v, dtype=np.float32) for v in (look_from, look_at, up)]
+    _check(load_library().wf_camera_make(ptr(a[0]), ptr(a[1]), ptr(a[2]), vfov, width, height, C.byref(cam)),
+           "wf_camera_make")
+    return cam
+
+
+def render_params(width, height, spp, max_depth, camera: WfCamera, *, policy=0, ray_sort=False,
+                  rr_min_depth=3, firefly=10.0, seed=1, first_sample=0, spp_per_wave=0,
+                  cost_aware_rr=False, rel_cost_material=None, rel_cost_texture=None) -> WfRenderParams:
+    p = WfRenderParams()
+    p.width, p.height, p.samples_per_pixel, p.max_depth = width, height, spp, max_depth
+    p.rr_min_depth, p.policy, p.enable_ray_sort = rr_min_depth, policy, int(bool(ray_sort))
+    p.enable_cost_aware_rr = int(bool(cost_aware_rr))
+    p.firefly_threshold = firefly
+    p.seed_lo, p.seed_hi = seed & 0xFFFFFFFF, (seed >> 32) & 0xFFFFFFFF
+    p.first_sample, p.spp_per_wave = first_sample, spp_per_wave
+    p._keep = []
+    if rel_cost_material is not None:
+        a = np.ascontiguousarray(rel_cost_material, dtype=np.float64)
+        p._keep.append(a)
+        p.rel_cost_material = ptr(a, C.c_double)
+    if rel_cost_texture is not None:
+        a = np.ascontiguousarray(rel_cost_texture, dtype=np.float64)
+        p._keep.append(a)
+        p.rel_cost_texture = ptr(a, C.c_double)
+    p.camera = camera
+    return p
+
+
+class Context:
+    """A device context (wf_create): one CUDA stream, a resident scene."""
+
+    def __init__(self, device: int = 0, max_paths_per_wave: int = 0):
+        lib = load_library()
+        self._h = C.c_void_p()
+        cfg = WfConfig(device, max_paths_per_wave)
+        rc = lib.wf_create(C.byref(cfg), C.byref(self._h))
+        _check(rc, "wf_create")
+
+    def close(self):
+        if self._h:
+            load_library().wf_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload(self, desc: WfSceneDesc) -> WfSceneInfo:
+        lib = load_library()
+        _check(lib.wf_scene_upload(self._h, C.byref(desc)), "wf_scene_upload", self)
+        info = WfSceneInfo()
+        _check(lib.wf_scene_get_info(self._h, C.byref(info)), "wf_scene_get_info", self)
+        return info
+
+    def trace_closest(self, o: np.ndarray, d: np.ndarray, tmin=0.001, tmax=1e9) -> dict:
+        o = np.ascontiguousarray(o, dtype=np.float32)
+        d = np.ascontiguousarray(d, dtype=np.float32)
+        n = o.shape[0]
+        cols, hc = make_hit_columns(n)
+        oc = [np.ascontiguousarray(o[:, k]) for k in range(3)]
+        dc = [np.ascontiguousarray(d[:, k]) for k in range(3)]
+        _check(load_library().wf_trace_closest_host(self._h, n, *[ptr(x) for x in oc + dc], tmin, tmax,
+                                                    C.byref(hc)), "wf_trace_closest_host", self)
+        return cols
+
+    def trace_occluded(self, o: np.ndarray, d: np.ndarray, maxd: np.ndarray) -> np.ndarray:
+        o = np.ascontiguousarray(o, dtype=np.float32)
+        d = np.ascontiguousarray(d, dtype=np.float32)
+        maxd = np.ascontiguousarray(maxd, dtype=np.float32)
+        n = o.shape[0]
+        out = np.zeros(n, dtype=np.uint8)
+        oc = [np.ascontiguousarray(o[:, k]) for k in range(3)]
+        dc = [np.ascontiguousarray(d[:, k]) for k in range(3)]
+        _check(load_library().wf_trace_occluded_host(self._h, n, *[ptr(x) for x in oc + dc], ptr(maxd),
+                                                     ptr(out, C.c_uint8)), "wf_trace_occluded_host", self)
+        return out
+
+    def generate_primary(self, cam: WfCamera, w: int, h: int, seed: int, first_sample: int, nspp: int) -> dict:
+        n = w * h * nspp
+        cols = {k: np.zeros(n, dtype=np.float32) for k in ("ox", "oy", "oz", "dx", "dy", "dz")}
+        pix = np.zeros(n, dtype=np.int32)
+        smp = np.zeros(n, dtype=np.int32)
+        _check(load_library().wf_generate_primary_host(
+            self._h, C.byref(cam), w, h, seed & 0xFFFFFFFF, (seed >> 32) & 0xFFFFFFFF, first_sample, nspp,
+            *[ptr(cols[k]) for k in ("ox", "oy", "oz", "dx", "dy", "dz")], ptr(pix, C.c_int32),
+            ptr(smp, C.c_int32)), "wf_generate_primary_host", self)
+        cols["pixel"], cols["sample"] = pix, smp
+        return cols
+
+    def ray_schedule(self, o, d, bmin, bmax):
+        o = np.ascontiguousarray(o, dtype=np.float32)
+        d = np.ascontiguousarray(d, dtype=np.float32)
+        n = o.shape[0]
+        out = np.zeros(n, dtype=np.int32)
+        keys = np.zeros(n, dtype=np.uint64)
+        bmin = np.asarray(bmin, dtype=np.float32)
+        bmax = np.asarray(bmax, dtype=np.float32)
+        oc = [np.ascontiguousarray(o[:, k]) for k in range(3)]
+        dc = [np.ascontiguousarray(d[:, k]) for k in range(3)]
+        _check(load_library().wf_ray_schedule_host(self._h, n, *[ptr(x) for x in oc + dc], ptr(bmin), ptr(bmax),
+                                                   ptr(out, C.c_int32), ptr(keys, C.c_uint64)),
+               "wf_ray_schedule_host", self)
+        return out, keys
+
+    def shading_schedule(self, policy, mat_ids, tex_ids, thr, pts, materials, texture_bytes,
+                         rel_cost_material=None, rel_cost_texture=None) -> np.ndarray:
+        mat_ids = np.ascontiguousarray(mat_ids, dtype=np.int32)
+        tex_ids = np.ascontiguousarray(tex_ids, dtype=np.int32)
+        thr = np.ascontiguousarray(thr, dtype=np.float32)
+        pts = np.ascontiguousarray(pts, dtype=np.float32)
+        n = mat_ids.shape[0]
+        out = np.zeros(n, dtype=np.int32)
+        marr = (WfMaterial * len(materials))(*materials)
+        tb = np.ascontiguousarray(texture_bytes, dtype=np.int64)
+        cols = [np.ascontiguousarray(thr[:, k]) for k in range(3)] + [np.ascontiguousarray(pts[:, k]) for k in range(3)]
+        rcm = None if rel_cost_material is None else np.ascontiguousarray(rel_cost_material, dtype=np.float64)
+        rct = None if rel_cost_texture is None else np.ascontiguousarray(rel_cost_texture, dtype=np.float64)
+        _check(load_library().wf_shading_schedule_host(
+            self._h, policy, n, ptr(mat_ids, C.c_int32), ptr(tex_ids, C.c_int32), *[ptr(c) for c in cols],
+            len(materials), marr, len(tb), ptr(tb, C.c_int64) if len(tb) else None,
+            ptr(rcm, C.c_double), ptr(rct, C.c_double), ptr(out, C.c_int32)), "wf_shading_schedule_host", self)
+        return out
+
+    def render_device(self, params: WfRenderParams) -> dict:
+        st = WfRenderStats()
+        _check(load_library().wf_render_device(self._h, C.byref(params), C.byref(st)), "wf_render_device", self)
+        return st.as_dict()
+
+    def image_download(self, width: int, height: int, out: np.ndarray | None = None) -> np.ndarray:
+        img = out if out is not None else np.zeros(width * height * 3, dtype=np.float32)
+        _check(load_library().wf_image_download(self._h, ptr(img), img.size), "wf_image_download", self)
+        return img.reshape(height, width, 3)
+
+    def timer_begin(self) -> None:
+        _check(load_library().wf_timer_begin(self._h), "wf_timer_begin", self)
+
+    def timer_end(self) -> float:
+        ms = C.c_double()
+        _check(load_library().wf_timer_end(self._h, C.byref(ms)), "wf_timer_end", self)
+        return ms.value
+
+    def stream(self) -> int:
+        s = C.c_void_p()
+        _check(load_library().wf_get_stream(self._h, C.byref(s)), "wf_get_stream", self)
+        return s.value or 0
+
+    def render(self, params: WfRenderParams, accumulate: bool = False):
+        img = np.zeros(params.width * params.height * 3, dtype=np.float32)
+        st = WfRenderStats()
+        fn = load_library().wf_render_accumulate if accumulate else load_library().wf_render
+        _check(fn(self._h, C.byref(params), ptr(img), C.byref(st)), "wf_render", self)
+        return img.reshape(params.height, params.width, 3), st.as_dict()

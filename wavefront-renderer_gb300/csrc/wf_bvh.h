@@ -1,0 +1,33 @@
+// wf_bvh.h — device BVH build (wf_bvh.cu).
+#pragma once
+
+#include <cstdint>
+#include <string>
+
+#include "wf_device.cuh"
+
+namespace wf {
+
+struct BvhBuildInput {
+    const float* px;           // device vertex positions
+    const float* py;
+    const float* pz;
+    const int32_t* idx;        // device indices, 3 per triangle (global)
+    const int32_t* tri_geom;   // device, per global triangle: mesh index
+    const int32_t* tri_prim;   // device, per global triangle: index in mesh
+    int32_t num_tris;
+    float bmin[3], bmax[3];    // vertex bounds (host values)
+};
+
+struct BvhBuildOutput {
+    float4* tris;      // 3 * num_tris float4 (cudaMalloc'd; caller frees)
+    BvhNode* nodes;    // num_nodes (cudaMalloc'd; caller frees)
+    int num_nodes;
+    int max_depth;
+};
+
+// Returns 0 on success, -1 with err set otherwise.
+int build_lbvh(const BvhBuildInput& in, BvhBuildOutput& out, int num_sms, cudaStream_t s,
+               std::string& err);
+
+}  // namespace wf

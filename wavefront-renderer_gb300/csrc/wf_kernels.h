@@ -1,0 +1,104 @@
+// wf_kernels.h — launchers of the render kernels (wf_render.cu).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "wf_device.cuh"
+
+namespace wf {
+
+using ull = unsigned long long;
+
+// Shading parameters fixed for one render (WavefrontRenderer public fields).
+struct ShadeParams {
+    uint32_t seed_lo, seed_hi;
+    float firefly;
+    int32_t rr_min_depth;
+    int32_t cost_aware_rr;
+    const float* rel_cost_material;  // device, float(relativeCost) per material, or null
+};
+
+struct LaunchCfg {
+    int grid;
+    int block;
+};
+
+// Camera rays of n = width*height*nspp paths, sample-major.
+void launch_camera(const wf_camera& cam, int width, int height, uint32_t seed_lo, uint32_t seed_hi,
+                   int first_sample, int nspp, RayQueueDev rq, cudaStream_t s);
+
+// Closest hit for the host API: per-ray HitRecord columns (device buffers).
+struct HitColumnsDev {
+    int32_t *geom, *prim;
+    float *t, *bu, *bv, *px, *py, *pz, *nx, *ny, *nz;
+    uint8_t* front;
+    float *u, *v;
+    int32_t *mat, *tex;
+};
+void launch_trace_api(const DeviceScene& S, int64_t n, const float* ox, const float* oy,
+                      const float* oz, const float* dx, const float* dy, const float* dz,
+                      float tmin, float tmax, HitColumnsDev out, int* err, LaunchCfg cfg,
+                      cudaStream_t s);
+void launch_occluded_api(const DeviceScene& S, int64_t n, const float* ox, const float* oy,
+                         const float* oz, const float* dx, const float* dy, const float* dz,
+                         const float* maxd, uint8_t* out, int* err, LaunchCfg cfg, cudaStream_t s);
+
+// Render loop stages.  Counts live in device memory.
+void launch_trace_render(const DeviceScene& S, RayQueueDev rq, const ull* d_n, HitQueueDev hq,
+                         ull* hq_n, float* accum, ull* work, int* err, LaunchCfg cfg,
+                         cudaStream_t s);
+void launch_shade(const DeviceScene& S, const ShadeParams& P, RayQueueDev rq, HitQueueDev hq,
+                  const ull* hq_n, ShadowQueueDev sh, ull* sh_n, RayQueueDev next, ull* next_n,
+                  float* accum, int* err, LaunchCfg cfg, cudaStream_t s);
+void launch_occluded_render(const DeviceScene& S, ShadowQueueDev sh, const ull* sh_n, float* accum,
+                            ull* work, int* err, LaunchCfg cfg, cudaStream_t s);
+
+// RayQueue::sortKey over the queue, (key, index) pairs for the radix sort.
+void launch_ray_keys(RayQueueDev rq, const ull* d_n, const float bmin[3], const float bmax[3],
+                     uint64_t* keys, uint32_t* vals, LaunchCfg cfg, cudaStream_t s);
+void launch_ray_keys_raw(int64_t n, const float* ox, const float* oy, const float* oz,
+                         const float* dx, const float* dy, const float* dz, const float bmin[3],
+                         const float bmax[3], uint64_t* keys, uint32_t* vals, LaunchCfg cfg,
+                         cudaStream_t s);
+// out[i] = in[perm[i]] for every column (RayQueue::materialize).
+void launch_gather_rays(RayQueueDev in, const uint32_t* perm, const ull* d_n, RayQueueDev out,
+                        LaunchCfg cfg, cudaStream_t s);
+
+// ShadingQueue scheduling on plain columns.
+struct ShadeColumnsDev {
+    const int32_t* mat;
+    const int32_t* tex;
+    const float *tr, *tg, *tb;
+    const float *px, *py, *pz;
+};
+// Per material type: hit count, texture bytes, first queue index.
+void launch_type_stats(ShadeColumnsDev c, const ull* d_n, const wf_material* mats, int num_tex,
+                       const int64_t* tex_bytes, ull* counts, ull* mem, int* first, LaunchCfg cfg,
+                       cudaStream_t s);
+// Material / texture policy keys: type_rank[type] << shift | secondary rank.
+void launch_policy_keys(ShadeColumnsDev c, const ull* d_n, const wf_material* mats, int policy,
+                        const int* type_rank8, const int* cost_rank, const int* tex_rank,
+                        int num_tex, int shift, uint64_t* keys, uint32_t* vals, LaunchCfg cfg,
+                        cudaStream_t s);
+// Cost-benefit: per material luminance sums and hit-point bounds.
+void launch_cb_reduce(ShadeColumnsDev c, const ull* d_n, double* benefit, int* present,
+                      unsigned* bounds6, LaunchCfg cfg, cudaStream_t s);
+void launch_cb_keys(ShadeColumnsDev c, const ull* d_n, const wf_material* mats,
+                    const int* prio_rank, int prio_bits, const unsigned* bounds6, uint64_t* keys,
+                    uint32_t* vals, LaunchCfg cfg, cudaStream_t s);
+// Columns of the render loop's hit queue for the schedulers.
+struct ShadeColumnsMut {
+    int32_t* mat;
+    int32_t* tex;
+    float *tr, *tg, *tb, *px, *py, *pz;
+};
+void launch_hit_columns(const DeviceScene& S, RayQueueDev rq, HitQueueDev hq, const ull* d_n,
+                        ShadeColumnsMut out, LaunchCfg cfg, cudaStream_t s);
+void launch_permute_hits(HitQueueDev in, const uint32_t* perm, const ull* d_n, HitQueueDev out,
+                         LaunchCfg cfg, cudaStream_t s);
+
+// image = accum / spp.
+void launch_finalize(const float* accum, int64_t nfloats, float spp, float* image, cudaStream_t s);
+
+}  // namespace wf

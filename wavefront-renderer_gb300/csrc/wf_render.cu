@@ -1,0 +1,765 @@
+// wf_render.cu — camera, traversal, shading and scheduling kernels of the
+// wavefront loop (reference src/render/WavefrontRenderer.cpp:401-877).
+#include <cuda_runtime.h>
+
+#include "wf_kernels.h"
+#include "wf_traverse.cuh"
+
+namespace wf {
+
+namespace {
+
+// Loop over [0, n) in block-wide steps so every warp runs the same number of
+// iterations (warp collectives stay converged).
+#define WF_BLOCK_LOOP(base, n)                                                       \
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < (n);                \
+         base += (int64_t)gridDim.x * blockDim.x)
+
+// ---------------------------------------------------------------------------
+// Camera rays: WavefrontRenderer::generatePrimaryRays (.cpp:401-457) with
+// Camera::getRay (include/core/Camera.h:35-40) and RayQueue::addPrimary
+// (RayQueue.h:113-116: throughput 1, depth 0, pdf -1).
+// ---------------------------------------------------------------------------
+__global__ void k_camera(wf_camera cam, int W, int H, uint32_t s0, uint32_t s1, int first_sample,
+                         int nspp, RayQueueDev rq)
+{
+    const int64_t np = (int64_t)W * H;
+    const int64_t n = np * nspp;
+    const V3 org = {cam.origin[0], cam.origin[1], cam.origin[2]};
+    const V3 tl = {cam.top_left[0], cam.top_left[1], cam.top_left[2]};
+    const V3 hz = {cam.horizontal[0], cam.horizontal[1], cam.horizontal[2]};
+    const V3 vt = {cam.vertical[0], cam.vertical[1], cam.vertical[2]};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int s = (int)(i / np);
+        const int p = (int)(i - (int64_t)s * np);
+        const int x = p % W, y = p / W;
+        const int sample = first_sample + s;
+        Stream rng(s0, s1, kPurposeCamera, 0, (uint32_t)p, (uint32_t)sample);
+        float u = ((float)x + rng.next()) / (float)(W - 1);
+        float v = 1.0f - ((float)y + rng.next()) / (float)(H - 1);
+        V3 d = normalized(tl + hz * u + vt * v - org);
+        rq.ox[i] = org.x;
+        rq.oy[i] = org.y;
+        rq.oz[i] = org.z;
+        rq.dx[i] = d.x;
+        rq.dy[i] = d.y;
+        rq.dz[i] = d.z;
+        rq.tr[i] = 1.0f;
+        rq.tg[i] = 1.0f;
+        rq.tb[i] = 1.0f;
+        rq.pdf[i] = -1.0f;
+        rq.pixel[i] = p;
+        rq.depth[i] = 0;
+        rq.sample[i] = sample;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Host-API traversal: one HitRecord per ray.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) k_trace_api(DeviceScene S, int64_t n, const float* ox,
+                                                   const float* oy, const float* oz,
+                                                   const float* dx, const float* dy,
+                                                   const float* dz, float tmin, float tmax,
+                                                   HitColumnsDev out, int* err)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        V3 o = {ox[i], oy[i], oz[i]}, d = {dx[i], dy[i], dz[i]};
+        TraceResult r;
+        traverse<false>(S, o, d, tmin, tmax, r, err);
+        if (r.leafpos < 0) {
+            if (out.geom) out.geom[i] = -1;
+            if (out.prim) out.prim[i] = -1;
+            if (out.mat) out.mat[i] = -1;
+            if (out.tex) out.tex[i] = -1;
+            if (out.t) out.t[i] = 0.0f;
+            continue;
+        }
+        HitRec h;
+        rebuild_hit(S, o, d, r.leafpos, r.t, r.bu, r.bv, h);
+        if (out.geom) out.geom[i] = h.geom;
+        if (out.prim) out.prim[i] = h.prim;
+        if (out.t) out.t[i] = h.t;
+        if (out.bu) out.bu[i] = r.bu;
+        if (out.bv) out.bv[i] = r.bv;
+        if (out.px) out.px[i] = h.p.x;
+        if (out.py) out.py[i] = h.p.y;
+        if (out.pz) out.pz[i] = h.p.z;
+        if (out.nx) out.nx[i] = h.n.x;
+        if (out.ny) out.ny[i] = h.n.y;
+        if (out.nz) out.nz[i] = h.n.z;
+        if (out.front) out.front[i] = h.front ? 1 : 0;
+        if (out.u) out.u[i] = h.u;
+        if (out.v) out.v[i] = h.v;
+        if (out.mat) out.mat[i] = h.mat;
+        if (out.tex) out.tex[i] = h.tex;
+    }
+}
+
+__global__ void __launch_bounds__(128) k_occluded_api(DeviceScene S, int64_t n, const float* ox,
+                                                      const float* oy, const float* oz,
+                                                      const float* dx, const float* dy,
+                                                      const float* dz, const float* maxd,
+                                                      uint8_t* out, int* err)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        V3 o = {ox[i], oy[i], oz[i]}, d = {dx[i], dy[i], dz[i]};
+        TraceResult r;
+        traverse<true>(S, o, d, 0.001f, maxd[i] - 0.001f, r, err);
+        out[i] = r.leafpos >= 0 ? 1 : 0;
+    }
+}
+
+__device__ __forceinline__ void accum_add(float* accum, int pixel, V3 c)
+{
+    float* p = accum + 3 * (int64_t)pixel;
+    atomicAdd(p + 0, c.x);
+    atomicAdd(p + 1, c.y);
+    atomicAdd(p + 2, c.z);
+}
+
+// ---------------------------------------------------------------------------
+// Render-loop closest hit (intersectAll, .cpp:459-567) fused with the miss
+// loop (.cpp:256-265): misses add throughput * sky to their pixel, hits are
+// appended to the hit queue with one atomic per warp.  Persistent threads:
+// each warp takes 32 rays at a time from a global counter.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) k_trace_render(DeviceScene S, RayQueueDev rq,
+                                                      const ull* __restrict__ d_n,
+                                                      HitQueueDev hq, ull* hq_n, float* accum,
+                                                      ull* work, int* err)
+{
+    const int64_t n = (int64_t)*d_n;
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        ull base = 0;
+        if (lane == 0) base = atomicAdd(work, 32ull);
+        base = __shfl_sync(0xFFFFFFFFu, base, 0);
+        if ((int64_t)base >= n) break;
+        const int64_t i = (int64_t)base + lane;
+        const bool active = i < n;
+        TraceResult r;
+        r.leafpos = -1;
+        V3 o = {0, 0, 0}, d = {0, 0, 1};
+        if (active) {
+            o = v3(rq.ox[i], rq.oy[i], rq.oz[i]);
+            d = v3(rq.dx[i], rq.dy[i], rq.dz[i]);
+            traverse<false>(S, o, d, 0.001f, 1e9f, r, err);
+        }
+        __syncwarp();
+        const bool hit = active && r.leafpos >= 0;
+        int64_t pos = warp_append(hq_n, hit);
+        if (hit) {
+            if (pos < hq.capacity) {
+                hq.ray[pos] = (int32_t)i;
+                hq.tri[pos] = r.leafpos;
+                hq.t[pos] = r.t;
+                hq.bu[pos] = r.bu;
+                hq.bv[pos] = r.bv;
+            } else {
+                atomicOr(err, 2);
+            }
+        } else if (active) {
+            V3 T = {rq.tr[i], rq.tg[i], rq.tb[i]};
+            accum_add(accum, rq.pixel[i], T * sky_color(S, d));
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// shadeAll per-hit body (.cpp:602-797): emission with MIS, area-light NEE
+// (Scene::sampleLight, src/core/Scene.cpp:192-238) and directional NEE become
+// shadow rays carrying their (clamped) contribution; scatter, Russian
+// roulette and the next ray.  Random streams per (purpose, depth, pixel,
+// sample) — the oracle uses the same ones.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) k_shade(DeviceScene S, ShadeParams P, RayQueueDev rq,
+                                               HitQueueDev hq, const ull* __restrict__ hq_n,
+                                               ShadowQueueDev sh, ull* sh_n, RayQueueDev nx,
+                                               ull* nx_n, float* accum, int* err)
+{
+    const int64_t n = (int64_t)*hq_n;
+    const float ff = P.firefly;
+    WF_BLOCK_LOOP(base, n)
+    {
+        const int64_t k = base + threadIdx.x;
+        const bool active = k < n;
+        bool want_area = false, want_dir = false, want_next = false;
+        V3 p = {0, 0, 0}, dir_area = {0, 0, 0}, c_area = {0, 0, 0}, dir_sun = {0, 0, 0},
+           c_sun = {0, 0, 0}, nd = {0, 0, 0}, Tn = {0, 0, 0};
+        float dist_area = 0.0f, next_pdf = 0.0f;
+        int pixel = 0, depth = 0, sample = 0;
+        if (active) {
+            const int ri = hq.ray[k];
+            const V3 o = {rq.ox[ri], rq.oy[ri], rq.oz[ri]};
+            const V3 d = {rq.dx[ri], rq.dy[ri], rq.dz[ri]};
+            const V3 T = {rq.tr[ri], rq.tg[ri], rq.tb[ri]};
+            const float in_pdf = rq.pdf[ri];
+            pixel = rq.pixel[ri];
+            depth = rq.depth[ri];
+            sample = rq.sample[ri];
+            HitRec h;
+            rebuild_hit(S, o, d, hq.tri[k], hq.t[k], hq.bu[k], hq.bv[k], h);
+            p = h.p;
+            const wf_material m = S.materials[h.mat];
+            // Emission with MIS (.cpp:629-658)
+            V3 Le = emitted(m, h.n, d * -1.0f);
+            if (Le.x > 0.0f || Le.y > 0.0f || Le.z > 0.0f) {
+                float w = 1.0f;
+                if (depth > 0 && in_pdf > 0.0f) {
+                    float cos_l = fmaxf(0.0f, dot(d * -1.0f, h.n));
+                    if (cos_l > 0.0f) {
+                        float lp = area_to_angle(S.light_area_pdf, h.t, cos_l);
+                        w = mis_balance(in_pdf, lp);
+                    }
+                }
+                Le = vmin(Le, ff);
+                accum_add(accum, pixel, T * Le * w);
+            }
+            V3 surf = {0, 0, 0};
+            bool have_surf = false;
+            // Area-light NEE (.cpp:660-710)
+            if ((m.type == WF_MATERIAL_DIFFUSE || m.type == WF_MATERIAL_PLASTIC) &&
+                S.num_emissive_meshes > 0) {
+                Stream lr(P.seed_lo, P.seed_hi, kPurposeLight, (uint32_t)depth, (uint32_t)pixel,
+                          (uint32_t)sample);
+                const int ne = S.num_emissive_meshes;
+                const EmissiveMesh em = S.emissive_meshes[(int)(lr.next() * (float)ne) % ne];
+                const float xi_tri = lr.next();
+                if (em.count > 0) {
+                    const int local = (int)(xi_tri * (float)em.count) % em.count;
+                    const float4* et = S.emissive_tris + 3 * (int64_t)(em.first + local);
+                    const float4 a = __ldg(et), b = __ldg(et + 1), c = __ldg(et + 2);
+                    const V3 v0 = {a.x, a.y, a.z}, v1 = {b.x, b.y, b.z}, v2 = {c.x, c.y, c.z};
+                    float r1 = lr.next();
+                    float r2 = lr.next();
+                    if (r1 + r2 > 1.0f) {
+                        r1 = 1.0f - r1;
+                        r2 = 1.0f - r2;
+                    }
+                    const float r3 = 1.0f - r1 - r2;
+                    const V3 lpnt = v0 * r3 + v1 * r1 + v2 * r2;
+                    const V3 ln = normalized(cross(v1 - v0, v2 - v0));
+                    const V3 from_light = normalized(p - lpnt);
+                    const V3 le = emitted(S.materials[em.material], ln, from_light);
+                    const V3 to = lpnt - p;
+                    const float dist = length(to);
+                    const V3 dl = to / dist;
+                    const float cos_s = dot(h.n, dl);
+                    const float cos_l = dot(dl * -1.0f, ln);
+                    if (cos_s > 0.0f && cos_l > 0.0f) {
+                        surf = surface_color(S, m, h);
+                        have_surf = true;
+                        const float g = (cos_s * cos_l) / (dist * dist);
+                        const V3 brdf = surf * (1.0f / kPi);
+                        const float lp = area_to_angle(S.light_area_pdf, dist, cos_l);
+                        const float bp = cos_s / kPi;
+                        const float w = mis_balance(lp, bp);
+                        const V3 direct = T * brdf * le * g * S.total_emissive_area * w;
+                        c_area = vmin(direct, ff);
+                        dir_area = dl;
+                        dist_area = dist;
+                        want_area = true;
+                    }
+                }
+            }
+            // Directional NEE (.cpp:712-737)
+            if (S.directional.intensity > 0.0f) {
+                const V3 to = v3(S.directional.direction[0], S.directional.direction[1],
+                                 S.directional.direction[2]) * -1.0f;
+                const float cos_s = dot(h.n, to);
+                if (cos_s > 0.0f) {
+                    if (!have_surf) surf = surface_color(S, m, h);
+                    const V3 brdf = surf * (1.0f / kPi);
+                    const V3 col = {S.directional.color[0], S.directional.color[1], S.directional.color[2]};
+                    const V3 direct = T * brdf * col * S.directional.intensity * cos_s;
+                    c_sun = vmin(direct, ff);
+                    dir_sun = to;
+                    want_dir = true;
+                }
+            }
+            // Scatter + Russian roulette (.cpp:739-796)
+            Stream sr(P.seed_lo, P.seed_hi, kPurposeScatter, (uint32_t)depth, (uint32_t)pixel,
+                      (uint32_t)sample);
+            V3 att;
+            float spdf;
+            if (scatter(S, m, d, h, sr, att, nd, spdf)) {
+                Tn = T * att;
+                bool alive = true;
+                if (depth + 1 >= P.rr_min_depth) {
+                    float q = fminf(0.95f, fmaxf(Tn.x, fmaxf(Tn.y, Tn.z)));
+                    if (P.cost_aware_rr) {
+                        float rc = P.rel_cost_material ? P.rel_cost_material[h.mat] : 1.0f;
+                        q = fminf(fmaxf(q / rc, 0.05f), 0.95f);
+                    }
+                    Stream rr(P.seed_lo, P.seed_hi, kPurposeRoulette, (uint32_t)depth,
+                              (uint32_t)pixel, (uint32_t)sample);
+                    if (rr.next() > q)
+                        alive = false;
+                    else
+                        Tn = Tn / q;
+                }
+                if (alive) {
+                    want_next = true;
+                    next_pdf = spdf;
+                }
+            }
+        }
+        __syncwarp();
+        int64_t pa = warp_append(sh_n, want_area);
+        if (want_area) {
+            if (pa < sh.capacity) {
+                sh.ox[pa] = p.x; sh.oy[pa] = p.y; sh.oz[pa] = p.z;
+                sh.dx[pa] = dir_area.x; sh.dy[pa] = dir_area.y; sh.dz[pa] = dir_area.z;
+                sh.dist[pa] = dist_area;
+                sh.cr[pa] = c_area.x; sh.cg[pa] = c_area.y; sh.cb[pa] = c_area.z;
+                sh.pixel[pa] = pixel;
+            } else {
+                atomicOr(err, 4);
+            }
+        }
+        __syncwarp();
+        int64_t pd = warp_append(sh_n, want_dir);
+        if (want_dir) {
+            if (pd < sh.capacity) {
+                sh.ox[pd] = p.x; sh.oy[pd] = p.y; sh.oz[pd] = p.z;
+                sh.dx[pd] = dir_sun.x; sh.dy[pd] = dir_sun.y; sh.dz[pd] = dir_sun.z;
+                sh.dist[pd] = 1e6f;
+                sh.cr[pd] = c_sun.x; sh.cg[pd] = c_sun.y; sh.cb[pd] = c_sun.z;
+                sh.pixel[pd] = pixel;
+            } else {
+                atomicOr(err, 4);
+            }
+        }
+        __syncwarp();
+        int64_t pn = warp_append(nx_n, want_next);
+        if (want_next) {
+            if (pn < nx.capacity) {
+                nx.ox[pn] = p.x; nx.oy[pn] = p.y; nx.oz[pn] = p.z;
+                nx.dx[pn] = nd.x; nx.dy[pn] = nd.y; nx.dz[pn] = nd.z;
+                nx.tr[pn] = Tn.x; nx.tg[pn] = Tn.y; nx.tb[pn] = Tn.z;
+                nx.pdf[pn] = next_pdf;
+                nx.pixel[pn] = pixel;
+                nx.depth[pn] = depth + 1;
+                nx.sample[pn] = sample;
+            } else {
+                atomicOr(err, 8);
+            }
+        }
+    }
+}
+
+// Shadow rays (EmbreeAccelerator::occluded): unblocked contributions are
+// added to their pixel.
+__global__ void __launch_bounds__(128) k_occluded_render(DeviceScene S, ShadowQueueDev sh,
+                                                         const ull* __restrict__ d_n,
+                                                         float* accum, ull* work, int* err)
+{
+    const int64_t n = (int64_t)*d_n;
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        ull base = 0;
+        if (lane == 0) base = atomicAdd(work, 32ull);
+        base = __shfl_sync(0xFFFFFFFFu, base, 0);
+        if ((int64_t)base >= n) break;
+        const int64_t i = (int64_t)base + lane;
+        if (i < n) {
+            V3 o = {sh.ox[i], sh.oy[i], sh.oz[i]}, d = {sh.dx[i], sh.dy[i], sh.dz[i]};
+            TraceResult r;
+            traverse<true>(S, o, d, 0.001f, sh.dist[i] - 0.001f, r, err);
+            if (r.leafpos < 0) accum_add(accum, sh.pixel[i], v3(sh.cr[i], sh.cg[i], sh.cb[i]));
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// RayQueue::sortKey (include/scheduling/RayQueue.h:135-162).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t spread10(uint32_t v)
+{
+    v &= 0x3FFu;
+    v = (v | (v << 16)) & 0x30000FFu;
+    v = (v | (v << 8)) & 0x300F00Fu;
+    v = (v | (v << 4)) & 0x30C30C3u;
+    v = (v | (v << 2)) & 0x9249249u;
+    return v;
+}
+
+__device__ __forceinline__ uint32_t quant_ray(float v, float mn, float ex)
+{
+    float t = (v - mn) / ex;
+    t = fminf(fmaxf(t, 0.0f), 1.0f);
+    return (uint32_t)(t * 1023.0f);
+}
+
+__device__ __forceinline__ uint64_t ray_key(float ox, float oy, float oz, float dx, float dy, float dz,
+                                            float3 mn, float3 ex)
+{
+    uint64_t oct = (dx < 0.0f ? 1u : 0u) | (dy < 0.0f ? 2u : 0u) | (dz < 0.0f ? 4u : 0u);
+    uint64_t m = spread10(quant_ray(ox, mn.x, ex.x)) | (spread10(quant_ray(oy, mn.y, ex.y)) << 1) |
+                 (spread10(quant_ray(oz, mn.z, ex.z)) << 2);
+    return (oct << 30) | m;
+}
+
+__global__ void k_ray_keys(RayQueueDev rq, const ull* __restrict__ d_n, float3 mn, float3 ex,
+                           uint64_t* keys, uint32_t* vals)
+{
+    const int64_t n = (int64_t)*d_n;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        keys[i] = ray_key(rq.ox[i], rq.oy[i], rq.oz[i], rq.dx[i], rq.dy[i], rq.dz[i], mn, ex);
+        vals[i] = (uint32_t)i;
+    }
+}
+
+__global__ void k_ray_keys_raw(int64_t n, const float* ox, const float* oy, const float* oz,
+                               const float* dx, const float* dy, const float* dz, float3 mn,
+                               float3 ex, uint64_t* keys, uint32_t* vals)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        keys[i] = ray_key(ox[i], oy[i], oz[i], dx[i], dy[i], dz[i], mn, ex);
+        vals[i] = (uint32_t)i;
+    }
+}
+
+__global__ void k_gather_rays(RayQueueDev in, const uint32_t* __restrict__ perm,
+                              const ull* __restrict__ d_n, RayQueueDev out)
+{
+    const int64_t n = (int64_t)*d_n;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t j = perm[i];
+        out.ox[i] = in.ox[j];
+        out.oy[i] = in.oy[j];
+        out.oz[i] = in.oz[j];
+        out.dx[i] = in.dx[j];
+        out.dy[i] = in.dy[j];
+        out.dz[i] = in.dz[j];
+        out.tr[i] = in.tr[j];
+        out.tg[i] = in.tg[j];
+        out.tb[i] = in.tb[j];
+        out.pdf[i] = in.pdf[j];
+        out.pixel[i] = in.pixel[j];
+        out.depth[i] = in.depth[j];
+        out.sample[i] = in.sample[j];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// ShadingQueue scheduling (include/scheduling/ShadingQueue.h:90-141,
+// 277-329, 437-550).
+// ---------------------------------------------------------------------------
+__global__ void k_type_stats(ShadeColumnsDev c, const ull* __restrict__ d_n,
+                             const wf_material* __restrict__ mats, int num_tex,
+                             const int64_t* __restrict__ tex_bytes, ull* counts, ull* mem,
+                             int* first)
+{
+    __shared__ unsigned long long s_cnt[8], s_mem[8];
+    __shared__ int s_first[8];
+    if (threadIdx.x < 8) {
+        s_cnt[threadIdx.x] = 0;
+        s_mem[threadIdx.x] = 0;
+        s_first[threadIdx.x] = 0x7FFFFFFF;
+    }
+    __syncthreads();
+    const int64_t n = (int64_t)*d_n;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int ty = mats[c.mat[i]].type & 7;
+        atomicAdd(&s_cnt[ty], 1ull);
+        atomicMin(&s_first[ty], (int)i);
+        const int tid = c.tex[i];
+        if (tid >= 0 && tid < num_tex) atomicAdd(&s_mem[ty], (ull)tex_bytes[tid]);
+    }
+    __syncthreads();
+    if (threadIdx.x < 8) {
+        if (s_cnt[threadIdx.x]) {
+            atomicAdd(&counts[threadIdx.x], s_cnt[threadIdx.x]);
+            atomicAdd(&mem[threadIdx.x], s_mem[threadIdx.x]);
+            atomicMin(&first[threadIdx.x], s_first[threadIdx.x]);
+        }
+    }
+}
+
+struct Rank8 {
+    int r[8];
+};
+
+__global__ void k_policy_keys(ShadeColumnsDev c, const ull* __restrict__ d_n,
+                              const wf_material* __restrict__ mats, int policy, Rank8 type_rank,
+                              const int* __restrict__ cost_rank, const int* __restrict__ tex_rank,
+                              int num_tex, int shift, uint64_t* keys, uint32_t* vals)
+{
+    const int64_t n = (int64_t)*d_n;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int m = c.mat[i];
+        const uint64_t tr = (uint64_t)type_rank.r[mats[m].type & 7];
+        uint64_t sec;
+        if (policy == WF_POLICY_TEXTURE_AWARE) {
+            const int tid = c.tex[i];
+            sec = (uint64_t)tex_rank[(tid >= 0 && tid < num_tex) ? tid : num_tex];
+        } else {
+            sec = (uint64_t)cost_rank[m];
+        }
+        keys[i] = (tr << shift) | sec;
+        vals[i] = (uint32_t)i;
+    }
+}
+
+__device__ __forceinline__ unsigned float_to_ordered(float f)
+{
+    unsigned b = __float_as_uint(f);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float ordered_to_float(unsigned u)
+{
+    unsigned b = (u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u;
+    return __uint_as_float(b);
+}
+
+__global__ void k_cb_reduce(ShadeColumnsDev c, const ull* __restrict__ d_n, double* benefit,
+                            int* present, unsigned* bounds6)
+{
+    const int64_t n = (int64_t)*d_n;
+    unsigned mn[3] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu}, mx[3] = {0u, 0u, 0u};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int m = c.mat[i];
+        // luminance, include/render/AdaptiveSampler.h:21-27 (float), summed in double
+        const float l = 0.2126f * c.tr[i] + 0.7152f * c.tg[i] + 0.0722f * c.tb[i];
+        atomicAdd(&benefit[m], (double)l);
+        present[m] = 1;
+        const float p3[3] = {c.px[i], c.py[i], c.pz[i]};
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            unsigned o = float_to_ordered(p3[k]);
+            mn[k] = min(mn[k], o);
+            mx[k] = max(mx[k], o);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        for (int off = 16; off > 0; off >>= 1) {
+            mn[k] = min(mn[k], __shfl_xor_sync(0xFFFFFFFFu, mn[k], off));
+            mx[k] = max(mx[k], __shfl_xor_sync(0xFFFFFFFFu, mx[k], off));
+        }
+    }
+    if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            atomicMin(&bounds6[k], mn[k]);
+            atomicMax(&bounds6[3 + k], mx[k]);
+        }
+    }
+}
+
+// computeMortonCode quantisation (ShadingQueue.h:523-529).
+__device__ __forceinline__ uint32_t quant_cb(float v, float lo, float hi)
+{
+    float t = (hi > lo) ? (v - lo) / (hi - lo) : 0.0f;
+    return (uint32_t)(fminf(fmaxf(t, 0.0f), 1.0f) * 1023.0f);
+}
+
+__global__ void k_cb_keys(ShadeColumnsDev c, const ull* __restrict__ d_n,
+                          const wf_material* __restrict__ mats, const int* __restrict__ prio_rank,
+                          int prio_bits, const unsigned* __restrict__ bounds6, uint64_t* keys,
+                          uint32_t* vals)
+{
+    const int64_t n = (int64_t)*d_n;
+    float lo[3], hi[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        lo[k] = ordered_to_float(bounds6[k]);
+        hi[k] = ordered_to_float(bounds6[3 + k]);
+    }
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int m = c.mat[i];
+        const uint64_t ty = (uint64_t)(mats[m].type & 7);
+        const uint64_t pr = (uint64_t)prio_rank[m];
+        const uint64_t morton = (uint64_t)spread10(quant_cb(c.px[i], lo[0], hi[0])) |
+                                ((uint64_t)spread10(quant_cb(c.py[i], lo[1], hi[1])) << 1) |
+                                ((uint64_t)spread10(quant_cb(c.pz[i], lo[2], hi[2])) << 2);
+        keys[i] = (ty << (prio_bits + 30)) | (pr << 30) | morton;
+        vals[i] = (uint32_t)i;
+    }
+}
+
+__global__ void k_hit_columns(DeviceScene S, RayQueueDev rq, HitQueueDev hq,
+                              const ull* __restrict__ d_n, ShadeColumnsMut out)
+{
+    const int64_t n = (int64_t)*d_n;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        const int ri = hq.ray[k];
+        const float4 b = __ldg(S.tris + 3 * (int64_t)hq.tri[k] + 1);
+        const int m = S.mesh_material[__float_as_int(b.w)];
+        out.mat[k] = m;
+        out.tex[k] = S.materials[m].texture_id;
+        out.tr[k] = rq.tr[ri];
+        out.tg[k] = rq.tg[ri];
+        out.tb[k] = rq.tb[ri];
+        const float t = hq.t[k];
+        out.px[k] = rq.ox[ri] + rq.dx[ri] * t;
+        out.py[k] = rq.oy[ri] + rq.dy[ri] * t;
+        out.pz[k] = rq.oz[ri] + rq.dz[ri] * t;
+    }
+}
+
+__global__ void k_permute_hits(HitQueueDev in, const uint32_t* __restrict__ perm,
+                               const ull* __restrict__ d_n, HitQueueDev out)
+{
+    const int64_t n = (int64_t)*d_n;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t j = perm[i];
+        out.ray[i] = in.ray[j];
+        out.tri[i] = in.tri[j];
+        out.t[i] = in.t[j];
+        out.bu[i] = in.bu[j];
+        out.bv[i] = in.bv[j];
+    }
+}
+
+__global__ void k_finalize(const float* accum, int64_t n, float spp, float* image)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        image[i] = accum[i] / spp;  // writeAveragedImage, WavefrontRenderer.cpp:127-137
+}
+
+inline int grid_for(int64_t n, int block, int cap)
+{
+    int64_t g = (n + block - 1) / block;
+    if (g > cap) g = cap;
+    if (g < 1) g = 1;
+    return (int)g;
+}
+
+}  // namespace
+
+void launch_camera(const wf_camera& cam, int W, int H, uint32_t s0, uint32_t s1, int first_sample,
+                   int nspp, RayQueueDev rq, cudaStream_t s)
+{
+    int64_t n = (int64_t)W * H * nspp;
+    k_camera<<<grid_for(n, 256, 65535), 256, 0, s>>>(cam, W, H, s0, s1, first_sample, nspp, rq);
+}
+
+void launch_trace_api(const DeviceScene& S, int64_t n, const float* ox, const float* oy,
+                      const float* oz, const float* dx, const float* dy, const float* dz,
+                      float tmin, float tmax, HitColumnsDev out, int* err, LaunchCfg cfg,
+                      cudaStream_t s)
+{
+    k_trace_api<<<grid_for(n, 128, cfg.grid), 128, 0, s>>>(S, n, ox, oy, oz, dx, dy, dz, tmin, tmax,
+                                                          out, err);
+}
+
+void launch_occluded_api(const DeviceScene& S, int64_t n, const float* ox, const float* oy,
+                         const float* oz, const float* dx, const float* dy, const float* dz,
+                         const float* maxd, uint8_t* out, int* err, LaunchCfg cfg, cudaStream_t s)
+{
+    k_occluded_api<<<grid_for(n, 128, cfg.grid), 128, 0, s>>>(S, n, ox, oy, oz, dx, dy, dz, maxd,
+                                                             out, err);
+}
+
+void launch_trace_render(const DeviceScene& S, RayQueueDev rq, const ull* d_n, HitQueueDev hq,
+                         ull* hq_n, float* accum, ull* work, int* err, LaunchCfg cfg,
+                         cudaStream_t s)
+{
+    k_trace_render<<<cfg.grid, 128, 0, s>>>(S, rq, d_n, hq, hq_n, accum, work, err);
+}
+
+void launch_shade(const DeviceScene& S, const ShadeParams& P, RayQueueDev rq, HitQueueDev hq,
+                  const ull* hq_n, ShadowQueueDev sh, ull* sh_n, RayQueueDev next, ull* next_n,
+                  float* accum, int* err, LaunchCfg cfg, cudaStream_t s)
+{
+    k_shade<<<cfg.grid, 128, 0, s>>>(S, P, rq, hq, hq_n, sh, sh_n, next, next_n, accum, err);
+}
+
+void launch_occluded_render(const DeviceScene& S, ShadowQueueDev sh, const ull* sh_n, float* accum,
+                            ull* work, int* err, LaunchCfg cfg, cudaStream_t s)
+{
+    k_occluded_render<<<cfg.grid, 128, 0, s>>>(S, sh, sh_n, accum, work, err);
+}
+
+void launch_ray_keys(RayQueueDev rq, const ull* d_n, const float bmin[3], const float bmax[3],
+                     uint64_t* keys, uint32_t* vals, LaunchCfg cfg, cudaStream_t s)
+{
+    float3 mn = make_float3(bmin[0], bmin[1], bmin[2]);
+    float3 ex = make_float3(fmaxf(bmax[0] - bmin[0], 1e-6f), fmaxf(bmax[1] - bmin[1], 1e-6f),
+                            fmaxf(bmax[2] - bmin[2], 1e-6f));
+    k_ray_keys<<<cfg.grid, 256, 0, s>>>(rq, d_n, mn, ex, keys, vals);
+}
+
+void launch_ray_keys_raw(int64_t n, const float* ox, const float* oy, const float* oz,
+                         const float* dx, const float* dy, const float* dz, const float bmin[3],
+                         const float bmax[3], uint64_t* keys, uint32_t* vals, LaunchCfg cfg,
+                         cudaStream_t s)
+{
+    float3 mn = make_float3(bmin[0], bmin[1], bmin[2]);
+    float3 ex = make_float3(fmaxf(bmax[0] - bmin[0], 1e-6f), fmaxf(bmax[1] - bmin[1], 1e-6f),
+                            fmaxf(bmax[2] - bmin[2], 1e-6f));
+    k_ray_keys_raw<<<grid_for(n, 256, cfg.grid), 256, 0, s>>>(n, ox, oy, oz, dx, dy, dz, mn, ex,
+                                                             keys, vals);
+}
+
+void launch_gather_rays(RayQueueDev in, const uint32_t* perm, const ull* d_n, RayQueueDev out,
+                        LaunchCfg cfg, cudaStream_t s)
+{
+    k_gather_rays<<<cfg.grid, 256, 0, s>>>(in, perm, d_n, out);
+}
+
+void launch_type_stats(ShadeColumnsDev c, const ull* d_n, const wf_material* mats, int num_tex,
+                       const int64_t* tex_bytes, ull* counts, ull* mem, int* first, LaunchCfg cfg,
+                       cudaStream_t s)
+{
+    k_type_stats<<<cfg.grid, 256, 0, s>>>(c, d_n, mats, num_tex, tex_bytes, counts, mem, first);
+}
+
+void launch_policy_keys(ShadeColumnsDev c, const ull* d_n, const wf_material* mats, int policy,
+                        const int* type_rank8, const int* cost_rank, const int* tex_rank,
+                        int num_tex, int shift, uint64_t* keys, uint32_t* vals, LaunchCfg cfg,
+                        cudaStream_t s)
+{
+    Rank8 r;
+    for (int k = 0; k < 8; ++k) r.r[k] = type_rank8[k];
+    k_policy_keys<<<cfg.grid, 256, 0, s>>>(c, d_n, mats, policy, r, cost_rank, tex_rank, num_tex,
+                                           shift, keys, vals);
+}
+
+void launch_cb_reduce(ShadeColumnsDev c, const ull* d_n, double* benefit, int* present,
+                      unsigned* bounds6, LaunchCfg cfg, cudaStream_t s)
+{
+    k_cb_reduce<<<cfg.grid, 256, 0, s>>>(c, d_n, benefit, present, bounds6);
+}
+
+void launch_cb_keys(ShadeColumnsDev c, const ull* d_n, const wf_material* mats,
+                    const int* prio_rank, int prio_bits, const unsigned* bounds6, uint64_t* keys,
+                    uint32_t* vals, LaunchCfg cfg, cudaStream_t s)
+{
+    k_cb_keys<<<cfg.grid, 256, 0, s>>>(c, d_n, mats, prio_rank, prio_bits, bounds6, keys, vals);
+}
+
+void launch_hit_columns(const DeviceScene& S, RayQueueDev rq, HitQueueDev hq, const ull* d_n,
+                        ShadeColumnsMut out, LaunchCfg cfg, cudaStream_t s)
+{
+    k_hit_columns<<<cfg.grid, 256, 0, s>>>(S, rq, hq, d_n, out);
+}
+
+void launch_permute_hits(HitQueueDev in, const uint32_t* perm, const ull* d_n, HitQueueDev out,
+                         LaunchCfg cfg, cudaStream_t s)
+{
+    k_permute_hits<<<cfg.grid, 256, 0, s>>>(in, perm, d_n, out);
+}
+
+void launch_finalize(const float* accum, int64_t n, float spp, float* image, cudaStream_t s)
+{
+    k_finalize<<<grid_for(n, 256, 65535), 256, 0, s>>>(accum, n, spp, image);
+}
+
+}  // namespace wf

@@ -1,0 +1,189 @@
+// wf_sort.cu — stable LSD radix sort of (uint64 key, uint32 value) pairs.
+//
+// Used for the BVH Morton order, the RayQueue sort (RayQueue::schedule,
+// reference include/scheduling/RayQueue.h:165-179) and the ShadingQueue
+// policy sorts (ShadingQueue.h:90-141, 437-510).  Stability matters: the
+// reference comparators tie often, and a stable sort of the policy key gives
+// exactly the permutation std::stable_sort gives with the reference
+// comparator.
+//
+// One pass per 8-bit digit, three kernels per pass:
+//   hist    — each block counts the digits of its contiguous chunk
+//   scan    — one block turns the [digit][block] counts into offsets
+//   scatter — each block walks its chunk in tiles of 256 keys; a key's rank
+//             among equal digits of its warp comes from __match_any_sync,
+//             warps are combined with a per-digit prefix in shared memory,
+//             so order within a digit follows input order (stable).
+// The element count is read from device memory, so a pass can be launched
+// (and graph-captured) before the count is known on the host.
+#include "wf_sort.h"
+
+#include <cuda_runtime.h>
+
+namespace wf {
+
+namespace {
+
+constexpr int kTile = 256;  // threads per block = keys per tile
+constexpr int kDigits = 256;
+
+__device__ __forceinline__ void chunk_of(int64_t n, int nb, int b, int64_t& start, int64_t& end)
+{
+    int64_t per = (n + nb - 1) / nb;
+    per = (per + kTile - 1) / kTile * kTile;
+    start = (int64_t)b * per;
+    end = start + per;
+    if (end > n) end = n;
+    if (start > n) start = n;
+}
+
+__global__ void __launch_bounds__(kTile) k_hist(const uint64_t* __restrict__ keys,
+                                                const unsigned long long* __restrict__ d_n,
+                                                int shift, uint32_t* __restrict__ hist, int nb)
+{
+    __shared__ uint32_t h[kDigits];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    int64_t start, end;
+    chunk_of((int64_t)*d_n, nb, blockIdx.x, start, end);
+    for (int64_t i = start + threadIdx.x; i < end; i += kTile)
+        atomicAdd(&h[(uint32_t)(__ldg(keys + i) >> shift) & 0xFFu], 1u);
+    __syncthreads();
+    hist[(int64_t)threadIdx.x * nb + blockIdx.x] = h[threadIdx.x];
+}
+
+// Exclusive scan of total = 256*nb counts by one block of 1024 threads.
+__global__ void __launch_bounds__(1024) k_scan(uint32_t* __restrict__ hist, int total)
+{
+    __shared__ uint32_t part[1024];
+    const int t = threadIdx.x;
+    const int per = (total + 1023) / 1024;
+    const int b = t * per, e = min(b + per, total);
+    uint32_t s = 0;
+    for (int i = b; i < e; ++i) s += hist[i];
+    part[t] = s;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {
+        uint32_t v = t >= off ? part[t - off] : 0u;
+        __syncthreads();
+        part[t] += v;
+        __syncthreads();
+    }
+    uint32_t run = part[t] - s;
+    for (int i = b; i < e; ++i) {
+        uint32_t c = hist[i];
+        hist[i] = run;
+        run += c;
+    }
+}
+
+__global__ void __launch_bounds__(kTile) k_scatter(const uint64_t* __restrict__ kin,
+                                                   const uint32_t* __restrict__ vin,
+                                                   uint64_t* __restrict__ kout,
+                                                   uint32_t* __restrict__ vout,
+                                                   const unsigned long long* __restrict__ d_n,
+                                                   int shift, const uint32_t* __restrict__ offs,
+                                                   int nb)
+{
+    __shared__ uint32_t running[kDigits];
+    __shared__ uint32_t wcnt[kTile / 32][kDigits];
+    __shared__ uint32_t tile_total[kDigits];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    running[tid] = offs[(int64_t)tid * nb + blockIdx.x];
+#pragma unroll
+    for (int w = 0; w < kTile / 32; ++w) wcnt[w][tid] = 0;
+    __syncthreads();
+    int64_t start, end;
+    chunk_of((int64_t)*d_n, nb, blockIdx.x, start, end);
+    const unsigned lt = (1u << lane) - 1u;
+    for (int64_t base = start; base < end; base += kTile) {
+        const int64_t i = base + tid;
+        const bool valid = i < end;
+        uint64_t key = 0;
+        uint32_t val = 0, digit = 0;
+        unsigned vmask = __ballot_sync(0xFFFFFFFFu, valid);
+        int rank = 0;
+        if (valid) {
+            key = kin[i];
+            val = vin[i];
+            digit = (uint32_t)(key >> shift) & 0xFFu;
+            unsigned peers = __match_any_sync(vmask, digit);
+            rank = __popc(peers & lt);
+            if (rank == 0) wcnt[warp][digit] = __popc(peers);
+        }
+        __syncthreads();
+        {
+            uint32_t acc = 0;
+#pragma unroll
+            for (int w = 0; w < kTile / 32; ++w) {
+                uint32_t c = wcnt[w][tid];
+                wcnt[w][tid] = acc;
+                acc += c;
+            }
+            tile_total[tid] = acc;
+        }
+        __syncthreads();
+        if (valid) {
+            uint32_t pos = running[digit] + wcnt[warp][digit] + (uint32_t)rank;
+            kout[pos] = key;
+            vout[pos] = val;
+        }
+        __syncthreads();
+        running[tid] += tile_total[tid];
+#pragma unroll
+        for (int w = 0; w < kTile / 32; ++w) wcnt[w][tid] = 0;
+        __syncthreads();
+    }
+}
+
+__global__ void k_iota(uint32_t* __restrict__ v, const unsigned long long* __restrict__ d_n)
+{
+    const int64_t n = (int64_t)*d_n;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        v[i] = (uint32_t)i;
+}
+
+}  // namespace
+
+int radix_blocks_for(int64_t capacity, int num_sms)
+{
+    // Enough blocks to fill the GPU, few enough that the scan stays cheap
+    // (256 * nb counts) and each chunk is at least a few tiles.
+    int64_t want = (capacity + 4 * kTile - 1) / (4 * kTile);
+    int64_t cap = (int64_t)num_sms * 6;
+    if (want > cap) want = cap;
+    if (want > 1024) want = 1024;
+    if (want < 1) want = 1;
+    return (int)want;
+}
+
+size_t radix_hist_words(int nb) { return (size_t)kDigits * nb; }
+
+void radix_sort_pairs(RadixSortArgs a, cudaStream_t s)
+{
+    uint64_t* kin = a.keys;
+    uint32_t* vin = a.vals;
+    uint64_t* kout = a.keys_tmp;
+    uint32_t* vout = a.vals_tmp;
+    for (int shift = a.begin_bit; shift < a.end_bit; shift += 8) {
+        k_hist<<<a.nb, kTile, 0, s>>>(kin, a.d_n, shift, a.hist, a.nb);
+        k_scan<<<1, 1024, 0, s>>>(a.hist, kDigits * a.nb);
+        k_scatter<<<a.nb, kTile, 0, s>>>(kin, vin, kout, vout, a.d_n, shift, a.hist, a.nb);
+        uint64_t* tk = kin;
+        kin = kout;
+        kout = tk;
+        uint32_t* tv = vin;
+        vin = vout;
+        vout = tv;
+    }
+    *a.result_keys = kin;
+    *a.result_vals = vin;
+}
+
+void launch_iota(uint32_t* v, const unsigned long long* d_n, int grid, cudaStream_t s)
+{
+    k_iota<<<grid, 256, 0, s>>>(v, d_n);
+}
+
+}  // namespace wf

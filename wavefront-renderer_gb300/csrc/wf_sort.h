@@ -1,0 +1,29 @@
+// wf_sort.h — launchers of the stable device radix sort (wf_sort.cu).
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace wf {
+
+struct RadixSortArgs {
+    uint64_t* keys;      // input keys (overwritten)
+    uint32_t* vals;      // input values (overwritten)
+    uint64_t* keys_tmp;  // ping-pong buffers, same capacity
+    uint32_t* vals_tmp;
+    uint32_t* hist;      // radix_hist_words(nb) words
+    const unsigned long long* d_n;  // element count, device memory
+    int nb;              // blocks per pass (radix_blocks_for)
+    int begin_bit;       // sort bits [begin_bit, end_bit), 8 per pass
+    int end_bit;
+    uint64_t** result_keys;  // set to the buffer holding the sorted keys
+    uint32_t** result_vals;
+};
+
+int radix_blocks_for(int64_t capacity, int num_sms);
+size_t radix_hist_words(int nb);
+void radix_sort_pairs(RadixSortArgs args, cudaStream_t stream);
+void launch_iota(uint32_t* v, const unsigned long long* d_n, int grid, cudaStream_t stream);
+
+}  // namespace wf
