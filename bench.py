@@ -56,9 +56,11 @@ BYTES_MISS = 16 + 24
 
 
 def load_pkg():
+    if "wavefront_gb300" in sys.modules:
+        return sys.modules["wavefront_gb300"]
     spec = importlib.util.spec_from_file_location("wavefront_gb300", ROOT / "wavefront-renderer_gb300" / "__init__.py")
     mod = importlib.util.module_from_spec(spec)
-    sys.modules.setdefault("wavefront_gb300", mod)
+    sys.modules["wavefront_gb300"] = mod
     spec.loader.exec_module(mod)
     if not mod.LIB_PATH.exists():
         spec_b = importlib.util.spec_from_file_location("wf_build", ROOT / "wavefront-renderer_gb300" / "build.py")

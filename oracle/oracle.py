@@ -28,9 +28,14 @@ REF_SRC = Path(os.environ.get("WF_REFERENCE_DIR", "/root/reference"))
 
 
 def _wf():
-    spec = importlib.util.spec_from_file_location("wavefront_gb300_types",
-                                                  ROOT / "wavefront-renderer_gb300" / "__init__.py")
+    """The binding module (for its ctypes structs), shared with the caller."""
+    import sys
+
+    if "wavefront_gb300" in sys.modules:
+        return sys.modules["wavefront_gb300"]
+    spec = importlib.util.spec_from_file_location("wavefront_gb300", ROOT / "wavefront-renderer_gb300" / "__init__.py")
     m = importlib.util.module_from_spec(spec)
+    sys.modules["wavefront_gb300"] = m
     spec.loader.exec_module(m)
     return m
 
