@@ -234,12 +234,16 @@ def main() -> int:
     ap.add_argument("--policy", default="none", choices=["none", "material", "texture", "costBenefit"])
     ap.add_argument("--ray-sort", type=int, default=0)
     ap.add_argument("--spp-per-wave", type=int, default=0)
+    ap.add_argument("--spp", type=int, default=0, help="override the workload's spp (profiling runs only)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ref-rows", type=int, default=32)
     ap.add_argument("--ref-spp", type=int, default=8)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 0)
-    wl = WORKLOADS[args.workload]
+    wl = dict(WORKLOADS[args.workload])
+    if args.spp > 0:
+        wl["spp"] = args.spp
+        wl["name"] = wl["name"].replace(f"_{WORKLOADS[args.workload]['spp']}spp", f"_{args.spp}spp")
     if args.impl == "reference":
         return run_reference(args, wl)
 
