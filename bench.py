@@ -236,6 +236,8 @@ def main() -> int:
     ap.add_argument("--spp-per-wave", type=int, default=0)
     ap.add_argument("--spp", type=int, default=0, help="override the workload's spp (profiling runs only)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--trace-variant", type=int, default=-1)
+    ap.add_argument("--blocks-per-sm", type=int, default=0)
     ap.add_argument("--ref-rows", type=int, default=32)
     ap.add_argument("--ref-spp", type=int, default=8)
     args = ap.parse_args()
@@ -252,6 +254,8 @@ def main() -> int:
     ctx = pkg.Context(local)
     scene = pkg.HostScene(wl["config"])
     info = ctx.upload(scene.desc)
+    if args.trace_variant >= 0 or args.blocks_per_sm > 0:
+        ctx.set_tuning(max(args.trace_variant, 0), args.blocks_per_sm)
     W, H = wl["width"], wl["height"]
     cam = scene.camera(W, H)
     policy = pkg.POLICIES[args.policy]
@@ -329,6 +333,7 @@ def main() -> int:
         "clocks": clocks,
         "gpu_launches": int(sum(s["kernel_launches"] for s in stats)),
         "bvh_build_ms": info.bvh_build_ms,
+        "tuning": ctx.get_tuning(),
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         rays, dt, sample = cpu_sample(pkg, wl, os.cpu_count() or 1, rows=48, spp=8, seed=7)

@@ -1,0 +1,319 @@
+// wavefront.hpp — C++17 mirror of the reference's per-bounce-loop API over the
+// C ABI of libwfgpu.so (include/wf_api.h).  Header-only.
+//
+// Same type and member names as fhidargue/wavefront-renderer, so code written
+// against the reference's loop ports by changing includes and passing a
+// wf::Context (the GPU and its resident scene):
+//   RayQueue          include/scheduling/RayQueue.h:63-245
+//   ShadingQueue      include/scheduling/ShadingQueue.h:27-551
+//   SchedulingPolicy  include/scheduling/ShadingQueue.h:18-24
+//   HitRecord         include/core/HitRecord.h:6-22 (plus geomID)
+//   WavefrontRenderer include/render/WavefrontRenderer.h:16-56
+// Errors: the reference throws from deep inside and catches in main
+// (src/main.cpp:218-222); here every failing ABI call throws wf::Error with
+// the library's message.
+#pragma once
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../wf_api.h"
+
+namespace wf {
+
+enum class SchedulingPolicy {
+    None = WF_POLICY_NONE,
+    MaterialAware = WF_POLICY_MATERIAL_AWARE,
+    TextureAware = WF_POLICY_TEXTURE_AWARE,
+    CostBenefitAware = WF_POLICY_COST_BENEFIT_AWARE,
+};
+
+class Error : public std::runtime_error {
+  public:
+    Error(int code, const std::string& msg) : std::runtime_error(msg), code(code) {}
+    int code;
+};
+
+inline void check(int rc, const wf_ctx* ctx, const char* what)
+{
+    if (rc != WF_OK)
+        throw Error(rc, std::string(what) + " failed (" + std::to_string(rc) + "): " + (ctx ? wf_last_error(ctx) : ""));
+}
+
+// One GPU, one stream, one resident scene.
+class Context {
+  public:
+    explicit Context(int device = 0, int64_t maxPathsPerWave = 0)
+    {
+        wf_config cfg{device, maxPathsPerWave};
+        check(wf_create(&cfg, &h_), nullptr, "wf_create");
+    }
+    ~Context() { wf_destroy(h_); }
+    Context(const Context&) = delete;
+    Context& operator=(const Context&) = delete;
+    Context(Context&& o) noexcept : h_(std::exchange(o.h_, nullptr)) {}
+    Context& operator=(Context&& o) noexcept
+    {
+        if (this != &o) {
+            wf_destroy(h_);
+            h_ = std::exchange(o.h_, nullptr);
+        }
+        return *this;
+    }
+    // Scene::buildAccelerator + EmbreeAccelerator::build
+    wf_scene_info upload(const wf_scene_desc& desc)
+    {
+        check(wf_scene_upload(h_, &desc), h_, "wf_scene_upload");
+        wf_scene_info info{};
+        check(wf_scene_get_info(h_, &info), h_, "wf_scene_get_info");
+        return info;
+    }
+    wf_ctx* handle() const { return h_; }
+
+  private:
+    wf_ctx* h_ = nullptr;
+};
+
+struct HitRecord {
+    float point[3] = {0, 0, 0};
+    float normal[3] = {0, 0, 0};
+    float distance = 0.0f;
+    int materialID = -1;
+    int textureID = -1;
+    int triangleIndex = -1;
+    float u = 0.0f, v = 0.0f;
+    bool frontFace = false;
+    int geomID = -1;  // device addition: the mesh index (Embree geomID)
+};
+
+namespace detail {
+template <class V>
+void permute(V& a, const std::vector<int>& idx)
+{
+    V out(idx.size());
+    for (size_t i = 0; i < idx.size(); ++i) out[i] = a[idx[i]];
+    a = std::move(out);
+}
+}  // namespace detail
+
+// include/scheduling/RayQueue.h:63-245
+struct RayQueue {
+    std::vector<float> originsX, originsY, originsZ;
+    std::vector<float> dirsX, dirsY, dirsZ;
+    std::vector<float> throughputsR, throughputsG, throughputsB;
+    std::vector<float> accumLightR, accumLightG, accumLightB;
+    std::vector<int> pixelIndices;
+    std::vector<int> depths;
+    std::vector<bool> alive;
+    std::vector<float> pdfs;
+    std::vector<int> sortedIndices;
+
+    void add(const float o[3], const float d[3], const float t[3], const float a[3], int pixel, int depth,
+             bool isAlive, float pdf)
+    {
+        originsX.push_back(o[0]); originsY.push_back(o[1]); originsZ.push_back(o[2]);
+        dirsX.push_back(d[0]); dirsY.push_back(d[1]); dirsZ.push_back(d[2]);
+        throughputsR.push_back(t[0]); throughputsG.push_back(t[1]); throughputsB.push_back(t[2]);
+        accumLightR.push_back(a[0]); accumLightG.push_back(a[1]); accumLightB.push_back(a[2]);
+        pixelIndices.push_back(pixel);
+        depths.push_back(depth);
+        alive.push_back(isAlive);
+        pdfs.push_back(pdf);
+    }
+    void addPrimary(const float o[3], const float d[3], int pixel)
+    {
+        const float one[3] = {1, 1, 1}, zero[3] = {0, 0, 0};
+        add(o, d, one, zero, pixel, 0, true, -1.0f);
+    }
+    int size() const { return (int)originsX.size(); }
+    bool empty() const { return originsX.empty(); }
+    void clear() { *this = RayQueue{}; }
+
+    // RayQueue::schedule on the GPU: sortedIndices = stable sort of sortKey.
+    void schedule(Context& ctx, const float sceneMin[3], const float sceneMax[3])
+    {
+        sortedIndices.assign(size(), 0);
+        if (empty()) return;
+        check(wf_ray_schedule_host(ctx.handle(), size(), originsX.data(), originsY.data(), originsZ.data(),
+                                   dirsX.data(), dirsY.data(), dirsZ.data(), sceneMin, sceneMax,
+                                   sortedIndices.data(), nullptr),
+              ctx.handle(), "wf_ray_schedule_host");
+    }
+    // RayQueue::materialize: gather every column, reset the identity.
+    void materialize()
+    {
+        if ((int)sortedIndices.size() != size()) return;
+        for (auto* c : {&originsX, &originsY, &originsZ, &dirsX, &dirsY, &dirsZ, &throughputsR, &throughputsG,
+                        &throughputsB, &accumLightR, &accumLightG, &accumLightB, &pdfs})
+            detail::permute(*c, sortedIndices);
+        detail::permute(pixelIndices, sortedIndices);
+        detail::permute(depths, sortedIndices);
+        detail::permute(alive, sortedIndices);
+        for (int i = 0; i < size(); ++i) sortedIndices[i] = i;
+    }
+};
+
+// include/scheduling/ShadingQueue.h:27-551
+struct ShadingQueue {
+    std::vector<float> hitPointsX, hitPointsY, hitPointsZ;
+    std::vector<float> hitNormalsX, hitNormalsY, hitNormalsZ;
+    std::vector<float> hitDistances, hitU, hitV;
+    std::vector<int> hitTriangleIndex;
+    std::vector<int> materialIDs, textureIDs;
+    std::vector<float> originsX, originsY, originsZ;
+    std::vector<float> dirsX, dirsY, dirsZ;
+    std::vector<float> throughputsR, throughputsG, throughputsB;
+    std::vector<int> pixelIndices, depths;
+    std::vector<float> pdfs;
+    std::vector<int> sortedIndices;
+    std::vector<int> geomIDs;       // device addition
+    std::vector<uint8_t> frontFaces; // carried (the reference's getHitRecord drops it)
+    SchedulingPolicy policy;
+
+    explicit ShadingQueue(SchedulingPolicy p = SchedulingPolicy::None) : policy(p) {}
+
+    void add(const RayQueue& r, int i, const HitRecord& h)
+    {
+        hitPointsX.push_back(h.point[0]); hitPointsY.push_back(h.point[1]); hitPointsZ.push_back(h.point[2]);
+        hitNormalsX.push_back(h.normal[0]); hitNormalsY.push_back(h.normal[1]); hitNormalsZ.push_back(h.normal[2]);
+        hitDistances.push_back(h.distance); hitU.push_back(h.u); hitV.push_back(h.v);
+        hitTriangleIndex.push_back(h.triangleIndex);
+        materialIDs.push_back(h.materialID); textureIDs.push_back(h.textureID);
+        originsX.push_back(r.originsX[i]); originsY.push_back(r.originsY[i]); originsZ.push_back(r.originsZ[i]);
+        dirsX.push_back(r.dirsX[i]); dirsY.push_back(r.dirsY[i]); dirsZ.push_back(r.dirsZ[i]);
+        throughputsR.push_back(r.throughputsR[i]); throughputsG.push_back(r.throughputsG[i]);
+        throughputsB.push_back(r.throughputsB[i]);
+        pixelIndices.push_back(r.pixelIndices[i]); depths.push_back(r.depths[i]); pdfs.push_back(r.pdfs[i]);
+        geomIDs.push_back(h.geomID);
+        frontFaces.push_back(h.frontFace ? 1 : 0);
+    }
+    int size() const { return (int)materialIDs.size(); }
+    bool empty() const { return materialIDs.empty(); }
+
+    // ShadingQueue::schedule on the GPU.  textureBytes[t] = Texture::memoryBytes();
+    // relative costs are frozen CostTracker::relativeCost values (null = 1.0).
+    void schedule(Context& ctx, const std::vector<wf_material>& materials, const std::vector<int64_t>& textureBytes,
+                  const std::vector<double>* relCostMaterial = nullptr,
+                  const std::vector<double>* relCostTexture = nullptr)
+    {
+        sortedIndices.assign(size(), 0);
+        if (empty()) return;
+        check(wf_shading_schedule_host(ctx.handle(), (int32_t)policy, size(), materialIDs.data(), textureIDs.data(),
+                                       throughputsR.data(), throughputsG.data(), throughputsB.data(),
+                                       hitPointsX.data(), hitPointsY.data(), hitPointsZ.data(),
+                                       (int32_t)materials.size(), materials.data(), (int32_t)textureBytes.size(),
+                                       textureBytes.data(), relCostMaterial ? relCostMaterial->data() : nullptr,
+                                       relCostTexture ? relCostTexture->data() : nullptr, sortedIndices.data()),
+              ctx.handle(), "wf_shading_schedule_host");
+    }
+    HitRecord getHitRecord(int pos) const
+    {
+        int i = sortedIndices.empty() ? pos : sortedIndices[pos];
+        HitRecord h;
+        h.point[0] = hitPointsX[i]; h.point[1] = hitPointsY[i]; h.point[2] = hitPointsZ[i];
+        h.normal[0] = hitNormalsX[i]; h.normal[1] = hitNormalsY[i]; h.normal[2] = hitNormalsZ[i];
+        h.distance = hitDistances[i]; h.u = hitU[i]; h.v = hitV[i];
+        h.triangleIndex = hitTriangleIndex[i]; h.materialID = materialIDs[i]; h.textureID = textureIDs[i];
+        h.geomID = geomIDs[i]; h.frontFace = frontFaces[i] != 0;
+        return h;
+    }
+    int getPixelIndex(int pos) const { return pixelIndices[sortedIndices.empty() ? pos : sortedIndices[pos]]; }
+    void materialize()
+    {
+        if ((int)sortedIndices.size() != size()) return;
+        for (auto* c : {&hitPointsX, &hitPointsY, &hitPointsZ, &hitNormalsX, &hitNormalsY, &hitNormalsZ,
+                        &hitDistances, &hitU, &hitV, &originsX, &originsY, &originsZ, &dirsX, &dirsY, &dirsZ,
+                        &throughputsR, &throughputsG, &throughputsB, &pdfs})
+            detail::permute(*c, sortedIndices);
+        for (auto* c : {&hitTriangleIndex, &materialIDs, &textureIDs, &pixelIndices, &depths, &geomIDs})
+            detail::permute(*c, sortedIndices);
+        detail::permute(frontFaces, sortedIndices);
+        for (int i = 0; i < size(); ++i) sortedIndices[i] = i;
+    }
+};
+
+// WavefrontRenderer::intersectAll (.cpp:459-567): closest hits of a queue on
+// the GPU, split into a ShadingQueue of hits and a RayQueue of misses.
+inline void intersectAll(Context& ctx, const RayQueue& in, ShadingQueue& hits, RayQueue& misses)
+{
+    const int n = in.size();
+    if (n == 0) return;
+    std::vector<int32_t> geom(n), prim(n), mat(n), tex(n);
+    std::vector<float> t(n), px(n), py(n), pz(n), nx(n), ny(n), nz(n), u(n), v(n);
+    std::vector<uint8_t> front(n);
+    wf_hit_columns cols{geom.data(), prim.data(), t.data(), nullptr, nullptr, px.data(), py.data(), pz.data(),
+                        nx.data(), ny.data(), nz.data(), front.data(), u.data(), v.data(), mat.data(), tex.data()};
+    check(wf_trace_closest_host(ctx.handle(), n, in.originsX.data(), in.originsY.data(), in.originsZ.data(),
+                                in.dirsX.data(), in.dirsY.data(), in.dirsZ.data(), 0.001f, 1e9f, &cols),
+          ctx.handle(), "wf_trace_closest_host");
+    for (int i = 0; i < n; ++i) {
+        if (geom[i] < 0) {
+            const float o[3] = {in.originsX[i], in.originsY[i], in.originsZ[i]};
+            const float d[3] = {in.dirsX[i], in.dirsY[i], in.dirsZ[i]};
+            const float T[3] = {in.throughputsR[i], in.throughputsG[i], in.throughputsB[i]};
+            const float A[3] = {in.accumLightR[i], in.accumLightG[i], in.accumLightB[i]};
+            misses.add(o, d, T, A, in.pixelIndices[i], in.depths[i], true, in.pdfs[i]);
+            continue;
+        }
+        HitRecord h;
+        h.point[0] = px[i]; h.point[1] = py[i]; h.point[2] = pz[i];
+        h.normal[0] = nx[i]; h.normal[1] = ny[i]; h.normal[2] = nz[i];
+        h.distance = t[i]; h.u = u[i]; h.v = v[i];
+        h.materialID = mat[i]; h.textureID = tex[i]; h.triangleIndex = prim[i]; h.geomID = geom[i];
+        h.frontFace = front[i] != 0;
+        hits.add(in, i, h);
+    }
+}
+
+// include/render/WavefrontRenderer.h:16-56.  Adaptive sampling is not
+// implemented on the device yet (enableAdaptiveSampling must stay false).
+class WavefrontRenderer {
+  public:
+    int samplesPerPixel;
+    int maxDepth;
+    int rrMinDepth = 3;
+    SchedulingPolicy policy;
+    bool enableCostAwareRR = true;
+    bool enableRaySort = true;
+    bool enableAdaptiveSampling = false;
+    float fireflyThreshold = 10.0f;
+    uint64_t seed = 1;
+    std::vector<double> relativeCostMaterial;  // frozen CostTracker::relativeCost, empty = 1.0
+    std::vector<double> relativeCostTexture;
+    wf_render_stats lastStats{};
+
+    WavefrontRenderer(int samples, int maxDepth, SchedulingPolicy policy)
+        : samplesPerPixel(samples), maxDepth(maxDepth), policy(policy)
+    {
+    }
+
+    // renderScene: writes the averaged image (width*height*3 floats) and
+    // returns the total shade milliseconds, as the reference does.
+    double renderScene(Context& ctx, const wf_camera& camera, int width, int height, std::vector<float>& pixels)
+    {
+        if (enableAdaptiveSampling) throw Error(WF_ERR_INVALID_ARGUMENT, "adaptive sampling is not supported");
+        wf_render_params p{};
+        p.width = width;
+        p.height = height;
+        p.samples_per_pixel = samplesPerPixel;
+        p.max_depth = maxDepth;
+        p.rr_min_depth = rrMinDepth;
+        p.policy = (int32_t)policy;
+        p.enable_ray_sort = enableRaySort ? 1 : 0;
+        p.enable_cost_aware_rr = enableCostAwareRR ? 1 : 0;
+        p.firefly_threshold = fireflyThreshold;
+        p.seed_lo = (uint32_t)seed;
+        p.seed_hi = (uint32_t)(seed >> 32);
+        p.rel_cost_material = relativeCostMaterial.empty() ? nullptr : relativeCostMaterial.data();
+        p.rel_cost_texture = relativeCostTexture.empty() ? nullptr : relativeCostTexture.data();
+        p.camera = camera;
+        pixels.assign((size_t)width * height * 3, 0.0f);
+        check(wf_render(ctx.handle(), &p, pixels.data(), &lastStats), ctx.handle(), "wf_render");
+        return lastStats.ms_shade;
+    }
+};
+
+}  // namespace wf

@@ -241,6 +241,18 @@ typedef struct wf_scene_info {
 } wf_scene_info;
 int wf_scene_get_info(wf_ctx* ctx, wf_scene_info* out_info);
 
+/* Launch tuning of a context (the autotuner's knobs).  trace_variant: 0 = no
+ * occupancy hint on the traversal kernels, 1 = 10 blocks of 128 threads per
+ * SM, 2 = 12 blocks.  persistent_blocks_per_sm: resident blocks launched per
+ * SM by the persistent traversal kernels (0 = 16). */
+typedef struct wf_tuning {
+    int32_t trace_variant;
+    int32_t persistent_blocks_per_sm;
+    int32_t reserved[6];
+} wf_tuning;
+int wf_set_tuning(wf_ctx* ctx, const wf_tuning* tuning);
+int wf_get_tuning(const wf_ctx* ctx, wf_tuning* out_tuning);
+
 /* ---- ray batches (host buffers) --------------------------------------------- */
 
 /* Closest hit of n rays, t in [tmin, tmax].  Replaces

@@ -116,6 +116,10 @@ class WfSceneInfo(C.Structure):
                 ("bvh_build_ms", C.c_double), ("device_bytes", C.c_int64)]
 
 
+class WfTuning(C.Structure):
+    _fields_ = [("trace_variant", C.c_int32), ("persistent_blocks_per_sm", C.c_int32), ("reserved", C.c_int32 * 6)]
+
+
 class WfHitColumns(C.Structure):
     _fields_ = [("geom_id", i32p), ("prim_id", i32p), ("distance", f32p), ("bary_u", f32p),
                 ("bary_v", f32p), ("point_x", f32p), ("point_y", f32p), ("point_z", f32p),
@@ -185,6 +189,8 @@ def _declare(lib: C.CDLL) -> None:
         "wf_image_download": ([V, f32p, C.c_int64], C.c_int),
         "wf_get_stream": ([V, C.POINTER(V)], C.c_int),
         "wf_timer_begin": ([V], C.c_int),
+        "wf_set_tuning": ([V, C.POINTER(WfTuning)], C.c_int),
+        "wf_get_tuning": ([V, C.POINTER(WfTuning)], C.c_int),
         "wf_timer_end": ([V, f64p], C.c_int),
         "wf_host_scene_generate": ([C.c_int32, C.c_uint64, C.POINTER(V)], C.c_int),
         "wf_host_scene_describe": ([V, C.POINTER(WfSceneDesc)], C.c_int),
@@ -390,6 +396,15 @@ class Context:
         img = out if out is not None else np.zeros(width * height * 3, dtype=np.float32)
         _check(load_library().wf_image_download(self._h, ptr(img), img.size), "wf_image_download", self)
         return img.reshape(height, width, 3)
+
+    def set_tuning(self, trace_variant: int = 0, persistent_blocks_per_sm: int = 0) -> None:
+        t = WfTuning(trace_variant, persistent_blocks_per_sm)
+        _check(load_library().wf_set_tuning(self._h, C.byref(t)), "wf_set_tuning", self)
+
+    def get_tuning(self) -> dict:
+        t = WfTuning()
+        _check(load_library().wf_get_tuning(self._h, C.byref(t)), "wf_get_tuning", self)
+        return {"trace_variant": t.trace_variant, "persistent_blocks_per_sm": t.persistent_blocks_per_sm}
 
     def timer_begin(self) -> None:
         _check(load_library().wf_timer_begin(self._h), "wf_timer_begin", self)

@@ -81,6 +81,7 @@ struct wf_ctx {
 
     cudaEvent_t ev[8]{};
     cudaEvent_t timer[2]{};
+    wf_tuning tuning{};
 };
 
 namespace {
@@ -114,7 +115,11 @@ void free_all(std::vector<void*>& v)
     v.clear();
 }
 
-LaunchCfg persist(const wf_ctx* c) { return LaunchCfg{c->num_sms * 16, 128}; }
+LaunchCfg persist(const wf_ctx* c)
+{
+    int per_sm = c->tuning.persistent_blocks_per_sm > 0 ? c->tuning.persistent_blocks_per_sm : 16;
+    return LaunchCfg{c->num_sms * per_sm, 128, c->tuning.trace_variant};
+}
 LaunchCfg wide(const wf_ctx* c) { return LaunchCfg{c->num_sms * 8, 256}; }
 
 // srgbToLinear, reference src/shading/Texture.cpp:20-27.
@@ -1097,6 +1102,23 @@ int wf_get_stream(wf_ctx* c, void** out)
 {
     if (!c || !out) return WF_ERR_INVALID_ARGUMENT;
     *out = (void*)c->stream;
+    return WF_OK;
+}
+
+int wf_set_tuning(wf_ctx* c, const wf_tuning* t)
+{
+    if (!c || !t) return WF_ERR_INVALID_ARGUMENT;
+    if (t->trace_variant < 0 || t->trace_variant > 2 || t->persistent_blocks_per_sm < 0 ||
+        t->persistent_blocks_per_sm > 32)
+        return set_err(c, WF_ERR_INVALID_ARGUMENT, "tuning out of range");
+    c->tuning = *t;
+    return WF_OK;
+}
+
+int wf_get_tuning(const wf_ctx* c, wf_tuning* out)
+{
+    if (!c || !out) return WF_ERR_INVALID_ARGUMENT;
+    *out = c->tuning;
     return WF_OK;
 }
 

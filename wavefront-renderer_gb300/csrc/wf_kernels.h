@@ -22,6 +22,7 @@ struct ShadeParams {
 struct LaunchCfg {
     int grid;
     int block;
+    int variant = 0;  // kernel variant (traversal occupancy hint)
 };
 
 // Camera rays of n = width*height*nspp paths, sample-major.

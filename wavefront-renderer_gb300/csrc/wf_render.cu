@@ -69,12 +69,15 @@ __global__ void __launch_bounds__(128) k_trace_api(DeviceScene S, int64_t n, con
         V3 o = {ox[i], oy[i], oz[i]}, d = {dx[i], dy[i], dz[i]};
         TraceResult r;
         traverse<false>(S, o, d, tmin, tmax, r, err);
-        if (r.leafpos < 0) {
+        if (r.leafpos < 0) {  // a miss: ids -1, every other column 0
             if (out.geom) out.geom[i] = -1;
             if (out.prim) out.prim[i] = -1;
             if (out.mat) out.mat[i] = -1;
             if (out.tex) out.tex[i] = -1;
-            if (out.t) out.t[i] = 0.0f;
+            float* zf[] = {out.t, out.bu, out.bv, out.px, out.py, out.pz, out.nx, out.ny, out.nz, out.u, out.v};
+            for (float* z : zf)
+                if (z) z[i] = 0.0f;
+            if (out.front) out.front[i] = 0;
             continue;
         }
         HitRec h;
@@ -124,49 +127,82 @@ __device__ __forceinline__ void accum_add(float* accum, int pixel, V3 c)
 // ---------------------------------------------------------------------------
 // Render-loop closest hit (intersectAll, .cpp:459-567) fused with the miss
 // loop (.cpp:256-265): misses add throughput * sky to their pixel, hits are
-// appended to the hit queue with one atomic per warp.  Persistent threads:
-// each warp takes 32 rays at a time from a global counter.
+// appended to the hit queue with one atomic per warp.
+//
+// Persistent threads with dynamic ray fetch (Aila & Laine 2009): between
+// traversal rounds, lanes whose ray has finished emit its result and take a
+// new ray from a global counter, so a warp is not held by its slowest ray.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) k_trace_render(DeviceScene S, RayQueueDev rq,
+template <int kMinBlocks>
+__global__ void __launch_bounds__(128, kMinBlocks) k_trace_render(DeviceScene S, RayQueueDev rq,
                                                       const ull* __restrict__ d_n,
                                                       HitQueueDev hq, ull* hq_n, float* accum,
                                                       ull* work, int* err)
 {
     const int64_t n = (int64_t)*d_n;
     const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    Traversal<false> tr;
+    uint32_t stack[kStackSize];
+    int64_t ray = -1;
+    bool exhausted = false;
+    bool overflow = false;
+    tr.cur = kSentinel;
     for (;;) {
-        ull base = 0;
-        if (lane == 0) base = atomicAdd(work, 32ull);
-        base = __shfl_sync(0xFFFFFFFFu, base, 0);
-        if ((int64_t)base >= n) break;
-        const int64_t i = (int64_t)base + lane;
-        const bool active = i < n;
-        TraceResult r;
-        r.leafpos = -1;
-        V3 o = {0, 0, 0}, d = {0, 0, 1};
-        if (active) {
-            o = v3(rq.ox[i], rq.oy[i], rq.oz[i]);
-            d = v3(rq.dx[i], rq.dy[i], rq.dz[i]);
-            traverse<false>(S, o, d, 0.001f, 1e9f, r, err);
-        }
-        __syncwarp();
-        const bool hit = active && r.leafpos >= 0;
-        int64_t pos = warp_append(hq_n, hit);
-        if (hit) {
-            if (pos < hq.capacity) {
-                hq.ray[pos] = (int32_t)i;
-                hq.tri[pos] = r.leafpos;
-                hq.t[pos] = r.t;
-                hq.bu[pos] = r.bu;
-                hq.bv[pos] = r.bv;
-            } else {
-                atomicOr(err, 2);
+        // 1. lanes whose traversal ended emit their result
+        const bool fin = ray >= 0 && tr.done();
+        const bool hit = fin && tr.res.leafpos >= 0;
+        const unsigned hm = __ballot_sync(0xFFFFFFFFu, hit);
+        if (hm) {
+            ull base = 0;
+            const int leader = __ffs(hm) - 1;
+            if (lane == leader) base = atomicAdd(hq_n, (ull)__popc(hm));
+            base = __shfl_sync(0xFFFFFFFFu, base, leader);
+            if (hit) {
+                const int64_t pos = (int64_t)base + __popc(hm & lt);
+                if (pos < hq.capacity) {
+                    hq.ray[pos] = (int32_t)ray;
+                    hq.tri[pos] = tr.res.leafpos;
+                    hq.t[pos] = tr.res.t;
+                    hq.bu[pos] = tr.res.bu;
+                    hq.bv[pos] = tr.res.bv;
+                } else {
+                    atomicOr(err, 2);
+                }
             }
-        } else if (active) {
-            V3 T = {rq.tr[i], rq.tg[i], rq.tb[i]};
-            accum_add(accum, rq.pixel[i], T * sky_color(S, d));
         }
+        if (fin && !hit) {
+            const V3 T = {rq.tr[ray], rq.tg[ray], rq.tb[ray]};
+            accum_add(accum, rq.pixel[ray], T * sky_color(S, tr.d));
+        }
+        if (fin) {
+            overflow = overflow || tr.overflow;
+            ray = -1;
+        }
+        // 2. lanes without a ray take new ones
+        const bool need = ray < 0 && !exhausted;
+        const unsigned nm = __ballot_sync(0xFFFFFFFFu, need);
+        if (nm) {
+            ull base = 0;
+            const int leader = __ffs(nm) - 1;
+            if (lane == leader) base = atomicAdd(work, (ull)__popc(nm));
+            base = __shfl_sync(0xFFFFFFFFu, base, leader);
+            if (need) {
+                const int64_t idx = (int64_t)base + __popc(nm & lt);
+                if (idx < n) {
+                    ray = idx;
+                    tr.init(S, stack, v3(rq.ox[idx], rq.oy[idx], rq.oz[idx]),
+                            v3(rq.dx[idx], rq.dy[idx], rq.dz[idx]), 0.001f, 1e9f);
+                } else {
+                    exhausted = true;
+                }
+            }
+        }
+        if (__all_sync(0xFFFFFFFFu, ray < 0)) break;
+        // 3. one traversal round
+        if (ray >= 0 && !tr.done()) tr.round(S, stack);
     }
+    if (overflow) atomicOr(err, 1);
 }
 
 // ---------------------------------------------------------------------------
@@ -353,26 +389,50 @@ __global__ void __launch_bounds__(128) k_shade(DeviceScene S, ShadeParams P, Ray
 }
 
 // Shadow rays (EmbreeAccelerator::occluded): unblocked contributions are
-// added to their pixel.
-__global__ void __launch_bounds__(128) k_occluded_render(DeviceScene S, ShadowQueueDev sh,
+// added to their pixel.  Same persistent, dynamic-fetch structure as
+// k_trace_render.
+template <int kMinBlocks>
+__global__ void __launch_bounds__(128, kMinBlocks) k_occluded_render(DeviceScene S, ShadowQueueDev sh,
                                                          const ull* __restrict__ d_n,
                                                          float* accum, ull* work, int* err)
 {
     const int64_t n = (int64_t)*d_n;
     const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    Traversal<true> tr;
+    uint32_t stack[kStackSize];
+    int64_t ray = -1;
+    bool exhausted = false;
+    bool overflow = false;
+    tr.cur = kSentinel;
     for (;;) {
-        ull base = 0;
-        if (lane == 0) base = atomicAdd(work, 32ull);
-        base = __shfl_sync(0xFFFFFFFFu, base, 0);
-        if ((int64_t)base >= n) break;
-        const int64_t i = (int64_t)base + lane;
-        if (i < n) {
-            V3 o = {sh.ox[i], sh.oy[i], sh.oz[i]}, d = {sh.dx[i], sh.dy[i], sh.dz[i]};
-            TraceResult r;
-            traverse<true>(S, o, d, 0.001f, sh.dist[i] - 0.001f, r, err);
-            if (r.leafpos < 0) accum_add(accum, sh.pixel[i], v3(sh.cr[i], sh.cg[i], sh.cb[i]));
+        if (ray >= 0 && tr.done()) {
+            if (tr.res.leafpos < 0) accum_add(accum, sh.pixel[ray], v3(sh.cr[ray], sh.cg[ray], sh.cb[ray]));
+            overflow = overflow || tr.overflow;
+            ray = -1;
         }
+        const bool need = ray < 0 && !exhausted;
+        const unsigned nm = __ballot_sync(0xFFFFFFFFu, need);
+        if (nm) {
+            ull base = 0;
+            const int leader = __ffs(nm) - 1;
+            if (lane == leader) base = atomicAdd(work, (ull)__popc(nm));
+            base = __shfl_sync(0xFFFFFFFFu, base, leader);
+            if (need) {
+                const int64_t idx = (int64_t)base + __popc(nm & lt);
+                if (idx < n) {
+                    ray = idx;
+                    tr.init(S, stack, v3(sh.ox[idx], sh.oy[idx], sh.oz[idx]),
+                            v3(sh.dx[idx], sh.dy[idx], sh.dz[idx]), 0.001f, sh.dist[idx] - 0.001f);
+                } else {
+                    exhausted = true;
+                }
+            }
+        }
+        if (__all_sync(0xFFFFFFFFu, ray < 0)) break;
+        if (ray >= 0 && !tr.done()) tr.round(S, stack);
     }
+    if (overflow) atomicOr(err, 1);
 }
 
 // ---------------------------------------------------------------------------
@@ -667,11 +727,18 @@ void launch_occluded_api(const DeviceScene& S, int64_t n, const float* ox, const
                                                              out, err);
 }
 
+// variant: 0 = no occupancy hint (~56 registers), 1 = 10 blocks of 128 per SM
+// (48 registers), 2 = 12 blocks (40 registers, small spills).
 void launch_trace_render(const DeviceScene& S, RayQueueDev rq, const ull* d_n, HitQueueDev hq,
                          ull* hq_n, float* accum, ull* work, int* err, LaunchCfg cfg,
                          cudaStream_t s)
 {
-    k_trace_render<<<cfg.grid, 128, 0, s>>>(S, rq, d_n, hq, hq_n, accum, work, err);
+    if (cfg.variant == 1)
+        k_trace_render<10><<<cfg.grid, 128, 0, s>>>(S, rq, d_n, hq, hq_n, accum, work, err);
+    else if (cfg.variant == 2)
+        k_trace_render<12><<<cfg.grid, 128, 0, s>>>(S, rq, d_n, hq, hq_n, accum, work, err);
+    else
+        k_trace_render<1><<<cfg.grid, 128, 0, s>>>(S, rq, d_n, hq, hq_n, accum, work, err);
 }
 
 void launch_shade(const DeviceScene& S, const ShadeParams& P, RayQueueDev rq, HitQueueDev hq,
@@ -684,7 +751,12 @@ void launch_shade(const DeviceScene& S, const ShadeParams& P, RayQueueDev rq, Hi
 void launch_occluded_render(const DeviceScene& S, ShadowQueueDev sh, const ull* sh_n, float* accum,
                             ull* work, int* err, LaunchCfg cfg, cudaStream_t s)
 {
-    k_occluded_render<<<cfg.grid, 128, 0, s>>>(S, sh, sh_n, accum, work, err);
+    if (cfg.variant == 1)
+        k_occluded_render<10><<<cfg.grid, 128, 0, s>>>(S, sh, sh_n, accum, work, err);
+    else if (cfg.variant == 2)
+        k_occluded_render<12><<<cfg.grid, 128, 0, s>>>(S, sh, sh_n, accum, work, err);
+    else
+        k_occluded_render<1><<<cfg.grid, 128, 0, s>>>(S, sh, sh_n, accum, work, err);
 }
 
 void launch_ray_keys(RayQueueDev rq, const ull* d_n, const float bmin[3], const float bmax[3],

@@ -53,82 +53,109 @@ __device__ __forceinline__ BvhNode load_node(const BvhNode* nodes, uint32_t i)
     return nd;
 }
 
-// Returns false (and sets *err_flag) only if the stack would overflow, which
-// the build rules out by checking the tree depth.
+constexpr uint32_t kSentinel = 0xFFFFFFFFu;
+
+// Resumable while-while traversal (Aila & Laine, "Understanding the
+// efficiency of ray traversal on GPUs", HPG 2009).  One call of round() walks
+// interior nodes down to a leaf, then leaves until it pops an interior node or
+// the stack's sentinel, so the lanes of a warp reconverge after every round
+// and a persistent kernel can hand a finished lane a new ray between rounds.
 template <bool kAnyHit>
-__device__ __forceinline__ bool traverse(const DeviceScene& S, V3 o, V3 d, float tmin, float tmax,
-                                         TraceResult& res, int* err_flag)
-{
-    res.leafpos = -1;
-    if (S.root_is_empty) return true;
-    V3 inv = {safe_inv(d.x), safe_inv(d.y), safe_inv(d.z)};
-    V3 oi = {o.x * inv.x, o.y * inv.y, o.z * inv.z};
-    uint32_t stack[kStackSize];
-    int sp = 0;
-    uint32_t cur = 0;
-    float best_t = tmax;
-    int best_g = -1;
-    for (;;) {
-        if (!(cur & kLeafFlag)) {
-            BvhNode nd = load_node(S.nodes, cur);
+struct Traversal {
+    V3 o, d, inv, oi;
+    float tmin, best_t;
+    int best_g;
+    uint32_t cur;
+    int sp;
+    bool overflow;
+    TraceResult res;
+
+    // The stack lives outside the struct (a dynamically indexed array would
+    // pull the whole struct into local memory); stack[0] holds the sentinel.
+    __device__ __forceinline__ void init(const DeviceScene& S, uint32_t* stack, V3 o_, V3 d_, float tmin_,
+                                         float tmax_)
+    {
+        o = o_;
+        d = d_;
+        inv = v3(safe_inv(d.x), safe_inv(d.y), safe_inv(d.z));
+        oi = v3(o.x * inv.x, o.y * inv.y, o.z * inv.z);
+        tmin = tmin_;
+        best_t = tmax_;
+        best_g = -1;
+        res.leafpos = -1;
+        sp = 0;
+        stack[sp++] = kSentinel;
+        cur = S.root_is_empty ? kSentinel : 0u;
+        overflow = false;
+    }
+    __device__ __forceinline__ bool done() const { return cur == kSentinel; }
+
+    __device__ __forceinline__ void round(const DeviceScene& S, uint32_t* stack)
+    {
+        while (!(cur & kLeafFlag)) {
+            const BvhNode nd = load_node(S.nodes, cur);
             float tn0, tn1;
             bool h0, h1;
             slab2(nd, inv, oi, tmin, best_t, tn0, tn1, h0, h1);
-            uint32_t c0 = (uint32_t)nd.kids.x, c1 = (uint32_t)nd.kids.y;
+            const uint32_t c0 = (uint32_t)nd.kids.x, c1 = (uint32_t)nd.kids.y;
             if (h0 && h1) {
-                uint32_t nearc = c0, farc = c1;
-                if (tn1 < tn0) {
-                    nearc = c1;
-                    farc = c0;
-                }
-                if (sp >= kStackSize) {
-                    atomicOr(err_flag, 1);
-                    return false;
-                }
-                stack[sp++] = farc;
-                cur = nearc;
-                continue;
-            } else if (h0) {
-                cur = c0;
-                continue;
-            } else if (h1) {
-                cur = c1;
-                continue;
+                const bool swap = tn1 < tn0;
+                const uint32_t farc = swap ? c0 : c1;
+                cur = swap ? c1 : c0;
+                if (sp < kStackSize)
+                    stack[sp++] = farc;
+                else
+                    overflow = true;
+            } else if (h0 || h1) {
+                cur = h0 ? c0 : c1;
+            } else {
+                cur = stack[--sp];
             }
-        } else {
-            int first = (int)((cur & ~kLeafFlag) >> 3);
-            int cnt = (int)(cur & 7u) + 1;
+        }
+        while (cur != kSentinel) {
+            if (!(cur & kLeafFlag)) break;
+            const int first = (int)((cur & ~kLeafFlag) >> 3);
+            const int cnt = (int)(cur & 7u) + 1;
+            bool stop = false;
             for (int k = 0; k < cnt; ++k) {
-                int lp = first + k;
-                float4 a = __ldg(S.tris + 3 * lp + 0);
-                float4 b = __ldg(S.tris + 3 * lp + 1);
-                float4 c = __ldg(S.tris + 3 * lp + 2);
+                const int lp = first + k;
+                const float4 a = __ldg(S.tris + 3 * lp + 0);
+                const float4 b = __ldg(S.tris + 3 * lp + 1);
+                const float4 c = __ldg(S.tris + 3 * lp + 2);
                 float th, uh, vh;
-                if (intersect_triangle(o, d, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), v3(c.x, c.y, c.z),
-                                       tmin, best_t, th, uh, vh)) {
-                    if (kAnyHit) {
-                        res.leafpos = lp;
-                        res.t = th;
-                        res.bu = uh;
-                        res.bv = vh;
-                        return true;
-                    }
-                    int g = __float_as_int(a.w);
-                    if (th < best_t || res.leafpos < 0 || g > best_g) {
+                if (intersect_triangle(o, d, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), v3(c.x, c.y, c.z), tmin,
+                                       best_t, th, uh, vh)) {
+                    const int g = __float_as_int(a.w);
+                    if (kAnyHit || th < best_t || res.leafpos < 0 || g > best_g) {
                         res.leafpos = lp;
                         res.t = th;
                         res.bu = uh;
                         res.bv = vh;
                         best_t = th;
                         best_g = g;
+                        if (kAnyHit) stop = true;
                     }
                 }
             }
+            cur = stop ? kSentinel : stack[--sp];
         }
-        if (sp == 0) break;
-        cur = stack[--sp];
     }
-    return true;
+};
+
+// Whole traversal of one ray (host-API kernels).  Returns false (and sets
+// *err_flag) only if the stack would overflow, which the build rules out by
+// checking the tree depth.
+template <bool kAnyHit>
+__device__ __forceinline__ bool traverse(const DeviceScene& S, V3 o, V3 d, float tmin, float tmax,
+                                         TraceResult& res, int* err_flag)
+{
+    Traversal<kAnyHit> tr;
+    uint32_t stack[kStackSize];
+    tr.init(S, stack, o, d, tmin, tmax);
+    while (!tr.done()) tr.round(S, stack);
+    res = tr.res;
+    if (tr.overflow) atomicOr(err_flag, 1);
+    return !tr.overflow;
 }
 
 }  // namespace wf
