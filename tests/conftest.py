@@ -72,3 +72,36 @@ def rays_in_box(rng, n, lo, hi):
     d = rng.normal(size=(n, 3))
     d /= np.linalg.norm(d, axis=1, keepdims=True)
     return o, d.astype(np.float32)
+
+
+def fp64_band(img, spp, golden, block=8):
+    """Check (c): an image rendered with `spp` samples against the
+    reference's FP64 per-pixel mean (`golden["mean"]`) and per-sample standard
+    deviation (`golden["sigma"]`) over 16384 spp.
+
+    Per-pixel samples are heavy-tailed here (rare paths clamped at the
+    firefly threshold of 10), so the 3-sigma band is applied to block means of
+    block x block pixels (block*block*spp samples each):
+      * bias: the mean of the block z-scores is within 3 standard errors of 0;
+      * variance: their standard deviation is 1 +- 0.15;
+      * tail: |z| > 3 on fewer than 3% of blocks (a normal tail gives 0.27%);
+      * MSE against the FP64 mean is within 20% of sum(sigma^2)/spp;
+      * channel means within 1%.
+    Returns the figures (MSE included) for reporting."""
+    H, W, _ = img.shape
+    mean, sigma = golden["mean"].astype(np.float64), golden["sigma"].astype(np.float64)
+    bm = mean.reshape(H // block, block, W // block, block, 3).mean((1, 3))
+    bx = img.astype(np.float64).reshape(H // block, block, W // block, block, 3).mean((1, 3))
+    bv = (sigma ** 2 / spp).reshape(H // block, block, W // block, block, 3).sum((1, 3)) / block ** 4
+    z = (bx - bm) / np.sqrt(np.maximum(bv, 1e-12))
+    mse = float(((img - mean) ** 2).mean())
+    expected = float((sigma ** 2 / spp).mean())
+    out = {"mse": mse, "expected_mse": expected, "z_mean": float(z.mean()), "z_std": float(z.std()),
+           "tail_frac": float((np.abs(z) > 3).mean()),
+           "channel_rel": (img.mean((0, 1)) / mean.mean((0, 1)) - 1).tolist()}
+    assert abs(out["z_mean"]) < 3.0 / np.sqrt(z.size), out
+    assert abs(out["z_std"] - 1.0) < 0.15, out
+    assert out["tail_frac"] < 0.03, out
+    assert mse < 1.2 * expected, out
+    assert max(abs(c) for c in out["channel_rel"]) < 0.01, out
+    return out
