@@ -303,6 +303,30 @@ int wf_generate_primary_host(wf_ctx* ctx, const wf_camera* camera, int32_t width
                              float* origins_y, float* origins_z, float* dirs_x, float* dirs_y,
                              float* dirs_z, int32_t* pixel_indices, int32_t* sample_indices);
 
+/* RayQueue sort for callers that cannot allocate device memory.  This entry
+ * point has no counterpart in the reference.  It computes the same keys and
+ * permutation as wf_ray_schedule_host, but takes DEVICE pointers (inputs and
+ * outputs owned by the caller), needs no context, and calls no cudaMalloc,
+ * cudaFree or other allocating routine: its scratch is one file-scope device
+ * array sized for WF_STATIC_SCHEDULE_MAX_RAYS rays (~25 MB, held by every GPU
+ * that loads the library until the process exits).  Callers it is for: code
+ * running under a framework that owns the device heap, loops with a
+ * no-allocation rule, code preparing work during stream capture.
+ *  - Work is enqueued on `stream` (a cudaStream_t; NULL = the legacy default
+ *    stream) of the CURRENT device; the call returns without waiting.
+ *  - The first call on a device looks up the array's device address
+ *    (cudaGetSymbolAddress); make that first call before any stream capture.
+ *  - All calls share the one array, which keeps the last call's contents:
+ *    calls whose GPU work overlaps (other streams, other host threads) race.
+ *    Serialise them on one stream.
+ *  - n > WF_STATIC_SCHEDULE_MAX_RAYS returns WF_ERR_CAPACITY and enqueues
+ *    nothing.  out_keys may be NULL. */
+#define WF_STATIC_SCHEDULE_MAX_RAYS (1 << 20)
+int wf_ray_schedule_static(void* stream, int64_t n, const float* origins_x, const float* origins_y,
+                           const float* origins_z, const float* dirs_x, const float* dirs_y,
+                           const float* dirs_z, const float bounds_min[3], const float bounds_max[3],
+                           int32_t* out_sorted_indices, uint64_t* out_keys);
+
 /* ---- scheduling (host buffers) ---------------------------------------------- */
 
 /* RayQueue::sortKey + RayQueue::schedule (include/scheduling/RayQueue.h

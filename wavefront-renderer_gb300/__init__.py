@@ -39,6 +39,7 @@ POLICY_NONE, POLICY_MATERIAL, POLICY_TEXTURE, POLICY_COST_BENEFIT = range(4)
 POLICIES = {"none": 0, "material": 1, "texture": 2, "costBenefit": 3}
 TEXEL_RGB32F, TEXEL_RGBA8_SRGB = 0, 1
 
+STATIC_SCHEDULE_MAX_RAYS = 1 << 20  # WF_STATIC_SCHEDULE_MAX_RAYS
 f32p = C.POINTER(C.c_float)
 i32p = C.POINTER(C.c_int32)
 u8p = C.POINTER(C.c_uint8)
@@ -180,6 +181,7 @@ def _declare(lib: C.CDLL) -> None:
         "wf_trace_occluded_host": ([V, C.c_int64] + [f32p] * 7 + [u8p], C.c_int),
         "wf_generate_primary_host": ([V, C.POINTER(WfCamera), C.c_int32, C.c_int32, C.c_uint32, C.c_uint32,
                                       C.c_int32, C.c_int32] + [f32p] * 6 + [i32p, i32p], C.c_int),
+        "wf_ray_schedule_static": ([V, C.c_int64] + [C.c_void_p] * 6 + [f32p, f32p, C.c_void_p, C.c_void_p], C.c_int),
         "wf_ray_schedule_host": ([V, C.c_int64] + [f32p] * 6 + [f32p, f32p, i32p, u64p], C.c_int),
         "wf_shading_schedule_host": ([V, C.c_int32, C.c_int64, i32p, i32p] + [f32p] * 6 +
                                      [C.c_int32, C.POINTER(WfMaterial), C.c_int32, i64p, f64p, f64p, i32p], C.c_int),
