@@ -244,11 +244,14 @@ int wf_scene_get_info(wf_ctx* ctx, wf_scene_info* out_info);
 /* Launch tuning of a context (the autotuner's knobs).  trace_variant: 0 = no
  * occupancy hint on the traversal kernels, 1 = 10 blocks of 128 threads per
  * SM, 2 = 12 blocks.  persistent_blocks_per_sm: resident blocks launched per
- * SM by the persistent traversal kernels (0 = 16). */
+ * SM by the persistent traversal kernels (0 = 16).  graph_mode: whether a
+ * wave's bounce chain is captured once as a CUDA graph and replayed. */
 typedef struct wf_tuning {
     int32_t trace_variant;
     int32_t persistent_blocks_per_sm;
-    int32_t reserved[6];
+    int32_t graph_mode;  /* 0 = graphs for batches and the server, 1 = also for
+                            single renders, 2 = never (policy != none never) */
+    int32_t reserved[5];
 } wf_tuning;
 int wf_set_tuning(wf_ctx* ctx, const wf_tuning* tuning);
 int wf_get_tuning(const wf_ctx* ctx, wf_tuning* out_tuning);
@@ -389,6 +392,95 @@ int wf_get_stream(wf_ctx* ctx, void** out_stream);
 int wf_timer_begin(wf_ctx* ctx);
 int wf_timer_end(wf_ctx* ctx, double* out_ms);
 
+/* ---- resident scenes, jobs, batches ------------------------------------------ */
+
+/* More scenes kept resident beside the current one (slot 0, set by
+ * wf_scene_upload): BVH, triangles, materials and textures stay on the device
+ * so jobs over several scenes can share one wavefront.  No counterpart in the
+ * reference (it renders one Scene per process). */
+int wf_scene_add(wf_ctx* ctx, const wf_scene_desc* scene, int32_t* out_scene_id);
+int wf_scene_remove(wf_ctx* ctx, int32_t scene_id);
+int wf_scene_get_info_id(wf_ctx* ctx, int32_t scene_id, wf_scene_info* out_info);
+
+/* One render request: a renderScene call (WavefrontRenderer.cpp:94-399,
+ * adaptive sampling off, policy none) on a resident scene. */
+typedef struct wf_job {
+    int32_t scene_id;
+    int32_t width;
+    int32_t height;
+    int32_t samples_per_pixel;
+    int32_t max_depth;
+    int32_t rr_min_depth;
+    int32_t enable_cost_aware_rr;
+    float firefly_threshold;
+    uint32_t seed_lo;
+    uint32_t seed_hi;
+    int32_t first_sample;
+    int32_t reserved;
+    const double* rel_cost_material; /* frozen relativeCost per material or NULL */
+    wf_camera camera;
+} wf_job;
+
+/* Renders njobs jobs to completion with the rays of all jobs sharing each
+ * wave (per-ray job ids); each job's random streams are keyed by its own
+ * seed, so its image equals a wf_render of it alone up to the order of float
+ * additions.  images[j] (host, width*height*3 floats) receives job j's
+ * averaged image; NULL skips it. */
+int wf_render_batch(wf_ctx* ctx, const wf_job* jobs, int32_t njobs, float* const* images,
+                    wf_render_stats* stats);
+
+/* ---- serving loop ------------------------------------------------------------- */
+
+/* A render service on one context: jobs are admitted while their
+ * accumulators fit the HBM budget (beside the fixed wave buffers), every step
+ * runs one wave over the admitted jobs (up to frame_spp samples of each), a
+ * job's progressive frame is ready every frame_spp samples.  Times are
+ * seconds on the server's monotonic clock.  No counterpart in the reference
+ * (it renders one image per process; its GUI polls a preview file). */
+typedef struct wf_server wf_server;
+typedef struct wf_server_config {
+    int64_t hbm_budget_bytes;   /* accumulators + wave buffers              */
+    int64_t max_paths_per_wave; /* 0 = context default                      */
+    int32_t frame_spp;          /* samples per progressive frame (8)        */
+    int32_t reserved[7];
+} wf_server_config;
+enum {
+    WF_JOB_QUEUED = 0,
+    WF_JOB_RUNNING = 1,
+    WF_JOB_DONE = 2,
+    WF_JOB_CANCELLED = 3,
+    WF_JOB_REJECTED = 4 /* larger than the whole budget */
+};
+typedef struct wf_job_status {
+    int32_t state;
+    int32_t samples_done;
+    int32_t frames;
+    int32_t reserved;
+    double t_submit;
+    double t_admit;
+    double t_first_frame;
+    double t_done;
+} wf_job_status;
+typedef struct wf_server_step_info {
+    int32_t queued;
+    int32_t running;
+    int32_t completed_this_step;
+    int32_t jobs_in_wave;
+    int64_t paths_in_wave;
+    uint64_t rays_traced;       /* closest + shadow rays of this step       */
+    double step_ms;             /* device time of the wave                  */
+    int64_t budget_used_bytes;
+} wf_server_step_info;
+int wf_server_create(wf_ctx* ctx, const wf_server_config* config, wf_server** out_server);
+int wf_server_destroy(wf_server* server);
+int wf_server_submit(wf_server* server, const wf_job* job, int64_t* out_job_id);
+int wf_server_step(wf_server* server, wf_server_step_info* out_info);
+int wf_server_status(wf_server* server, int64_t job_id, wf_job_status* out_status);
+/* The job's current averaged image (progressive) or final image. */
+int wf_server_image(wf_server* server, int64_t job_id, float* image_rgb, int64_t num_floats);
+int wf_server_cancel(wf_server* server, int64_t job_id);
+double wf_server_clock(const wf_server* server);
+
 /* ---- procedural scenes (host only) ------------------------------------------- */
 
 /* The synthetic workloads that stand in for the reference's stress scenes:
@@ -396,6 +488,9 @@ int wf_timer_end(wf_ctx* ctx, double* out_ms);
  *      reference's CornellBox::addQuad/addRotatedBox build it)
  *   1  config-0 room plus a displaced icosphere (subdivision 8, 1,310,720
  *      triangles) split into Lambert / metal / glass regions
+ *   3  a job scene of the batched workload: seeded variant `seed` of config 0
+ *      (albedos, metal roughness, light position, camera jitter)
+ * 100  config 1 at subdivision 4 (5,132 triangles), for fast tests
  * The scene owns its arrays until wf_host_scene_free. */
 typedef struct wf_host_scene wf_host_scene;
 int wf_host_scene_generate(int32_t config, uint64_t seed, wf_host_scene** out_scene);

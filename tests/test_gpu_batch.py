@@ -1,0 +1,139 @@
+"""Batched jobs (config 3) and the serving loop (config 4) on the GPU.
+
+A job's random streams are keyed by its own seed and (pixel, sample, depth),
+so the paths it traces do not depend on which other jobs share its waves; only
+the order of the float additions into its pixels does (atomics).  Tolerance:
+the image of a job in a mix equals its image alone within 1e-4 relative +
+1e-6 absolute on at least 99.9% of pixels.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+RES = [(24, 16), (32, 32), (48, 40), (64, 64)]
+
+
+def _jobs(wf, ctx, n, seed0=100, scenes=None):
+    """n config-3 jobs on their own resident scene variants."""
+    jobs, hosts = [], []
+    rng = np.random.default_rng(seed0)
+    for k in range(n):
+        hs = wf.HostScene(3, seed=seed0 + k)
+        sid = ctx.add_scene(hs.desc)
+        w, h = RES[k % len(RES)]
+        spp = int(rng.choice([2, 4, 8]))
+        cam = hs.camera(w, h)
+        jobs.append(wf.make_job(sid, w, h, spp, 8, cam, seed=7000 + k))
+        hosts.append(hs)
+    return jobs, hosts
+
+
+def _same(a, b):
+    return np.isclose(a, b, rtol=1e-4, atol=1e-6).all(axis=2).mean()
+
+
+def test_batch_job_equals_job_alone(wf, ctx):
+    jobs, hosts = _jobs(wf, ctx, 12)
+    imgs, st = ctx.render_batch(jobs)
+    assert st["closest_rays"] > 0 and st["waves"] >= 1
+    for j, hs, img in zip(jobs, hosts, imgs):
+        ctx.upload(hs.desc)  # slot 0: the single-scene path
+        alone, _ = ctx.render(wf.render_params(j.width, j.height, j.samples_per_pixel, j.max_depth, j.camera,
+                                               seed=j.seed_lo))
+        assert _same(img, alone) >= 0.999
+
+
+def test_batch_job_matches_oracle(wf, orc, ctx):
+    jobs, hosts = _jobs(wf, ctx, 3, seed0=300)
+    imgs, _ = ctx.render_batch(jobs)
+    for j, hs, img in zip(jobs, hosts, imgs):
+        port = orc.Port(hs.desc)
+        p = wf.render_params(j.width, j.height, j.samples_per_pixel, j.max_depth, j.camera, seed=j.seed_lo)
+        acc, _ = port.render_window(p, 0, 0, j.width, j.height)
+        agree = np.isclose(img, acc / j.samples_per_pixel, rtol=1e-3, atol=1e-4).all(axis=2).mean()
+        assert agree >= 0.97
+
+
+def test_graph_replay_equals_host_loop(wf, ctx, scene_small):
+    ctx.upload(scene_small.desc)
+    cam = scene_small.camera(48, 48)
+    p = wf.render_params(48, 48, 8, 12, cam, seed=11, spp_per_wave=3)
+    ctx.set_tuning(graph_mode=2)
+    host, st_h = ctx.render(p)
+    ctx.set_tuning(graph_mode=1)
+    graph, st_g = ctx.render(p)
+    ctx.set_tuning()
+    assert _same(graph, host) >= 0.999
+    assert st_g["closest_rays"] == st_h["closest_rays"]
+    assert st_g["shadow_rays"] == st_h["shadow_rays"]
+
+
+def test_server_progressive_frames_and_final_images(wf, ctx):
+    jobs, hosts = _jobs(wf, ctx, 10, seed0=500)
+    for j in jobs:
+        j.samples_per_pixel = 16
+    srv = wf.Server(ctx, hbm_budget_bytes=64 << 20, frame_spp=4, max_paths_per_wave=1 << 16)
+    ids = [srv.submit(j) for j in jobs]
+    saw_progressive = False
+    for _ in range(200):
+        info = srv.step()
+        assert info["budget_used_bytes"] <= 64 << 20
+        for i, j in zip(ids, jobs):
+            st = srv.status(i)
+            if st["state"] == wf.JOB_RUNNING and 0 < st["samples_done"] < 16:
+                srv.image(i, j.width, j.height)  # a progressive frame is readable
+                saw_progressive = True
+        if info["running"] == 0 and info["queued"] == 0:
+            break
+    assert saw_progressive
+    for i, j, hs in zip(ids, jobs, hosts):
+        st = srv.status(i)
+        assert st["state"] == wf.JOB_DONE and st["samples_done"] == 16 and st["frames"] == 4
+        assert st["t_submit"] <= st["t_admit"] <= st["t_first_frame"] <= st["t_done"]
+        final = srv.image(i, j.width, j.height)
+        ctx.upload(hs.desc)
+        alone, _ = ctx.render(wf.render_params(j.width, j.height, 16, j.max_depth, j.camera, seed=j.seed_lo))
+        assert _same(final, alone) >= 0.999
+    srv.close()
+
+
+def test_server_admission_respects_budget(wf, ctx):
+    jobs, hosts = _jobs(wf, ctx, 6, seed0=700)
+    for j in jobs:
+        j.width, j.height, j.samples_per_pixel = 64, 64, 8
+    wave = 1 << 14
+    per_path = 2 * 14 * 4 + 2 * 5 * 4 + 2 * 12 * 4 + 2 * 12 + 8 * 4
+    budget = wave * per_path + 2 * 64 * 64 * 3 * 4  # room for two accumulators
+    srv = wf.Server(ctx, hbm_budget_bytes=budget, frame_spp=8, max_paths_per_wave=wave)
+    ids = [srv.submit(j) for j in jobs]
+    big = wf.make_job(jobs[0].scene_id, 512, 512, 4, 8, jobs[0].camera)
+    big_id = srv.submit(big)
+    assert srv.status(big_id)["state"] == wf.JOB_REJECTED
+    max_running = 0
+    for _ in range(100):
+        info = srv.step()
+        max_running = max(max_running, info["running"] + info["completed_this_step"])
+        assert info["budget_used_bytes"] <= budget
+        if info["running"] == 0 and info["queued"] == 0:
+            break
+    assert max_running <= 2
+    assert all(srv.status(i)["state"] == wf.JOB_DONE for i in ids)
+    srv.close()
+
+
+def test_server_cancel(wf, ctx):
+    jobs, hosts = _jobs(wf, ctx, 3, seed0=900)
+    srv = wf.Server(ctx, hbm_budget_bytes=64 << 20, frame_spp=2, max_paths_per_wave=1 << 14)
+    ids = [srv.submit(j) for j in jobs]
+    srv.step()
+    srv.cancel(ids[0])
+    for _ in range(50):
+        info = srv.step()
+        if info["running"] == 0 and info["queued"] == 0:
+            break
+    assert srv.status(ids[0])["state"] == wf.JOB_CANCELLED
+    assert all(srv.status(i)["state"] == wf.JOB_DONE for i in ids[1:])
+    srv.close()

@@ -118,7 +118,42 @@ class WfSceneInfo(C.Structure):
 
 
 class WfTuning(C.Structure):
-    _fields_ = [("trace_variant", C.c_int32), ("persistent_blocks_per_sm", C.c_int32), ("reserved", C.c_int32 * 6)]
+    _fields_ = [("trace_variant", C.c_int32), ("persistent_blocks_per_sm", C.c_int32), ("graph_mode", C.c_int32),
+                ("reserved", C.c_int32 * 5)]
+
+
+class WfJob(C.Structure):
+    _fields_ = [("scene_id", C.c_int32), ("width", C.c_int32), ("height", C.c_int32),
+                ("samples_per_pixel", C.c_int32), ("max_depth", C.c_int32), ("rr_min_depth", C.c_int32),
+                ("enable_cost_aware_rr", C.c_int32), ("firefly_threshold", C.c_float), ("seed_lo", C.c_uint32),
+                ("seed_hi", C.c_uint32), ("first_sample", C.c_int32), ("reserved", C.c_int32),
+                ("rel_cost_material", f64p), ("camera", WfCamera)]
+
+
+class WfServerConfig(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_int64), ("max_paths_per_wave", C.c_int64), ("frame_spp", C.c_int32),
+                ("reserved", C.c_int32 * 7)]
+
+
+class WfJobStatus(C.Structure):
+    _fields_ = [("state", C.c_int32), ("samples_done", C.c_int32), ("frames", C.c_int32), ("reserved", C.c_int32),
+                ("t_submit", C.c_double), ("t_admit", C.c_double), ("t_first_frame", C.c_double),
+                ("t_done", C.c_double)]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_ if name != "reserved"}
+
+
+class WfServerStepInfo(C.Structure):
+    _fields_ = [("queued", C.c_int32), ("running", C.c_int32), ("completed_this_step", C.c_int32),
+                ("jobs_in_wave", C.c_int32), ("paths_in_wave", C.c_int64), ("rays_traced", C.c_uint64),
+                ("step_ms", C.c_double), ("budget_used_bytes", C.c_int64)]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+JOB_QUEUED, JOB_RUNNING, JOB_DONE, JOB_CANCELLED, JOB_REJECTED = range(5)
 
 
 class WfHitColumns(C.Structure):
@@ -192,6 +227,18 @@ def _declare(lib: C.CDLL) -> None:
         "wf_get_stream": ([V, C.POINTER(V)], C.c_int),
         "wf_timer_begin": ([V], C.c_int),
         "wf_set_tuning": ([V, C.POINTER(WfTuning)], C.c_int),
+        "wf_scene_add": ([V, C.POINTER(WfSceneDesc), C.POINTER(C.c_int32)], C.c_int),
+        "wf_scene_remove": ([V, C.c_int32], C.c_int),
+        "wf_scene_get_info_id": ([V, C.c_int32, C.POINTER(WfSceneInfo)], C.c_int),
+        "wf_render_batch": ([V, C.POINTER(WfJob), C.c_int32, C.POINTER(f32p), C.POINTER(WfRenderStats)], C.c_int),
+        "wf_server_create": ([V, C.POINTER(WfServerConfig), C.POINTER(V)], C.c_int),
+        "wf_server_destroy": ([V], C.c_int),
+        "wf_server_submit": ([V, C.POINTER(WfJob), C.POINTER(C.c_int64)], C.c_int),
+        "wf_server_step": ([V, C.POINTER(WfServerStepInfo)], C.c_int),
+        "wf_server_status": ([V, C.c_int64, C.POINTER(WfJobStatus)], C.c_int),
+        "wf_server_image": ([V, C.c_int64, f32p, C.c_int64], C.c_int),
+        "wf_server_cancel": ([V, C.c_int64], C.c_int),
+        "wf_server_clock": ([V], C.c_double),
         "wf_get_tuning": ([V, C.POINTER(WfTuning)], C.c_int),
         "wf_timer_end": ([V, f64p], C.c_int),
         "wf_host_scene_generate": ([C.c_int32, C.c_uint64, C.POINTER(V)], C.c_int),
@@ -209,7 +256,7 @@ def header_symbols() -> list[str]:
     """Every function the C header declares."""
     import re
     text = HEADER.read_text()
-    return sorted(set(re.findall(r"^(?:int|const char\*|void)\s+(wf_\w+)\s*\(", text, re.M)))
+    return sorted(set(re.findall(r"^(?:int|const char\*|void|double)\s+(wf_\w+)\s*\(", text, re.M)))
 
 
 class WfError(RuntimeError):
@@ -267,6 +314,64 @@ def camera_make(look_from, look_at, up, vfov, width, height) -> WfCamera:
     _check(load_library().wf_camera_make(ptr(a[0]), ptr(a[1]), ptr(a[2]), vfov, width, height, C.byref(cam)),
            "wf_camera_make")
     return cam
+
+
+def make_job(scene_id, width, height, spp, max_depth, camera: WfCamera, *, seed=1, rr_min_depth=3, firefly=10.0,
+             first_sample=0) -> WfJob:
+    j = WfJob()
+    j.scene_id, j.width, j.height, j.samples_per_pixel, j.max_depth = scene_id, width, height, spp, max_depth
+    j.rr_min_depth, j.firefly_threshold, j.first_sample = rr_min_depth, firefly, first_sample
+    j.seed_lo, j.seed_hi = seed & 0xFFFFFFFF, (seed >> 32) & 0xFFFFFFFF
+    j.camera = camera
+    return j
+
+
+class Server:
+    """The serving loop (wf_server_*): admission by HBM budget, one shared
+    wave per step, progressive frames every frame_spp samples."""
+
+    def __init__(self, ctx: "Context", hbm_budget_bytes: int, frame_spp: int = 8, max_paths_per_wave: int = 0):
+        self.ctx = ctx
+        self._h = C.c_void_p()
+        cfg = WfServerConfig(hbm_budget_bytes, max_paths_per_wave, frame_spp)
+        _check(load_library().wf_server_create(ctx._h, C.byref(cfg), C.byref(self._h)), "wf_server_create", ctx)
+
+    def close(self):
+        if self._h:
+            load_library().wf_server_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, job: WfJob) -> int:
+        jid = C.c_int64()
+        _check(load_library().wf_server_submit(self._h, C.byref(job), C.byref(jid)), "wf_server_submit", self.ctx)
+        return jid.value
+
+    def step(self) -> dict:
+        info = WfServerStepInfo()
+        _check(load_library().wf_server_step(self._h, C.byref(info)), "wf_server_step", self.ctx)
+        return info.as_dict()
+
+    def status(self, jid: int) -> dict:
+        st = WfJobStatus()
+        _check(load_library().wf_server_status(self._h, jid, C.byref(st)), "wf_server_status", self.ctx)
+        return st.as_dict()
+
+    def image(self, jid: int, width: int, height: int) -> np.ndarray:
+        img = np.zeros(width * height * 3, np.float32)
+        _check(load_library().wf_server_image(self._h, jid, ptr(img), img.size), "wf_server_image", self.ctx)
+        return img.reshape(height, width, 3)
+
+    def cancel(self, jid: int) -> None:
+        _check(load_library().wf_server_cancel(self._h, jid), "wf_server_cancel", self.ctx)
+
+    def clock(self) -> float:
+        return load_library().wf_server_clock(self._h)
 
 
 def render_params(width, height, spp, max_depth, camera: WfCamera, *, policy=0, ray_sort=False,
@@ -399,14 +504,33 @@ class Context:
         _check(load_library().wf_image_download(self._h, ptr(img), img.size), "wf_image_download", self)
         return img.reshape(height, width, 3)
 
-    def set_tuning(self, trace_variant: int = 0, persistent_blocks_per_sm: int = 0) -> None:
-        t = WfTuning(trace_variant, persistent_blocks_per_sm)
+    def set_tuning(self, trace_variant: int = 0, persistent_blocks_per_sm: int = 0, graph_mode: int = 0) -> None:
+        t = WfTuning(trace_variant, persistent_blocks_per_sm, graph_mode)
         _check(load_library().wf_set_tuning(self._h, C.byref(t)), "wf_set_tuning", self)
 
     def get_tuning(self) -> dict:
         t = WfTuning()
         _check(load_library().wf_get_tuning(self._h, C.byref(t)), "wf_get_tuning", self)
-        return {"trace_variant": t.trace_variant, "persistent_blocks_per_sm": t.persistent_blocks_per_sm}
+        return {"trace_variant": t.trace_variant, "persistent_blocks_per_sm": t.persistent_blocks_per_sm,
+                "graph_mode": t.graph_mode}
+
+    def add_scene(self, desc: WfSceneDesc) -> int:
+        sid = C.c_int32()
+        _check(load_library().wf_scene_add(self._h, C.byref(desc), C.byref(sid)), "wf_scene_add", self)
+        return sid.value
+
+    def remove_scene(self, sid: int) -> None:
+        _check(load_library().wf_scene_remove(self._h, sid), "wf_scene_remove", self)
+
+    def render_batch(self, jobs: list, want_images: bool = True):
+        n = len(jobs)
+        arr = (WfJob * n)(*jobs)
+        imgs = [np.zeros(j.width * j.height * 3, np.float32) for j in jobs] if want_images else []
+        ptrs = (f32p * n)(*[ptr(a) for a in imgs]) if want_images else None
+        st = WfRenderStats()
+        _check(load_library().wf_render_batch(self._h, arr, n, ptrs, C.byref(st)), "wf_render_batch", self)
+        out = [a.reshape(j.height, j.width, 3) for a, j in zip(imgs, jobs)]
+        return out, st.as_dict()
 
     def timer_begin(self) -> None:
         _check(load_library().wf_timer_begin(self._h), "wf_timer_begin", self)

@@ -1,6 +1,7 @@
-// wf_api.cpp — the C ABI (include/wf_api.h): context, scene upload, stage
-// entry points and the wavefront render loop
-// (reference src/render/WavefrontRenderer.cpp:94-399).
+// wf_api.cpp — the C ABI (include/wf_api.h): context, resident scenes, the
+// stage entry points on host buffers, tuning and timers.  The render loop
+// itself (single renders, batches of jobs, the serving loop) is in
+// wf_loop.cpp.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -14,99 +15,19 @@
 
 #include "../../include/wf_api.h"
 #include "wf_bvh.h"
+#include "wf_ctx.h"
 #include "wf_device.cuh"
 #include "wf_kernels.h"
 #include "wf_sort.h"
 
 using namespace wf;
 
-namespace {
-
-constexpr int64_t kDefaultPathsPerWave = int64_t(1) << 23;  // ~8.4 M paths in flight
-
-// Device allocation owned by a context.
-struct DevBuf {
-    void* p = nullptr;
-    size_t bytes = 0;
-};
-
-}  // namespace
-
-struct wf_ctx {
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    int num_sms = 1;
-    std::string last_error;
-    int64_t paths_per_wave = kDefaultPathsPerWave;
-
-    // Scene
-    bool has_scene = false;
-    DeviceScene S{};
-    std::vector<void*> scene_allocs;
-    wf_scene_info info{};
-    std::vector<wf_material> mats;
-    std::vector<int64_t> tex_bytes;
-    int64_t* d_tex_bytes = nullptr;
-
-    // Render buffers (grown on demand)
-    int64_t cap = 0;
-    RayQueueDev rq[2]{};
-    HitQueueDev hq[2]{};
-    ShadowQueueDev sh{};
-    uint64_t *keys = nullptr, *keys_tmp = nullptr;
-    uint32_t *vals = nullptr, *vals_tmp = nullptr, *hist = nullptr;
-    int nb = 1;
-    // scheduling columns
-    int32_t *col_mat = nullptr, *col_tex = nullptr;
-    float *col_tr = nullptr, *col_tg = nullptr, *col_tb = nullptr, *col_px = nullptr,
-          *col_py = nullptr, *col_pz = nullptr;
-    std::vector<void*> render_allocs;
-
-    // Small device state
-    ull* counters = nullptr;  // [0] rays [1] hits [2] shadows [3] next [4] work [5] work2 [6] aux
-    int* err_flag = nullptr;
-    ull* stats8 = nullptr;     // type counts [8], mem [8]
-    int* first8 = nullptr;     // first index per type
-    int* rank_buf = nullptr;   // cost / texture / priority ranks
-    int rank_cap = 0;
-    double* benefit = nullptr; // per material
-    int* present = nullptr;    // per material
-    unsigned* bounds6 = nullptr;
-    float* rel_cost_f = nullptr;
-    int rel_cost_cap = 0;
-    int last_schedule_launches = 0;
-    // Image of the last wf_render_device
-    float* image = nullptr;
-    int64_t image_floats = 0;
-
-    cudaEvent_t ev[8]{};
-    cudaEvent_t timer[2]{};
-    wf_tuning tuning{};
-};
-
-namespace {
+namespace wf {
 
 int set_err(wf_ctx* c, int code, const std::string& msg)
 {
     if (c) c->last_error = msg;
     return code;
-}
-
-#define WF_CK(ctx, x)                                                                 \
-    do {                                                                              \
-        cudaError_t e_ = (x);                                                         \
-        if (e_ != cudaSuccess)                                                        \
-            return set_err(ctx, WF_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_)); \
-    } while (0)
-
-template <class T>
-cudaError_t dalloc(std::vector<void*>& owner, T** p, size_t count)
-{
-    *p = nullptr;
-    if (count == 0) count = 1;
-    cudaError_t e = cudaMalloc((void**)p, sizeof(T) * count);
-    if (e == cudaSuccess) owner.push_back((void*)*p);
-    return e;
 }
 
 void free_all(std::vector<void*>& v)
@@ -115,69 +36,122 @@ void free_all(std::vector<void*>& v)
     v.clear();
 }
 
-LaunchCfg persist(const wf_ctx* c)
+LaunchCfg persist_cfg(const wf_ctx* c)
 {
     int per_sm = c->tuning.persistent_blocks_per_sm > 0 ? c->tuning.persistent_blocks_per_sm : 16;
     return LaunchCfg{c->num_sms * per_sm, 128, c->tuning.trace_variant};
 }
-LaunchCfg wide(const wf_ctx* c) { return LaunchCfg{c->num_sms * 8, 256}; }
 
-// srgbToLinear, reference src/shading/Texture.cpp:20-27.
-float srgb_to_linear(float s)
-{
-    if (s <= 0.04045f) return s / 12.92f;
-    return std::pow((s + 0.055f) / 1.055f, 2.4f);
-}
+LaunchCfg wide_cfg(const wf_ctx* c) { return LaunchCfg{c->num_sms * 8, 256}; }
 
-struct HostV3 {
-    float x, y, z;
-};
-inline HostV3 hsub(HostV3 a, HostV3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
-inline HostV3 hcross(HostV3 a, HostV3 b)
+void drop_graphs(wf_ctx* c)
 {
-    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+    for (auto& g : c->graphs)
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+    c->graphs.clear();
 }
-inline float hlen(HostV3 a) { return std::sqrt(a.x * a.x + a.y * a.y + a.z * a.z); }
 
 int ensure_render_buffers(wf_ctx* c, int64_t paths)
 {
     if (paths <= c->cap) return WF_OK;
     free_all(c->render_allocs);
+    drop_graphs(c);
     c->cap = 0;
     auto& A = c->render_allocs;
     const size_t n = (size_t)paths;
     for (int q = 0; q < 2; ++q) {
         RayQueueDev& r = c->rq[q];
-        WF_CK(c, dalloc(A, &r.ox, n)); WF_CK(c, dalloc(A, &r.oy, n)); WF_CK(c, dalloc(A, &r.oz, n));
-        WF_CK(c, dalloc(A, &r.dx, n)); WF_CK(c, dalloc(A, &r.dy, n)); WF_CK(c, dalloc(A, &r.dz, n));
-        WF_CK(c, dalloc(A, &r.tr, n)); WF_CK(c, dalloc(A, &r.tg, n)); WF_CK(c, dalloc(A, &r.tb, n));
-        WF_CK(c, dalloc(A, &r.pdf, n));
-        WF_CK(c, dalloc(A, &r.pixel, n)); WF_CK(c, dalloc(A, &r.depth, n)); WF_CK(c, dalloc(A, &r.sample, n));
+        WF_CK(c, wf_dalloc(A, &r.ox, n)); WF_CK(c, wf_dalloc(A, &r.oy, n)); WF_CK(c, wf_dalloc(A, &r.oz, n));
+        WF_CK(c, wf_dalloc(A, &r.dx, n)); WF_CK(c, wf_dalloc(A, &r.dy, n)); WF_CK(c, wf_dalloc(A, &r.dz, n));
+        WF_CK(c, wf_dalloc(A, &r.tr, n)); WF_CK(c, wf_dalloc(A, &r.tg, n)); WF_CK(c, wf_dalloc(A, &r.tb, n));
+        WF_CK(c, wf_dalloc(A, &r.pdf, n));
+        WF_CK(c, wf_dalloc(A, &r.pixel, n)); WF_CK(c, wf_dalloc(A, &r.depth, n)); WF_CK(c, wf_dalloc(A, &r.sample, n));
+        WF_CK(c, wf_dalloc(A, &r.job, n));
         r.capacity = paths;
         HitQueueDev& h = c->hq[q];
-        WF_CK(c, dalloc(A, &h.ray, n)); WF_CK(c, dalloc(A, &h.tri, n)); WF_CK(c, dalloc(A, &h.t, n));
-        WF_CK(c, dalloc(A, &h.bu, n)); WF_CK(c, dalloc(A, &h.bv, n));
+        WF_CK(c, wf_dalloc(A, &h.ray, n)); WF_CK(c, wf_dalloc(A, &h.tri, n)); WF_CK(c, wf_dalloc(A, &h.t, n));
+        WF_CK(c, wf_dalloc(A, &h.bu, n)); WF_CK(c, wf_dalloc(A, &h.bv, n));
         h.capacity = paths;
     }
     const size_t ns = 2 * n;
     ShadowQueueDev& s = c->sh;
-    WF_CK(c, dalloc(A, &s.ox, ns)); WF_CK(c, dalloc(A, &s.oy, ns)); WF_CK(c, dalloc(A, &s.oz, ns));
-    WF_CK(c, dalloc(A, &s.dx, ns)); WF_CK(c, dalloc(A, &s.dy, ns)); WF_CK(c, dalloc(A, &s.dz, ns));
-    WF_CK(c, dalloc(A, &s.dist, ns));
-    WF_CK(c, dalloc(A, &s.cr, ns)); WF_CK(c, dalloc(A, &s.cg, ns)); WF_CK(c, dalloc(A, &s.cb, ns));
-    WF_CK(c, dalloc(A, &s.pixel, ns));
+    WF_CK(c, wf_dalloc(A, &s.ox, ns)); WF_CK(c, wf_dalloc(A, &s.oy, ns)); WF_CK(c, wf_dalloc(A, &s.oz, ns));
+    WF_CK(c, wf_dalloc(A, &s.dx, ns)); WF_CK(c, wf_dalloc(A, &s.dy, ns)); WF_CK(c, wf_dalloc(A, &s.dz, ns));
+    WF_CK(c, wf_dalloc(A, &s.dist, ns));
+    WF_CK(c, wf_dalloc(A, &s.cr, ns)); WF_CK(c, wf_dalloc(A, &s.cg, ns)); WF_CK(c, wf_dalloc(A, &s.cb, ns));
+    WF_CK(c, wf_dalloc(A, &s.pixel, ns));
+    WF_CK(c, wf_dalloc(A, &s.job, ns));
     s.capacity = (int64_t)ns;
-    WF_CK(c, dalloc(A, &c->keys, n)); WF_CK(c, dalloc(A, &c->keys_tmp, n));
-    WF_CK(c, dalloc(A, &c->vals, n)); WF_CK(c, dalloc(A, &c->vals_tmp, n));
+    WF_CK(c, wf_dalloc(A, &c->keys, n)); WF_CK(c, wf_dalloc(A, &c->keys_tmp, n));
+    WF_CK(c, wf_dalloc(A, &c->vals, n)); WF_CK(c, wf_dalloc(A, &c->vals_tmp, n));
     c->nb = radix_blocks_for(paths, c->num_sms);
-    WF_CK(c, dalloc(A, &c->hist, radix_hist_words(c->nb)));
-    WF_CK(c, dalloc(A, &c->col_mat, n)); WF_CK(c, dalloc(A, &c->col_tex, n));
-    WF_CK(c, dalloc(A, &c->col_tr, n)); WF_CK(c, dalloc(A, &c->col_tg, n)); WF_CK(c, dalloc(A, &c->col_tb, n));
-    WF_CK(c, dalloc(A, &c->col_px, n)); WF_CK(c, dalloc(A, &c->col_py, n)); WF_CK(c, dalloc(A, &c->col_pz, n));
+    WF_CK(c, wf_dalloc(A, &c->hist, radix_hist_words(c->nb)));
+    WF_CK(c, wf_dalloc(A, &c->col_mat, n)); WF_CK(c, wf_dalloc(A, &c->col_tex, n));
+    WF_CK(c, wf_dalloc(A, &c->col_tr, n)); WF_CK(c, wf_dalloc(A, &c->col_tg, n)); WF_CK(c, wf_dalloc(A, &c->col_tb, n));
+    WF_CK(c, wf_dalloc(A, &c->col_px, n)); WF_CK(c, wf_dalloc(A, &c->col_py, n)); WF_CK(c, wf_dalloc(A, &c->col_pz, n));
     c->cap = paths;
     return WF_OK;
 }
 
+int ensure_arena(wf_ctx* c, int64_t floats)
+{
+    if (floats <= c->arena_floats) return WF_OK;
+    drop_graphs(c);
+    cudaFree(c->arena);
+    c->arena = nullptr;
+    c->arena_floats = 0;
+    WF_CK(c, cudaMalloc(&c->arena, sizeof(float) * (size_t)floats));
+    c->arena_floats = floats;
+    return WF_OK;
+}
+
+int ensure_job_tables(wf_ctx* c, int jobs, int chunks)
+{
+    if (jobs > c->jobs_cap) {
+        drop_graphs(c);
+        cudaFree(c->d_jobs);
+        c->d_jobs = nullptr;
+        c->jobs_cap = 0;
+        int cap = std::max(jobs, 64);
+        WF_CK(c, cudaMalloc(&c->d_jobs, sizeof(DeviceJob) * (size_t)cap));
+        c->jobs_cap = cap;
+    }
+    if (chunks > c->chunks_cap) {
+        drop_graphs(c);
+        cudaFree(c->d_chunks);
+        c->d_chunks = nullptr;
+        c->chunks_cap = 0;
+        int cap = std::max(chunks, 64);
+        WF_CK(c, cudaMalloc(&c->d_chunks, sizeof(WaveChunk) * (size_t)cap));
+        c->chunks_cap = cap;
+    }
+    return WF_OK;
+}
+
+// The device copy of every resident scene's descriptor, indexed by scene id.
+int sync_scene_table(wf_ctx* c)
+{
+    if (!c->scene_table_dirty) return WF_OK;
+    const int n = std::max<int>(1, (int)c->scenes.size());
+    if (n > c->scene_table_cap) {
+        drop_graphs(c);
+        cudaFree(c->d_scene_table);
+        c->d_scene_table = nullptr;
+        c->scene_table_cap = 0;
+        int cap = std::max(n, 16);
+        WF_CK(c, cudaMalloc(&c->d_scene_table, sizeof(DeviceScene) * (size_t)cap));
+        c->scene_table_cap = cap;
+    }
+    std::vector<DeviceScene> host(n);
+    for (int i = 0; i < (int)c->scenes.size(); ++i) host[i] = c->scenes[i].S;
+    WF_CK(c, cudaMemcpyAsync(c->d_scene_table, host.data(), sizeof(DeviceScene) * n, cudaMemcpyHostToDevice,
+                             c->stream));
+    WF_CK(c, cudaStreamSynchronize(c->stream));
+    c->scene_table_dirty = false;
+    return WF_OK;
+}
+
+namespace {
 int ensure_rank_buffers(wf_ctx* c, int count)
 {
     if (count <= c->rank_cap) return WF_OK;
@@ -230,6 +204,8 @@ void type_ranks(int policy, const ull cnt[8], const ull mem[8], const int first[
     for (int r = 0; r < (int)types.size(); ++r) rank[types[r]] = r;
 }
 
+}  // namespace
+
 // Sorts the n scheduling columns under the policy; perm (device) receives the
 // permutation.  Requires c->keys etc. with capacity >= n and d_n on device.
 int schedule_columns(wf_ctx* c, int policy, const ull* d_n, int64_t n, ShadeColumnsDev cols,
@@ -238,7 +214,7 @@ int schedule_columns(wf_ctx* c, int policy, const ull* d_n, int64_t n, ShadeColu
                      const double* rc_mat, const double* rc_tex, uint32_t** perm_out)
 {
     cudaStream_t s = c->stream;
-    LaunchCfg W = wide(c);
+    LaunchCfg W = wide_cfg(c);
     uint64_t* rk = nullptr;
     uint32_t* rv = nullptr;
     c->last_schedule_launches = 1;
@@ -338,265 +314,40 @@ int check_device_flag(wf_ctx* c)
     return WF_OK;
 }
 
-void free_scene(wf_ctx* c)
+}  // namespace wf
+
+namespace {
+
+// srgbToLinear, reference src/shading/Texture.cpp:20-27.
+float srgb_to_linear(float s)
 {
-    free_all(c->scene_allocs);
-    c->has_scene = false;
-    c->S = DeviceScene{};
-    c->d_tex_bytes = nullptr;
+    if (s <= 0.04045f) return s / 12.92f;
+    return std::pow((s + 0.055f) / 1.055f, 2.4f);
 }
 
-// The render loop shared by wf_render and wf_render_accumulate: leaves the
-// per-pixel sums in accum (device, W*H*3 floats, zeroed here).
-int render_into(wf_ctx* c, const wf_render_params* P, float* accum, wf_render_stats* st)
+struct HostV3 {
+    float x, y, z;
+};
+inline HostV3 hsub(HostV3 a, HostV3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline HostV3 hcross(HostV3 a, HostV3 b)
 {
-    cudaStream_t s = c->stream;
-    const int W = P->width, H = P->height;
-    const int64_t np = (int64_t)W * H;
-    int spw = P->spp_per_wave > 0 ? P->spp_per_wave : (int)std::max<int64_t>(1, c->paths_per_wave / np);
-    spw = std::max(1, std::min(spw, P->samples_per_pixel));
-    const int64_t cap = np * spw;
-    int rc = ensure_render_buffers(c, cap);
-    if (rc) return rc;
-    WF_CK(c, cudaMemsetAsync(accum, 0, sizeof(float) * 3 * (size_t)np, s));
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+inline float hlen(HostV3 a) { return std::sqrt(a.x * a.x + a.y * a.y + a.z * a.z); }
 
-    // Cost-aware RR uses float(relativeCost) (WavefrontRenderer.cpp:781-785).
-    const float* d_rel = nullptr;
-    if (P->enable_cost_aware_rr && P->rel_cost_material) {
-        int nm = c->S.num_materials;
-        if (nm > c->rel_cost_cap) {
-            if (c->rel_cost_f) cudaFree(c->rel_cost_f);
-            WF_CK(c, cudaMalloc(&c->rel_cost_f, sizeof(float) * nm));
-            c->rel_cost_cap = nm;
-        }
-        std::vector<float> f(nm);
-        for (int m = 0; m < nm; ++m) f[m] = (float)P->rel_cost_material[m];
-        WF_CK(c, cudaMemcpyAsync(c->rel_cost_f, f.data(), sizeof(float) * nm, cudaMemcpyHostToDevice, s));
-        d_rel = c->rel_cost_f;
-    }
-    ShadeParams SP{P->seed_lo, P->seed_hi, P->firefly_threshold, P->rr_min_depth,
-                   P->enable_cost_aware_rr, d_rel};
-    wf_render_stats stats{};
-    const LaunchCfg PC = persist(c), WC = wide(c);
-    float ms = 0.0f;
-    cudaEvent_t* ev = c->ev;
-    WF_CK(c, cudaEventRecord(ev[0], s));
-    for (int s0 = 0; s0 < P->samples_per_pixel; s0 += spw) {
-        const int nspp = std::min(spw, P->samples_per_pixel - s0);
-        int64_t count = np * nspp;
-        int cur = 0;
-        launch_camera(P->camera, W, H, P->seed_lo, P->seed_hi, P->first_sample + s0, nspp, c->rq[cur], s);
-        stats.kernel_launches += 1;
-        ull hc = (ull)count;
-        WF_CK(c, cudaMemcpyAsync(c->counters, &hc, sizeof(ull), cudaMemcpyHostToDevice, s));
-        stats.waves++;
-        for (int depth = 0; depth < P->max_depth && count > 0; ++depth) {
-            stats.bounces++;
-            stats.closest_rays += (uint64_t)count;
-            if (P->enable_ray_sort) {
-                // RayQueue::schedule + materialize (.cpp:159-168)
-                WF_CK(c, cudaEventRecord(ev[2], s));
-                launch_ray_keys(c->rq[cur], c->counters, c->S.bmin, c->S.bmax, c->keys, c->vals, WC, s);
-                uint64_t* rk;
-                uint32_t* rv;
-                RadixSortArgs a{c->keys, c->vals, c->keys_tmp, c->vals_tmp, c->hist, c->counters,
-                                c->nb, 0, 33, &rk, &rv};
-                radix_sort_pairs(a, s);
-                launch_gather_rays(c->rq[cur], rv, c->counters, c->rq[1 - cur], WC, s);
-                stats.kernel_launches += 2 + 3 * 5;  // keys, gather, 5 radix passes
-                cur = 1 - cur;
-                WF_CK(c, cudaEventRecord(ev[3], s));
-                stats.sorted_elements += (uint64_t)count;
-            }
-            WF_CK(c, cudaMemsetAsync(c->counters + 1, 0, sizeof(ull) * 5, s));
-            WF_CK(c, cudaEventRecord(ev[4], s));
-            launch_trace_render(c->S, c->rq[cur], c->counters, c->hq[0], c->counters + 1, accum,
-                                c->counters + 4, c->err_flag, PC, s);
-            WF_CK(c, cudaEventRecord(ev[5], s));
-            HitQueueDev hq_use = c->hq[0];
-            if (P->policy != WF_POLICY_NONE) {
-                ull hits = 0;
-                WF_CK(c, cudaMemcpyAsync(&hits, c->counters + 1, sizeof(ull), cudaMemcpyDeviceToHost, s));
-                WF_CK(c, cudaStreamSynchronize(s));
-                ShadeColumnsMut cm{c->col_mat, c->col_tex, c->col_tr, c->col_tg, c->col_tb,
-                                   c->col_px, c->col_py, c->col_pz};
-                launch_hit_columns(c->S, c->rq[cur], c->hq[0], c->counters + 1, cm, WC, s);
-                ShadeColumnsDev cd{c->col_mat, c->col_tex, c->col_tr, c->col_tg, c->col_tb,
-                                   c->col_px, c->col_py, c->col_pz};
-                uint32_t* perm = nullptr;
-                rc = schedule_columns(c, P->policy, c->counters + 1, (int64_t)hits, cd, c->S.materials,
-                                      c->S.num_materials, c->mats, c->S.num_textures, c->d_tex_bytes,
-                                      c->tex_bytes, P->rel_cost_material, P->rel_cost_texture, &perm);
-                if (rc) return rc;
-                launch_permute_hits(c->hq[0], perm, c->counters + 1, c->hq[1], WC, s);
-                stats.kernel_launches += c->last_schedule_launches + 2;  // + columns, permute
-                hq_use = c->hq[1];
-                stats.sorted_elements += hits;
-            }
-            WF_CK(c, cudaEventRecord(ev[6], s));
-            launch_shade(c->S, SP, c->rq[cur], hq_use, c->counters + 1, c->sh, c->counters + 2,
-                         c->rq[1 - cur], c->counters + 3, accum, c->err_flag, PC, s);
-            launch_occluded_render(c->S, c->sh, c->counters + 2, accum, c->counters + 5, c->err_flag, PC, s);
-            stats.kernel_launches += 3;  // trace, shade, occluded
-            WF_CK(c, cudaEventRecord(ev[7], s));
-            ull cnt[4];
-            WF_CK(c, cudaMemcpyAsync(cnt, c->counters, sizeof(cnt), cudaMemcpyDeviceToHost, s));
-            WF_CK(c, cudaMemcpyAsync(c->counters, c->counters + 3, sizeof(ull), cudaMemcpyDeviceToDevice, s));
-            WF_CK(c, cudaStreamSynchronize(s));
-            if (P->enable_ray_sort) {
-                WF_CK(c, cudaEventElapsedTime(&ms, ev[2], ev[3]));
-                stats.ms_ray_sort += ms;
-            }
-            WF_CK(c, cudaEventElapsedTime(&ms, ev[4], ev[5]));
-            stats.ms_intersect += ms;
-            WF_CK(c, cudaEventElapsedTime(&ms, ev[5], ev[6]));
-            stats.ms_schedule += ms;
-            WF_CK(c, cudaEventElapsedTime(&ms, ev[6], ev[7]));
-            stats.ms_shade += ms;
-            stats.shaded_hits += cnt[1];
-            stats.misses += (uint64_t)count - cnt[1];
-            stats.shadow_rays += cnt[2];
-            count = (int64_t)cnt[3];
-            cur = 1 - cur;
-        }
-    }
-    WF_CK(c, cudaEventRecord(ev[1], s));
-    WF_CK(c, cudaEventSynchronize(ev[1]));
-    WF_CK(c, cudaEventElapsedTime(&ms, ev[0], ev[1]));
-    stats.ms_total = ms;
-    rc = check_device_flag(c);
-    if (rc) return rc;
-    if (st) *st = stats;
-    return WF_OK;
+void free_scene_res(ResidentScene& R)
+{
+    free_all(R.allocs);
+    R = ResidentScene{};
 }
 
-int validate_params(wf_ctx* c, const wf_render_params* P)
-{
-    if (!P) return set_err(c, WF_ERR_INVALID_ARGUMENT, "params is null");
-    if (P->width < 2 || P->height < 2)
-        return set_err(c, WF_ERR_INVALID_ARGUMENT, "width and height must be >= 2 (u = x/(width-1))");
-    if ((int64_t)P->width * P->height > (int64_t)1 << 28)
-        return set_err(c, WF_ERR_INVALID_ARGUMENT, "image larger than 2^28 pixels");
-    if (P->samples_per_pixel < 1) return set_err(c, WF_ERR_INVALID_ARGUMENT, "samples_per_pixel < 1");
-    if (P->max_depth < 0 || P->max_depth > 0xFFFF) return set_err(c, WF_ERR_INVALID_ARGUMENT, "max_depth out of range");
-    if (P->policy < 0 || P->policy > 3) return set_err(c, WF_ERR_INVALID_ARGUMENT, "unknown policy");
-    if (!c->has_scene) return set_err(c, WF_ERR_STATE, "no scene uploaded");
-    return WF_OK;
-}
+bool has_scene(const wf_ctx* c) { return !c->scenes.empty() && c->scenes[0].live; }
 
-}  // namespace
-
-// ===========================================================================
-// C ABI
-// ===========================================================================
-extern "C" {
-
-int wf_version(void) { return WF_API_VERSION; }
-
-int wf_create(const wf_config* cfg, wf_ctx** out)
-{
-    if (!out) return WF_ERR_INVALID_ARGUMENT;
-    *out = nullptr;
-    int ndev = 0;
-    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return WF_ERR_NO_DEVICE;
-    wf_ctx* c = new wf_ctx();
-    c->device = cfg ? cfg->device : 0;
-    if (c->device < 0 || c->device >= ndev) {
-        delete c;
-        return WF_ERR_INVALID_ARGUMENT;
-    }
-    if (cfg && cfg->max_paths_per_wave > 0) c->paths_per_wave = cfg->max_paths_per_wave;
-    if (cudaSetDevice(c->device) != cudaSuccess) {
-        delete c;
-        return WF_ERR_CUDA;
-    }
-    cudaDeviceProp prop;
-    cudaGetDeviceProperties(&prop, c->device);
-    c->num_sms = prop.multiProcessorCount;
-    bool ok = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) == cudaSuccess;
-    for (auto& e : c->ev) ok = ok && cudaEventCreate(&e) == cudaSuccess;
-    for (auto& e : c->timer) ok = ok && cudaEventCreate(&e) == cudaSuccess;
-    ok = ok && cudaMalloc(&c->counters, sizeof(ull) * 8) == cudaSuccess;
-    ok = ok && cudaMalloc(&c->err_flag, sizeof(int)) == cudaSuccess;
-    ok = ok && cudaMalloc(&c->stats8, sizeof(ull) * 16) == cudaSuccess;
-    ok = ok && cudaMalloc(&c->first8, sizeof(int) * 8) == cudaSuccess;
-    ok = ok && cudaMalloc(&c->bounds6, sizeof(unsigned) * 6) == cudaSuccess;
-    ok = ok && cudaMemset(c->err_flag, 0, sizeof(int)) == cudaSuccess;
-    ok = ok && cudaMemset(c->counters, 0, sizeof(ull) * 8) == cudaSuccess;
-    if (!ok) {
-        wf_destroy(c);
-        return WF_ERR_CUDA;
-    }
-    *out = c;
-    return WF_OK;
-}
-
-int wf_destroy(wf_ctx* c)
-{
-    if (!c) return WF_OK;
-    cudaSetDevice(c->device);
-    if (c->stream) cudaStreamSynchronize(c->stream);
-    free_scene(c);
-    free_all(c->render_allocs);
-    cudaFree(c->counters);
-    cudaFree(c->err_flag);
-    cudaFree(c->stats8);
-    cudaFree(c->first8);
-    cudaFree(c->bounds6);
-    cudaFree(c->rank_buf);
-    cudaFree(c->benefit);
-    cudaFree(c->present);
-    cudaFree(c->rel_cost_f);
-    cudaFree(c->image);
-    for (auto& e : c->ev)
-        if (e) cudaEventDestroy(e);
-    for (auto& e : c->timer)
-        if (e) cudaEventDestroy(e);
-    if (c->stream) cudaStreamDestroy(c->stream);
-    delete c;
-    return WF_OK;
-}
-
-const char* wf_last_error(const wf_ctx* c) { return c ? c->last_error.c_str() : ""; }
-
-int wf_camera_make(const float look_from[3], const float look_at[3], const float up[3],
-                   float vfov, int32_t w, int32_t h, wf_camera* out)
-{
-    if (!look_from || !look_at || !up || !out || w <= 0 || h <= 0) return WF_ERR_INVALID_ARGUMENT;
-    // Camera::Camera, include/core/Camera.h:13-33 (float arithmetic as written).
-    float aspect = (float)w / h;
-    float theta = vfov * 3.14159265f / 180.0f;
-    float vh = 2.0f * std::tan(theta / 2.0f);
-    float vw = aspect * vh;
-    HostV3 from = {look_from[0], look_from[1], look_from[2]};
-    HostV3 at = {look_at[0], look_at[1], look_at[2]};
-    HostV3 u = {up[0], up[1], up[2]};
-    HostV3 fw = hsub(from, at);
-    float lf = hlen(fw);
-    fw = {fw.x / lf, fw.y / lf, fw.z / lf};
-    HostV3 right = hcross(u, fw);
-    float lr = hlen(right);
-    right = {right.x / lr, right.y / lr, right.z / lr};
-    HostV3 upv = hcross(fw, right);
-    HostV3 hz = {right.x * vw, right.y * vw, right.z * vw};
-    HostV3 vt = {upv.x * vh, upv.y * vh, upv.z * vh};
-    HostV3 tl = {from.x - hz.x / 2.0f, from.y - hz.y / 2.0f, from.z - hz.z / 2.0f};
-    tl = {tl.x - vt.x / 2.0f, tl.y - vt.y / 2.0f, tl.z - vt.z / 2.0f};
-    tl = hsub(tl, fw);
-    float* dsts[4] = {out->origin, out->top_left, out->horizontal, out->vertical};
-    HostV3 srcs[4] = {from, tl, hz, vt};
-    for (int k = 0; k < 4; ++k) {
-        dsts[k][0] = srcs[k].x;
-        dsts[k][1] = srcs[k].y;
-        dsts[k][2] = srcs[k].z;
-    }
-    return WF_OK;
-}
-
-int wf_scene_upload(wf_ctx* c, const wf_scene_desc* D)
+// Uploads one scene and builds its BVH: Scene::buildAccelerator
+// (src/core/Scene.cpp:79-113) + EmbreeAccelerator::build (Embree.cpp:66-119).
+int build_scene(wf_ctx* c, const wf_scene_desc* D, ResidentScene& R)
 {
     if (!c || !D) return WF_ERR_INVALID_ARGUMENT;
-    cudaSetDevice(c->device);
     if (D->num_indices % 3 != 0 || D->num_indices < 0 || D->num_vertices < 0 || D->num_meshes < 0)
         return set_err(c, WF_ERR_INVALID_ARGUMENT, "index count must be a multiple of 3");
     if (D->num_materials <= 0 || !D->materials)
@@ -620,10 +371,8 @@ int wf_scene_upload(wf_ctx* c, const wf_scene_desc* D)
         int t = D->materials[m].type;
         if (t < 0 || t > 5) return set_err(c, WF_ERR_INVALID_ARGUMENT, "unknown material type");
     }
-    free_scene(c);
-    auto t_start = std::chrono::steady_clock::now();
     cudaStream_t s = c->stream;
-    auto& A = c->scene_allocs;
+    auto& A = R.allocs;
     DeviceScene S{};
 
     // Per-triangle ids, emissive meshes, area, bounds — host, as the reference.
@@ -674,9 +423,9 @@ int wf_scene_upload(wf_ctx* c, const wf_scene_desc* D)
     BvhBuildOutput bo{};
     std::string err;
     if (ntri > 0) {
-        if (dalloc(tmp, &dpx, D->num_vertices) || dalloc(tmp, &dpy, D->num_vertices) ||
-            dalloc(tmp, &dpz, D->num_vertices) || dalloc(tmp, &didx, D->num_indices) ||
-            dalloc(tmp, &dgeom, ntri) || dalloc(tmp, &dprim, ntri)) {
+        if (wf_dalloc(tmp, &dpx, D->num_vertices) || wf_dalloc(tmp, &dpy, D->num_vertices) ||
+            wf_dalloc(tmp, &dpz, D->num_vertices) || wf_dalloc(tmp, &didx, D->num_indices) ||
+            wf_dalloc(tmp, &dgeom, ntri) || wf_dalloc(tmp, &dprim, ntri)) {
             cleanup_tmp();
             return set_err(c, WF_ERR_OUT_OF_MEMORY, "geometry upload allocation failed");
         }
@@ -694,7 +443,7 @@ int wf_scene_upload(wf_ctx* c, const wf_scene_desc* D)
         if (brc) return set_err(c, WF_ERR_CUDA, "BVH build failed: " + err);
         A.push_back(bo.tris);
         A.push_back(bo.nodes);
-        c->info.bvh_build_ms = std::chrono::duration<double, std::milli>(b1 - b0).count();
+        R.info.bvh_build_ms = std::chrono::duration<double, std::milli>(b1 - b0).count();
     }
     S.tris = bo.tris;
     S.nodes = bo.nodes;
@@ -705,8 +454,8 @@ int wf_scene_upload(wf_ctx* c, const wf_scene_desc* D)
 
 #define UP(dst, src, count)                                                                     \
     do {                                                                                        \
-        if (dalloc(A, &dst, (count)) != cudaSuccess) {                                          \
-            free_scene(c);                                                                      \
+        if (wf_dalloc(A, &dst, (count)) != cudaSuccess) {                                          \
+            free_scene_res(R);                                                                      \
             return set_err(c, WF_ERR_OUT_OF_MEMORY, "scene allocation failed");                 \
         }                                                                                       \
         if ((count) > 0)                                                                        \
@@ -738,16 +487,16 @@ int wf_scene_upload(wf_ctx* c, const wf_scene_desc* D)
     UP(d_mats, D->materials, D->num_materials);
     S.materials = d_mats;
     S.num_materials = D->num_materials;
-    c->mats.assign(D->materials, D->materials + D->num_materials);
+    R.mats.assign(D->materials, D->materials + D->num_materials);
     // Textures
     std::vector<TexDesc> td(std::max(1, D->num_textures));
     std::vector<float> pool_f;
     std::vector<uint32_t> pool_b;
-    c->tex_bytes.assign(D->num_textures, 0);
+    R.tex_bytes.assign(D->num_textures, 0);
     for (int t = 0; t < D->num_textures; ++t) {
         const wf_texture& x = D->textures[t];
         if (x.width <= 0 || x.height <= 0 || !x.data) {
-            free_scene(c);
+            free_scene_res(R);
             return set_err(c, WF_ERR_INVALID_ARGUMENT, "texture without texels");
         }
         size_t n = (size_t)x.width * x.height;
@@ -755,7 +504,7 @@ int wf_scene_upload(wf_ctx* c, const wf_scene_desc* D)
         td[t].height = x.height;
         td[t].format = x.format;
         // Texture::memoryBytes = pixels.size() * sizeof(Color) (Texture.h:51-54)
-        c->tex_bytes[t] = (int64_t)(n * 12);
+        R.tex_bytes[t] = (int64_t)(n * 12);
         if (x.format == WF_TEXEL_RGB32F) {
             td[t].offset = (int64_t)pool_f.size();
             const float* f = (const float*)x.data;
@@ -782,8 +531,8 @@ int wf_scene_upload(wf_ctx* c, const wf_scene_desc* D)
     UP(d_lut, lut, 256);
     S.srgb_lut = d_lut;
     int64_t* d_tb = nullptr;
-    UP(d_tb, c->tex_bytes.data(), (int64_t)c->tex_bytes.size());
-    c->d_tex_bytes = d_tb;
+    UP(d_tb, R.tex_bytes.data(), (int64_t)R.tex_bytes.size());
+    R.d_tex_bytes = d_tb;
     // Lights
     EmissiveMesh* d_em = nullptr;
     UP(d_em, em.data(), (int64_t)em.size());
@@ -811,12 +560,12 @@ int wf_scene_upload(wf_ctx* c, const wf_scene_desc* D)
     }
 #undef UP
     if (cudaStreamSynchronize(s) != cudaSuccess) {
-        free_scene(c);
+        free_scene_res(R);
         return set_err(c, WF_ERR_CUDA, "scene upload failed");
     }
-    c->S = S;
-    c->has_scene = true;
-    wf_scene_info& I = c->info;
+    R.S = S;
+    R.live = true;
+    wf_scene_info& I = R.info;
     for (int k = 0; k < 3; ++k) {
         I.bounds_min[k] = bmin[k];
         I.bounds_max[k] = bmax[k];
@@ -829,15 +578,189 @@ int wf_scene_upload(wf_ctx* c, const wf_scene_desc* D)
     int64_t bytes = (int64_t)ntri * 48 + (int64_t)bo.num_nodes * (int64_t)sizeof(BvhNode) +
                     (int64_t)pool_f.size() * 4 + (int64_t)pool_b.size() * 4;
     I.device_bytes = bytes;
-    (void)t_start;
     return WF_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+int wf_version(void) { return WF_API_VERSION; }
+
+int wf_create(const wf_config* cfg, wf_ctx** out)
+{
+    if (!out) return WF_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return WF_ERR_NO_DEVICE;
+    wf_ctx* c = new wf_ctx();
+    c->device = cfg ? cfg->device : 0;
+    if (c->device < 0 || c->device >= ndev) {
+        delete c;
+        return WF_ERR_INVALID_ARGUMENT;
+    }
+    if (cfg && cfg->max_paths_per_wave > 0) c->paths_per_wave = cfg->max_paths_per_wave;
+    if (cudaSetDevice(c->device) != cudaSuccess) {
+        delete c;
+        return WF_ERR_CUDA;
+    }
+    cudaDeviceProp prop;
+    cudaGetDeviceProperties(&prop, c->device);
+    c->num_sms = prop.multiProcessorCount;
+    bool ok = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) == cudaSuccess;
+    for (auto& e : c->ev) ok = ok && cudaEventCreate(&e) == cudaSuccess;
+    for (auto& e : c->timer) ok = ok && cudaEventCreate(&e) == cudaSuccess;
+    ok = ok && cudaMalloc(&c->counters, sizeof(ull) * 8) == cudaSuccess;
+    ok = ok && cudaMalloc(&c->tally, sizeof(ull) * 8) == cudaSuccess;
+    ok = ok && cudaMalloc(&c->d_wave_header, sizeof(long long) * 2) == cudaSuccess;
+    ok = ok && cudaMalloc(&c->err_flag, sizeof(int)) == cudaSuccess;
+    ok = ok && cudaMalloc(&c->stats8, sizeof(ull) * 16) == cudaSuccess;
+    ok = ok && cudaMalloc(&c->first8, sizeof(int) * 8) == cudaSuccess;
+    ok = ok && cudaMalloc(&c->bounds6, sizeof(unsigned) * 6) == cudaSuccess;
+    ok = ok && cudaMemset(c->err_flag, 0, sizeof(int)) == cudaSuccess;
+    ok = ok && cudaMemset(c->counters, 0, sizeof(ull) * 8) == cudaSuccess;
+    if (!ok) {
+        wf_destroy(c);
+        return WF_ERR_CUDA;
+    }
+    *out = c;
+    return WF_OK;
+}
+
+int wf_destroy(wf_ctx* c)
+{
+    if (!c) return WF_OK;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    drop_graphs(c);
+    for (auto& r : c->scenes) free_scene_res(r);
+    free_all(c->render_allocs);
+    free_all(c->rel_cost_allocs);
+    cudaFree(c->d_scene_table);
+    cudaFree(c->d_jobs);
+    cudaFree(c->d_chunks);
+    cudaFree(c->d_wave_header);
+    cudaFree(c->arena);
+    cudaFree(c->tally);
+    cudaFree(c->counters);
+    cudaFree(c->err_flag);
+    cudaFree(c->stats8);
+    cudaFree(c->first8);
+    cudaFree(c->bounds6);
+    cudaFree(c->rank_buf);
+    cudaFree(c->benefit);
+    cudaFree(c->present);
+    cudaFree(c->image);
+    for (auto& e : c->ev)
+        if (e) cudaEventDestroy(e);
+    for (auto& e : c->timer)
+        if (e) cudaEventDestroy(e);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return WF_OK;
+}
+
+const char* wf_last_error(const wf_ctx* c) { return c ? c->last_error.c_str() : ""; }
+
+int wf_camera_make(const float look_from[3], const float look_at[3], const float up[3],
+                   float vfov, int32_t w, int32_t h, wf_camera* out)
+{
+    if (!look_from || !look_at || !up || !out || w <= 0 || h <= 0) return WF_ERR_INVALID_ARGUMENT;
+    // Camera::Camera, include/core/Camera.h:13-33 (float arithmetic as written).
+    float aspect = (float)w / h;
+    float theta = vfov * 3.14159265f / 180.0f;
+    float vh = 2.0f * std::tan(theta / 2.0f);
+    float vw = aspect * vh;
+    HostV3 from = {look_from[0], look_from[1], look_from[2]};
+    HostV3 at = {look_at[0], look_at[1], look_at[2]};
+    HostV3 u = {up[0], up[1], up[2]};
+    HostV3 fw = hsub(from, at);
+    float lf = hlen(fw);
+    fw = {fw.x / lf, fw.y / lf, fw.z / lf};
+    HostV3 right = hcross(u, fw);
+    float lr = hlen(right);
+    right = {right.x / lr, right.y / lr, right.z / lr};
+    HostV3 upv = hcross(fw, right);
+    HostV3 hz = {right.x * vw, right.y * vw, right.z * vw};
+    HostV3 vt = {upv.x * vh, upv.y * vh, upv.z * vh};
+    HostV3 tl = {from.x - hz.x / 2.0f, from.y - hz.y / 2.0f, from.z - hz.z / 2.0f};
+    tl = {tl.x - vt.x / 2.0f, tl.y - vt.y / 2.0f, tl.z - vt.z / 2.0f};
+    tl = hsub(tl, fw);
+    float* dsts[4] = {out->origin, out->top_left, out->horizontal, out->vertical};
+    HostV3 srcs[4] = {from, tl, hz, vt};
+    for (int k = 0; k < 4; ++k) {
+        dsts[k][0] = srcs[k].x;
+        dsts[k][1] = srcs[k].y;
+        dsts[k][2] = srcs[k].z;
+    }
+    return WF_OK;
+}
+
+int wf_scene_upload(wf_ctx* c, const wf_scene_desc* D)
+{
+    if (!c || !D) return WF_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(c->device);
+    if (c->scenes.empty()) c->scenes.resize(1);
+    drop_graphs(c);
+    free_scene_res(c->scenes[0]);
+    c->scene_table_dirty = true;
+    int rc = build_scene(c, D, c->scenes[0]);
+    if (rc) return rc;
+    return sync_scene_table(c);
+}
+
+int wf_scene_add(wf_ctx* c, const wf_scene_desc* D, int32_t* out_id)
+{
+    if (!c || !D || !out_id) return WF_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(c->device);
+    if (c->scenes.empty()) c->scenes.resize(1);  // slot 0 stays the current scene
+    int slot = -1;
+    for (int i = 1; i < (int)c->scenes.size(); ++i)
+        if (!c->scenes[i].live) {
+            slot = i;
+            break;
+        }
+    if (slot < 0) {
+        c->scenes.emplace_back();
+        slot = (int)c->scenes.size() - 1;
+    }
+    int rc = build_scene(c, D, c->scenes[slot]);
+    if (rc) return rc;
+    c->scene_table_dirty = true;
+    rc = sync_scene_table(c);
+    if (rc) return rc;
+    *out_id = slot;
+    return WF_OK;
+}
+
+int wf_scene_remove(wf_ctx* c, int32_t id)
+{
+    if (!c || id < 0 || id >= (int)c->scenes.size() || !c->scenes[id].live)
+        return set_err(c, WF_ERR_INVALID_ARGUMENT, "no such scene");
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    free_scene_res(c->scenes[id]);
+    c->scene_table_dirty = true;
+    return sync_scene_table(c);
 }
 
 int wf_scene_get_info(wf_ctx* c, wf_scene_info* out)
 {
     if (!c || !out) return WF_ERR_INVALID_ARGUMENT;
-    if (!c->has_scene) return set_err(c, WF_ERR_STATE, "no scene uploaded");
-    *out = c->info;
+    if (!has_scene(c)) return set_err(c, WF_ERR_STATE, "no scene uploaded");
+    *out = c->scenes[0].info;
+    return WF_OK;
+}
+
+int wf_scene_get_info_id(wf_ctx* c, int32_t id, wf_scene_info* out)
+{
+    if (!c || !out) return WF_ERR_INVALID_ARGUMENT;
+    if (id < 0 || id >= (int)c->scenes.size() || !c->scenes[id].live)
+        return set_err(c, WF_ERR_INVALID_ARGUMENT, "no such scene");
+    *out = c->scenes[id].info;
     return WF_OK;
 }
 
@@ -847,7 +770,7 @@ int wf_trace_closest_host(wf_ctx* c, int64_t n, const float* ox, const float* oy
 {
     if (!c || !out || n < 0 || (n > 0 && (!ox || !oy || !oz || !dx || !dy || !dz)))
         return set_err(c, WF_ERR_INVALID_ARGUMENT, "null argument");
-    if (!c->has_scene) return set_err(c, WF_ERR_STATE, "no scene uploaded");
+    if (!has_scene(c)) return set_err(c, WF_ERR_STATE, "no scene uploaded");
     if (n == 0) return WF_OK;
     cudaSetDevice(c->device);
     cudaStream_t s = c->stream;
@@ -855,18 +778,18 @@ int wf_trace_closest_host(wf_ctx* c, int64_t n, const float* ox, const float* oy
     float* in[6];
     const float* src[6] = {ox, oy, oz, dx, dy, dz};
     for (int k = 0; k < 6; ++k) {
-        WF_CK(c, dalloc(tmp, &in[k], n));
+        WF_CK(c, wf_dalloc(tmp, &in[k], n));
         WF_CK(c, cudaMemcpyAsync(in[k], src[k], sizeof(float) * n, cudaMemcpyHostToDevice, s));
     }
     HitColumnsDev d{};
-    WF_CK(c, dalloc(tmp, &d.geom, n)); WF_CK(c, dalloc(tmp, &d.prim, n));
-    WF_CK(c, dalloc(tmp, &d.t, n)); WF_CK(c, dalloc(tmp, &d.bu, n)); WF_CK(c, dalloc(tmp, &d.bv, n));
-    WF_CK(c, dalloc(tmp, &d.px, n)); WF_CK(c, dalloc(tmp, &d.py, n)); WF_CK(c, dalloc(tmp, &d.pz, n));
-    WF_CK(c, dalloc(tmp, &d.nx, n)); WF_CK(c, dalloc(tmp, &d.ny, n)); WF_CK(c, dalloc(tmp, &d.nz, n));
-    WF_CK(c, dalloc(tmp, &d.front, n)); WF_CK(c, dalloc(tmp, &d.u, n)); WF_CK(c, dalloc(tmp, &d.v, n));
-    WF_CK(c, dalloc(tmp, &d.mat, n)); WF_CK(c, dalloc(tmp, &d.tex, n));
-    launch_trace_api(c->S, n, in[0], in[1], in[2], in[3], in[4], in[5], tmin, tmax, d, c->err_flag,
-                     persist(c), s);
+    WF_CK(c, wf_dalloc(tmp, &d.geom, n)); WF_CK(c, wf_dalloc(tmp, &d.prim, n));
+    WF_CK(c, wf_dalloc(tmp, &d.t, n)); WF_CK(c, wf_dalloc(tmp, &d.bu, n)); WF_CK(c, wf_dalloc(tmp, &d.bv, n));
+    WF_CK(c, wf_dalloc(tmp, &d.px, n)); WF_CK(c, wf_dalloc(tmp, &d.py, n)); WF_CK(c, wf_dalloc(tmp, &d.pz, n));
+    WF_CK(c, wf_dalloc(tmp, &d.nx, n)); WF_CK(c, wf_dalloc(tmp, &d.ny, n)); WF_CK(c, wf_dalloc(tmp, &d.nz, n));
+    WF_CK(c, wf_dalloc(tmp, &d.front, n)); WF_CK(c, wf_dalloc(tmp, &d.u, n)); WF_CK(c, wf_dalloc(tmp, &d.v, n));
+    WF_CK(c, wf_dalloc(tmp, &d.mat, n)); WF_CK(c, wf_dalloc(tmp, &d.tex, n));
+    launch_trace_api(c->scenes[0].S, n, in[0], in[1], in[2], in[3], in[4], in[5], tmin, tmax, d, c->err_flag,
+                     persist_cfg(c), s);
     WF_CK(c, cudaGetLastError());
     struct Pair {
         void* host;
@@ -891,7 +814,7 @@ int wf_trace_occluded_host(wf_ctx* c, int64_t n, const float* ox, const float* o
 {
     if (!c || n < 0 || (n > 0 && (!ox || !oy || !oz || !dx || !dy || !dz || !maxd || !out)))
         return set_err(c, WF_ERR_INVALID_ARGUMENT, "null argument");
-    if (!c->has_scene) return set_err(c, WF_ERR_STATE, "no scene uploaded");
+    if (!has_scene(c)) return set_err(c, WF_ERR_STATE, "no scene uploaded");
     if (n == 0) return WF_OK;
     cudaSetDevice(c->device);
     cudaStream_t s = c->stream;
@@ -899,13 +822,13 @@ int wf_trace_occluded_host(wf_ctx* c, int64_t n, const float* ox, const float* o
     float* in[7];
     const float* src[7] = {ox, oy, oz, dx, dy, dz, maxd};
     for (int k = 0; k < 7; ++k) {
-        WF_CK(c, dalloc(tmp, &in[k], n));
+        WF_CK(c, wf_dalloc(tmp, &in[k], n));
         WF_CK(c, cudaMemcpyAsync(in[k], src[k], sizeof(float) * n, cudaMemcpyHostToDevice, s));
     }
     uint8_t* d_out = nullptr;
-    WF_CK(c, dalloc(tmp, &d_out, n));
-    launch_occluded_api(c->S, n, in[0], in[1], in[2], in[3], in[4], in[5], in[6], d_out, c->err_flag,
-                        persist(c), s);
+    WF_CK(c, wf_dalloc(tmp, &d_out, n));
+    launch_occluded_api(c->scenes[0].S, n, in[0], in[1], in[2], in[3], in[4], in[5], in[6], d_out, c->err_flag,
+                        persist_cfg(c), s);
     WF_CK(c, cudaGetLastError());
     WF_CK(c, cudaMemcpyAsync(out, d_out, (size_t)n, cudaMemcpyDeviceToHost, s));
     WF_CK(c, cudaStreamSynchronize(s));
@@ -924,11 +847,12 @@ int wf_generate_primary_host(wf_ctx* c, const wf_camera* cam, int32_t W, int32_t
     cudaStream_t s = c->stream;
     std::vector<void*> tmp;
     RayQueueDev rq{};
-    WF_CK(c, dalloc(tmp, &rq.ox, n)); WF_CK(c, dalloc(tmp, &rq.oy, n)); WF_CK(c, dalloc(tmp, &rq.oz, n));
-    WF_CK(c, dalloc(tmp, &rq.dx, n)); WF_CK(c, dalloc(tmp, &rq.dy, n)); WF_CK(c, dalloc(tmp, &rq.dz, n));
-    WF_CK(c, dalloc(tmp, &rq.tr, n)); WF_CK(c, dalloc(tmp, &rq.tg, n)); WF_CK(c, dalloc(tmp, &rq.tb, n));
-    WF_CK(c, dalloc(tmp, &rq.pdf, n)); WF_CK(c, dalloc(tmp, &rq.pixel, n));
-    WF_CK(c, dalloc(tmp, &rq.depth, n)); WF_CK(c, dalloc(tmp, &rq.sample, n));
+    WF_CK(c, wf_dalloc(tmp, &rq.ox, n)); WF_CK(c, wf_dalloc(tmp, &rq.oy, n)); WF_CK(c, wf_dalloc(tmp, &rq.oz, n));
+    WF_CK(c, wf_dalloc(tmp, &rq.dx, n)); WF_CK(c, wf_dalloc(tmp, &rq.dy, n)); WF_CK(c, wf_dalloc(tmp, &rq.dz, n));
+    WF_CK(c, wf_dalloc(tmp, &rq.tr, n)); WF_CK(c, wf_dalloc(tmp, &rq.tg, n)); WF_CK(c, wf_dalloc(tmp, &rq.tb, n));
+    WF_CK(c, wf_dalloc(tmp, &rq.pdf, n)); WF_CK(c, wf_dalloc(tmp, &rq.pixel, n));
+    WF_CK(c, wf_dalloc(tmp, &rq.depth, n)); WF_CK(c, wf_dalloc(tmp, &rq.sample, n));
+    rq.job = nullptr;
     rq.capacity = n;
     launch_camera(*cam, W, H, s0, s1, first_sample, nspp, rq, s);
     WF_CK(c, cudaGetLastError());
@@ -955,20 +879,20 @@ int wf_ray_schedule_host(wf_ctx* c, int64_t n, const float* ox, const float* oy,
     float* in[6];
     const float* src[6] = {ox, oy, oz, dx, dy, dz};
     for (int k = 0; k < 6; ++k) {
-        WF_CK(c, dalloc(tmp, &in[k], n));
+        WF_CK(c, wf_dalloc(tmp, &in[k], n));
         WF_CK(c, cudaMemcpyAsync(in[k], src[k], sizeof(float) * n, cudaMemcpyHostToDevice, s));
     }
     uint64_t *k0, *k1;
     uint32_t *v0, *v1, *hist;
     ull* d_n;
     int nb = radix_blocks_for(n, c->num_sms);
-    WF_CK(c, dalloc(tmp, &k0, n)); WF_CK(c, dalloc(tmp, &k1, n));
-    WF_CK(c, dalloc(tmp, &v0, n)); WF_CK(c, dalloc(tmp, &v1, n));
-    WF_CK(c, dalloc(tmp, &hist, radix_hist_words(nb)));
-    WF_CK(c, dalloc(tmp, &d_n, 1));
+    WF_CK(c, wf_dalloc(tmp, &k0, n)); WF_CK(c, wf_dalloc(tmp, &k1, n));
+    WF_CK(c, wf_dalloc(tmp, &v0, n)); WF_CK(c, wf_dalloc(tmp, &v1, n));
+    WF_CK(c, wf_dalloc(tmp, &hist, radix_hist_words(nb)));
+    WF_CK(c, wf_dalloc(tmp, &d_n, 1));
     ull hn = (ull)n;
     WF_CK(c, cudaMemcpyAsync(d_n, &hn, sizeof(hn), cudaMemcpyHostToDevice, s));
-    launch_ray_keys_raw(n, in[0], in[1], in[2], in[3], in[4], in[5], bmin, bmax, k0, v0, wide(c), s);
+    launch_ray_keys_raw(n, in[0], in[1], in[2], in[3], in[4], in[5], bmin, bmax, k0, v0, wide_cfg(c), s);
     if (out_keys) WF_CK(c, cudaMemcpyAsync(out_keys, k0, 8 * (size_t)n, cudaMemcpyDeviceToHost, s));
     uint64_t* rk;
     uint32_t* rv;
@@ -1013,9 +937,9 @@ int wf_shading_schedule_host(wf_ctx* c, int32_t policy, int64_t n, const int32_t
     wf_material* d_mats;
     int64_t* d_tb;
     ull* d_n;
-    WF_CK(c, dalloc(tmp, &d_mats, num_materials));
-    WF_CK(c, dalloc(tmp, &d_tb, std::max(1, num_textures)));
-    WF_CK(c, dalloc(tmp, &d_n, 1));
+    WF_CK(c, wf_dalloc(tmp, &d_mats, num_materials));
+    WF_CK(c, wf_dalloc(tmp, &d_tb, std::max(1, num_textures)));
+    WF_CK(c, wf_dalloc(tmp, &d_n, 1));
     WF_CK(c, cudaMemcpyAsync(d_mats, materials, sizeof(wf_material) * num_materials, cudaMemcpyHostToDevice, s));
     if (num_textures > 0)
         WF_CK(c, cudaMemcpyAsync(d_tb, texture_bytes, 8 * (size_t)num_textures, cudaMemcpyHostToDevice, s));
@@ -1035,66 +959,6 @@ int wf_shading_schedule_host(wf_ctx* c, int32_t policy, int64_t n, const int32_t
     WF_CK(c, cudaMemcpyAsync(out_sorted, perm, 4 * (size_t)n, cudaMemcpyDeviceToHost, s));
     WF_CK(c, cudaStreamSynchronize(s));
     free_all(tmp);
-    return WF_OK;
-}
-
-int wf_render(wf_ctx* c, const wf_render_params* P, float* image, wf_render_stats* st)
-{
-    if (!c || !image) return set_err(c, WF_ERR_INVALID_ARGUMENT, "null argument");
-    int rc = validate_params(c, P);
-    if (rc) return rc;
-    cudaSetDevice(c->device);
-    const int64_t nf = 3 * (int64_t)P->width * P->height;
-    float *accum = nullptr, *img = nullptr;
-    WF_CK(c, cudaMallocAsync(&accum, sizeof(float) * nf, c->stream));
-    WF_CK(c, cudaMallocAsync(&img, sizeof(float) * nf, c->stream));
-    rc = render_into(c, P, accum, st);
-    if (rc == WF_OK) {
-        launch_finalize(accum, nf, (float)P->samples_per_pixel, img, c->stream);
-        if (st) st->kernel_launches += 1;
-        cudaError_t e = cudaMemcpyAsync(image, img, sizeof(float) * nf, cudaMemcpyDeviceToHost, c->stream);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-        if (e != cudaSuccess) rc = set_err(c, WF_ERR_CUDA, cudaGetErrorString(e));
-    }
-    cudaFreeAsync(accum, c->stream);
-    cudaFreeAsync(img, c->stream);
-    cudaStreamSynchronize(c->stream);
-    return rc;
-}
-
-int wf_render_device(wf_ctx* c, const wf_render_params* P, wf_render_stats* st)
-{
-    if (!c) return WF_ERR_INVALID_ARGUMENT;
-    int rc = validate_params(c, P);
-    if (rc) return rc;
-    cudaSetDevice(c->device);
-    const int64_t nf = 3 * (int64_t)P->width * P->height;
-    if (nf > c->image_floats) {
-        cudaFree(c->image);
-        c->image = nullptr;
-        c->image_floats = 0;
-        WF_CK(c, cudaMalloc(&c->image, sizeof(float) * nf));
-        c->image_floats = nf;
-    }
-    float* accum = nullptr;
-    WF_CK(c, cudaMallocAsync(&accum, sizeof(float) * nf, c->stream));
-    rc = render_into(c, P, accum, st);
-    if (rc == WF_OK) {
-        launch_finalize(accum, nf, (float)P->samples_per_pixel, c->image, c->stream);
-        if (st) st->kernel_launches += 1;
-    }
-    cudaFreeAsync(accum, c->stream);
-    cudaError_t e = cudaStreamSynchronize(c->stream);
-    if (rc == WF_OK && e != cudaSuccess) rc = set_err(c, WF_ERR_CUDA, cudaGetErrorString(e));
-    return rc;
-}
-
-int wf_image_download(wf_ctx* c, float* image, int64_t nf)
-{
-    if (!c || !image || nf < 0) return set_err(c, WF_ERR_INVALID_ARGUMENT, "null argument");
-    if (nf > c->image_floats) return set_err(c, WF_ERR_CAPACITY, "no image of that size");
-    WF_CK(c, cudaMemcpyAsync(image, c->image, sizeof(float) * (size_t)nf, cudaMemcpyDeviceToHost, c->stream));
-    WF_CK(c, cudaStreamSynchronize(c->stream));
     return WF_OK;
 }
 
@@ -1139,26 +1003,6 @@ int wf_timer_end(wf_ctx* c, double* out_ms)
     WF_CK(c, cudaEventElapsedTime(&ms, c->timer[0], c->timer[1]));
     *out_ms = ms;
     return WF_OK;
-}
-
-int wf_render_accumulate(wf_ctx* c, const wf_render_params* P, float* accum_rgb, wf_render_stats* st)
-{
-    if (!c || !accum_rgb) return set_err(c, WF_ERR_INVALID_ARGUMENT, "null argument");
-    int rc = validate_params(c, P);
-    if (rc) return rc;
-    cudaSetDevice(c->device);
-    const int64_t nf = 3 * (int64_t)P->width * P->height;
-    float* accum = nullptr;
-    WF_CK(c, cudaMallocAsync(&accum, sizeof(float) * nf, c->stream));
-    rc = render_into(c, P, accum, st);
-    if (rc == WF_OK) {
-        cudaError_t e = cudaMemcpyAsync(accum_rgb, accum, sizeof(float) * nf, cudaMemcpyDeviceToHost, c->stream);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-        if (e != cudaSuccess) rc = set_err(c, WF_ERR_CUDA, cudaGetErrorString(e));
-    }
-    cudaFreeAsync(accum, c->stream);
-    cudaStreamSynchronize(c->stream);
-    return rc;
 }
 
 }  // extern "C"

@@ -99,6 +99,7 @@ struct RayQueueDev {
     float *tr, *tg, *tb;
     float* pdf;
     int32_t *pixel, *depth, *sample;
+    int32_t* job;  // device addition: the render job the path belongs to
     int64_t capacity;
 };
 
@@ -119,7 +120,36 @@ struct ShadowQueueDev {
     float *ox, *oy, *oz, *dx, *dy, *dz, *dist;
     float *cr, *cg, *cb;
     int32_t* pixel;
+    int32_t* job;
     int64_t capacity;
+};
+
+// A render job as the kernels see it: which resident scene, the shading
+// parameters (WavefrontRenderer's public fields), its RNG key and where its
+// per-pixel sums live.  Rays of many jobs share one wavefront; each ray finds
+// its job, scene and accumulator through this table.
+struct DeviceJob {
+    int32_t scene;
+    int32_t width, height;
+    int32_t max_depth;
+    int32_t rr_min_depth;
+    int32_t cost_aware_rr;
+    float firefly;
+    uint32_t seed_lo, seed_hi;
+    int32_t pad;
+    int64_t accum_offset;            // float index of the job's first pixel sum
+    const float* rel_cost_material;  // float(relativeCost) per material, or null
+    wf_camera camera;
+};
+
+// One slice of a wave: samples [first_sample, first_sample + nspp) of every
+// pixel of a job, as paths [path_offset, path_offset + width*height*nspp).
+struct WaveChunk {
+    int32_t job;
+    int32_t first_sample;
+    int32_t nspp;
+    int32_t pad;
+    int64_t path_offset;
 };
 
 // ---------------------------------------------------------------------------

@@ -45,18 +45,26 @@ void launch_occluded_api(const DeviceScene& S, int64_t n, const float* ox, const
                          const float* oz, const float* dx, const float* dy, const float* dz,
                          const float* maxd, uint8_t* out, int* err, LaunchCfg cfg, cudaStream_t s);
 
-// Render loop stages.  Counts live in device memory.
-void launch_trace_render(const DeviceScene& S, RayQueueDev rq, const ull* d_n, HitQueueDev hq,
-                         ull* hq_n, float* accum, ull* work, int* err, LaunchCfg cfg,
+// Render loop stages over a job table and a scene table (device memory).
+// Counts live in device memory; accumulators at accum + job.accum_offset.
+// header[0] = paths in the wave, header[1] = chunks (device memory, so a
+// captured wave can be replayed for any job mix).
+void launch_camera_chunks(const WaveChunk* chunks, const long long* header, const DeviceJob* jobs, RayQueueDev rq,
+                          LaunchCfg cfg, cudaStream_t s);
+void launch_trace_render(const DeviceScene* scenes, const DeviceJob* jobs, RayQueueDev rq, const ull* d_n,
+                         HitQueueDev hq, ull* hq_n, float* accum, ull* work, int* err, LaunchCfg cfg,
                          cudaStream_t s);
-void launch_shade(const DeviceScene& S, const ShadeParams& P, RayQueueDev rq, HitQueueDev hq,
+void launch_shade(const DeviceScene* scenes, const DeviceJob* jobs, RayQueueDev rq, HitQueueDev hq,
                   const ull* hq_n, ShadowQueueDev sh, ull* sh_n, RayQueueDev next, ull* next_n,
                   float* accum, int* err, LaunchCfg cfg, cudaStream_t s);
-void launch_occluded_render(const DeviceScene& S, ShadowQueueDev sh, const ull* sh_n, float* accum,
-                            ull* work, int* err, LaunchCfg cfg, cudaStream_t s);
+void launch_occluded_render(const DeviceScene* scenes, const DeviceJob* jobs, ShadowQueueDev sh,
+                            const ull* sh_n, float* accum, ull* work, int* err, LaunchCfg cfg, cudaStream_t s);
+// tally[0..3] += rays, hits, shadow rays, (rays > 0) of the bounce just run.
+void launch_tally(const ull* counters, ull* tally, cudaStream_t s);
 
-// RayQueue::sortKey over the queue, (key, index) pairs for the radix sort.
-void launch_ray_keys(RayQueueDev rq, const ull* d_n, const float bmin[3], const float bmax[3],
+// RayQueue::sortKey over the queue (each ray's scene bounds), (key, index)
+// pairs for the radix sort.
+void launch_ray_keys(const DeviceScene* scenes, const DeviceJob* jobs, RayQueueDev rq, const ull* d_n,
                      uint64_t* keys, uint32_t* vals, LaunchCfg cfg, cudaStream_t s);
 void launch_ray_keys_raw(int64_t n, const float* ox, const float* oy, const float* oz,
                          const float* dx, const float* dy, const float* dz, const float bmin[3],
@@ -94,8 +102,8 @@ struct ShadeColumnsMut {
     int32_t* tex;
     float *tr, *tg, *tb, *px, *py, *pz;
 };
-void launch_hit_columns(const DeviceScene& S, RayQueueDev rq, HitQueueDev hq, const ull* d_n,
-                        ShadeColumnsMut out, LaunchCfg cfg, cudaStream_t s);
+void launch_hit_columns(const DeviceScene* scenes, const DeviceJob* jobs, RayQueueDev rq, HitQueueDev hq,
+                        const ull* d_n, ShadeColumnsMut out, LaunchCfg cfg, cudaStream_t s);
 void launch_permute_hits(HitQueueDev in, const uint32_t* perm, const ull* d_n, HitQueueDev out,
                          LaunchCfg cfg, cudaStream_t s);
 

@@ -1,0 +1,852 @@
+// wf_loop.cpp — the wavefront render loop behind wf_render*, wf_render_batch
+// and the serving loop (reference src/render/WavefrontRenderer.cpp:94-399).
+//
+// A wave is a set of chunks — (job, range of samples) — whose paths are
+// generated together and bounce together: trace, shade, shadow rays, once
+// per depth.  Two executors run a wave:
+//   host loop  one host round trip per bounce (counts read back); needed for
+//              the ShadingQueue policies, whose type order is decided on the
+//              host, and for per-stage timings;
+//   graph      the whole bounce chain captured once as a CUDA graph (all
+//              counts stay on the device; empty bounces cost only launches)
+//              and replayed for every wave with the same depth.
+// Jobs share waves through the job table: each ray carries its job id, the
+// job names its resident scene, RNG seed and accumulator offset.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/wf_api.h"
+#include "wf_ctx.h"
+#include "wf_kernels.h"
+#include "wf_sort.h"
+
+using namespace wf;
+
+namespace {
+
+int validate_job(wf_ctx* c, const wf_job& j)
+{
+    if (j.scene_id < 0 || j.scene_id >= (int)c->scenes.size() || !c->scenes[j.scene_id].live)
+        return set_err(c, WF_ERR_STATE, "job names a scene that is not resident");
+    if (j.width < 2 || j.height < 2)
+        return set_err(c, WF_ERR_INVALID_ARGUMENT, "width and height must be >= 2 (u = x/(width-1))");
+    if ((int64_t)j.width * j.height > (int64_t)1 << 28)
+        return set_err(c, WF_ERR_INVALID_ARGUMENT, "image larger than 2^28 pixels");
+    if (j.samples_per_pixel < 1) return set_err(c, WF_ERR_INVALID_ARGUMENT, "samples_per_pixel < 1");
+    if (j.max_depth < 0 || j.max_depth > 0xFFFF) return set_err(c, WF_ERR_INVALID_ARGUMENT, "max_depth out of range");
+    return WF_OK;
+}
+
+// Device job: cost-aware RR reads float(relativeCost) per material
+// (WavefrontRenderer.cpp:781-785) from a table copied here.
+int make_device_job(wf_ctx* c, const wf_job& j, int64_t accum_offset, DeviceJob& dj)
+{
+    std::memset(&dj, 0, sizeof(dj));
+    dj.scene = j.scene_id;
+    dj.width = j.width;
+    dj.height = j.height;
+    dj.max_depth = j.max_depth;
+    dj.rr_min_depth = j.rr_min_depth;
+    dj.cost_aware_rr = j.enable_cost_aware_rr;
+    dj.firefly = j.firefly_threshold;
+    dj.seed_lo = j.seed_lo;
+    dj.seed_hi = j.seed_hi;
+    dj.accum_offset = accum_offset;
+    dj.camera = j.camera;
+    if (j.enable_cost_aware_rr && j.rel_cost_material) {
+        const int nm = c->scenes[j.scene_id].S.num_materials;
+        std::vector<float> f(nm);
+        for (int m = 0; m < nm; ++m) f[m] = (float)j.rel_cost_material[m];
+        float* d = nullptr;
+        WF_CK(c, wf_dalloc(c->rel_cost_allocs, &d, nm));
+        WF_CK(c, cudaMemcpyAsync(d, f.data(), sizeof(float) * nm, cudaMemcpyHostToDevice, c->stream));
+        dj.rel_cost_material = d;
+    }
+    return WF_OK;
+}
+
+int upload_jobs(wf_ctx* c, const std::vector<DeviceJob>& jobs)
+{
+    int rc = ensure_job_tables(c, (int)jobs.size(), 1);
+    if (rc) return rc;
+    WF_CK(c, cudaMemcpyAsync(c->d_jobs, jobs.data(), sizeof(DeviceJob) * jobs.size(), cudaMemcpyHostToDevice,
+                             c->stream));
+    return WF_OK;
+}
+
+// Chunks of the next wave and the device header (total paths, chunk count).
+int upload_wave(wf_ctx* c, const std::vector<WaveChunk>& chunks, int64_t total)
+{
+    int rc = ensure_job_tables(c, 1, (int)chunks.size());
+    if (rc) return rc;
+    WF_CK(c, cudaMemcpyAsync(c->d_chunks, chunks.data(), sizeof(WaveChunk) * chunks.size(), cudaMemcpyHostToDevice,
+                             c->stream));
+    long long hdr[2] = {(long long)total, (long long)chunks.size()};
+    WF_CK(c, cudaMemcpyAsync(c->d_wave_header, hdr, sizeof(hdr), cudaMemcpyHostToDevice, c->stream));
+    // a pageable source may be read after the call returns; make it safe
+    WF_CK(c, cudaStreamSynchronize(c->stream));
+    return WF_OK;
+}
+
+// One wave, one host round trip per bounce.  policy / ray sort as in the
+// reference (RayQueue::schedule + ShadingQueue::schedule), materials of
+// scene `policy_scene`.
+int wave_host(wf_ctx* c, int64_t total, int max_depth, int policy, bool ray_sort, int policy_scene,
+              const double* rc_mat, const double* rc_tex, wf_render_stats& stats)
+{
+    cudaStream_t s = c->stream;
+    const LaunchCfg PC = persist_cfg(c), WC = wide_cfg(c);
+    cudaEvent_t* ev = c->ev;
+    float ms = 0.0f;
+    int cur = 0;
+    launch_camera_chunks(c->d_chunks, c->d_wave_header, c->d_jobs, c->rq[cur], WC, s);
+    stats.kernel_launches += 1;
+    ull hc = (ull)total;
+    WF_CK(c, cudaMemcpyAsync(c->counters, &hc, sizeof(ull), cudaMemcpyHostToDevice, s));
+    int64_t count = total;
+    stats.waves++;
+    for (int depth = 0; depth < max_depth && count > 0; ++depth) {
+        stats.bounces++;
+        stats.closest_rays += (uint64_t)count;
+        if (ray_sort) {  // RayQueue::schedule + materialize (.cpp:159-168)
+            WF_CK(c, cudaEventRecord(ev[2], s));
+            launch_ray_keys(c->d_scene_table, c->d_jobs, c->rq[cur], c->counters, c->keys, c->vals, WC, s);
+            uint64_t* rk;
+            uint32_t* rv;
+            RadixSortArgs a{c->keys, c->vals, c->keys_tmp, c->vals_tmp, c->hist, c->counters, c->nb, 0, 33, &rk, &rv};
+            radix_sort_pairs(a, s);
+            launch_gather_rays(c->rq[cur], rv, c->counters, c->rq[1 - cur], WC, s);
+            stats.kernel_launches += 2 + 3 * 5;
+            cur = 1 - cur;
+            WF_CK(c, cudaEventRecord(ev[3], s));
+            stats.sorted_elements += (uint64_t)count;
+        }
+        WF_CK(c, cudaMemsetAsync(c->counters + 1, 0, sizeof(ull) * 5, s));
+        WF_CK(c, cudaEventRecord(ev[4], s));
+        launch_trace_render(c->d_scene_table, c->d_jobs, c->rq[cur], c->counters, c->hq[0], c->counters + 1,
+                            c->arena, c->counters + 4, c->err_flag, PC, s);
+        WF_CK(c, cudaEventRecord(ev[5], s));
+        HitQueueDev hq_use = c->hq[0];
+        if (policy != WF_POLICY_NONE) {
+            ull hits = 0;
+            WF_CK(c, cudaMemcpyAsync(&hits, c->counters + 1, sizeof(ull), cudaMemcpyDeviceToHost, s));
+            WF_CK(c, cudaStreamSynchronize(s));
+            ShadeColumnsMut cm{c->col_mat, c->col_tex, c->col_tr, c->col_tg, c->col_tb, c->col_px, c->col_py, c->col_pz};
+            launch_hit_columns(c->d_scene_table, c->d_jobs, c->rq[cur], c->hq[0], c->counters + 1, cm, WC, s);
+            ShadeColumnsDev cd{c->col_mat, c->col_tex, c->col_tr, c->col_tg, c->col_tb, c->col_px, c->col_py, c->col_pz};
+            const ResidentScene& R = c->scenes[policy_scene];
+            uint32_t* perm = nullptr;
+            int rc = schedule_columns(c, policy, c->counters + 1, (int64_t)hits, cd, R.S.materials, R.S.num_materials,
+                                      R.mats, R.S.num_textures, R.d_tex_bytes, R.tex_bytes, rc_mat, rc_tex, &perm);
+            if (rc) return rc;
+            launch_permute_hits(c->hq[0], perm, c->counters + 1, c->hq[1], WC, s);
+            stats.kernel_launches += c->last_schedule_launches + 2;
+            hq_use = c->hq[1];
+            stats.sorted_elements += hits;
+        }
+        WF_CK(c, cudaEventRecord(ev[6], s));
+        launch_shade(c->d_scene_table, c->d_jobs, c->rq[cur], hq_use, c->counters + 1, c->sh, c->counters + 2,
+                     c->rq[1 - cur], c->counters + 3, c->arena, c->err_flag, PC, s);
+        launch_occluded_render(c->d_scene_table, c->d_jobs, c->sh, c->counters + 2, c->arena, c->counters + 5,
+                               c->err_flag, PC, s);
+        stats.kernel_launches += 3;
+        WF_CK(c, cudaEventRecord(ev[7], s));
+        ull cnt[4];
+        WF_CK(c, cudaMemcpyAsync(cnt, c->counters, sizeof(cnt), cudaMemcpyDeviceToHost, s));
+        WF_CK(c, cudaMemcpyAsync(c->counters, c->counters + 3, sizeof(ull), cudaMemcpyDeviceToDevice, s));
+        WF_CK(c, cudaStreamSynchronize(s));
+        if (ray_sort) {
+            WF_CK(c, cudaEventElapsedTime(&ms, ev[2], ev[3]));
+            stats.ms_ray_sort += ms;
+        }
+        WF_CK(c, cudaEventElapsedTime(&ms, ev[4], ev[5]));
+        stats.ms_intersect += ms;
+        WF_CK(c, cudaEventElapsedTime(&ms, ev[5], ev[6]));
+        stats.ms_schedule += ms;
+        WF_CK(c, cudaEventElapsedTime(&ms, ev[6], ev[7]));
+        stats.ms_shade += ms;
+        stats.shaded_hits += cnt[1];
+        stats.misses += (uint64_t)count - cnt[1];
+        stats.shadow_rays += cnt[2];
+        count = (int64_t)cnt[3];
+        cur = 1 - cur;
+    }
+    return WF_OK;
+}
+
+// The launches of one wave with every count on the device: what a graph
+// captures.  Returns the number of kernels.
+int record_chain(wf_ctx* c, int max_depth, bool ray_sort)
+{
+    cudaStream_t s = c->stream;
+    const LaunchCfg PC = persist_cfg(c), WC = wide_cfg(c);
+    int kernels = 0;
+    int cur = 0;
+    launch_camera_chunks(c->d_chunks, c->d_wave_header, c->d_jobs, c->rq[cur], WC, s);
+    cudaMemcpyAsync(c->counters, c->d_wave_header, sizeof(ull), cudaMemcpyDeviceToDevice, s);
+    kernels += 1;
+    for (int depth = 0; depth < max_depth; ++depth) {
+        if (ray_sort) {
+            launch_ray_keys(c->d_scene_table, c->d_jobs, c->rq[cur], c->counters, c->keys, c->vals, WC, s);
+            uint64_t* rk;
+            uint32_t* rv;
+            RadixSortArgs a{c->keys, c->vals, c->keys_tmp, c->vals_tmp, c->hist, c->counters, c->nb, 0, 33, &rk, &rv};
+            radix_sort_pairs(a, s);
+            launch_gather_rays(c->rq[cur], rv, c->counters, c->rq[1 - cur], WC, s);
+            kernels += 2 + 3 * 5;
+            cur = 1 - cur;
+        }
+        cudaMemsetAsync(c->counters + 1, 0, sizeof(ull) * 5, s);
+        launch_trace_render(c->d_scene_table, c->d_jobs, c->rq[cur], c->counters, c->hq[0], c->counters + 1, c->arena,
+                            c->counters + 4, c->err_flag, PC, s);
+        launch_shade(c->d_scene_table, c->d_jobs, c->rq[cur], c->hq[0], c->counters + 1, c->sh, c->counters + 2,
+                     c->rq[1 - cur], c->counters + 3, c->arena, c->err_flag, PC, s);
+        launch_occluded_render(c->d_scene_table, c->d_jobs, c->sh, c->counters + 2, c->arena, c->counters + 5,
+                               c->err_flag, PC, s);
+        launch_tally(c->counters, c->tally, s);
+        cudaMemcpyAsync(c->counters, c->counters + 3, sizeof(ull), cudaMemcpyDeviceToDevice, s);
+        kernels += 4;
+        cur = 1 - cur;
+    }
+    return kernels;
+}
+
+int wave_graph(wf_ctx* c, int max_depth, bool ray_sort, wf_render_stats& stats)
+{
+    cudaStream_t s = c->stream;
+    CapturedWave* g = nullptr;
+    for (auto& x : c->graphs)
+        if (x.max_depth == max_depth && x.ray_sort == ray_sort && x.variant == c->tuning.trace_variant &&
+            x.key_ptr == c->arena && x.key_cap == c->cap)
+            g = &x;
+    if (!g) {
+        cudaGraph_t graph = nullptr;
+        WF_CK(c, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        int k = record_chain(c, max_depth, ray_sort);
+        cudaError_t e = cudaStreamEndCapture(s, &graph);
+        if (e != cudaSuccess) return set_err(c, WF_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+        CapturedWave w;
+        e = cudaGraphInstantiate(&w.exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) return set_err(c, WF_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+        w.max_depth = max_depth;
+        w.ray_sort = ray_sort;
+        w.variant = c->tuning.trace_variant;
+        w.key_ptr = c->arena;
+        w.key_cap = c->cap;
+        w.kernels = k;
+        c->graphs.push_back(w);
+        g = &c->graphs.back();
+    }
+    WF_CK(c, cudaGraphLaunch(g->exec, s));
+    stats.waves++;
+    stats.kernel_launches += g->kernels;
+    return WF_OK;
+}
+
+int zero_tally(wf_ctx* c) { WF_CK(c, cudaMemsetAsync(c->tally, 0, sizeof(ull) * 8, c->stream)); return WF_OK; }
+
+int read_tally(wf_ctx* c, wf_render_stats& stats)
+{
+    ull t[4];
+    WF_CK(c, cudaMemcpyAsync(t, c->tally, sizeof(t), cudaMemcpyDeviceToHost, c->stream));
+    WF_CK(c, cudaStreamSynchronize(c->stream));
+    stats.closest_rays += t[0];
+    stats.shaded_hits += t[1];
+    stats.misses += t[0] - t[1];
+    stats.shadow_rays += t[2];
+    stats.bounces += (int32_t)t[3];
+    return WF_OK;
+}
+
+bool use_graph(const wf_ctx* c, bool batch, int policy)
+{
+    if (policy != WF_POLICY_NONE || c->tuning.graph_mode == 2) return false;
+    return batch || c->tuning.graph_mode == 1;
+}
+
+int validate_params(wf_ctx* c, const wf_render_params* P)
+{
+    if (!P) return set_err(c, WF_ERR_INVALID_ARGUMENT, "params is null");
+    if (P->policy < 0 || P->policy > 3) return set_err(c, WF_ERR_INVALID_ARGUMENT, "unknown policy");
+    if (c->scenes.empty() || !c->scenes[0].live) return set_err(c, WF_ERR_STATE, "no scene uploaded");
+    wf_job j{};
+    j.scene_id = 0;
+    j.width = P->width;
+    j.height = P->height;
+    j.samples_per_pixel = P->samples_per_pixel;
+    j.max_depth = P->max_depth;
+    return validate_job(c, j);
+}
+
+// renderScene for the current scene: leaves the per-pixel sums in the arena
+// at offset 0 (W*H*3 floats).
+int render_single(wf_ctx* c, const wf_render_params* P, wf_render_stats* st)
+{
+    cudaStream_t s = c->stream;
+    const int W = P->width, H = P->height;
+    const int64_t np = (int64_t)W * H;
+    int spw = P->spp_per_wave > 0 ? P->spp_per_wave : (int)std::max<int64_t>(1, c->paths_per_wave / np);
+    spw = std::max(1, std::min(spw, P->samples_per_pixel));
+    int rc = ensure_render_buffers(c, np * spw);
+    if (rc) return rc;
+    rc = ensure_arena(c, 3 * np);
+    if (rc) return rc;
+    rc = sync_scene_table(c);
+    if (rc) return rc;
+    free_all(c->rel_cost_allocs);
+    wf_job j{};
+    j.scene_id = 0;
+    j.width = W;
+    j.height = H;
+    j.samples_per_pixel = P->samples_per_pixel;
+    j.max_depth = P->max_depth;
+    j.rr_min_depth = P->rr_min_depth;
+    j.enable_cost_aware_rr = P->enable_cost_aware_rr;
+    j.firefly_threshold = P->firefly_threshold;
+    j.seed_lo = P->seed_lo;
+    j.seed_hi = P->seed_hi;
+    j.first_sample = P->first_sample;
+    j.rel_cost_material = P->rel_cost_material;
+    j.camera = P->camera;
+    std::vector<DeviceJob> table(1);
+    rc = make_device_job(c, j, 0, table[0]);
+    if (rc) return rc;
+    rc = upload_jobs(c, table);
+    if (rc) return rc;
+    WF_CK(c, cudaMemsetAsync(c->arena, 0, sizeof(float) * 3 * (size_t)np, s));
+    const bool graph = use_graph(c, false, P->policy);
+    wf_render_stats stats{};
+    if (graph) {
+        rc = zero_tally(c);
+        if (rc) return rc;
+    }
+    float ms = 0.0f;
+    WF_CK(c, cudaEventRecord(c->ev[0], s));
+    for (int s0 = 0; s0 < P->samples_per_pixel; s0 += spw) {
+        const int nspp = std::min(spw, P->samples_per_pixel - s0);
+        std::vector<WaveChunk> ch(1);
+        ch[0] = WaveChunk{0, P->first_sample + s0, nspp, 0, 0};
+        rc = upload_wave(c, ch, np * nspp);
+        if (rc) return rc;
+        rc = graph ? wave_graph(c, P->max_depth, P->enable_ray_sort != 0, stats)
+                   : wave_host(c, np * nspp, P->max_depth, P->policy, P->enable_ray_sort != 0, 0,
+                               P->rel_cost_material, P->rel_cost_texture, stats);
+        if (rc) return rc;
+    }
+    WF_CK(c, cudaEventRecord(c->ev[1], s));
+    WF_CK(c, cudaEventSynchronize(c->ev[1]));
+    WF_CK(c, cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]));
+    stats.ms_total = ms;
+    if (graph) {
+        rc = read_tally(c, stats);
+        if (rc) return rc;
+    }
+    rc = check_device_flag(c);
+    if (rc) return rc;
+    if (st) *st = stats;
+    return WF_OK;
+}
+
+// --------------------------------------------------------------------------
+// Serving loop
+// --------------------------------------------------------------------------
+
+// First-fit allocator of accumulator ranges (floats) inside the arena.
+struct RangeAllocator {
+    std::map<int64_t, int64_t> free;  // offset -> length
+    int64_t total = 0;
+    int64_t used = 0;
+    void reset(int64_t n)
+    {
+        free.clear();
+        if (n > 0) free[0] = n;
+        total = n;
+        used = 0;
+    }
+    int64_t alloc(int64_t n)
+    {
+        for (auto it = free.begin(); it != free.end(); ++it) {
+            if (it->second < n) continue;
+            const int64_t off = it->first, len = it->second;
+            free.erase(it);
+            if (len > n) free[off + n] = len - n;
+            used += n;
+            return off;
+        }
+        return -1;
+    }
+    void release(int64_t off, int64_t n)
+    {
+        used -= n;
+        auto it = free.emplace(off, n).first;
+        auto nx = std::next(it);
+        if (nx != free.end() && it->first + it->second == nx->first) {
+            it->second += nx->second;
+            free.erase(nx);
+        }
+        if (it != free.begin()) {
+            auto pv = std::prev(it);
+            if (pv->first + pv->second == it->first) {
+                pv->second += it->second;
+                free.erase(it);
+            }
+        }
+    }
+};
+
+struct ServedJob {
+    wf_job spec{};
+    int state = WF_JOB_QUEUED;
+    int samples_done = 0;
+    int frames = 0;
+    int64_t accum_off = -1;
+    int64_t accum_floats = 0;
+    double t_submit = 0, t_admit = -1, t_first = -1, t_done = -1;
+    std::vector<float> final_image;
+};
+
+double seconds_since(std::chrono::steady_clock::time_point t0)
+{
+    return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+}
+
+}  // namespace
+
+struct wf_server {
+    wf_ctx* c = nullptr;
+    wf_server_config cfg{};
+    std::map<int64_t, ServedJob> jobs;
+    std::deque<int64_t> queue;
+    std::vector<int64_t> running;
+    int64_t next_id = 1;
+    std::chrono::steady_clock::time_point t0;
+    RangeAllocator alloc;
+    int64_t wave_paths = 0;
+    int64_t wave_bytes = 0;
+    size_t rr = 0;
+    float* tmp = nullptr;  // averaged image staging (largest job)
+    int64_t tmp_floats = 0;
+};
+
+namespace {
+
+// Bytes of the wave buffers per path in flight: two RayQueues (14 columns),
+// two hit queues (5), the shadow queue (2 x 12), sort keys and values (2 x 12)
+// and the policy columns (8).
+constexpr int64_t kBytesPerPath = 2 * 14 * 4 + 2 * 5 * 4 + 2 * 12 * 4 + 2 * 12 + 8 * 4;
+
+int finish_job(wf_server* sv, int64_t id, ServedJob& j)
+{
+    wf_ctx* c = sv->c;
+    const int64_t nf = j.accum_floats;
+    if (nf > sv->tmp_floats) {
+        cudaFree(sv->tmp);
+        sv->tmp = nullptr;
+        sv->tmp_floats = 0;
+        WF_CK(c, cudaMalloc(&sv->tmp, sizeof(float) * nf));
+        sv->tmp_floats = nf;
+    }
+    launch_finalize(c->arena + j.accum_off, nf, (float)j.samples_done, sv->tmp, c->stream);
+    j.final_image.resize(nf);
+    WF_CK(c, cudaMemcpyAsync(j.final_image.data(), sv->tmp, sizeof(float) * nf, cudaMemcpyDeviceToHost, c->stream));
+    WF_CK(c, cudaStreamSynchronize(c->stream));
+    sv->alloc.release(j.accum_off, j.accum_floats);
+    j.accum_off = -1;
+    (void)id;
+    return WF_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+int wf_render(wf_ctx* c, const wf_render_params* P, float* image, wf_render_stats* st)
+{
+    if (!c || !image) return set_err(c, WF_ERR_INVALID_ARGUMENT, "null argument");
+    int rc = validate_params(c, P);
+    if (rc) return rc;
+    cudaSetDevice(c->device);
+    rc = render_single(c, P, st);
+    if (rc) return rc;
+    const int64_t nf = 3 * (int64_t)P->width * P->height;
+    if (nf > c->image_floats) {
+        cudaFree(c->image);
+        c->image = nullptr;
+        c->image_floats = 0;
+        WF_CK(c, cudaMalloc(&c->image, sizeof(float) * nf));
+        c->image_floats = nf;
+    }
+    launch_finalize(c->arena, nf, (float)P->samples_per_pixel, c->image, c->stream);  // writeAveragedImage
+    if (st) st->kernel_launches += 1;
+    WF_CK(c, cudaMemcpyAsync(image, c->image, sizeof(float) * nf, cudaMemcpyDeviceToHost, c->stream));
+    WF_CK(c, cudaStreamSynchronize(c->stream));
+    return WF_OK;
+}
+
+int wf_render_device(wf_ctx* c, const wf_render_params* P, wf_render_stats* st)
+{
+    if (!c) return WF_ERR_INVALID_ARGUMENT;
+    int rc = validate_params(c, P);
+    if (rc) return rc;
+    cudaSetDevice(c->device);
+    rc = render_single(c, P, st);
+    if (rc) return rc;
+    const int64_t nf = 3 * (int64_t)P->width * P->height;
+    if (nf > c->image_floats) {
+        cudaFree(c->image);
+        c->image = nullptr;
+        c->image_floats = 0;
+        WF_CK(c, cudaMalloc(&c->image, sizeof(float) * nf));
+        c->image_floats = nf;
+    }
+    launch_finalize(c->arena, nf, (float)P->samples_per_pixel, c->image, c->stream);
+    if (st) st->kernel_launches += 1;
+    WF_CK(c, cudaStreamSynchronize(c->stream));
+    return WF_OK;
+}
+
+int wf_image_download(wf_ctx* c, float* image, int64_t nf)
+{
+    if (!c || !image || nf < 0) return set_err(c, WF_ERR_INVALID_ARGUMENT, "null argument");
+    if (nf > c->image_floats) return set_err(c, WF_ERR_CAPACITY, "no image of that size");
+    WF_CK(c, cudaMemcpyAsync(image, c->image, sizeof(float) * (size_t)nf, cudaMemcpyDeviceToHost, c->stream));
+    WF_CK(c, cudaStreamSynchronize(c->stream));
+    return WF_OK;
+}
+
+int wf_render_accumulate(wf_ctx* c, const wf_render_params* P, float* accum_rgb, wf_render_stats* st)
+{
+    if (!c || !accum_rgb) return set_err(c, WF_ERR_INVALID_ARGUMENT, "null argument");
+    int rc = validate_params(c, P);
+    if (rc) return rc;
+    cudaSetDevice(c->device);
+    rc = render_single(c, P, st);
+    if (rc) return rc;
+    const int64_t nf = 3 * (int64_t)P->width * P->height;
+    WF_CK(c, cudaMemcpyAsync(accum_rgb, c->arena, sizeof(float) * nf, cudaMemcpyDeviceToHost, c->stream));
+    WF_CK(c, cudaStreamSynchronize(c->stream));
+    return WF_OK;
+}
+
+int wf_render_batch(wf_ctx* c, const wf_job* jobs, int32_t njobs, float* const* images, wf_render_stats* st)
+{
+    if (!c || (njobs > 0 && !jobs) || njobs < 0) return set_err(c, WF_ERR_INVALID_ARGUMENT, "null argument");
+    if (njobs == 0) return WF_OK;
+    cudaSetDevice(c->device);
+    cudaStream_t s = c->stream;
+    int rc;
+    int64_t floats = 0, max_np = 0;
+    int max_depth = 0;
+    std::vector<int64_t> offs(njobs);
+    for (int j = 0; j < njobs; ++j) {
+        if ((rc = validate_job(c, jobs[j]))) return rc;
+        const int64_t np = (int64_t)jobs[j].width * jobs[j].height;
+        offs[j] = floats;
+        floats += 3 * np;
+        max_np = std::max(max_np, np);
+        max_depth = std::max(max_depth, jobs[j].max_depth);
+    }
+    const int64_t cap = std::max(c->paths_per_wave, max_np);
+    if ((rc = ensure_render_buffers(c, cap))) return rc;
+    if ((rc = ensure_arena(c, floats))) return rc;
+    if ((rc = sync_scene_table(c))) return rc;
+    free_all(c->rel_cost_allocs);
+    std::vector<DeviceJob> table(njobs);
+    for (int j = 0; j < njobs; ++j)
+        if ((rc = make_device_job(c, jobs[j], offs[j], table[j]))) return rc;
+    if ((rc = upload_jobs(c, table))) return rc;
+    WF_CK(c, cudaMemsetAsync(c->arena, 0, sizeof(float) * (size_t)floats, s));
+    const bool graph = use_graph(c, true, WF_POLICY_NONE);
+    wf_render_stats stats{};
+    if (graph && (rc = zero_tally(c))) return rc;
+    std::vector<int> done(njobs, 0);
+    float ms = 0.0f;
+    WF_CK(c, cudaEventRecord(c->ev[0], s));
+    int next = 0;  // first job with samples left
+    while (next < njobs) {
+        std::vector<WaveChunk> chunks;
+        int64_t total = 0;
+        int wave_depth = 0;
+        for (int j = next; j < njobs; ++j) {
+            const int64_t np = (int64_t)jobs[j].width * jobs[j].height;
+            const int left = jobs[j].samples_per_pixel - done[j];
+            if (left <= 0) continue;
+            const int64_t room = cap - total;
+            if (np > room) break;
+            const int nspp = (int)std::min<int64_t>(left, room / np);
+            chunks.push_back(WaveChunk{j, jobs[j].first_sample + done[j], nspp, 0, total});
+            total += np * nspp;
+            done[j] += nspp;
+            wave_depth = std::max(wave_depth, jobs[j].max_depth);
+        }
+        if (chunks.empty()) return set_err(c, WF_ERR_CAPACITY, "no job fits a wave");
+        if ((rc = upload_wave(c, chunks, total))) return rc;
+        rc = graph ? wave_graph(c, max_depth, false, stats)
+                   : wave_host(c, total, wave_depth, WF_POLICY_NONE, false, 0, nullptr, nullptr, stats);
+        if (rc) return rc;
+        while (next < njobs && done[next] >= jobs[next].samples_per_pixel) ++next;
+    }
+    WF_CK(c, cudaEventRecord(c->ev[1], s));
+    WF_CK(c, cudaEventSynchronize(c->ev[1]));
+    WF_CK(c, cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]));
+    stats.ms_total = ms;
+    if (graph && (rc = read_tally(c, stats))) return rc;
+    if ((rc = check_device_flag(c))) return rc;
+    if (images) {
+        float* tmp = nullptr;
+        WF_CK(c, cudaMalloc(&tmp, sizeof(float) * 3 * (size_t)max_np));
+        for (int j = 0; j < njobs; ++j) {
+            if (!images[j]) continue;
+            const int64_t nf = 3 * (int64_t)jobs[j].width * jobs[j].height;
+            launch_finalize(c->arena + offs[j], nf, (float)jobs[j].samples_per_pixel, tmp, s);
+            cudaMemcpyAsync(images[j], tmp, sizeof(float) * nf, cudaMemcpyDeviceToHost, s);
+            stats.kernel_launches += 1;
+        }
+        cudaError_t e = cudaStreamSynchronize(s);
+        cudaFree(tmp);
+        if (e != cudaSuccess) return set_err(c, WF_ERR_CUDA, cudaGetErrorString(e));
+    }
+    if (st) *st = stats;
+    return WF_OK;
+}
+
+// ---- serving loop ---------------------------------------------------------
+
+int wf_server_create(wf_ctx* c, const wf_server_config* cfg, wf_server** out)
+{
+    if (!c || !cfg || !out) return WF_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    cudaSetDevice(c->device);
+    wf_server* sv = new wf_server();
+    sv->c = c;
+    sv->cfg = *cfg;
+    if (sv->cfg.frame_spp <= 0) sv->cfg.frame_spp = 8;
+    sv->wave_paths = cfg->max_paths_per_wave > 0 ? cfg->max_paths_per_wave : c->paths_per_wave;
+    sv->wave_bytes = sv->wave_paths * kBytesPerPath;
+    const int64_t accum_bytes = cfg->hbm_budget_bytes - sv->wave_bytes;
+    if (accum_bytes <= 0) {
+        delete sv;
+        return set_err(c, WF_ERR_OUT_OF_MEMORY, "HBM budget smaller than the wave buffers");
+    }
+    int rc = ensure_render_buffers(c, sv->wave_paths);
+    if (!rc) rc = ensure_arena(c, accum_bytes / 4);
+    if (!rc) rc = sync_scene_table(c);
+    if (rc) {
+        delete sv;
+        return rc;
+    }
+    sv->alloc.reset(accum_bytes / 4);
+    sv->t0 = std::chrono::steady_clock::now();
+    *out = sv;
+    return WF_OK;
+}
+
+int wf_server_destroy(wf_server* sv)
+{
+    if (!sv) return WF_OK;
+    cudaFree(sv->tmp);
+    delete sv;
+    return WF_OK;
+}
+
+double wf_server_clock(const wf_server* sv) { return sv ? seconds_since(sv->t0) : 0.0; }
+
+int wf_server_submit(wf_server* sv, const wf_job* job, int64_t* out_id)
+{
+    if (!sv || !job || !out_id) return WF_ERR_INVALID_ARGUMENT;
+    int rc = validate_job(sv->c, *job);
+    if (rc) return rc;
+    ServedJob j;
+    j.spec = *job;
+    j.spec.rel_cost_material = nullptr;  // a request carries no cost table across calls
+    j.spec.enable_cost_aware_rr = 0;
+    j.t_submit = seconds_since(sv->t0);
+    j.accum_floats = 3 * (int64_t)job->width * job->height;
+    const int64_t id = sv->next_id++;
+    if (j.accum_floats > sv->alloc.total || (int64_t)job->width * job->height > sv->wave_paths) {
+        j.state = WF_JOB_REJECTED;
+    } else {
+        sv->queue.push_back(id);
+    }
+    sv->jobs.emplace(id, std::move(j));
+    *out_id = id;
+    return WF_OK;
+}
+
+int wf_server_step(wf_server* sv, wf_server_step_info* info)
+{
+    if (!sv) return WF_ERR_INVALID_ARGUMENT;
+    wf_ctx* c = sv->c;
+    cudaSetDevice(c->device);
+    cudaStream_t s = c->stream;
+    int rc;
+    // 1. admit in arrival order while accumulators fit the budget
+    while (!sv->queue.empty()) {
+        ServedJob& j = sv->jobs[sv->queue.front()];
+        if (j.state != WF_JOB_QUEUED) {
+            sv->queue.pop_front();
+            continue;
+        }
+        const int64_t off = sv->alloc.alloc(j.accum_floats);
+        if (off < 0) break;
+        j.accum_off = off;
+        j.state = WF_JOB_RUNNING;
+        j.t_admit = seconds_since(sv->t0);
+        WF_CK(c, cudaMemsetAsync(c->arena + off, 0, sizeof(float) * (size_t)j.accum_floats, s));
+        sv->running.push_back(sv->queue.front());
+        sv->queue.pop_front();
+    }
+    wf_server_step_info si{};
+    if (sv->running.empty()) {
+        si.queued = (int32_t)sv->queue.size();
+        si.budget_used_bytes = sv->wave_bytes + 4 * sv->alloc.used;
+        if (info) *info = si;
+        return WF_OK;
+    }
+    // 2. one wave: up to frame_spp samples of each running job, round robin
+    std::vector<DeviceJob> table;
+    std::vector<WaveChunk> chunks;
+    std::vector<std::pair<int64_t, int>> taken;  // job id, samples
+    int64_t total = 0;
+    int depth = 0;
+    const size_t nr = sv->running.size();
+    free_all(c->rel_cost_allocs);
+    for (size_t k = 0; k < nr; ++k) {
+        const int64_t id = sv->running[(sv->rr + k) % nr];
+        ServedJob& j = sv->jobs[id];
+        const int64_t np = (int64_t)j.spec.width * j.spec.height;
+        const int left = j.spec.samples_per_pixel - j.samples_done;
+        const int64_t room = sv->wave_paths - total;
+        if (left <= 0 || np > room) continue;
+        const int nspp = (int)std::min<int64_t>({(int64_t)left, (int64_t)sv->cfg.frame_spp, room / np});
+        DeviceJob dj;
+        if ((rc = make_device_job(c, j.spec, j.accum_off, dj))) return rc;
+        table.push_back(dj);
+        chunks.push_back(WaveChunk{(int32_t)table.size() - 1, j.spec.first_sample + j.samples_done, nspp, 0, total});
+        taken.emplace_back(id, nspp);
+        total += np * nspp;
+        depth = std::max(depth, j.spec.max_depth);
+    }
+    sv->rr = (sv->rr + 1) % std::max<size_t>(nr, 1);
+    if (!chunks.empty()) {
+        if ((rc = upload_jobs(c, table))) return rc;
+        if ((rc = upload_wave(c, chunks, total))) return rc;
+        wf_render_stats stats{};
+        if ((rc = zero_tally(c))) return rc;
+        WF_CK(c, cudaEventRecord(c->ev[0], s));
+        const bool graph = use_graph(c, true, WF_POLICY_NONE);
+        rc = graph ? wave_graph(c, depth, false, stats)
+                   : wave_host(c, total, depth, WF_POLICY_NONE, false, 0, nullptr, nullptr, stats);
+        if (rc) return rc;
+        WF_CK(c, cudaEventRecord(c->ev[1], s));
+        WF_CK(c, cudaEventSynchronize(c->ev[1]));
+        float ms = 0.0f;
+        WF_CK(c, cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]));
+        if (graph && (rc = read_tally(c, stats))) return rc;
+        if ((rc = check_device_flag(c))) return rc;
+        si.step_ms = ms;
+        si.rays_traced = stats.closest_rays + stats.shadow_rays;
+        si.paths_in_wave = total;
+        si.jobs_in_wave = (int32_t)chunks.size();
+    }
+    // 3. progress, frames, completion
+    const double now = seconds_since(sv->t0);
+    for (auto& [id, n] : taken) {
+        ServedJob& j = sv->jobs[id];
+        j.samples_done += n;
+        const bool complete = j.samples_done >= j.spec.samples_per_pixel;
+        if (j.samples_done % sv->cfg.frame_spp == 0 || complete) {
+            j.frames++;
+            if (j.t_first < 0) j.t_first = now;
+        }
+        if (complete) {
+            if ((rc = finish_job(sv, id, j))) return rc;
+            j.state = WF_JOB_DONE;
+            j.t_done = seconds_since(sv->t0);
+            si.completed_this_step++;
+        }
+    }
+    sv->running.erase(std::remove_if(sv->running.begin(), sv->running.end(),
+                                     [&](int64_t id) { return sv->jobs[id].state != WF_JOB_RUNNING; }),
+                      sv->running.end());
+    si.queued = (int32_t)sv->queue.size();
+    si.running = (int32_t)sv->running.size();
+    si.budget_used_bytes = sv->wave_bytes + 4 * sv->alloc.used;
+    if (info) *info = si;
+    return WF_OK;
+}
+
+int wf_server_status(wf_server* sv, int64_t id, wf_job_status* out)
+{
+    if (!sv || !out) return WF_ERR_INVALID_ARGUMENT;
+    auto it = sv->jobs.find(id);
+    if (it == sv->jobs.end()) return set_err(sv->c, WF_ERR_INVALID_ARGUMENT, "no such job");
+    const ServedJob& j = it->second;
+    out->state = j.state;
+    out->samples_done = j.samples_done;
+    out->frames = j.frames;
+    out->reserved = 0;
+    out->t_submit = j.t_submit;
+    out->t_admit = j.t_admit;
+    out->t_first_frame = j.t_first;
+    out->t_done = j.t_done;
+    return WF_OK;
+}
+
+int wf_server_image(wf_server* sv, int64_t id, float* image, int64_t nf)
+{
+    if (!sv || !image) return WF_ERR_INVALID_ARGUMENT;
+    auto it = sv->jobs.find(id);
+    if (it == sv->jobs.end()) return set_err(sv->c, WF_ERR_INVALID_ARGUMENT, "no such job");
+    ServedJob& j = it->second;
+    if (nf < j.accum_floats) return set_err(sv->c, WF_ERR_CAPACITY, "image buffer too small");
+    if (j.state == WF_JOB_DONE) {
+        std::memcpy(image, j.final_image.data(), sizeof(float) * j.accum_floats);
+        return WF_OK;
+    }
+    if (j.state != WF_JOB_RUNNING || j.samples_done == 0) return set_err(sv->c, WF_ERR_STATE, "no frame yet");
+    wf_ctx* c = sv->c;
+    if (j.accum_floats > sv->tmp_floats) {
+        cudaFree(sv->tmp);
+        sv->tmp = nullptr;
+        sv->tmp_floats = 0;
+        WF_CK(c, cudaMalloc(&sv->tmp, sizeof(float) * j.accum_floats));
+        sv->tmp_floats = j.accum_floats;
+    }
+    launch_finalize(c->arena + j.accum_off, j.accum_floats, (float)j.samples_done, sv->tmp, c->stream);
+    WF_CK(c, cudaMemcpyAsync(image, sv->tmp, sizeof(float) * j.accum_floats, cudaMemcpyDeviceToHost, c->stream));
+    WF_CK(c, cudaStreamSynchronize(c->stream));
+    return WF_OK;
+}
+
+int wf_server_cancel(wf_server* sv, int64_t id)
+{
+    if (!sv) return WF_ERR_INVALID_ARGUMENT;
+    auto it = sv->jobs.find(id);
+    if (it == sv->jobs.end()) return set_err(sv->c, WF_ERR_INVALID_ARGUMENT, "no such job");
+    ServedJob& j = it->second;
+    if (j.state == WF_JOB_RUNNING) {
+        cudaStreamSynchronize(sv->c->stream);
+        sv->alloc.release(j.accum_off, j.accum_floats);
+        j.accum_off = -1;
+        sv->running.erase(std::remove(sv->running.begin(), sv->running.end(), id), sv->running.end());
+    }
+    if (j.state == WF_JOB_RUNNING || j.state == WF_JOB_QUEUED) {
+        j.state = WF_JOB_CANCELLED;
+        j.t_done = seconds_since(sv->t0);
+    }
+    return WF_OK;
+}
+
+}  // extern "C"

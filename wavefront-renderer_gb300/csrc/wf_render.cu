@@ -52,7 +52,66 @@ __global__ void k_camera(wf_camera cam, int W, int H, uint32_t s0, uint32_t s1, 
         rq.pixel[i] = p;
         rq.depth[i] = 0;
         rq.sample[i] = sample;
+        if (rq.job) rq.job[i] = 0;
     }
+}
+
+// Camera rays of one wave made of chunks (job, samples) of several jobs: the
+// same arithmetic as k_camera, the job's camera and seed.
+__global__ void k_camera_chunks(const WaveChunk* __restrict__ chunks, const long long* __restrict__ header,
+                                const DeviceJob* __restrict__ jobs, RayQueueDev rq)
+{
+    const int64_t total = header[0];
+    const int nchunks = (int)header[1];
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        int lo = 0, hi = nchunks - 1;  // last chunk with path_offset <= i
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (chunks[mid].path_offset <= i) lo = mid; else hi = mid - 1;
+        }
+        const WaveChunk ch = chunks[lo];
+        const DeviceJob& J = jobs[ch.job];
+        const int64_t np = (int64_t)J.width * J.height;
+        const int64_t local = i - ch.path_offset;
+        const int s = (int)(local / np);
+        const int p = (int)(local - (int64_t)s * np);
+        const int x = p % J.width, y = p / J.width;
+        const int sample = ch.first_sample + s;
+        const wf_camera& cam = J.camera;
+        const V3 org = {cam.origin[0], cam.origin[1], cam.origin[2]};
+        const V3 tl = {cam.top_left[0], cam.top_left[1], cam.top_left[2]};
+        const V3 hz = {cam.horizontal[0], cam.horizontal[1], cam.horizontal[2]};
+        const V3 vt = {cam.vertical[0], cam.vertical[1], cam.vertical[2]};
+        Stream rng(J.seed_lo, J.seed_hi, kPurposeCamera, 0, (uint32_t)p, (uint32_t)sample);
+        float u = ((float)x + rng.next()) / (float)(J.width - 1);
+        float v = 1.0f - ((float)y + rng.next()) / (float)(J.height - 1);
+        V3 d = normalized(tl + hz * u + vt * v - org);
+        rq.ox[i] = org.x;
+        rq.oy[i] = org.y;
+        rq.oz[i] = org.z;
+        rq.dx[i] = d.x;
+        rq.dy[i] = d.y;
+        rq.dz[i] = d.z;
+        rq.tr[i] = 1.0f;
+        rq.tg[i] = 1.0f;
+        rq.tb[i] = 1.0f;
+        rq.pdf[i] = -1.0f;
+        rq.pixel[i] = p;
+        rq.depth[i] = 0;
+        rq.sample[i] = sample;
+        rq.job[i] = ch.job;
+    }
+}
+
+// Per-bounce counters accumulated on the device (so a captured bounce chain
+// needs no host round trip): tally[0] += rays, [1] += hits, [2] += shadow rays.
+__global__ void k_tally(const ull* __restrict__ counters, ull* tally)
+{
+    tally[0] += counters[0];
+    tally[1] += counters[1];
+    tally[2] += counters[2];
+    tally[3] += counters[0] ? 1ull : 0ull;
 }
 
 // ---------------------------------------------------------------------------
@@ -134,16 +193,19 @@ __device__ __forceinline__ void accum_add(float* accum, int pixel, V3 c)
 // new ray from a global counter, so a warp is not held by its slowest ray.
 // ---------------------------------------------------------------------------
 template <int kMinBlocks>
-__global__ void __launch_bounds__(128, kMinBlocks) k_trace_render(DeviceScene S, RayQueueDev rq,
-                                                      const ull* __restrict__ d_n,
-                                                      HitQueueDev hq, ull* hq_n, float* accum,
-                                                      ull* work, int* err)
+__global__ void __launch_bounds__(128, kMinBlocks) k_trace_render(const DeviceScene* __restrict__ scenes,
+                                                                  const DeviceJob* __restrict__ jobs,
+                                                                  RayQueueDev rq, const ull* __restrict__ d_n,
+                                                                  HitQueueDev hq, ull* hq_n, float* accum,
+                                                                  ull* work, int* err)
 {
     const int64_t n = (int64_t)*d_n;
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     Traversal<false> tr;
     uint32_t stack[kStackSize];
+    const DeviceScene* S = scenes;
+    int job = 0;
     int64_t ray = -1;
     bool exhausted = false;
     bool overflow = false;
@@ -173,7 +235,7 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_trace_render(DeviceScene S,
         }
         if (fin && !hit) {
             const V3 T = {rq.tr[ray], rq.tg[ray], rq.tb[ray]};
-            accum_add(accum, rq.pixel[ray], T * sky_color(S, tr.d));
+            accum_add(accum + jobs[job].accum_offset, rq.pixel[ray], T * sky_color(*S, tr.d));
         }
         if (fin) {
             overflow = overflow || tr.overflow;
@@ -191,7 +253,9 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_trace_render(DeviceScene S,
                 const int64_t idx = (int64_t)base + __popc(nm & lt);
                 if (idx < n) {
                     ray = idx;
-                    tr.init(S, stack, v3(rq.ox[idx], rq.oy[idx], rq.oz[idx]),
+                    job = rq.job[idx];
+                    S = scenes + jobs[job].scene;
+                    tr.init(*S, stack, v3(rq.ox[idx], rq.oy[idx], rq.oz[idx]),
                             v3(rq.dx[idx], rq.dy[idx], rq.dz[idx]), 0.001f, 1e9f);
                 } else {
                     exhausted = true;
@@ -200,7 +264,7 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_trace_render(DeviceScene S,
         }
         if (__all_sync(0xFFFFFFFFu, ray < 0)) break;
         // 3. one traversal round
-        if (ray >= 0 && !tr.done()) tr.round(S, stack);
+        if (ray >= 0 && !tr.done()) tr.round(stack);
     }
     if (overflow) atomicOr(err, 1);
 }
@@ -212,13 +276,13 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_trace_render(DeviceScene S,
 // roulette and the next ray.  Random streams per (purpose, depth, pixel,
 // sample) — the oracle uses the same ones.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) k_shade(DeviceScene S, ShadeParams P, RayQueueDev rq,
+__global__ void __launch_bounds__(128) k_shade(const DeviceScene* __restrict__ scenes,
+                                               const DeviceJob* __restrict__ jobs, RayQueueDev rq,
                                                HitQueueDev hq, const ull* __restrict__ hq_n,
                                                ShadowQueueDev sh, ull* sh_n, RayQueueDev nx,
-                                               ull* nx_n, float* accum, int* err)
+                                               ull* nx_n, float* accum_base, int* err)
 {
     const int64_t n = (int64_t)*hq_n;
-    const float ff = P.firefly;
     WF_BLOCK_LOOP(base, n)
     {
         const int64_t k = base + threadIdx.x;
@@ -227,9 +291,15 @@ __global__ void __launch_bounds__(128) k_shade(DeviceScene S, ShadeParams P, Ray
         V3 p = {0, 0, 0}, dir_area = {0, 0, 0}, c_area = {0, 0, 0}, dir_sun = {0, 0, 0},
            c_sun = {0, 0, 0}, nd = {0, 0, 0}, Tn = {0, 0, 0};
         float dist_area = 0.0f, next_pdf = 0.0f;
-        int pixel = 0, depth = 0, sample = 0;
+        int pixel = 0, depth = 0, sample = 0, job = 0;
         if (active) {
             const int ri = hq.ray[k];
+            job = rq.job[ri];
+            const DeviceJob& J = jobs[job];
+            const DeviceScene& S = scenes[J.scene];
+            float* accum = accum_base + J.accum_offset;
+            const float ff = J.firefly;
+            const uint32_t seed_lo = J.seed_lo, seed_hi = J.seed_hi;
             const V3 o = {rq.ox[ri], rq.oy[ri], rq.oz[ri]};
             const V3 d = {rq.dx[ri], rq.dy[ri], rq.dz[ri]};
             const V3 T = {rq.tr[ri], rq.tg[ri], rq.tb[ri]};
@@ -260,7 +330,7 @@ __global__ void __launch_bounds__(128) k_shade(DeviceScene S, ShadeParams P, Ray
             // Area-light NEE (.cpp:660-710)
             if ((m.type == WF_MATERIAL_DIFFUSE || m.type == WF_MATERIAL_PLASTIC) &&
                 S.num_emissive_meshes > 0) {
-                Stream lr(P.seed_lo, P.seed_hi, kPurposeLight, (uint32_t)depth, (uint32_t)pixel,
+                Stream lr(seed_lo, seed_hi, kPurposeLight, (uint32_t)depth, (uint32_t)pixel,
                           (uint32_t)sample);
                 const int ne = S.num_emissive_meshes;
                 const EmissiveMesh em = S.emissive_meshes[(int)(lr.next() * (float)ne) % ne];
@@ -318,27 +388,28 @@ __global__ void __launch_bounds__(128) k_shade(DeviceScene S, ShadeParams P, Ray
                 }
             }
             // Scatter + Russian roulette (.cpp:739-796)
-            Stream sr(P.seed_lo, P.seed_hi, kPurposeScatter, (uint32_t)depth, (uint32_t)pixel,
+            Stream sr(seed_lo, seed_hi, kPurposeScatter, (uint32_t)depth, (uint32_t)pixel,
                       (uint32_t)sample);
             V3 att;
             float spdf;
             if (scatter(S, m, d, h, sr, att, nd, spdf)) {
                 Tn = T * att;
                 bool alive = true;
-                if (depth + 1 >= P.rr_min_depth) {
+                if (depth + 1 >= J.rr_min_depth) {
                     float q = fminf(0.95f, fmaxf(Tn.x, fmaxf(Tn.y, Tn.z)));
-                    if (P.cost_aware_rr) {
-                        float rc = P.rel_cost_material ? P.rel_cost_material[h.mat] : 1.0f;
+                    if (J.cost_aware_rr) {
+                        float rc = J.rel_cost_material ? J.rel_cost_material[h.mat] : 1.0f;
                         q = fminf(fmaxf(q / rc, 0.05f), 0.95f);
                     }
-                    Stream rr(P.seed_lo, P.seed_hi, kPurposeRoulette, (uint32_t)depth,
+                    Stream rr(seed_lo, seed_hi, kPurposeRoulette, (uint32_t)depth,
                               (uint32_t)pixel, (uint32_t)sample);
                     if (rr.next() > q)
                         alive = false;
                     else
                         Tn = Tn / q;
                 }
-                if (alive) {
+                // the reference traces depths 0 .. maxDepth-1 (.cpp:154)
+                if (alive && depth + 1 < J.max_depth) {
                     want_next = true;
                     next_pdf = spdf;
                 }
@@ -353,6 +424,7 @@ __global__ void __launch_bounds__(128) k_shade(DeviceScene S, ShadeParams P, Ray
                 sh.dist[pa] = dist_area;
                 sh.cr[pa] = c_area.x; sh.cg[pa] = c_area.y; sh.cb[pa] = c_area.z;
                 sh.pixel[pa] = pixel;
+                sh.job[pa] = job;
             } else {
                 atomicOr(err, 4);
             }
@@ -366,6 +438,7 @@ __global__ void __launch_bounds__(128) k_shade(DeviceScene S, ShadeParams P, Ray
                 sh.dist[pd] = 1e6f;
                 sh.cr[pd] = c_sun.x; sh.cg[pd] = c_sun.y; sh.cb[pd] = c_sun.z;
                 sh.pixel[pd] = pixel;
+                sh.job[pd] = job;
             } else {
                 atomicOr(err, 4);
             }
@@ -381,6 +454,7 @@ __global__ void __launch_bounds__(128) k_shade(DeviceScene S, ShadeParams P, Ray
                 nx.pixel[pn] = pixel;
                 nx.depth[pn] = depth + 1;
                 nx.sample[pn] = sample;
+                nx.job[pn] = job;
             } else {
                 atomicOr(err, 8);
             }
@@ -392,22 +466,27 @@ __global__ void __launch_bounds__(128) k_shade(DeviceScene S, ShadeParams P, Ray
 // added to their pixel.  Same persistent, dynamic-fetch structure as
 // k_trace_render.
 template <int kMinBlocks>
-__global__ void __launch_bounds__(128, kMinBlocks) k_occluded_render(DeviceScene S, ShadowQueueDev sh,
-                                                         const ull* __restrict__ d_n,
-                                                         float* accum, ull* work, int* err)
+__global__ void __launch_bounds__(128, kMinBlocks) k_occluded_render(const DeviceScene* __restrict__ scenes,
+                                                                     const DeviceJob* __restrict__ jobs,
+                                                                     ShadowQueueDev sh,
+                                                                     const ull* __restrict__ d_n,
+                                                                     float* accum, ull* work, int* err)
 {
     const int64_t n = (int64_t)*d_n;
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     Traversal<true> tr;
     uint32_t stack[kStackSize];
+    const DeviceScene* S = scenes;
+    int job = 0;
     int64_t ray = -1;
     bool exhausted = false;
     bool overflow = false;
     tr.cur = kSentinel;
     for (;;) {
         if (ray >= 0 && tr.done()) {
-            if (tr.res.leafpos < 0) accum_add(accum, sh.pixel[ray], v3(sh.cr[ray], sh.cg[ray], sh.cb[ray]));
+            if (tr.res.leafpos < 0)
+                accum_add(accum + jobs[job].accum_offset, sh.pixel[ray], v3(sh.cr[ray], sh.cg[ray], sh.cb[ray]));
             overflow = overflow || tr.overflow;
             ray = -1;
         }
@@ -422,7 +501,9 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_occluded_render(DeviceScene
                 const int64_t idx = (int64_t)base + __popc(nm & lt);
                 if (idx < n) {
                     ray = idx;
-                    tr.init(S, stack, v3(sh.ox[idx], sh.oy[idx], sh.oz[idx]),
+                    job = sh.job[idx];
+                    S = scenes + jobs[job].scene;
+                    tr.init(*S, stack, v3(sh.ox[idx], sh.oy[idx], sh.oz[idx]),
                             v3(sh.dx[idx], sh.dy[idx], sh.dz[idx]), 0.001f, sh.dist[idx] - 0.001f);
                 } else {
                     exhausted = true;
@@ -430,7 +511,7 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_occluded_render(DeviceScene
             }
         }
         if (__all_sync(0xFFFFFFFFu, ray < 0)) break;
-        if (ray >= 0 && !tr.done()) tr.round(S, stack);
+        if (ray >= 0 && !tr.done()) tr.round(stack);
     }
     if (overflow) atomicOr(err, 1);
 }
@@ -464,12 +545,18 @@ __device__ __forceinline__ uint64_t ray_key(float ox, float oy, float oz, float 
     return (oct << 30) | m;
 }
 
-__global__ void k_ray_keys(RayQueueDev rq, const ull* __restrict__ d_n, float3 mn, float3 ex,
-                           uint64_t* keys, uint32_t* vals)
+// Scene bounds of each ray's own scene (Scene::computeBounds), extent
+// floored at 1e-6 (RayQueue.h:143-145).
+__global__ void k_ray_keys(const DeviceScene* __restrict__ scenes, const DeviceJob* __restrict__ jobs,
+                           RayQueueDev rq, const ull* __restrict__ d_n, uint64_t* keys, uint32_t* vals)
 {
     const int64_t n = (int64_t)*d_n;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x) {
+        const DeviceScene& S = scenes[jobs[rq.job[i]].scene];
+        const float3 mn = make_float3(S.bmin[0], S.bmin[1], S.bmin[2]);
+        const float3 ex = make_float3(fmaxf(S.bmax[0] - S.bmin[0], 1e-6f), fmaxf(S.bmax[1] - S.bmin[1], 1e-6f),
+                                      fmaxf(S.bmax[2] - S.bmin[2], 1e-6f));
         keys[i] = ray_key(rq.ox[i], rq.oy[i], rq.oz[i], rq.dx[i], rq.dy[i], rq.dz[i], mn, ex);
         vals[i] = (uint32_t)i;
     }
@@ -506,6 +593,7 @@ __global__ void k_gather_rays(RayQueueDev in, const uint32_t* __restrict__ perm,
         out.pixel[i] = in.pixel[j];
         out.depth[i] = in.depth[j];
         out.sample[i] = in.sample[j];
+        out.job[i] = in.job[j];
     }
 }
 
@@ -650,13 +738,15 @@ __global__ void k_cb_keys(ShadeColumnsDev c, const ull* __restrict__ d_n,
     }
 }
 
-__global__ void k_hit_columns(DeviceScene S, RayQueueDev rq, HitQueueDev hq,
-                              const ull* __restrict__ d_n, ShadeColumnsMut out)
+__global__ void k_hit_columns(const DeviceScene* __restrict__ scenes, const DeviceJob* __restrict__ jobs,
+                              RayQueueDev rq, HitQueueDev hq, const ull* __restrict__ d_n,
+                              ShadeColumnsMut out)
 {
     const int64_t n = (int64_t)*d_n;
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
          k += (int64_t)gridDim.x * blockDim.x) {
         const int ri = hq.ray[k];
+        const DeviceScene& S = scenes[jobs[rq.job[ri]].scene];
         const float4 b = __ldg(S.tris + 3 * (int64_t)hq.tri[k] + 1);
         const int m = S.mesh_material[__float_as_int(b.w)];
         out.mat[k] = m;
@@ -729,43 +819,48 @@ void launch_occluded_api(const DeviceScene& S, int64_t n, const float* ox, const
 
 // variant: 0 = no occupancy hint (~56 registers), 1 = 10 blocks of 128 per SM
 // (48 registers), 2 = 12 blocks (40 registers, small spills).
-void launch_trace_render(const DeviceScene& S, RayQueueDev rq, const ull* d_n, HitQueueDev hq,
-                         ull* hq_n, float* accum, ull* work, int* err, LaunchCfg cfg,
+void launch_trace_render(const DeviceScene* scenes, const DeviceJob* jobs, RayQueueDev rq, const ull* d_n,
+                         HitQueueDev hq, ull* hq_n, float* accum, ull* work, int* err, LaunchCfg cfg,
                          cudaStream_t s)
 {
     if (cfg.variant == 1)
-        k_trace_render<10><<<cfg.grid, 128, 0, s>>>(S, rq, d_n, hq, hq_n, accum, work, err);
+        k_trace_render<10><<<cfg.grid, 128, 0, s>>>(scenes, jobs, rq, d_n, hq, hq_n, accum, work, err);
     else if (cfg.variant == 2)
-        k_trace_render<12><<<cfg.grid, 128, 0, s>>>(S, rq, d_n, hq, hq_n, accum, work, err);
+        k_trace_render<12><<<cfg.grid, 128, 0, s>>>(scenes, jobs, rq, d_n, hq, hq_n, accum, work, err);
     else
-        k_trace_render<1><<<cfg.grid, 128, 0, s>>>(S, rq, d_n, hq, hq_n, accum, work, err);
+        k_trace_render<1><<<cfg.grid, 128, 0, s>>>(scenes, jobs, rq, d_n, hq, hq_n, accum, work, err);
 }
 
-void launch_shade(const DeviceScene& S, const ShadeParams& P, RayQueueDev rq, HitQueueDev hq,
+void launch_camera_chunks(const WaveChunk* chunks, const long long* header, const DeviceJob* jobs, RayQueueDev rq,
+                          LaunchCfg cfg, cudaStream_t s)
+{
+    k_camera_chunks<<<cfg.grid, 256, 0, s>>>(chunks, header, jobs, rq);
+}
+
+void launch_tally(const ull* counters, ull* tally, cudaStream_t s) { k_tally<<<1, 1, 0, s>>>(counters, tally); }
+
+void launch_shade(const DeviceScene* scenes, const DeviceJob* jobs, RayQueueDev rq, HitQueueDev hq,
                   const ull* hq_n, ShadowQueueDev sh, ull* sh_n, RayQueueDev next, ull* next_n,
                   float* accum, int* err, LaunchCfg cfg, cudaStream_t s)
 {
-    k_shade<<<cfg.grid, 128, 0, s>>>(S, P, rq, hq, hq_n, sh, sh_n, next, next_n, accum, err);
+    k_shade<<<cfg.grid, 128, 0, s>>>(scenes, jobs, rq, hq, hq_n, sh, sh_n, next, next_n, accum, err);
 }
 
-void launch_occluded_render(const DeviceScene& S, ShadowQueueDev sh, const ull* sh_n, float* accum,
-                            ull* work, int* err, LaunchCfg cfg, cudaStream_t s)
+void launch_occluded_render(const DeviceScene* scenes, const DeviceJob* jobs, ShadowQueueDev sh,
+                            const ull* sh_n, float* accum, ull* work, int* err, LaunchCfg cfg, cudaStream_t s)
 {
     if (cfg.variant == 1)
-        k_occluded_render<10><<<cfg.grid, 128, 0, s>>>(S, sh, sh_n, accum, work, err);
+        k_occluded_render<10><<<cfg.grid, 128, 0, s>>>(scenes, jobs, sh, sh_n, accum, work, err);
     else if (cfg.variant == 2)
-        k_occluded_render<12><<<cfg.grid, 128, 0, s>>>(S, sh, sh_n, accum, work, err);
+        k_occluded_render<12><<<cfg.grid, 128, 0, s>>>(scenes, jobs, sh, sh_n, accum, work, err);
     else
-        k_occluded_render<1><<<cfg.grid, 128, 0, s>>>(S, sh, sh_n, accum, work, err);
+        k_occluded_render<1><<<cfg.grid, 128, 0, s>>>(scenes, jobs, sh, sh_n, accum, work, err);
 }
 
-void launch_ray_keys(RayQueueDev rq, const ull* d_n, const float bmin[3], const float bmax[3],
+void launch_ray_keys(const DeviceScene* scenes, const DeviceJob* jobs, RayQueueDev rq, const ull* d_n,
                      uint64_t* keys, uint32_t* vals, LaunchCfg cfg, cudaStream_t s)
 {
-    float3 mn = make_float3(bmin[0], bmin[1], bmin[2]);
-    float3 ex = make_float3(fmaxf(bmax[0] - bmin[0], 1e-6f), fmaxf(bmax[1] - bmin[1], 1e-6f),
-                            fmaxf(bmax[2] - bmin[2], 1e-6f));
-    k_ray_keys<<<cfg.grid, 256, 0, s>>>(rq, d_n, mn, ex, keys, vals);
+    k_ray_keys<<<cfg.grid, 256, 0, s>>>(scenes, jobs, rq, d_n, keys, vals);
 }
 
 void launch_ray_keys_raw(int64_t n, const float* ox, const float* oy, const float* oz,
@@ -817,10 +912,10 @@ void launch_cb_keys(ShadeColumnsDev c, const ull* d_n, const wf_material* mats,
     k_cb_keys<<<cfg.grid, 256, 0, s>>>(c, d_n, mats, prio_rank, prio_bits, bounds6, keys, vals);
 }
 
-void launch_hit_columns(const DeviceScene& S, RayQueueDev rq, HitQueueDev hq, const ull* d_n,
-                        ShadeColumnsMut out, LaunchCfg cfg, cudaStream_t s)
+void launch_hit_columns(const DeviceScene* scenes, const DeviceJob* jobs, RayQueueDev rq, HitQueueDev hq,
+                        const ull* d_n, ShadeColumnsMut out, LaunchCfg cfg, cudaStream_t s)
 {
-    k_hit_columns<<<cfg.grid, 256, 0, s>>>(S, rq, hq, d_n, out);
+    k_hit_columns<<<cfg.grid, 256, 0, s>>>(scenes, jobs, rq, hq, d_n, out);
 }
 
 void launch_permute_hits(HitQueueDev in, const uint32_t* perm, const ull* d_n, HitQueueDev out,

@@ -303,6 +303,37 @@ void build_config1(wf_host_scene& s, uint64_t seed, int subdiv)
     set_camera(s);
 }
 
+// Config 3 job scenes: seeded variants of config 0 — wall, box and metal
+// albedos, metal roughness, the light quad's position on the ceiling and a
+// jitter of the camera position.
+void build_config3(wf_host_scene& s, uint64_t seed)
+{
+    uint64_t rs = seed * 0x9E3779B97F4A7C15ull + 12345u;
+    auto u = [&](float lo, float hi) { return lo + (hi - lo) * uniform01(rs); };
+    const float g = u(0.5f, 0.85f);
+    s.mats.push_back(diffuse(g, g, g));                                  // 0 white
+    s.mats.push_back(diffuse(u(0.5f, 0.8f), u(0.02f, 0.1f), u(0.02f, 0.1f)));  // 1 red
+    s.mats.push_back(diffuse(u(0.05f, 0.2f), u(0.3f, 0.6f), u(0.05f, 0.2f)));  // 2 green
+    s.mats.push_back(emissive(17.0f, 12.0f, 4.0f, 1.0f));               // 3 light
+    s.mats.push_back(metal(u(0.6f, 0.95f), u(0.6f, 0.95f), u(0.6f, 0.95f), u(0.1f, 0.5f)));  // 4 metal box
+    const float b = u(0.4f, 0.9f);
+    s.mats.push_back(diffuse(b, b, b));                                  // 5 short box
+    const float X = 0.275f, Y = 0.55f, Z = -0.55f;
+    add_quad(s, 0, {-X, 0, 0}, {X, 0, 0}, {X, 0, Z}, {-X, 0, Z});
+    add_quad(s, 0, {-X, Y, Z}, {X, Y, Z}, {X, Y, 0}, {-X, Y, 0});
+    add_quad(s, 0, {-X, 0, Z}, {X, 0, Z}, {X, Y, Z}, {-X, Y, Z});
+    add_quad(s, 1, {-X, 0, 0}, {-X, 0, Z}, {-X, Y, Z}, {-X, Y, 0});
+    add_quad(s, 2, {X, 0, Z}, {X, 0, 0}, {X, Y, 0}, {X, Y, Z});
+    const float cx = u(-0.12f, 0.12f), cz = u(-0.42f, -0.13f), ly = Y - 0.001f;
+    add_quad(s, 3, {cx - 0.065f, ly, cz - 0.055f}, {cx + 0.065f, ly, cz - 0.055f}, {cx + 0.065f, ly, cz + 0.055f},
+             {cx - 0.065f, ly, cz + 0.055f});
+    add_box(s, 4, {-0.19f, 0.0f, -0.42f}, {-0.025f, 0.33f, -0.255f}, 0.96592583f, 0.25881905f);
+    add_box(s, 5, {0.0325f, 0.0f, -0.2225f}, {0.1975f, 0.165f, -0.0575f}, 0.95105652f, -0.30901699f);
+    set_camera(s);
+    s.look_from[0] += u(-0.03f, 0.03f);
+    s.look_from[1] += u(-0.03f, 0.03f);
+}
+
 }  // namespace
 
 extern "C" {
@@ -319,6 +350,9 @@ int wf_host_scene_generate(int32_t config, uint64_t seed, wf_host_scene** out)
         break;
     case 1:
         build_config1(*s, seed, 8);
+        break;
+    case 3:  // a job scene of the batched workload: variant `seed` of config 0
+        build_config3(*s, seed);
         break;
     case 100:  // small variant of config 1 (subdivision 4) for fast tests
         build_config1(*s, seed, 4);

@@ -63,6 +63,8 @@ constexpr uint32_t kSentinel = 0xFFFFFFFFu;
 template <bool kAnyHit>
 struct Traversal {
     V3 o, d, inv, oi;
+    const BvhNode* nodes;  // the ray's scene, kept in registers
+    const float4* tris;
     float tmin, best_t;
     int best_g;
     uint32_t cur;
@@ -77,6 +79,8 @@ struct Traversal {
     {
         o = o_;
         d = d_;
+        nodes = S.nodes;
+        tris = S.tris;
         inv = v3(safe_inv(d.x), safe_inv(d.y), safe_inv(d.z));
         oi = v3(o.x * inv.x, o.y * inv.y, o.z * inv.z);
         tmin = tmin_;
@@ -90,10 +94,10 @@ struct Traversal {
     }
     __device__ __forceinline__ bool done() const { return cur == kSentinel; }
 
-    __device__ __forceinline__ void round(const DeviceScene& S, uint32_t* stack)
+    __device__ __forceinline__ void round(uint32_t* stack)
     {
         while (!(cur & kLeafFlag)) {
-            const BvhNode nd = load_node(S.nodes, cur);
+            const BvhNode nd = load_node(nodes, cur);
             float tn0, tn1;
             bool h0, h1;
             slab2(nd, inv, oi, tmin, best_t, tn0, tn1, h0, h1);
@@ -119,9 +123,9 @@ struct Traversal {
             bool stop = false;
             for (int k = 0; k < cnt; ++k) {
                 const int lp = first + k;
-                const float4 a = __ldg(S.tris + 3 * lp + 0);
-                const float4 b = __ldg(S.tris + 3 * lp + 1);
-                const float4 c = __ldg(S.tris + 3 * lp + 2);
+                const float4 a = __ldg(tris + 3 * lp + 0);
+                const float4 b = __ldg(tris + 3 * lp + 1);
+                const float4 c = __ldg(tris + 3 * lp + 2);
                 float th, uh, vh;
                 if (intersect_triangle(o, d, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), v3(c.x, c.y, c.z), tmin,
                                        best_t, th, uh, vh)) {
@@ -152,7 +156,7 @@ __device__ __forceinline__ bool traverse(const DeviceScene& S, V3 o, V3 d, float
     Traversal<kAnyHit> tr;
     uint32_t stack[kStackSize];
     tr.init(S, stack, o, d, tmin, tmax);
-    while (!tr.done()) tr.round(S, stack);
+    while (!tr.done()) tr.round(stack);
     res = tr.res;
     if (tr.overflow) atomicOr(err_flag, 1);
     return !tr.overflow;
