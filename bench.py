@@ -224,13 +224,152 @@ def run_reference(args, wl):
     return 0
 
 
+def percentile(xs, q):
+    return float(np.percentile(np.asarray(xs, dtype=np.float64), q)) if len(xs) else None
+
+
+def c3_jobs(pkg, ctx, n, seed):
+    """Config 3: n seeded variants of the Cornell box, each its own resident
+    scene, resolution from {64^2, 128^2, 256^2}, spp from {4, 16, 64}, depth 8."""
+    rng = np.random.default_rng(seed)
+    jobs = []
+    for k in range(n):
+        hs = pkg.HostScene(3, seed=k)
+        sid = ctx.add_scene(hs.desc)
+        res = int(rng.choice([64, 128, 256]))
+        spp = int(rng.choice([4, 16, 64]))
+        jobs.append(pkg.make_job(sid, res, res, spp, 8, hs.camera(res, res), seed=10_000 + k))
+    return jobs
+
+
+def run_batched(args) -> int:
+    """Batched small renders (config 3): all jobs' rays share waves, the
+    bounce chain replays a captured CUDA graph; against the plain loop (each
+    job rendered alone, one host round trip per bounce)."""
+    world, rank, local, dist = dist_init()
+    pkg = load_pkg()
+    ctx = pkg.Context(local)
+    jobs = c3_jobs(pkg, ctx, args.jobs, seed=2026)
+    ctx.set_tuning(graph_mode=0)
+    ctx.render_batch(jobs[:16], want_images=False)  # warm-up (captures the graph)
+    ctx.set_tuning(graph_mode=2)
+    ctx.render_batch(jobs[:4], want_images=False)
+    # plain loop: one job per render, host round trip per bounce
+    ctx.set_tuning(graph_mode=2)
+    ctx.timer_begin()
+    plain_rays = 0
+    for j in jobs:
+        _, st = ctx.render_batch([j], want_images=False)
+        plain_rays += st["closest_rays"] + st["shadow_rays"]
+    plain_ms = ctx.timer_end()
+    # batched: one call, waves shared by all jobs, graph replay
+    ctx.set_tuning(graph_mode=0)
+    ctx.timer_begin()
+    _, st = ctx.render_batch(jobs, want_images=False)
+    ms = ctx.timer_end()
+    rays = st["closest_rays"] + st["shadow_rays"]
+    value = rays / ms / 1e3
+    plain = plain_rays / plain_ms / 1e3
+    paths = sum(j.width * j.height * j.samples_per_pixel for j in jobs)
+    line = {
+        "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": 1, "warmup": 1,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": f"c3_batched_{len(jobs)}_jobs_cornell_variants_depth8", "paths": paths,
+                   "form": "batched waves + CUDA graph bounce chain"},
+        "plain_loop": {"value": plain, "unit": "Mrays/s", "ms": plain_ms, "form": "one job per render"},
+        "speedup_vs_plain_loop": value / plain,
+        "samples_per_s": paths / (ms / 1e3), "waves": st["waves"], "gpu_launches": st["kernel_launches"],
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_serving(args) -> int:
+    """Serving workload (config 4): Poisson arrivals over resident scenes of
+    configs 0, 1 and 3; admission by an HBM budget; progressive frames every
+    8 spp.  Reports Mrays/s and p50/p99 time-to-first-frame / to-complete."""
+    world, rank, local, dist = dist_init()
+    pkg = load_pkg()
+    ctx = pkg.Context(local)
+    rng = np.random.default_rng(4242)
+    scenes = []
+    for cfg in (0, 1):
+        hs = pkg.HostScene(cfg)
+        scenes.append((ctx.add_scene(hs.desc), hs))
+    for k in range(16):
+        hs = pkg.HostScene(3, seed=k)
+        scenes.append((ctx.add_scene(hs.desc), hs))
+    srv = pkg.Server(ctx, hbm_budget_bytes=int(args.budget_gb * (1 << 30)), frame_spp=8)
+    # warm-up: one small job per scene kind
+    for sid, hs in scenes[:3]:
+        srv.submit(pkg.make_job(sid, 64, 64, 8, 8, hs.camera(64, 64), seed=1))
+    for _ in range(10):
+        if srv.step()["running"] == 0:
+            break
+    t_end = args.duration
+    lam = args.rate
+    arrivals = []
+    t = 0.0
+    while t < t_end:
+        t += rng.exponential(1.0 / lam)
+        side = int(round(np.exp(rng.uniform(np.log(128), np.log(1024)))))
+        spp = int(rng.choice([8, 32, 128]))
+        depth = int(rng.integers(4, 13))
+        kind = int(rng.integers(0, 3))
+        sid, hs = scenes[kind] if kind < 2 else scenes[2 + int(rng.integers(0, 16))]
+        arrivals.append((t, pkg.make_job(sid, side, side, spp, depth, hs.camera(side, side),
+                                         seed=int(rng.integers(1, 2**31)))))
+    ids = []
+    rays, dev_ms = 0, 0.0
+    base = srv.clock()
+    k = 0
+    while True:
+        now = srv.clock() - base
+        while k < len(arrivals) and arrivals[k][0] <= now:
+            ids.append(srv.submit(arrivals[k][1]))
+            k += 1
+        if now > t_end:
+            break
+        info = srv.step()
+        rays += info["rays_traced"]
+        dev_ms += info["step_ms"]
+    wall = srv.clock() - base
+    st = [srv.status(i) for i in ids]
+    ttff = [s["t_first_frame"] - s["t_submit"] for s in st if s["t_first_frame"] >= 0]
+    ttc = [s["t_done"] - s["t_submit"] for s in st if s["state"] == pkg.JOB_DONE]
+    line = {
+        "metric": METRIC, "value": rays / wall / 1e6, "unit": "Mrays/s", "n_gpus": world, "steps": 1,
+        "warmup": 1, "ms_per_step": wall * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "c4_serving_poisson", "rate_per_s": lam, "duration_s": t_end,
+                   "hbm_budget_gb": args.budget_gb, "frame_spp": 8,
+                   "scenes": "config 0, config 1 (1.31 M tris), 16 config-3 variants"},
+        "device_busy_mrays_per_s": rays / (dev_ms / 1e3) / 1e6 if dev_ms else None,
+        "submitted": len(ids), "completed": len(ttc), "with_first_frame": len(ttff),
+        "rejected": sum(1 for s in st if s["state"] == pkg.JOB_REJECTED),
+        "queued_at_end": sum(1 for s in st if s["state"] == pkg.JOB_QUEUED),
+        "ttff_s": {"p50": percentile(ttff, 50), "p99": percentile(ttff, 99)},
+        "ttc_s": {"p50": percentile(ttc, 50), "p99": percentile(ttc, 99)},
+    }
+    srv.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def main() -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="c1", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="c1", choices=sorted(WORKLOADS) + ["c3", "c4"])
+    ap.add_argument("--jobs", type=int, default=512, help="config 3: number of jobs")
+    ap.add_argument("--duration", type=float, default=20.0, help="config 4: seconds of arrivals")
+    ap.add_argument("--rate", type=float, default=200.0, help="config 4: arrivals per second")
+    ap.add_argument("--budget-gb", type=float, default=60.0, help="config 4: HBM budget")
     ap.add_argument("--policy", default="none", choices=["none", "material", "texture", "costBenefit"])
     ap.add_argument("--ray-sort", type=int, default=0)
     ap.add_argument("--spp-per-wave", type=int, default=0)
@@ -242,6 +381,10 @@ def main() -> int:
     ap.add_argument("--ref-spp", type=int, default=8)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 0)
+    if args.workload == "c3":
+        return run_batched(args)
+    if args.workload == "c4":
+        return run_serving(args)
     wl = dict(WORKLOADS[args.workload])
     if args.spp > 0:
         wl["spp"] = args.spp

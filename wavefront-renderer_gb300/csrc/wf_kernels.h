@@ -51,14 +51,21 @@ void launch_occluded_api(const DeviceScene& S, int64_t n, const float* ox, const
 // captured wave can be replayed for any job mix).
 void launch_camera_chunks(const WaveChunk* chunks, const long long* header, const DeviceJob* jobs, RayQueueDev rq,
                           LaunchCfg cfg, cudaStream_t s);
-void launch_trace_render(const DeviceScene* scenes, const DeviceJob* jobs, RayQueueDev rq, const ull* d_n,
-                         HitQueueDev hq, ull* hq_n, float* accum, ull* work, int* err, LaunchCfg cfg,
-                         cudaStream_t s);
-void launch_shade(const DeviceScene* scenes, const DeviceJob* jobs, RayQueueDev rq, HitQueueDev hq,
-                  const ull* hq_n, ShadowQueueDev sh, ull* sh_n, RayQueueDev next, ull* next_n,
-                  float* accum, int* err, LaunchCfg cfg, cudaStream_t s);
-void launch_occluded_render(const DeviceScene* scenes, const DeviceJob* jobs, ShadowQueueDev sh,
-                            const ull* sh_n, float* accum, ull* work, int* err, LaunchCfg cfg, cudaStream_t s);
+// The job and scene tables of a wave.  multi = false: a single job (job0 on
+// scene0, passed by value); true: rays look up their job and scene.
+struct WaveTables {
+    const DeviceScene* scenes;
+    const DeviceJob* jobs;
+    DeviceScene scene0;
+    DeviceJob job0;
+    bool multi;
+};
+void launch_trace_render(const WaveTables& t, RayQueueDev rq, const ull* d_n, HitQueueDev hq, ull* hq_n,
+                         float* accum, ull* work, int* err, LaunchCfg cfg, cudaStream_t s);
+void launch_shade(const WaveTables& t, RayQueueDev rq, HitQueueDev hq, const ull* hq_n, ShadowQueueDev sh,
+                  ull* sh_n, RayQueueDev next, ull* next_n, float* accum, int* err, LaunchCfg cfg, cudaStream_t s);
+void launch_occluded_render(const WaveTables& t, ShadowQueueDev sh, const ull* sh_n, float* accum, ull* work,
+                            int* err, LaunchCfg cfg, cudaStream_t s);
 // tally[0..3] += rays, hits, shadow rays, (rays > 0) of the bounce just run.
 void launch_tally(const ull* counters, ull* tally, cudaStream_t s);
 

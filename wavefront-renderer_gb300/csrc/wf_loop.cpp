@@ -99,9 +99,14 @@ int upload_wave(wf_ctx* c, const std::vector<WaveChunk>& chunks, int64_t total)
 // reference (RayQueue::schedule + ShadingQueue::schedule), materials of
 // scene `policy_scene`.
 int wave_host(wf_ctx* c, int64_t total, int max_depth, int policy, bool ray_sort, int policy_scene,
-              const double* rc_mat, const double* rc_tex, wf_render_stats& stats)
+              const double* rc_mat, const double* rc_tex, const DeviceJob* single_job, wf_render_stats& stats)
 {
     cudaStream_t s = c->stream;
+    WaveTables T{c->d_scene_table, c->d_jobs, DeviceScene{}, DeviceJob{}, single_job == nullptr};
+    if (single_job) {
+        T.job0 = *single_job;
+        T.scene0 = c->scenes[single_job->scene].S;
+    }
     const LaunchCfg PC = persist_cfg(c), WC = wide_cfg(c);
     cudaEvent_t* ev = c->ev;
     float ms = 0.0f;
@@ -130,8 +135,8 @@ int wave_host(wf_ctx* c, int64_t total, int max_depth, int policy, bool ray_sort
         }
         WF_CK(c, cudaMemsetAsync(c->counters + 1, 0, sizeof(ull) * 5, s));
         WF_CK(c, cudaEventRecord(ev[4], s));
-        launch_trace_render(c->d_scene_table, c->d_jobs, c->rq[cur], c->counters, c->hq[0], c->counters + 1,
-                            c->arena, c->counters + 4, c->err_flag, PC, s);
+        launch_trace_render(T, c->rq[cur], c->counters, c->hq[0], c->counters + 1, c->arena, c->counters + 4,
+                            c->err_flag, PC, s);
         WF_CK(c, cudaEventRecord(ev[5], s));
         HitQueueDev hq_use = c->hq[0];
         if (policy != WF_POLICY_NONE) {
@@ -152,10 +157,9 @@ int wave_host(wf_ctx* c, int64_t total, int max_depth, int policy, bool ray_sort
             stats.sorted_elements += hits;
         }
         WF_CK(c, cudaEventRecord(ev[6], s));
-        launch_shade(c->d_scene_table, c->d_jobs, c->rq[cur], hq_use, c->counters + 1, c->sh, c->counters + 2,
-                     c->rq[1 - cur], c->counters + 3, c->arena, c->err_flag, PC, s);
-        launch_occluded_render(c->d_scene_table, c->d_jobs, c->sh, c->counters + 2, c->arena, c->counters + 5,
-                               c->err_flag, PC, s);
+        launch_shade(T, c->rq[cur], hq_use, c->counters + 1, c->sh, c->counters + 2, c->rq[1 - cur], c->counters + 3,
+                     c->arena, c->err_flag, PC, s);
+        launch_occluded_render(T, c->sh, c->counters + 2, c->arena, c->counters + 5, c->err_flag, PC, s);
         stats.kernel_launches += 3;
         WF_CK(c, cudaEventRecord(ev[7], s));
         ull cnt[4];
@@ -189,6 +193,7 @@ int record_chain(wf_ctx* c, int max_depth, bool ray_sort)
     const LaunchCfg PC = persist_cfg(c), WC = wide_cfg(c);
     int kernels = 0;
     int cur = 0;
+    const WaveTables T{c->d_scene_table, c->d_jobs, DeviceScene{}, DeviceJob{}, true};
     launch_camera_chunks(c->d_chunks, c->d_wave_header, c->d_jobs, c->rq[cur], WC, s);
     cudaMemcpyAsync(c->counters, c->d_wave_header, sizeof(ull), cudaMemcpyDeviceToDevice, s);
     kernels += 1;
@@ -204,12 +209,11 @@ int record_chain(wf_ctx* c, int max_depth, bool ray_sort)
             cur = 1 - cur;
         }
         cudaMemsetAsync(c->counters + 1, 0, sizeof(ull) * 5, s);
-        launch_trace_render(c->d_scene_table, c->d_jobs, c->rq[cur], c->counters, c->hq[0], c->counters + 1, c->arena,
-                            c->counters + 4, c->err_flag, PC, s);
-        launch_shade(c->d_scene_table, c->d_jobs, c->rq[cur], c->hq[0], c->counters + 1, c->sh, c->counters + 2,
-                     c->rq[1 - cur], c->counters + 3, c->arena, c->err_flag, PC, s);
-        launch_occluded_render(c->d_scene_table, c->d_jobs, c->sh, c->counters + 2, c->arena, c->counters + 5,
-                               c->err_flag, PC, s);
+        launch_trace_render(T, c->rq[cur], c->counters, c->hq[0], c->counters + 1, c->arena, c->counters + 4,
+                            c->err_flag, PC, s);
+        launch_shade(T, c->rq[cur], c->hq[0], c->counters + 1, c->sh, c->counters + 2, c->rq[1 - cur], c->counters + 3,
+                     c->arena, c->err_flag, PC, s);
+        launch_occluded_render(T, c->sh, c->counters + 2, c->arena, c->counters + 5, c->err_flag, PC, s);
         launch_tally(c->counters, c->tally, s);
         cudaMemcpyAsync(c->counters, c->counters + 3, sizeof(ull), cudaMemcpyDeviceToDevice, s);
         kernels += 4;
@@ -338,7 +342,7 @@ int render_single(wf_ctx* c, const wf_render_params* P, wf_render_stats* st)
         if (rc) return rc;
         rc = graph ? wave_graph(c, P->max_depth, P->enable_ray_sort != 0, stats)
                    : wave_host(c, np * nspp, P->max_depth, P->policy, P->enable_ray_sort != 0, 0,
-                               P->rel_cost_material, P->rel_cost_texture, stats);
+                               P->rel_cost_material, P->rel_cost_texture, &table[0], stats);
         if (rc) return rc;
     }
     WF_CK(c, cudaEventRecord(c->ev[1], s));
@@ -593,7 +597,8 @@ int wf_render_batch(wf_ctx* c, const wf_job* jobs, int32_t njobs, float* const* 
         if (chunks.empty()) return set_err(c, WF_ERR_CAPACITY, "no job fits a wave");
         if ((rc = upload_wave(c, chunks, total))) return rc;
         rc = graph ? wave_graph(c, max_depth, false, stats)
-                   : wave_host(c, total, wave_depth, WF_POLICY_NONE, false, 0, nullptr, nullptr, stats);
+                   : wave_host(c, total, wave_depth, WF_POLICY_NONE, false, 0, nullptr, nullptr,
+                               njobs == 1 ? &table[0] : nullptr, stats);
         if (rc) return rc;
         while (next < njobs && done[next] >= jobs[next].samples_per_pixel) ++next;
     }
@@ -747,7 +752,7 @@ int wf_server_step(wf_server* sv, wf_server_step_info* info)
         WF_CK(c, cudaEventRecord(c->ev[0], s));
         const bool graph = use_graph(c, true, WF_POLICY_NONE);
         rc = graph ? wave_graph(c, depth, false, stats)
-                   : wave_host(c, total, depth, WF_POLICY_NONE, false, 0, nullptr, nullptr, stats);
+                   : wave_host(c, total, depth, WF_POLICY_NONE, false, 0, nullptr, nullptr, nullptr, stats);
         if (rc) return rc;
         WF_CK(c, cudaEventRecord(c->ev[1], s));
         WF_CK(c, cudaEventSynchronize(c->ev[1]));

@@ -192,8 +192,11 @@ __device__ __forceinline__ void accum_add(float* accum, int pixel, V3 c)
 // traversal rounds, lanes whose ray has finished emit its result and take a
 // new ray from a global counter, so a warp is not held by its slowest ray.
 // ---------------------------------------------------------------------------
-template <int kMinBlocks>
-__global__ void __launch_bounds__(128, kMinBlocks) k_trace_render(const DeviceScene* __restrict__ scenes,
+// kMulti = false: every ray belongs to job0 on scene0 (passed by value, read
+// from the constant bank); true: each ray looks its job and scene up.
+template <bool kMulti, int kMinBlocks>
+__global__ void __launch_bounds__(128, kMinBlocks) k_trace_render(DeviceScene scene0, DeviceJob job0,
+                                                                  const DeviceScene* __restrict__ scenes,
                                                                   const DeviceJob* __restrict__ jobs,
                                                                   RayQueueDev rq, const ull* __restrict__ d_n,
                                                                   HitQueueDev hq, ull* hq_n, float* accum,
@@ -204,7 +207,7 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_trace_render(const DeviceSc
     const unsigned lt = (1u << lane) - 1u;
     Traversal<false> tr;
     uint32_t stack[kStackSize];
-    const DeviceScene* S = scenes;
+    const DeviceScene* S = kMulti ? scenes : &scene0;
     int job = 0;
     int64_t ray = -1;
     bool exhausted = false;
@@ -235,7 +238,8 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_trace_render(const DeviceSc
         }
         if (fin && !hit) {
             const V3 T = {rq.tr[ray], rq.tg[ray], rq.tb[ray]};
-            accum_add(accum + jobs[job].accum_offset, rq.pixel[ray], T * sky_color(*S, tr.d));
+            const int64_t off = kMulti ? jobs[job].accum_offset : job0.accum_offset;
+            accum_add(accum + off, rq.pixel[ray], T * sky_color(*S, tr.d));
         }
         if (fin) {
             overflow = overflow || tr.overflow;
@@ -253,8 +257,10 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_trace_render(const DeviceSc
                 const int64_t idx = (int64_t)base + __popc(nm & lt);
                 if (idx < n) {
                     ray = idx;
-                    job = rq.job[idx];
-                    S = scenes + jobs[job].scene;
+                    if (kMulti) {
+                        job = rq.job[idx];
+                        S = scenes + jobs[job].scene;
+                    }
                     tr.init(*S, stack, v3(rq.ox[idx], rq.oy[idx], rq.oz[idx]),
                             v3(rq.dx[idx], rq.dy[idx], rq.dz[idx]), 0.001f, 1e9f);
                 } else {
@@ -264,7 +270,7 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_trace_render(const DeviceSc
         }
         if (__all_sync(0xFFFFFFFFu, ray < 0)) break;
         // 3. one traversal round
-        if (ray >= 0 && !tr.done()) tr.round(stack);
+        if (ray >= 0 && !tr.done()) tr.round(S->nodes, S->tris, stack);
     }
     if (overflow) atomicOr(err, 1);
 }
@@ -276,7 +282,9 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_trace_render(const DeviceSc
 // roulette and the next ray.  Random streams per (purpose, depth, pixel,
 // sample) — the oracle uses the same ones.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) k_shade(const DeviceScene* __restrict__ scenes,
+template <bool kMulti>
+__global__ void __launch_bounds__(128) k_shade(DeviceScene scene0, DeviceJob job0,
+                                               const DeviceScene* __restrict__ scenes,
                                                const DeviceJob* __restrict__ jobs, RayQueueDev rq,
                                                HitQueueDev hq, const ull* __restrict__ hq_n,
                                                ShadowQueueDev sh, ull* sh_n, RayQueueDev nx,
@@ -294,9 +302,9 @@ __global__ void __launch_bounds__(128) k_shade(const DeviceScene* __restrict__ s
         int pixel = 0, depth = 0, sample = 0, job = 0;
         if (active) {
             const int ri = hq.ray[k];
-            job = rq.job[ri];
-            const DeviceJob& J = jobs[job];
-            const DeviceScene& S = scenes[J.scene];
+            job = kMulti ? rq.job[ri] : 0;
+            const DeviceJob& J = kMulti ? jobs[job] : job0;
+            const DeviceScene& S = kMulti ? scenes[J.scene] : scene0;
             float* accum = accum_base + J.accum_offset;
             const float ff = J.firefly;
             const uint32_t seed_lo = J.seed_lo, seed_hi = J.seed_hi;
@@ -465,8 +473,9 @@ __global__ void __launch_bounds__(128) k_shade(const DeviceScene* __restrict__ s
 // Shadow rays (EmbreeAccelerator::occluded): unblocked contributions are
 // added to their pixel.  Same persistent, dynamic-fetch structure as
 // k_trace_render.
-template <int kMinBlocks>
-__global__ void __launch_bounds__(128, kMinBlocks) k_occluded_render(const DeviceScene* __restrict__ scenes,
+template <bool kMulti, int kMinBlocks>
+__global__ void __launch_bounds__(128, kMinBlocks) k_occluded_render(DeviceScene scene0, DeviceJob job0,
+                                                                     const DeviceScene* __restrict__ scenes,
                                                                      const DeviceJob* __restrict__ jobs,
                                                                      ShadowQueueDev sh,
                                                                      const ull* __restrict__ d_n,
@@ -477,7 +486,7 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_occluded_render(const Devic
     const unsigned lt = (1u << lane) - 1u;
     Traversal<true> tr;
     uint32_t stack[kStackSize];
-    const DeviceScene* S = scenes;
+    const DeviceScene* S = kMulti ? scenes : &scene0;
     int job = 0;
     int64_t ray = -1;
     bool exhausted = false;
@@ -485,8 +494,10 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_occluded_render(const Devic
     tr.cur = kSentinel;
     for (;;) {
         if (ray >= 0 && tr.done()) {
-            if (tr.res.leafpos < 0)
-                accum_add(accum + jobs[job].accum_offset, sh.pixel[ray], v3(sh.cr[ray], sh.cg[ray], sh.cb[ray]));
+            if (tr.res.leafpos < 0) {
+                const int64_t off = kMulti ? jobs[job].accum_offset : job0.accum_offset;
+                accum_add(accum + off, sh.pixel[ray], v3(sh.cr[ray], sh.cg[ray], sh.cb[ray]));
+            }
             overflow = overflow || tr.overflow;
             ray = -1;
         }
@@ -501,8 +512,10 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_occluded_render(const Devic
                 const int64_t idx = (int64_t)base + __popc(nm & lt);
                 if (idx < n) {
                     ray = idx;
-                    job = sh.job[idx];
-                    S = scenes + jobs[job].scene;
+                    if (kMulti) {
+                        job = sh.job[idx];
+                        S = scenes + jobs[job].scene;
+                    }
                     tr.init(*S, stack, v3(sh.ox[idx], sh.oy[idx], sh.oz[idx]),
                             v3(sh.dx[idx], sh.dy[idx], sh.dz[idx]), 0.001f, sh.dist[idx] - 0.001f);
                 } else {
@@ -511,7 +524,7 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_occluded_render(const Devic
             }
         }
         if (__all_sync(0xFFFFFFFFu, ray < 0)) break;
-        if (ray >= 0 && !tr.done()) tr.round(stack);
+        if (ray >= 0 && !tr.done()) tr.round(S->nodes, S->tris, stack);
     }
     if (overflow) atomicOr(err, 1);
 }
@@ -819,16 +832,17 @@ void launch_occluded_api(const DeviceScene& S, int64_t n, const float* ox, const
 
 // variant: 0 = no occupancy hint (~56 registers), 1 = 10 blocks of 128 per SM
 // (48 registers), 2 = 12 blocks (40 registers, small spills).
-void launch_trace_render(const DeviceScene* scenes, const DeviceJob* jobs, RayQueueDev rq, const ull* d_n,
-                         HitQueueDev hq, ull* hq_n, float* accum, ull* work, int* err, LaunchCfg cfg,
-                         cudaStream_t s)
+void launch_trace_render(const WaveTables& t, RayQueueDev rq, const ull* d_n, HitQueueDev hq, ull* hq_n,
+                         float* accum, ull* work, int* err, LaunchCfg cfg, cudaStream_t s)
 {
-    if (cfg.variant == 1)
-        k_trace_render<10><<<cfg.grid, 128, 0, s>>>(scenes, jobs, rq, d_n, hq, hq_n, accum, work, err);
-    else if (cfg.variant == 2)
-        k_trace_render<12><<<cfg.grid, 128, 0, s>>>(scenes, jobs, rq, d_n, hq, hq_n, accum, work, err);
-    else
-        k_trace_render<1><<<cfg.grid, 128, 0, s>>>(scenes, jobs, rq, d_n, hq, hq_n, accum, work, err);
+#define WF_TRACE(M, B) \
+    k_trace_render<M, B><<<cfg.grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, d_n, hq, hq_n, accum, work, err)
+    if (t.multi) {
+        if (cfg.variant == 1) WF_TRACE(true, 10); else if (cfg.variant == 2) WF_TRACE(true, 12); else WF_TRACE(true, 1);
+    } else {
+        if (cfg.variant == 1) WF_TRACE(false, 10); else if (cfg.variant == 2) WF_TRACE(false, 12); else WF_TRACE(false, 1);
+    }
+#undef WF_TRACE
 }
 
 void launch_camera_chunks(const WaveChunk* chunks, const long long* header, const DeviceJob* jobs, RayQueueDev rq,
@@ -839,22 +853,28 @@ void launch_camera_chunks(const WaveChunk* chunks, const long long* header, cons
 
 void launch_tally(const ull* counters, ull* tally, cudaStream_t s) { k_tally<<<1, 1, 0, s>>>(counters, tally); }
 
-void launch_shade(const DeviceScene* scenes, const DeviceJob* jobs, RayQueueDev rq, HitQueueDev hq,
-                  const ull* hq_n, ShadowQueueDev sh, ull* sh_n, RayQueueDev next, ull* next_n,
-                  float* accum, int* err, LaunchCfg cfg, cudaStream_t s)
+void launch_shade(const WaveTables& t, RayQueueDev rq, HitQueueDev hq, const ull* hq_n, ShadowQueueDev sh,
+                  ull* sh_n, RayQueueDev next, ull* next_n, float* accum, int* err, LaunchCfg cfg, cudaStream_t s)
 {
-    k_shade<<<cfg.grid, 128, 0, s>>>(scenes, jobs, rq, hq, hq_n, sh, sh_n, next, next_n, accum, err);
+    if (t.multi)
+        k_shade<true><<<cfg.grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, hq, hq_n, sh, sh_n, next,
+                                               next_n, accum, err);
+    else
+        k_shade<false><<<cfg.grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, hq, hq_n, sh, sh_n, next,
+                                                next_n, accum, err);
 }
 
-void launch_occluded_render(const DeviceScene* scenes, const DeviceJob* jobs, ShadowQueueDev sh,
-                            const ull* sh_n, float* accum, ull* work, int* err, LaunchCfg cfg, cudaStream_t s)
+void launch_occluded_render(const WaveTables& t, ShadowQueueDev sh, const ull* sh_n, float* accum, ull* work,
+                            int* err, LaunchCfg cfg, cudaStream_t s)
 {
-    if (cfg.variant == 1)
-        k_occluded_render<10><<<cfg.grid, 128, 0, s>>>(scenes, jobs, sh, sh_n, accum, work, err);
-    else if (cfg.variant == 2)
-        k_occluded_render<12><<<cfg.grid, 128, 0, s>>>(scenes, jobs, sh, sh_n, accum, work, err);
-    else
-        k_occluded_render<1><<<cfg.grid, 128, 0, s>>>(scenes, jobs, sh, sh_n, accum, work, err);
+#define WF_OCC(M, B) \
+    k_occluded_render<M, B><<<cfg.grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, sh, sh_n, accum, work, err)
+    if (t.multi) {
+        if (cfg.variant == 1) WF_OCC(true, 10); else if (cfg.variant == 2) WF_OCC(true, 12); else WF_OCC(true, 1);
+    } else {
+        if (cfg.variant == 1) WF_OCC(false, 10); else if (cfg.variant == 2) WF_OCC(false, 12); else WF_OCC(false, 1);
+    }
+#undef WF_OCC
 }
 
 void launch_ray_keys(const DeviceScene* scenes, const DeviceJob* jobs, RayQueueDev rq, const ull* d_n,

@@ -63,8 +63,6 @@ constexpr uint32_t kSentinel = 0xFFFFFFFFu;
 template <bool kAnyHit>
 struct Traversal {
     V3 o, d, inv, oi;
-    const BvhNode* nodes;  // the ray's scene, kept in registers
-    const float4* tris;
     float tmin, best_t;
     int best_g;
     uint32_t cur;
@@ -79,8 +77,6 @@ struct Traversal {
     {
         o = o_;
         d = d_;
-        nodes = S.nodes;
-        tris = S.tris;
         inv = v3(safe_inv(d.x), safe_inv(d.y), safe_inv(d.z));
         oi = v3(o.x * inv.x, o.y * inv.y, o.z * inv.z);
         tmin = tmin_;
@@ -94,7 +90,10 @@ struct Traversal {
     }
     __device__ __forceinline__ bool done() const { return cur == kSentinel; }
 
-    __device__ __forceinline__ void round(uint32_t* stack)
+    // nodes / tris of the ray's scene: from the kernel's parameter bank when
+    // every ray shares one scene, else from the scene table.
+    __device__ __forceinline__ void round(const BvhNode* __restrict__ nodes, const float4* __restrict__ tris,
+                                          uint32_t* stack)
     {
         while (!(cur & kLeafFlag)) {
             const BvhNode nd = load_node(nodes, cur);
@@ -156,7 +155,7 @@ __device__ __forceinline__ bool traverse(const DeviceScene& S, V3 o, V3 d, float
     Traversal<kAnyHit> tr;
     uint32_t stack[kStackSize];
     tr.init(S, stack, o, d, tmin, tmax);
-    while (!tr.done()) tr.round(stack);
+    while (!tr.done()) tr.round(S.nodes, S.tris, stack);
     res = tr.res;
     if (tr.overflow) atomicOr(err_flag, 1);
     return !tr.overflow;
