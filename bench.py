@@ -42,6 +42,8 @@ WORKLOADS = {
                name="c1_icosphere_1310720tri_1024x1024_64spp_depth12"),
     "c0": dict(config=0, width=256, height=256, spp=16, depth=8,
                name="c0_cornell_36tri_256x256_16spp_depth8"),
+    "c2": dict(config=2, width=2048, height=2048, spp=32, depth=8,
+               name="c2_lattice_4096meshes_15127922tri_256mat_64tex_hdri_2048x2048_32spp_depth8"),
 }
 METRIC = "Mrays/s (closest-hit + shadow rays) at equal MSE vs FP64 oracle"
 
@@ -177,13 +179,19 @@ def barrier(dist):
         dist.barrier()
 
 
+_CPU_SCENES: dict = {}
+
+
 def cpu_sample(pkg, wl, threads: int, rows: int, spp: int, seed: int):
-    """The oracle port over a centred band of the workload (rank 0 only)."""
+    """The oracle port over a centred band of the workload (rank 0 only).
+    The scene and the port's BVH are built once per workload, untimed."""
     sys.path.insert(0, str(ROOT / "oracle"))
     import oracle
 
-    scene = pkg.HostScene(wl["config"])
-    port = oracle.Port(scene.desc)
+    if wl["config"] not in _CPU_SCENES:
+        sc = pkg.HostScene(wl["config"])
+        _CPU_SCENES[wl["config"]] = (sc, oracle.Port(sc.desc))
+    scene, port = _CPU_SCENES[wl["config"]]
     W, H = wl["width"], wl["height"]
     cam = scene.camera(W, H)
     p = pkg.render_params(W, H, spp, wl["depth"], cam, seed=seed)
@@ -372,6 +380,7 @@ def main() -> int:
     ap.add_argument("--budget-gb", type=float, default=60.0, help="config 4: HBM budget")
     ap.add_argument("--policy", default="none", choices=["none", "material", "texture", "costBenefit"])
     ap.add_argument("--ray-sort", type=int, default=0)
+    ap.add_argument("--env-nee", type=int, default=0, help="environment NEE + MIS (same mean, lower variance)")
     ap.add_argument("--spp-per-wave", type=int, default=0)
     ap.add_argument("--spp", type=int, default=0, help="override the workload's spp (profiling runs only)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -405,7 +414,7 @@ def main() -> int:
 
     def params(seed):
         return pkg.render_params(W, H, wl["spp"], wl["depth"], cam, policy=policy, ray_sort=bool(args.ray_sort),
-                                 seed=seed, spp_per_wave=args.spp_per_wave)
+                                 seed=seed, spp_per_wave=args.spp_per_wave, env_nee=bool(args.env_nee))
 
     for w in range(max(args.warmup, 0)):
         ctx.render_device(params(1000 + w))
@@ -459,8 +468,10 @@ def main() -> int:
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": wl["name"], "policy": args.policy, "ray_sort": bool(args.ray_sort),
+                   "env_nee": bool(args.env_nee),
                    "triangles": info.num_triangles, "spp_per_wave": args.spp_per_wave or "auto",
-                   "l2": "inputs larger than L2 (ray queues ~0.9 GB per wave, BVH+triangles ~130 MB)",
+                   "l2": "inputs larger than L2 (ray queues ~1 GB per wave of 8.4 M paths; "
+                         f"BVH + triangles {info.num_triangles * 96 / 1e6:.0f} MB)",
                    "parallelism": f"replicas x{world}"},
         "samples_per_s": samples_all / (ms_max / 1e3),
         "closest_rays_per_step": stats[0]["closest_rays"], "shadow_rays_per_step": stats[0]["shadow_rays"],

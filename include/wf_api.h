@@ -168,6 +168,12 @@ typedef struct wf_render_params {
     uint32_t seed_hi;
     int32_t first_sample;          /* samples [first, first+spp) are drawn  */
     int32_t spp_per_wave;          /* samples per wavefront; 0 = automatic  */
+    /* Environment-map next-event estimation with balance-heuristic MIS.
+     * No reference counterpart (the reference only adds throughput * sky on
+     * a miss, WavefrontRenderer.cpp:256-265); 0 keeps that estimator, 1 adds
+     * an importance-sampled environment shadow ray at Diffuse and Plastic
+     * hits and weights the misses after them: same mean, lower variance. */
+    int32_t enable_env_nee;
     /* CostTracker::relativeCost per material / texture, frozen for the
      * render (include/render/CostTracker.h:42-55).  NULL = 1.0 for all. */
     const double* rel_cost_material;
@@ -416,7 +422,7 @@ typedef struct wf_job {
     uint32_t seed_lo;
     uint32_t seed_hi;
     int32_t first_sample;
-    int32_t reserved;
+    int32_t enable_env_nee;          /* as wf_render_params::enable_env_nee */
     const double* rel_cost_material; /* frozen relativeCost per material or NULL */
     wf_camera camera;
 } wf_job;

@@ -262,7 +262,8 @@ def ref_lib() -> C.CDLL:
         "ref_shading_schedule": ([C.c_int, C.c_longlong, i32p, i32p] + [f32p] * 6 +
                                  [C.c_int, C.POINTER(wf.WfMaterial), C.c_int, i32p,
                                   C.c_longlong, i32p, f64p, C.c_longlong, i32p, f64p, C.c_int, i32p], None),
-        "ref_render": ([V, f32p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_float, i32p, f32p], None),
+        "ref_render": ([V, f32p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_float, C.c_char_p, f32p],
+                       None),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -303,14 +304,35 @@ class Ref:
                               ptr(np.ascontiguousarray(maxd, np.float32)), ptr(out, C.c_uint8))
         return out
 
-    def render(self, cam12, w, h, spp, max_depth, policy=0, ray_sort=False, firefly=10.0, seed=1, threads=0):
+    def render(self, cam12, w, h, spp, max_depth, policy=0, ray_sort=False, firefly=10.0, seed=1, threads=0,
+               env_path=None):
+        """env_path: a PFM (write_pfm) loaded as the renderer's environment map."""
         if threads:
             self.lib.ref_set_threads(threads)
         self.lib.ref_set_seed(seed)
         img = np.zeros(w * h * 3, np.float32)
         cam12 = np.ascontiguousarray(cam12, np.float32)
-        self.lib.ref_render(self.h, ptr(cam12), w, h, spp, max_depth, policy, int(ray_sort), firefly, None, ptr(img))
+        env = str(env_path).encode() if env_path else None
+        self.lib.ref_render(self.h, ptr(cam12), w, h, spp, max_depth, policy, int(ray_sort), firefly, env, ptr(img))
         return img.reshape(h, w, 3)
+
+
+def write_pfm(path, rgb: np.ndarray) -> None:
+    """Writes an (h, w, 3) float image, top row first in memory, as a
+    little-endian PFM (rows stored bottom to top)."""
+    rgb = np.ascontiguousarray(rgb, np.float32)
+    h, w, _ = rgb.shape
+    with open(path, "wb") as f:
+        f.write(f"PF\n{w} {h}\n-1.0\n".encode())
+        f.write(rgb[::-1].astype("<f4").tobytes())
+
+
+def scene_environment(desc) -> np.ndarray | None:
+    """The (h, w, 3) environment map of a wf_scene_desc, or None."""
+    e = desc.environment
+    if e.width <= 0 or not e.rgb:
+        return None
+    return np.ctypeslib.as_array(e.rgb, shape=(e.height * e.width * 3,)).reshape(e.height, e.width, 3).copy()
 
 
 def ref_camera(look_from, look_at, up, vfov, w, h) -> np.ndarray:

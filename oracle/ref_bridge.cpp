@@ -289,9 +289,10 @@ void ref_shading_schedule(int policy, long long n, const int* mat_ids, const int
 }
 
 // WavefrontRenderer::renderScene with adaptive sampling and cost-aware RR
-// off; writes the averaged image (width*height*3).
+// off; writes the averaged image (width*height*3).  env_path (may be null)
+// names a PFM the renderer loads as its environment map.
 void ref_render(void* sp, const float c12[12], int w, int h, int spp, int max_depth, int policy, int ray_sort,
-                float firefly, int* counts_out, float* image_out)
+                float firefly, const char* env_path, float* image_out)
 {
     Scene* s = (Scene*)sp;
     Camera cam = camera_from12(c12);
@@ -302,6 +303,7 @@ void ref_render(void* sp, const float c12[12], int w, int h, int spp, int max_de
     r.enableRaySort = ray_sort != 0;
     r.enableSampleLogging = true;
     r.fireflyThreshold = firefly;
+    if (env_path) r.environmentMapPath = env_path;
     void (*old_term)(int) = std::signal(SIGTERM, SIG_DFL);
     void (*old_int)(int) = std::signal(SIGINT, SIG_DFL);
     {
@@ -315,7 +317,6 @@ void ref_render(void* sp, const float c12[12], int w, int h, int spp, int max_de
         image_out[3 * i + 1] = img.pixels[i].y;
         image_out[3 * i + 2] = img.pixels[i].z;
     }
-    (void)counts_out;
 }
 
 }  // extern "C"

@@ -73,7 +73,7 @@ inline void philox10(const uint32_t in[4], const uint32_t key[2], uint32_t out[4
 
 // Random-number purposes.  Each (purpose, depth) of a path is its own stream,
 // so the numbers a path sees do not depend on queue order or batching.
-enum : uint32_t { kPurposeCamera = 1, kPurposeLight = 2, kPurposeScatter = 3, kPurposeRoulette = 4 };
+enum : uint32_t { kPurposeCamera = 1, kPurposeLight = 2, kPurposeScatter = 3, kPurposeRoulette = 4, kPurposeEnvironment = 5 };
 
 // A sequential stream of floats in [0, 1) with 24 random bits each.
 struct Stream {
@@ -131,6 +131,9 @@ struct orc_scene {
     std::vector<float> env_rgb;
     float env_scale = 1.0f;
     float env_tint[3] = {1, 1, 1};
+    // environment importance sampler (no reference counterpart)
+    std::vector<float> env_prob, env_pdf;
+    std::vector<int> env_alias;
     wf_directional_light dir{};
     // derived
     std::vector<int> tri_mesh;        // global triangle -> mesh (geomID)
@@ -655,17 +658,23 @@ LightSample sample_light(const orc_scene& S, V3 shading_point, Stream& rng)
     return ls;
 }
 
+// EnvironmentMap::sample's texel of a normalized direction
+// (src/core/EnvironmentMap.cpp:34-42).
+size_t env_texel(const orc_scene& S, V3 d)
+{
+    float u = 0.5f + std::atan2(d.z, d.x) / (2.0f * (float)M_PI);
+    float v = 0.5f - std::asin(std::max(-1.0f, std::min(1.0f, d.y))) / (float)M_PI;
+    int x = std::min(S.env_w - 1, std::max(0, (int)(u * S.env_w)));
+    int y = std::min(S.env_h - 1, std::max(0, (int)(v * S.env_h)));
+    return (size_t)y * S.env_w + x;
+}
+
 // WavefrontRenderer::getSkyColor (.cpp:879-888) and EnvironmentMap::sample
 // (src/core/EnvironmentMap.cpp:30-49).
 V3 sky_color(const orc_scene& S, V3 dir)
 {
     if (S.env_w > 0) {
-        V3 d = normalized(dir);
-        float u = 0.5f + std::atan2(d.z, d.x) / (2.0f * (float)M_PI);
-        float v = 0.5f - std::asin(std::max(-1.0f, std::min(1.0f, d.y))) / (float)M_PI;
-        int x = std::min(S.env_w - 1, std::max(0, (int)(u * S.env_w)));
-        int y = std::min(S.env_h - 1, std::max(0, (int)(v * S.env_h)));
-        size_t k = ((size_t)y * S.env_w + x) * 3;
+        size_t k = env_texel(S, normalized(dir)) * 3;
         V3 raw = {S.env_rgb[k], S.env_rgb[k + 1], S.env_rgb[k + 2]};
         return raw * S.env_scale * V3{S.env_tint[0], S.env_tint[1], S.env_tint[2]};
     }
@@ -676,6 +685,79 @@ V3 sky_color(const orc_scene& S, V3 dir)
 }
 
 inline V3 vmin(V3 a, float c) { return {std::min(a.x, c), std::min(a.y, c), std::min(a.z, c)}; }
+
+// --- environment NEE (an addition of the GPU path, restated here so the
+// GPU's paths can be checked one by one; the reference has only the miss
+// term).  Texel weights f = luminance(rgb * scale * tint) * cos(elevation of
+// the texel row's centre); p_i = N f_i / sum f; Walker alias table by Vose's
+// method with index-ordered stacks of p < 1 and p >= 1.
+
+void build_env_sampler(orc_scene& S)
+{
+    const size_t W = (size_t)S.env_w, H = (size_t)S.env_h, N = W * H;
+    std::vector<double> w(N);
+    double total = 0.0;
+    for (size_t y = 0; y < H; ++y) {
+        const double row_cos = std::cos((0.5 - ((double)y + 0.5) / (double)H) * M_PI);
+        for (size_t x = 0; x < W; ++x) {
+            const float* t = &S.env_rgb[3 * (y * W + x)];
+            double lum = 0.2126 * ((double)t[0] * S.env_scale * S.env_tint[0]) +
+                         0.7152 * ((double)t[1] * S.env_scale * S.env_tint[1]) +
+                         0.0722 * ((double)t[2] * S.env_scale * S.env_tint[2]);
+            w[y * W + x] = std::max(0.0, lum) * row_cos;
+            total += w[y * W + x];
+        }
+    }
+    if (!(total > 0.0) || !std::isfinite(total)) return;
+    S.env_prob.assign(N, 1.0f);
+    S.env_pdf.resize(N);
+    S.env_alias.resize(N);
+    std::vector<int64_t> lo, hi;
+    for (size_t i = 0; i < N; ++i) {
+        w[i] = w[i] * (double)N / total;
+        S.env_pdf[i] = (float)w[i];
+        S.env_alias[i] = (int)i;
+        if (w[i] < 1.0)
+            lo.push_back((int64_t)i);
+        else
+            hi.push_back((int64_t)i);
+    }
+    while (!lo.empty() && !hi.empty()) {
+        int64_t a = lo.back(), b = hi.back();
+        lo.pop_back();
+        hi.pop_back();
+        S.env_prob[a] = (float)w[a];
+        S.env_alias[a] = (int)b;
+        w[b] = (w[b] + w[a]) - 1.0;
+        if (w[b] < 1.0)
+            lo.push_back(b);
+        else
+            hi.push_back(b);
+    }
+}
+
+// Solid-angle density of env_sample at a normalized direction:
+// p W H / (2 pi^2 cos(elevation)).
+float env_pdf(const orc_scene& S, V3 d)
+{
+    float c = std::sqrt(std::max(0.0f, 1.0f - d.y * d.y));
+    if (!(c > 0.0f)) return 0.0f;
+    return S.env_pdf[env_texel(S, d)] / (2.0f * kPi * kPi * c);
+}
+
+V3 env_sample(const orc_scene& S, float x1, float x2, float x3, float x4)
+{
+    const int64_t n = (int64_t)S.env_w * S.env_h;
+    int64_t i = std::min(n - 1, (int64_t)(x1 * (float)n));
+    if (!(x2 < S.env_prob[i])) i = S.env_alias[i];
+    int y = (int)(i / S.env_w), x = (int)(i - (int64_t)y * S.env_w);
+    float u = ((float)x + x3) / (float)S.env_w;
+    float v = ((float)y + x4) / (float)S.env_h;
+    float phi = (u - 0.5f) * (2.0f * kPi);
+    float el = (0.5f - v) * kPi;
+    float ce = std::cos(el), se = std::sin(el);
+    return {ce * std::cos(phi), se, ce * std::sin(phi)};
+}
 
 // Camera::getRay, include/core/Camera.h:35-40.
 void camera_ray(const wf_camera& c, float u, float v, V3& o, V3& d)
@@ -715,7 +797,10 @@ void render_path(const orc_scene& S, const wf_render_params& P, int x, int y, in
         Closest c = closest_bvh(S, o, d, 0.001f, 1e9f);
         if (c.tri < 0) {  // miss loop, .cpp:256-265
             cnt.misses++;
-            add(T * sky_color(S, d));
+            V3 sky = T * sky_color(S, d);
+            if (P.enable_env_nee && !S.env_prob.empty() && in_pdf > 0.0f)
+                sky = sky * mis_balance(in_pdf, env_pdf(S, normalized(d)));
+            add(sky);
             break;
         }
         cnt.shaded_hits++;
@@ -773,6 +858,25 @@ void render_path(const orc_scene& S, const wf_render_params& P, int x, int y, in
                     V3 col = {S.dir.color[0], S.dir.color[1], S.dir.color[2]};
                     V3 direct = T * brdf * col * S.dir.intensity * cos_s;
                     add(vmin(direct, ff));
+                }
+            }
+        }
+        // Environment NEE (GPU addition, see build_env_sampler), unclamped
+        if (P.enable_env_nee && !S.env_prob.empty() && depth + 1 < P.max_depth &&
+            (m.type == WF_MATERIAL_DIFFUSE || m.type == WF_MATERIAL_PLASTIC)) {
+            Stream erng(P.seed_lo, P.seed_hi, kPurposeEnvironment, (uint32_t)depth, pixel, (uint32_t)sample);
+            float x1 = erng.next(), x2 = erng.next(), x3 = erng.next(), x4 = erng.next();
+            V3 wi = env_sample(S, x1, x2, x3, x4);
+            float cos_s = dot(h.n, wi);
+            float pe = env_pdf(S, wi);
+            if (cos_s > 0.0f && pe > 0.0f) {
+                cnt.shadow_rays++;
+                if (!occluded_bvh(S, h.p, wi, 1e6f)) {
+                    V3 surf = surface_color(S, m, h);
+                    float kd = 1.0f;
+                    if (m.type == WF_MATERIAL_PLASTIC) kd = 1.0f - schlick(std::max(0.0f, dot(d * -1.0f, h.n)), 1.5f);
+                    float bp = cos_s / kPi;
+                    add(T * surf * (kd / kPi) * sky_color(S, wi) * (cos_s / (pe + bp)));
                 }
             }
         }
@@ -865,6 +969,7 @@ orc_scene* orc_scene_create(const wf_scene_desc* D)
                           D->environment.rgb + 3 * (size_t)S->env_w * S->env_h);
         S->env_scale = D->environment.intensity_scale;
         for (int k = 0; k < 3; ++k) S->env_tint[k] = D->environment.tint[k];
+        build_env_sampler(*S);
     }
     S->dir = D->directional;
     // Per-triangle mesh ids; meshes are contiguous in index order.

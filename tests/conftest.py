@@ -66,6 +66,12 @@ def scene_small(wf):
     return wf.HostScene(100, seed=3)
 
 
+@pytest.fixture(scope="session")
+def scene_c2small(wf):
+    """16 x 16 meshes, 256 materials (glass, metal, textured Lambert), HDRI."""
+    return wf.HostScene(102)
+
+
 def rays_in_box(rng, n, lo, hi):
     """Random rays from points inside an axis box, directions uniform on the sphere."""
     o = rng.uniform(lo, hi, size=(n, 3)).astype(np.float32)
@@ -105,3 +111,47 @@ def fp64_band(img, spp, golden, block=8):
     assert mse < 1.2 * expected, out
     assert max(abs(c) for c in out["channel_rel"]) < 0.01, out
     return out
+
+
+class PlaneUnderSky:
+    """A Lambertian ground quad (albedo 0.5, 2000 x 2000 at y = 0, normal +y)
+    under an equirect environment, seen from 1 m above, looking down.  With
+    max depth 2 every pixel's expectation is albedo/pi times the
+    cosine-weighted integral of the map over the upper hemisphere, which is
+    exact per texel row: (2 pi / W) (sin^2 e_hi - sin^2 e_lo) / 2 for the
+    row's elevations clipped at the horizon."""
+
+    def __init__(self, wf, env: np.ndarray):
+        import ctypes as C
+
+        self.env = np.ascontiguousarray(env, np.float32)
+        H, W, _ = self.env.shape
+        self.px = np.array([-1000, 1000, 1000, -1000], np.float32)
+        self.py = np.zeros(4, np.float32)
+        self.pz = np.array([-1000, -1000, 1000, 1000], np.float32)
+        self.idx = np.array([0, 2, 1, 0, 3, 2], np.int32)
+        self.off, self.cnt, self.mm = (np.array([v], np.int32) for v in (0, 6, 0))
+        self.mats = (wf.WfMaterial * 1)(wf.WfMaterial(type=0, albedo=(0.5, 0.5, 0.5), texture_id=-1))
+        d = wf.WfSceneDesc()
+        d.num_vertices = 4
+        d.positions_x, d.positions_y, d.positions_z = wf.ptr(self.px), wf.ptr(self.py), wf.ptr(self.pz)
+        d.num_indices = 6
+        d.indices = wf.ptr(self.idx, C.c_int32)
+        d.num_meshes = 1
+        d.mesh_index_offsets = wf.ptr(self.off, C.c_int32)
+        d.mesh_index_counts = wf.ptr(self.cnt, C.c_int32)
+        d.mesh_material_ids = wf.ptr(self.mm, C.c_int32)
+        d.num_materials = 1
+        d.materials = C.cast(self.mats, C.POINTER(wf.WfMaterial))
+        d.environment.width, d.environment.height = W, H
+        d.environment.rgb = wf.ptr(self.env)
+        d.environment.intensity_scale = 1.0
+        d.environment.tint[:] = (1.0, 1.0, 1.0)
+        self.desc = d
+        e = (0.5 - np.arange(H + 1) / H) * np.pi
+        hi, lo = np.maximum(e[:-1], 0.0), np.maximum(e[1:], 0.0)
+        row = (np.sin(hi) ** 2 - np.sin(lo) ** 2) / 2.0 * (2.0 * np.pi / W)
+        self.expected = 0.5 / np.pi * (self.env.astype(np.float64) * row[:, None, None]).sum(axis=(0, 1))
+
+    def camera(self, wf, w, h):
+        return wf.camera_make([0, 1, 0], [0, 0, 0.001], [0, 0, -1], 30.0, w, h)

@@ -105,7 +105,7 @@ def test_server_admission_respects_budget(wf, ctx):
     for j in jobs:
         j.width, j.height, j.samples_per_pixel = 64, 64, 8
     wave = 1 << 14
-    per_path = 2 * 14 * 4 + 2 * 5 * 4 + 2 * 12 * 4 + 2 * 12 + 8 * 4
+    per_path = 2 * 14 * 4 + 2 * 5 * 4 + 3 * 12 * 4 + 2 * 12 + 8 * 4
     budget = wave * per_path + 2 * 64 * 64 * 3 * 4  # room for two accumulators
     srv = wf.Server(ctx, hbm_budget_bytes=budget, frame_spp=8, max_paths_per_wave=wave)
     ids = [srv.submit(j) for j in jobs]
@@ -137,3 +137,15 @@ def test_server_cancel(wf, ctx):
     assert srv.status(ids[0])["state"] == wf.JOB_CANCELLED
     assert all(srv.status(i)["state"] == wf.JOB_DONE for i in ids[1:])
     srv.close()
+
+
+def test_batch_env_nee_job_equals_job_alone(wf, ctx, scene_c2small):
+    """A job with environment NEE among jobs without it (per-ray job flags)."""
+    sid = ctx.add_scene(scene_c2small.desc)
+    jobs, hosts = _jobs(wf, ctx, 3, seed0=1100)
+    cam = scene_c2small.camera(40, 32)
+    nee = wf.make_job(sid, 40, 32, 4, 8, cam, seed=4242, env_nee=True)
+    imgs, _ = ctx.render_batch(jobs + [nee])
+    ctx.upload(scene_c2small.desc)
+    alone, _ = ctx.render(wf.render_params(40, 32, 4, 8, cam, seed=4242, env_nee=True))
+    assert _same(imgs[-1], alone) >= 0.999

@@ -37,16 +37,19 @@ def test_camera_rays_bit_exact(wf, orc, ctx, scene0):
         assert np.array_equal(g[k], c[k]), k
 
 
-@pytest.mark.parametrize("which", ["c0", "small"])
-def test_trace_closest_matches_oracle(wf, orc, ctx, scene0, scene_small, which):
-    scene = scene0 if which == "c0" else scene_small
+@pytest.mark.parametrize("which", ["c0", "small", "c2small"])
+def test_trace_closest_matches_oracle(wf, orc, ctx, scene0, scene_small, scene_c2small, which):
+    scene = {"c0": scene0, "small": scene_small, "c2small": scene_c2small}[which]
     ctx.upload(scene.desc)
     port = orc.Port(scene.desc)
     rng = np.random.default_rng(11)
     cam = scene.camera(128, 128)
     prim = orc.generate_primary(cam, 128, 128, 3, 0, 1)
     o1, d1 = _od(prim)
-    o2, d2 = rays_in_box(rng, 50000, [-0.27, 0.01, -0.54], [0.27, 0.54, -0.01])
+    if which == "c2small":  # 16 x 16 lattice on the ground plane, meshes below y = 0.9
+        o2, d2 = rays_in_box(rng, 50000, [0.0, 0.01, 0.0], [16.0, 0.9, 16.0])
+    else:
+        o2, d2 = rays_in_box(rng, 50000, [-0.27, 0.01, -0.54], [0.27, 0.54, -0.01])
     o = np.concatenate([o1, o2])
     d = np.concatenate([d1, d2])
     g = ctx.trace_closest(o, d)
@@ -256,12 +259,12 @@ def _mean_close(a, b, rel):
     return np.all(np.abs(ma - mb) <= rel * np.abs(mb))
 
 
-@pytest.mark.parametrize("which", ["c0", "small"])
-def test_render_matches_oracle_paths(wf, orc, ctx, scene0, scene_small, which):
+@pytest.mark.parametrize("which", ["c0", "small", "c2small"])
+def test_render_matches_oracle_paths(wf, orc, ctx, scene0, scene_small, scene_c2small, which):
     """Same seed, same random streams: pixels agree except where a
     transcendental's last ulp moves a path.  Tolerance: 98% of pixels within
     1e-3 relative + 1e-4 absolute, channel means within 1%."""
-    scene = scene0 if which == "c0" else scene_small
+    scene = {"c0": scene0, "small": scene_small, "c2small": scene_c2small}[which]
     ctx.upload(scene.desc)
     port = orc.Port(scene.desc)
     W = H = 64
@@ -277,14 +280,17 @@ def test_render_matches_oracle_paths(wf, orc, ctx, scene0, scene_small, which):
     assert st["closest_rays"] == cnt["closest_rays"] or abs(st["closest_rays"] - cnt["closest_rays"]) < 0.01 * cnt["closest_rays"]
 
 
-def test_render_is_order_independent(wf, ctx, scene_small):
+@pytest.mark.parametrize("which", ["small", "c2small"])
+def test_render_is_order_independent(wf, ctx, scene_small, scene_c2small, which):
     """Ray sort, policies and wave size change only the order of work: with
     path-keyed random streams the image is the same up to float-add order
     (atomic accumulation); tolerance 1e-4 relative on 99.9% of pixels."""
-    ctx.upload(scene_small.desc)
+    scene = scene_small if which == "small" else scene_c2small
+    ctx.upload(scene.desc)
     W = H = 48
-    cam = scene_small.camera(W, H)
+    cam = scene.camera(W, H)
     base, _ = ctx.render(wf.render_params(W, H, 8, 12, cam, seed=5))
+    assert np.isfinite(base).all()
     for kw in [dict(ray_sort=True), dict(policy=1), dict(policy=2), dict(policy=3), dict(spp_per_wave=3)]:
         img, _ = ctx.render(wf.render_params(W, H, 8, 12, cam, seed=5, **kw))
         agree = np.isclose(img, base, rtol=1e-4, atol=1e-6).all(axis=2).mean()
@@ -371,3 +377,41 @@ def test_gpu_render_within_fp64_band(wf, ctx, scene0):
     img, st = ctx.render(wf.render_params(W, H, spp, 8, scene0.camera(W, H), seed=31337))
     out = fp64_band(img, spp, g)
     print(f"MSE vs FP64 oracle {out['mse']:.4e} (variance predicts {out['expected_mse']:.4e}), {out}")
+
+
+# ------------------------------------ environment NEE (GPU addition) -------
+
+def test_gpu_env_nee_matches_analytic_irradiance(wf, orc, ctx):
+    """The GPU's environment NEE converges to the exact cosine-weighted
+    integral of the map (plane under the config-102 HDRI, sun lobe 1e4):
+    within 4 standard errors of 8 runs + 1e-3 relative."""
+    from conftest import PlaneUnderSky
+
+    sky = PlaneUnderSky(wf, orc.scene_environment(wf.HostScene(102).desc))
+    ctx.upload(sky.desc)
+    W = H = 64
+    spp, N = 256, 8
+    cam = sky.camera(wf, W, H)
+    X = np.array([ctx.render(wf.render_params(W, H, spp, 2, cam, seed=900 + k, env_nee=True))[0]
+                  for k in range(N)], np.float64).mean(axis=(1, 2))
+    m, se = X.mean(0), X.std(0, ddof=1) / np.sqrt(N)
+    assert np.all(np.abs(m - sky.expected) <= 4 * se + 1e-3 * sky.expected), (m, se, sky.expected)
+
+
+def test_gpu_env_nee_matches_oracle_paths(wf, orc, ctx, scene_c2small):
+    """Environment NEE on the textured 16 x 16 lattice: the GPU's paths are
+    the port's (same alias table, same random streams); tolerance as for the
+    other path-level checks."""
+    ctx.upload(scene_c2small.desc)
+    port = orc.Port(scene_c2small.desc)
+    W = H = 64
+    spp = 8
+    cam = scene_c2small.camera(W, H)
+    p = wf.render_params(W, H, spp, 8, cam, seed=77, env_nee=True)
+    img, st = ctx.render(p)
+    acc, cnt = port.render_window(p, 0, 0, W, H)
+    ref = acc / spp
+    agree = np.isclose(img, ref, rtol=1e-3, atol=1e-4).all(axis=2).mean()
+    assert agree >= 0.98, agree
+    assert _mean_close(img, ref, 0.01)
+    assert abs(int(st["shadow_rays"]) - int(cnt["shadow_rays"])) <= 0.01 * cnt["shadow_rays"]

@@ -91,7 +91,7 @@ class WfRenderParams(C.Structure):
                 ("max_depth", C.c_int32), ("rr_min_depth", C.c_int32), ("policy", C.c_int32),
                 ("enable_ray_sort", C.c_int32), ("enable_cost_aware_rr", C.c_int32),
                 ("firefly_threshold", C.c_float), ("seed_lo", C.c_uint32), ("seed_hi", C.c_uint32),
-                ("first_sample", C.c_int32), ("spp_per_wave", C.c_int32),
+                ("first_sample", C.c_int32), ("spp_per_wave", C.c_int32), ("enable_env_nee", C.c_int32),
                 ("rel_cost_material", f64p), ("rel_cost_texture", f64p), ("camera", WfCamera)]
 
 
@@ -126,7 +126,7 @@ class WfJob(C.Structure):
     _fields_ = [("scene_id", C.c_int32), ("width", C.c_int32), ("height", C.c_int32),
                 ("samples_per_pixel", C.c_int32), ("max_depth", C.c_int32), ("rr_min_depth", C.c_int32),
                 ("enable_cost_aware_rr", C.c_int32), ("firefly_threshold", C.c_float), ("seed_lo", C.c_uint32),
-                ("seed_hi", C.c_uint32), ("first_sample", C.c_int32), ("reserved", C.c_int32),
+                ("seed_hi", C.c_uint32), ("first_sample", C.c_int32), ("enable_env_nee", C.c_int32),
                 ("rel_cost_material", f64p), ("camera", WfCamera)]
 
 
@@ -317,11 +317,12 @@ def camera_make(look_from, look_at, up, vfov, width, height) -> WfCamera:
 
 
 def make_job(scene_id, width, height, spp, max_depth, camera: WfCamera, *, seed=1, rr_min_depth=3, firefly=10.0,
-             first_sample=0) -> WfJob:
+             first_sample=0, env_nee=False) -> WfJob:
     j = WfJob()
     j.scene_id, j.width, j.height, j.samples_per_pixel, j.max_depth = scene_id, width, height, spp, max_depth
     j.rr_min_depth, j.firefly_threshold, j.first_sample = rr_min_depth, firefly, first_sample
     j.seed_lo, j.seed_hi = seed & 0xFFFFFFFF, (seed >> 32) & 0xFFFFFFFF
+    j.enable_env_nee = int(bool(env_nee))
     j.camera = camera
     return j
 
@@ -376,7 +377,8 @@ class Server:
 
 def render_params(width, height, spp, max_depth, camera: WfCamera, *, policy=0, ray_sort=False,
                   rr_min_depth=3, firefly=10.0, seed=1, first_sample=0, spp_per_wave=0,
-                  cost_aware_rr=False, rel_cost_material=None, rel_cost_texture=None) -> WfRenderParams:
+                  cost_aware_rr=False, rel_cost_material=None, rel_cost_texture=None,
+                  env_nee=False) -> WfRenderParams:
     p = WfRenderParams()
     p.width, p.height, p.samples_per_pixel, p.max_depth = width, height, spp, max_depth
     p.rr_min_depth, p.policy, p.enable_ray_sort = rr_min_depth, policy, int(bool(ray_sort))
@@ -384,6 +386,7 @@ def render_params(width, height, spp, max_depth, camera: WfCamera, *, policy=0, 
     p.firefly_threshold = firefly
     p.seed_lo, p.seed_hi = seed & 0xFFFFFFFF, (seed >> 32) & 0xFFFFFFFF
     p.first_sample, p.spp_per_wave = first_sample, spp_per_wave
+    p.enable_env_nee = int(bool(env_nee))
     p._keep = []
     if rel_cost_material is not None:
         a = np.ascontiguousarray(rel_cost_material, dtype=np.float64)

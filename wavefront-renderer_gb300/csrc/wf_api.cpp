@@ -73,7 +73,7 @@ int ensure_render_buffers(wf_ctx* c, int64_t paths)
         WF_CK(c, wf_dalloc(A, &h.bu, n)); WF_CK(c, wf_dalloc(A, &h.bv, n));
         h.capacity = paths;
     }
-    const size_t ns = 2 * n;
+    const size_t ns = 3 * n;  // area, directional and environment NEE per hit
     ShadowQueueDev& s = c->sh;
     WF_CK(c, wf_dalloc(A, &s.ox, ns)); WF_CK(c, wf_dalloc(A, &s.oy, ns)); WF_CK(c, wf_dalloc(A, &s.oz, ns));
     WF_CK(c, wf_dalloc(A, &s.dx, ns)); WF_CK(c, wf_dalloc(A, &s.dy, ns)); WF_CK(c, wf_dalloc(A, &s.dz, ns));
@@ -345,6 +345,56 @@ bool has_scene(const wf_ctx* c) { return !c->scenes.empty() && c->scenes[0].live
 
 // Uploads one scene and builds its BVH: Scene::buildAccelerator
 // (src/core/Scene.cpp:79-113) + EmbreeAccelerator::build (Embree.cpp:66-119).
+// Environment importance sampler (no reference counterpart): texel weights
+// luminance(rgb * scale * tint) x cos(elevation of the texel's centre row),
+// normalised to p_i = N f_i / sum f (N texels, stored as texel_pdf), and
+// Walker's alias table built by Vose's method: texels with p < 1 and p >= 1
+// on two stacks in index order; repeatedly pop one of each, give the small
+// one (prob = p_s, alias = the large one) and move the large one's excess
+// p_l + p_s - 1 back onto the stack it now belongs to; leftovers get
+// prob 1.  Returns false when the map carries no energy.
+bool build_env_sampler(const wf_environment& e, std::vector<float>& prob, std::vector<int32_t>& alias,
+                       std::vector<float>& texel_pdf)
+{
+    const int64_t W = e.width, H = e.height, N = W * H;
+    std::vector<double> p((size_t)N);
+    double sum = 0.0;
+    const double pi = 3.14159265358979323846;
+    for (int64_t y = 0; y < H; ++y) {
+        const double ce = std::cos((0.5 - (y + 0.5) / (double)H) * pi);
+        for (int64_t x = 0; x < W; ++x) {
+            const float* t = e.rgb + 3 * (y * W + x);
+            const double r = (double)t[0] * e.intensity_scale * e.tint[0];
+            const double g = (double)t[1] * e.intensity_scale * e.tint[1];
+            const double b = (double)t[2] * e.intensity_scale * e.tint[2];
+            const double f = std::max(0.0, 0.2126 * r + 0.7152 * g + 0.0722 * b) * ce;
+            p[(size_t)(y * W + x)] = f;
+            sum += f;
+        }
+    }
+    if (!(sum > 0.0) || !std::isfinite(sum)) return false;
+    prob.assign((size_t)N, 1.0f);
+    alias.resize((size_t)N);
+    texel_pdf.resize((size_t)N);
+    std::vector<int64_t> small, large;
+    for (int64_t i = 0; i < N; ++i) {
+        p[(size_t)i] = p[(size_t)i] * (double)N / sum;
+        texel_pdf[(size_t)i] = (float)p[(size_t)i];
+        alias[(size_t)i] = (int32_t)i;
+        (p[(size_t)i] < 1.0 ? small : large).push_back(i);
+    }
+    while (!small.empty() && !large.empty()) {
+        const int64_t sm = small.back(), lg = large.back();
+        small.pop_back();
+        large.pop_back();
+        prob[(size_t)sm] = (float)p[(size_t)sm];
+        alias[(size_t)sm] = (int32_t)lg;
+        p[(size_t)lg] = (p[(size_t)lg] + p[(size_t)sm]) - 1.0;
+        (p[(size_t)lg] < 1.0 ? small : large).push_back(lg);
+    }
+    return true;
+}
+
 int build_scene(wf_ctx* c, const wf_scene_desc* D, ResidentScene& R)
 {
     if (!c || !D) return WF_ERR_INVALID_ARGUMENT;
@@ -452,6 +502,8 @@ int build_scene(wf_ctx* c, const wf_scene_desc* D, ResidentScene& R)
     S.root_is_empty = ntri == 0 ? 1 : 0;
     S.num_meshes = D->num_meshes;
 
+    std::vector<float> env_prob, env_pdf;
+    std::vector<int32_t> env_alias;
 #define UP(dst, src, count)                                                                     \
     do {                                                                                        \
         if (wf_dalloc(A, &dst, (count)) != cudaSuccess) {                                          \
@@ -553,6 +605,16 @@ int build_scene(wf_ctx* c, const wf_scene_desc* D, ResidentScene& R)
         S.env_h = D->environment.height;
         S.env_scale = D->environment.intensity_scale;
         for (int k = 0; k < 3; ++k) S.env_tint[k] = D->environment.tint[k];
+        if (build_env_sampler(D->environment, env_prob, env_alias, env_pdf)) {
+            float *d_prob = nullptr, *d_pdf = nullptr;
+            int32_t* d_alias = nullptr;
+            UP(d_prob, env_prob.data(), (int64_t)env_prob.size());
+            UP(d_alias, env_alias.data(), (int64_t)env_alias.size());
+            UP(d_pdf, env_pdf.data(), (int64_t)env_pdf.size());
+            S.env_alias_prob = d_prob;
+            S.env_alias = d_alias;
+            S.env_texel_pdf = d_pdf;
+        }
     }
     for (int k = 0; k < 3; ++k) {
         S.bmin[k] = bmin[k];

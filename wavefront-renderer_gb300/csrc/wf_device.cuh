@@ -84,6 +84,12 @@ struct DeviceScene {
     const float* env_rgb;
     float env_scale;
     float env_tint[3];
+    // Environment importance sampling (device addition): an alias table over
+    // the texels, weighted by luminance x cos(elevation), and each texel's
+    // probability times the texel count.  Null without a map.
+    const float* env_alias_prob;
+    const int32_t* env_alias;
+    const float* env_texel_pdf;
     // Bounds (Scene::computeBounds) for the ray sort
     float bmin[3], bmax[3];
 };
@@ -136,7 +142,7 @@ struct DeviceJob {
     int32_t cost_aware_rr;
     float firefly;
     uint32_t seed_lo, seed_hi;
-    int32_t pad;
+    int32_t env_nee;                 // environment NEE + MIS on
     int64_t accum_offset;            // float index of the job's first pixel sum
     const float* rel_cost_material;  // float(relativeCost) per material, or null
     wf_camera camera;
@@ -179,7 +185,13 @@ __device__ __forceinline__ V3 vmin(V3 a, float c) { return {fminf(a.x, c), fminf
 // sample), so a path's numbers do not depend on which thread, queue slot or
 // wave handles it.  Floats carry 24 random bits in [0, 1).
 // ---------------------------------------------------------------------------
-enum : uint32_t { kPurposeCamera = 1, kPurposeLight = 2, kPurposeScatter = 3, kPurposeRoulette = 4 };
+enum : uint32_t {
+    kPurposeCamera = 1,
+    kPurposeLight = 2,
+    kPurposeScatter = 3,
+    kPurposeRoulette = 4,
+    kPurposeEnvironment = 5
+};
 
 __host__ __device__ __forceinline__ void philox10(uint32_t c[4], uint32_t k0, uint32_t k1)
 {
@@ -488,17 +500,24 @@ __device__ __forceinline__ float mis_balance(float a, float b)
     return a / den;
 }
 
+// Texel of a normalized direction: EnvironmentMap::sample's mapping
+// (src/core/EnvironmentMap.cpp:34-42), u = 0.5 + atan2(z,x)/2pi,
+// v = 0.5 - asin(y)/pi, nearest texel.
+__device__ __forceinline__ int64_t env_texel(const DeviceScene& S, V3 d)
+{
+    float u = 0.5f + atan2f(d.z, d.x) / (2.0f * 3.14159265358979323846f);
+    float v = 0.5f - asinf(fmaxf(-1.0f, fminf(1.0f, d.y))) / 3.14159265358979323846f;
+    int x = min(S.env_w - 1, max(0, (int)(u * S.env_w)));
+    int y = min(S.env_h - 1, max(0, (int)(v * S.env_h)));
+    return (int64_t)y * S.env_w + x;
+}
+
 // WavefrontRenderer::getSkyColor (.cpp:879-888) / EnvironmentMap::sample
 // (src/core/EnvironmentMap.cpp:30-49).
 __device__ __forceinline__ V3 sky_color(const DeviceScene& S, V3 dir)
 {
     if (S.env_w > 0) {
-        V3 d = normalized(dir);
-        float u = 0.5f + atan2f(d.z, d.x) / (2.0f * 3.14159265358979323846f);
-        float v = 0.5f - asinf(fmaxf(-1.0f, fminf(1.0f, d.y))) / 3.14159265358979323846f;
-        int x = min(S.env_w - 1, max(0, (int)(u * S.env_w)));
-        int y = min(S.env_h - 1, max(0, (int)(v * S.env_h)));
-        int64_t k = ((int64_t)y * S.env_w + x) * 3;
+        int64_t k = env_texel(S, normalized(dir)) * 3;
         V3 raw = {__ldg(S.env_rgb + k), __ldg(S.env_rgb + k + 1), __ldg(S.env_rgb + k + 2)};
         return raw * S.env_scale * v3(S.env_tint[0], S.env_tint[1], S.env_tint[2]);
     }
@@ -506,6 +525,35 @@ __device__ __forceinline__ V3 sky_color(const DeviceScene& S, V3 dir)
     V3 dark = {0.02f, 0.02f, 0.05f};
     V3 horizon = {0.05f, 0.04f, 0.03f};
     return horizon * (1.0f - b) + dark * b;
+}
+
+// Solid-angle density of env_sample at a normalized direction: a texel's
+// probability p spread uniformly over its (u, v) cell, whose solid angle is
+// (2 pi / W)(pi / H) cos(elevation), gives p W H / (2 pi^2 cos(elevation)).
+__device__ __forceinline__ float env_pdf(const DeviceScene& S, V3 d)
+{
+    const float c = sqrtf(fmaxf(0.0f, 1.0f - d.y * d.y));
+    if (!(c > 0.0f)) return 0.0f;
+    return __ldg(S.env_texel_pdf + env_texel(S, d)) / (2.0f * kPi * kPi * c);
+}
+
+// Draws a direction from the environment: texel i = floor(x1 N), kept when
+// x2 < prob[i] else alias[i] (Walker's alias method), then a uniform point
+// of the texel's (u, v) cell from x3, x4, mapped back through the inverse of
+// env_texel's mapping.
+__device__ __forceinline__ V3 env_sample(const DeviceScene& S, float x1, float x2, float x3, float x4)
+{
+    const int64_t n = (int64_t)S.env_w * S.env_h;
+    int64_t i = min(n - 1, (int64_t)(x1 * (float)n));
+    if (!(x2 < __ldg(S.env_alias_prob + i))) i = __ldg(S.env_alias + i);
+    const int y = (int)(i / S.env_w);
+    const int x = (int)(i - (int64_t)y * S.env_w);
+    const float u = ((float)x + x3) / (float)S.env_w;
+    const float v = ((float)y + x4) / (float)S.env_h;
+    const float phi = (u - 0.5f) * (2.0f * kPi);
+    const float el = (0.5f - v) * kPi;
+    const float ce = cosf(el), se = sinf(el);
+    return {ce * cosf(phi), se, ce * sinf(phi)};
 }
 
 // ---------------------------------------------------------------------------

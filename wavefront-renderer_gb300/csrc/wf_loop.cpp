@@ -58,6 +58,7 @@ int make_device_job(wf_ctx* c, const wf_job& j, int64_t accum_offset, DeviceJob&
     dj.firefly = j.firefly_threshold;
     dj.seed_lo = j.seed_lo;
     dj.seed_hi = j.seed_hi;
+    dj.env_nee = j.enable_env_nee ? 1 : 0;
     dj.accum_offset = accum_offset;
     dj.camera = j.camera;
     if (j.enable_cost_aware_rr && j.rel_cost_material) {
@@ -318,6 +319,7 @@ int render_single(wf_ctx* c, const wf_render_params* P, wf_render_stats* st)
     j.seed_lo = P->seed_lo;
     j.seed_hi = P->seed_hi;
     j.first_sample = P->first_sample;
+    j.enable_env_nee = P->enable_env_nee;
     j.rel_cost_material = P->rel_cost_material;
     j.camera = P->camera;
     std::vector<DeviceJob> table(1);
@@ -445,7 +447,7 @@ namespace {
 // Bytes of the wave buffers per path in flight: two RayQueues (14 columns),
 // two hit queues (5), the shadow queue (2 x 12), sort keys and values (2 x 12)
 // and the policy columns (8).
-constexpr int64_t kBytesPerPath = 2 * 14 * 4 + 2 * 5 * 4 + 2 * 12 * 4 + 2 * 12 + 8 * 4;
+constexpr int64_t kBytesPerPath = 2 * 14 * 4 + 2 * 5 * 4 + 3 * 12 * 4 + 2 * 12 + 8 * 4;
 
 int finish_job(wf_server* sv, int64_t id, ServedJob& j)
 {

@@ -239,7 +239,14 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_trace_render(DeviceScene sc
         if (fin && !hit) {
             const V3 T = {rq.tr[ray], rq.tg[ray], rq.tb[ray]};
             const int64_t off = kMulti ? jobs[job].accum_offset : job0.accum_offset;
-            accum_add(accum + off, rq.pixel[ray], T * sky_color(*S, tr.d));
+            V3 c = T * sky_color(*S, tr.d);
+            // With environment NEE the bounce that sampled this direction by
+            // its BSDF (pdf > 0) shares the estimate: balance-heuristic weight.
+            if ((kMulti ? jobs[job].env_nee : job0.env_nee) && S->env_alias_prob) {
+                const float ip = rq.pdf[ray];
+                if (ip > 0.0f) c = c * mis_balance(ip, env_pdf(*S, normalized(tr.d)));
+            }
+            accum_add(accum + off, rq.pixel[ray], c);
         }
         if (fin) {
             overflow = overflow || tr.overflow;
@@ -295,9 +302,9 @@ __global__ void __launch_bounds__(128) k_shade(DeviceScene scene0, DeviceJob job
     {
         const int64_t k = base + threadIdx.x;
         const bool active = k < n;
-        bool want_area = false, want_dir = false, want_next = false;
+        bool want_area = false, want_dir = false, want_env = false, want_next = false;
         V3 p = {0, 0, 0}, dir_area = {0, 0, 0}, c_area = {0, 0, 0}, dir_sun = {0, 0, 0},
-           c_sun = {0, 0, 0}, nd = {0, 0, 0}, Tn = {0, 0, 0};
+           c_sun = {0, 0, 0}, dir_env = {0, 0, 0}, c_env = {0, 0, 0}, nd = {0, 0, 0}, Tn = {0, 0, 0};
         float dist_area = 0.0f, next_pdf = 0.0f;
         int pixel = 0, depth = 0, sample = 0, job = 0;
         if (active) {
@@ -387,12 +394,44 @@ __global__ void __launch_bounds__(128) k_shade(DeviceScene scene0, DeviceJob job
                 const float cos_s = dot(h.n, to);
                 if (cos_s > 0.0f) {
                     if (!have_surf) surf = surface_color(S, m, h);
+                    have_surf = true;
                     const V3 brdf = surf * (1.0f / kPi);
                     const V3 col = {S.directional.color[0], S.directional.color[1], S.directional.color[2]};
                     const V3 direct = T * brdf * col * S.directional.intensity * cos_s;
                     c_sun = vmin(direct, ff);
                     dir_sun = to;
                     want_dir = true;
+                }
+            }
+            // Environment NEE (device addition, off unless the job asks): one
+            // importance-sampled direction, balance-heuristic MIS against the
+            // cosine lobe (pdf cos/pi, the pdf scatter records), unclamped like
+            // the miss term it shares the estimate with.  Plastic's diffuse
+            // lobe is chosen with probability 1 - F (Material.cpp:235-260), so
+            // its NEE carries that factor.  The last depth gets none: the ray
+            // it would share with is never traced (.cpp:154), so the mean stays
+            // the miss-only estimator's.
+            if (J.env_nee && S.env_alias_prob && depth + 1 < J.max_depth &&
+                (m.type == WF_MATERIAL_DIFFUSE || m.type == WF_MATERIAL_PLASTIC)) {
+                Stream er(seed_lo, seed_hi, kPurposeEnvironment, (uint32_t)depth, (uint32_t)pixel,
+                          (uint32_t)sample);
+                const float x1 = er.next();
+                const float x2 = er.next();
+                const float x3 = er.next();
+                const float x4 = er.next();
+                const V3 wi = env_sample(S, x1, x2, x3, x4);
+                const float cos_s = dot(h.n, wi);
+                const float pe = env_pdf(S, wi);
+                if (cos_s > 0.0f && pe > 0.0f) {
+                    if (!have_surf) surf = surface_color(S, m, h);
+                    have_surf = true;
+                    float kd = 1.0f;
+                    if (m.type == WF_MATERIAL_PLASTIC)
+                        kd = 1.0f - schlick(fmaxf(0.0f, dot(d * -1.0f, h.n)), 1.5f);
+                    const float bp = cos_s / kPi;
+                    c_env = T * surf * (kd / kPi) * sky_color(S, wi) * (cos_s / (pe + bp));
+                    dir_env = wi;
+                    want_env = true;
                 }
             }
             // Scatter + Russian roulette (.cpp:739-796)
@@ -447,6 +486,20 @@ __global__ void __launch_bounds__(128) k_shade(DeviceScene scene0, DeviceJob job
                 sh.cr[pd] = c_sun.x; sh.cg[pd] = c_sun.y; sh.cb[pd] = c_sun.z;
                 sh.pixel[pd] = pixel;
                 sh.job[pd] = job;
+            } else {
+                atomicOr(err, 4);
+            }
+        }
+        __syncwarp();
+        int64_t pe = warp_append(sh_n, want_env);
+        if (want_env) {
+            if (pe < sh.capacity) {
+                sh.ox[pe] = p.x; sh.oy[pe] = p.y; sh.oz[pe] = p.z;
+                sh.dx[pe] = dir_env.x; sh.dy[pe] = dir_env.y; sh.dz[pe] = dir_env.z;
+                sh.dist[pe] = 1e6f;
+                sh.cr[pe] = c_env.x; sh.cg[pe] = c_env.y; sh.cb[pe] = c_env.z;
+                sh.pixel[pe] = pixel;
+                sh.job[pe] = job;
             } else {
                 atomicOr(err, 4);
             }

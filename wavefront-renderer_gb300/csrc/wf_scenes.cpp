@@ -21,6 +21,12 @@ struct wf_host_scene {
     std::vector<int32_t> idx;
     std::vector<int32_t> mesh_off, mesh_cnt, mesh_mat;
     std::vector<wf_material> mats;
+    std::vector<float> cu, cv;          // per triangle corner (only with UVs)
+    std::vector<uint8_t> has_uv;        // per mesh
+    std::vector<std::vector<uint32_t>> tex_pixels;  // RGBA8 texels
+    std::vector<wf_texture> textures;
+    std::vector<float> env;             // equirect RGB (width*height*3)
+    int32_t env_w = 0, env_h = 0;
     float look_from[3], look_at[3], up[3];
     float vfov = 40.0f;
 };
@@ -303,6 +309,260 @@ void build_config1(wf_host_scene& s, uint64_t seed, int subdiv)
     set_camera(s);
 }
 
+// --- config 2: the shading-divergence stress scene ------------------------
+
+struct LocalMesh {
+    std::vector<P3> v;
+    std::vector<int> t;  // 3 per triangle
+};
+
+LocalMesh icosphere_local(int subdiv)
+{
+    const float tt = 1.61803399f;
+    LocalMesh m;
+    m.v = {{-1, tt, 0}, {1, tt, 0}, {-1, -tt, 0}, {1, -tt, 0}, {0, -1, tt}, {0, 1, tt},
+           {0, -1, -tt}, {0, 1, -tt}, {tt, 0, -1}, {tt, 0, 1}, {-tt, 0, -1}, {-tt, 0, 1}};
+    for (P3& p : m.v) {
+        float l = std::sqrt(p.x * p.x + p.y * p.y + p.z * p.z);
+        p = {p.x / l, p.y / l, p.z / l};
+    }
+    m.t = {0, 11, 5, 0, 5, 1, 0, 1, 7, 0, 7, 10, 0, 10, 11, 1, 5, 9, 5, 11, 4, 11, 10, 2, 10, 7, 6, 7, 1, 8,
+           3, 9, 4, 3, 4, 2, 3, 2, 6, 3, 6, 8, 3, 8, 9, 4, 9, 5, 2, 4, 11, 6, 2, 10, 8, 6, 7, 9, 8, 1};
+    for (int level = 0; level < subdiv; ++level) {
+        std::unordered_map<uint64_t, int> mid;
+        auto midpoint = [&](int a, int b) {
+            uint64_t key = a < b ? ((uint64_t)a << 32 | (uint32_t)b) : ((uint64_t)b << 32 | (uint32_t)a);
+            auto it = mid.find(key);
+            if (it != mid.end()) return it->second;
+            P3 q = {(m.v[a].x + m.v[b].x) * 0.5f, (m.v[a].y + m.v[b].y) * 0.5f, (m.v[a].z + m.v[b].z) * 0.5f};
+            float l = std::sqrt(q.x * q.x + q.y * q.y + q.z * q.z);
+            m.v.push_back({q.x / l, q.y / l, q.z / l});
+            mid.emplace(key, (int)m.v.size() - 1);
+            return (int)m.v.size() - 1;
+        };
+        std::vector<int> next;
+        for (size_t i = 0; i < m.t.size(); i += 3) {
+            int a = m.t[i], b = m.t[i + 1], c = m.t[i + 2];
+            int ab = midpoint(a, b), bc = midpoint(b, c), ca = midpoint(c, a);
+            int tri[12] = {a, ab, ca, b, bc, ab, c, ca, bc, ab, bc, ca};
+            next.insert(next.end(), tri, tri + 12);
+        }
+        m.t.swap(next);
+    }
+    return m;
+}
+
+// Torus around the y axis; angles from double-precision cos/sin rounded to
+// float (the only libm use in the generators).
+LocalMesh torus_local(int nu, int nv, float R, float r)
+{
+    LocalMesh m;
+    for (int i = 0; i < nu; ++i) {
+        const double a = 2.0 * 3.14159265358979323846 * i / nu;
+        const float ca = (float)std::cos(a), sa = (float)std::sin(a);
+        for (int j = 0; j < nv; ++j) {
+            const double b = 2.0 * 3.14159265358979323846 * j / nv;
+            const float cb = (float)std::cos(b), sb = (float)std::sin(b);
+            m.v.push_back({(R + r * cb) * ca, r * sb, (R + r * cb) * sa});
+        }
+    }
+    for (int i = 0; i < nu; ++i)
+        for (int j = 0; j < nv; ++j) {
+            int a = i * nv + j, b = ((i + 1) % nu) * nv + j, c = ((i + 1) % nu) * nv + (j + 1) % nv,
+                d = i * nv + (j + 1) % nv;
+            int tri[6] = {a, b, c, a, c, d};
+            m.t.insert(m.t.end(), tri, tri + 6);
+        }
+    return m;
+}
+
+// Cube [-1,1]^3 with every face split into n x n quads.
+LocalMesh cube_local(int n)
+{
+    LocalMesh m;
+    const int axes[6][3] = {{0, 1, 2}, {0, 1, 2}, {1, 2, 0}, {1, 2, 0}, {2, 0, 1}, {2, 0, 1}};
+    for (int f = 0; f < 6; ++f) {
+        const float sgn = (f % 2) ? -1.0f : 1.0f;
+        const int base = (int)m.v.size();
+        for (int i = 0; i <= n; ++i)
+            for (int j = 0; j <= n; ++j) {
+                float c[3];
+                c[axes[f][0]] = -1.0f + 2.0f * i / n;
+                c[axes[f][1]] = -1.0f + 2.0f * j / n;
+                c[axes[f][2]] = sgn;
+                m.v.push_back({c[0], c[1], c[2]});
+            }
+        for (int i = 0; i < n; ++i)
+            for (int j = 0; j < n; ++j) {
+                int a = base + i * (n + 1) + j, b = a + n + 1, c = b + 1, d = a + 1;
+                if (sgn > 0) {
+                    int tri[6] = {a, b, c, a, c, d};
+                    m.t.insert(m.t.end(), tri, tri + 6);
+                } else {
+                    int tri[6] = {a, c, b, a, d, c};
+                    m.t.insert(m.t.end(), tri, tri + 6);
+                }
+            }
+    }
+    return m;
+}
+
+// 512x512 RGBA8 texture: a checker (even ids) or value noise (odd ids).
+std::vector<uint32_t> make_texture(int id, int size, uint64_t seed)
+{
+    std::vector<uint32_t> px((size_t)size * size);
+    uint64_t rs = seed * 977u + (uint64_t)id * 0x9E3779B97F4A7C15ull;
+    uint8_t ca[3], cb[3];
+    for (int k = 0; k < 3; ++k) {
+        ca[k] = (uint8_t)(40 + (splitmix64(rs) % 200));
+        cb[k] = (uint8_t)(40 + (splitmix64(rs) % 200));
+    }
+    const int cell = 8 + (int)(splitmix64(rs) % 56);
+    const uint32_t nseed = (uint32_t)splitmix64(rs);
+    for (int y = 0; y < size; ++y)
+        for (int x = 0; x < size; ++x) {
+            uint8_t c[3];
+            if (id % 2 == 0) {
+                const bool odd = ((x / cell) + (y / cell)) % 2;
+                for (int k = 0; k < 3; ++k) c[k] = odd ? ca[k] : cb[k];
+            } else {
+                float nz = 0.5f + 0.5f * fbm(x * 0.02f, y * 0.02f, 0.5f, nseed);
+                nz = std::fmin(1.0f, std::fmax(0.0f, nz));
+                for (int k = 0; k < 3; ++k) c[k] = (uint8_t)(ca[k] * nz + cb[k] * (1.0f - nz));
+            }
+            px[(size_t)y * size + x] = (uint32_t)c[0] | ((uint32_t)c[1] << 8) | ((uint32_t)c[2] << 16) | 0xFF000000u;
+        }
+    return px;
+}
+
+// Equirect HDRI in the mapping of EnvironmentMap::sample (u = 0.5 +
+// atan2(z,x)/2pi, v = 0.5 - asin(y)/pi): a sky gradient, a dim ground and a
+// sun lobe `sun` times brighter than the sky around it.
+void make_hdri(wf_host_scene& s, int w, int h, float sun)
+{
+    s.env_w = w;
+    s.env_h = h;
+    s.env.assign((size_t)w * h * 3, 0.0f);
+    const double pi = 3.14159265358979323846;
+    const double se = 35.0 * pi / 180.0, sp = 40.0 * pi / 180.0;
+    const double sx = std::cos(se) * std::cos(sp), sy = std::sin(se), sz = std::cos(se) * std::sin(sp);
+    const double cos_r = std::cos(1.5 * pi / 180.0);
+    for (int y = 0; y < h; ++y) {
+        const double elev = (0.5 - (y + 0.5) / h) * pi;
+        const double dyv = std::sin(elev), ce = std::cos(elev);
+        for (int x = 0; x < w; ++x) {
+            const double phi = ((x + 0.5) / w - 0.5) * 2.0 * pi;
+            const double dx = ce * std::cos(phi), dz = ce * std::sin(phi);
+            double r, g, b;
+            if (dyv >= 0.0) {
+                const double t = std::pow(dyv, 0.5);
+                r = 0.9 * (1 - t) + 0.25 * t;
+                g = 0.85 * (1 - t) + 0.45 * t;
+                b = 0.8 * (1 - t) + 0.9 * t;
+            } else {
+                r = 0.18;
+                g = 0.17;
+                b = 0.16;
+            }
+            const double cd = dx * sx + dyv * sy + dz * sz;
+            if (cd > cos_r) {
+                const double f = (cd - cos_r) / (1.0 - cos_r);
+                const double k = 1.0 + (sun - 1.0) * std::sqrt(f);
+                r *= k;
+                g *= k * 0.95;
+                b *= k * 0.85;
+            }
+            float* o = &s.env[((size_t)y * w + x) * 3];
+            o[0] = (float)r;
+            o[1] = (float)g;
+            o[2] = (float)b;
+        }
+    }
+}
+
+// Config 2: a grid x grid lattice of meshes (icospheres, tori, subdivided
+// cubes of ~1.3k-20k triangles) resting on a ground quad, 256 materials
+// spread evenly over Diffuse / Metal / Glass, the first 64 non-glass ones
+// textured (512^2 RGBA8 checker or noise, planar UVs), lit by an HDRI with a
+// sun lobe of 1e4.
+void build_config2(wf_host_scene& s, uint64_t seed, int grid, int tex_size, int env_w, int env_h)
+{
+    uint64_t rs = seed * 0xD1B54A32D192ED03ull + 77u;
+    auto u = [&](float lo, float hi) { return lo + (hi - lo) * uniform01(rs); };
+    const int nmat = 256, ntex = 64;
+    int textured = 0;
+    for (int m = 0; m < nmat; ++m) {
+        const int type = m % 3;
+        wf_material mt;
+        if (type == 0)
+            mt = diffuse(u(0.2f, 0.9f), u(0.2f, 0.9f), u(0.2f, 0.9f));
+        else if (type == 1)
+            mt = metal(u(0.5f, 0.95f), u(0.5f, 0.95f), u(0.5f, 0.95f), u(0.05f, 0.5f));
+        else
+            mt = glass(1.5f);
+        if (type != 2 && textured < ntex) mt.texture_id = textured++;
+        s.mats.push_back(mt);
+    }
+    const int ground_mat = (int)s.mats.size();
+    s.mats.push_back(diffuse(0.45f, 0.45f, 0.42f));
+    for (int t = 0; t < ntex; ++t) {
+        s.tex_pixels.push_back(make_texture(t, tex_size, seed));
+        s.textures.push_back(wf_texture{tex_size, tex_size, WF_TEXEL_RGBA8_SRGB, nullptr});
+    }
+    // ground
+    const float G = (float)grid;
+    begin_mesh(s, ground_mat);
+    {
+        int a = add_vertex(s, {-1, 0, -1}), b = add_vertex(s, {G + 1, 0, -1}), c = add_vertex(s, {G + 1, 0, G + 1}),
+            d = add_vertex(s, {-1, 0, G + 1});
+        int tri[6] = {a, b, c, a, c, d};
+        s.idx.insert(s.idx.end(), tri, tri + 6);
+        for (int k = 0; k < 6; ++k) {
+            s.cu.push_back(0.0f);
+            s.cv.push_back(0.0f);
+        }
+    }
+    end_mesh(s);
+    s.has_uv.push_back(0);
+    const LocalMesh shapes[9] = {icosphere_local(3), icosphere_local(4), icosphere_local(5),
+                                 torus_local(40, 26, 1.0f, 0.35f), torus_local(80, 64, 1.0f, 0.35f),
+                                 torus_local(128, 80, 1.0f, 0.35f), cube_local(10), cube_local(20), cube_local(40)};
+    for (int gz = 0; gz < grid; ++gz)
+        for (int gx = 0; gx < grid; ++gx) {
+            const float pick = uniform01(rs);
+            const int size_class = pick < 0.72f ? 0 : (pick < 0.95f ? 1 : 2);
+            const int kind = (int)(splitmix64(rs) % 3);
+            const LocalMesh& L = shapes[kind * 3 + size_class];
+            const int mat = (int)(splitmix64(rs) % nmat);
+            const float scale = u(0.28f, 0.42f);
+            const float t = u(-1.0f, 1.0f);  // rotation about y: cos/sin from tan(angle/2) = t
+            const float ca = (1.0f - t * t) / (1.0f + t * t), sa = 2.0f * t / (1.0f + t * t);
+            const float cx = gx + 0.5f + u(-0.08f, 0.08f), cz = gz + 0.5f + u(-0.08f, 0.08f);
+            const float lift = kind == 1 ? 0.35f : 1.0f;  // the torus is 0.35 tall
+            const float cy = scale * lift;
+            begin_mesh(s, mat);
+            const int base = (int)s.px.size();
+            for (const P3& p : L.v) {
+                const float x = p.x * scale, y = p.y * scale, z = p.z * scale;
+                add_vertex(s, {ca * x - sa * z + cx, y + cy, sa * x + ca * z + cz});
+            }
+            for (size_t i = 0; i < L.t.size(); ++i) {
+                s.idx.push_back(base + L.t[i]);
+                const P3& p = L.v[L.t[i]];
+                s.cu.push_back(0.5f + 0.5f * p.x);
+                s.cv.push_back(0.5f + 0.5f * p.y);
+            }
+            end_mesh(s);
+            s.has_uv.push_back(s.mats[mat].texture_id >= 0 ? 1 : 0);
+        }
+    make_hdri(s, env_w, env_h, 1.0e4f);
+    const float f[3] = {G * 0.5f, G * 0.28f, G * 1.12f}, a[3] = {G * 0.5f, 0.0f, G * 0.38f}, up[3] = {0, 1, 0};
+    std::memcpy(s.look_from, f, sizeof(f));
+    std::memcpy(s.look_at, a, sizeof(a));
+    std::memcpy(s.up, up, sizeof(up));
+    s.vfov = 50.0f;
+}
+
 // Config 3 job scenes: seeded variants of config 0 — wall, box and metal
 // albedos, metal roughness, the light quad's position on the ceiling and a
 // jitter of the camera position.
@@ -354,6 +614,12 @@ int wf_host_scene_generate(int32_t config, uint64_t seed, wf_host_scene** out)
     case 3:  // a job scene of the batched workload: variant `seed` of config 0
         build_config3(*s, seed);
         break;
+    case 2:
+        build_config2(*s, seed, 64, 512, 2048, 1024);
+        break;
+    case 102:  // small variant of config 2 (16 x 16 meshes, 128^2 textures, 256x128 HDRI)
+        build_config2(*s, seed, 16, 128, 256, 128);
+        break;
     case 100:  // small variant of config 1 (subdivision 4) for fast tests
         build_config1(*s, seed, 4);
         break;
@@ -381,6 +647,22 @@ int wf_host_scene_describe(const wf_host_scene* s, wf_scene_desc* d)
     d->mesh_material_ids = s->mesh_mat.data();
     d->num_materials = (int32_t)s->mats.size();
     d->materials = s->mats.data();
+    if (!s->cu.empty()) {
+        d->corner_u = s->cu.data();
+        d->corner_v = s->cv.data();
+        d->mesh_has_uv = s->has_uv.data();
+    }
+    if (!s->textures.empty()) {
+        auto* tex = const_cast<wf_host_scene*>(s);
+        for (size_t t = 0; t < tex->textures.size(); ++t) tex->textures[t].data = tex->tex_pixels[t].data();
+        d->num_textures = (int32_t)s->textures.size();
+        d->textures = s->textures.data();
+    }
+    if (s->env_w > 0) {
+        d->environment.width = s->env_w;
+        d->environment.height = s->env_h;
+        d->environment.rgb = s->env.data();
+    }
     d->environment.intensity_scale = 1.0f;
     d->environment.tint[0] = d->environment.tint[1] = d->environment.tint[2] = 1.0f;
     d->directional.color[0] = d->directional.color[1] = d->directional.color[2] = 1.0f;
