@@ -387,7 +387,8 @@ def test_gpu_env_nee_matches_analytic_irradiance(wf, orc, ctx):
     within 4 standard errors of 8 runs + 1e-3 relative."""
     from conftest import PlaneUnderSky
 
-    sky = PlaneUnderSky(wf, orc.scene_environment(wf.HostScene(102).desc))
+    hs = wf.HostScene(102)  # owns the map scene_environment copies
+    sky = PlaneUnderSky(wf, orc.scene_environment(hs.desc))
     ctx.upload(sky.desc)
     W = H = 64
     spp, N = 256, 8

@@ -314,7 +314,8 @@ def test_port_env_nee_matches_analytic_irradiance(wf, orc, clip):
     independent runs (plus 1e-3 relative for the finite plane)."""
     from conftest import PlaneUnderSky
 
-    env = orc.scene_environment(wf.HostScene(102).desc)
+    hs = wf.HostScene(102)  # owns the map scene_environment copies
+    env = orc.scene_environment(hs.desc)
     if clip is not None:
         env = np.minimum(env, clip)
     sky = PlaneUnderSky(wf, env)
