@@ -174,6 +174,15 @@ typedef struct wf_render_params {
      * an importance-sampled environment shadow ray at Diffuse and Plastic
      * hits and weights the misses after them: same mean, lower variance. */
     int32_t enable_env_nee;
+    /* enableAdaptiveSampling / adaptiveSamplingThreshold
+     * (WavefrontRenderer.h:31-33, AdaptiveSampler.h:27-105): per-pixel
+     * Welford statistics of each sample's luminance, a convergence check
+     * after every 16th sample once a pixel has 32 (standard error of the
+     * mean < threshold * (mean + 0.01)); converged pixels trace no more
+     * paths, the render stops when none is left, and each pixel is divided
+     * by its own sample count.  0 = every pixel gets samples_per_pixel. */
+    int32_t enable_adaptive_sampling;
+    float adaptive_threshold;      /* 0.05 in the reference                 */
     /* CostTracker::relativeCost per material / texture, frozen for the
      * render (include/render/CostTracker.h:42-55).  NULL = 1.0 for all. */
     const double* rel_cost_material;
@@ -197,6 +206,8 @@ typedef struct wf_render_stats {
     int32_t waves;              /* wavefronts launched                    */
     int32_t bounces;            /* bounce iterations over all waves       */
     int64_t kernel_launches;    /* kernels this library launched          */
+    int32_t samples_run;        /* samplesActuallyRun (adaptive stop)     */
+    int32_t active_pixels;      /* pixels still unconverged at the end    */
 } wf_render_stats;
 
 /* ---- library / context ------------------------------------------------------- */
@@ -387,6 +398,11 @@ int wf_render_accumulate(wf_ctx* ctx, const wf_render_params* params, float* acc
 int wf_render_device(wf_ctx* ctx, const wf_render_params* params, wf_render_stats* stats);
 /* Copies the image of the last wf_render_device (width*height*3 floats). */
 int wf_image_download(wf_ctx* ctx, float* image_rgb, int64_t num_floats);
+
+/* Per-pixel sample counts of the last render (AdaptiveSampler::
+ * getSampleCount, AdaptiveSampler.h:85-88): width*height int32 values.  Every
+ * pixel holds samples_per_pixel when the render was not adaptive. */
+int wf_adaptive_sample_counts(wf_ctx* ctx, int32_t* counts, int64_t num_pixels);
 
 /* The context's CUDA stream (a cudaStream_t), so a caller can record its own
  * events around library calls. */

@@ -91,6 +91,8 @@ def port_lib() -> C.CDLL:
                                  [C.c_int32, C.POINTER(wf.WfMaterial), C.c_int32, i64p, f64p, f64p, i32p], None),
         "orc_render_window": ([V, C.POINTER(wf.WfRenderParams), C.c_int32, C.c_int32, C.c_int32, C.c_int32,
                                C.c_int32, f32p, C.POINTER(OrcCounters)], None),
+        "orc_render_window_counts": ([V, C.POINTER(wf.WfRenderParams), C.c_int32, C.c_int32, C.c_int32,
+                                      C.c_int32, C.c_int32, f32p, i32p, C.POINTER(OrcCounters)], None),
         "orc_cost_tracker_relative": ([C.c_int32, C.c_int64, i32p, f64p, f64p], None),
     }
     for name, (args, res) in sig.items():
@@ -142,9 +144,16 @@ class Port:
                                     ptr(out, C.c_uint8))
         return out
 
-    def render_window(self, params, x0, y0, w, h, threads=0):
+    def render_window(self, params, x0, y0, w, h, threads=0, counts=False):
+        """Per-pixel sums of the window; with counts=True also each pixel's
+        sample count (adaptive sampling stops pixels early)."""
         acc = np.zeros(w * h * 3, np.float32)
         cnt = OrcCounters()
+        if counts:
+            n = np.zeros(w * h, np.int32)
+            self.lib.orc_render_window_counts(self.h, C.byref(params), x0, y0, w, h, threads, ptr(acc),
+                                              ptr(n, C.c_int32), C.byref(cnt))
+            return acc.reshape(h, w, 3), {k: getattr(cnt, k) for k, _ in OrcCounters._fields_}, n.reshape(h, w)
         self.lib.orc_render_window(self.h, C.byref(params), x0, y0, w, h, threads, ptr(acc), C.byref(cnt))
         return acc.reshape(h, w, 3), {k: getattr(cnt, k) for k, _ in OrcCounters._fields_}
 
@@ -264,6 +273,7 @@ def ref_lib() -> C.CDLL:
                                   C.c_longlong, i32p, f64p, C.c_longlong, i32p, f64p, C.c_int, i32p], None),
         "ref_render": ([V, f32p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_float, C.c_char_p, f32p],
                        None),
+        "ref_render_adaptive": ([V, f32p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_float, f32p], None),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -314,6 +324,17 @@ class Ref:
         cam12 = np.ascontiguousarray(cam12, np.float32)
         env = str(env_path).encode() if env_path else None
         self.lib.ref_render(self.h, ptr(cam12), w, h, spp, max_depth, policy, int(ray_sort), firefly, env, ptr(img))
+        return img.reshape(h, w, 3)
+
+
+    def render_adaptive(self, cam12, w, h, spp, max_depth, threshold=0.05, seed=1, threads=0):
+        """renderScene with the reference's AdaptiveSampler on."""
+        if threads:
+            self.lib.ref_set_threads(threads)
+        self.lib.ref_set_seed(seed)
+        img = np.zeros(w * h * 3, np.float32)
+        cam12 = np.ascontiguousarray(cam12, np.float32)
+        self.lib.ref_render_adaptive(self.h, ptr(cam12), w, h, spp, max_depth, threshold, ptr(img))
         return img.reshape(h, w, 3)
 
 

@@ -319,4 +319,33 @@ void ref_render(void* sp, const float c12[12], int w, int h, int spp, int max_de
     }
 }
 
+// renderScene in the reference's default sampling mode: adaptive sampling
+// on (threshold as given), cost-aware RR off, no ray sort.
+void ref_render_adaptive(void* sp, const float c12[12], int w, int h, int spp, int max_depth, float threshold,
+                         float* image_out)
+{
+    Scene* s = (Scene*)sp;
+    Camera cam = camera_from12(c12);
+    Image img(w, h);
+    WavefrontRenderer r(spp, max_depth, SchedulingPolicy::None);
+    r.enableAdaptiveSampling = true;
+    r.adaptiveSamplingThreshold = threshold;
+    r.enableCostAwareRR = false;
+    r.enableRaySort = false;
+    r.enableSampleLogging = true;
+    void (*old_term)(int) = std::signal(SIGTERM, SIG_DFL);
+    void (*old_int)(int) = std::signal(SIGINT, SIG_DFL);
+    {
+        Silence q;
+        r.renderScene(*s, cam, img);
+    }
+    std::signal(SIGTERM, old_term);
+    std::signal(SIGINT, old_int);
+    for (int i = 0; i < w * h; ++i) {
+        image_out[3 * i] = img.pixels[i].x;
+        image_out[3 * i + 1] = img.pixels[i].y;
+        image_out[3 * i + 2] = img.pixels[i].z;
+    }
+}
+
 }  // extern "C"

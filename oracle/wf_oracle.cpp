@@ -1271,6 +1271,20 @@ void orc_shading_schedule(int32_t policy, int64_t n, const int32_t* mat_ids,
 void orc_render_window(const orc_scene* S, const wf_render_params* P, int32_t x0, int32_t y0,
                        int32_t w, int32_t h, int32_t threads, float* accum, orc_counters* counters)
 {
+    orc_render_window_counts(S, P, x0, y0, w, h, threads, accum, nullptr, counters);
+}
+
+// renderScene's AdaptiveSampler per pixel (AdaptiveSampler.h:41-78 and
+// WavefrontRenderer.cpp:270-294): a pixel's samples run in order; after each
+// one luminance(sum after - sum before) feeds Welford's update, and after
+// every 16th sample, from 32 on, the pixel stops once the standard error of
+// its mean is below threshold * (mean + 0.01).  Pixels are independent (the
+// reference's early exit only fires when every pixel has stopped), so the
+// port runs the rule pixel by pixel.
+void orc_render_window_counts(const orc_scene* S, const wf_render_params* P, int32_t x0, int32_t y0,
+                              int32_t w, int32_t h, int32_t threads, float* accum, int32_t* counts,
+                              orc_counters* counters)
+{
     if (threads <= 0) threads = (int)std::max(1u, std::thread::hardware_concurrency());
     std::atomic<int> next_row{0};
     std::vector<orc_counters> per(threads);
@@ -1282,8 +1296,30 @@ void orc_render_window(const orc_scene* S, const wf_render_params* P, int32_t x0
             if (r >= h) break;
             for (int c = 0; c < w; ++c) {
                 float acc[3] = {0.0f, 0.0f, 0.0f};
-                for (int s = 0; s < P->samples_per_pixel; ++s)
-                    render_path(*S, *P, x0 + c, y0 + r, P->first_sample + s, acc, cnt);
+                int n = 0;
+                if (P->enable_adaptive_sampling) {
+                    float mean = 0.0f, m2 = 0.0f;
+                    for (int s = 0; s < P->samples_per_pixel; ++s) {
+                        const float b0 = acc[0], b1 = acc[1], b2 = acc[2];
+                        render_path(*S, *P, x0 + c, y0 + r, P->first_sample + s, acc, cnt);
+                        const float lum = 0.2126f * (acc[0] - b0) + 0.7152f * (acc[1] - b1) + 0.0722f * (acc[2] - b2);
+                        n += 1;
+                        const float d1 = lum - mean;
+                        mean += d1 / (float)n;
+                        const float d2 = lum - mean;
+                        m2 += d1 * d2;
+                        if ((s + 1) % 16 == 0 && n >= 32) {
+                            const float var = m2 / (float)(n - 1);
+                            const float se = std::sqrt(var / (float)n);
+                            if (se < P->adaptive_threshold * (mean + 0.01f)) break;
+                        }
+                    }
+                } else {
+                    for (int s = 0; s < P->samples_per_pixel; ++s)
+                        render_path(*S, *P, x0 + c, y0 + r, P->first_sample + s, acc, cnt);
+                    n = P->samples_per_pixel;
+                }
+                if (counts) counts[(size_t)r * w + c] = n;
                 size_t k = 3 * ((size_t)r * w + c);
                 accum[k + 0] = acc[0];
                 accum[k + 1] = acc[1];

@@ -111,6 +111,11 @@ typedef struct orc_counters {
 void orc_render_window(const orc_scene* scene, const wf_render_params* params, int32_t x0,
                        int32_t y0, int32_t w, int32_t h, int32_t threads, float* accum_rgb,
                        orc_counters* counters);
+/* Same with AdaptiveSampler when params->enable_adaptive_sampling: counts
+ * (w*h, may be null) receives each pixel's sample count. */
+void orc_render_window_counts(const orc_scene* scene, const wf_render_params* params, int32_t x0, int32_t y0,
+                              int32_t w, int32_t h, int32_t threads, float* accum, int32_t* counts,
+                              orc_counters* counters);
 
 /* CostTracker (include/render/CostTracker.h:8-63): feeds cost samples
  * (id, ns) in order and returns relativeCost for every id. */

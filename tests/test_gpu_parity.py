@@ -416,3 +416,36 @@ def test_gpu_env_nee_matches_oracle_paths(wf, orc, ctx, scene_c2small):
     assert agree >= 0.98, agree
     assert _mean_close(img, ref, 0.01)
     assert abs(int(st["shadow_rays"]) - int(cnt["shadow_rays"])) <= 0.01 * cnt["shadow_rays"]
+
+
+# ------------------------------------------------ adaptive sampling --------
+
+@pytest.mark.parametrize("spw", [0, 4])
+def test_gpu_adaptive_matches_oracle(wf, orc, ctx, scene0, spw):
+    """AdaptiveSampler on the GPU: each pixel's sample count and image equal
+    the port's (same random streams; the Welford inputs differ only by the
+    order of float additions, so a stop may move by one check on a few
+    pixels).  Tolerance: counts equal on 99% of pixels, image within 1e-3
+    relative + 1e-4 on 98%."""
+    ctx.upload(scene0.desc)
+    port = orc.Port(scene0.desc)
+    W = H = 64
+    spp = 64
+    cam = scene0.camera(W, H)
+    p = wf.render_params(W, H, spp, 8, cam, seed=31, adaptive=True, adaptive_threshold=0.1, spp_per_wave=spw)
+    img, st = ctx.render(p)
+    counts = ctx.sample_counts(W, H)
+    acc, _, pc = port.render_window(p, 0, 0, W, H, counts=True)
+    assert (counts == pc).mean() >= 0.99
+    assert (counts < spp).mean() > 0.2
+    ref = acc / np.maximum(pc, 1)[..., None]
+    assert np.isclose(img, ref, rtol=1e-3, atol=1e-4).all(axis=2).mean() >= 0.98
+    assert st["samples_run"] == spp or (counts < spp).all()
+    assert st["active_pixels"] <= int((counts == spp).sum())
+
+
+def test_gpu_adaptive_off_counts_are_spp(wf, ctx, scene0):
+    ctx.upload(scene0.desc)
+    cam = scene0.camera(16, 16)
+    ctx.render(wf.render_params(16, 16, 4, 8, cam, seed=3))
+    assert (ctx.sample_counts(16, 16) == 4).all()

@@ -355,3 +355,33 @@ def test_port_env_nee_mean_matches_reference_live(wf, orc, tmp_path):
     live = var > 1e-12
     z = (P.mean(0) - R.mean(0))[live] / np.sqrt(var[live])
     assert (np.abs(z) > 3).mean() < 0.02
+
+
+# ------------------------------------------------ adaptive sampling --------
+
+def test_port_adaptive_statistics_match_reference_live(wf, orc, scene0):
+    """The reference's default sampling mode (AdaptiveSampler on): the
+    port's per-pixel means over 12 runs agree with the reference's
+    (|z| > 3 on < 1.5% of pixel channels, variance ratio within 20%), and
+    pixels do stop early."""
+    if not orc.ref_available():
+        pytest.skip("reference checkout not present")
+    ref = orc.Ref(scene0.desc, True)
+    port = orc.Port(scene0.desc)
+    W = H = 32
+    spp, N, thr = 64, 12, 0.1
+    cam = scene0.camera(W, H)
+    runs = [port.render_window(wf.render_params(W, H, spp, 8, cam, seed=900 + k, adaptive=True,
+                                                adaptive_threshold=thr), 0, 0, W, H, counts=True)
+            for k in range(N)]
+    P = np.array([a / np.maximum(n, 1)[..., None] for a, _, n in runs], np.float64)
+    counts = np.array([n for _, _, n in runs])
+    assert (counts < spp).mean() > 0.2 and counts.min() >= 32
+    assert set(np.unique(counts)) <= {32, 48, 64}
+    R = np.array([ref.render_adaptive(cam.as_array(), W, H, spp, 8, thr, seed=700 + k) for k in range(N)],
+                 np.float64)
+    var = P.var(0, ddof=1) / N + R.var(0, ddof=1) / N
+    live = var > 1e-12
+    z = (P.mean(0) - R.mean(0))[live] / np.sqrt(var[live])
+    assert (np.abs(z) > 3).mean() < 0.015
+    assert abs(np.median(P.var(0) / (R.var(0) + 1e-30)) - 1.0) < 0.2

@@ -92,6 +92,7 @@ class WfRenderParams(C.Structure):
                 ("enable_ray_sort", C.c_int32), ("enable_cost_aware_rr", C.c_int32),
                 ("firefly_threshold", C.c_float), ("seed_lo", C.c_uint32), ("seed_hi", C.c_uint32),
                 ("first_sample", C.c_int32), ("spp_per_wave", C.c_int32), ("enable_env_nee", C.c_int32),
+                ("enable_adaptive_sampling", C.c_int32), ("adaptive_threshold", C.c_float),
                 ("rel_cost_material", f64p), ("rel_cost_texture", f64p), ("camera", WfCamera)]
 
 
@@ -100,7 +101,7 @@ class WfRenderStats(C.Structure):
                 ("misses", C.c_uint64), ("sorted_elements", C.c_uint64), ("ms_total", C.c_double),
                 ("ms_ray_sort", C.c_double), ("ms_intersect", C.c_double), ("ms_shade", C.c_double),
                 ("ms_schedule", C.c_double), ("waves", C.c_int32), ("bounces", C.c_int32),
-                ("kernel_launches", C.c_int64)]
+                ("kernel_launches", C.c_int64), ("samples_run", C.c_int32), ("active_pixels", C.c_int32)]
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}
@@ -224,6 +225,7 @@ def _declare(lib: C.CDLL) -> None:
         "wf_render_accumulate": ([V, C.POINTER(WfRenderParams), f32p, C.POINTER(WfRenderStats)], C.c_int),
         "wf_render_device": ([V, C.POINTER(WfRenderParams), C.POINTER(WfRenderStats)], C.c_int),
         "wf_image_download": ([V, f32p, C.c_int64], C.c_int),
+        "wf_adaptive_sample_counts": ([V, i32p, C.c_int64], C.c_int),
         "wf_get_stream": ([V, C.POINTER(V)], C.c_int),
         "wf_timer_begin": ([V], C.c_int),
         "wf_set_tuning": ([V, C.POINTER(WfTuning)], C.c_int),
@@ -378,7 +380,7 @@ class Server:
 def render_params(width, height, spp, max_depth, camera: WfCamera, *, policy=0, ray_sort=False,
                   rr_min_depth=3, firefly=10.0, seed=1, first_sample=0, spp_per_wave=0,
                   cost_aware_rr=False, rel_cost_material=None, rel_cost_texture=None,
-                  env_nee=False) -> WfRenderParams:
+                  env_nee=False, adaptive=False, adaptive_threshold=0.05) -> WfRenderParams:
     p = WfRenderParams()
     p.width, p.height, p.samples_per_pixel, p.max_depth = width, height, spp, max_depth
     p.rr_min_depth, p.policy, p.enable_ray_sort = rr_min_depth, policy, int(bool(ray_sort))
@@ -387,6 +389,8 @@ def render_params(width, height, spp, max_depth, camera: WfCamera, *, policy=0, 
     p.seed_lo, p.seed_hi = seed & 0xFFFFFFFF, (seed >> 32) & 0xFFFFFFFF
     p.first_sample, p.spp_per_wave = first_sample, spp_per_wave
     p.enable_env_nee = int(bool(env_nee))
+    p.enable_adaptive_sampling = int(bool(adaptive))
+    p.adaptive_threshold = adaptive_threshold
     p._keep = []
     if rel_cost_material is not None:
         a = np.ascontiguousarray(rel_cost_material, dtype=np.float64)
@@ -506,6 +510,13 @@ class Context:
         img = out if out is not None else np.zeros(width * height * 3, dtype=np.float32)
         _check(load_library().wf_image_download(self._h, ptr(img), img.size), "wf_image_download", self)
         return img.reshape(height, width, 3)
+
+    def sample_counts(self, width: int, height: int) -> np.ndarray:
+        """Per-pixel sample counts of the last render (adaptive sampling)."""
+        n = np.zeros(width * height, dtype=np.int32)
+        _check(load_library().wf_adaptive_sample_counts(self._h, ptr(n, C.c_int32), n.size),
+               "wf_adaptive_sample_counts", self)
+        return n.reshape(height, width)
 
     def set_tuning(self, trace_variant: int = 0, persistent_blocks_per_sm: int = 0, graph_mode: int = 0) -> None:
         t = WfTuning(trace_variant, persistent_blocks_per_sm, graph_mode)

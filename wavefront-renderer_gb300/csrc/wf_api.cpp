@@ -105,6 +105,26 @@ int ensure_arena(wf_ctx* c, int64_t floats)
     return WF_OK;
 }
 
+int ensure_adaptive(wf_ctx* c, int64_t np, int64_t buf_floats)
+{
+    if (np <= c->ad_np_cap && buf_floats <= c->ad_buf_cap) return WF_OK;
+    drop_graphs(c);
+    free_all(c->adaptive_allocs);
+    c->ad_np_cap = c->ad_buf_cap = 0;
+    auto& A = c->adaptive_allocs;
+    const size_t n = (size_t)np;
+    WF_CK(c, wf_dalloc(A, &c->ad_mean, n));
+    WF_CK(c, wf_dalloc(A, &c->ad_m2, n));
+    WF_CK(c, wf_dalloc(A, &c->ad_count, n));
+    WF_CK(c, wf_dalloc(A, &c->ad_active, n));
+    WF_CK(c, wf_dalloc(A, &c->ad_flag, n));
+    WF_CK(c, wf_dalloc(A, &c->ad_nactive, 1));
+    WF_CK(c, wf_dalloc(A, &c->ad_buf, (size_t)buf_floats));
+    c->ad_np_cap = np;
+    c->ad_buf_cap = buf_floats;
+    return WF_OK;
+}
+
 int ensure_job_tables(wf_ctx* c, int jobs, int chunks)
 {
     if (jobs > c->jobs_cap) {
@@ -701,6 +721,7 @@ int wf_destroy(wf_ctx* c)
     for (auto& r : c->scenes) free_scene_res(r);
     free_all(c->render_allocs);
     free_all(c->rel_cost_allocs);
+    free_all(c->adaptive_allocs);
     cudaFree(c->d_scene_table);
     cudaFree(c->d_jobs);
     cudaFree(c->d_chunks);

@@ -94,6 +94,18 @@ struct wf_ctx {
     float* image = nullptr;
     int64_t image_floats = 0;
 
+    // Adaptive sampling state (AdaptiveSampler) of the last single render:
+    // per-pixel Welford mean / M2 / count, active flags and list, and the
+    // per-sample sums of one wave.
+    std::vector<void*> adaptive_allocs;
+    int64_t ad_np_cap = 0, ad_buf_cap = 0;
+    float *ad_mean = nullptr, *ad_m2 = nullptr, *ad_buf = nullptr;
+    int32_t *ad_count = nullptr, *ad_active = nullptr, *ad_nactive = nullptr;
+    uint8_t* ad_flag = nullptr;
+    bool last_adaptive = false;
+    int64_t last_np = 0;
+    int32_t last_spp = 0;
+
     std::vector<wf::CapturedWave> graphs;
 
     cudaEvent_t ev[8]{};
@@ -109,6 +121,7 @@ LaunchCfg persist_cfg(const wf_ctx* c);
 LaunchCfg wide_cfg(const wf_ctx* c);
 int ensure_render_buffers(wf_ctx* c, int64_t paths);
 int ensure_arena(wf_ctx* c, int64_t floats);
+int ensure_adaptive(wf_ctx* c, int64_t np, int64_t buf_floats);
 int ensure_job_tables(wf_ctx* c, int jobs, int chunks);
 int sync_scene_table(wf_ctx* c);
 int check_device_flag(wf_ctx* c);

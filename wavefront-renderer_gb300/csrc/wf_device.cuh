@@ -146,7 +146,28 @@ struct DeviceJob {
     int64_t accum_offset;            // float index of the job's first pixel sum
     const float* rel_cost_material;  // float(relativeCost) per material, or null
     wf_camera camera;
+    // Adaptive sampling: the wave's contributions land in per-sample sums
+    // sample_buf[(sample - sample0) % wave_spp][pixel] (folded into the pixel
+    // sums in sample order after the wave), and the camera draws only the
+    // pixels of `active` (the chunk gives their count).  Null when off.
+    float* sample_buf;
+    const int32_t* active;
+    int32_t sample0;
+    int32_t wave_spp;
 };
+
+// Where a path's contributions go: the job's pixel sums, or with adaptive
+// sampling the per-sample slot of its pixel.
+__device__ __forceinline__ float* job_accum(const DeviceJob& J, float* arena)
+{
+    return J.sample_buf ? J.sample_buf : arena + J.accum_offset;
+}
+
+__device__ __forceinline__ int32_t job_slot(const DeviceJob& J, int32_t pixel, int32_t sample)
+{
+    if (!J.sample_buf) return pixel;
+    return ((sample - J.sample0) % J.wave_spp) * (J.width * J.height) + pixel;
+}
 
 // One slice of a wave: samples [first_sample, first_sample + nspp) of every
 // pixel of a job, as paths [path_offset, path_offset + width*height*nspp).
@@ -154,7 +175,7 @@ struct WaveChunk {
     int32_t job;
     int32_t first_sample;
     int32_t nspp;
-    int32_t pad;
+    int32_t active_count;  // > 0: paths cover job.active[0 .. active_count)
     int64_t path_offset;
 };
 

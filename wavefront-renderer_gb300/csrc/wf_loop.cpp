@@ -16,6 +16,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cstdint>
 #include <cstring>
 #include <deque>
 #include <map>
@@ -288,6 +289,12 @@ int validate_params(wf_ctx* c, const wf_render_params* P)
     j.height = P->height;
     j.samples_per_pixel = P->samples_per_pixel;
     j.max_depth = P->max_depth;
+    if (P->enable_adaptive_sampling) {
+        if (!(P->adaptive_threshold > 0.0f))
+            return set_err(c, WF_ERR_INVALID_ARGUMENT, "adaptive_threshold must be > 0");
+        if ((int64_t)P->width * P->height * 16 > INT32_MAX)
+            return set_err(c, WF_ERR_INVALID_ARGUMENT, "adaptive sampling needs width*height*16 < 2^31");
+    }
     return validate_job(c, j);
 }
 
@@ -300,6 +307,12 @@ int render_single(wf_ctx* c, const wf_render_params* P, wf_render_stats* st)
     const int64_t np = (int64_t)W * H;
     int spw = P->spp_per_wave > 0 ? P->spp_per_wave : (int)std::max<int64_t>(1, c->paths_per_wave / np);
     spw = std::max(1, std::min(spw, P->samples_per_pixel));
+    const bool adaptive = P->enable_adaptive_sampling != 0;
+    if (adaptive) {  // waves end on the convergence checks (every 16th sample)
+        int p2 = 1;
+        while (p2 * 2 <= std::min(spw, 16)) p2 *= 2;
+        spw = p2;
+    }
     int rc = ensure_render_buffers(c, np * spw);
     if (rc) return rc;
     rc = ensure_arena(c, 3 * np);
@@ -325,28 +338,70 @@ int render_single(wf_ctx* c, const wf_render_params* P, wf_render_stats* st)
     std::vector<DeviceJob> table(1);
     rc = make_device_job(c, j, 0, table[0]);
     if (rc) return rc;
+    int64_t kernels_setup = 0;
+    if (adaptive) {
+        rc = ensure_adaptive(c, np, 3 * np * spw);
+        if (rc) return rc;
+        table[0].sample_buf = c->ad_buf;
+        table[0].active = c->ad_active;
+        table[0].sample0 = P->first_sample;
+        table[0].wave_spp = spw;
+        WF_CK(c, cudaMemsetAsync(c->ad_buf, 0, sizeof(float) * 3 * (size_t)(np * spw), s));
+        WF_CK(c, cudaMemsetAsync(c->ad_mean, 0, sizeof(float) * (size_t)np, s));
+        WF_CK(c, cudaMemsetAsync(c->ad_m2, 0, sizeof(float) * (size_t)np, s));
+        WF_CK(c, cudaMemsetAsync(c->ad_count, 0, sizeof(int32_t) * (size_t)np, s));
+        WF_CK(c, cudaMemsetAsync(c->ad_flag, 1, (size_t)np, s));
+        launch_fill_i32(c->ad_active, np, 0, true, s);
+        kernels_setup = 1;
+    }
     rc = upload_jobs(c, table);
     if (rc) return rc;
     WF_CK(c, cudaMemsetAsync(c->arena, 0, sizeof(float) * 3 * (size_t)np, s));
     const bool graph = use_graph(c, false, P->policy);
     wf_render_stats stats{};
+    stats.kernel_launches = kernels_setup;
     if (graph) {
         rc = zero_tally(c);
         if (rc) return rc;
     }
     float ms = 0.0f;
+    int32_t n_active = (int32_t)np;
+    int samples_run = P->samples_per_pixel;
     WF_CK(c, cudaEventRecord(c->ev[0], s));
     for (int s0 = 0; s0 < P->samples_per_pixel; s0 += spw) {
         const int nspp = std::min(spw, P->samples_per_pixel - s0);
+        const int64_t pix = adaptive ? (int64_t)n_active : np;
         std::vector<WaveChunk> ch(1);
-        ch[0] = WaveChunk{0, P->first_sample + s0, nspp, 0, 0};
-        rc = upload_wave(c, ch, np * nspp);
+        ch[0] = WaveChunk{0, P->first_sample + s0, nspp, adaptive ? n_active : 0, 0};
+        rc = upload_wave(c, ch, pix * nspp);
         if (rc) return rc;
         rc = graph ? wave_graph(c, P->max_depth, P->enable_ray_sort != 0, stats)
-                   : wave_host(c, np * nspp, P->max_depth, P->policy, P->enable_ray_sort != 0, 0,
+                   : wave_host(c, pix * nspp, P->max_depth, P->policy, P->enable_ray_sort != 0, 0,
                                P->rel_cost_material, P->rel_cost_texture, &table[0], stats);
         if (rc) return rc;
+        if (adaptive) {  // renderScene's per-sample adaptive block (.cpp:270-294)
+            launch_adaptive_fold(c->ad_buf, np, nspp, c->arena, c->ad_mean, c->ad_m2, c->ad_count, c->ad_active,
+                                 n_active, s);
+            stats.kernel_launches += 1;
+            if ((s0 + nspp) % 16 == 0) {
+                launch_adaptive_check(c->ad_mean, c->ad_m2, c->ad_count, c->ad_active, n_active,
+                                      P->adaptive_threshold, c->ad_flag, s);
+                launch_compact_active(c->ad_flag, np, c->ad_active, c->ad_nactive, s);
+                stats.kernel_launches += 2;
+                WF_CK(c, cudaMemcpyAsync(&n_active, c->ad_nactive, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+                WF_CK(c, cudaStreamSynchronize(s));
+                if (n_active == 0) {
+                    samples_run = s0 + nspp;
+                    break;
+                }
+            }
+        }
     }
+    stats.samples_run = samples_run;
+    stats.active_pixels = adaptive ? n_active : (int32_t)np;
+    c->last_adaptive = adaptive;
+    c->last_np = np;
+    c->last_spp = samples_run;
     WF_CK(c, cudaEventRecord(c->ev[1], s));
     WF_CK(c, cudaEventSynchronize(c->ev[1]));
     WF_CK(c, cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]));
@@ -477,6 +532,29 @@ int finish_job(wf_server* sv, int64_t id, ServedJob& j)
 // ===========================================================================
 extern "C" {
 
+namespace {
+
+// writeAveragedImage (.cpp:127-137) into the context's image buffer.
+int finalize_image(wf_ctx* c, const wf_render_params* P, wf_render_stats* st)
+{
+    const int64_t np = (int64_t)P->width * P->height, nf = 3 * np;
+    if (nf > c->image_floats) {
+        cudaFree(c->image);
+        c->image = nullptr;
+        c->image_floats = 0;
+        WF_CK(c, cudaMalloc(&c->image, sizeof(float) * nf));
+        c->image_floats = nf;
+    }
+    if (c->last_adaptive)
+        launch_finalize_counts(c->arena, c->ad_count, np, c->image, c->stream);
+    else
+        launch_finalize(c->arena, nf, (float)P->samples_per_pixel, c->image, c->stream);
+    if (st) st->kernel_launches += 1;
+    return WF_OK;
+}
+
+}  // namespace
+
 int wf_render(wf_ctx* c, const wf_render_params* P, float* image, wf_render_stats* st)
 {
     if (!c || !image) return set_err(c, WF_ERR_INVALID_ARGUMENT, "null argument");
@@ -486,15 +564,8 @@ int wf_render(wf_ctx* c, const wf_render_params* P, float* image, wf_render_stat
     rc = render_single(c, P, st);
     if (rc) return rc;
     const int64_t nf = 3 * (int64_t)P->width * P->height;
-    if (nf > c->image_floats) {
-        cudaFree(c->image);
-        c->image = nullptr;
-        c->image_floats = 0;
-        WF_CK(c, cudaMalloc(&c->image, sizeof(float) * nf));
-        c->image_floats = nf;
-    }
-    launch_finalize(c->arena, nf, (float)P->samples_per_pixel, c->image, c->stream);  // writeAveragedImage
-    if (st) st->kernel_launches += 1;
+    rc = finalize_image(c, P, st);
+    if (rc) return rc;
     WF_CK(c, cudaMemcpyAsync(image, c->image, sizeof(float) * nf, cudaMemcpyDeviceToHost, c->stream));
     WF_CK(c, cudaStreamSynchronize(c->stream));
     return WF_OK;
@@ -508,16 +579,21 @@ int wf_render_device(wf_ctx* c, const wf_render_params* P, wf_render_stats* st)
     cudaSetDevice(c->device);
     rc = render_single(c, P, st);
     if (rc) return rc;
-    const int64_t nf = 3 * (int64_t)P->width * P->height;
-    if (nf > c->image_floats) {
-        cudaFree(c->image);
-        c->image = nullptr;
-        c->image_floats = 0;
-        WF_CK(c, cudaMalloc(&c->image, sizeof(float) * nf));
-        c->image_floats = nf;
+    rc = finalize_image(c, P, st);
+    if (rc) return rc;
+    WF_CK(c, cudaStreamSynchronize(c->stream));
+    return WF_OK;
+}
+
+int wf_adaptive_sample_counts(wf_ctx* c, int32_t* counts, int64_t n)
+{
+    if (!c || !counts) return set_err(c, WF_ERR_INVALID_ARGUMENT, "null argument");
+    if (n != c->last_np || n <= 0) return set_err(c, WF_ERR_INVALID_ARGUMENT, "pixel count differs from the last render");
+    if (!c->last_adaptive) {
+        std::fill(counts, counts + n, c->last_spp);
+        return WF_OK;
     }
-    launch_finalize(c->arena, nf, (float)P->samples_per_pixel, c->image, c->stream);
-    if (st) st->kernel_launches += 1;
+    WF_CK(c, cudaMemcpyAsync(counts, c->ad_count, sizeof(int32_t) * (size_t)n, cudaMemcpyDeviceToHost, c->stream));
     WF_CK(c, cudaStreamSynchronize(c->stream));
     return WF_OK;
 }

@@ -72,10 +72,11 @@ __global__ void k_camera_chunks(const WaveChunk* __restrict__ chunks, const long
         }
         const WaveChunk ch = chunks[lo];
         const DeviceJob& J = jobs[ch.job];
-        const int64_t np = (int64_t)J.width * J.height;
+        const int64_t np = ch.active_count > 0 ? ch.active_count : (int64_t)J.width * J.height;
         const int64_t local = i - ch.path_offset;
         const int s = (int)(local / np);
-        const int p = (int)(local - (int64_t)s * np);
+        int p = (int)(local - (int64_t)s * np);
+        if (ch.active_count > 0) p = J.active[p];  // generatePrimaryRays' activePixels mask
         const int x = p % J.width, y = p / J.width;
         const int sample = ch.first_sample + s;
         const wf_camera& cam = J.camera;
@@ -175,9 +176,9 @@ __global__ void __launch_bounds__(128) k_occluded_api(DeviceScene S, int64_t n, 
     }
 }
 
-__device__ __forceinline__ void accum_add(float* accum, int pixel, V3 c)
+__device__ __forceinline__ void accum_add(float* accum, int32_t slot, V3 c)
 {
-    float* p = accum + 3 * (int64_t)pixel;
+    float* p = accum + 3 * (int64_t)slot;
     atomicAdd(p + 0, c.x);
     atomicAdd(p + 1, c.y);
     atomicAdd(p + 2, c.z);
@@ -237,16 +238,17 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_trace_render(DeviceScene sc
             }
         }
         if (fin && !hit) {
+            const DeviceJob& J = kMulti ? jobs[job] : job0;
             const V3 T = {rq.tr[ray], rq.tg[ray], rq.tb[ray]};
-            const int64_t off = kMulti ? jobs[job].accum_offset : job0.accum_offset;
             V3 c = T * sky_color(*S, tr.d);
             // With environment NEE the bounce that sampled this direction by
             // its BSDF (pdf > 0) shares the estimate: balance-heuristic weight.
-            if ((kMulti ? jobs[job].env_nee : job0.env_nee) && S->env_alias_prob) {
+            if (J.env_nee && S->env_alias_prob) {
                 const float ip = rq.pdf[ray];
                 if (ip > 0.0f) c = c * mis_balance(ip, env_pdf(*S, normalized(tr.d)));
             }
-            accum_add(accum + off, rq.pixel[ray], c);
+            const int32_t slot = job_slot(J, rq.pixel[ray], J.sample_buf ? rq.sample[ray] : 0);
+            accum_add(job_accum(J, accum), slot, c);
         }
         if (fin) {
             overflow = overflow || tr.overflow;
@@ -306,13 +308,13 @@ __global__ void __launch_bounds__(128) k_shade(DeviceScene scene0, DeviceJob job
         V3 p = {0, 0, 0}, dir_area = {0, 0, 0}, c_area = {0, 0, 0}, dir_sun = {0, 0, 0},
            c_sun = {0, 0, 0}, dir_env = {0, 0, 0}, c_env = {0, 0, 0}, nd = {0, 0, 0}, Tn = {0, 0, 0};
         float dist_area = 0.0f, next_pdf = 0.0f;
-        int pixel = 0, depth = 0, sample = 0, job = 0;
+        int pixel = 0, depth = 0, sample = 0, job = 0, slot = 0;
         if (active) {
             const int ri = hq.ray[k];
             job = kMulti ? rq.job[ri] : 0;
             const DeviceJob& J = kMulti ? jobs[job] : job0;
             const DeviceScene& S = kMulti ? scenes[J.scene] : scene0;
-            float* accum = accum_base + J.accum_offset;
+            float* accum = job_accum(J, accum_base);
             const float ff = J.firefly;
             const uint32_t seed_lo = J.seed_lo, seed_hi = J.seed_hi;
             const V3 o = {rq.ox[ri], rq.oy[ri], rq.oz[ri]};
@@ -322,6 +324,7 @@ __global__ void __launch_bounds__(128) k_shade(DeviceScene scene0, DeviceJob job
             pixel = rq.pixel[ri];
             depth = rq.depth[ri];
             sample = rq.sample[ri];
+            slot = job_slot(J, pixel, sample);
             HitRec h;
             rebuild_hit(S, o, d, hq.tri[k], hq.t[k], hq.bu[k], hq.bv[k], h);
             p = h.p;
@@ -338,7 +341,7 @@ __global__ void __launch_bounds__(128) k_shade(DeviceScene scene0, DeviceJob job
                     }
                 }
                 Le = vmin(Le, ff);
-                accum_add(accum, pixel, T * Le * w);
+                accum_add(accum, slot, T * Le * w);
             }
             V3 surf = {0, 0, 0};
             bool have_surf = false;
@@ -470,7 +473,7 @@ __global__ void __launch_bounds__(128) k_shade(DeviceScene scene0, DeviceJob job
                 sh.dx[pa] = dir_area.x; sh.dy[pa] = dir_area.y; sh.dz[pa] = dir_area.z;
                 sh.dist[pa] = dist_area;
                 sh.cr[pa] = c_area.x; sh.cg[pa] = c_area.y; sh.cb[pa] = c_area.z;
-                sh.pixel[pa] = pixel;
+                sh.pixel[pa] = slot;
                 sh.job[pa] = job;
             } else {
                 atomicOr(err, 4);
@@ -484,7 +487,7 @@ __global__ void __launch_bounds__(128) k_shade(DeviceScene scene0, DeviceJob job
                 sh.dx[pd] = dir_sun.x; sh.dy[pd] = dir_sun.y; sh.dz[pd] = dir_sun.z;
                 sh.dist[pd] = 1e6f;
                 sh.cr[pd] = c_sun.x; sh.cg[pd] = c_sun.y; sh.cb[pd] = c_sun.z;
-                sh.pixel[pd] = pixel;
+                sh.pixel[pd] = slot;
                 sh.job[pd] = job;
             } else {
                 atomicOr(err, 4);
@@ -498,7 +501,7 @@ __global__ void __launch_bounds__(128) k_shade(DeviceScene scene0, DeviceJob job
                 sh.dx[pe] = dir_env.x; sh.dy[pe] = dir_env.y; sh.dz[pe] = dir_env.z;
                 sh.dist[pe] = 1e6f;
                 sh.cr[pe] = c_env.x; sh.cg[pe] = c_env.y; sh.cb[pe] = c_env.z;
-                sh.pixel[pe] = pixel;
+                sh.pixel[pe] = slot;
                 sh.job[pe] = job;
             } else {
                 atomicOr(err, 4);
@@ -547,10 +550,9 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_occluded_render(DeviceScene
     tr.cur = kSentinel;
     for (;;) {
         if (ray >= 0 && tr.done()) {
-            if (tr.res.leafpos < 0) {
-                const int64_t off = kMulti ? jobs[job].accum_offset : job0.accum_offset;
-                accum_add(accum + off, sh.pixel[ray], v3(sh.cr[ray], sh.cg[ray], sh.cb[ray]));
-            }
+            if (tr.res.leafpos < 0)  // sh.pixel holds the slot (job_slot)
+                accum_add(job_accum(kMulti ? jobs[job] : job0, accum), sh.pixel[ray],
+                          v3(sh.cr[ray], sh.cg[ray], sh.cb[ray]));
             overflow = overflow || tr.overflow;
             ray = -1;
         }
@@ -849,6 +851,116 @@ __global__ void k_finalize(const float* accum, int64_t n, float spp, float* imag
         image[i] = accum[i] / spp;  // writeAveragedImage, WavefrontRenderer.cpp:127-137
 }
 
+// ---------------------------------------------------------------------------
+// Adaptive sampling (AdaptiveSampler.h:27-105 and its use in renderScene,
+// WavefrontRenderer.cpp:141-145, 270-294, 127-137).
+// ---------------------------------------------------------------------------
+
+// After a wave: every sample of every active pixel, in sample order, is added
+// to the pixel sum and luminance(sum after - sum before) goes to Welford's
+// update (AdaptiveSampler::addSample, :41-53); the slot is cleared.
+__global__ void k_adaptive_fold(float* __restrict__ sample_buf, int64_t np, int nspp, float* __restrict__ accum,
+                                float* __restrict__ mean, float* __restrict__ m2, int32_t* __restrict__ count,
+                                const int32_t* __restrict__ active, int32_t n_active)
+{
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n_active;
+         r += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t p = active[r];
+        float ar = accum[3 * p], ag = accum[3 * p + 1], ab = accum[3 * p + 2];
+        float mu = mean[p], M2 = m2[p];
+        int n = count[p];
+        for (int k = 0; k < nspp; ++k) {
+            float* b = sample_buf + 3 * ((int64_t)k * np + p);
+            const float nr = ar + b[0], ng = ag + b[1], nb = ab + b[2];
+            b[0] = 0.0f;
+            b[1] = 0.0f;
+            b[2] = 0.0f;
+            const float lum = 0.2126f * (nr - ar) + 0.7152f * (ng - ag) + 0.0722f * (nb - ab);
+            ar = nr;
+            ag = ng;
+            ab = nb;
+            n += 1;
+            const float d1 = lum - mu;
+            mu += d1 / (float)n;
+            const float d2 = lum - mu;
+            M2 += d1 * d2;
+        }
+        accum[3 * p] = ar;
+        accum[3 * p + 1] = ag;
+        accum[3 * p + 2] = ab;
+        mean[p] = mu;
+        m2[p] = M2;
+        count[p] = n;
+    }
+}
+
+// AdaptiveSampler::updateConvergence (:55-78): from 32 samples on, a pixel
+// whose standard error of the mean falls below threshold * (mean + 0.01)
+// stops.
+__global__ void k_adaptive_check(const float* __restrict__ mean, const float* __restrict__ m2,
+                                 const int32_t* __restrict__ count, const int32_t* __restrict__ active,
+                                 int32_t n_active, float threshold, uint8_t* __restrict__ flag)
+{
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n_active;
+         r += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t p = active[r];
+        const int n = count[p];
+        if (n < 32) continue;
+        const float var = m2[p] / (float)(n - 1);
+        const float se = sqrtf(var / (float)n);
+        if (se < threshold * (mean[p] + 0.01f)) flag[p] = 0;
+    }
+}
+
+// The pixels still active, in index order (one block: a ballot per warp and
+// a scan of the 32 warp counts per tile of 1024 pixels).
+__global__ void __launch_bounds__(1024) k_compact_active(const uint8_t* __restrict__ flag, int64_t np,
+                                                         int32_t* __restrict__ out, int32_t* __restrict__ n_out)
+{
+    __shared__ int warp_incl[32];
+    __shared__ int base;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (threadIdx.x == 0) base = 0;
+    __syncthreads();
+    for (int64_t t0 = 0; t0 < np; t0 += 1024) {
+        const int64_t i = t0 + threadIdx.x;
+        const bool f = i < np && flag[i] != 0;
+        const unsigned b = __ballot_sync(0xFFFFFFFFu, f);
+        if (lane == 0) warp_incl[w] = __popc(b);
+        __syncthreads();
+        if (w == 0) {
+            int v = warp_incl[lane];
+            for (int o = 1; o < 32; o <<= 1) {
+                const int u = __shfl_up_sync(0xFFFFFFFFu, v, o);
+                if (lane >= o) v += u;
+            }
+            warp_incl[lane] = v;
+        }
+        __syncthreads();
+        const int before = (w > 0 ? warp_incl[w - 1] : 0) + __popc(b & ((1u << lane) - 1u));
+        if (f) out[base + before] = (int32_t)i;
+        __syncthreads();
+        if (threadIdx.x == 0) base += warp_incl[31];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *n_out = base;
+}
+
+// writeAveragedImage with per-pixel counts (.cpp:127-137).
+__global__ void k_finalize_counts(const float* __restrict__ accum, const int32_t* __restrict__ count, int64_t np,
+                                  float* __restrict__ image)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < 3 * np;
+         i += (int64_t)gridDim.x * blockDim.x)
+        image[i] = accum[i] / (float)max(count[i / 3], 1);
+}
+
+__global__ void k_fill_i32(int32_t* __restrict__ a, int64_t n, int32_t v, int identity)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        a[i] = identity ? (int32_t)i : v;
+}
+
 inline int grid_for(int64_t n, int block, int cap)
 {
     int64_t g = (n + block - 1) / block;
@@ -1000,6 +1112,37 @@ void launch_permute_hits(HitQueueDev in, const uint32_t* perm, const ull* d_n, H
 void launch_finalize(const float* accum, int64_t n, float spp, float* image, cudaStream_t s)
 {
     k_finalize<<<grid_for(n, 256, 65535), 256, 0, s>>>(accum, n, spp, image);
+}
+
+void launch_adaptive_fold(float* sample_buf, int64_t np, int nspp, float* accum, float* mean, float* m2,
+                          int32_t* count, const int32_t* active, int32_t n_active, cudaStream_t s)
+{
+    if (n_active <= 0) return;
+    k_adaptive_fold<<<grid_for(n_active, 256, 65535), 256, 0, s>>>(sample_buf, np, nspp, accum, mean, m2, count,
+                                                                   active, n_active);
+}
+
+void launch_adaptive_check(const float* mean, const float* m2, const int32_t* count, const int32_t* active,
+                           int32_t n_active, float threshold, uint8_t* flag, cudaStream_t s)
+{
+    if (n_active <= 0) return;
+    k_adaptive_check<<<grid_for(n_active, 256, 65535), 256, 0, s>>>(mean, m2, count, active, n_active, threshold,
+                                                                    flag);
+}
+
+void launch_compact_active(const uint8_t* flag, int64_t np, int32_t* out, int32_t* n_out, cudaStream_t s)
+{
+    k_compact_active<<<1, 1024, 0, s>>>(flag, np, out, n_out);
+}
+
+void launch_finalize_counts(const float* accum, const int32_t* count, int64_t np, float* image, cudaStream_t s)
+{
+    k_finalize_counts<<<grid_for(3 * np, 256, 65535), 256, 0, s>>>(accum, count, np, image);
+}
+
+void launch_fill_i32(int32_t* a, int64_t n, int32_t v, bool identity, cudaStream_t s)
+{
+    k_fill_i32<<<grid_for(n, 256, 65535), 256, 0, s>>>(a, n, v, identity ? 1 : 0);
 }
 
 }  // namespace wf
