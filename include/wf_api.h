@@ -183,6 +183,16 @@ typedef struct wf_render_params {
      * by its own sample count.  0 = every pixel gets samples_per_pixel. */
     int32_t enable_adaptive_sampling;
     float adaptive_threshold;      /* 0.05 in the reference                 */
+    /* Live CostTracker (include/render/CostTracker.h:8-63, fed as in
+     * WavefrontRenderer.cpp:612-625, 742-760, 800-844): a quarter of the
+     * shaded hits time their scatter (and, when textured, their surface
+     * colour lookup) in SM clock cycles; after every bounce each material's
+     * and texture's mean enters its EMA (weight 0.05), and relativeCost
+     * (1.0 below 50 records) drives cost-aware RR and the material /
+     * costBenefit orders of the next bounce, as in the reference.  Takes
+     * precedence over rel_cost_*.  Single renders only. */
+    int32_t enable_cost_tracking;
+    int32_t reserved0;
     /* CostTracker::relativeCost per material / texture, frozen for the
      * render (include/render/CostTracker.h:42-55).  NULL = 1.0 for all. */
     const double* rel_cost_material;
@@ -398,6 +408,20 @@ int wf_render_accumulate(wf_ctx* ctx, const wf_render_params* params, float* acc
 int wf_render_device(wf_ctx* ctx, const wf_render_params* params, wf_render_stats* stats);
 /* Copies the image of the last wf_render_device (width*height*3 floats). */
 int wf_image_download(wf_ctx* ctx, float* image_rgb, int64_t num_floats);
+
+/* Relative costs (CostTracker::relativeCost) of the live trackers after
+ * the last render with enable_cost_tracking: num_materials doubles, then
+ * num_textures doubles (either pointer may be NULL). */
+int wf_cost_tracker_state(wf_ctx* ctx, double* rel_material, int32_t num_materials, double* rel_texture,
+                          int32_t num_textures);
+
+/* Replays recorded cost samples through the device CostTracker: for step
+ * k = 0..steps-1, every item i with counts[k*items+i] > 0 records the mean
+ * sums[k*items+i] / counts[k*items+i] (CostTracker::record), in item order;
+ * rel_out (items doubles) receives relativeCost afterwards.  The update
+ * kernel is the one the render loop runs after each bounce. */
+int wf_cost_tracker_replay(wf_ctx* ctx, int32_t items, int32_t steps, const uint64_t* sums,
+                           const uint32_t* counts, double* rel_out);
 
 /* Per-pixel sample counts of the last render (AdaptiveSampler::
  * getSampleCount, AdaptiveSampler.h:85-88): width*height int32 values.  Every

@@ -449,3 +449,60 @@ def test_gpu_adaptive_off_counts_are_spp(wf, ctx, scene0):
     cam = scene0.camera(16, 16)
     ctx.render(wf.render_params(16, 16, 4, 8, cam, seed=3))
     assert (ctx.sample_counts(16, 16) == 4).all()
+
+
+# ------------------------------------------------ live CostTracker ---------
+
+def test_gpu_cost_tracker_replay_matches_oracle(wf, orc, ctx):
+    """The device CostTracker update (run after every bounce) is the
+    reference's record/relativeCost: replaying per-step cycle sums gives the
+    port's relative costs bit for bit (EMA weight 0.05, 50-record floor)."""
+    rng = np.random.default_rng(5)
+    items, steps = 7, 160
+    counts = rng.integers(0, 40, size=(steps, items)).astype(np.uint32)
+    counts[rng.random((steps, items)) < 0.3] = 0
+    per_call = rng.integers(200, 5000, size=items)
+    sums = (counts * per_call[None, :] * rng.uniform(0.5, 1.5, size=(steps, items))).astype(np.uint64)
+    got = ctx.cost_tracker_replay(sums, counts)
+    ids, costs = [], []
+    for k in range(steps):
+        for i in range(items):
+            if counts[k, i]:
+                ids.append(i)
+                costs.append(float(sums[k, i]) / float(counts[k, i]))
+    want = orc.cost_tracker_relative(items, ids, costs)
+    assert np.array_equal(got, want)
+    assert (got != 1.0).any()
+
+
+def test_gpu_live_cost_aware_rr_is_unbiased(wf, ctx, scene0):
+    """Cost-aware RR driven by live device timings changes which paths
+    survive but not the expectation: channel means of 8 runs with and
+    without it agree within 4 standard errors."""
+    ctx.upload(scene0.desc)
+    W = H = 64
+    cam = scene0.camera(W, H)
+    def runs(**kw):
+        return np.array([ctx.render(wf.render_params(W, H, 32, 8, cam, seed=100 + k, **kw))[0].mean(axis=(0, 1))
+                         for k in range(8)], np.float64)
+    a = runs()
+    b = runs(cost_aware_rr=True, cost_tracking=True)
+    se = np.sqrt(a.var(0, ddof=1) / 8 + b.var(0, ddof=1) / 8)
+    assert np.all(np.abs(a.mean(0) - b.mean(0)) <= 4 * se + 1e-6)
+    rel_m, _ = ctx.cost_tracker_state(scene0.desc.num_materials, scene0.desc.num_textures)
+    assert np.all(rel_m > 0) and (rel_m != 1.0).any()
+
+
+@pytest.mark.parametrize("policy", [1, 3])
+def test_gpu_live_costs_only_reorder_shading(wf, ctx, scene_c2small, policy):
+    """With cost-aware RR off, live costs only change the material /
+    costBenefit orders: the image is the plain render's up to float-add
+    order."""
+    ctx.upload(scene_c2small.desc)
+    W = H = 48
+    cam = scene_c2small.camera(W, H)
+    base, _ = ctx.render(wf.render_params(W, H, 4, 8, cam, seed=9))
+    img, st = ctx.render(wf.render_params(W, H, 4, 8, cam, seed=9, policy=policy, cost_tracking=True))
+    assert np.isclose(img, base, rtol=1e-4, atol=1e-6).all(axis=2).mean() >= 0.999
+    rel_m, rel_t = ctx.cost_tracker_state(scene_c2small.desc.num_materials, scene_c2small.desc.num_textures)
+    assert np.all(rel_m > 0) and np.all(rel_t > 0)

@@ -93,6 +93,7 @@ class WfRenderParams(C.Structure):
                 ("firefly_threshold", C.c_float), ("seed_lo", C.c_uint32), ("seed_hi", C.c_uint32),
                 ("first_sample", C.c_int32), ("spp_per_wave", C.c_int32), ("enable_env_nee", C.c_int32),
                 ("enable_adaptive_sampling", C.c_int32), ("adaptive_threshold", C.c_float),
+                ("enable_cost_tracking", C.c_int32), ("reserved0", C.c_int32),
                 ("rel_cost_material", f64p), ("rel_cost_texture", f64p), ("camera", WfCamera)]
 
 
@@ -226,6 +227,9 @@ def _declare(lib: C.CDLL) -> None:
         "wf_render_device": ([V, C.POINTER(WfRenderParams), C.POINTER(WfRenderStats)], C.c_int),
         "wf_image_download": ([V, f32p, C.c_int64], C.c_int),
         "wf_adaptive_sample_counts": ([V, i32p, C.c_int64], C.c_int),
+        "wf_cost_tracker_state": ([V, f64p, C.c_int32, f64p, C.c_int32], C.c_int),
+        "wf_cost_tracker_replay": ([V, C.c_int32, C.c_int32, C.POINTER(C.c_uint64), C.POINTER(C.c_uint32), f64p],
+                                   C.c_int),
         "wf_get_stream": ([V, C.POINTER(V)], C.c_int),
         "wf_timer_begin": ([V], C.c_int),
         "wf_set_tuning": ([V, C.POINTER(WfTuning)], C.c_int),
@@ -380,7 +384,7 @@ class Server:
 def render_params(width, height, spp, max_depth, camera: WfCamera, *, policy=0, ray_sort=False,
                   rr_min_depth=3, firefly=10.0, seed=1, first_sample=0, spp_per_wave=0,
                   cost_aware_rr=False, rel_cost_material=None, rel_cost_texture=None,
-                  env_nee=False, adaptive=False, adaptive_threshold=0.05) -> WfRenderParams:
+                  env_nee=False, adaptive=False, adaptive_threshold=0.05, cost_tracking=False) -> WfRenderParams:
     p = WfRenderParams()
     p.width, p.height, p.samples_per_pixel, p.max_depth = width, height, spp, max_depth
     p.rr_min_depth, p.policy, p.enable_ray_sort = rr_min_depth, policy, int(bool(ray_sort))
@@ -391,6 +395,7 @@ def render_params(width, height, spp, max_depth, camera: WfCamera, *, policy=0, 
     p.enable_env_nee = int(bool(env_nee))
     p.enable_adaptive_sampling = int(bool(adaptive))
     p.adaptive_threshold = adaptive_threshold
+    p.enable_cost_tracking = int(bool(cost_tracking))
     p._keep = []
     if rel_cost_material is not None:
         a = np.ascontiguousarray(rel_cost_material, dtype=np.float64)
@@ -517,6 +522,27 @@ class Context:
         _check(load_library().wf_adaptive_sample_counts(self._h, ptr(n, C.c_int32), n.size),
                "wf_adaptive_sample_counts", self)
         return n.reshape(height, width)
+
+    def cost_tracker_state(self, num_materials: int, num_textures: int) -> tuple[np.ndarray, np.ndarray]:
+        """relativeCost per material and per texture of the live trackers."""
+        m = np.zeros(max(num_materials, 1), np.float64)
+        t = np.zeros(max(num_textures, 1), np.float64)
+        _check(load_library().wf_cost_tracker_state(self._h, ptr(m, C.c_double), num_materials,
+                                                    ptr(t, C.c_double) if num_textures else None, num_textures),
+               "wf_cost_tracker_state", self)
+        return m[:num_materials], t[:num_textures]
+
+    def cost_tracker_replay(self, sums: np.ndarray, counts: np.ndarray) -> np.ndarray:
+        """Feeds (steps, items) cycle sums and counts through the device
+        CostTracker; returns relativeCost per item."""
+        sums = np.ascontiguousarray(sums, np.uint64)
+        counts = np.ascontiguousarray(counts, np.uint32)
+        steps, items = sums.shape
+        out = np.zeros(items, np.float64)
+        _check(load_library().wf_cost_tracker_replay(self._h, items, steps, ptr(sums, C.c_uint64),
+                                                     ptr(counts, C.c_uint32), ptr(out, C.c_double)),
+               "wf_cost_tracker_replay", self)
+        return out
 
     def set_tuning(self, trace_variant: int = 0, persistent_blocks_per_sm: int = 0, graph_mode: int = 0) -> None:
         t = WfTuning(trace_variant, persistent_blocks_per_sm, graph_mode)

@@ -125,6 +125,61 @@ int ensure_adaptive(wf_ctx* c, int64_t np, int64_t buf_floats)
     return WF_OK;
 }
 
+namespace {
+int alloc_tracker(wf_ctx* c, CostTrackerDev& T, int cap)
+{
+    auto& A = c->cost_allocs;
+    const size_t n = (size_t)std::max(cap, 1);
+    WF_CK(c, wf_dalloc(A, &T.sum, n));
+    WF_CK(c, wf_dalloc(A, &T.cnt, n));
+    WF_CK(c, wf_dalloc(A, &T.avg, n));
+    WF_CK(c, wf_dalloc(A, &T.samples, n));
+    WF_CK(c, wf_dalloc(A, &T.init, n));
+    WF_CK(c, wf_dalloc(A, &T.total, 1));
+    WF_CK(c, wf_dalloc(A, &T.tracked, 1));
+    WF_CK(c, wf_dalloc(A, &T.rel, n));
+    WF_CK(c, wf_dalloc(A, &T.rel_f, n));
+    return WF_OK;
+}
+
+int zero_tracker(wf_ctx* c, CostTrackerDev& T, int items)
+{
+    cudaStream_t s = c->stream;
+    const size_t n = (size_t)std::max(items, 1);
+    T.items = items;
+    WF_CK(c, cudaMemsetAsync(T.sum, 0, sizeof(*T.sum) * n, s));
+    WF_CK(c, cudaMemsetAsync(T.cnt, 0, sizeof(*T.cnt) * n, s));
+    WF_CK(c, cudaMemsetAsync(T.avg, 0, sizeof(*T.avg) * n, s));
+    WF_CK(c, cudaMemsetAsync(T.samples, 0, sizeof(*T.samples) * n, s));
+    WF_CK(c, cudaMemsetAsync(T.init, 0, sizeof(*T.init) * n, s));
+    WF_CK(c, cudaMemsetAsync(T.total, 0, sizeof(*T.total), s));
+    WF_CK(c, cudaMemsetAsync(T.tracked, 0, sizeof(*T.tracked), s));
+    return WF_OK;
+}
+}  // namespace
+
+int reset_cost_trackers(wf_ctx* c, int nmat, int ntex)
+{
+    if (nmat > c->ct_mat_cap || ntex > c->ct_tex_cap) {
+        free_all(c->cost_allocs);
+        c->ct_mat = CostTrackerDev{};
+        c->ct_tex = CostTrackerDev{};
+        c->ct_mat_cap = c->ct_tex_cap = 0;
+        int rc = alloc_tracker(c, c->ct_mat, nmat);
+        if (rc) return rc;
+        rc = alloc_tracker(c, c->ct_tex, ntex);
+        if (rc) return rc;
+        c->ct_mat_cap = nmat;
+        c->ct_tex_cap = ntex;
+    }
+    int rc = zero_tracker(c, c->ct_mat, nmat);
+    if (rc) return rc;
+    rc = zero_tracker(c, c->ct_tex, ntex);
+    if (rc) return rc;
+    launch_cost_update(c->ct_mat, c->ct_tex, c->stream);  // no records yet: relativeCost 1.0
+    return WF_OK;
+}
+
 int ensure_job_tables(wf_ctx* c, int jobs, int chunks)
 {
     if (jobs > c->jobs_cap) {
@@ -722,6 +777,7 @@ int wf_destroy(wf_ctx* c)
     free_all(c->render_allocs);
     free_all(c->rel_cost_allocs);
     free_all(c->adaptive_allocs);
+    free_all(c->cost_allocs);
     cudaFree(c->d_scene_table);
     cudaFree(c->d_jobs);
     cudaFree(c->d_chunks);

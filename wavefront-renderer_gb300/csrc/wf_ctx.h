@@ -106,6 +106,11 @@ struct wf_ctx {
     int64_t last_np = 0;
     int32_t last_spp = 0;
 
+    // Live CostTrackers (materials, textures) of the last single render
+    std::vector<void*> cost_allocs;
+    wf::CostTrackerDev ct_mat{}, ct_tex{};
+    int ct_mat_cap = 0, ct_tex_cap = 0;
+
     std::vector<wf::CapturedWave> graphs;
 
     cudaEvent_t ev[8]{};
@@ -122,6 +127,9 @@ LaunchCfg wide_cfg(const wf_ctx* c);
 int ensure_render_buffers(wf_ctx* c, int64_t paths);
 int ensure_arena(wf_ctx* c, int64_t floats);
 int ensure_adaptive(wf_ctx* c, int64_t np, int64_t buf_floats);
+// Cost trackers for nmat materials and ntex textures, reset to their initial
+// state (relativeCost 1.0) on the context's stream.
+int reset_cost_trackers(wf_ctx* c, int nmat, int ntex);
 int ensure_job_tables(wf_ctx* c, int jobs, int chunks);
 int sync_scene_table(wf_ctx* c);
 int check_device_flag(wf_ctx* c);

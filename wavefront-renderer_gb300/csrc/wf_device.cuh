@@ -154,6 +154,28 @@ struct DeviceJob {
     const int32_t* active;
     int32_t sample0;
     int32_t wave_spp;
+    // Live cost tracking: this bounce's timed cycles and counts per material
+    // and per texture (null when off; single-job renders only).
+    unsigned long long* cost_sum_mat;
+    unsigned int* cost_cnt_mat;
+    unsigned long long* cost_sum_tex;
+    unsigned int* cost_cnt_tex;
+};
+
+// CostTracker state on the device (include/render/CostTracker.h:8-63).  Costs
+// are SM clock cycles instead of nanoseconds: relativeCost is a ratio, so the
+// unit cancels.
+struct CostTrackerDev {
+    unsigned long long* sum;  // per item: cycles recorded this bounce
+    unsigned int* cnt;        // per item: timed calls this bounce
+    double* avg;              // averageCostNanoseconds
+    int32_t* samples;         // sampleCount
+    int32_t* init;            // initialized
+    double* total;            // cachedTotalCost (one value)
+    int32_t* tracked;         // trackedItemCount (one value)
+    double* rel;              // relativeCost per item
+    float* rel_f;             // float(relativeCost) for RR, or null
+    int32_t items;
 };
 
 // Where a path's contributions go: the job's pixel sums, or with adaptive
@@ -211,7 +233,8 @@ enum : uint32_t {
     kPurposeLight = 2,
     kPurposeScatter = 3,
     kPurposeRoulette = 4,
-    kPurposeEnvironment = 5
+    kPurposeEnvironment = 5,
+    kPurposeCostSample = 6
 };
 
 __host__ __device__ __forceinline__ void philox10(uint32_t c[4], uint32_t k0, uint32_t k1)

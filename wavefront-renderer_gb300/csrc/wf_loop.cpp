@@ -101,8 +101,10 @@ int upload_wave(wf_ctx* c, const std::vector<WaveChunk>& chunks, int64_t total)
 // reference (RayQueue::schedule + ShadingQueue::schedule), materials of
 // scene `policy_scene`.
 int wave_host(wf_ctx* c, int64_t total, int max_depth, int policy, bool ray_sort, int policy_scene,
-              const double* rc_mat, const double* rc_tex, const DeviceJob* single_job, wf_render_stats& stats)
+              const double* rc_mat, const double* rc_tex, const DeviceJob* single_job, wf_render_stats& stats,
+              bool track_costs = false)
 {
+    std::vector<double> live_mat, live_tex;  // relativeCost of the live trackers, for the policies
     cudaStream_t s = c->stream;
     WaveTables T{c->d_scene_table, c->d_jobs, DeviceScene{}, DeviceJob{}, single_job == nullptr};
     if (single_job) {
@@ -149,6 +151,17 @@ int wave_host(wf_ctx* c, int64_t total, int max_depth, int policy, bool ray_sort
             launch_hit_columns(c->d_scene_table, c->d_jobs, c->rq[cur], c->hq[0], c->counters + 1, cm, WC, s);
             ShadeColumnsDev cd{c->col_mat, c->col_tex, c->col_tr, c->col_tg, c->col_tb, c->col_px, c->col_py, c->col_pz};
             const ResidentScene& R = c->scenes[policy_scene];
+            if (track_costs) {  // the trackers' state after the previous bounce
+                live_mat.resize((size_t)std::max(c->ct_mat.items, 1));
+                live_tex.resize((size_t)std::max(c->ct_tex.items, 1));
+                WF_CK(c, cudaMemcpyAsync(live_mat.data(), c->ct_mat.rel, sizeof(double) * live_mat.size(),
+                                         cudaMemcpyDeviceToHost, s));
+                WF_CK(c, cudaMemcpyAsync(live_tex.data(), c->ct_tex.rel, sizeof(double) * live_tex.size(),
+                                         cudaMemcpyDeviceToHost, s));
+                WF_CK(c, cudaStreamSynchronize(s));
+                rc_mat = live_mat.data();
+                rc_tex = live_tex.data();
+            }
             uint32_t* perm = nullptr;
             int rc = schedule_columns(c, policy, c->counters + 1, (int64_t)hits, cd, R.S.materials, R.S.num_materials,
                                       R.mats, R.S.num_textures, R.d_tex_bytes, R.tex_bytes, rc_mat, rc_tex, &perm);
@@ -161,6 +174,10 @@ int wave_host(wf_ctx* c, int64_t total, int max_depth, int policy, bool ray_sort
         WF_CK(c, cudaEventRecord(ev[6], s));
         launch_shade(T, c->rq[cur], hq_use, c->counters + 1, c->sh, c->counters + 2, c->rq[1 - cur], c->counters + 3,
                      c->arena, c->err_flag, PC, s);
+        if (track_costs) {  // the tracker merge at the end of shadeAll (.cpp:800-844)
+            launch_cost_update(c->ct_mat, c->ct_tex, s);
+            stats.kernel_launches += 1;
+        }
         launch_occluded_render(T, c->sh, c->counters + 2, c->arena, c->counters + 5, c->err_flag, PC, s);
         stats.kernel_launches += 3;
         WF_CK(c, cudaEventRecord(ev[7], s));
@@ -354,10 +371,22 @@ int render_single(wf_ctx* c, const wf_render_params* P, wf_render_stats* st)
         launch_fill_i32(c->ad_active, np, 0, true, s);
         kernels_setup = 1;
     }
+    const bool tracking = P->enable_cost_tracking != 0;
+    if (tracking) {
+        const DeviceScene& S0 = c->scenes[0].S;
+        rc = reset_cost_trackers(c, S0.num_materials, S0.num_textures);
+        if (rc) return rc;
+        kernels_setup += 1;
+        table[0].cost_sum_mat = c->ct_mat.sum;
+        table[0].cost_cnt_mat = c->ct_mat.cnt;
+        table[0].cost_sum_tex = c->ct_tex.sum;
+        table[0].cost_cnt_tex = c->ct_tex.cnt;
+        table[0].rel_cost_material = c->ct_mat.rel_f;
+    }
     rc = upload_jobs(c, table);
     if (rc) return rc;
     WF_CK(c, cudaMemsetAsync(c->arena, 0, sizeof(float) * 3 * (size_t)np, s));
-    const bool graph = use_graph(c, false, P->policy);
+    const bool graph = !tracking && use_graph(c, false, P->policy);
     wf_render_stats stats{};
     stats.kernel_launches = kernels_setup;
     if (graph) {
@@ -377,7 +406,7 @@ int render_single(wf_ctx* c, const wf_render_params* P, wf_render_stats* st)
         if (rc) return rc;
         rc = graph ? wave_graph(c, P->max_depth, P->enable_ray_sort != 0, stats)
                    : wave_host(c, pix * nspp, P->max_depth, P->policy, P->enable_ray_sort != 0, 0,
-                               P->rel_cost_material, P->rel_cost_texture, &table[0], stats);
+                               P->rel_cost_material, P->rel_cost_texture, &table[0], stats, tracking);
         if (rc) return rc;
         if (adaptive) {  // renderScene's per-sample adaptive block (.cpp:270-294)
             launch_adaptive_fold(c->ad_buf, np, nspp, c->arena, c->ad_mean, c->ad_m2, c->ad_count, c->ad_active,
@@ -581,6 +610,40 @@ int wf_render_device(wf_ctx* c, const wf_render_params* P, wf_render_stats* st)
     if (rc) return rc;
     rc = finalize_image(c, P, st);
     if (rc) return rc;
+    WF_CK(c, cudaStreamSynchronize(c->stream));
+    return WF_OK;
+}
+
+int wf_cost_tracker_state(wf_ctx* c, double* rel_mat, int32_t nmat, double* rel_tex, int32_t ntex)
+{
+    if (!c) return WF_ERR_INVALID_ARGUMENT;
+    if ((rel_mat && nmat != c->ct_mat.items) || (rel_tex && ntex != c->ct_tex.items) || !c->ct_mat.rel)
+        return set_err(c, WF_ERR_INVALID_ARGUMENT, "no tracker of that size (render with enable_cost_tracking)");
+    if (rel_mat && nmat > 0)
+        WF_CK(c, cudaMemcpyAsync(rel_mat, c->ct_mat.rel, sizeof(double) * nmat, cudaMemcpyDeviceToHost, c->stream));
+    if (rel_tex && ntex > 0)
+        WF_CK(c, cudaMemcpyAsync(rel_tex, c->ct_tex.rel, sizeof(double) * ntex, cudaMemcpyDeviceToHost, c->stream));
+    WF_CK(c, cudaStreamSynchronize(c->stream));
+    return WF_OK;
+}
+
+int wf_cost_tracker_replay(wf_ctx* c, int32_t items, int32_t steps, const uint64_t* sums, const uint32_t* counts,
+                           double* rel_out)
+{
+    if (!c || items <= 0 || steps < 0 || (steps > 0 && (!sums || !counts)) || !rel_out)
+        return set_err(c, WF_ERR_INVALID_ARGUMENT, "bad replay arguments");
+    cudaSetDevice(c->device);
+    int rc = reset_cost_trackers(c, items, 0);
+    if (rc) return rc;
+    for (int k = 0; k < steps; ++k) {
+        WF_CK(c, cudaMemcpyAsync(c->ct_mat.sum, sums + (size_t)k * items, sizeof(uint64_t) * items,
+                                 cudaMemcpyHostToDevice, c->stream));
+        WF_CK(c, cudaMemcpyAsync(c->ct_mat.cnt, counts + (size_t)k * items, sizeof(uint32_t) * items,
+                                 cudaMemcpyHostToDevice, c->stream));
+        launch_cost_update(c->ct_mat, c->ct_tex, c->stream);
+        WF_CK(c, cudaStreamSynchronize(c->stream));  // the host rows are read before the next step
+    }
+    WF_CK(c, cudaMemcpyAsync(rel_out, c->ct_mat.rel, sizeof(double) * items, cudaMemcpyDeviceToHost, c->stream));
     WF_CK(c, cudaStreamSynchronize(c->stream));
     return WF_OK;
 }

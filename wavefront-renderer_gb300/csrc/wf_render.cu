@@ -284,6 +284,69 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_trace_render(DeviceScene sc
     if (overflow) atomicOr(err, 1);
 }
 
+// Adds the cycles of the lanes timing the same item with one atomic per item
+// and warp (all 32 lanes call; id < 0 = nothing timed).
+__device__ __forceinline__ void warp_cost_add(unsigned long long* sum, unsigned int* cnt, int id, unsigned cyc)
+{
+    const unsigned peers = __match_any_sync(0xFFFFFFFFu, id);
+    unsigned long long total = 0;
+    for (int k = 0; k < 32; ++k) {
+        const unsigned v = __shfl_sync(0xFFFFFFFFu, cyc, k);
+        if ((peers >> k) & 1u) total += v;
+    }
+    if (id >= 0 && (threadIdx.x & 31) == (unsigned)(__ffs(peers) - 1)) {
+        atomicAdd(sum + id, total);
+        atomicAdd(cnt + id, (unsigned)__popc(peers));
+    }
+}
+
+// CostTracker::record for every item timed in the last bounce, in item order
+// (WavefrontRenderer.cpp:833-844), then relativeCost (CostTracker.h:42-55);
+// the bounce's sums are cleared.  Block 0 runs the materials, block 1 the
+// textures, each on one thread (the EMA total is a serial dependency).
+__device__ void cost_update_one(CostTrackerDev T)
+{
+    if (T.items <= 0) return;
+    double total = *T.total;
+    int tracked = *T.tracked;
+    for (int i = 0; i < T.items; ++i) {
+        const unsigned n = T.cnt[i];
+        if (n == 0) continue;
+        const double c = (double)T.sum[i] / (double)n;
+        T.sum[i] = 0ull;
+        T.cnt[i] = 0u;
+        T.samples[i] += 1;
+        if (!T.init[i]) {
+            T.avg[i] = c;
+            T.init[i] = 1;
+            tracked += 1;
+            total += c;
+        } else {
+            const double old = T.avg[i];
+            const double nw = (1.0 - 0.05) * old + 0.05 * c;
+            T.avg[i] = nw;
+            total += (nw - old);
+        }
+    }
+    *T.total = total;
+    *T.tracked = tracked;
+    for (int i = 0; i < T.items; ++i) {
+        double r = 1.0;
+        if (T.samples[i] >= 50 && tracked != 0) {
+            const double g = total / tracked;
+            if (g > 0.0) r = T.avg[i] / g;
+        }
+        T.rel[i] = r;
+        if (T.rel_f) T.rel_f[i] = (float)r;
+    }
+}
+
+__global__ void k_cost_update(CostTrackerDev mat, CostTrackerDev tex)
+{
+    if (threadIdx.x != 0) return;
+    cost_update_one(blockIdx.x == 0 ? mat : tex);
+}
+
 // ---------------------------------------------------------------------------
 // shadeAll per-hit body (.cpp:602-797): emission with MIS, area-light NEE
 // (Scene::sampleLight, src/core/Scene.cpp:192-238) and directional NEE become
@@ -309,6 +372,8 @@ __global__ void __launch_bounds__(128) k_shade(DeviceScene scene0, DeviceJob job
            c_sun = {0, 0, 0}, dir_env = {0, 0, 0}, c_env = {0, 0, 0}, nd = {0, 0, 0}, Tn = {0, 0, 0};
         float dist_area = 0.0f, next_pdf = 0.0f;
         int pixel = 0, depth = 0, sample = 0, job = 0, slot = 0;
+        int cost_mat = -1, cost_tex = -1;
+        unsigned cyc_mat = 0, cyc_tex = 0;
         if (active) {
             const int ri = hq.ray[k];
             job = kMulti ? rq.job[ri] : 0;
@@ -329,6 +394,25 @@ __global__ void __launch_bounds__(128) k_shade(DeviceScene scene0, DeviceJob job
             rebuild_hit(S, o, d, hq.tri[k], hq.t[k], hq.bu[k], hq.bv[k], h);
             p = h.p;
             const wf_material m = S.materials[h.mat];
+            V3 surf = {0, 0, 0};
+            bool have_surf = false;
+            // Live cost tracking (.cpp:612-625): a quarter of the hits time
+            // their surface colour lookup (textured materials) and their
+            // scatter with the SM clock.
+            bool timed = false;
+            if (!kMulti && J.cost_sum_mat) {
+                Stream cs(seed_lo, seed_hi, kPurposeCostSample, (uint32_t)depth, (uint32_t)pixel,
+                          (uint32_t)sample);
+                timed = cs.next() < 0.25f;
+            }
+            if (timed && m.texture_id >= 0) {
+                const long long t0 = clock64();
+                surf = surface_color(S, m, h);
+                const long long t1 = clock64();
+                have_surf = true;
+                cost_tex = m.texture_id;
+                cyc_tex = (unsigned)min(t1 - t0, (long long)(1 << 26));
+            }
             // Emission with MIS (.cpp:629-658)
             V3 Le = emitted(m, h.n, d * -1.0f);
             if (Le.x > 0.0f || Le.y > 0.0f || Le.z > 0.0f) {
@@ -343,8 +427,6 @@ __global__ void __launch_bounds__(128) k_shade(DeviceScene scene0, DeviceJob job
                 Le = vmin(Le, ff);
                 accum_add(accum, slot, T * Le * w);
             }
-            V3 surf = {0, 0, 0};
-            bool have_surf = false;
             // Area-light NEE (.cpp:660-710)
             if ((m.type == WF_MATERIAL_DIFFUSE || m.type == WF_MATERIAL_PLASTIC) &&
                 S.num_emissive_meshes > 0) {
@@ -442,7 +524,13 @@ __global__ void __launch_bounds__(128) k_shade(DeviceScene scene0, DeviceJob job
                       (uint32_t)sample);
             V3 att;
             float spdf;
-            if (scatter(S, m, d, h, sr, att, nd, spdf)) {
+            const long long ts0 = timed ? clock64() : 0;
+            const bool scattered = scatter(S, m, d, h, sr, att, nd, spdf);
+            if (timed) {
+                cost_mat = h.mat;
+                cyc_mat = (unsigned)min(clock64() - ts0, (long long)(1 << 26));
+            }
+            if (scattered) {
                 Tn = T * att;
                 bool alive = true;
                 if (depth + 1 >= J.rr_min_depth) {
@@ -466,6 +554,10 @@ __global__ void __launch_bounds__(128) k_shade(DeviceScene scene0, DeviceJob job
             }
         }
         __syncwarp();
+        if (!kMulti && job0.cost_sum_mat) {
+            warp_cost_add(job0.cost_sum_mat, job0.cost_cnt_mat, cost_mat, cyc_mat);
+            warp_cost_add(job0.cost_sum_tex, job0.cost_cnt_tex, cost_tex, cyc_tex);
+        }
         int64_t pa = warp_append(sh_n, want_area);
         if (want_area) {
             if (pa < sh.capacity) {
@@ -1112,6 +1204,11 @@ void launch_permute_hits(HitQueueDev in, const uint32_t* perm, const ull* d_n, H
 void launch_finalize(const float* accum, int64_t n, float spp, float* image, cudaStream_t s)
 {
     k_finalize<<<grid_for(n, 256, 65535), 256, 0, s>>>(accum, n, spp, image);
+}
+
+void launch_cost_update(const CostTrackerDev& mat, const CostTrackerDev& tex, cudaStream_t s)
+{
+    k_cost_update<<<2, 32, 0, s>>>(mat, tex);
 }
 
 void launch_adaptive_fold(float* sample_buf, int64_t np, int nspp, float* accum, float* mean, float* m2,
