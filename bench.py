@@ -386,8 +386,9 @@ def main() -> int:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--trace-variant", type=int, default=-1)
     ap.add_argument("--blocks-per-sm", type=int, default=0)
-    ap.add_argument("--ref-rows", type=int, default=32)
-    ap.add_argument("--ref-spp", type=int, default=8)
+    ap.add_argument("--ref-rows", type=int, default=256)
+    ap.add_argument("--ref-spp", type=int, default=16)
+    ap.add_argument("--bvh", default="ploc", choices=["ploc", "lbvh"])
     args = ap.parse_args()
     args.warmup = max(args.warmup, 0)
     if args.workload == "c3":
@@ -405,9 +406,8 @@ def main() -> int:
     pkg = load_pkg()
     ctx = pkg.Context(local)
     scene = pkg.HostScene(wl["config"])
+    ctx.set_tuning(max(args.trace_variant, 0), args.blocks_per_sm, bvh_builder=1 if args.bvh == "lbvh" else 0)
     info = ctx.upload(scene.desc)
-    if args.trace_variant >= 0 or args.blocks_per_sm > 0:
-        ctx.set_tuning(max(args.trace_variant, 0), args.blocks_per_sm)
     W, H = wl["width"], wl["height"]
     cam = scene.camera(W, H)
     policy = pkg.POLICIES[args.policy]
@@ -487,10 +487,12 @@ def main() -> int:
         "clocks": clocks,
         "gpu_launches": int(sum(s["kernel_launches"] for s in stats)),
         "bvh_build_ms": info.bvh_build_ms,
+        "bvh": {"builder": ["ploc", "lbvh"][info.bvh_builder], "nodes": info.bvh_nodes, "depth": info.bvh_depth},
         "tuning": ctx.get_tuning(),
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        rays, dt, sample = cpu_sample(pkg, wl, os.cpu_count() or 1, rows=48, spp=8, seed=7)
+        rays, dt, sample = cpu_sample(pkg, wl, os.cpu_count() or 1, rows=wl["height"], spp=wl.get("cpu_spp", 32),
+                                      seed=7)
         line["cpu_baseline"] = {"value": rays / dt / 1e6, "unit": "Mrays/s", "cores": os.cpu_count() or 1,
                                 "kind": "port", "sample": sample}
     if rank == 0:

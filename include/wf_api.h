@@ -265,6 +265,8 @@ typedef struct wf_scene_info {
     int32_t bvh_nodes;
     double bvh_build_ms;
     int64_t device_bytes;
+    int32_t bvh_builder;   /* wf_tuning::bvh_builder that built the tree  */
+    int32_t bvh_depth;     /* interior levels below the root              */
 } wf_scene_info;
 int wf_scene_get_info(wf_ctx* ctx, wf_scene_info* out_info);
 
@@ -278,7 +280,11 @@ typedef struct wf_tuning {
     int32_t persistent_blocks_per_sm;
     int32_t graph_mode;  /* 0 = graphs for batches and the server, 1 = also for
                             single renders, 2 = never (policy != none never) */
-    int32_t reserved[5];
+    int32_t bvh_builder; /* scenes uploaded afterwards: 0 = PLOC (locally-
+                            ordered clustering, default), 1 = LBVH (Karras
+                            radix tree); PLOC falls back to LBVH if its tree is
+                            deeper than the traversal stack */
+    int32_t reserved[4];
 } wf_tuning;
 int wf_set_tuning(wf_ctx* ctx, const wf_tuning* tuning);
 int wf_get_tuning(const wf_ctx* ctx, wf_tuning* out_tuning);

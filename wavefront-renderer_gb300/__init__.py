@@ -116,12 +116,13 @@ class WfSceneInfo(C.Structure):
     _fields_ = [("bounds_min", C.c_float * 3), ("bounds_max", C.c_float * 3),
                 ("total_emissive_area", C.c_float), ("num_triangles", C.c_int32),
                 ("num_meshes", C.c_int32), ("num_emissive_meshes", C.c_int32), ("bvh_nodes", C.c_int32),
-                ("bvh_build_ms", C.c_double), ("device_bytes", C.c_int64)]
+                ("bvh_build_ms", C.c_double), ("device_bytes", C.c_int64), ("bvh_builder", C.c_int32),
+                ("bvh_depth", C.c_int32)]
 
 
 class WfTuning(C.Structure):
     _fields_ = [("trace_variant", C.c_int32), ("persistent_blocks_per_sm", C.c_int32), ("graph_mode", C.c_int32),
-                ("reserved", C.c_int32 * 5)]
+                ("bvh_builder", C.c_int32), ("reserved", C.c_int32 * 4)]
 
 
 class WfJob(C.Structure):
@@ -544,15 +545,16 @@ class Context:
                "wf_cost_tracker_replay", self)
         return out
 
-    def set_tuning(self, trace_variant: int = 0, persistent_blocks_per_sm: int = 0, graph_mode: int = 0) -> None:
-        t = WfTuning(trace_variant, persistent_blocks_per_sm, graph_mode)
+    def set_tuning(self, trace_variant: int = 0, persistent_blocks_per_sm: int = 0, graph_mode: int = 0,
+                   bvh_builder: int = 0) -> None:
+        t = WfTuning(trace_variant, persistent_blocks_per_sm, graph_mode, bvh_builder)
         _check(load_library().wf_set_tuning(self._h, C.byref(t)), "wf_set_tuning", self)
 
     def get_tuning(self) -> dict:
         t = WfTuning()
         _check(load_library().wf_get_tuning(self._h, C.byref(t)), "wf_get_tuning", self)
         return {"trace_variant": t.trace_variant, "persistent_blocks_per_sm": t.persistent_blocks_per_sm,
-                "graph_mode": t.graph_mode}
+                "graph_mode": t.graph_mode, "bvh_builder": t.bvh_builder}
 
     def add_scene(self, desc: WfSceneDesc) -> int:
         sid = C.c_int32()

@@ -562,13 +562,22 @@ int build_scene(wf_ctx* c, const wf_scene_desc* D, ResidentScene& R)
         cudaMemcpyAsync(dprim, tri_prim.data(), sizeof(int32_t) * ntri, cudaMemcpyHostToDevice, s);
         BvhBuildInput bi{dpx, dpy, dpz, didx, dgeom, dprim, ntri, {bmin[0], bmin[1], bmin[2]}, {bmax[0], bmax[1], bmax[2]}};
         auto b0 = std::chrono::steady_clock::now();
-        int brc = build_lbvh(bi, bo, c->num_sms, s, err);
+        int brc = -1;
+        if (c->tuning.bvh_builder == 0) {
+            brc = build_ploc(bi, bo, c->num_sms, s, err);
+            R.info.bvh_builder = 0;
+        }
+        if (brc) {  // LBVH on request, or when the PLOC tree is too deep
+            brc = build_lbvh(bi, bo, c->num_sms, s, err);
+            R.info.bvh_builder = 1;
+        }
         auto b1 = std::chrono::steady_clock::now();
         cleanup_tmp();
         if (brc) return set_err(c, WF_ERR_CUDA, "BVH build failed: " + err);
         A.push_back(bo.tris);
         A.push_back(bo.nodes);
         R.info.bvh_build_ms = std::chrono::duration<double, std::milli>(b1 - b0).count();
+        R.info.bvh_depth = bo.max_depth;
     }
     S.tris = bo.tris;
     S.nodes = bo.nodes;
@@ -1112,7 +1121,7 @@ int wf_set_tuning(wf_ctx* c, const wf_tuning* t)
 {
     if (!c || !t) return WF_ERR_INVALID_ARGUMENT;
     if (t->trace_variant < 0 || t->trace_variant > 2 || t->persistent_blocks_per_sm < 0 ||
-        t->persistent_blocks_per_sm > 32)
+        t->persistent_blocks_per_sm > 32 || t->bvh_builder < 0 || t->bvh_builder > 1)
         return set_err(c, WF_ERR_INVALID_ARGUMENT, "tuning out of range");
     c->tuning = *t;
     return WF_OK;

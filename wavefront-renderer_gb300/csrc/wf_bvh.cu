@@ -16,7 +16,10 @@
 //   6. triangles in leaf order as (v0, v1-v0, v2-v0) plus ids.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <string>
+#include <utility>
+#include <vector>
 
 #include "wf_bvh.h"
 #include "wf_sort.h"
@@ -241,6 +244,280 @@ __global__ void k_depth(int n, const int* __restrict__ parent_int, int* max_dept
     }
 }
 
+// ===========================================================================
+// PLOC: Meister & Bittner, "Parallel Locally-Ordered Clustering for Bounding
+// Volume Hierarchy Construction" (IEEE TVCG 2018).  Clusters start as the
+// Morton-sorted triangles; every iteration each cluster finds, among the
+// kPlocRadius clusters on either side, the one whose union box has the
+// smallest surface area (ties: the lower position), mutual nearest
+// neighbours merge into a new node at the lower position, and the cluster
+// array is compacted in order.  Node ids: triangles 0..N-1 (sorted
+// position), internal nodes N.. in creation order, so children are created
+// before their parents and the root is created last.
+// ===========================================================================
+
+constexpr int kPlocRadius = 16;
+constexpr int kPlocBlock = 256;
+
+__device__ __forceinline__ float union_half_area(const float* a, const float* b)
+{
+    const float dx = fmaxf(a[3], b[3]) - fminf(a[0], b[0]);
+    const float dy = fmaxf(a[4], b[4]) - fminf(a[1], b[1]);
+    const float dz = fmaxf(a[5], b[5]) - fminf(a[2], b[2]);
+    return dx * dy + dy * dz + dz * dx;
+}
+
+__global__ void __launch_bounds__(kPlocBlock) k_ploc_nn(const int* __restrict__ cl, int n,
+                                                       const float* __restrict__ nbox, int* __restrict__ nn)
+{
+    __shared__ float sb[(kPlocBlock + 2 * kPlocRadius) * 6];
+    const int block0 = blockIdx.x * kPlocBlock;
+    for (int k = threadIdx.x; k < kPlocBlock + 2 * kPlocRadius; k += kPlocBlock) {
+        const int g = block0 - kPlocRadius + k;
+        if (g >= 0 && g < n) {
+            const float* b = nbox + 6 * (int64_t)cl[g];
+#pragma unroll
+            for (int c = 0; c < 6; ++c) sb[k * 6 + c] = b[c];
+        }
+    }
+    __syncthreads();
+    const int i = block0 + threadIdx.x;
+    if (i >= n) return;
+    const float* bi = sb + (threadIdx.x + kPlocRadius) * 6;
+    float best = 3.0e38f;
+    int bj = -1;
+    const int lo = max(0, i - kPlocRadius), hi = min(n - 1, i + kPlocRadius);
+    for (int j = lo; j <= hi; ++j) {
+        if (j == i) continue;
+        const float a = union_half_area(bi, sb + (j - block0 + kPlocRadius) * 6);
+        if (a < best) {
+            best = a;
+            bj = j;
+        }
+    }
+    nn[i] = bj;
+}
+
+__global__ void k_ploc_flags(const int* __restrict__ nn, int n, int* __restrict__ merge, int* __restrict__ valid)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int j = nn[i];
+        const bool mutual = j >= 0 && nn[j] == i;
+        merge[i] = (mutual && i < j) ? 1 : 0;
+        valid[i] = (mutual && i > j) ? 0 : 1;
+    }
+}
+
+__global__ void k_ploc_apply(const int* __restrict__ cl, const int* __restrict__ nn, int n,
+                             const int* __restrict__ merge, const int* __restrict__ m_off,
+                             const int* __restrict__ valid, const int* __restrict__ v_off, int node_base,
+                             int num_tris, float* __restrict__ nbox, int* __restrict__ left,
+                             int* __restrict__ right, int* __restrict__ cnt, int* __restrict__ cl_out)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (!valid[i]) continue;
+        int id = cl[i];
+        if (merge[i]) {
+            const int a = cl[i], b = cl[nn[i]];
+            id = node_base + m_off[i];
+            left[id - num_tris] = a;
+            right[id - num_tris] = b;
+            const float* ba = nbox + 6 * (int64_t)a;
+            const float* bb = nbox + 6 * (int64_t)b;
+            float* o = nbox + 6 * (int64_t)id;
+            o[0] = fminf(ba[0], bb[0]);
+            o[1] = fminf(ba[1], bb[1]);
+            o[2] = fminf(ba[2], bb[2]);
+            o[3] = fmaxf(ba[3], bb[3]);
+            o[4] = fmaxf(ba[4], bb[4]);
+            o[5] = fmaxf(ba[5], bb[5]);
+            cnt[id] = cnt[a] + cnt[b];
+        }
+        cl_out[v_off[i]] = id;
+    }
+}
+
+// Exclusive scan of n ints (three passes: per-block scans of 1024, one block
+// scanning the block totals, then the carries); *total gets the sum.
+__global__ void __launch_bounds__(1024) k_scan_blocks(const int* __restrict__ in, int n, int* __restrict__ out,
+                                                      int* __restrict__ block_sums)
+{
+    __shared__ int warp_incl[32];
+    const int i = blockIdx.x * 1024 + threadIdx.x;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int v = i < n ? in[i] : 0;
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int u = __shfl_up_sync(0xFFFFFFFFu, x, o);
+        if (lane >= o) x += u;
+    }
+    if (lane == 31) warp_incl[w] = x;
+    __syncthreads();
+    if (w == 0) {
+        int y = warp_incl[lane];
+        for (int o = 1; o < 32; o <<= 1) {
+            const int u = __shfl_up_sync(0xFFFFFFFFu, y, o);
+            if (lane >= o) y += u;
+        }
+        warp_incl[lane] = y;
+    }
+    __syncthreads();
+    const int excl = x - v + (w > 0 ? warp_incl[w - 1] : 0);
+    if (i < n) out[i] = excl;
+    if (threadIdx.x == 0) block_sums[blockIdx.x] = warp_incl[31];
+}
+
+__global__ void __launch_bounds__(1024) k_scan_sums(int* __restrict__ sums, int nb, int* __restrict__ total)
+{
+    __shared__ int warp_incl[32];
+    __shared__ int carry;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int t0 = 0; t0 < nb; t0 += 1024) {
+        const int i = t0 + threadIdx.x;
+        const int v = i < nb ? sums[i] : 0;
+        int x = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int u = __shfl_up_sync(0xFFFFFFFFu, x, o);
+            if (lane >= o) x += u;
+        }
+        if (lane == 31) warp_incl[w] = x;
+        __syncthreads();
+        if (w == 0) {
+            int y = warp_incl[lane];
+            for (int o = 1; o < 32; o <<= 1) {
+                const int u = __shfl_up_sync(0xFFFFFFFFu, y, o);
+                if (lane >= o) y += u;
+            }
+            warp_incl[lane] = y;
+        }
+        __syncthreads();
+        const int excl = x - v + (w > 0 ? warp_incl[w - 1] : 0);
+        if (i < nb) sums[i] = carry + excl;
+        __syncthreads();
+        if (threadIdx.x == 0) carry += warp_incl[31];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *total = carry;
+}
+
+__global__ void k_scan_add(int* __restrict__ out, int n, const int* __restrict__ sums)
+{
+    const int i = blockIdx.x * 1024 + threadIdx.x;
+    if (i < n) out[i] += sums[blockIdx.x];
+}
+
+void scan_i32(const int* in, int n, int* out, int* block_sums, int* total, cudaStream_t s)
+{
+    const int nb = (n + 1023) / 1024;
+    k_scan_blocks<<<nb, 1024, 0, s>>>(in, n, out, block_sums);
+    k_scan_sums<<<1, 1024, 0, s>>>(block_sums, nb, total);
+    k_scan_add<<<nb, 1024, 0, s>>>(out, n, block_sums);
+}
+
+// Top-down over one iteration's nodes: children's first triangle position
+// (depth-first order, left subtree first) and depth.
+__global__ void k_ploc_topdown(int first_id, int count, int num_tris, const int* __restrict__ left,
+                               const int* __restrict__ right, const int* __restrict__ cnt, int* __restrict__ offset,
+                               int* __restrict__ depth)
+{
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
+        const int id = first_id + k;
+        const int l = left[id - num_tris], r = right[id - num_tris];
+        offset[l] = offset[id];
+        offset[r] = offset[id] + cnt[l];
+        depth[l] = depth[id] + 1;
+        depth[r] = depth[id] + 1;
+    }
+}
+
+__global__ void k_ploc_root(int root, int* offset, int* depth)
+{
+    offset[root] = 0;
+    depth[root] = 0;
+}
+
+// Kept interior nodes (more than kLeafMax triangles), numbered from the root
+// down: q = (last id) - id, so the root gets 0.
+__global__ void k_ploc_keep(int num_tris, int last_id, const int* __restrict__ cnt, int* __restrict__ keep)
+{
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q <= last_id - num_tris; q += gridDim.x * blockDim.x)
+        keep[q] = cnt[last_id - q] > kLeafMax ? 1 : 0;
+}
+
+__device__ __forceinline__ uint32_t ploc_child(int c, int num_tris, int last_id, const int* cnt, const int* offset,
+                                               const int* newid)
+{
+    if (c < num_tris || cnt[c] <= kLeafMax)
+        return kLeafFlag | ((uint32_t)offset[c] << 3) | (uint32_t)(cnt[c] - 1);
+    return (uint32_t)newid[last_id - c];
+}
+
+__global__ void k_ploc_emit(int num_tris, int last_id, const int* __restrict__ left, const int* __restrict__ right,
+                            const int* __restrict__ cnt, const int* __restrict__ offset,
+                            const int* __restrict__ depth, const int* __restrict__ keep,
+                            const int* __restrict__ newid, const float* __restrict__ nbox,
+                            BvhNode* __restrict__ nodes, int* __restrict__ max_depth)
+{
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q <= last_id - num_tris; q += gridDim.x * blockDim.x) {
+        if (!keep[q]) continue;
+        const int id = last_id - q;
+        const int l = left[id - num_tris], r = right[id - num_tris];
+        float a[6], b[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            a[k] = nbox[6 * (int64_t)l + k];
+            b[k] = nbox[6 * (int64_t)r + k];
+        }
+        pad_box(a);
+        pad_box(b);
+        BvhNode nd;
+        nd.c0xy = make_float4(a[0], a[3], a[1], a[4]);
+        nd.c1xy = make_float4(b[0], b[3], b[1], b[4]);
+        nd.cz = make_float4(a[2], a[5], b[2], b[5]);
+        nd.kids = make_int4((int)ploc_child(l, num_tris, last_id, cnt, offset, newid),
+                            (int)ploc_child(r, num_tris, last_id, cnt, offset, newid), 0, 0);
+        nodes[newid[q]] = nd;
+        atomicMax(max_depth, depth[id]);
+    }
+}
+
+// Whole tree in one leaf (N <= kLeafMax): a root with that leaf and an
+// unreachable second child.
+__global__ void k_ploc_single(int num_tris, int root, const float* __restrict__ nbox, BvhNode* nodes)
+{
+    float a[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) a[k] = nbox[6 * (int64_t)root + k];
+    pad_box(a);
+    BvhNode nd;
+    nd.c0xy = make_float4(a[0], a[3], a[1], a[4]);
+    nd.c1xy = make_float4(1e30f, 1e30f, 1e30f, 1e30f);
+    nd.cz = make_float4(a[2], a[5], 1e30f, 1e30f);
+    nd.kids = make_int4((int)(kLeafFlag | (uint32_t)(num_tris - 1)), (int)kLeafFlag, 0, 0);
+    nodes[0] = nd;
+}
+
+// Triangle order of the tree: sorted position p goes to offset[p].
+__global__ void k_ploc_order(int n, const int* __restrict__ offset, const uint32_t* __restrict__ sorted_ids,
+                             uint32_t* __restrict__ final_ids)
+{
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x)
+        final_ids[offset[p]] = sorted_ids[p];
+}
+
+__global__ void k_ploc_init(int n, const float* __restrict__ leaf_box, float* __restrict__ nbox,
+                            int* __restrict__ cnt, int* __restrict__ cl)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+#pragma unroll
+        for (int k = 0; k < 6; ++k) nbox[6 * (int64_t)i + k] = leaf_box[6 * (int64_t)i + k];
+        cnt[i] = 1;
+        cl[i] = i;
+    }
+}
+
 #define WF_TRY(x)                                                      \
     do {                                                               \
         cudaError_t e_ = (x);                                          \
@@ -376,6 +653,155 @@ fail:
     cudaFree(flags);
     cudaFree(d_depth);
     cudaFree(d_n);
+    cudaFree(out.tris);
+    cudaFree(out.nodes);
+    out.tris = nullptr;
+    out.nodes = nullptr;
+    return -1;
+}
+
+
+namespace {
+
+// Device buffers of one build, freed together.
+struct BuildScratch {
+    std::vector<void*> ptrs;
+    template <class T>
+    cudaError_t alloc(T** p, size_t count)
+    {
+        *p = nullptr;
+        cudaError_t e = cudaMalloc((void**)p, sizeof(T) * (count ? count : 1));
+        if (e == cudaSuccess) ptrs.push_back((void*)*p);
+        return e;
+    }
+    ~BuildScratch()
+    {
+        for (void* p : ptrs) cudaFree(p);
+    }
+};
+
+}  // namespace
+
+int build_ploc(const BvhBuildInput& in, BvhBuildOutput& out, int num_sms, cudaStream_t s, std::string& err)
+{
+    const int n = in.num_tris;
+    out.tris = nullptr;
+    out.nodes = nullptr;
+    out.num_nodes = 0;
+    out.max_depth = 0;
+    if (n <= 0) return 0;
+    BuildScratch B;
+    float *tri_box, *leaf_box, *nbox;
+    uint64_t *codes, *codes_tmp;
+    uint32_t *ids, *ids_tmp, *hist, *final_ids;
+    unsigned long long* d_n;
+    int *cnt, *left, *right, *cl, *cl2, *nn, *merge, *valid, *m_off, *v_off, *block_sums, *d_total, *offset,
+        *depth, *keep, *newid, *d_depth;
+    uint64_t* sorted_codes = nullptr;
+    uint32_t* sorted_ids = nullptr;
+    const int64_t nn_all = 2 * (int64_t)n - 1;
+    const int grid = num_sms * 8;
+    const int nb = radix_blocks_for(n, num_sms);
+    const float3 smin = make_float3(in.bmin[0], in.bmin[1], in.bmin[2]);
+    const float3 sext = make_float3(in.bmax[0] - in.bmin[0], in.bmax[1] - in.bmin[1], in.bmax[2] - in.bmin[2]);
+    const unsigned long long hn = (unsigned long long)n;
+    std::vector<std::pair<int, int>> iters;  // (first node id, nodes) per iteration
+    int cur_n = n, next_id = n, h_depth = 0, root = 0;
+
+    WF_TRY(B.alloc(&tri_box, 6 * (size_t)n));
+    WF_TRY(B.alloc(&leaf_box, 6 * (size_t)n));
+    WF_TRY(B.alloc(&nbox, 6 * (size_t)nn_all));
+    WF_TRY(B.alloc(&codes, (size_t)n));
+    WF_TRY(B.alloc(&codes_tmp, (size_t)n));
+    WF_TRY(B.alloc(&ids, (size_t)n));
+    WF_TRY(B.alloc(&ids_tmp, (size_t)n));
+    WF_TRY(B.alloc(&hist, radix_hist_words(nb)));
+    WF_TRY(B.alloc(&final_ids, (size_t)n));
+    WF_TRY(B.alloc(&d_n, 1));
+    WF_TRY(B.alloc(&cnt, (size_t)nn_all));
+    WF_TRY(B.alloc(&left, (size_t)n));
+    WF_TRY(B.alloc(&right, (size_t)n));
+    WF_TRY(B.alloc(&cl, (size_t)n));
+    WF_TRY(B.alloc(&cl2, (size_t)n));
+    WF_TRY(B.alloc(&nn, (size_t)n));
+    WF_TRY(B.alloc(&merge, (size_t)n));
+    WF_TRY(B.alloc(&valid, (size_t)n));
+    WF_TRY(B.alloc(&m_off, (size_t)n));
+    WF_TRY(B.alloc(&v_off, (size_t)n));
+    WF_TRY(B.alloc(&block_sums, (size_t)(n + 1023) / 1024 + 1));
+    WF_TRY(B.alloc(&d_total, 2));
+    WF_TRY(B.alloc(&offset, (size_t)nn_all));
+    WF_TRY(B.alloc(&depth, (size_t)nn_all));
+    WF_TRY(B.alloc(&keep, (size_t)n));
+    WF_TRY(B.alloc(&newid, (size_t)n));
+    WF_TRY(B.alloc(&d_depth, 1));
+    WF_TRY(cudaMemsetAsync(d_depth, 0, sizeof(int), s));
+    WF_TRY(cudaMemcpyAsync(d_n, &hn, sizeof(hn), cudaMemcpyHostToDevice, s));
+
+    k_tri_prep<<<grid, 256, 0, s>>>(in.px, in.py, in.pz, in.idx, n, smin, sext, tri_box, codes, ids);
+    {
+        RadixSortArgs a{codes, ids, codes_tmp, ids_tmp, hist, d_n, nb, 0, 64, &sorted_codes, &sorted_ids};
+        radix_sort_pairs(a, s);
+    }
+    k_leaf_boxes<<<grid, 256, 0, s>>>(tri_box, sorted_ids, n, leaf_box);
+    k_ploc_init<<<grid, 256, 0, s>>>(n, leaf_box, nbox, cnt, cl);
+    while (cur_n > 1) {
+        if (iters.size() > 100000) {
+            err = "PLOC did not converge";
+            return -1;
+        }
+        k_ploc_nn<<<(cur_n + kPlocBlock - 1) / kPlocBlock, kPlocBlock, 0, s>>>(cl, cur_n, nbox, nn);
+        k_ploc_flags<<<grid, 256, 0, s>>>(nn, cur_n, merge, valid);
+        scan_i32(merge, cur_n, m_off, block_sums, d_total, s);
+        scan_i32(valid, cur_n, v_off, block_sums, d_total + 1, s);
+        int tot[2] = {0, 0};
+        WF_TRY(cudaMemcpyAsync(tot, d_total, sizeof(tot), cudaMemcpyDeviceToHost, s));
+        WF_TRY(cudaStreamSynchronize(s));
+        if (tot[0] <= 0 || tot[1] != cur_n - tot[0]) {
+            err = "PLOC iteration merged no clusters";
+            return -1;
+        }
+        k_ploc_apply<<<grid, 256, 0, s>>>(cl, nn, cur_n, merge, m_off, valid, v_off, next_id, n, nbox, left, right,
+                                         cnt, cl2);
+        iters.push_back({next_id, tot[0]});
+        next_id += tot[0];
+        std::swap(cl, cl2);
+        cur_n = tot[1];
+    }
+    root = n == 1 ? 0 : next_id - 1;
+    k_ploc_root<<<1, 1, 0, s>>>(root, offset, depth);
+    for (auto it = iters.rbegin(); it != iters.rend(); ++it)
+        k_ploc_topdown<<<std::max(1, std::min(grid, (it->second + 255) / 256)), 256, 0, s>>>(
+            it->first, it->second, n, left, right, cnt, offset, depth);
+    k_ploc_order<<<grid, 256, 0, s>>>(n, offset, sorted_ids, final_ids);
+    if (n <= kLeafMax) {
+        WF_TRY(cudaMalloc(&out.nodes, sizeof(BvhNode)));
+        k_ploc_single<<<1, 1, 0, s>>>(n, root, nbox, out.nodes);
+        out.num_nodes = 1;
+    } else {
+        const int ninternal = root - n + 1;
+        k_ploc_keep<<<grid, 256, 0, s>>>(n, root, cnt, keep);
+        scan_i32(keep, ninternal, newid, block_sums, d_total, s);
+        int kept = 0;
+        WF_TRY(cudaMemcpyAsync(&kept, d_total, sizeof(int), cudaMemcpyDeviceToHost, s));
+        WF_TRY(cudaStreamSynchronize(s));
+        WF_TRY(cudaMalloc(&out.nodes, sizeof(BvhNode) * (size_t)std::max(kept, 1)));
+        k_ploc_emit<<<grid, 256, 0, s>>>(n, root, left, right, cnt, offset, depth, keep, newid, nbox, out.nodes,
+                                        d_depth);
+        out.num_nodes = kept;
+        WF_TRY(cudaMemcpyAsync(&h_depth, d_depth, sizeof(int), cudaMemcpyDeviceToHost, s));
+    }
+    WF_TRY(cudaMalloc(&out.tris, 3 * sizeof(float4) * (size_t)n));
+    k_emit_tris<<<grid, 256, 0, s>>>(in.px, in.py, in.pz, in.idx, in.tri_geom, in.tri_prim, final_ids, n, out.tris);
+    WF_TRY(cudaGetLastError());
+    WF_TRY(cudaStreamSynchronize(s));
+    out.max_depth = h_depth;
+    if (h_depth + 2 > kStackSize) {
+        err = "BVH deeper than the traversal stack: depth " + std::to_string(h_depth);
+        goto fail;
+    }
+    return 0;
+fail:
     cudaFree(out.tris);
     cudaFree(out.nodes);
     out.tris = nullptr;

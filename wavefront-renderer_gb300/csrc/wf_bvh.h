@@ -30,4 +30,9 @@ struct BvhBuildOutput {
 int build_lbvh(const BvhBuildInput& in, BvhBuildOutput& out, int num_sms, cudaStream_t s,
                std::string& err);
 
+// PLOC (Meister & Bittner 2018) over the same Morton order: higher-quality
+// trees (smaller surface-area cost) for the same traversal layout.
+int build_ploc(const BvhBuildInput& in, BvhBuildOutput& out, int num_sms, cudaStream_t s,
+               std::string& err);
+
 }  // namespace wf
