@@ -552,6 +552,22 @@ int wf_host_scene_camera(const wf_host_scene* scene, int32_t width, int32_t heig
                          wf_camera* out_camera);
 int wf_host_scene_free(wf_host_scene* scene);
 
+/* ---- scene files and images (host only) -------------------------------------- */
+
+/* The reference loads scenes through OpenUSD (src/scene/UsdSceneLoader.cpp)
+ * and writes images through OpenImageIO, neither of which this build links.
+ * A scene file holds what the render path consumes — the flat
+ * Scene/SceneGeometry arrays, materials, textures, environment map,
+ * directional light — plus a default camera (look_from, look_at, up, vfov).
+ * wf_scene_load returns a wf_host_scene for wf_host_scene_describe /
+ * wf_host_scene_camera / wf_host_scene_free.  The layout is documented in
+ * wavefront-renderer_gb300/csrc/wf_scene_io.cpp. */
+int wf_scene_save(const char* path, const wf_scene_desc* desc, const float look_from[3], const float look_at[3],
+                  const float up[3], float vfov);
+int wf_scene_load(const char* path, wf_host_scene** out_scene);
+/* width*height*3 floats, top row first, as a little-endian PFM. */
+int wf_image_write_pfm(const char* path, const float* image_rgb, int32_t width, int32_t height);
+
 #ifdef __cplusplus
 }
 #endif

@@ -228,6 +228,9 @@ def _declare(lib: C.CDLL) -> None:
         "wf_render_device": ([V, C.POINTER(WfRenderParams), C.POINTER(WfRenderStats)], C.c_int),
         "wf_image_download": ([V, f32p, C.c_int64], C.c_int),
         "wf_adaptive_sample_counts": ([V, i32p, C.c_int64], C.c_int),
+        "wf_scene_save": ([C.c_char_p, C.POINTER(WfSceneDesc), f32p, f32p, f32p, C.c_float], C.c_int),
+        "wf_scene_load": ([C.c_char_p, C.POINTER(V)], C.c_int),
+        "wf_image_write_pfm": ([C.c_char_p, f32p, C.c_int32, C.c_int32], C.c_int),
         "wf_cost_tracker_state": ([V, f64p, C.c_int32, f64p, C.c_int32], C.c_int),
         "wf_cost_tracker_replay": ([V, C.c_int32, C.c_int32, C.POINTER(C.c_uint64), C.POINTER(C.c_uint32), f64p],
                                    C.c_int),
@@ -278,17 +281,44 @@ def _check(rc: int, what: str, ctx=None) -> None:
         raise WfError(f"{what} failed: {ERRORS.get(rc, rc)} {msg}")
 
 
+def save_scene(path, desc: WfSceneDesc, look_from, look_at, up, vfov: float) -> None:
+    """Writes a scene description and its default camera (wf_scene_save)."""
+    v = [(C.c_float * 3)(*map(float, x)) for x in (look_from, look_at, up)]
+    _check(load_library().wf_scene_save(str(path).encode(), C.byref(desc), v[0], v[1], v[2], float(vfov)),
+           "wf_scene_save")
+
+
+def write_pfm(path, image: np.ndarray) -> None:
+    """An (h, w, 3) float image, top row first, as a PFM (wf_image_write_pfm)."""
+    img = np.ascontiguousarray(image, np.float32)
+    h, w, _ = img.shape
+    _check(load_library().wf_image_write_pfm(str(path).encode(), ptr(img), w, h), "wf_image_write_pfm")
+
+
 class HostScene:
     """A procedural workload (wf_host_scene_*): 0 Cornell box, 1 icosphere
     scene (1.31 M triangles), 100 the icosphere scene at subdivision 4."""
 
-    def __init__(self, config: int, seed: int = 1):
+    def __init__(self, config: int, seed: int = 1, *, _handle: C.c_void_p | None = None):
         lib = load_library()
-        self._h = C.c_void_p()
-        _check(lib.wf_host_scene_generate(config, seed, C.byref(self._h)), "wf_host_scene_generate")
+        if _handle is None:
+            self._h = C.c_void_p()
+            _check(lib.wf_host_scene_generate(config, seed, C.byref(self._h)), "wf_host_scene_generate")
+        else:
+            self._h = _handle
         self.desc = WfSceneDesc()
         _check(lib.wf_host_scene_describe(self._h, C.byref(self.desc)), "wf_host_scene_describe")
         self.config = config
+
+    @classmethod
+    def load(cls, path) -> "HostScene":
+        """A scene file written by save_scene (wf_scene_load)."""
+        h = C.c_void_p()
+        _check(load_library().wf_scene_load(str(path).encode(), C.byref(h)), "wf_scene_load")
+        return cls(-1, _handle=h)
+
+    def save(self, path, look_from, look_at, up, vfov) -> None:
+        save_scene(path, self.desc, look_from, look_at, up, vfov)
 
     def camera(self, width: int, height: int) -> WfCamera:
         cam = WfCamera()

@@ -29,7 +29,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-prec-div=true",
 CXX_FLAGS = ["-O2", "-fPIC", "-std=c++17", "-ffp-contract=off", "-I", str(ROOT / "include")]
 
 CUDA_SOURCES = ["wf_sort.cu", "wf_bvh.cu", "wf_render.cu", "wf_api.cpp", "wf_loop.cpp", "wf_static.cu"]
-HOST_SOURCES = ["wf_scenes.cpp"]
+HOST_SOURCES = ["wf_scenes.cpp", "wf_scene_io.cpp"]
 
 
 def nvcc() -> str:

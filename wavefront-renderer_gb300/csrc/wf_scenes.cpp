@@ -15,21 +15,7 @@
 
 #include "../../include/wf_api.h"
 
-struct wf_host_scene {
-    int32_t config = 0;
-    std::vector<float> px, py, pz;
-    std::vector<int32_t> idx;
-    std::vector<int32_t> mesh_off, mesh_cnt, mesh_mat;
-    std::vector<wf_material> mats;
-    std::vector<float> cu, cv;          // per triangle corner (only with UVs)
-    std::vector<uint8_t> has_uv;        // per mesh
-    std::vector<std::vector<uint32_t>> tex_pixels;  // RGBA8 texels
-    std::vector<wf_texture> textures;
-    std::vector<float> env;             // equirect RGB (width*height*3)
-    int32_t env_w = 0, env_h = 0;
-    float look_from[3], look_at[3], up[3];
-    float vfov = 40.0f;
-};
+#include "wf_host_scene.h"
 
 namespace {
 
@@ -506,7 +492,10 @@ void build_config2(wf_host_scene& s, uint64_t seed, int grid, int tex_size, int 
     const int ground_mat = (int)s.mats.size();
     s.mats.push_back(diffuse(0.45f, 0.45f, 0.42f));
     for (int t = 0; t < ntex; ++t) {
-        s.tex_pixels.push_back(make_texture(t, tex_size, seed));
+        const std::vector<uint32_t> px = make_texture(t, tex_size, seed);
+        std::vector<uint8_t> raw(px.size() * 4);
+        std::memcpy(raw.data(), px.data(), raw.size());
+        s.tex_data.push_back(std::move(raw));
         s.textures.push_back(wf_texture{tex_size, tex_size, WF_TEXEL_RGBA8_SRGB, nullptr});
     }
     // ground
@@ -654,7 +643,7 @@ int wf_host_scene_describe(const wf_host_scene* s, wf_scene_desc* d)
     }
     if (!s->textures.empty()) {
         auto* tex = const_cast<wf_host_scene*>(s);
-        for (size_t t = 0; t < tex->textures.size(); ++t) tex->textures[t].data = tex->tex_pixels[t].data();
+        for (size_t t = 0; t < tex->textures.size(); ++t) tex->textures[t].data = tex->tex_data[t].data();
         d->num_textures = (int32_t)s->textures.size();
         d->textures = s->textures.data();
     }
@@ -663,9 +652,9 @@ int wf_host_scene_describe(const wf_host_scene* s, wf_scene_desc* d)
         d->environment.height = s->env_h;
         d->environment.rgb = s->env.data();
     }
-    d->environment.intensity_scale = 1.0f;
-    d->environment.tint[0] = d->environment.tint[1] = d->environment.tint[2] = 1.0f;
-    d->directional.color[0] = d->directional.color[1] = d->directional.color[2] = 1.0f;
+    d->environment.intensity_scale = s->env_scale;
+    for (int k = 0; k < 3; ++k) d->environment.tint[k] = s->env_tint[k];
+    d->directional = s->dir;
     return WF_OK;
 }
 
