@@ -187,7 +187,9 @@ typedef struct wf_render_params {
      * WavefrontRenderer.cpp:612-625, 742-760, 800-844): a quarter of the
      * shaded hits time their scatter (and, when textured, their surface
      * colour lookup) in SM clock cycles; after every bounce each material's
-     * and texture's mean enters its EMA (weight 0.05), and relativeCost
+     * and texture's mean enters its EMA (weight 0.05) once per sample of the
+     * wave (the reference records once per bounce of a one-sample pass),
+     * and relativeCost
      * (1.0 below 50 records) drives cost-aware RR and the material /
      * costBenefit orders of the next bounce, as in the reference.  Takes
      * precedence over rel_cost_*.  Single renders only. */

@@ -176,7 +176,7 @@ int reset_cost_trackers(wf_ctx* c, int nmat, int ntex)
     if (rc) return rc;
     rc = zero_tracker(c, c->ct_tex, ntex);
     if (rc) return rc;
-    launch_cost_update(c->ct_mat, c->ct_tex, c->stream);  // no records yet: relativeCost 1.0
+    launch_cost_update(c->ct_mat, c->ct_tex, 1, c->stream);  // no records yet: relativeCost 1.0
     return WF_OK;
 }
 

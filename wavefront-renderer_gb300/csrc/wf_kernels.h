@@ -128,7 +128,8 @@ void launch_compact_active(const uint8_t* flag, int64_t np, int32_t* out, int32_
 void launch_finalize_counts(const float* accum, const int32_t* count, int64_t np, float* image, cudaStream_t s);
 void launch_fill_i32(int32_t* a, int64_t n, int32_t v, bool identity, cudaStream_t s);
 
-// Live CostTracker: fold the last bounce's timings into both trackers.
-void launch_cost_update(const CostTrackerDev& mat, const CostTrackerDev& tex, cudaStream_t s);
+// Live CostTracker: fold the last bounce's timings into both trackers
+// (`repeat` records of the bounce mean per item).
+void launch_cost_update(const CostTrackerDev& mat, const CostTrackerDev& tex, int repeat, cudaStream_t s);
 
 }  // namespace wf

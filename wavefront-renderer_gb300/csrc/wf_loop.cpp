@@ -102,7 +102,7 @@ int upload_wave(wf_ctx* c, const std::vector<WaveChunk>& chunks, int64_t total)
 // scene `policy_scene`.
 int wave_host(wf_ctx* c, int64_t total, int max_depth, int policy, bool ray_sort, int policy_scene,
               const double* rc_mat, const double* rc_tex, const DeviceJob* single_job, wf_render_stats& stats,
-              bool track_costs = false)
+              bool track_costs = false, int cost_records = 1)
 {
     std::vector<double> live_mat, live_tex;  // relativeCost of the live trackers, for the policies
     cudaStream_t s = c->stream;
@@ -175,7 +175,7 @@ int wave_host(wf_ctx* c, int64_t total, int max_depth, int policy, bool ray_sort
         launch_shade(T, c->rq[cur], hq_use, c->counters + 1, c->sh, c->counters + 2, c->rq[1 - cur], c->counters + 3,
                      c->arena, c->err_flag, PC, s);
         if (track_costs) {  // the tracker merge at the end of shadeAll (.cpp:800-844)
-            launch_cost_update(c->ct_mat, c->ct_tex, s);
+            launch_cost_update(c->ct_mat, c->ct_tex, cost_records, s);
             stats.kernel_launches += 1;
         }
         launch_occluded_render(T, c->sh, c->counters + 2, c->arena, c->counters + 5, c->err_flag, PC, s);
@@ -406,7 +406,7 @@ int render_single(wf_ctx* c, const wf_render_params* P, wf_render_stats* st)
         if (rc) return rc;
         rc = graph ? wave_graph(c, P->max_depth, P->enable_ray_sort != 0, stats)
                    : wave_host(c, pix * nspp, P->max_depth, P->policy, P->enable_ray_sort != 0, 0,
-                               P->rel_cost_material, P->rel_cost_texture, &table[0], stats, tracking);
+                               P->rel_cost_material, P->rel_cost_texture, &table[0], stats, tracking, nspp);
         if (rc) return rc;
         if (adaptive) {  // renderScene's per-sample adaptive block (.cpp:270-294)
             launch_adaptive_fold(c->ad_buf, np, nspp, c->arena, c->ad_mean, c->ad_m2, c->ad_count, c->ad_active,
@@ -640,7 +640,7 @@ int wf_cost_tracker_replay(wf_ctx* c, int32_t items, int32_t steps, const uint64
                                  cudaMemcpyHostToDevice, c->stream));
         WF_CK(c, cudaMemcpyAsync(c->ct_mat.cnt, counts + (size_t)k * items, sizeof(uint32_t) * items,
                                  cudaMemcpyHostToDevice, c->stream));
-        launch_cost_update(c->ct_mat, c->ct_tex, c->stream);
+        launch_cost_update(c->ct_mat, c->ct_tex, 1, c->stream);
         WF_CK(c, cudaStreamSynchronize(c->stream));  // the host rows are read before the next step
     }
     WF_CK(c, cudaMemcpyAsync(rel_out, c->ct_mat.rel, sizeof(double) * items, cudaMemcpyDeviceToHost, c->stream));

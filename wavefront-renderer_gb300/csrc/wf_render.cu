@@ -302,9 +302,12 @@ __device__ __forceinline__ void warp_cost_add(unsigned long long* sum, unsigned 
 
 // CostTracker::record for every item timed in the last bounce, in item order
 // (WavefrontRenderer.cpp:833-844), then relativeCost (CostTracker.h:42-55);
-// the bounce's sums are cleared.  Block 0 runs the materials, block 1 the
-// textures, each on one thread (the EMA total is a serial dependency).
-__device__ void cost_update_one(CostTrackerDev T)
+// the bounce's sums are cleared.  The reference records once per bounce of a
+// one-sample pass; a wave of k samples per pixel records its bounce mean k
+// times (`repeat`), so the EMA and the 50-record floor see the same number
+// of records.  Block 0 runs the materials, block 1 the textures, each on one
+// thread (the EMA total is a serial dependency).
+__device__ void cost_update_one(CostTrackerDev T, int repeat)
 {
     if (T.items <= 0) return;
     double total = *T.total;
@@ -315,17 +318,19 @@ __device__ void cost_update_one(CostTrackerDev T)
         const double c = (double)T.sum[i] / (double)n;
         T.sum[i] = 0ull;
         T.cnt[i] = 0u;
-        T.samples[i] += 1;
-        if (!T.init[i]) {
-            T.avg[i] = c;
-            T.init[i] = 1;
-            tracked += 1;
-            total += c;
-        } else {
-            const double old = T.avg[i];
-            const double nw = (1.0 - 0.05) * old + 0.05 * c;
-            T.avg[i] = nw;
-            total += (nw - old);
+        for (int r = 0; r < repeat; ++r) {
+            T.samples[i] += 1;
+            if (!T.init[i]) {
+                T.avg[i] = c;
+                T.init[i] = 1;
+                tracked += 1;
+                total += c;
+            } else {
+                const double old = T.avg[i];
+                const double nw = (1.0 - 0.05) * old + 0.05 * c;
+                T.avg[i] = nw;
+                total += (nw - old);
+            }
         }
     }
     *T.total = total;
@@ -341,10 +346,10 @@ __device__ void cost_update_one(CostTrackerDev T)
     }
 }
 
-__global__ void k_cost_update(CostTrackerDev mat, CostTrackerDev tex)
+__global__ void k_cost_update(CostTrackerDev mat, CostTrackerDev tex, int repeat)
 {
     if (threadIdx.x != 0) return;
-    cost_update_one(blockIdx.x == 0 ? mat : tex);
+    cost_update_one(blockIdx.x == 0 ? mat : tex, repeat);
 }
 
 // ---------------------------------------------------------------------------
@@ -1206,9 +1211,9 @@ void launch_finalize(const float* accum, int64_t n, float spp, float* image, cud
     k_finalize<<<grid_for(n, 256, 65535), 256, 0, s>>>(accum, n, spp, image);
 }
 
-void launch_cost_update(const CostTrackerDev& mat, const CostTrackerDev& tex, cudaStream_t s)
+void launch_cost_update(const CostTrackerDev& mat, const CostTrackerDev& tex, int repeat, cudaStream_t s)
 {
-    k_cost_update<<<2, 32, 0, s>>>(mat, tex);
+    k_cost_update<<<2, 32, 0, s>>>(mat, tex, repeat);
 }
 
 void launch_adaptive_fold(float* sample_buf, int64_t np, int nspp, float* accum, float* mean, float* m2,
