@@ -388,7 +388,7 @@ def main() -> int:
     ap.add_argument("--blocks-per-sm", type=int, default=0)
     ap.add_argument("--ref-rows", type=int, default=256)
     ap.add_argument("--ref-spp", type=int, default=16)
-    ap.add_argument("--bvh", default="ploc", choices=["ploc", "lbvh"])
+    ap.add_argument("--bvh", default="wide", choices=["wide", "ploc", "lbvh"])
     args = ap.parse_args()
     args.warmup = max(args.warmup, 0)
     if args.workload == "c3":
@@ -406,7 +406,8 @@ def main() -> int:
     pkg = load_pkg()
     ctx = pkg.Context(local)
     scene = pkg.HostScene(wl["config"])
-    ctx.set_tuning(max(args.trace_variant, 0), args.blocks_per_sm, bvh_builder=1 if args.bvh == "lbvh" else 0)
+    ctx.set_tuning(max(args.trace_variant, 0), args.blocks_per_sm,
+                   bvh_builder={"wide": 0, "lbvh": 1, "ploc": 2}[args.bvh])
     info = ctx.upload(scene.desc)
     W, H = wl["width"], wl["height"]
     cam = scene.camera(W, H)
@@ -487,7 +488,8 @@ def main() -> int:
         "clocks": clocks,
         "gpu_launches": int(sum(s["kernel_launches"] for s in stats)),
         "bvh_build_ms": info.bvh_build_ms,
-        "bvh": {"builder": ["ploc", "lbvh"][info.bvh_builder], "nodes": info.bvh_nodes, "depth": info.bvh_depth},
+        "bvh": {"builder": ["ploc_wide8", "lbvh", "ploc"][info.bvh_builder], "nodes": info.bvh_nodes,
+                "depth": info.bvh_depth},
         "tuning": ctx.get_tuning(),
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

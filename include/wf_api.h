@@ -273,8 +273,8 @@ typedef struct wf_scene_info {
 int wf_scene_get_info(wf_ctx* ctx, wf_scene_info* out_info);
 
 /* Launch tuning of a context (the autotuner's knobs).  trace_variant: 0 = no
- * occupancy hint on the traversal kernels, 1 = 10 blocks of 128 threads per
- * SM, 2 = 12 blocks.  persistent_blocks_per_sm: resident blocks launched per
+ * occupancy hint on the traversal kernels, 1 and 2 = 10 blocks of 128
+ * threads per SM.  persistent_blocks_per_sm: resident blocks launched per
  * SM by the persistent traversal kernels (0 = 16).  graph_mode: whether a
  * wave's bounce chain is captured once as a CUDA graph and replayed. */
 typedef struct wf_tuning {
@@ -282,10 +282,12 @@ typedef struct wf_tuning {
     int32_t persistent_blocks_per_sm;
     int32_t graph_mode;  /* 0 = graphs for batches and the server, 1 = also for
                             single renders, 2 = never (policy != none never) */
-    int32_t bvh_builder; /* scenes uploaded afterwards: 0 = PLOC (locally-
-                            ordered clustering, default), 1 = LBVH (Karras
-                            radix tree); PLOC falls back to LBVH if its tree is
-                            deeper than the traversal stack */
+    int32_t bvh_builder; /* scenes uploaded afterwards: 0 = PLOC tree
+                            (locally-ordered clustering) collapsed into
+                            compressed 8-wide nodes (default), 1 = LBVH binary
+                            tree (Karras radix tree), 2 = PLOC binary tree; a
+                            PLOC tree deeper than its traversal stack falls
+                            back to LBVH */
     int32_t reserved[4];
 } wf_tuning;
 int wf_set_tuning(wf_ctx* ctx, const wf_tuning* tuning);

@@ -506,3 +506,34 @@ def test_gpu_live_costs_only_reorder_shading(wf, ctx, scene_c2small, policy):
     assert np.isclose(img, base, rtol=1e-4, atol=1e-6).all(axis=2).mean() >= 0.999
     rel_m, rel_t = ctx.cost_tracker_state(scene_c2small.desc.num_materials, scene_c2small.desc.num_textures)
     assert np.all(rel_m > 0) and np.all(rel_t > 0)
+
+
+# ------------------------------------------------ BVH builders -------------
+
+@pytest.mark.parametrize("which", ["c0", "small", "c2small"])
+def test_bvh_builders_give_identical_hits(wf, orc, ctx, scene0, scene_small, scene_c2small, which):
+    """The compressed 8-wide PLOC tree, the binary PLOC tree and the LBVH
+    return the same closest hits and occlusion bit for bit (and the port's),
+    and each passes the build's structural check."""
+    scene = {"c0": scene0, "small": scene_small, "c2small": scene_c2small}[which]
+    rng = np.random.default_rng(21)
+    lo, hi = ([0.0, 0.01, 0.0], [16.0, 0.9, 16.0]) if which == "c2small" else \
+        ([-0.27, 0.01, -0.54], [0.27, 0.54, -0.01])
+    o, d = rays_in_box(rng, 60000, lo, hi)
+    maxd = rng.uniform(0.01, 2.0, len(o)).astype(np.float32)
+    port = orc.Port(scene.desc)
+    want = port.trace_closest(o, d)
+    want_occ = port.trace_occluded(o, d, maxd)
+    infos = []
+    try:
+        for builder in (0, 1, 2):
+            ctx.set_tuning(bvh_builder=builder)
+            infos.append(ctx.upload(scene.desc))
+            got = ctx.trace_closest(o, d)
+            for k in HIT_KEYS_EXACT:
+                assert np.array_equal(got[k], want[k]), (builder, k)
+            assert np.array_equal(ctx.trace_occluded(o, d, maxd), want_occ), builder
+    finally:
+        ctx.set_tuning()
+    assert [i.bvh_builder for i in infos] == [0, 1, 2]
+    assert infos[0].bvh_nodes < infos[2].bvh_nodes

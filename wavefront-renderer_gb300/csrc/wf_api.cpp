@@ -564,10 +564,13 @@ int build_scene(wf_ctx* c, const wf_scene_desc* D, ResidentScene& R)
         auto b0 = std::chrono::steady_clock::now();
         int brc = -1;
         if (c->tuning.bvh_builder == 0) {
-            brc = build_ploc(bi, bo, c->num_sms, s, err);
+            brc = build_ploc_wide(bi, bo, c->num_sms, s, err);
             R.info.bvh_builder = 0;
+        } else if (c->tuning.bvh_builder == 2) {
+            brc = build_ploc(bi, bo, c->num_sms, s, err);
+            R.info.bvh_builder = 2;
         }
-        if (brc) {  // LBVH on request, or when the PLOC tree is too deep
+        if (brc) {  // LBVH on request, or when a PLOC tree is too deep for its stack
             brc = build_lbvh(bi, bo, c->num_sms, s, err);
             R.info.bvh_builder = 1;
         }
@@ -575,12 +578,14 @@ int build_scene(wf_ctx* c, const wf_scene_desc* D, ResidentScene& R)
         cleanup_tmp();
         if (brc) return set_err(c, WF_ERR_CUDA, "BVH build failed: " + err);
         A.push_back(bo.tris);
-        A.push_back(bo.nodes);
+        if (bo.nodes) A.push_back(bo.nodes);
+        if (bo.wnodes) A.push_back(bo.wnodes);
         R.info.bvh_build_ms = std::chrono::duration<double, std::milli>(b1 - b0).count();
         R.info.bvh_depth = bo.max_depth;
     }
     S.tris = bo.tris;
     S.nodes = bo.nodes;
+    S.wnodes = bo.wnodes;
     S.num_tris = ntri;
     S.num_nodes = bo.num_nodes;
     S.root_is_empty = ntri == 0 ? 1 : 0;
@@ -721,7 +726,8 @@ int build_scene(wf_ctx* c, const wf_scene_desc* D, ResidentScene& R)
     I.num_meshes = D->num_meshes;
     I.num_emissive_meshes = (int32_t)em.size();
     I.bvh_nodes = bo.num_nodes;
-    int64_t bytes = (int64_t)ntri * 48 + (int64_t)bo.num_nodes * (int64_t)sizeof(BvhNode) +
+    int64_t bytes = (int64_t)ntri * 48 +
+                    (int64_t)bo.num_nodes * (int64_t)(bo.wnodes ? sizeof(WideNode) : sizeof(BvhNode)) +
                     (int64_t)pool_f.size() * 4 + (int64_t)pool_b.size() * 4;
     I.device_bytes = bytes;
     return WF_OK;
@@ -1121,7 +1127,7 @@ int wf_set_tuning(wf_ctx* c, const wf_tuning* t)
 {
     if (!c || !t) return WF_ERR_INVALID_ARGUMENT;
     if (t->trace_variant < 0 || t->trace_variant > 2 || t->persistent_blocks_per_sm < 0 ||
-        t->persistent_blocks_per_sm > 32 || t->bvh_builder < 0 || t->bvh_builder > 1)
+        t->persistent_blocks_per_sm > 32 || t->bvh_builder < 0 || t->bvh_builder > 2)
         return set_err(c, WF_ERR_INVALID_ARGUMENT, "tuning out of range");
     c->tuning = *t;
     return WF_OK;

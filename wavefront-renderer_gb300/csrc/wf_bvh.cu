@@ -518,6 +518,243 @@ __global__ void k_ploc_init(int n, const float* __restrict__ leaf_box, float* __
     }
 }
 
+// ---------------------------------------------------------------------------
+// Compressed 8-wide collapse of the PLOC tree, one level of wide nodes per
+// pass (items = binary node ids of the level's wide nodes).
+// ---------------------------------------------------------------------------
+
+// Children of each wide node: open the binary subtree greedily, always the
+// child of largest surface area among those with more than kWideLeafMax
+// triangles, until eight children or none left to open.
+__global__ void k_wide_gather(const int* __restrict__ items, int count, int num_tris, const int* __restrict__ left,
+                              const int* __restrict__ right, const int* __restrict__ cnt,
+                              const float* __restrict__ nbox, int* __restrict__ kids, int* __restrict__ n_int,
+                              int* __restrict__ n_tri)
+{
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
+        const int b = items[k];
+        int ch[8];
+        int m = 0;
+        if (cnt[b] <= kWideLeafMax) {  // a whole tree of <= 3 triangles: one leaf child
+            ch[m++] = b;
+        } else {
+            ch[m++] = left[b - num_tris];
+            ch[m++] = right[b - num_tris];
+            while (m < 8) {
+                int best = -1;
+                float best_a = -1.0f;
+                for (int i = 0; i < m; ++i) {
+                    if (cnt[ch[i]] <= kWideLeafMax) continue;
+                    const float* x = nbox + 6 * (int64_t)ch[i];
+                    const float dx = x[3] - x[0], dy = x[4] - x[1], dz = x[5] - x[2];
+                    const float a = dx * dy + dy * dz + dz * dx;
+                    if (a > best_a) {
+                        best_a = a;
+                        best = i;
+                    }
+                }
+                if (best < 0) break;
+                const int x = ch[best];
+                ch[best] = left[x - num_tris];
+                ch[m++] = right[x - num_tris];
+            }
+        }
+        int ni = 0, nt = 0;
+        for (int i = 0; i < 8; ++i) {
+            kids[8 * (int64_t)k + i] = i < m ? ch[i] : -1;
+            if (i < m) {
+                if (cnt[ch[i]] > kWideLeafMax)
+                    ++ni;
+                else
+                    nt += cnt[ch[i]];
+            }
+        }
+        n_int[k] = ni;
+        n_tri[k] = nt;
+    }
+}
+
+// Smallest power-of-two step 2^e (e in [-126, 127]) with lo + 255 * 2^e >= hi.
+__device__ __forceinline__ int wide_exponent(float lo, float hi)
+{
+    const double ext = (double)hi - (double)lo;
+    int e = -126;
+    if (ext > 0.0) e = max(-126, min(127, (int)ceil(log2(ext / 255.0))));
+    while (e < 127 && (double)lo + 255.0 * ldexp(1.0, e) < (double)hi) ++e;
+    return e;
+}
+
+__global__ void k_wide_emit(const int* __restrict__ items, int count, int level_base, int next_base, int tri_base0,
+                            const int* __restrict__ kids, const int* __restrict__ int_off,
+                            const int* __restrict__ tri_off, int num_tris, const int* __restrict__ cnt,
+                            const float* __restrict__ nbox, const int* __restrict__ offset,
+                            const uint32_t* __restrict__ final_ids, WideNode* __restrict__ wn,
+                            int* __restrict__ next_items, uint32_t* __restrict__ wide_ids)
+{
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
+        int ch[8];
+        int m = 0;
+        for (int i = 0; i < 8; ++i) {
+            const int c = kids[8 * (int64_t)k + i];
+            if (c >= 0) ch[m++] = c;
+        }
+        // padded child boxes and the node box
+        float bx[8][6];
+        float lo[3] = {3.0e38f, 3.0e38f, 3.0e38f}, hi[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
+        for (int i = 0; i < m; ++i) {
+            for (int a = 0; a < 6; ++a) bx[i][a] = nbox[6 * (int64_t)ch[i] + a];
+            pad_box(bx[i]);
+            for (int a = 0; a < 3; ++a) {
+                lo[a] = fminf(lo[a], bx[i][a]);
+                hi[a] = fmaxf(hi[a], bx[i][a + 3]);
+            }
+        }
+        // slot q takes the child nearest for rays of direction octant q
+        // (greedy on dot(child centre - node centre, octant direction))
+        int slot_child[8];
+        for (int q = 0; q < 8; ++q) slot_child[q] = -1;
+        bool placed[8] = {false, false, false, false, false, false, false, false};
+        for (int round = 0; round < m; ++round) {
+            float best = 3.0e38f;
+            int bi = -1, bs = -1;
+            for (int i = 0; i < m; ++i) {
+                if (placed[i]) continue;
+                const float cx = 0.5f * (bx[i][0] + bx[i][3]) - 0.5f * (lo[0] + hi[0]);
+                const float cy = 0.5f * (bx[i][1] + bx[i][4]) - 0.5f * (lo[1] + hi[1]);
+                const float cz = 0.5f * (bx[i][2] + bx[i][5]) - 0.5f * (lo[2] + hi[2]);
+                for (int q = 0; q < 8; ++q) {
+                    if (slot_child[q] >= 0) continue;
+                    const float cost = ((q & 1) ? -cx : cx) + ((q & 2) ? -cy : cy) + ((q & 4) ? -cz : cz);
+                    if (bi < 0 || cost < best) {
+                        best = cost;
+                        bi = i;
+                        bs = q;
+                    }
+                }
+            }
+            placed[bi] = true;
+            slot_child[bs] = bi;
+        }
+        WideNode nd;
+        uint8_t* raw = reinterpret_cast<uint8_t*>(&nd);
+        for (int a = 0; a < (int)sizeof(WideNode); ++a) raw[a] = 0;
+        double scale[3];
+        for (int a = 0; a < 3; ++a) {
+            const int e = wide_exponent(lo[a], hi[a]);
+            nd.p[a] = lo[a];
+            nd.e[a] = (uint8_t)(e + 127);
+            scale[a] = ldexp(1.0, e);
+        }
+        const uint32_t child_base = (uint32_t)(next_base + int_off[k]);
+        const uint32_t tri_base = (uint32_t)(tri_base0 + tri_off[k]);
+        nd.child_base = child_base;
+        nd.tri_base = tri_base;
+        int irank = 0, toff = 0;
+        for (int q = 0; q < 8; ++q) {
+            const int i = slot_child[q];
+            if (i < 0) continue;
+            const int c = ch[i];
+            if (cnt[c] > kWideLeafMax) {
+                nd.meta[q] = (uint8_t)(0x20 | (24 + q));
+                nd.imask |= (uint8_t)(1u << q);
+                next_items[child_base - next_base + irank] = c;
+                ++irank;
+            } else {
+                const int nc = cnt[c];
+                nd.meta[q] = (uint8_t)((((1u << nc) - 1u) << 5) | (uint32_t)toff);
+                for (int j = 0; j < nc; ++j) wide_ids[tri_base + toff + j] = final_ids[offset[c] + j];
+                toff += nc;
+            }
+            for (int a = 0; a < 3; ++a) {
+                const double ql = floor(((double)bx[i][a] - (double)lo[a]) / scale[a]);
+                const double qh = ceil(((double)bx[i][a + 3] - (double)lo[a]) / scale[a]);
+                nd.qlo[a][q] = (uint8_t)fmin(255.0, fmax(0.0, ql));
+                nd.qhi[a][q] = (uint8_t)fmin(255.0, fmax(0.0, qh));
+            }
+        }
+        wn[level_base + k] = nd;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Structural checks of a finished tree before it is used: every child index
+// and triangle range must lie inside the arrays (a failed check rejects the
+// tree; the traversal kernels then never see it).
+// ---------------------------------------------------------------------------
+__global__ void k_validate_wide(const WideNode* __restrict__ wn, int num_nodes, int num_tris, int* __restrict__ bad)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < num_nodes; i += gridDim.x * blockDim.x) {
+        const WideNode& nd = wn[i];
+        const int ni = __popc((unsigned)nd.imask);
+        bool ok = true;
+        if (ni > 0) ok = ok && nd.child_base > (uint32_t)i && (int64_t)nd.child_base + ni <= (int64_t)num_nodes;
+        for (int a = 0; a < 3; ++a) ok = ok && nd.e[a] >= 1 && nd.e[a] <= 254;
+        for (int q = 0; q < 8; ++q) {
+            const uint32_t m = nd.meta[q];
+            const bool interior = ((nd.imask >> q) & 1u) != 0;
+            if (m == 0) {
+                ok = ok && !interior;
+                continue;
+            }
+            if ((m & 0x1Fu) >= 24u) {
+                ok = ok && interior && (m & 0x1Fu) == 24u + (uint32_t)q && (m >> 5) == 1u;
+            } else {
+                const uint32_t u = m >> 5, off = m & 0x1Fu;
+                const int c = u == 1u ? 1 : (u == 3u ? 2 : (u == 7u ? 3 : 0));
+                ok = ok && !interior && c > 0 && off + (uint32_t)c <= 24u &&
+                     (int64_t)nd.tri_base + off + c <= (int64_t)num_tris;
+            }
+        }
+        if (!ok) atomicOr(bad, 1);
+    }
+}
+
+__global__ void k_validate_binary(const BvhNode* __restrict__ nodes, int num_nodes, int num_tris, int* __restrict__ bad)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < num_nodes; i += gridDim.x * blockDim.x) {
+        bool ok = true;
+        const int kid[2] = {nodes[i].kids.x, nodes[i].kids.y};
+        for (int c = 0; c < 2; ++c) {
+            const uint32_t k = (uint32_t)kid[c];
+            if (k & kLeafFlag) {
+                const int64_t first = (int64_t)((k & ~kLeafFlag) >> 3), cnt = (int64_t)(k & 7u) + 1;
+                // an unreachable empty child (inverted box) may carry count 1 at 0
+                ok = ok && first + cnt <= (int64_t)num_tris;
+            } else {
+                ok = ok && (int)k >= 0 && (int)k < num_nodes && (int)k != i;
+            }
+        }
+        if (!ok) atomicOr(bad, 1);
+    }
+}
+
+int validate_tree(const BvhBuildOutput& out, int num_tris, int num_sms, cudaStream_t s, std::string& err)
+{
+    int* d_bad = nullptr;
+    int bad = 0;
+    if (cudaMalloc(&d_bad, sizeof(int)) != cudaSuccess) {
+        err = "validation buffer";
+        return -1;
+    }
+    cudaMemsetAsync(d_bad, 0, sizeof(int), s);
+    if (out.wnodes)
+        k_validate_wide<<<num_sms * 8, 256, 0, s>>>(out.wnodes, out.num_nodes, num_tris, d_bad);
+    else if (out.nodes)
+        k_validate_binary<<<num_sms * 8, 256, 0, s>>>(out.nodes, out.num_nodes, num_tris, d_bad);
+    cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, s);
+    const cudaError_t e = cudaStreamSynchronize(s);
+    cudaFree(d_bad);
+    if (e != cudaSuccess) {
+        err = std::string("tree validation: ") + cudaGetErrorString(e);
+        return -1;
+    }
+    if (bad) {
+        err = "tree failed its structural check";
+        return -1;
+    }
+    return 0;
+}
+
 #define WF_TRY(x)                                                      \
     do {                                                               \
         cudaError_t e_ = (x);                                          \
@@ -680,23 +917,27 @@ struct BuildScratch {
     }
 };
 
-}  // namespace
+// The binary PLOC tree: node ids 0..n-1 triangles (Morton position), n..
+// interior nodes; boxes unpadded; offset = first triangle position of a
+// node's subtree in depth-first order (final_ids maps positions to
+// triangles); depth from the root.
+struct PlocTree {
+    int n = 0, root = 0;
+    float* nbox = nullptr;
+    int *cnt = nullptr, *left = nullptr, *right = nullptr, *offset = nullptr, *depth = nullptr;
+    int *block_sums = nullptr, *d_total = nullptr;
+    uint32_t* final_ids = nullptr;
+};
 
-int build_ploc(const BvhBuildInput& in, BvhBuildOutput& out, int num_sms, cudaStream_t s, std::string& err)
+int ploc_tree(const BvhBuildInput& in, int num_sms, cudaStream_t s, std::string& err, BuildScratch& B, PlocTree& T)
 {
     const int n = in.num_tris;
-    out.tris = nullptr;
-    out.nodes = nullptr;
-    out.num_nodes = 0;
-    out.max_depth = 0;
-    if (n <= 0) return 0;
-    BuildScratch B;
-    float *tri_box, *leaf_box, *nbox;
+    T.n = n;
+    float *tri_box, *leaf_box;
     uint64_t *codes, *codes_tmp;
-    uint32_t *ids, *ids_tmp, *hist, *final_ids;
+    uint32_t *ids, *ids_tmp, *hist;
     unsigned long long* d_n;
-    int *cnt, *left, *right, *cl, *cl2, *nn, *merge, *valid, *m_off, *v_off, *block_sums, *d_total, *offset,
-        *depth, *keep, *newid, *d_depth;
+    int *cl, *cl2, *nn, *merge, *valid, *m_off, *v_off;
     uint64_t* sorted_codes = nullptr;
     uint32_t* sorted_ids = nullptr;
     const int64_t nn_all = 2 * (int64_t)n - 1;
@@ -706,21 +947,21 @@ int build_ploc(const BvhBuildInput& in, BvhBuildOutput& out, int num_sms, cudaSt
     const float3 sext = make_float3(in.bmax[0] - in.bmin[0], in.bmax[1] - in.bmin[1], in.bmax[2] - in.bmin[2]);
     const unsigned long long hn = (unsigned long long)n;
     std::vector<std::pair<int, int>> iters;  // (first node id, nodes) per iteration
-    int cur_n = n, next_id = n, h_depth = 0, root = 0;
+    int cur_n = n, next_id = n;
 
     WF_TRY(B.alloc(&tri_box, 6 * (size_t)n));
     WF_TRY(B.alloc(&leaf_box, 6 * (size_t)n));
-    WF_TRY(B.alloc(&nbox, 6 * (size_t)nn_all));
+    WF_TRY(B.alloc(&T.nbox, 6 * (size_t)nn_all));
     WF_TRY(B.alloc(&codes, (size_t)n));
     WF_TRY(B.alloc(&codes_tmp, (size_t)n));
     WF_TRY(B.alloc(&ids, (size_t)n));
     WF_TRY(B.alloc(&ids_tmp, (size_t)n));
     WF_TRY(B.alloc(&hist, radix_hist_words(nb)));
-    WF_TRY(B.alloc(&final_ids, (size_t)n));
+    WF_TRY(B.alloc(&T.final_ids, (size_t)n));
     WF_TRY(B.alloc(&d_n, 1));
-    WF_TRY(B.alloc(&cnt, (size_t)nn_all));
-    WF_TRY(B.alloc(&left, (size_t)n));
-    WF_TRY(B.alloc(&right, (size_t)n));
+    WF_TRY(B.alloc(&T.cnt, (size_t)nn_all));
+    WF_TRY(B.alloc(&T.left, (size_t)n));
+    WF_TRY(B.alloc(&T.right, (size_t)n));
     WF_TRY(B.alloc(&cl, (size_t)n));
     WF_TRY(B.alloc(&cl2, (size_t)n));
     WF_TRY(B.alloc(&nn, (size_t)n));
@@ -728,14 +969,10 @@ int build_ploc(const BvhBuildInput& in, BvhBuildOutput& out, int num_sms, cudaSt
     WF_TRY(B.alloc(&valid, (size_t)n));
     WF_TRY(B.alloc(&m_off, (size_t)n));
     WF_TRY(B.alloc(&v_off, (size_t)n));
-    WF_TRY(B.alloc(&block_sums, (size_t)(n + 1023) / 1024 + 1));
-    WF_TRY(B.alloc(&d_total, 2));
-    WF_TRY(B.alloc(&offset, (size_t)nn_all));
-    WF_TRY(B.alloc(&depth, (size_t)nn_all));
-    WF_TRY(B.alloc(&keep, (size_t)n));
-    WF_TRY(B.alloc(&newid, (size_t)n));
-    WF_TRY(B.alloc(&d_depth, 1));
-    WF_TRY(cudaMemsetAsync(d_depth, 0, sizeof(int), s));
+    WF_TRY(B.alloc(&T.block_sums, (size_t)(n + 1023) / 1024 + 1));
+    WF_TRY(B.alloc(&T.d_total, 2));
+    WF_TRY(B.alloc(&T.offset, (size_t)nn_all));
+    WF_TRY(B.alloc(&T.depth, (size_t)nn_all));
     WF_TRY(cudaMemcpyAsync(d_n, &hn, sizeof(hn), cudaMemcpyHostToDevice, s));
 
     k_tri_prep<<<grid, 256, 0, s>>>(in.px, in.py, in.pz, in.idx, n, smin, sext, tri_box, codes, ids);
@@ -744,55 +981,79 @@ int build_ploc(const BvhBuildInput& in, BvhBuildOutput& out, int num_sms, cudaSt
         radix_sort_pairs(a, s);
     }
     k_leaf_boxes<<<grid, 256, 0, s>>>(tri_box, sorted_ids, n, leaf_box);
-    k_ploc_init<<<grid, 256, 0, s>>>(n, leaf_box, nbox, cnt, cl);
+    k_ploc_init<<<grid, 256, 0, s>>>(n, leaf_box, T.nbox, T.cnt, cl);
     while (cur_n > 1) {
-        if (iters.size() > 100000) {
-            err = "PLOC did not converge";
-            return -1;
-        }
-        k_ploc_nn<<<(cur_n + kPlocBlock - 1) / kPlocBlock, kPlocBlock, 0, s>>>(cl, cur_n, nbox, nn);
+        k_ploc_nn<<<(cur_n + kPlocBlock - 1) / kPlocBlock, kPlocBlock, 0, s>>>(cl, cur_n, T.nbox, nn);
         k_ploc_flags<<<grid, 256, 0, s>>>(nn, cur_n, merge, valid);
-        scan_i32(merge, cur_n, m_off, block_sums, d_total, s);
-        scan_i32(valid, cur_n, v_off, block_sums, d_total + 1, s);
+        scan_i32(merge, cur_n, m_off, T.block_sums, T.d_total, s);
+        scan_i32(valid, cur_n, v_off, T.block_sums, T.d_total + 1, s);
         int tot[2] = {0, 0};
-        WF_TRY(cudaMemcpyAsync(tot, d_total, sizeof(tot), cudaMemcpyDeviceToHost, s));
+        WF_TRY(cudaMemcpyAsync(tot, T.d_total, sizeof(tot), cudaMemcpyDeviceToHost, s));
         WF_TRY(cudaStreamSynchronize(s));
         if (tot[0] <= 0 || tot[1] != cur_n - tot[0]) {
             err = "PLOC iteration merged no clusters";
             return -1;
         }
-        k_ploc_apply<<<grid, 256, 0, s>>>(cl, nn, cur_n, merge, m_off, valid, v_off, next_id, n, nbox, left, right,
-                                         cnt, cl2);
+        k_ploc_apply<<<grid, 256, 0, s>>>(cl, nn, cur_n, merge, m_off, valid, v_off, next_id, n, T.nbox, T.left,
+                                         T.right, T.cnt, cl2);
         iters.push_back({next_id, tot[0]});
         next_id += tot[0];
         std::swap(cl, cl2);
         cur_n = tot[1];
     }
-    root = n == 1 ? 0 : next_id - 1;
-    k_ploc_root<<<1, 1, 0, s>>>(root, offset, depth);
+    T.root = n == 1 ? 0 : next_id - 1;
+    k_ploc_root<<<1, 1, 0, s>>>(T.root, T.offset, T.depth);
     for (auto it = iters.rbegin(); it != iters.rend(); ++it)
         k_ploc_topdown<<<std::max(1, std::min(grid, (it->second + 255) / 256)), 256, 0, s>>>(
-            it->first, it->second, n, left, right, cnt, offset, depth);
-    k_ploc_order<<<grid, 256, 0, s>>>(n, offset, sorted_ids, final_ids);
+            it->first, it->second, n, T.left, T.right, T.cnt, T.offset, T.depth);
+    k_ploc_order<<<grid, 256, 0, s>>>(n, T.offset, sorted_ids, T.final_ids);
+    WF_TRY(cudaGetLastError());
+    return 0;
+fail:
+    return -1;
+}
+
+}  // namespace
+
+int build_ploc(const BvhBuildInput& in, BvhBuildOutput& out, int num_sms, cudaStream_t s, std::string& err)
+{
+    const int n = in.num_tris;
+    out.tris = nullptr;
+    out.nodes = nullptr;
+    out.wnodes = nullptr;
+    out.num_nodes = 0;
+    out.max_depth = 0;
+    if (n <= 0) return 0;
+    BuildScratch B;
+    PlocTree T;
+    int *keep, *newid, *d_depth;
+    const int grid = num_sms * 8;
+    int h_depth = 0;
+    if (ploc_tree(in, num_sms, s, err, B, T)) goto fail;
+    WF_TRY(B.alloc(&keep, (size_t)n));
+    WF_TRY(B.alloc(&newid, (size_t)n));
+    WF_TRY(B.alloc(&d_depth, 1));
+    WF_TRY(cudaMemsetAsync(d_depth, 0, sizeof(int), s));
     if (n <= kLeafMax) {
         WF_TRY(cudaMalloc(&out.nodes, sizeof(BvhNode)));
-        k_ploc_single<<<1, 1, 0, s>>>(n, root, nbox, out.nodes);
+        k_ploc_single<<<1, 1, 0, s>>>(n, T.root, T.nbox, out.nodes);
         out.num_nodes = 1;
     } else {
-        const int ninternal = root - n + 1;
-        k_ploc_keep<<<grid, 256, 0, s>>>(n, root, cnt, keep);
-        scan_i32(keep, ninternal, newid, block_sums, d_total, s);
+        const int ninternal = T.root - n + 1;
+        k_ploc_keep<<<grid, 256, 0, s>>>(n, T.root, T.cnt, keep);
+        scan_i32(keep, ninternal, newid, T.block_sums, T.d_total, s);
         int kept = 0;
-        WF_TRY(cudaMemcpyAsync(&kept, d_total, sizeof(int), cudaMemcpyDeviceToHost, s));
+        WF_TRY(cudaMemcpyAsync(&kept, T.d_total, sizeof(int), cudaMemcpyDeviceToHost, s));
         WF_TRY(cudaStreamSynchronize(s));
         WF_TRY(cudaMalloc(&out.nodes, sizeof(BvhNode) * (size_t)std::max(kept, 1)));
-        k_ploc_emit<<<grid, 256, 0, s>>>(n, root, left, right, cnt, offset, depth, keep, newid, nbox, out.nodes,
-                                        d_depth);
+        k_ploc_emit<<<grid, 256, 0, s>>>(n, T.root, T.left, T.right, T.cnt, T.offset, T.depth, keep, newid, T.nbox,
+                                        out.nodes, d_depth);
         out.num_nodes = kept;
         WF_TRY(cudaMemcpyAsync(&h_depth, d_depth, sizeof(int), cudaMemcpyDeviceToHost, s));
     }
     WF_TRY(cudaMalloc(&out.tris, 3 * sizeof(float4) * (size_t)n));
-    k_emit_tris<<<grid, 256, 0, s>>>(in.px, in.py, in.pz, in.idx, in.tri_geom, in.tri_prim, final_ids, n, out.tris);
+    k_emit_tris<<<grid, 256, 0, s>>>(in.px, in.py, in.pz, in.idx, in.tri_geom, in.tri_prim, T.final_ids, n,
+                                     out.tris);
     WF_TRY(cudaGetLastError());
     WF_TRY(cudaStreamSynchronize(s));
     out.max_depth = h_depth;
@@ -800,12 +1061,97 @@ int build_ploc(const BvhBuildInput& in, BvhBuildOutput& out, int num_sms, cudaSt
         err = "BVH deeper than the traversal stack: depth " + std::to_string(h_depth);
         goto fail;
     }
+    if (validate_tree(out, n, num_sms, s, err)) goto fail;
     return 0;
 fail:
     cudaFree(out.tris);
     cudaFree(out.nodes);
     out.tris = nullptr;
     out.nodes = nullptr;
+    return -1;
+}
+
+int build_ploc_wide(const BvhBuildInput& in, BvhBuildOutput& out, int num_sms, cudaStream_t s, std::string& err)
+{
+    const int n = in.num_tris;
+    out.tris = nullptr;
+    out.nodes = nullptr;
+    out.wnodes = nullptr;
+    out.num_nodes = 0;
+    out.max_depth = 0;
+    if (n <= 0) return 0;
+    BuildScratch B;
+    PlocTree T;
+    const int grid = num_sms * 8;
+    int *items, *next_items, *kids, *n_int, *n_tri, *int_off, *tri_off;
+    uint32_t* wide_ids;
+    int64_t cap_items = std::max(16, n / 2 + 16);
+    int64_t cap_nodes = std::max<int64_t>(16, n / 4 + 16);
+    int level_base = 0, count = 1, next_base = 1, tri_base = 0, levels = 0;
+    if (ploc_tree(in, num_sms, s, err, B, T)) goto fail;
+    WF_TRY(B.alloc(&items, (size_t)cap_items));
+    WF_TRY(B.alloc(&next_items, (size_t)cap_items));
+    WF_TRY(B.alloc(&kids, 8 * (size_t)cap_items));
+    WF_TRY(B.alloc(&n_int, (size_t)cap_items));
+    WF_TRY(B.alloc(&n_tri, (size_t)cap_items));
+    WF_TRY(B.alloc(&int_off, (size_t)cap_items));
+    WF_TRY(B.alloc(&tri_off, (size_t)cap_items));
+    WF_TRY(B.alloc(&wide_ids, (size_t)n));
+    WF_TRY(cudaMalloc(&out.wnodes, sizeof(WideNode) * (size_t)cap_nodes));
+    WF_TRY(cudaMemcpyAsync(items, &T.root, sizeof(int), cudaMemcpyHostToDevice, s));
+    while (count > 0) {
+        if (++levels > kWideStack) {
+            err = "wide BVH deeper than the traversal stack";
+            goto fail;
+        }
+        const int g = std::max(1, std::min(grid, (count + 127) / 128));
+        k_wide_gather<<<g, 128, 0, s>>>(items, count, n, T.left, T.right, T.cnt, T.nbox, kids, n_int, n_tri);
+        scan_i32(n_int, count, int_off, T.block_sums, T.d_total, s);
+        scan_i32(n_tri, count, tri_off, T.block_sums, T.d_total + 1, s);
+        int tot[2] = {0, 0};
+        WF_TRY(cudaMemcpyAsync(tot, T.d_total, sizeof(tot), cudaMemcpyDeviceToHost, s));
+        WF_TRY(cudaStreamSynchronize(s));
+        if (tot[0] > cap_items) {  // a level holds disjoint subtrees of > 3 triangles: at most n/4
+            err = "wide BVH level larger than its buffers";
+            goto fail;
+        }
+        if ((int64_t)next_base + tot[0] > cap_nodes) {
+            // grow the node array (and the level buffers) and carry on
+            const int64_t need_nodes = std::max<int64_t>(2 * cap_nodes, (int64_t)next_base + tot[0]);
+            WideNode* bigger = nullptr;
+            WF_TRY(cudaMalloc(&bigger, sizeof(WideNode) * (size_t)need_nodes));
+            WF_TRY(cudaMemcpyAsync(bigger, out.wnodes, sizeof(WideNode) * (size_t)level_base, cudaMemcpyDeviceToDevice,
+                                   s));
+            WF_TRY(cudaStreamSynchronize(s));
+            cudaFree(out.wnodes);
+            out.wnodes = bigger;
+            cap_nodes = need_nodes;
+        }
+        k_wide_emit<<<g, 128, 0, s>>>(items, count, level_base, next_base, tri_base, kids, int_off, tri_off, n,
+                                      T.cnt, T.nbox, T.offset, T.final_ids, out.wnodes, next_items, wide_ids);
+        std::swap(items, next_items);
+        level_base = next_base;
+        next_base += tot[0];
+        tri_base += tot[1];
+        count = tot[0];
+    }
+    if (tri_base != n) {
+        err = "wide BVH lost triangles";
+        goto fail;
+    }
+    WF_TRY(cudaMalloc(&out.tris, 3 * sizeof(float4) * (size_t)n));
+    k_emit_tris<<<grid, 256, 0, s>>>(in.px, in.py, in.pz, in.idx, in.tri_geom, in.tri_prim, wide_ids, n, out.tris);
+    WF_TRY(cudaGetLastError());
+    WF_TRY(cudaStreamSynchronize(s));
+    out.num_nodes = level_base;  // every level written: total nodes
+    out.max_depth = levels;
+    if (validate_tree(out, n, num_sms, s, err)) goto fail;
+    return 0;
+fail:
+    cudaFree(out.tris);
+    cudaFree(out.wnodes);
+    out.tris = nullptr;
+    out.wnodes = nullptr;
     return -1;
 }
 

@@ -21,9 +21,10 @@ struct BvhBuildInput {
 
 struct BvhBuildOutput {
     float4* tris;      // 3 * num_tris float4 (cudaMalloc'd; caller frees)
-    BvhNode* nodes;    // num_nodes (cudaMalloc'd; caller frees)
+    BvhNode* nodes;    // num_nodes (cudaMalloc'd; caller frees), binary trees
     int num_nodes;
     int max_depth;
+    WideNode* wnodes = nullptr;  // compressed 8-wide tree instead of nodes
 };
 
 // Returns 0 on success, -1 with err set otherwise.
@@ -34,5 +35,12 @@ int build_lbvh(const BvhBuildInput& in, BvhBuildOutput& out, int num_sms, cudaSt
 // trees (smaller surface-area cost) for the same traversal layout.
 int build_ploc(const BvhBuildInput& in, BvhBuildOutput& out, int num_sms, cudaStream_t s,
                std::string& err);
+
+// PLOC tree collapsed top-down into compressed 8-wide nodes (WideNode):
+// each wide node opens the binary subtree greedily (largest surface area
+// first) up to eight children; subtrees of <= kWideLeafMax triangles become
+// leaf children.  out.wnodes / out.num_nodes / out.max_depth (wide levels).
+int build_ploc_wide(const BvhBuildInput& in, BvhBuildOutput& out, int num_sms, cudaStream_t s,
+                    std::string& err);
 
 }  // namespace wf

@@ -50,13 +50,39 @@ struct EmissiveMesh {
     int32_t pad;
 };
 
+// Compressed 8-wide BVH node (Ylitie, Karras & Laine, "Efficient Incoherent
+// Ray Traversal on GPUs Through Compressed Wide BVHs", HPG 2017): the child
+// boxes are quantized to 8 bits per plane on a power-of-two grid anchored
+// at p, conservatively (floor for lower planes, ceil for upper planes, boxes
+// padded before quantizing).  Interior children are stored contiguously
+// from child_base in slot order; leaf children (1-3 triangles) contiguously
+// from tri_base.  meta[s]: 0 = empty slot; interior 0x20 | (24 + s); leaf
+// (unary triangle count << 5) | offset from tri_base.  Slot s holds the child
+// nearest for rays whose direction octant (bit set = negative component) is
+// s, so popping hit slots by descending (s ^ octant ^ 7) visits near
+// children first.
+struct alignas(16) WideNode {
+    float p[3];
+    uint8_t e[3];         // per-axis scale 2^(e - 127)
+    uint8_t imask;        // bit s: slot s holds an interior child
+    uint32_t child_base;
+    uint32_t tri_base;
+    uint8_t meta[8];
+    uint8_t qlo[3][8];
+    uint8_t qhi[3][8];
+};
+static_assert(sizeof(WideNode) == 80, "WideNode is five 16-byte words");
+constexpr int kWideLeafMax = 3;   // triangles per leaf child
+constexpr int kWideStack = 32;    // node-group stack entries (checked at build)
+
 struct DeviceScene {
     // Triangles in BVH leaf order: 3 float4 each.
     //   [0] = v0.xyz, w = global triangle index (bits)
     //   [1] = (v1 - v0).xyz, w = geomID (mesh index)
     //   [2] = (v2 - v0).xyz, w = primID (index within the mesh)
     const float4* tris;
-    const BvhNode* nodes;
+    const BvhNode* nodes;      // binary tree, or null when wnodes is set
+    const WideNode* wnodes;    // compressed 8-wide tree, or null
     int32_t num_tris;
     int32_t num_nodes;
     int32_t root_is_empty;  // scene without triangles

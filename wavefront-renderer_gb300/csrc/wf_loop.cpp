@@ -97,6 +97,20 @@ int upload_wave(wf_ctx* c, const std::vector<WaveChunk>& chunks, int64_t total)
     return WF_OK;
 }
 
+// Whether the resident scenes carry compressed 8-wide trees; a wave's
+// kernels use one traversal, so the formats must not be mixed.
+int table_wide(wf_ctx* c, bool& wide)
+{
+    int w = 0, b = 0;
+    for (const auto& r : c->scenes)
+        if (r.live && r.S.num_tris > 0) ++(r.S.wnodes ? w : b);
+    if (w && b)
+        return set_err(c, WF_ERR_STATE,
+                       "resident scenes were built with different BVH formats (wf_tuning::bvh_builder)");
+    wide = w > 0;
+    return WF_OK;
+}
+
 // One wave, one host round trip per bounce.  policy / ray sort as in the
 // reference (RayQueue::schedule + ShadingQueue::schedule), materials of
 // scene `policy_scene`.
@@ -106,10 +120,14 @@ int wave_host(wf_ctx* c, int64_t total, int max_depth, int policy, bool ray_sort
 {
     std::vector<double> live_mat, live_tex;  // relativeCost of the live trackers, for the policies
     cudaStream_t s = c->stream;
-    WaveTables T{c->d_scene_table, c->d_jobs, DeviceScene{}, DeviceJob{}, single_job == nullptr};
+    WaveTables T{c->d_scene_table, c->d_jobs, DeviceScene{}, DeviceJob{}, single_job == nullptr, false};
     if (single_job) {
         T.job0 = *single_job;
         T.scene0 = c->scenes[single_job->scene].S;
+        T.wide = T.scene0.wnodes != nullptr;
+    } else {
+        int rc = table_wide(c, T.wide);
+        if (rc) return rc;
     }
     const LaunchCfg PC = persist_cfg(c), WC = wide_cfg(c);
     cudaEvent_t* ev = c->ev;
@@ -206,13 +224,13 @@ int wave_host(wf_ctx* c, int64_t total, int max_depth, int policy, bool ray_sort
 
 // The launches of one wave with every count on the device: what a graph
 // captures.  Returns the number of kernels.
-int record_chain(wf_ctx* c, int max_depth, bool ray_sort)
+int record_chain(wf_ctx* c, int max_depth, bool ray_sort, bool wide)
 {
     cudaStream_t s = c->stream;
     const LaunchCfg PC = persist_cfg(c), WC = wide_cfg(c);
     int kernels = 0;
     int cur = 0;
-    const WaveTables T{c->d_scene_table, c->d_jobs, DeviceScene{}, DeviceJob{}, true};
+    const WaveTables T{c->d_scene_table, c->d_jobs, DeviceScene{}, DeviceJob{}, true, wide};
     launch_camera_chunks(c->d_chunks, c->d_wave_header, c->d_jobs, c->rq[cur], WC, s);
     cudaMemcpyAsync(c->counters, c->d_wave_header, sizeof(ull), cudaMemcpyDeviceToDevice, s);
     kernels += 1;
@@ -244,15 +262,18 @@ int record_chain(wf_ctx* c, int max_depth, bool ray_sort)
 int wave_graph(wf_ctx* c, int max_depth, bool ray_sort, wf_render_stats& stats)
 {
     cudaStream_t s = c->stream;
+    bool wide = false;
+    int rc = table_wide(c, wide);
+    if (rc) return rc;
     CapturedWave* g = nullptr;
     for (auto& x : c->graphs)
         if (x.max_depth == max_depth && x.ray_sort == ray_sort && x.variant == c->tuning.trace_variant &&
-            x.key_ptr == c->arena && x.key_cap == c->cap)
+            x.key_ptr == c->arena && x.key_cap == c->cap && x.wide == wide)
             g = &x;
     if (!g) {
         cudaGraph_t graph = nullptr;
         WF_CK(c, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-        int k = record_chain(c, max_depth, ray_sort);
+        int k = record_chain(c, max_depth, ray_sort, wide);
         cudaError_t e = cudaStreamEndCapture(s, &graph);
         if (e != cudaSuccess) return set_err(c, WF_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
         CapturedWave w;
@@ -264,6 +285,7 @@ int wave_graph(wf_ctx* c, int max_depth, bool ray_sort, wf_render_stats& stats)
         w.variant = c->tuning.trace_variant;
         w.key_ptr = c->arena;
         w.key_cap = c->cap;
+        w.wide = wide;
         w.kernels = k;
         c->graphs.push_back(w);
         g = &c->graphs.back();

@@ -195,7 +195,7 @@ __device__ __forceinline__ void accum_add(float* accum, int32_t slot, V3 c)
 // ---------------------------------------------------------------------------
 // kMulti = false: every ray belongs to job0 on scene0 (passed by value, read
 // from the constant bank); true: each ray looks its job and scene up.
-template <bool kMulti, int kMinBlocks>
+template <bool kMulti, int kMinBlocks, class Tr>
 __global__ void __launch_bounds__(128, kMinBlocks) k_trace_render(DeviceScene scene0, DeviceJob job0,
                                                                   const DeviceScene* __restrict__ scenes,
                                                                   const DeviceJob* __restrict__ jobs,
@@ -206,14 +206,14 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_trace_render(DeviceScene sc
     const int64_t n = (int64_t)*d_n;
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
-    Traversal<false> tr;
-    uint32_t stack[kStackSize];
+    Tr tr;
+    typename Tr::Entry stack[Tr::kStack];
     const DeviceScene* S = kMulti ? scenes : &scene0;
     int job = 0;
     int64_t ray = -1;
     bool exhausted = false;
     bool overflow = false;
-    tr.cur = kSentinel;
+    tr.idle();
     for (;;) {
         // 1. lanes whose traversal ended emit their result
         const bool fin = ray >= 0 && tr.done();
@@ -279,7 +279,7 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_trace_render(DeviceScene sc
         }
         if (__all_sync(0xFFFFFFFFu, ray < 0)) break;
         // 3. one traversal round
-        if (ray >= 0 && !tr.done()) tr.round(S->nodes, S->tris, stack);
+        if (ray >= 0 && !tr.done()) tr.round(*S, stack);
     }
     if (overflow) atomicOr(err, 1);
 }
@@ -626,7 +626,7 @@ __global__ void __launch_bounds__(128) k_shade(DeviceScene scene0, DeviceJob job
 // Shadow rays (EmbreeAccelerator::occluded): unblocked contributions are
 // added to their pixel.  Same persistent, dynamic-fetch structure as
 // k_trace_render.
-template <bool kMulti, int kMinBlocks>
+template <bool kMulti, int kMinBlocks, class Tr>
 __global__ void __launch_bounds__(128, kMinBlocks) k_occluded_render(DeviceScene scene0, DeviceJob job0,
                                                                      const DeviceScene* __restrict__ scenes,
                                                                      const DeviceJob* __restrict__ jobs,
@@ -637,14 +637,14 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_occluded_render(DeviceScene
     const int64_t n = (int64_t)*d_n;
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
-    Traversal<true> tr;
-    uint32_t stack[kStackSize];
+    Tr tr;
+    typename Tr::Entry stack[Tr::kStack];
     const DeviceScene* S = kMulti ? scenes : &scene0;
     int job = 0;
     int64_t ray = -1;
     bool exhausted = false;
     bool overflow = false;
-    tr.cur = kSentinel;
+    tr.idle();
     for (;;) {
         if (ray >= 0 && tr.done()) {
             if (tr.res.leafpos < 0)  // sh.pixel holds the slot (job_slot)
@@ -676,7 +676,7 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_occluded_render(DeviceScene
             }
         }
         if (__all_sync(0xFFFFFFFFu, ray < 0)) break;
-        if (ray >= 0 && !tr.done()) tr.round(S->nodes, S->tris, stack);
+        if (ray >= 0 && !tr.done()) tr.round(*S, stack);
     }
     if (overflow) atomicOr(err, 1);
 }
@@ -1092,18 +1092,22 @@ void launch_occluded_api(const DeviceScene& S, int64_t n, const float* ox, const
                                                              out, err);
 }
 
-// variant: 0 = no occupancy hint (~56 registers), 1 = 10 blocks of 128 per SM
-// (48 registers), 2 = 12 blocks (40 registers, small spills).
+// variant: 0 = no occupancy hint, 1 = 10 blocks of 128 per SM; the traversal
+// follows the scene's tree (compressed 8-wide or binary).
 void launch_trace_render(const WaveTables& t, RayQueueDev rq, const ull* d_n, HitQueueDev hq, ull* hq_n,
                          float* accum, ull* work, int* err, LaunchCfg cfg, cudaStream_t s)
 {
-#define WF_TRACE(M, B) \
-    k_trace_render<M, B><<<cfg.grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, d_n, hq, hq_n, accum, work, err)
-    if (t.multi) {
-        if (cfg.variant == 1) WF_TRACE(true, 10); else if (cfg.variant == 2) WF_TRACE(true, 12); else WF_TRACE(true, 1);
+#define WF_TRACE(M, B, T)                                                                                   \
+    k_trace_render<M, B, T><<<cfg.grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, d_n, hq, hq_n, \
+                                                     accum, work, err)
+#define WF_TRACE2(M, T) \
+    if (cfg.variant == 1) WF_TRACE(M, 10, T); else WF_TRACE(M, 1, T)
+    if (t.wide) {
+        if (t.multi) { WF_TRACE2(true, WideTraversal<false>); } else { WF_TRACE2(false, WideTraversal<false>); }
     } else {
-        if (cfg.variant == 1) WF_TRACE(false, 10); else if (cfg.variant == 2) WF_TRACE(false, 12); else WF_TRACE(false, 1);
+        if (t.multi) { WF_TRACE2(true, Traversal<false>); } else { WF_TRACE2(false, Traversal<false>); }
     }
+#undef WF_TRACE2
 #undef WF_TRACE
 }
 
@@ -1129,13 +1133,17 @@ void launch_shade(const WaveTables& t, RayQueueDev rq, HitQueueDev hq, const ull
 void launch_occluded_render(const WaveTables& t, ShadowQueueDev sh, const ull* sh_n, float* accum, ull* work,
                             int* err, LaunchCfg cfg, cudaStream_t s)
 {
-#define WF_OCC(M, B) \
-    k_occluded_render<M, B><<<cfg.grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, sh, sh_n, accum, work, err)
-    if (t.multi) {
-        if (cfg.variant == 1) WF_OCC(true, 10); else if (cfg.variant == 2) WF_OCC(true, 12); else WF_OCC(true, 1);
+#define WF_OCC(M, B, T)                                                                                       \
+    k_occluded_render<M, B, T><<<cfg.grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, sh, sh_n, accum, work, \
+                                                        err)
+#define WF_OCC2(M, T) \
+    if (cfg.variant == 1) WF_OCC(M, 10, T); else WF_OCC(M, 1, T)
+    if (t.wide) {
+        if (t.multi) { WF_OCC2(true, WideTraversal<true>); } else { WF_OCC2(false, WideTraversal<true>); }
     } else {
-        if (cfg.variant == 1) WF_OCC(false, 10); else if (cfg.variant == 2) WF_OCC(false, 12); else WF_OCC(false, 1);
+        if (t.multi) { WF_OCC2(true, Traversal<true>); } else { WF_OCC2(false, Traversal<true>); }
     }
+#undef WF_OCC2
 #undef WF_OCC
 }
 

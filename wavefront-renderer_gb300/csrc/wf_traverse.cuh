@@ -62,6 +62,8 @@ constexpr uint32_t kSentinel = 0xFFFFFFFFu;
 // and a persistent kernel can hand a finished lane a new ray between rounds.
 template <bool kAnyHit>
 struct Traversal {
+    using Entry = uint32_t;
+    static constexpr int kStack = kStackSize;
     V3 o, d, inv, oi;
     float tmin, best_t;
     int best_g;
@@ -89,6 +91,8 @@ struct Traversal {
         overflow = false;
     }
     __device__ __forceinline__ bool done() const { return cur == kSentinel; }
+    __device__ __forceinline__ void idle() { cur = kSentinel; }
+    __device__ __forceinline__ void round(const DeviceScene& S, uint32_t* stack) { round(S.nodes, S.tris, stack); }
 
     // nodes / tris of the ray's scene: from the kernel's parameter bank when
     // every ray shares one scene, else from the scene table.
@@ -145,20 +149,167 @@ struct Traversal {
     }
 };
 
+// Traversal of the compressed 8-wide BVH (WideNode), after Ylitie, Karras &
+// Laine (HPG 2017): the stack holds node groups (x = first interior child,
+// y = hit keys << 24 | interior mask); one round descends into the nearest
+// remaining hit child — pushing the rest of its group — intersects that
+// node's eight child boxes, and tests the triangles of the leaf children it
+// hit, or pops a group when nothing is left.  Same acceptance rule as the
+// binary traversal (smallest t, ties to the larger global index), so the
+// result does not depend on the tree.
+template <bool kAnyHit>
+struct WideTraversal {
+    using Entry = uint2;
+    static constexpr int kStack = kWideStack;
+    V3 o, d, inv, oi;
+    float tmin, best_t;
+    int best_g;
+    uint32_t octinv;
+    uint2 ng;  // node group
+    int sp;
+    bool fin;
+    bool overflow;
+    TraceResult res;
+
+    __device__ __forceinline__ void init(const DeviceScene& S, uint2* stack, V3 o_, V3 d_, float tmin_,
+                                         float tmax_)
+    {
+        (void)stack;
+        o = o_;
+        d = d_;
+        inv = v3(safe_inv(d.x), safe_inv(d.y), safe_inv(d.z));
+        oi = v3(o.x * inv.x, o.y * inv.y, o.z * inv.z);
+        tmin = tmin_;
+        best_t = tmax_;
+        best_g = -1;
+        res.leafpos = -1;
+        octinv = 7u ^ ((d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u));
+        // the root as the only interior child (slot 0) of a virtual group
+        ng = make_uint2(0u, (1u << (24u + octinv)) | 1u);
+        sp = 0;
+        fin = S.root_is_empty != 0;
+        overflow = false;
+    }
+    __device__ __forceinline__ bool done() const { return fin; }
+    __device__ __forceinline__ void idle() { fin = true; }
+
+    __device__ __forceinline__ void round(const DeviceScene& S, uint2* stack)
+    {
+        uint32_t tri_base = 0, tri_hits = 0;
+        if (ng.y > 0x00FFFFFFu) {
+            const uint32_t b = 31u - (uint32_t)__clz(ng.y);
+            ng.y &= ~(1u << b);
+            const uint32_t slot = (b - 24u) ^ octinv;
+            const uint32_t node = ng.x + (uint32_t)__popc(ng.y & ((1u << slot) - 1u) & 0xFFu);
+            if (ng.y > 0x00FFFFFFu) {
+                if (sp < kStack)
+                    stack[sp++] = ng;
+                else
+                    overflow = true;
+            }
+            intersect_node(S.wnodes + node, tri_base, tri_hits);
+        } else if (sp > 0) {
+            ng = stack[--sp];
+            return;
+        } else {
+            fin = true;
+            return;
+        }
+        while (tri_hits) {
+            const int lp = (int)tri_base + __ffs(tri_hits) - 1;
+            tri_hits &= tri_hits - 1u;
+            const float4 a = __ldg(S.tris + 3 * lp + 0);
+            const float4 bq = __ldg(S.tris + 3 * lp + 1);
+            const float4 c = __ldg(S.tris + 3 * lp + 2);
+            float th, uh, vh;
+            if (intersect_triangle(o, d, v3(a.x, a.y, a.z), v3(bq.x, bq.y, bq.z), v3(c.x, c.y, c.z), tmin, best_t,
+                                   th, uh, vh)) {
+                const int g = __float_as_int(a.w);
+                if (kAnyHit || th < best_t || res.leafpos < 0 || g > best_g) {
+                    res.leafpos = lp;
+                    res.t = th;
+                    res.bu = uh;
+                    res.bv = vh;
+                    best_t = th;
+                    best_g = g;
+                    if (kAnyHit) {
+                        fin = true;
+                        return;
+                    }
+                }
+            }
+        }
+    }
+
+    // Eight quantized child boxes; boxes are decoded as p + q * 2^e (one
+    // rounding) and slab-tested like the binary nodes.
+    __device__ __forceinline__ void intersect_node(const WideNode* nodep, uint32_t& tri_base, uint32_t& tri_hits)
+    {
+        const float4* q = reinterpret_cast<const float4*>(nodep);
+        const float4 w0 = __ldg(q), w1 = __ldg(q + 1), w2 = __ldg(q + 2), w3 = __ldg(q + 3), w4 = __ldg(q + 4);
+        const uint32_t hdr = __float_as_uint(w0.w);
+        const float sx = __uint_as_float((hdr & 0xFFu) << 23);
+        const float sy = __uint_as_float(((hdr >> 8) & 0xFFu) << 23);
+        const float sz = __uint_as_float(((hdr >> 16) & 0xFFu) << 23);
+        const uint32_t imask = hdr >> 24;
+        const uint32_t meta[2] = {__float_as_uint(w1.z), __float_as_uint(w1.w)};
+        const uint32_t lox[2] = {__float_as_uint(w2.x), __float_as_uint(w2.y)};
+        const uint32_t loy[2] = {__float_as_uint(w2.z), __float_as_uint(w2.w)};
+        const uint32_t loz[2] = {__float_as_uint(w3.x), __float_as_uint(w3.y)};
+        const uint32_t hix[2] = {__float_as_uint(w3.z), __float_as_uint(w3.w)};
+        const uint32_t hiy[2] = {__float_as_uint(w4.x), __float_as_uint(w4.y)};
+        const uint32_t hiz[2] = {__float_as_uint(w4.z), __float_as_uint(w4.w)};
+        uint32_t hits_i = 0, hits_t = 0;
+#pragma unroll
+        for (int s = 0; s < 8; ++s) {
+            const int wd = s >> 2, sh = 8 * (s & 3);
+            const uint32_t m = (meta[wd] >> sh) & 0xFFu;
+            const float lx = __fmaf_rn((float)((lox[wd] >> sh) & 0xFFu), sx, w0.x);
+            const float hx = __fmaf_rn((float)((hix[wd] >> sh) & 0xFFu), sx, w0.x);
+            const float ly = __fmaf_rn((float)((loy[wd] >> sh) & 0xFFu), sy, w0.y);
+            const float hy = __fmaf_rn((float)((hiy[wd] >> sh) & 0xFFu), sy, w0.y);
+            const float lz = __fmaf_rn((float)((loz[wd] >> sh) & 0xFFu), sz, w0.z);
+            const float hz = __fmaf_rn((float)((hiz[wd] >> sh) & 0xFFu), sz, w0.z);
+            const float tlx = __fmaf_rn(lx, inv.x, -oi.x), thx = __fmaf_rn(hx, inv.x, -oi.x);
+            const float tly = __fmaf_rn(ly, inv.y, -oi.y), thy = __fmaf_rn(hy, inv.y, -oi.y);
+            const float tlz = __fmaf_rn(lz, inv.z, -oi.z), thz = __fmaf_rn(hz, inv.z, -oi.z);
+            const float tn = fmaxf(fmaxf(fminf(tlx, thx), fminf(tly, thy)), fmaxf(fminf(tlz, thz), tmin));
+            const float tf = fminf(fminf(fmaxf(tlx, thx), fmaxf(tly, thy)), fminf(fmaxf(tlz, thz), best_t));
+            if (m != 0u && tn <= tf) {
+                if ((m & 0x1Fu) >= 24u)
+                    hits_i |= 1u << (24u + ((uint32_t)s ^ octinv));
+                else
+                    hits_t |= (m >> 5) << (m & 0x1Fu);
+            }
+        }
+        ng = make_uint2(__float_as_uint(w1.x), hits_i | imask);
+        tri_base = __float_as_uint(w1.y);
+        tri_hits = hits_t;
+    }
+};
+
 // Whole traversal of one ray (host-API kernels).  Returns false (and sets
 // *err_flag) only if the stack would overflow, which the build rules out by
 // checking the tree depth.
+template <class Tr>
+__device__ __forceinline__ bool traverse_with(const DeviceScene& S, V3 o, V3 d, float tmin, float tmax,
+                                              TraceResult& res, int* err_flag)
+{
+    Tr tr;
+    typename Tr::Entry stack[Tr::kStack];
+    tr.init(S, stack, o, d, tmin, tmax);
+    while (!tr.done()) tr.round(S, stack);
+    res = tr.res;
+    if (tr.overflow) atomicOr(err_flag, 1);
+    return !tr.overflow;
+}
+
 template <bool kAnyHit>
 __device__ __forceinline__ bool traverse(const DeviceScene& S, V3 o, V3 d, float tmin, float tmax,
                                          TraceResult& res, int* err_flag)
 {
-    Traversal<kAnyHit> tr;
-    uint32_t stack[kStackSize];
-    tr.init(S, stack, o, d, tmin, tmax);
-    while (!tr.done()) tr.round(S.nodes, S.tris, stack);
-    res = tr.res;
-    if (tr.overflow) atomicOr(err_flag, 1);
-    return !tr.overflow;
+    if (S.wnodes) return traverse_with<WideTraversal<kAnyHit>>(S, o, d, tmin, tmax, res, err_flag);
+    return traverse_with<Traversal<kAnyHit>>(S, o, d, tmin, tmax, res, err_flag);
 }
 
 }  // namespace wf
