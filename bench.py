@@ -388,7 +388,8 @@ def main() -> int:
     ap.add_argument("--blocks-per-sm", type=int, default=0)
     ap.add_argument("--ref-rows", type=int, default=256)
     ap.add_argument("--ref-spp", type=int, default=16)
-    ap.add_argument("--bvh", default="wide", choices=["wide", "ploc", "lbvh"])
+    ap.add_argument("--bvh", default="ploc", choices=["ploc", "lbvh", "wide"])
+    ap.add_argument("--autotune", type=int, default=0, help="run wf_autotune on the workload before timing")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 0)
     if args.workload == "c3":
@@ -407,7 +408,7 @@ def main() -> int:
     ctx = pkg.Context(local)
     scene = pkg.HostScene(wl["config"])
     ctx.set_tuning(max(args.trace_variant, 0), args.blocks_per_sm,
-                   bvh_builder={"wide": 0, "lbvh": 1, "ploc": 2}[args.bvh])
+                   bvh_builder={"ploc": 0, "lbvh": 1, "wide": 2}[args.bvh])
     info = ctx.upload(scene.desc)
     W, H = wl["width"], wl["height"]
     cam = scene.camera(W, H)
@@ -417,6 +418,9 @@ def main() -> int:
         return pkg.render_params(W, H, wl["spp"], wl["depth"], cam, policy=policy, ray_sort=bool(args.ray_sort),
                                  seed=seed, spp_per_wave=args.spp_per_wave, env_nee=bool(args.env_nee))
 
+    tune_ms = None
+    if args.autotune:
+        _, tune_ms = ctx.autotune(params(999))
     for w in range(max(args.warmup, 0)):
         ctx.render_device(params(1000 + w))
 
@@ -488,9 +492,9 @@ def main() -> int:
         "clocks": clocks,
         "gpu_launches": int(sum(s["kernel_launches"] for s in stats)),
         "bvh_build_ms": info.bvh_build_ms,
-        "bvh": {"builder": ["ploc_wide8", "lbvh", "ploc"][info.bvh_builder], "nodes": info.bvh_nodes,
+        "bvh": {"builder": ["ploc", "lbvh", "ploc_wide8"][info.bvh_builder], "nodes": info.bvh_nodes,
                 "depth": info.bvh_depth},
-        "tuning": ctx.get_tuning(),
+        "tuning": dict(ctx.get_tuning(), autotuned=bool(args.autotune), autotune_wave_ms=tune_ms),
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         rays, dt, sample = cpu_sample(pkg, wl, os.cpu_count() or 1, rows=wl["height"], spp=wl.get("cpu_spp", 32),

@@ -282,16 +282,25 @@ typedef struct wf_tuning {
     int32_t persistent_blocks_per_sm;
     int32_t graph_mode;  /* 0 = graphs for batches and the server, 1 = also for
                             single renders, 2 = never (policy != none never) */
-    int32_t bvh_builder; /* scenes uploaded afterwards: 0 = PLOC tree
-                            (locally-ordered clustering) collapsed into
-                            compressed 8-wide nodes (default), 1 = LBVH binary
-                            tree (Karras radix tree), 2 = PLOC binary tree; a
-                            PLOC tree deeper than its traversal stack falls
-                            back to LBVH */
+    int32_t bvh_builder; /* scenes uploaded afterwards: 0 = PLOC binary tree
+                            (locally-ordered clustering, default), 1 = LBVH
+                            binary tree (Karras radix tree), 2 = the PLOC tree
+                            collapsed into compressed 8-wide nodes; a PLOC
+                            tree deeper than its traversal stack falls back
+                            to LBVH */
     int32_t reserved[4];
 } wf_tuning;
 int wf_set_tuning(wf_ctx* ctx, const wf_tuning* tuning);
 int wf_get_tuning(const wf_ctx* ctx, wf_tuning* out_tuning);
+
+/* Autotuner (no reference counterpart): renders one wave of `params` on the
+ * current scene (samples capped at one wave, adaptive sampling and cost
+ * tracking off) under every combination of trace_variant {0, 1},
+ * persistent_blocks_per_sm {4, 8, 12, 16, 24} and graph_mode {2, 1}, each
+ * once untimed and twice timed on the device, keeps the fastest on the
+ * context (bvh_builder is left as it is) and returns it with its time per
+ * wave.  Images and statistics of the trial renders are discarded. */
+int wf_autotune(wf_ctx* ctx, const wf_render_params* params, wf_tuning* out_tuning, double* out_wave_ms);
 
 /* ---- ray batches (host buffers) --------------------------------------------- */
 

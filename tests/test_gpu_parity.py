@@ -512,7 +512,7 @@ def test_gpu_live_costs_only_reorder_shading(wf, ctx, scene_c2small, policy):
 
 @pytest.mark.parametrize("which", ["c0", "small", "c2small"])
 def test_bvh_builders_give_identical_hits(wf, orc, ctx, scene0, scene_small, scene_c2small, which):
-    """The compressed 8-wide PLOC tree, the binary PLOC tree and the LBVH
+    """The binary PLOC tree, the LBVH and the compressed 8-wide PLOC tree
     return the same closest hits and occlusion bit for bit (and the port's),
     and each passes the build's structural check."""
     scene = {"c0": scene0, "small": scene_small, "c2small": scene_c2small}[which]
@@ -536,4 +536,4 @@ def test_bvh_builders_give_identical_hits(wf, orc, ctx, scene0, scene_small, sce
     finally:
         ctx.set_tuning()
     assert [i.bvh_builder for i in infos] == [0, 1, 2]
-    assert infos[0].bvh_nodes < infos[2].bvh_nodes
+    assert infos[2].bvh_nodes < infos[0].bvh_nodes  # the 8-wide tree has fewer nodes

@@ -228,6 +228,7 @@ def _declare(lib: C.CDLL) -> None:
         "wf_render_device": ([V, C.POINTER(WfRenderParams), C.POINTER(WfRenderStats)], C.c_int),
         "wf_image_download": ([V, f32p, C.c_int64], C.c_int),
         "wf_adaptive_sample_counts": ([V, i32p, C.c_int64], C.c_int),
+        "wf_autotune": ([V, C.POINTER(WfRenderParams), C.POINTER(WfTuning), C.POINTER(C.c_double)], C.c_int),
         "wf_scene_save": ([C.c_char_p, C.POINTER(WfSceneDesc), f32p, f32p, f32p, C.c_float], C.c_int),
         "wf_scene_load": ([C.c_char_p, C.POINTER(V)], C.c_int),
         "wf_image_write_pfm": ([C.c_char_p, f32p, C.c_int32, C.c_int32], C.c_int),
@@ -579,6 +580,14 @@ class Context:
                    bvh_builder: int = 0) -> None:
         t = WfTuning(trace_variant, persistent_blocks_per_sm, graph_mode, bvh_builder)
         _check(load_library().wf_set_tuning(self._h, C.byref(t)), "wf_set_tuning", self)
+
+    def autotune(self, params: WfRenderParams) -> tuple[dict, float]:
+        """wf_autotune: the fastest launch tuning for one wave of params
+        (kept on the context) and its device time per wave in ms."""
+        t = WfTuning()
+        ms = C.c_double()
+        _check(load_library().wf_autotune(self._h, C.byref(params), C.byref(t), C.byref(ms)), "wf_autotune", self)
+        return self.get_tuning(), ms.value
 
     def get_tuning(self) -> dict:
         t = WfTuning()

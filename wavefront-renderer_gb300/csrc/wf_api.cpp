@@ -564,10 +564,10 @@ int build_scene(wf_ctx* c, const wf_scene_desc* D, ResidentScene& R)
         auto b0 = std::chrono::steady_clock::now();
         int brc = -1;
         if (c->tuning.bvh_builder == 0) {
-            brc = build_ploc_wide(bi, bo, c->num_sms, s, err);
+            brc = build_ploc(bi, bo, c->num_sms, s, err);
             R.info.bvh_builder = 0;
         } else if (c->tuning.bvh_builder == 2) {
-            brc = build_ploc(bi, bo, c->num_sms, s, err);
+            brc = build_ploc_wide(bi, bo, c->num_sms, s, err);
             R.info.bvh_builder = 2;
         }
         if (brc) {  // LBVH on request, or when a PLOC tree is too deep for its stack

@@ -622,6 +622,55 @@ int wf_render(wf_ctx* c, const wf_render_params* P, float* image, wf_render_stat
     return WF_OK;
 }
 
+int wf_autotune(wf_ctx* c, const wf_render_params* P, wf_tuning* out, double* out_ms)
+{
+    if (!c || !P) return set_err(c, WF_ERR_INVALID_ARGUMENT, "null argument");
+    int rc = validate_params(c, P);
+    if (rc) return rc;
+    cudaSetDevice(c->device);
+    wf_render_params trial = *P;
+    const int64_t np = (int64_t)P->width * P->height;
+    int spw = P->spp_per_wave > 0 ? P->spp_per_wave : (int)std::max<int64_t>(1, c->paths_per_wave / np);
+    trial.samples_per_pixel = std::max(1, std::min(spw, P->samples_per_pixel));
+    trial.spp_per_wave = trial.samples_per_pixel;
+    trial.enable_adaptive_sampling = 0;
+    trial.enable_cost_tracking = 0;
+    const wf_tuning base = c->tuning;
+    wf_tuning best = base;
+    double best_ms = -1.0;
+    const int variants[2] = {0, 1};
+    const int blocks[5] = {4, 8, 12, 16, 24};
+    const int graphs[2] = {2, 1};
+    for (int v : variants)
+        for (int b : blocks)
+            for (int g : graphs) {
+                wf_tuning t = base;
+                t.trace_variant = v;
+                t.persistent_blocks_per_sm = b;
+                t.graph_mode = g;
+                c->tuning = t;
+                double ms = 0.0;
+                for (int rep = 0; rep < 3; ++rep) {
+                    wf_render_stats st{};
+                    rc = render_single(c, &trial, &st);
+                    if (rc) {
+                        c->tuning = base;
+                        return rc;
+                    }
+                    if (rep > 0) ms += st.ms_total;
+                }
+                ms *= 0.5;
+                if (best_ms < 0.0 || ms < best_ms) {
+                    best_ms = ms;
+                    best = t;
+                }
+            }
+    c->tuning = best;
+    if (out) *out = best;
+    if (out_ms) *out_ms = best_ms;
+    return WF_OK;
+}
+
 int wf_render_device(wf_ctx* c, const wf_render_params* P, wf_render_stats* st)
 {
     if (!c) return WF_ERR_INVALID_ARGUMENT;
