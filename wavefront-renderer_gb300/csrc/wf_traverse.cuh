@@ -241,9 +241,9 @@ struct WideTraversal {
         }
     }
 
-    // Quantized child boxes of the occupied slots; boxes are decoded as
-    // p + q * 2^e (q made a float exactly from its byte, one rounding in the
-    // fma) and slab-tested like the binary nodes.
+    // Eight quantized child boxes, decoded as p + q * 2^e (q made a float
+    // exactly from its byte, one rounding in the fma) and slab-tested like
+    // the binary nodes; empty slots are masked out.
     __device__ __forceinline__ static float byte_float(uint32_t word, uint32_t shift)
     {
         return __uint_as_float(0x4B000000u | ((word >> shift) & 0xFFu)) - 8388608.0f;
@@ -258,31 +258,33 @@ struct WideTraversal {
         const float sz = __uint_as_float(((hdr >> 16) & 0xFFu) << 23);
         const uint32_t imask = hdr >> 24;
         const uint32_t meta0 = __float_as_uint(w1.z), meta1 = __float_as_uint(w1.w);
-        // occupied slots: bytes of meta that are not zero
-        const uint32_t nz0 = __vcmpne4(meta0, 0u), nz1 = __vcmpne4(meta1, 0u);
-        uint32_t occupied = ((nz0 >> 7) & 1u) | ((nz0 >> 14) & 2u) | ((nz0 >> 21) & 4u) | ((nz0 >> 28) & 8u) |
-                            (((nz1 >> 7) & 1u) | ((nz1 >> 14) & 2u) | ((nz1 >> 21) & 4u) | ((nz1 >> 28) & 8u)) << 4;
+        const uint32_t lox[2] = {__float_as_uint(w2.x), __float_as_uint(w2.y)};
+        const uint32_t loy[2] = {__float_as_uint(w2.z), __float_as_uint(w2.w)};
+        const uint32_t loz[2] = {__float_as_uint(w3.x), __float_as_uint(w3.y)};
+        const uint32_t hix[2] = {__float_as_uint(w3.z), __float_as_uint(w3.w)};
+        const uint32_t hiy[2] = {__float_as_uint(w4.x), __float_as_uint(w4.y)};
+        const uint32_t hiz[2] = {__float_as_uint(w4.z), __float_as_uint(w4.w)};
+        const uint32_t meta[2] = {meta0, meta1};
         uint32_t hits_i = 0, hits_t = 0;
-        while (occupied) {
-            const uint32_t s = (uint32_t)__ffs(occupied) - 1u;
-            occupied &= occupied - 1u;
-            const bool hi_word = s >= 4u;
-            const uint32_t sh = 8u * (s & 3u);
-            const uint32_t m = ((hi_word ? meta1 : meta0) >> sh) & 0xFFu;
-            const float lx = __fmaf_rn(byte_float(__float_as_uint(hi_word ? w2.y : w2.x), sh), sx, w0.x);
-            const float ly = __fmaf_rn(byte_float(__float_as_uint(hi_word ? w2.w : w2.z), sh), sy, w0.y);
-            const float lz = __fmaf_rn(byte_float(__float_as_uint(hi_word ? w3.y : w3.x), sh), sz, w0.z);
-            const float hx = __fmaf_rn(byte_float(__float_as_uint(hi_word ? w3.w : w3.z), sh), sx, w0.x);
-            const float hy = __fmaf_rn(byte_float(__float_as_uint(hi_word ? w4.y : w4.x), sh), sy, w0.y);
-            const float hz = __fmaf_rn(byte_float(__float_as_uint(hi_word ? w4.w : w4.z), sh), sz, w0.z);
+#pragma unroll
+        for (int s = 0; s < 8; ++s) {
+            const int wd = s >> 2;
+            const uint32_t sh = 8u * (uint32_t)(s & 3);
+            const uint32_t m = (meta[wd] >> sh) & 0xFFu;
+            const float lx = __fmaf_rn(byte_float(lox[wd], sh), sx, w0.x);
+            const float hx = __fmaf_rn(byte_float(hix[wd], sh), sx, w0.x);
+            const float ly = __fmaf_rn(byte_float(loy[wd], sh), sy, w0.y);
+            const float hy = __fmaf_rn(byte_float(hiy[wd], sh), sy, w0.y);
+            const float lz = __fmaf_rn(byte_float(loz[wd], sh), sz, w0.z);
+            const float hz = __fmaf_rn(byte_float(hiz[wd], sh), sz, w0.z);
             const float tlx = __fmaf_rn(lx, inv.x, -oi.x), thx = __fmaf_rn(hx, inv.x, -oi.x);
             const float tly = __fmaf_rn(ly, inv.y, -oi.y), thy = __fmaf_rn(hy, inv.y, -oi.y);
             const float tlz = __fmaf_rn(lz, inv.z, -oi.z), thz = __fmaf_rn(hz, inv.z, -oi.z);
             const float tn = fmaxf(fmaxf(fminf(tlx, thx), fminf(tly, thy)), fmaxf(fminf(tlz, thz), tmin));
             const float tf = fminf(fminf(fmaxf(tlx, thx), fmaxf(tly, thy)), fminf(fmaxf(tlz, thz), best_t));
-            if (tn <= tf) {
+            if (m != 0u && tn <= tf) {
                 if ((m & 0x1Fu) >= 24u)
-                    hits_i |= 1u << (24u + (s ^ octinv));
+                    hits_i |= 1u << (24u + ((uint32_t)s ^ octinv));
                 else
                     hits_t |= (m >> 5) << (m & 0x1Fu);
             }
