@@ -268,8 +268,11 @@ inline void intersectAll(Context& ctx, const RayQueue& in, ShadingQueue& hits, R
     }
 }
 
-// include/render/WavefrontRenderer.h:16-56.  Adaptive sampling is not
-// implemented on the device yet (enableAdaptiveSampling must stay false).
+// include/render/WavefrontRenderer.h:16-56, with the reference's defaults:
+// adaptive sampling on (threshold 0.05), cost-aware RR on with costs from the
+// live device CostTracker, ray sort on.  Frozen relative costs (for
+// reproducible runs) replace the live tracker when given.  envNEE is a
+// device addition (environment next-event estimation, same mean).
 class WavefrontRenderer {
   public:
     int samplesPerPixel;
@@ -278,23 +281,25 @@ class WavefrontRenderer {
     SchedulingPolicy policy;
     bool enableCostAwareRR = true;
     bool enableRaySort = true;
-    bool enableAdaptiveSampling = false;
+    bool enableAdaptiveSampling = true;
+    float adaptiveSamplingThreshold = 0.05f;
     float fireflyThreshold = 10.0f;
+    bool envNEE = false;
     uint64_t seed = 1;
-    std::vector<double> relativeCostMaterial;  // frozen CostTracker::relativeCost, empty = 1.0
+    std::vector<double> relativeCostMaterial;  // frozen CostTracker::relativeCost; empty = live tracker
     std::vector<double> relativeCostTexture;
     wf_render_stats lastStats{};
 
-    WavefrontRenderer(int samples, int maxDepth, SchedulingPolicy policy)
-        : samplesPerPixel(samples), maxDepth(maxDepth), policy(policy)
+    WavefrontRenderer(int samples, int maxDepth, SchedulingPolicy policy, int rrMinDepth_ = 3)
+        : samplesPerPixel(samples), maxDepth(maxDepth), rrMinDepth(rrMinDepth_), policy(policy)
     {
     }
 
-    // renderScene: writes the averaged image (width*height*3 floats) and
-    // returns the total shade milliseconds, as the reference does.
+    // renderScene: writes the averaged image (width*height*3 floats; with
+    // adaptive sampling each pixel over its own sample count) and returns
+    // the total shade milliseconds, as the reference does.
     double renderScene(Context& ctx, const wf_camera& camera, int width, int height, std::vector<float>& pixels)
     {
-        if (enableAdaptiveSampling) throw Error(WF_ERR_INVALID_ARGUMENT, "adaptive sampling is not supported");
         wf_render_params p{};
         p.width = width;
         p.height = height;
@@ -307,12 +312,26 @@ class WavefrontRenderer {
         p.firefly_threshold = fireflyThreshold;
         p.seed_lo = (uint32_t)seed;
         p.seed_hi = (uint32_t)(seed >> 32);
+        p.enable_env_nee = envNEE ? 1 : 0;
+        p.enable_adaptive_sampling = enableAdaptiveSampling ? 1 : 0;
+        p.adaptive_threshold = adaptiveSamplingThreshold;
+        const bool frozen = !relativeCostMaterial.empty() || !relativeCostTexture.empty();
+        p.enable_cost_tracking = frozen ? 0 : 1;
         p.rel_cost_material = relativeCostMaterial.empty() ? nullptr : relativeCostMaterial.data();
         p.rel_cost_texture = relativeCostTexture.empty() ? nullptr : relativeCostTexture.data();
         p.camera = camera;
         pixels.assign((size_t)width * height * 3, 0.0f);
         check(wf_render(ctx.handle(), &p, pixels.data(), &lastStats), ctx.handle(), "wf_render");
         return lastStats.ms_shade;
+    }
+
+    // AdaptiveSampler::getSampleCount of every pixel of the last render.
+    std::vector<int32_t> sampleCounts(Context& ctx, int width, int height) const
+    {
+        std::vector<int32_t> n((size_t)width * height);
+        check(wf_adaptive_sample_counts(ctx.handle(), n.data(), (int64_t)n.size()), ctx.handle(),
+              "wf_adaptive_sample_counts");
+        return n;
     }
 };
 

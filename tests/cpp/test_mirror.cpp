@@ -120,6 +120,10 @@ int main()
         EXPECT(finite);
         EXPECT(mean > 0);
         EXPECT(r.lastStats.closest_rays > 0);
+        // the reference's defaults: adaptive sampling (no pixel stops before
+        // 32 samples) and cost-aware RR fed by the live tracker
+        const std::vector<int32_t> counts = r.sampleCounts(ctx, 16, 16);
+        EXPECT(counts.size() == 256 && counts[0] == 8 && counts[255] == 8);
         wf_host_scene_free(hs);
     }
     std::printf("%s (%d failures)\n", failures ? "FAIL" : "OK", failures);
