@@ -99,53 +99,80 @@ struct Traversal {
     __device__ __forceinline__ void round(const BvhNode* __restrict__ nodes, const float4* __restrict__ tris,
                                           uint32_t* stack)
     {
-        while (!(cur & kLeafFlag)) {
-            const BvhNode nd = load_node(nodes, cur);
-            float tn0, tn1;
-            bool h0, h1;
-            slab2(nd, inv, oi, tmin, best_t, tn0, tn1, h0, h1);
-            const uint32_t c0 = (uint32_t)nd.kids.x, c1 = (uint32_t)nd.kids.y;
-            if (h0 && h1) {
-                const bool swap = tn1 < tn0;
-                const uint32_t farc = swap ? c0 : c1;
-                cur = swap ? c1 : c0;
-                if (sp < kStackSize)
-                    stack[sp++] = farc;
-                else
-                    overflow = true;
-            } else if (h0 || h1) {
-                cur = h0 ? c0 : c1;
-            } else {
-                cur = stack[--sp];
-            }
-        }
-        while (cur != kSentinel) {
-            if (!(cur & kLeafFlag)) break;
-            const int first = (int)((cur & ~kLeafFlag) >> 3);
-            const int cnt = (int)(cur & 7u) + 1;
-            bool stop = false;
-            for (int k = 0; k < cnt; ++k) {
-                const int lp = first + k;
-                const float4 a = __ldg(tris + 3 * lp + 0);
-                const float4 b = __ldg(tris + 3 * lp + 1);
-                const float4 c = __ldg(tris + 3 * lp + 2);
-                float th, uh, vh;
-                if (intersect_triangle(o, d, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), v3(c.x, c.y, c.z), tmin,
-                                       best_t, th, uh, vh)) {
-                    const int g = __float_as_int(a.w);
-                    if (kAnyHit || th < best_t || res.leafpos < 0 || g > best_g) {
-                        res.leafpos = lp;
-                        res.t = th;
-                        res.bu = uh;
-                        res.bv = vh;
-                        best_t = th;
-                        best_g = g;
-                        if (kAnyHit) stop = true;
-                    }
+        // Speculative while-while (Aila & Laine 2009): a lane that reaches a
+        // leaf postpones it and keeps descending while another lane of the
+        // warp is still looking for its first leaf; then all lanes test
+        // their leaves together.
+        const unsigned active = __activemask();
+        uint32_t postponed = 0u;  // leaf words always carry kLeafFlag, so 0 = none
+        for (;;) {
+            if (cur != kSentinel && !(cur & kLeafFlag)) {
+                const BvhNode nd = load_node(nodes, cur);
+                float tn0, tn1;
+                bool h0, h1;
+                slab2(nd, inv, oi, tmin, best_t, tn0, tn1, h0, h1);
+                const uint32_t c0 = (uint32_t)nd.kids.x, c1 = (uint32_t)nd.kids.y;
+                if (h0 && h1) {
+                    const bool swap = tn1 < tn0;
+                    const uint32_t farc = swap ? c0 : c1;
+                    cur = swap ? c1 : c0;
+                    if (sp < kStackSize)
+                        stack[sp++] = farc;
+                    else
+                        overflow = true;
+                } else if (h0 || h1) {
+                    cur = h0 ? c0 : c1;
+                } else {
+                    cur = stack[--sp];
                 }
             }
-            cur = stop ? kSentinel : stack[--sp];
+            if (postponed == 0u && cur != kSentinel && (cur & kLeafFlag)) {
+                postponed = cur;
+                cur = stack[--sp];
+            }
+            const bool searching = postponed == 0u && cur != kSentinel;
+            if (!__any_sync(active, searching)) break;
         }
+        if (postponed != 0u && test_leaf(tris, postponed)) {
+            cur = kSentinel;  // any hit: done
+            return;
+        }
+        while (cur != kSentinel && (cur & kLeafFlag)) {
+            const uint32_t leaf = cur;
+            cur = stack[--sp];
+            if (test_leaf(tris, leaf)) {
+                cur = kSentinel;
+                return;
+            }
+        }
+    }
+
+    // The triangles of one leaf; true when an any-hit query may stop.
+    __device__ __forceinline__ bool test_leaf(const float4* __restrict__ tris, uint32_t leaf)
+    {
+        const int first = (int)((leaf & ~kLeafFlag) >> 3);
+        const int cnt = (int)(leaf & 7u) + 1;
+        for (int k = 0; k < cnt; ++k) {
+            const int lp = first + k;
+            const float4 a = __ldg(tris + 3 * lp + 0);
+            const float4 b = __ldg(tris + 3 * lp + 1);
+            const float4 c = __ldg(tris + 3 * lp + 2);
+            float th, uh, vh;
+            if (intersect_triangle(o, d, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), v3(c.x, c.y, c.z), tmin, best_t, th,
+                                   uh, vh)) {
+                const int g = __float_as_int(a.w);
+                if (kAnyHit || th < best_t || res.leafpos < 0 || g > best_g) {
+                    res.leafpos = lp;
+                    res.t = th;
+                    res.bu = uh;
+                    res.bv = vh;
+                    best_t = th;
+                    best_g = g;
+                    if (kAnyHit) return true;
+                }
+            }
+        }
+        return false;
     }
 };
 
