@@ -390,6 +390,7 @@ def main() -> int:
     ap.add_argument("--ref-spp", type=int, default=16)
     ap.add_argument("--bvh", default="ploc", choices=["ploc", "lbvh", "wide"])
     ap.add_argument("--autotune", type=int, default=0, help="run wf_autotune on the workload before timing")
+    ap.add_argument("--plain-traversal", type=int, default=0, help="1 = while-while without speculation")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 0)
     if args.workload == "c3":
@@ -408,7 +409,7 @@ def main() -> int:
     ctx = pkg.Context(local)
     scene = pkg.HostScene(wl["config"])
     ctx.set_tuning(max(args.trace_variant, 0), args.blocks_per_sm,
-                   bvh_builder={"ploc": 0, "lbvh": 1, "wide": 2}[args.bvh])
+                   bvh_builder={"ploc": 0, "lbvh": 1, "wide": 2}[args.bvh], plain_traversal=args.plain_traversal)
     info = ctx.upload(scene.desc)
     W, H = wl["width"], wl["height"]
     cam = scene.camera(W, H)

@@ -295,6 +295,34 @@ def test_render_is_order_independent(wf, ctx, scene_small, scene_c2small, which)
         img, _ = ctx.render(wf.render_params(W, H, 8, 12, cam, seed=5, **kw))
         agree = np.isclose(img, base, rtol=1e-4, atol=1e-6).all(axis=2).mean()
         assert agree >= 0.999, (kw, agree)
+    # launch tuning: occupancy variant, shared-memory stack, grid size,
+    # graph replay and the sort-or-skip threshold change no pixel beyond that
+    try:
+        for tune, kw in [(dict(trace_variant=1), {}), (dict(trace_variant=2), {}),
+                         (dict(persistent_blocks_per_sm=4), {}), (dict(graph_mode=1), {}),
+                         (dict(sort_min_queue=6000), dict(policy=1, ray_sort=True))]:
+            ctx.set_tuning(**tune)
+            img, _ = ctx.render(wf.render_params(W, H, 8, 12, cam, seed=5, **kw))
+            agree = np.isclose(img, base, rtol=1e-4, atol=1e-6).all(axis=2).mean()
+            assert agree >= 0.999, (tune, agree)
+    finally:
+        ctx.set_tuning()
+
+
+def test_autotune_picks_a_valid_tuning(wf, ctx, scene_small):
+    ctx.upload(scene_small.desc)
+    cam = scene_small.camera(64, 64)
+    p = wf.render_params(64, 64, 4, 8, cam, seed=2, policy=1)
+    try:
+        tuning, ms = ctx.autotune(p)
+        assert ms > 0
+        assert tuning["trace_variant"] in (0, 1, 2) and tuning["persistent_blocks_per_sm"] in (4, 8, 12, 16, 24)
+        assert tuning["sort_min_queue"] in (0, 1 << 18, 1 << 20, 1 << 22, 2**31 - 1)
+        assert ctx.get_tuning() == tuning
+        img, _ = ctx.render(p)
+        assert np.isfinite(img).all()
+    finally:
+        ctx.set_tuning()
 
 
 def test_render_accumulate_and_device_paths(wf, ctx, scene0):

@@ -22,7 +22,8 @@ struct ShadeParams {
 struct LaunchCfg {
     int grid;
     int block;
-    int variant = 0;  // kernel variant (traversal occupancy hint)
+    int variant = 0;   // kernel variant (traversal occupancy hint / stack placement)
+    int plain = 0;     // 1 = while-while traversal without speculation
 };
 
 // Camera rays of n = width*height*nspp paths, sample-major.

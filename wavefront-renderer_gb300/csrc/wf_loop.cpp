@@ -142,7 +142,8 @@ int wave_host(wf_ctx* c, int64_t total, int max_depth, int policy, bool ray_sort
     for (int depth = 0; depth < max_depth && count > 0; ++depth) {
         stats.bounces++;
         stats.closest_rays += (uint64_t)count;
-        if (ray_sort) {  // RayQueue::schedule + materialize (.cpp:159-168)
+        const bool sort_rays = ray_sort && count >= (int64_t)c->tuning.sort_min_queue;
+        if (sort_rays) {  // RayQueue::schedule + materialize (.cpp:159-168)
             WF_CK(c, cudaEventRecord(ev[2], s));
             launch_ray_keys(c->d_scene_table, c->d_jobs, c->rq[cur], c->counters, c->keys, c->vals, WC, s);
             uint64_t* rk;
@@ -161,10 +162,12 @@ int wave_host(wf_ctx* c, int64_t total, int max_depth, int policy, bool ray_sort
                             c->err_flag, PC, s);
         WF_CK(c, cudaEventRecord(ev[5], s));
         HitQueueDev hq_use = c->hq[0];
+        ull hits = 0;
         if (policy != WF_POLICY_NONE) {
-            ull hits = 0;
             WF_CK(c, cudaMemcpyAsync(&hits, c->counters + 1, sizeof(ull), cudaMemcpyDeviceToHost, s));
             WF_CK(c, cudaStreamSynchronize(s));
+        }
+        if (policy != WF_POLICY_NONE && hits >= (ull)c->tuning.sort_min_queue) {
             ShadeColumnsMut cm{c->col_mat, c->col_tex, c->col_tr, c->col_tg, c->col_tb, c->col_px, c->col_py, c->col_pz};
             launch_hit_columns(c->d_scene_table, c->d_jobs, c->rq[cur], c->hq[0], c->counters + 1, cm, WC, s);
             ShadeColumnsDev cd{c->col_mat, c->col_tex, c->col_tr, c->col_tg, c->col_tb, c->col_px, c->col_py, c->col_pz};
@@ -203,7 +206,7 @@ int wave_host(wf_ctx* c, int64_t total, int max_depth, int policy, bool ray_sort
         WF_CK(c, cudaMemcpyAsync(cnt, c->counters, sizeof(cnt), cudaMemcpyDeviceToHost, s));
         WF_CK(c, cudaMemcpyAsync(c->counters, c->counters + 3, sizeof(ull), cudaMemcpyDeviceToDevice, s));
         WF_CK(c, cudaStreamSynchronize(s));
-        if (ray_sort) {
+        if (sort_rays) {
             WF_CK(c, cudaEventElapsedTime(&ms, ev[2], ev[3]));
             stats.ms_ray_sort += ms;
         }
@@ -638,16 +641,19 @@ int wf_autotune(wf_ctx* c, const wf_render_params* P, wf_tuning* out, double* ou
     const wf_tuning base = c->tuning;
     wf_tuning best = base;
     double best_ms = -1.0;
-    const int variants[2] = {0, 1};
+    const int variants[3] = {0, 1, 2};
     const int blocks[5] = {4, 8, 12, 16, 24};
     const int graphs[2] = {2, 1};
+    const int plains[2] = {0, 1};
     for (int v : variants)
         for (int b : blocks)
-            for (int g : graphs) {
+            for (int g : graphs)
+                for (int pl : plains) {
                 wf_tuning t = base;
                 t.trace_variant = v;
                 t.persistent_blocks_per_sm = b;
                 t.graph_mode = g;
+                t.plain_traversal = pl;
                 c->tuning = t;
                 double ms = 0.0;
                 for (int rep = 0; rep < 3; ++rep) {
@@ -665,6 +671,30 @@ int wf_autotune(wf_ctx* c, const wf_render_params* P, wf_tuning* out, double* ou
                     best = t;
                 }
             }
+    if (P->policy != WF_POLICY_NONE || P->enable_ray_sort) {  // sort-or-skip threshold
+        const int thresholds[5] = {0, 1 << 18, 1 << 20, 1 << 22, INT32_MAX};
+        const wf_tuning launch = best;
+        for (int th : thresholds) {
+            wf_tuning t = launch;
+            t.sort_min_queue = th;
+            c->tuning = t;
+            double ms = 0.0;
+            for (int rep = 0; rep < 3; ++rep) {
+                wf_render_stats st{};
+                rc = render_single(c, &trial, &st);
+                if (rc) {
+                    c->tuning = base;
+                    return rc;
+                }
+                if (rep > 0) ms += st.ms_total;
+            }
+            ms *= 0.5;
+            if (th == 0 || ms < best_ms) {  // the launch winner re-timed at 0 sets the bar
+                best_ms = ms;
+                best = t;
+            }
+        }
+    }
     c->tuning = best;
     if (out) *out = best;
     if (out_ms) *out_ms = best_ms;

@@ -2,6 +2,8 @@
 // wavefront loop (reference src/render/WavefrontRenderer.cpp:401-877).
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "wf_kernels.h"
 #include "wf_traverse.cuh"
 
@@ -176,6 +178,25 @@ __global__ void __launch_bounds__(128) k_occluded_api(DeviceScene S, int64_t n, 
     }
 }
 
+// Speculation switch of the binary traversal (the wide one has none).
+template <class Tr>
+__device__ __forceinline__ void set_plain(Tr& tr, bool plain)
+{
+    if constexpr (std::is_same<Tr, Traversal<false>>::value || std::is_same<Tr, Traversal<true>>::value)
+        tr.speculative = !plain;
+}
+
+// The traversal stack of a thread: its local array, or its column of the
+// block's shared array.
+template <bool kShared, class E>
+__device__ __forceinline__ auto pick_stack(E* local, uint32_t* shared)
+{
+    if constexpr (kShared)
+        return SharedStack32{shared + threadIdx.x};
+    else
+        return local;
+}
+
 __device__ __forceinline__ void accum_add(float* accum, int32_t slot, V3 c)
 {
     float* p = accum + 3 * (int64_t)slot;
@@ -195,20 +216,23 @@ __device__ __forceinline__ void accum_add(float* accum, int32_t slot, V3 c)
 // ---------------------------------------------------------------------------
 // kMulti = false: every ray belongs to job0 on scene0 (passed by value, read
 // from the constant bank); true: each ray looks its job and scene up.
-template <bool kMulti, int kMinBlocks, class Tr>
+template <bool kMulti, int kMinBlocks, class Tr, bool kSharedStack = false>
 __global__ void __launch_bounds__(128, kMinBlocks) k_trace_render(DeviceScene scene0, DeviceJob job0,
                                                                   const DeviceScene* __restrict__ scenes,
                                                                   const DeviceJob* __restrict__ jobs,
                                                                   RayQueueDev rq, const ull* __restrict__ d_n,
                                                                   HitQueueDev hq, ull* hq_n, float* accum,
-                                                                  ull* work, int* err)
+                                                                  ull* work, int* err, int plain)
 {
     const int64_t n = (int64_t)*d_n;
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     Tr tr;
-    typename Tr::Entry stack[Tr::kStack];
+    typename Tr::Entry local_stack[kSharedStack ? 1 : Tr::kStack];
+    __shared__ uint32_t shared_stack[kSharedStack ? kStackSize * 128 : 1];
+    const auto stack = pick_stack<kSharedStack>(local_stack, shared_stack);
     const DeviceScene* S = kMulti ? scenes : &scene0;
+    set_plain(tr, plain != 0);
     int job = 0;
     int64_t ray = -1;
     bool exhausted = false;
@@ -626,20 +650,24 @@ __global__ void __launch_bounds__(128) k_shade(DeviceScene scene0, DeviceJob job
 // Shadow rays (EmbreeAccelerator::occluded): unblocked contributions are
 // added to their pixel.  Same persistent, dynamic-fetch structure as
 // k_trace_render.
-template <bool kMulti, int kMinBlocks, class Tr>
+template <bool kMulti, int kMinBlocks, class Tr, bool kSharedStack = false>
 __global__ void __launch_bounds__(128, kMinBlocks) k_occluded_render(DeviceScene scene0, DeviceJob job0,
                                                                      const DeviceScene* __restrict__ scenes,
                                                                      const DeviceJob* __restrict__ jobs,
                                                                      ShadowQueueDev sh,
                                                                      const ull* __restrict__ d_n,
-                                                                     float* accum, ull* work, int* err)
+                                                                     float* accum, ull* work, int* err,
+                                                                     int plain)
 {
     const int64_t n = (int64_t)*d_n;
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     Tr tr;
-    typename Tr::Entry stack[Tr::kStack];
+    typename Tr::Entry local_stack[kSharedStack ? 1 : Tr::kStack];
+    __shared__ uint32_t shared_stack[kSharedStack ? kStackSize * 128 : 1];
+    const auto stack = pick_stack<kSharedStack>(local_stack, shared_stack);
     const DeviceScene* S = kMulti ? scenes : &scene0;
+    set_plain(tr, plain != 0);
     int job = 0;
     int64_t ray = -1;
     bool exhausted = false;
@@ -1092,21 +1120,29 @@ void launch_occluded_api(const DeviceScene& S, int64_t n, const float* ox, const
                                                              out, err);
 }
 
-// variant: 0 = no occupancy hint, 1 = 10 blocks of 128 per SM; the traversal
-// follows the scene's tree (compressed 8-wide or binary).
+// variant: 0 = no occupancy hint, 1 = 10 blocks of 128 per SM, 2 = the
+// traversal stack in shared memory (binary trees); the traversal follows the
+// scene's tree (compressed 8-wide or binary).
 void launch_trace_render(const WaveTables& t, RayQueueDev rq, const ull* d_n, HitQueueDev hq, ull* hq_n,
                          float* accum, ull* work, int* err, LaunchCfg cfg, cudaStream_t s)
 {
 #define WF_TRACE(M, B, T)                                                                                   \
     k_trace_render<M, B, T><<<cfg.grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, d_n, hq, hq_n, \
-                                                     accum, work, err)
+                                                     accum, work, err, cfg.plain)
 #define WF_TRACE2(M, T) \
     if (cfg.variant == 1) WF_TRACE(M, 10, T); else WF_TRACE(M, 1, T)
+#define WF_TRACE_SHARED(M)                                                                                \
+    k_trace_render<M, 1, Traversal<false>, true><<<cfg.grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, \
+                                                                         rq, d_n, hq, hq_n, accum, work, err, \
+                                                                         cfg.plain)
     if (t.wide) {
         if (t.multi) { WF_TRACE2(true, WideTraversal<false>); } else { WF_TRACE2(false, WideTraversal<false>); }
+    } else if (cfg.variant == 2) {
+        if (t.multi) { WF_TRACE_SHARED(true); } else { WF_TRACE_SHARED(false); }
     } else {
         if (t.multi) { WF_TRACE2(true, Traversal<false>); } else { WF_TRACE2(false, Traversal<false>); }
     }
+#undef WF_TRACE_SHARED
 #undef WF_TRACE2
 #undef WF_TRACE
 }
@@ -1135,14 +1171,21 @@ void launch_occluded_render(const WaveTables& t, ShadowQueueDev sh, const ull* s
 {
 #define WF_OCC(M, B, T)                                                                                       \
     k_occluded_render<M, B, T><<<cfg.grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, sh, sh_n, accum, work, \
-                                                        err)
+                                                        err, cfg.plain)
 #define WF_OCC2(M, T) \
     if (cfg.variant == 1) WF_OCC(M, 10, T); else WF_OCC(M, 1, T)
+#define WF_OCC_SHARED(M)                                                                                     \
+    k_occluded_render<M, 1, Traversal<true>, true><<<cfg.grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, \
+                                                                           sh, sh_n, accum, work, err, \
+                                                                           cfg.plain)
     if (t.wide) {
         if (t.multi) { WF_OCC2(true, WideTraversal<true>); } else { WF_OCC2(false, WideTraversal<true>); }
+    } else if (cfg.variant == 2) {
+        if (t.multi) { WF_OCC_SHARED(true); } else { WF_OCC_SHARED(false); }
     } else {
         if (t.multi) { WF_OCC2(true, Traversal<true>); } else { WF_OCC2(false, Traversal<true>); }
     }
+#undef WF_OCC_SHARED
 #undef WF_OCC2
 #undef WF_OCC
 }

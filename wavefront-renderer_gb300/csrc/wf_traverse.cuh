@@ -60,6 +60,13 @@ constexpr uint32_t kSentinel = 0xFFFFFFFFu;
 // interior nodes down to a leaf, then leaves until it pops an interior node or
 // the stack's sentinel, so the lanes of a warp reconverge after every round
 // and a persistent kernel can hand a finished lane a new ray between rounds.
+// A traversal stack kept in shared memory, entry i of thread t at
+// base[i * 128 + t] (one 128-thread block, no bank conflicts between lanes).
+struct SharedStack32 {
+    uint32_t* p;  // shared array + threadIdx.x
+    __device__ __forceinline__ uint32_t& operator[](int i) const { return p[i * 128]; }
+};
+
 template <bool kAnyHit>
 struct Traversal {
     using Entry = uint32_t;
@@ -70,12 +77,13 @@ struct Traversal {
     uint32_t cur;
     int sp;
     bool overflow;
+    bool speculative = true;
     TraceResult res;
 
     // The stack lives outside the struct (a dynamically indexed array would
     // pull the whole struct into local memory); stack[0] holds the sentinel.
-    __device__ __forceinline__ void init(const DeviceScene& S, uint32_t* stack, V3 o_, V3 d_, float tmin_,
-                                         float tmax_)
+    template <class Stk>
+    __device__ __forceinline__ void init(const DeviceScene& S, Stk stack, V3 o_, V3 d_, float tmin_, float tmax_)
     {
         o = o_;
         d = d_;
@@ -92,12 +100,17 @@ struct Traversal {
     }
     __device__ __forceinline__ bool done() const { return cur == kSentinel; }
     __device__ __forceinline__ void idle() { cur = kSentinel; }
-    __device__ __forceinline__ void round(const DeviceScene& S, uint32_t* stack) { round(S.nodes, S.tris, stack); }
+    template <class Stk>
+    __device__ __forceinline__ void round(const DeviceScene& S, Stk stack)
+    {
+        round(S.nodes, S.tris, stack);
+    }
 
     // nodes / tris of the ray's scene: from the kernel's parameter bank when
     // every ray shares one scene, else from the scene table.
+    template <class Stk>
     __device__ __forceinline__ void round(const BvhNode* __restrict__ nodes, const float4* __restrict__ tris,
-                                          uint32_t* stack)
+                                          Stk stack)
     {
         // Speculative while-while (Aila & Laine 2009): a lane that reaches a
         // leaf postpones it and keeps descending while another lane of the
@@ -126,11 +139,12 @@ struct Traversal {
                     cur = stack[--sp];
                 }
             }
-            if (postponed == 0u && cur != kSentinel && (cur & kLeafFlag)) {
+            if (speculative && postponed == 0u && cur != kSentinel && (cur & kLeafFlag)) {
                 postponed = cur;
                 cur = stack[--sp];
             }
-            const bool searching = postponed == 0u && cur != kSentinel;
+            const bool searching = speculative ? (postponed == 0u && cur != kSentinel)
+                                               : (cur != kSentinel && !(cur & kLeafFlag));
             if (!__any_sync(active, searching)) break;
         }
         if (postponed != 0u && test_leaf(tris, postponed)) {
