@@ -461,12 +461,16 @@ def main() -> int:
     alg_bytes = closest * BYTES_RAY + hits * BYTES_HIT + misses * BYTES_MISS
     achieved = alg_bytes / (trace_ms / 1e3) / 1e9
     peak, peak_kind = measured_peaks()
+    # DRAM bytes per closest-hit ray of k_trace_render, measured by ncu over
+    # every launch of a smaller render of the same scene (profiles/); scaled to
+    # this run's average launch by its rays.
     traffic = None
     tp = ROOT / "profiles" / "traffic.json"
     if tp.exists():
         try:
-            traffic = json.loads(tp.read_text()).get(wl["name"])
-        except Exception:
+            per_ray = json.loads(tp.read_text())[f"config{wl['config']}"]["dram_bytes_per_closest_ray"]
+            traffic = per_ray * closest / max(launches, 1)
+        except (KeyError, ValueError, TypeError):
             traffic = None
 
     line = {

@@ -272,9 +272,9 @@ typedef struct wf_scene_info {
 } wf_scene_info;
 int wf_scene_get_info(wf_ctx* ctx, wf_scene_info* out_info);
 
-/* Launch tuning of a context (the autotuner's knobs).  trace_variant: 0 = no
- * occupancy hint on the traversal kernels, 1 = 10 blocks of 128 threads per
- * SM, 2 = the traversal stack in shared memory instead of local memory
+/* Launch tuning of a context (the autotuner's knobs).  trace_variant: 0 = the
+ * default occupancy of the traversal kernels, 1 = 10 blocks of 128 threads
+ * per SM, 2 = the traversal stack in shared memory instead of local memory
  * (binary trees; 32 KB per block).  persistent_blocks_per_sm: resident blocks launched per
  * SM by the persistent traversal kernels (0 = 16).  graph_mode: whether a
  * wave's bounce chain is captured once as a CUDA graph and replayed. */

@@ -237,6 +237,10 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_trace_render(DeviceScene sc
     int64_t ray = -1;
     bool exhausted = false;
     bool overflow = false;
+    // the ray's payload, read with the ray (consecutive indices per fetch)
+    // and parked in this thread's shared-memory slot until the ray ends
+    __shared__ float4 pay_f[128];  // throughput, pdf
+    __shared__ int2 pay_i[128];    // pixel, sample
     tr.idle();
     for (;;) {
         // 1. lanes whose traversal ended emit their result
@@ -251,7 +255,21 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_trace_render(DeviceScene sc
             if (hit) {
                 const int64_t pos = (int64_t)base + __popc(hm & lt);
                 if (pos < hq.capacity) {
-                    hq.ray[pos] = (int32_t)ray;
+                    const float4 pf = pay_f[threadIdx.x];
+                    const int2 pi = pay_i[threadIdx.x];
+                    hq.ox[pos] = tr.o.x;
+                    hq.oy[pos] = tr.o.y;
+                    hq.oz[pos] = tr.o.z;
+                    hq.dx[pos] = tr.d.x;
+                    hq.dy[pos] = tr.d.y;
+                    hq.dz[pos] = tr.d.z;
+                    hq.tr[pos] = pf.x;
+                    hq.tg[pos] = pf.y;
+                    hq.tb[pos] = pf.z;
+                    hq.pdf[pos] = pf.w;
+                    hq.pixel[pos] = pi.x;
+                    hq.sample[pos] = pi.y;
+                    hq.job[pos] = job;
                     hq.tri[pos] = tr.res.leafpos;
                     hq.t[pos] = tr.res.t;
                     hq.bu[pos] = tr.res.bu;
@@ -263,16 +281,14 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_trace_render(DeviceScene sc
         }
         if (fin && !hit) {
             const DeviceJob& J = kMulti ? jobs[job] : job0;
-            const V3 T = {rq.tr[ray], rq.tg[ray], rq.tb[ray]};
-            V3 c = T * sky_color(*S, tr.d);
+            const float4 pf = pay_f[threadIdx.x];
+            const int2 pi = pay_i[threadIdx.x];
+            V3 c = v3(pf.x, pf.y, pf.z) * sky_color(*S, tr.d);
             // With environment NEE the bounce that sampled this direction by
             // its BSDF (pdf > 0) shares the estimate: balance-heuristic weight.
-            if (J.env_nee && S->env_alias_prob) {
-                const float ip = rq.pdf[ray];
-                if (ip > 0.0f) c = c * mis_balance(ip, env_pdf(*S, normalized(tr.d)));
-            }
-            const int32_t slot = job_slot(J, rq.pixel[ray], J.sample_buf ? rq.sample[ray] : 0);
-            accum_add(job_accum(J, accum), slot, c);
+            if (J.env_nee && S->env_alias_prob && pf.w > 0.0f)
+                c = c * mis_balance(pf.w, env_pdf(*S, normalized(tr.d)));
+            accum_add(job_accum(J, accum), job_slot(J, pi.x, pi.y), c);
         }
         if (fin) {
             overflow = overflow || tr.overflow;
@@ -294,6 +310,8 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_trace_render(DeviceScene sc
                         job = rq.job[idx];
                         S = scenes + jobs[job].scene;
                     }
+                    pay_f[threadIdx.x] = make_float4(rq.tr[idx], rq.tg[idx], rq.tb[idx], rq.pdf[idx]);
+                    pay_i[threadIdx.x] = make_int2(rq.pixel[idx], rq.sample[idx]);
                     tr.init(*S, stack, v3(rq.ox[idx], rq.oy[idx], rq.oz[idx]),
                             v3(rq.dx[idx], rq.dy[idx], rq.dz[idx]), 0.001f, 1e9f);
                 } else {
@@ -386,7 +404,7 @@ __global__ void k_cost_update(CostTrackerDev mat, CostTrackerDev tex, int repeat
 template <bool kMulti>
 __global__ void __launch_bounds__(128) k_shade(DeviceScene scene0, DeviceJob job0,
                                                const DeviceScene* __restrict__ scenes,
-                                               const DeviceJob* __restrict__ jobs, RayQueueDev rq,
+                                               const DeviceJob* __restrict__ jobs, int bounce,
                                                HitQueueDev hq, const ull* __restrict__ hq_n,
                                                ShadowQueueDev sh, ull* sh_n, RayQueueDev nx,
                                                ull* nx_n, float* accum_base, int* err)
@@ -404,20 +422,19 @@ __global__ void __launch_bounds__(128) k_shade(DeviceScene scene0, DeviceJob job
         int cost_mat = -1, cost_tex = -1;
         unsigned cyc_mat = 0, cyc_tex = 0;
         if (active) {
-            const int ri = hq.ray[k];
-            job = kMulti ? rq.job[ri] : 0;
+            job = kMulti ? hq.job[k] : 0;
             const DeviceJob& J = kMulti ? jobs[job] : job0;
             const DeviceScene& S = kMulti ? scenes[J.scene] : scene0;
             float* accum = job_accum(J, accum_base);
             const float ff = J.firefly;
             const uint32_t seed_lo = J.seed_lo, seed_hi = J.seed_hi;
-            const V3 o = {rq.ox[ri], rq.oy[ri], rq.oz[ri]};
-            const V3 d = {rq.dx[ri], rq.dy[ri], rq.dz[ri]};
-            const V3 T = {rq.tr[ri], rq.tg[ri], rq.tb[ri]};
-            const float in_pdf = rq.pdf[ri];
-            pixel = rq.pixel[ri];
-            depth = rq.depth[ri];
-            sample = rq.sample[ri];
+            const V3 o = {hq.ox[k], hq.oy[k], hq.oz[k]};
+            const V3 d = {hq.dx[k], hq.dy[k], hq.dz[k]};
+            const V3 T = {hq.tr[k], hq.tg[k], hq.tb[k]};
+            const float in_pdf = hq.pdf[k];
+            pixel = hq.pixel[k];
+            depth = bounce;  // every ray of a wave's bounce has this depth
+            sample = hq.sample[k];
             slot = job_slot(J, pixel, sample);
             HitRec h;
             rebuild_hit(S, o, d, hq.tri[k], hq.t[k], hq.bu[k], hq.bv[k], h);
@@ -932,25 +949,23 @@ __global__ void k_cb_keys(ShadeColumnsDev c, const ull* __restrict__ d_n,
 }
 
 __global__ void k_hit_columns(const DeviceScene* __restrict__ scenes, const DeviceJob* __restrict__ jobs,
-                              RayQueueDev rq, HitQueueDev hq, const ull* __restrict__ d_n,
-                              ShadeColumnsMut out)
+                              HitQueueDev hq, const ull* __restrict__ d_n, ShadeColumnsMut out)
 {
     const int64_t n = (int64_t)*d_n;
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
          k += (int64_t)gridDim.x * blockDim.x) {
-        const int ri = hq.ray[k];
-        const DeviceScene& S = scenes[jobs[rq.job[ri]].scene];
+        const DeviceScene& S = scenes[jobs[hq.job[k]].scene];
         const float4 b = __ldg(S.tris + 3 * (int64_t)hq.tri[k] + 1);
         const int m = S.mesh_material[__float_as_int(b.w)];
         out.mat[k] = m;
         out.tex[k] = S.materials[m].texture_id;
-        out.tr[k] = rq.tr[ri];
-        out.tg[k] = rq.tg[ri];
-        out.tb[k] = rq.tb[ri];
+        out.tr[k] = hq.tr[k];
+        out.tg[k] = hq.tg[k];
+        out.tb[k] = hq.tb[k];
         const float t = hq.t[k];
-        out.px[k] = rq.ox[ri] + rq.dx[ri] * t;
-        out.py[k] = rq.oy[ri] + rq.dy[ri] * t;
-        out.pz[k] = rq.oz[ri] + rq.dz[ri] * t;
+        out.px[k] = hq.ox[k] + hq.dx[k] * t;
+        out.py[k] = hq.oy[k] + hq.dy[k] * t;
+        out.pz[k] = hq.oz[k] + hq.dz[k] * t;
     }
 }
 
@@ -961,7 +976,19 @@ __global__ void k_permute_hits(HitQueueDev in, const uint32_t* __restrict__ perm
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x) {
         const uint32_t j = perm[i];
-        out.ray[i] = in.ray[j];
+        out.ox[i] = in.ox[j];
+        out.oy[i] = in.oy[j];
+        out.oz[i] = in.oz[j];
+        out.dx[i] = in.dx[j];
+        out.dy[i] = in.dy[j];
+        out.dz[i] = in.dz[j];
+        out.tr[i] = in.tr[j];
+        out.tg[i] = in.tg[j];
+        out.tb[i] = in.tb[j];
+        out.pdf[i] = in.pdf[j];
+        out.pixel[i] = in.pixel[j];
+        out.sample[i] = in.sample[j];
+        out.job[i] = in.job[j];
         out.tri[i] = in.tri[j];
         out.t[i] = in.t[j];
         out.bu[i] = in.bu[j];
@@ -1120,9 +1147,10 @@ void launch_occluded_api(const DeviceScene& S, int64_t n, const float* ox, const
                                                              out, err);
 }
 
-// variant: 0 = no occupancy hint, 1 = 10 blocks of 128 per SM, 2 = the
-// traversal stack in shared memory (binary trees); the traversal follows the
-// scene's tree (compressed 8-wide or binary).
+// variant: 0 = at least 8 resident blocks of 128 per SM for the closest-hit
+// kernel (no hint for the shadow kernel), 1 = 10 blocks, 2 = the traversal
+// stack in shared memory (binary trees); the traversal follows the scene's
+// tree (compressed 8-wide or binary).
 void launch_trace_render(const WaveTables& t, RayQueueDev rq, const ull* d_n, HitQueueDev hq, ull* hq_n,
                          float* accum, ull* work, int* err, LaunchCfg cfg, cudaStream_t s)
 {
@@ -1130,7 +1158,7 @@ void launch_trace_render(const WaveTables& t, RayQueueDev rq, const ull* d_n, Hi
     k_trace_render<M, B, T><<<cfg.grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, d_n, hq, hq_n, \
                                                      accum, work, err, cfg.plain)
 #define WF_TRACE2(M, T) \
-    if (cfg.variant == 1) WF_TRACE(M, 10, T); else WF_TRACE(M, 1, T)
+    if (cfg.variant == 1) WF_TRACE(M, 10, T); else WF_TRACE(M, 8, T)
 #define WF_TRACE_SHARED(M)                                                                                \
     k_trace_render<M, 1, Traversal<false>, true><<<cfg.grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, \
                                                                          rq, d_n, hq, hq_n, accum, work, err, \
@@ -1155,14 +1183,14 @@ void launch_camera_chunks(const WaveChunk* chunks, const long long* header, cons
 
 void launch_tally(const ull* counters, ull* tally, cudaStream_t s) { k_tally<<<1, 1, 0, s>>>(counters, tally); }
 
-void launch_shade(const WaveTables& t, RayQueueDev rq, HitQueueDev hq, const ull* hq_n, ShadowQueueDev sh,
+void launch_shade(const WaveTables& t, int bounce, HitQueueDev hq, const ull* hq_n, ShadowQueueDev sh,
                   ull* sh_n, RayQueueDev next, ull* next_n, float* accum, int* err, LaunchCfg cfg, cudaStream_t s)
 {
     if (t.multi)
-        k_shade<true><<<cfg.grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, hq, hq_n, sh, sh_n, next,
+        k_shade<true><<<cfg.grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, bounce, hq, hq_n, sh, sh_n, next,
                                                next_n, accum, err);
     else
-        k_shade<false><<<cfg.grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, hq, hq_n, sh, sh_n, next,
+        k_shade<false><<<cfg.grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, bounce, hq, hq_n, sh, sh_n, next,
                                                 next_n, accum, err);
 }
 
@@ -1245,10 +1273,10 @@ void launch_cb_keys(ShadeColumnsDev c, const ull* d_n, const wf_material* mats,
     k_cb_keys<<<cfg.grid, 256, 0, s>>>(c, d_n, mats, prio_rank, prio_bits, bounds6, keys, vals);
 }
 
-void launch_hit_columns(const DeviceScene* scenes, const DeviceJob* jobs, RayQueueDev rq, HitQueueDev hq,
-                        const ull* d_n, ShadeColumnsMut out, LaunchCfg cfg, cudaStream_t s)
+void launch_hit_columns(const DeviceScene* scenes, const DeviceJob* jobs, HitQueueDev hq, const ull* d_n,
+                        ShadeColumnsMut out, LaunchCfg cfg, cudaStream_t s)
 {
-    k_hit_columns<<<cfg.grid, 256, 0, s>>>(scenes, jobs, rq, hq, d_n, out);
+    k_hit_columns<<<cfg.grid, 256, 0, s>>>(scenes, jobs, hq, d_n, out);
 }
 
 void launch_permute_hits(HitQueueDev in, const uint32_t* perm, const ull* d_n, HitQueueDev out,
