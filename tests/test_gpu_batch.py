@@ -105,7 +105,7 @@ def test_server_admission_respects_budget(wf, ctx):
     for j in jobs:
         j.width, j.height, j.samples_per_pixel = 64, 64, 8
     wave = 1 << 14
-    per_path = 2 * 14 * 4 + 2 * 17 * 4 + 3 * 12 * 4 + 2 * 12 + 8 * 4
+    per_path = 2 * 14 * 4 + 2 * 5 * 4 + 3 * 12 * 4 + 2 * 12 + 8 * 4
     budget = wave * per_path + 2 * 64 * 64 * 3 * 4  # room for two accumulators
     srv = wf.Server(ctx, hbm_budget_bytes=budget, frame_spp=8, max_paths_per_wave=wave)
     ids = [srv.submit(j) for j in jobs]

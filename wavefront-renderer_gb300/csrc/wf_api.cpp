@@ -69,12 +69,7 @@ int ensure_render_buffers(wf_ctx* c, int64_t paths)
         WF_CK(c, wf_dalloc(A, &r.job, n));
         r.capacity = paths;
         HitQueueDev& h = c->hq[q];
-        WF_CK(c, wf_dalloc(A, &h.ox, n)); WF_CK(c, wf_dalloc(A, &h.oy, n)); WF_CK(c, wf_dalloc(A, &h.oz, n));
-        WF_CK(c, wf_dalloc(A, &h.dx, n)); WF_CK(c, wf_dalloc(A, &h.dy, n)); WF_CK(c, wf_dalloc(A, &h.dz, n));
-        WF_CK(c, wf_dalloc(A, &h.tr, n)); WF_CK(c, wf_dalloc(A, &h.tg, n)); WF_CK(c, wf_dalloc(A, &h.tb, n));
-        WF_CK(c, wf_dalloc(A, &h.pdf, n));
-        WF_CK(c, wf_dalloc(A, &h.pixel, n)); WF_CK(c, wf_dalloc(A, &h.sample, n)); WF_CK(c, wf_dalloc(A, &h.job, n));
-        WF_CK(c, wf_dalloc(A, &h.tri, n)); WF_CK(c, wf_dalloc(A, &h.t, n));
+        WF_CK(c, wf_dalloc(A, &h.ray, n)); WF_CK(c, wf_dalloc(A, &h.tri, n)); WF_CK(c, wf_dalloc(A, &h.t, n));
         WF_CK(c, wf_dalloc(A, &h.bu, n)); WF_CK(c, wf_dalloc(A, &h.bv, n));
         h.capacity = paths;
     }

@@ -138,14 +138,7 @@ struct RayQueueDev {
 // Compact hit queue: one entry per ray that hit (the ShadingQueue of the
 // render loop).  The full HitRecord is rebuilt from the triangle on demand.
 struct HitQueueDev {
-    // The ray that hit, copied by the closest-hit kernel (which read it in
-    // ray order when it took the ray) so that shading reads every column in
-    // queue order — the ShadingQueue's ray columns (ShadingQueue.h:27-51).
-    float *ox, *oy, *oz, *dx, *dy, *dz;
-    float *tr, *tg, *tb;
-    float* pdf;
-    int32_t *pixel, *sample, *job;
-    // The hit
+    int32_t* ray;   // index into the ray queue
     int32_t* tri;   // leaf-order triangle position
     float* t;       // HitRecord::distance
     float* bu;      // barycentrics from Moller-Trumbore

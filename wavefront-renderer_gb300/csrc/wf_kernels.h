@@ -64,7 +64,7 @@ struct WaveTables {
 };
 void launch_trace_render(const WaveTables& t, RayQueueDev rq, const ull* d_n, HitQueueDev hq, ull* hq_n,
                          float* accum, ull* work, int* err, LaunchCfg cfg, cudaStream_t s);
-void launch_shade(const WaveTables& t, int bounce, HitQueueDev hq, const ull* hq_n, ShadowQueueDev sh,
+void launch_shade(const WaveTables& t, RayQueueDev rq, HitQueueDev hq, const ull* hq_n, ShadowQueueDev sh,
                   ull* sh_n, RayQueueDev next, ull* next_n, float* accum, int* err, LaunchCfg cfg, cudaStream_t s);
 void launch_occluded_render(const WaveTables& t, ShadowQueueDev sh, const ull* sh_n, float* accum, ull* work,
                             int* err, LaunchCfg cfg, cudaStream_t s);
@@ -111,8 +111,8 @@ struct ShadeColumnsMut {
     int32_t* tex;
     float *tr, *tg, *tb, *px, *py, *pz;
 };
-void launch_hit_columns(const DeviceScene* scenes, const DeviceJob* jobs, HitQueueDev hq, const ull* d_n,
-                        ShadeColumnsMut out, LaunchCfg cfg, cudaStream_t s);
+void launch_hit_columns(const DeviceScene* scenes, const DeviceJob* jobs, RayQueueDev rq, HitQueueDev hq,
+                        const ull* d_n, ShadeColumnsMut out, LaunchCfg cfg, cudaStream_t s);
 void launch_permute_hits(HitQueueDev in, const uint32_t* perm, const ull* d_n, HitQueueDev out,
                          LaunchCfg cfg, cudaStream_t s);
 

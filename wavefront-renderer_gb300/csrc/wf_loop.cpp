@@ -169,7 +169,7 @@ int wave_host(wf_ctx* c, int64_t total, int max_depth, int policy, bool ray_sort
         }
         if (policy != WF_POLICY_NONE && hits >= (ull)c->tuning.sort_min_queue) {
             ShadeColumnsMut cm{c->col_mat, c->col_tex, c->col_tr, c->col_tg, c->col_tb, c->col_px, c->col_py, c->col_pz};
-            launch_hit_columns(c->d_scene_table, c->d_jobs, c->hq[0], c->counters + 1, cm, WC, s);
+            launch_hit_columns(c->d_scene_table, c->d_jobs, c->rq[cur], c->hq[0], c->counters + 1, cm, WC, s);
             ShadeColumnsDev cd{c->col_mat, c->col_tex, c->col_tr, c->col_tg, c->col_tb, c->col_px, c->col_py, c->col_pz};
             const ResidentScene& R = c->scenes[policy_scene];
             if (track_costs) {  // the trackers' state after the previous bounce
@@ -193,7 +193,7 @@ int wave_host(wf_ctx* c, int64_t total, int max_depth, int policy, bool ray_sort
             stats.sorted_elements += hits;
         }
         WF_CK(c, cudaEventRecord(ev[6], s));
-        launch_shade(T, depth, hq_use, c->counters + 1, c->sh, c->counters + 2, c->rq[1 - cur], c->counters + 3,
+        launch_shade(T, c->rq[cur], hq_use, c->counters + 1, c->sh, c->counters + 2, c->rq[1 - cur], c->counters + 3,
                      c->arena, c->err_flag, PC, s);
         if (track_costs) {  // the tracker merge at the end of shadeAll (.cpp:800-844)
             launch_cost_update(c->ct_mat, c->ct_tex, cost_records, s);
@@ -251,7 +251,7 @@ int record_chain(wf_ctx* c, int max_depth, bool ray_sort, bool wide)
         cudaMemsetAsync(c->counters + 1, 0, sizeof(ull) * 5, s);
         launch_trace_render(T, c->rq[cur], c->counters, c->hq[0], c->counters + 1, c->arena, c->counters + 4,
                             c->err_flag, PC, s);
-        launch_shade(T, depth, c->hq[0], c->counters + 1, c->sh, c->counters + 2, c->rq[1 - cur], c->counters + 3,
+        launch_shade(T, c->rq[cur], c->hq[0], c->counters + 1, c->sh, c->counters + 2, c->rq[1 - cur], c->counters + 3,
                      c->arena, c->err_flag, PC, s);
         launch_occluded_render(T, c->sh, c->counters + 2, c->arena, c->counters + 5, c->err_flag, PC, s);
         launch_tally(c->counters, c->tally, s);
@@ -554,9 +554,9 @@ struct wf_server {
 namespace {
 
 // Bytes of the wave buffers per path in flight: two RayQueues (14 columns),
-// two hit queues (17), the shadow queue (3 x 12), sort keys and values
-// (2 x 12) and the policy columns (8).
-constexpr int64_t kBytesPerPath = 2 * 14 * 4 + 2 * 17 * 4 + 3 * 12 * 4 + 2 * 12 + 8 * 4;
+// two hit queues (5), the shadow queue (2 x 12), sort keys and values (2 x 12)
+// and the policy columns (8).
+constexpr int64_t kBytesPerPath = 2 * 14 * 4 + 2 * 5 * 4 + 3 * 12 * 4 + 2 * 12 + 8 * 4;
 
 int finish_job(wf_server* sv, int64_t id, ServedJob& j)
 {

@@ -237,10 +237,6 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_trace_render(DeviceScene sc
     int64_t ray = -1;
     bool exhausted = false;
     bool overflow = false;
-    // the ray's payload, read with the ray (consecutive indices per fetch)
-    // and parked in this thread's shared-memory slot until the ray ends
-    __shared__ float4 pay_f[128];  // throughput, pdf
-    __shared__ int2 pay_i[128];    // pixel, sample
     tr.idle();
     for (;;) {
         // 1. lanes whose traversal ended emit their result
@@ -255,21 +251,7 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_trace_render(DeviceScene sc
             if (hit) {
                 const int64_t pos = (int64_t)base + __popc(hm & lt);
                 if (pos < hq.capacity) {
-                    const float4 pf = pay_f[threadIdx.x];
-                    const int2 pi = pay_i[threadIdx.x];
-                    hq.ox[pos] = tr.o.x;
-                    hq.oy[pos] = tr.o.y;
-                    hq.oz[pos] = tr.o.z;
-                    hq.dx[pos] = tr.d.x;
-                    hq.dy[pos] = tr.d.y;
-                    hq.dz[pos] = tr.d.z;
-                    hq.tr[pos] = pf.x;
-                    hq.tg[pos] = pf.y;
-                    hq.tb[pos] = pf.z;
-                    hq.pdf[pos] = pf.w;
-                    hq.pixel[pos] = pi.x;
-                    hq.sample[pos] = pi.y;
-                    hq.job[pos] = job;
+                    hq.ray[pos] = (int32_t)ray;
                     hq.tri[pos] = tr.res.leafpos;
                     hq.t[pos] = tr.res.t;
                     hq.bu[pos] = tr.res.bu;
@@ -281,14 +263,16 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_trace_render(DeviceScene sc
         }
         if (fin && !hit) {
             const DeviceJob& J = kMulti ? jobs[job] : job0;
-            const float4 pf = pay_f[threadIdx.x];
-            const int2 pi = pay_i[threadIdx.x];
-            V3 c = v3(pf.x, pf.y, pf.z) * sky_color(*S, tr.d);
+            const V3 T = {rq.tr[ray], rq.tg[ray], rq.tb[ray]};
+            V3 c = T * sky_color(*S, tr.d);
             // With environment NEE the bounce that sampled this direction by
             // its BSDF (pdf > 0) shares the estimate: balance-heuristic weight.
-            if (J.env_nee && S->env_alias_prob && pf.w > 0.0f)
-                c = c * mis_balance(pf.w, env_pdf(*S, normalized(tr.d)));
-            accum_add(job_accum(J, accum), job_slot(J, pi.x, pi.y), c);
+            if (J.env_nee && S->env_alias_prob) {
+                const float ip = rq.pdf[ray];
+                if (ip > 0.0f) c = c * mis_balance(ip, env_pdf(*S, normalized(tr.d)));
+            }
+            const int32_t slot = job_slot(J, rq.pixel[ray], J.sample_buf ? rq.sample[ray] : 0);
+            accum_add(job_accum(J, accum), slot, c);
         }
         if (fin) {
             overflow = overflow || tr.overflow;
@@ -310,8 +294,6 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_trace_render(DeviceScene sc
                         job = rq.job[idx];
                         S = scenes + jobs[job].scene;
                     }
-                    pay_f[threadIdx.x] = make_float4(rq.tr[idx], rq.tg[idx], rq.tb[idx], rq.pdf[idx]);
-                    pay_i[threadIdx.x] = make_int2(rq.pixel[idx], rq.sample[idx]);
                     tr.init(*S, stack, v3(rq.ox[idx], rq.oy[idx], rq.oz[idx]),
                             v3(rq.dx[idx], rq.dy[idx], rq.dz[idx]), 0.001f, 1e9f);
                 } else {
@@ -404,7 +386,7 @@ __global__ void k_cost_update(CostTrackerDev mat, CostTrackerDev tex, int repeat
 template <bool kMulti>
 __global__ void __launch_bounds__(128) k_shade(DeviceScene scene0, DeviceJob job0,
                                                const DeviceScene* __restrict__ scenes,
-                                               const DeviceJob* __restrict__ jobs, int bounce,
+                                               const DeviceJob* __restrict__ jobs, RayQueueDev rq,
                                                HitQueueDev hq, const ull* __restrict__ hq_n,
                                                ShadowQueueDev sh, ull* sh_n, RayQueueDev nx,
                                                ull* nx_n, float* accum_base, int* err)
@@ -422,19 +404,20 @@ __global__ void __launch_bounds__(128) k_shade(DeviceScene scene0, DeviceJob job
         int cost_mat = -1, cost_tex = -1;
         unsigned cyc_mat = 0, cyc_tex = 0;
         if (active) {
-            job = kMulti ? hq.job[k] : 0;
+            const int ri = hq.ray[k];
+            job = kMulti ? rq.job[ri] : 0;
             const DeviceJob& J = kMulti ? jobs[job] : job0;
             const DeviceScene& S = kMulti ? scenes[J.scene] : scene0;
             float* accum = job_accum(J, accum_base);
             const float ff = J.firefly;
             const uint32_t seed_lo = J.seed_lo, seed_hi = J.seed_hi;
-            const V3 o = {hq.ox[k], hq.oy[k], hq.oz[k]};
-            const V3 d = {hq.dx[k], hq.dy[k], hq.dz[k]};
-            const V3 T = {hq.tr[k], hq.tg[k], hq.tb[k]};
-            const float in_pdf = hq.pdf[k];
-            pixel = hq.pixel[k];
-            depth = bounce;  // every ray of a wave's bounce has this depth
-            sample = hq.sample[k];
+            const V3 o = {rq.ox[ri], rq.oy[ri], rq.oz[ri]};
+            const V3 d = {rq.dx[ri], rq.dy[ri], rq.dz[ri]};
+            const V3 T = {rq.tr[ri], rq.tg[ri], rq.tb[ri]};
+            const float in_pdf = rq.pdf[ri];
+            pixel = rq.pixel[ri];
+            depth = rq.depth[ri];
+            sample = rq.sample[ri];
             slot = job_slot(J, pixel, sample);
             HitRec h;
             rebuild_hit(S, o, d, hq.tri[k], hq.t[k], hq.bu[k], hq.bv[k], h);
@@ -949,23 +932,25 @@ __global__ void k_cb_keys(ShadeColumnsDev c, const ull* __restrict__ d_n,
 }
 
 __global__ void k_hit_columns(const DeviceScene* __restrict__ scenes, const DeviceJob* __restrict__ jobs,
-                              HitQueueDev hq, const ull* __restrict__ d_n, ShadeColumnsMut out)
+                              RayQueueDev rq, HitQueueDev hq, const ull* __restrict__ d_n,
+                              ShadeColumnsMut out)
 {
     const int64_t n = (int64_t)*d_n;
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
          k += (int64_t)gridDim.x * blockDim.x) {
-        const DeviceScene& S = scenes[jobs[hq.job[k]].scene];
+        const int ri = hq.ray[k];
+        const DeviceScene& S = scenes[jobs[rq.job[ri]].scene];
         const float4 b = __ldg(S.tris + 3 * (int64_t)hq.tri[k] + 1);
         const int m = S.mesh_material[__float_as_int(b.w)];
         out.mat[k] = m;
         out.tex[k] = S.materials[m].texture_id;
-        out.tr[k] = hq.tr[k];
-        out.tg[k] = hq.tg[k];
-        out.tb[k] = hq.tb[k];
+        out.tr[k] = rq.tr[ri];
+        out.tg[k] = rq.tg[ri];
+        out.tb[k] = rq.tb[ri];
         const float t = hq.t[k];
-        out.px[k] = hq.ox[k] + hq.dx[k] * t;
-        out.py[k] = hq.oy[k] + hq.dy[k] * t;
-        out.pz[k] = hq.oz[k] + hq.dz[k] * t;
+        out.px[k] = rq.ox[ri] + rq.dx[ri] * t;
+        out.py[k] = rq.oy[ri] + rq.dy[ri] * t;
+        out.pz[k] = rq.oz[ri] + rq.dz[ri] * t;
     }
 }
 
@@ -976,19 +961,7 @@ __global__ void k_permute_hits(HitQueueDev in, const uint32_t* __restrict__ perm
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x) {
         const uint32_t j = perm[i];
-        out.ox[i] = in.ox[j];
-        out.oy[i] = in.oy[j];
-        out.oz[i] = in.oz[j];
-        out.dx[i] = in.dx[j];
-        out.dy[i] = in.dy[j];
-        out.dz[i] = in.dz[j];
-        out.tr[i] = in.tr[j];
-        out.tg[i] = in.tg[j];
-        out.tb[i] = in.tb[j];
-        out.pdf[i] = in.pdf[j];
-        out.pixel[i] = in.pixel[j];
-        out.sample[i] = in.sample[j];
-        out.job[i] = in.job[j];
+        out.ray[i] = in.ray[j];
         out.tri[i] = in.tri[j];
         out.t[i] = in.t[j];
         out.bu[i] = in.bu[j];
@@ -1183,14 +1156,14 @@ void launch_camera_chunks(const WaveChunk* chunks, const long long* header, cons
 
 void launch_tally(const ull* counters, ull* tally, cudaStream_t s) { k_tally<<<1, 1, 0, s>>>(counters, tally); }
 
-void launch_shade(const WaveTables& t, int bounce, HitQueueDev hq, const ull* hq_n, ShadowQueueDev sh,
+void launch_shade(const WaveTables& t, RayQueueDev rq, HitQueueDev hq, const ull* hq_n, ShadowQueueDev sh,
                   ull* sh_n, RayQueueDev next, ull* next_n, float* accum, int* err, LaunchCfg cfg, cudaStream_t s)
 {
     if (t.multi)
-        k_shade<true><<<cfg.grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, bounce, hq, hq_n, sh, sh_n, next,
+        k_shade<true><<<cfg.grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, hq, hq_n, sh, sh_n, next,
                                                next_n, accum, err);
     else
-        k_shade<false><<<cfg.grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, bounce, hq, hq_n, sh, sh_n, next,
+        k_shade<false><<<cfg.grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, hq, hq_n, sh, sh_n, next,
                                                 next_n, accum, err);
 }
 
@@ -1273,10 +1246,10 @@ void launch_cb_keys(ShadeColumnsDev c, const ull* d_n, const wf_material* mats,
     k_cb_keys<<<cfg.grid, 256, 0, s>>>(c, d_n, mats, prio_rank, prio_bits, bounds6, keys, vals);
 }
 
-void launch_hit_columns(const DeviceScene* scenes, const DeviceJob* jobs, HitQueueDev hq, const ull* d_n,
-                        ShadeColumnsMut out, LaunchCfg cfg, cudaStream_t s)
+void launch_hit_columns(const DeviceScene* scenes, const DeviceJob* jobs, RayQueueDev rq, HitQueueDev hq,
+                        const ull* d_n, ShadeColumnsMut out, LaunchCfg cfg, cudaStream_t s)
 {
-    k_hit_columns<<<cfg.grid, 256, 0, s>>>(scenes, jobs, hq, d_n, out);
+    k_hit_columns<<<cfg.grid, 256, 0, s>>>(scenes, jobs, rq, hq, d_n, out);
 }
 
 void launch_permute_hits(HitQueueDev in, const uint32_t* perm, const ull* d_n, HitQueueDev out,
