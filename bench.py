@@ -390,7 +390,7 @@ def main() -> int:
     ap.add_argument("--ref-spp", type=int, default=16)
     ap.add_argument("--bvh", default="ploc", choices=["ploc", "lbvh", "wide"])
     ap.add_argument("--autotune", type=int, default=0, help="run wf_autotune on the workload before timing")
-    ap.add_argument("--plain-traversal", type=int, default=0, help="1 = while-while without speculation")
+    ap.add_argument("--speculative", type=int, default=0, help="1 = speculative while-while traversal")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 0)
     if args.workload == "c3":
@@ -409,7 +409,8 @@ def main() -> int:
     ctx = pkg.Context(local)
     scene = pkg.HostScene(wl["config"])
     ctx.set_tuning(max(args.trace_variant, 0), args.blocks_per_sm,
-                   bvh_builder={"ploc": 0, "lbvh": 1, "wide": 2}[args.bvh], plain_traversal=args.plain_traversal)
+                   bvh_builder={"ploc": 0, "lbvh": 1, "wide": 2}[args.bvh],
+                   speculative_traversal=args.speculative)
     info = ctx.upload(scene.desc)
     W, H = wl["width"], wl["height"]
     cam = scene.camera(W, H)

@@ -272,9 +272,9 @@ typedef struct wf_scene_info {
 } wf_scene_info;
 int wf_scene_get_info(wf_ctx* ctx, wf_scene_info* out_info);
 
-/* Launch tuning of a context (the autotuner's knobs).  trace_variant: 0 = the
- * default occupancy of the traversal kernels, 1 = 10 blocks of 128 threads
- * per SM, 2 = the traversal stack in shared memory instead of local memory
+/* Launch tuning of a context (the autotuner's knobs).  trace_variant: 0 = no
+ * occupancy hint on the traversal kernels, 1 = 10 blocks of 128 threads per
+ * SM, 2 = the traversal stack in shared memory instead of local memory
  * (binary trees; 32 KB per block).  persistent_blocks_per_sm: resident blocks launched per
  * SM by the persistent traversal kernels (0 = 16).  graph_mode: whether a
  * wave's bounce chain is captured once as a CUDA graph and replayed. */
@@ -294,9 +294,9 @@ typedef struct wf_tuning {
                             at least this many entries (0 = always, as the
                             reference does); skipping reorders nothing that
                             changes the image */
-    int32_t plain_traversal; /* 1 = while-while traversal; 0 = speculative
-                            while-while (lanes postpone their first leaf until
-                            every lane of the warp has one) */
+    int32_t speculative_traversal; /* 0 = while-while traversal (default);
+                            1 = speculative while-while (lanes postpone their
+                            first leaf until every lane of the warp has one) */
     int32_t reserved[2];
 } wf_tuning;
 int wf_set_tuning(wf_ctx* ctx, const wf_tuning* tuning);
@@ -306,7 +306,7 @@ int wf_get_tuning(const wf_ctx* ctx, wf_tuning* out_tuning);
  * current scene (samples capped at one wave, adaptive sampling and cost
  * tracking off) under every combination of trace_variant {0, 1, 2} (block
  * occupancy and traversal-stack placement), persistent_blocks_per_sm
- * {4, 8, 12, 16, 24}, graph_mode {2, 1} and plain_traversal {0, 1}, each
+ * {4, 8, 12, 16, 24}, graph_mode {2, 1} and speculative_traversal {0, 1}, each
  * once untimed and twice
  * timed on the device; then, when params sort rays or shading, the
  * sort-or-skip threshold sort_min_queue over {0, 2^18, 2^20, 2^22, never}

@@ -39,7 +39,7 @@ void free_all(std::vector<void*>& v)
 LaunchCfg persist_cfg(const wf_ctx* c)
 {
     int per_sm = c->tuning.persistent_blocks_per_sm > 0 ? c->tuning.persistent_blocks_per_sm : 16;
-    return LaunchCfg{c->num_sms * per_sm, 128, c->tuning.trace_variant, c->tuning.plain_traversal};
+    return LaunchCfg{c->num_sms * per_sm, 128, c->tuning.trace_variant, c->tuning.speculative_traversal};
 }
 
 LaunchCfg wide_cfg(const wf_ctx* c) { return LaunchCfg{c->num_sms * 8, 256}; }

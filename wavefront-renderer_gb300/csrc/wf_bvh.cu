@@ -256,7 +256,10 @@ __global__ void k_depth(int n, const int* __restrict__ parent_int, int* max_dept
 // before their parents and the root is created last.
 // ===========================================================================
 
-constexpr int kPlocRadius = 16;
+#ifndef WF_PLOC_RADIUS
+#define WF_PLOC_RADIUS 16
+#endif
+constexpr int kPlocRadius = WF_PLOC_RADIUS;
 constexpr int kPlocBlock = 256;
 
 __device__ __forceinline__ float union_half_area(const float* a, const float* b)

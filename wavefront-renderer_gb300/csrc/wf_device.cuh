@@ -17,7 +17,10 @@
 namespace wf {
 
 constexpr float kPi = 3.14159265f;  // reference WavefrontRenderer.h:22, Material.cpp:8
-constexpr int kLeafMax = 4;         // triangles per BVH leaf
+#ifndef WF_LEAF_MAX
+#define WF_LEAF_MAX 4
+#endif
+constexpr int kLeafMax = WF_LEAF_MAX;  // triangles per BVH leaf (<= 8)
 constexpr int kStackSize = 64;      // traversal stack entries (checked at build)
 constexpr uint32_t kLeafFlag = 0x80000000u;
 

@@ -23,7 +23,7 @@ struct LaunchCfg {
     int grid;
     int block;
     int variant = 0;   // kernel variant (traversal occupancy hint / stack placement)
-    int plain = 0;     // 1 = while-while traversal without speculation
+    int speculative = 0;  // 1 = speculative while-while traversal
 };
 
 // Camera rays of n = width*height*nspp paths, sample-major.

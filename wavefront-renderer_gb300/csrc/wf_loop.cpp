@@ -644,16 +644,16 @@ int wf_autotune(wf_ctx* c, const wf_render_params* P, wf_tuning* out, double* ou
     const int variants[3] = {0, 1, 2};
     const int blocks[5] = {4, 8, 12, 16, 24};
     const int graphs[2] = {2, 1};
-    const int plains[2] = {0, 1};
+    const int specs[2] = {0, 1};
     for (int v : variants)
         for (int b : blocks)
             for (int g : graphs)
-                for (int pl : plains) {
+                for (int sp : specs) {
                 wf_tuning t = base;
                 t.trace_variant = v;
                 t.persistent_blocks_per_sm = b;
                 t.graph_mode = g;
-                t.plain_traversal = pl;
+                t.speculative_traversal = sp;
                 c->tuning = t;
                 double ms = 0.0;
                 for (int rep = 0; rep < 3; ++rep) {

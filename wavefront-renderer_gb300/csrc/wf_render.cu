@@ -180,10 +180,10 @@ __global__ void __launch_bounds__(128) k_occluded_api(DeviceScene S, int64_t n, 
 
 // Speculation switch of the binary traversal (the wide one has none).
 template <class Tr>
-__device__ __forceinline__ void set_plain(Tr& tr, bool plain)
+__device__ __forceinline__ void set_speculative(Tr& tr, bool on)
 {
     if constexpr (std::is_same<Tr, Traversal<false>>::value || std::is_same<Tr, Traversal<true>>::value)
-        tr.speculative = !plain;
+        tr.speculative = on;
 }
 
 // The traversal stack of a thread: its local array, or its column of the
@@ -222,7 +222,7 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_trace_render(DeviceScene sc
                                                                   const DeviceJob* __restrict__ jobs,
                                                                   RayQueueDev rq, const ull* __restrict__ d_n,
                                                                   HitQueueDev hq, ull* hq_n, float* accum,
-                                                                  ull* work, int* err, int plain)
+                                                                  ull* work, int* err, int speculative)
 {
     const int64_t n = (int64_t)*d_n;
     const int lane = threadIdx.x & 31;
@@ -232,7 +232,7 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_trace_render(DeviceScene sc
     __shared__ uint32_t shared_stack[kSharedStack ? kStackSize * 128 : 1];
     const auto stack = pick_stack<kSharedStack>(local_stack, shared_stack);
     const DeviceScene* S = kMulti ? scenes : &scene0;
-    set_plain(tr, plain != 0);
+    set_speculative(tr, speculative != 0);
     int job = 0;
     int64_t ray = -1;
     bool exhausted = false;
@@ -657,7 +657,7 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_occluded_render(DeviceScene
                                                                      ShadowQueueDev sh,
                                                                      const ull* __restrict__ d_n,
                                                                      float* accum, ull* work, int* err,
-                                                                     int plain)
+                                                                     int speculative)
 {
     const int64_t n = (int64_t)*d_n;
     const int lane = threadIdx.x & 31;
@@ -667,7 +667,7 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_occluded_render(DeviceScene
     __shared__ uint32_t shared_stack[kSharedStack ? kStackSize * 128 : 1];
     const auto stack = pick_stack<kSharedStack>(local_stack, shared_stack);
     const DeviceScene* S = kMulti ? scenes : &scene0;
-    set_plain(tr, plain != 0);
+    set_speculative(tr, speculative != 0);
     int job = 0;
     int64_t ray = -1;
     bool exhausted = false;
@@ -1120,22 +1120,21 @@ void launch_occluded_api(const DeviceScene& S, int64_t n, const float* ox, const
                                                              out, err);
 }
 
-// variant: 0 = at least 8 resident blocks of 128 per SM for the closest-hit
-// kernel (no hint for the shadow kernel), 1 = 10 blocks, 2 = the traversal
-// stack in shared memory (binary trees); the traversal follows the scene's
-// tree (compressed 8-wide or binary).
+// variant: 0 = no occupancy hint, 1 = 10 blocks of 128 per SM, 2 = the
+// traversal stack in shared memory (binary trees); the traversal follows the
+// scene's tree (compressed 8-wide or binary).
 void launch_trace_render(const WaveTables& t, RayQueueDev rq, const ull* d_n, HitQueueDev hq, ull* hq_n,
                          float* accum, ull* work, int* err, LaunchCfg cfg, cudaStream_t s)
 {
 #define WF_TRACE(M, B, T)                                                                                   \
     k_trace_render<M, B, T><<<cfg.grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, d_n, hq, hq_n, \
-                                                     accum, work, err, cfg.plain)
+                                                     accum, work, err, cfg.speculative)
 #define WF_TRACE2(M, T) \
-    if (cfg.variant == 1) WF_TRACE(M, 10, T); else WF_TRACE(M, 8, T)
+    if (cfg.variant == 1) WF_TRACE(M, 10, T); else WF_TRACE(M, 1, T)
 #define WF_TRACE_SHARED(M)                                                                                \
     k_trace_render<M, 1, Traversal<false>, true><<<cfg.grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, \
                                                                          rq, d_n, hq, hq_n, accum, work, err, \
-                                                                         cfg.plain)
+                                                                         cfg.speculative)
     if (t.wide) {
         if (t.multi) { WF_TRACE2(true, WideTraversal<false>); } else { WF_TRACE2(false, WideTraversal<false>); }
     } else if (cfg.variant == 2) {
@@ -1172,13 +1171,13 @@ void launch_occluded_render(const WaveTables& t, ShadowQueueDev sh, const ull* s
 {
 #define WF_OCC(M, B, T)                                                                                       \
     k_occluded_render<M, B, T><<<cfg.grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, sh, sh_n, accum, work, \
-                                                        err, cfg.plain)
+                                                        err, cfg.speculative)
 #define WF_OCC2(M, T) \
     if (cfg.variant == 1) WF_OCC(M, 10, T); else WF_OCC(M, 1, T)
 #define WF_OCC_SHARED(M)                                                                                     \
     k_occluded_render<M, 1, Traversal<true>, true><<<cfg.grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, \
                                                                            sh, sh_n, accum, work, err, \
-                                                                           cfg.plain)
+                                                                           cfg.speculative)
     if (t.wide) {
         if (t.multi) { WF_OCC2(true, WideTraversal<true>); } else { WF_OCC2(false, WideTraversal<true>); }
     } else if (cfg.variant == 2) {

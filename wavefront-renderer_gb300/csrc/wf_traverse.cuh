@@ -77,7 +77,7 @@ struct Traversal {
     uint32_t cur;
     int sp;
     bool overflow;
-    bool speculative = true;
+    bool speculative = false;
     TraceResult res;
 
     // The stack lives outside the struct (a dynamically indexed array would
@@ -112,6 +112,40 @@ struct Traversal {
     __device__ __forceinline__ void round(const BvhNode* __restrict__ nodes, const float4* __restrict__ tris,
                                           Stk stack)
     {
+        if (!speculative) {
+            // While-while: walk interior nodes down to a leaf, then test
+            // leaves until an interior node or the sentinel comes off the
+            // stack.
+            while (!(cur & kLeafFlag)) {
+                const BvhNode nd = load_node(nodes, cur);
+                float tn0, tn1;
+                bool h0, h1;
+                slab2(nd, inv, oi, tmin, best_t, tn0, tn1, h0, h1);
+                const uint32_t c0 = (uint32_t)nd.kids.x, c1 = (uint32_t)nd.kids.y;
+                if (h0 && h1) {
+                    const bool swap = tn1 < tn0;
+                    const uint32_t farc = swap ? c0 : c1;
+                    cur = swap ? c1 : c0;
+                    if (sp < kStackSize)
+                        stack[sp++] = farc;
+                    else
+                        overflow = true;
+                } else if (h0 || h1) {
+                    cur = h0 ? c0 : c1;
+                } else {
+                    cur = stack[--sp];
+                }
+            }
+            while (cur != kSentinel && (cur & kLeafFlag)) {
+                const uint32_t leaf = cur;
+                cur = stack[--sp];
+                if (test_leaf(tris, leaf)) {
+                    cur = kSentinel;
+                    return;
+                }
+            }
+            return;
+        }
         // Speculative while-while (Aila & Laine 2009): a lane that reaches a
         // leaf postpones it and keeps descending while another lane of the
         // warp is still looking for its first leaf; then all lanes test
@@ -139,13 +173,11 @@ struct Traversal {
                     cur = stack[--sp];
                 }
             }
-            if (speculative && postponed == 0u && cur != kSentinel && (cur & kLeafFlag)) {
+            if (postponed == 0u && cur != kSentinel && (cur & kLeafFlag)) {
                 postponed = cur;
                 cur = stack[--sp];
             }
-            const bool searching = speculative ? (postponed == 0u && cur != kSentinel)
-                                               : (cur != kSentinel && !(cur & kLeafFlag));
-            if (!__any_sync(active, searching)) break;
+            if (!__any_sync(active, postponed == 0u && cur != kSentinel)) break;
         }
         if (postponed != 0u && test_leaf(tris, postponed)) {
             cur = kSentinel;  // any hit: done
