@@ -391,6 +391,8 @@ def main() -> int:
     ap.add_argument("--bvh", default="ploc", choices=["ploc", "lbvh", "wide"])
     ap.add_argument("--autotune", type=int, default=0, help="run wf_autotune on the workload before timing")
     ap.add_argument("--speculative", type=int, default=0, help="1 = speculative while-while traversal")
+    ap.add_argument("--adaptive", type=int, default=0, help="the reference's adaptive sampling (threshold 0.05)")
+    ap.add_argument("--cost-rr", type=int, default=0, help="cost-aware RR fed by the live device CostTracker")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 0)
     if args.workload == "c3":
@@ -418,7 +420,9 @@ def main() -> int:
 
     def params(seed):
         return pkg.render_params(W, H, wl["spp"], wl["depth"], cam, policy=policy, ray_sort=bool(args.ray_sort),
-                                 seed=seed, spp_per_wave=args.spp_per_wave, env_nee=bool(args.env_nee))
+                                 seed=seed, spp_per_wave=args.spp_per_wave, env_nee=bool(args.env_nee),
+                                 adaptive=bool(args.adaptive), cost_aware_rr=bool(args.cost_rr),
+                                 cost_tracking=bool(args.cost_rr))
 
     tune_ms = None
     if args.autotune:
@@ -442,6 +446,8 @@ def main() -> int:
     rays_all = allreduce_sum(dist, rays_local)
     value = rays_all / (ms_max / 1e3) / 1e6
     samples_all = world * args.steps * W * H * wl["spp"]
+    if args.adaptive:  # pixels stop early: the last step's per-pixel counts stand for every step
+        samples_all = world * args.steps * int(ctx.sample_counts(W, H).sum())
 
     # ---- end to end through the C ABI with host buffers ----
     barrier(dist)
@@ -479,7 +485,7 @@ def main() -> int:
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": wl["name"], "policy": args.policy, "ray_sort": bool(args.ray_sort),
-                   "env_nee": bool(args.env_nee),
+                   "env_nee": bool(args.env_nee), "adaptive": bool(args.adaptive), "cost_aware_rr": bool(args.cost_rr),
                    "triangles": info.num_triangles, "spp_per_wave": args.spp_per_wave or "auto",
                    "l2": "inputs larger than L2 (ray queues ~1 GB per wave of 8.4 M paths; "
                          f"BVH + triangles {info.num_triangles * 96 / 1e6:.0f} MB)",

@@ -275,7 +275,9 @@ int wf_scene_get_info(wf_ctx* ctx, wf_scene_info* out_info);
 /* Launch tuning of a context (the autotuner's knobs).  trace_variant: 0 = no
  * occupancy hint on the traversal kernels, 1 = 10 blocks of 128 threads per
  * SM, 2 = the traversal stack in shared memory instead of local memory
- * (binary trees; 32 KB per block).  persistent_blocks_per_sm: resident blocks launched per
+ * (binary trees; 32 KB per block), 3 = the top 256 nodes of the tree staged
+ * in shared memory (binary trees, single-scene renders).
+ * persistent_blocks_per_sm: resident blocks launched per
  * SM by the persistent traversal kernels (0 = 16).  graph_mode: whether a
  * wave's bounce chain is captured once as a CUDA graph and replayed. */
 typedef struct wf_tuning {
@@ -304,8 +306,8 @@ int wf_get_tuning(const wf_ctx* ctx, wf_tuning* out_tuning);
 
 /* Autotuner (no reference counterpart): renders one wave of `params` on the
  * current scene (samples capped at one wave, adaptive sampling and cost
- * tracking off) under every combination of trace_variant {0, 1, 2} (block
- * occupancy and traversal-stack placement), persistent_blocks_per_sm
+ * tracking off) under every combination of trace_variant {0, 1, 2, 3}
+ * (block occupancy, stack placement, node staging), persistent_blocks_per_sm
  * {4, 8, 12, 16, 24}, graph_mode {2, 1} and speculative_traversal {0, 1}, each
  * once untimed and twice
  * timed on the device; then, when params sort rays or shading, the

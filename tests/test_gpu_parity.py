@@ -298,7 +298,8 @@ def test_render_is_order_independent(wf, ctx, scene_small, scene_c2small, which)
     # launch tuning: occupancy variant, shared-memory stack, grid size,
     # graph replay and the sort-or-skip threshold change no pixel beyond that
     try:
-        for tune, kw in [(dict(trace_variant=1), {}), (dict(trace_variant=2), {}), (dict(speculative_traversal=1), {}),
+        for tune, kw in [(dict(trace_variant=1), {}), (dict(trace_variant=2), {}), (dict(trace_variant=3), {}),
+                         (dict(speculative_traversal=1), {}),
                          (dict(persistent_blocks_per_sm=4), {}), (dict(graph_mode=1), {}),
                          (dict(sort_min_queue=6000), dict(policy=1, ray_sort=True))]:
             ctx.set_tuning(**tune)
@@ -316,7 +317,7 @@ def test_autotune_picks_a_valid_tuning(wf, ctx, scene_small):
     try:
         tuning, ms = ctx.autotune(p)
         assert ms > 0
-        assert tuning["trace_variant"] in (0, 1, 2) and tuning["persistent_blocks_per_sm"] in (4, 8, 12, 16, 24)
+        assert tuning["trace_variant"] in (0, 1, 2, 3) and tuning["persistent_blocks_per_sm"] in (4, 8, 12, 16, 24)
         assert tuning["sort_min_queue"] in (0, 1 << 18, 1 << 20, 1 << 22, 2**31 - 1)
         assert ctx.get_tuning() == tuning
         img, _ = ctx.render(p)

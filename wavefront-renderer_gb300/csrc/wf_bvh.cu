@@ -257,7 +257,7 @@ __global__ void k_depth(int n, const int* __restrict__ parent_int, int* max_dept
 // ===========================================================================
 
 #ifndef WF_PLOC_RADIUS
-#define WF_PLOC_RADIUS 16
+#define WF_PLOC_RADIUS 32  // 16 -> 32: lattice +10%, dense mesh unchanged, build +15%
 #endif
 constexpr int kPlocRadius = WF_PLOC_RADIUS;
 constexpr int kPlocBlock = 256;

@@ -178,6 +178,8 @@ __global__ void __launch_bounds__(128) k_occluded_api(DeviceScene S, int64_t n, 
     }
 }
 
+constexpr int kTopNodes = 256;  // 16 KB of the tree's top staged per block
+
 // Speculation switch of the binary traversal (the wide one has none).
 template <class Tr>
 __device__ __forceinline__ void set_speculative(Tr& tr, bool on)
@@ -216,7 +218,7 @@ __device__ __forceinline__ void accum_add(float* accum, int32_t slot, V3 c)
 // ---------------------------------------------------------------------------
 // kMulti = false: every ray belongs to job0 on scene0 (passed by value, read
 // from the constant bank); true: each ray looks its job and scene up.
-template <bool kMulti, int kMinBlocks, class Tr, bool kSharedStack = false>
+template <bool kMulti, int kMinBlocks, class Tr, bool kSharedStack = false, bool kTopStage = false>
 __global__ void __launch_bounds__(128, kMinBlocks) k_trace_render(DeviceScene scene0, DeviceJob job0,
                                                                   const DeviceScene* __restrict__ scenes,
                                                                   const DeviceJob* __restrict__ jobs,
@@ -233,6 +235,16 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_trace_render(DeviceScene sc
     const auto stack = pick_stack<kSharedStack>(local_stack, shared_stack);
     const DeviceScene* S = kMulti ? scenes : &scene0;
     set_speculative(tr, speculative != 0);
+    // top of the single scene's tree in shared memory (node staging)
+    __shared__ BvhNode top_nodes[kTopStage ? kTopNodes : 1];
+    uint32_t num_top = 0;
+    if constexpr (kTopStage) {
+        num_top = (uint32_t)min(kTopNodes, scene0.num_nodes);
+        const float4* src = reinterpret_cast<const float4*>(scene0.nodes);
+        float4* dst = reinterpret_cast<float4*>(top_nodes);
+        for (uint32_t i = threadIdx.x; i < 4u * num_top; i += blockDim.x) dst[i] = __ldg(src + i);
+        __syncthreads();
+    }
     int job = 0;
     int64_t ray = -1;
     bool exhausted = false;
@@ -303,7 +315,12 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_trace_render(DeviceScene sc
         }
         if (__all_sync(0xFFFFFFFFu, ray < 0)) break;
         // 3. one traversal round
-        if (ray >= 0 && !tr.done()) tr.round(*S, stack);
+        if (ray >= 0 && !tr.done()) {
+            if constexpr (kTopStage)
+                tr.round(*S, stack, top_nodes, num_top);
+            else
+                tr.round(*S, stack);
+        }
     }
     if (overflow) atomicOr(err, 1);
 }
@@ -650,7 +667,7 @@ __global__ void __launch_bounds__(128) k_shade(DeviceScene scene0, DeviceJob job
 // Shadow rays (EmbreeAccelerator::occluded): unblocked contributions are
 // added to their pixel.  Same persistent, dynamic-fetch structure as
 // k_trace_render.
-template <bool kMulti, int kMinBlocks, class Tr, bool kSharedStack = false>
+template <bool kMulti, int kMinBlocks, class Tr, bool kSharedStack = false, bool kTopStage = false>
 __global__ void __launch_bounds__(128, kMinBlocks) k_occluded_render(DeviceScene scene0, DeviceJob job0,
                                                                      const DeviceScene* __restrict__ scenes,
                                                                      const DeviceJob* __restrict__ jobs,
@@ -668,6 +685,16 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_occluded_render(DeviceScene
     const auto stack = pick_stack<kSharedStack>(local_stack, shared_stack);
     const DeviceScene* S = kMulti ? scenes : &scene0;
     set_speculative(tr, speculative != 0);
+    // top of the single scene's tree in shared memory (node staging)
+    __shared__ BvhNode top_nodes[kTopStage ? kTopNodes : 1];
+    uint32_t num_top = 0;
+    if constexpr (kTopStage) {
+        num_top = (uint32_t)min(kTopNodes, scene0.num_nodes);
+        const float4* src = reinterpret_cast<const float4*>(scene0.nodes);
+        float4* dst = reinterpret_cast<float4*>(top_nodes);
+        for (uint32_t i = threadIdx.x; i < 4u * num_top; i += blockDim.x) dst[i] = __ldg(src + i);
+        __syncthreads();
+    }
     int job = 0;
     int64_t ray = -1;
     bool exhausted = false;
@@ -704,7 +731,12 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_occluded_render(DeviceScene
             }
         }
         if (__all_sync(0xFFFFFFFFu, ray < 0)) break;
-        if (ray >= 0 && !tr.done()) tr.round(*S, stack);
+        if (ray >= 0 && !tr.done()) {
+            if constexpr (kTopStage)
+                tr.round(*S, stack, top_nodes, num_top);
+            else
+                tr.round(*S, stack);
+        }
     }
     if (overflow) atomicOr(err, 1);
 }
@@ -1121,8 +1153,9 @@ void launch_occluded_api(const DeviceScene& S, int64_t n, const float* ox, const
 }
 
 // variant: 0 = no occupancy hint, 1 = 10 blocks of 128 per SM, 2 = the
-// traversal stack in shared memory (binary trees); the traversal follows the
-// scene's tree (compressed 8-wide or binary).
+// traversal stack in shared memory (binary trees), 3 = the top 256 nodes of
+// the tree staged in shared memory (binary trees, single-scene waves; else
+// variant 0); the traversal follows the scene's tree (8-wide or binary).
 void launch_trace_render(const WaveTables& t, RayQueueDev rq, const ull* d_n, HitQueueDev hq, ull* hq_n,
                          float* accum, ull* work, int* err, LaunchCfg cfg, cudaStream_t s)
 {
@@ -1139,6 +1172,9 @@ void launch_trace_render(const WaveTables& t, RayQueueDev rq, const ull* d_n, Hi
         if (t.multi) { WF_TRACE2(true, WideTraversal<false>); } else { WF_TRACE2(false, WideTraversal<false>); }
     } else if (cfg.variant == 2) {
         if (t.multi) { WF_TRACE_SHARED(true); } else { WF_TRACE_SHARED(false); }
+    } else if (cfg.variant == 3 && !t.multi && t.scene0.nodes) {
+        k_trace_render<false, 1, Traversal<false>, false, true><<<cfg.grid, 128, 0, s>>>(
+            t.scene0, t.job0, t.scenes, t.jobs, rq, d_n, hq, hq_n, accum, work, err, cfg.speculative);
     } else {
         if (t.multi) { WF_TRACE2(true, Traversal<false>); } else { WF_TRACE2(false, Traversal<false>); }
     }
@@ -1182,6 +1218,9 @@ void launch_occluded_render(const WaveTables& t, ShadowQueueDev sh, const ull* s
         if (t.multi) { WF_OCC2(true, WideTraversal<true>); } else { WF_OCC2(false, WideTraversal<true>); }
     } else if (cfg.variant == 2) {
         if (t.multi) { WF_OCC_SHARED(true); } else { WF_OCC_SHARED(false); }
+    } else if (cfg.variant == 3 && !t.multi && t.scene0.nodes) {
+        k_occluded_render<false, 1, Traversal<true>, false, true><<<cfg.grid, 128, 0, s>>>(
+            t.scene0, t.job0, t.scenes, t.jobs, sh, sh_n, accum, work, err, cfg.speculative);
     } else {
         if (t.multi) { WF_OCC2(true, Traversal<true>); } else { WF_OCC2(false, Traversal<true>); }
     }

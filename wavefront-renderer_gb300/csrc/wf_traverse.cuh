@@ -78,6 +78,8 @@ struct Traversal {
     int sp;
     bool overflow;
     bool speculative = false;
+    const BvhNode* top_nodes = nullptr;  // staged top of the tree (shared memory)
+    uint32_t num_top = 0;
     TraceResult res;
 
     // The stack lives outside the struct (a dynamically indexed array would
@@ -106,6 +108,16 @@ struct Traversal {
         round(S.nodes, S.tris, stack);
     }
 
+    // With the top of the tree staged in shared memory: nodes [0, ntop)
+    // (the root and the last clustering passes' nodes) come from `top`.
+    template <class Stk>
+    __device__ __forceinline__ void round(const DeviceScene& S, Stk stack, const BvhNode* top, uint32_t ntop)
+    {
+        top_nodes = top;
+        num_top = ntop;
+        round(S.nodes, S.tris, stack);
+    }
+
     // nodes / tris of the ray's scene: from the kernel's parameter bank when
     // every ray shares one scene, else from the scene table.
     template <class Stk>
@@ -117,7 +129,7 @@ struct Traversal {
             // leaves until an interior node or the sentinel comes off the
             // stack.
             while (!(cur & kLeafFlag)) {
-                const BvhNode nd = load_node(nodes, cur);
+                const BvhNode nd = cur < num_top ? top_nodes[cur] : load_node(nodes, cur);
                 float tn0, tn1;
                 bool h0, h1;
                 slab2(nd, inv, oi, tmin, best_t, tn0, tn1, h0, h1);
@@ -154,7 +166,7 @@ struct Traversal {
         uint32_t postponed = 0u;  // leaf words always carry kLeafFlag, so 0 = none
         for (;;) {
             if (cur != kSentinel && !(cur & kLeafFlag)) {
-                const BvhNode nd = load_node(nodes, cur);
+                const BvhNode nd = cur < num_top ? top_nodes[cur] : load_node(nodes, cur);
                 float tn0, tn1;
                 bool h0, h1;
                 slab2(nd, inv, oi, tmin, best_t, tn0, tn1, h0, h1);
