@@ -118,6 +118,8 @@ int ensure_adaptive(wf_ctx* c, int64_t np, int64_t buf_floats)
     WF_CK(c, wf_dalloc(A, &c->ad_count, n));
     WF_CK(c, wf_dalloc(A, &c->ad_active, n));
     WF_CK(c, wf_dalloc(A, &c->ad_flag, n));
+    WF_CK(c, wf_dalloc(A, &c->ad_pos, n));
+    WF_CK(c, wf_dalloc(A, &c->ad_bsums, (size_t)scan_block_words(np)));
     WF_CK(c, wf_dalloc(A, &c->ad_nactive, 1));
     WF_CK(c, wf_dalloc(A, &c->ad_buf, (size_t)buf_floats));
     c->ad_np_cap = np;

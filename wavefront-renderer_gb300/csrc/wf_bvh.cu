@@ -340,84 +340,6 @@ __global__ void k_ploc_apply(const int* __restrict__ cl, const int* __restrict__
     }
 }
 
-// Exclusive scan of n ints (three passes: per-block scans of 1024, one block
-// scanning the block totals, then the carries); *total gets the sum.
-__global__ void __launch_bounds__(1024) k_scan_blocks(const int* __restrict__ in, int n, int* __restrict__ out,
-                                                      int* __restrict__ block_sums)
-{
-    __shared__ int warp_incl[32];
-    const int i = blockIdx.x * 1024 + threadIdx.x;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int v = i < n ? in[i] : 0;
-    int x = v;
-    for (int o = 1; o < 32; o <<= 1) {
-        const int u = __shfl_up_sync(0xFFFFFFFFu, x, o);
-        if (lane >= o) x += u;
-    }
-    if (lane == 31) warp_incl[w] = x;
-    __syncthreads();
-    if (w == 0) {
-        int y = warp_incl[lane];
-        for (int o = 1; o < 32; o <<= 1) {
-            const int u = __shfl_up_sync(0xFFFFFFFFu, y, o);
-            if (lane >= o) y += u;
-        }
-        warp_incl[lane] = y;
-    }
-    __syncthreads();
-    const int excl = x - v + (w > 0 ? warp_incl[w - 1] : 0);
-    if (i < n) out[i] = excl;
-    if (threadIdx.x == 0) block_sums[blockIdx.x] = warp_incl[31];
-}
-
-__global__ void __launch_bounds__(1024) k_scan_sums(int* __restrict__ sums, int nb, int* __restrict__ total)
-{
-    __shared__ int warp_incl[32];
-    __shared__ int carry;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    if (threadIdx.x == 0) carry = 0;
-    __syncthreads();
-    for (int t0 = 0; t0 < nb; t0 += 1024) {
-        const int i = t0 + threadIdx.x;
-        const int v = i < nb ? sums[i] : 0;
-        int x = v;
-        for (int o = 1; o < 32; o <<= 1) {
-            const int u = __shfl_up_sync(0xFFFFFFFFu, x, o);
-            if (lane >= o) x += u;
-        }
-        if (lane == 31) warp_incl[w] = x;
-        __syncthreads();
-        if (w == 0) {
-            int y = warp_incl[lane];
-            for (int o = 1; o < 32; o <<= 1) {
-                const int u = __shfl_up_sync(0xFFFFFFFFu, y, o);
-                if (lane >= o) y += u;
-            }
-            warp_incl[lane] = y;
-        }
-        __syncthreads();
-        const int excl = x - v + (w > 0 ? warp_incl[w - 1] : 0);
-        if (i < nb) sums[i] = carry + excl;
-        __syncthreads();
-        if (threadIdx.x == 0) carry += warp_incl[31];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) *total = carry;
-}
-
-__global__ void k_scan_add(int* __restrict__ out, int n, const int* __restrict__ sums)
-{
-    const int i = blockIdx.x * 1024 + threadIdx.x;
-    if (i < n) out[i] += sums[blockIdx.x];
-}
-
-void scan_i32(const int* in, int n, int* out, int* block_sums, int* total, cudaStream_t s)
-{
-    const int nb = (n + 1023) / 1024;
-    k_scan_blocks<<<nb, 1024, 0, s>>>(in, n, out, block_sums);
-    k_scan_sums<<<1, 1024, 0, s>>>(block_sums, nb, total);
-    k_scan_add<<<nb, 1024, 0, s>>>(out, n, block_sums);
-}
 
 // Top-down over one iteration's nodes: children's first triangle position
 // (depth-first order, left subtree first) and depth.
@@ -991,8 +913,8 @@ int ploc_tree(const BvhBuildInput& in, int num_sms, cudaStream_t s, std::string&
     while (cur_n > 1) {
         k_ploc_nn<<<(cur_n + kPlocBlock - 1) / kPlocBlock, kPlocBlock, 0, s>>>(cl, cur_n, T.nbox, nn);
         k_ploc_flags<<<grid, 256, 0, s>>>(nn, cur_n, merge, valid);
-        scan_i32(merge, cur_n, m_off, T.block_sums, T.d_total, s);
-        scan_i32(valid, cur_n, v_off, T.block_sums, T.d_total + 1, s);
+        exclusive_scan_i32(merge, cur_n, m_off, T.block_sums, T.d_total, s);
+        exclusive_scan_i32(valid, cur_n, v_off, T.block_sums, T.d_total + 1, s);
         int tot[2] = {0, 0};
         WF_TRY(cudaMemcpyAsync(tot, T.d_total, sizeof(tot), cudaMemcpyDeviceToHost, s));
         WF_TRY(cudaStreamSynchronize(s));
@@ -1047,7 +969,7 @@ int build_ploc(const BvhBuildInput& in, BvhBuildOutput& out, int num_sms, cudaSt
     } else {
         const int ninternal = T.root - n + 1;
         k_ploc_keep<<<grid, 256, 0, s>>>(n, T.root, T.cnt, keep);
-        scan_i32(keep, ninternal, newid, T.block_sums, T.d_total, s);
+        exclusive_scan_i32(keep, ninternal, newid, T.block_sums, T.d_total, s);
         int kept = 0;
         WF_TRY(cudaMemcpyAsync(&kept, T.d_total, sizeof(int), cudaMemcpyDeviceToHost, s));
         WF_TRY(cudaStreamSynchronize(s));
@@ -1112,8 +1034,8 @@ int build_ploc_wide(const BvhBuildInput& in, BvhBuildOutput& out, int num_sms, c
         }
         const int g = std::max(1, std::min(grid, (count + 127) / 128));
         k_wide_gather<<<g, 128, 0, s>>>(items, count, n, T.left, T.right, T.cnt, T.nbox, kids, n_int, n_tri);
-        scan_i32(n_int, count, int_off, T.block_sums, T.d_total, s);
-        scan_i32(n_tri, count, tri_off, T.block_sums, T.d_total + 1, s);
+        exclusive_scan_i32(n_int, count, int_off, T.block_sums, T.d_total, s);
+        exclusive_scan_i32(n_tri, count, tri_off, T.block_sums, T.d_total + 1, s);
         int tot[2] = {0, 0};
         WF_TRY(cudaMemcpyAsync(tot, T.d_total, sizeof(tot), cudaMemcpyDeviceToHost, s));
         WF_TRY(cudaStreamSynchronize(s));

@@ -102,7 +102,7 @@ struct wf_ctx {
     int64_t ad_np_cap = 0, ad_buf_cap = 0;
     float *ad_mean = nullptr, *ad_m2 = nullptr, *ad_buf = nullptr;
     int32_t *ad_count = nullptr, *ad_active = nullptr, *ad_nactive = nullptr;
-    uint8_t* ad_flag = nullptr;
+    int32_t *ad_flag = nullptr, *ad_pos = nullptr, *ad_bsums = nullptr;
     bool last_adaptive = false;
     int64_t last_np = 0;
     int32_t last_spp = 0;

@@ -125,8 +125,9 @@ void launch_finalize(const float* accum, int64_t nfloats, float spp, float* imag
 void launch_adaptive_fold(float* sample_buf, int64_t np, int nspp, float* accum, float* mean, float* m2,
                           int32_t* count, const int32_t* active, int32_t n_active, cudaStream_t s);
 void launch_adaptive_check(const float* mean, const float* m2, const int32_t* count, const int32_t* active,
-                           int32_t n_active, float threshold, uint8_t* flag, cudaStream_t s);
-void launch_compact_active(const uint8_t* flag, int64_t np, int32_t* out, int32_t* n_out, cudaStream_t s);
+                           int32_t n_active, float threshold, int32_t* flag, cudaStream_t s);
+void launch_compact_active(const int32_t* flag, int64_t np, int32_t* pos, int32_t* block_sums, int32_t* out,
+                           int32_t* n_out, cudaStream_t s);
 void launch_finalize_counts(const float* accum, const int32_t* count, int64_t np, float* image, cudaStream_t s);
 void launch_fill_i32(int32_t* a, int64_t n, int32_t v, bool identity, cudaStream_t s);
 

@@ -392,9 +392,9 @@ int render_single(wf_ctx* c, const wf_render_params* P, wf_render_stats* st)
         WF_CK(c, cudaMemsetAsync(c->ad_mean, 0, sizeof(float) * (size_t)np, s));
         WF_CK(c, cudaMemsetAsync(c->ad_m2, 0, sizeof(float) * (size_t)np, s));
         WF_CK(c, cudaMemsetAsync(c->ad_count, 0, sizeof(int32_t) * (size_t)np, s));
-        WF_CK(c, cudaMemsetAsync(c->ad_flag, 1, (size_t)np, s));
+        launch_fill_i32(c->ad_flag, np, 1, false, s);
         launch_fill_i32(c->ad_active, np, 0, true, s);
-        kernels_setup = 1;
+        kernels_setup = 2;
     }
     const bool tracking = P->enable_cost_tracking != 0;
     if (tracking) {
@@ -440,8 +440,8 @@ int render_single(wf_ctx* c, const wf_render_params* P, wf_render_stats* st)
             if ((s0 + nspp) % 16 == 0) {
                 launch_adaptive_check(c->ad_mean, c->ad_m2, c->ad_count, c->ad_active, n_active,
                                       P->adaptive_threshold, c->ad_flag, s);
-                launch_compact_active(c->ad_flag, np, c->ad_active, c->ad_nactive, s);
-                stats.kernel_launches += 2;
+                launch_compact_active(c->ad_flag, np, c->ad_pos, c->ad_bsums, c->ad_active, c->ad_nactive, s);
+                stats.kernel_launches += 5;
                 WF_CK(c, cudaMemcpyAsync(&n_active, c->ad_nactive, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
                 WF_CK(c, cudaStreamSynchronize(s));
                 if (n_active == 0) {

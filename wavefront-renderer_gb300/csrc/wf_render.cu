@@ -5,6 +5,7 @@
 #include <type_traits>
 
 #include "wf_kernels.h"
+#include "wf_sort.h"
 #include "wf_traverse.cuh"
 
 namespace wf {
@@ -1056,7 +1057,7 @@ __global__ void k_adaptive_fold(float* __restrict__ sample_buf, int64_t np, int 
 // stops.
 __global__ void k_adaptive_check(const float* __restrict__ mean, const float* __restrict__ m2,
                                  const int32_t* __restrict__ count, const int32_t* __restrict__ active,
-                                 int32_t n_active, float threshold, uint8_t* __restrict__ flag)
+                                 int32_t n_active, float threshold, int32_t* __restrict__ flag)
 {
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n_active;
          r += (int64_t)gridDim.x * blockDim.x) {
@@ -1069,38 +1070,13 @@ __global__ void k_adaptive_check(const float* __restrict__ mean, const float* __
     }
 }
 
-// The pixels still active, in index order (one block: a ballot per warp and
-// a scan of the 32 warp counts per tile of 1024 pixels).
-__global__ void __launch_bounds__(1024) k_compact_active(const uint8_t* __restrict__ flag, int64_t np,
-                                                         int32_t* __restrict__ out, int32_t* __restrict__ n_out)
+// The pixels still active, in index order: their flags' exclusive prefix sum
+// gives each one its position.
+__global__ void k_scatter_active(const int32_t* __restrict__ flag, const int32_t* __restrict__ pos, int64_t np,
+                                 int32_t* __restrict__ out)
 {
-    __shared__ int warp_incl[32];
-    __shared__ int base;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    if (threadIdx.x == 0) base = 0;
-    __syncthreads();
-    for (int64_t t0 = 0; t0 < np; t0 += 1024) {
-        const int64_t i = t0 + threadIdx.x;
-        const bool f = i < np && flag[i] != 0;
-        const unsigned b = __ballot_sync(0xFFFFFFFFu, f);
-        if (lane == 0) warp_incl[w] = __popc(b);
-        __syncthreads();
-        if (w == 0) {
-            int v = warp_incl[lane];
-            for (int o = 1; o < 32; o <<= 1) {
-                const int u = __shfl_up_sync(0xFFFFFFFFu, v, o);
-                if (lane >= o) v += u;
-            }
-            warp_incl[lane] = v;
-        }
-        __syncthreads();
-        const int before = (w > 0 ? warp_incl[w - 1] : 0) + __popc(b & ((1u << lane) - 1u));
-        if (f) out[base + before] = (int32_t)i;
-        __syncthreads();
-        if (threadIdx.x == 0) base += warp_incl[31];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) *n_out = base;
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < np; p += (int64_t)gridDim.x * blockDim.x)
+        if (flag[p]) out[pos[p]] = (int32_t)p;
 }
 
 // writeAveragedImage with per-pixel counts (.cpp:127-137).
@@ -1315,16 +1291,18 @@ void launch_adaptive_fold(float* sample_buf, int64_t np, int nspp, float* accum,
 }
 
 void launch_adaptive_check(const float* mean, const float* m2, const int32_t* count, const int32_t* active,
-                           int32_t n_active, float threshold, uint8_t* flag, cudaStream_t s)
+                           int32_t n_active, float threshold, int32_t* flag, cudaStream_t s)
 {
     if (n_active <= 0) return;
     k_adaptive_check<<<grid_for(n_active, 256, 65535), 256, 0, s>>>(mean, m2, count, active, n_active, threshold,
                                                                     flag);
 }
 
-void launch_compact_active(const uint8_t* flag, int64_t np, int32_t* out, int32_t* n_out, cudaStream_t s)
+void launch_compact_active(const int32_t* flag, int64_t np, int32_t* pos, int32_t* block_sums, int32_t* out,
+                           int32_t* n_out, cudaStream_t s)
 {
-    k_compact_active<<<1, 1024, 0, s>>>(flag, np, out, n_out);
+    exclusive_scan_i32(flag, (int)np, pos, block_sums, n_out, s);
+    k_scatter_active<<<grid_for(np, 256, 65535), 256, 0, s>>>(flag, pos, np, out);
 }
 
 void launch_finalize_counts(const float* accum, const int32_t* count, int64_t np, float* image, cudaStream_t s)

@@ -26,4 +26,10 @@ size_t radix_hist_words(int nb);
 void radix_sort_pairs(RadixSortArgs args, cudaStream_t stream);
 void launch_iota(uint32_t* v, const unsigned long long* d_n, int grid, cudaStream_t stream);
 
+// Exclusive prefix sum of n ints (n > 0): per-block scans of 1024, one block
+// over the block totals, then the carries.  block_sums needs
+// scan_block_words(n) ints; *total (device) receives the sum.
+void exclusive_scan_i32(const int* in, int n, int* out, int* block_sums, int* total, cudaStream_t stream);
+inline int scan_block_words(int64_t n) { return (int)((n + 1023) / 1024) + 1; }
+
 }  // namespace wf
