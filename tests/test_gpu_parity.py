@@ -566,3 +566,18 @@ def test_bvh_builders_give_identical_hits(wf, orc, ctx, scene0, scene_small, sce
         ctx.set_tuning()
     assert [i.bvh_builder for i in infos] == [0, 1, 2]
     assert infos[2].bvh_nodes < infos[0].bvh_nodes  # the 8-wide tree has fewer nodes
+
+
+def test_scene_file_renders_like_the_original(wf, ctx, scene_c2small, tmp_path):
+    """A scene written with wf_scene_save and read back renders the same image
+    on the GPU (same arrays, same tree, same random streams)."""
+    path = tmp_path / "lattice.wfscene"
+    scene_c2small.save(path, [8.0, 4.48, 17.9], [8.0, 0.0, 6.08], [0, 1, 0], 50.0)
+    back = wf.HostScene.load(path)
+    cam = back.camera(40, 30)
+    p = wf.render_params(40, 30, 4, 6, cam, seed=12)
+    ctx.upload(scene_c2small.desc)
+    a, _ = ctx.render(p)
+    ctx.upload(back.desc)
+    b, _ = ctx.render(p)
+    assert np.isclose(a, b, rtol=1e-4, atol=1e-6).all(axis=2).mean() >= 0.999

@@ -307,7 +307,7 @@ int schedule_columns(wf_ctx* c, int policy, const ull* d_n, int64_t n, ShadeColu
         WF_CK(c, cudaMemsetAsync(c->present, 0, sizeof(int) * num_materials, s));
         unsigned init[6] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0u, 0u, 0u};
         WF_CK(c, cudaMemcpyAsync(c->bounds6, init, sizeof(init), cudaMemcpyHostToDevice, s));
-        launch_cb_reduce(cols, d_n, c->benefit, c->present, c->bounds6, W, s);
+        launch_cb_reduce(cols, d_n, c->benefit, c->present, c->bounds6, num_materials, W, s);
         std::vector<double> ben(num_materials);
         std::vector<int> pres(num_materials);
         WF_CK(c, cudaMemcpyAsync(ben.data(), c->benefit, sizeof(double) * num_materials, cudaMemcpyDeviceToHost, s));

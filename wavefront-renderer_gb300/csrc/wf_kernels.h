@@ -101,7 +101,7 @@ void launch_policy_keys(ShadeColumnsDev c, const ull* d_n, const wf_material* ma
                         cudaStream_t s);
 // Cost-benefit: per material luminance sums and hit-point bounds.
 void launch_cb_reduce(ShadeColumnsDev c, const ull* d_n, double* benefit, int* present,
-                      unsigned* bounds6, LaunchCfg cfg, cudaStream_t s);
+                      unsigned* bounds6, int num_materials, LaunchCfg cfg, cudaStream_t s);
 void launch_cb_keys(ShadeColumnsDev c, const ull* d_n, const wf_material* mats,
                     const int* prio_rank, int prio_bits, const unsigned* bounds6, uint64_t* keys,
                     uint32_t* vals, LaunchCfg cfg, cudaStream_t s);

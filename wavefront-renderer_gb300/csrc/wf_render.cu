@@ -827,6 +827,8 @@ __global__ void k_gather_rays(RayQueueDev in, const uint32_t* __restrict__ perm,
 // ShadingQueue scheduling (include/scheduling/ShadingQueue.h:90-141,
 // 277-329, 437-550).
 // ---------------------------------------------------------------------------
+constexpr int kCbSharedMaterials = 4096;  // per-block benefit sums up to 32 KB
+
 __global__ void k_type_stats(ShadeColumnsDev c, const ull* __restrict__ d_n,
                              const wf_material* __restrict__ mats, int num_tex,
                              const int64_t* __restrict__ tex_bytes, ull* counts, ull* mem,
@@ -841,13 +843,25 @@ __global__ void k_type_stats(ShadeColumnsDev c, const ull* __restrict__ d_n,
     }
     __syncthreads();
     const int64_t n = (int64_t)*d_n;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-         i += (int64_t)gridDim.x * blockDim.x) {
-        const int ty = mats[c.mat[i]].type & 7;
-        atomicAdd(&s_cnt[ty], 1ull);
-        atomicMin(&s_first[ty], (int)i);
-        const int tid = c.tex[i];
-        if (tid >= 0 && tid < num_tex) atomicAdd(&s_mem[ty], (ull)tex_bytes[tid]);
+    const int lane = threadIdx.x & 31;
+    // whole warps iterate together so that equal types aggregate per warp
+    for (int64_t b = blockIdx.x * (int64_t)blockDim.x; b < n; b += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = b + threadIdx.x;
+        const bool ok = i < n;
+        const int ty = ok ? (mats[c.mat[i]].type & 7) : -1;
+        const int tid = ok ? c.tex[i] : -1;
+        const ull mem = (tid >= 0 && tid < num_tex) ? (ull)tex_bytes[tid] : 0ull;
+        const unsigned peers = __match_any_sync(0xFFFFFFFFu, ty);
+        ull msum = 0;
+        for (int k = 0; k < 32; ++k) {
+            const ull v = __shfl_sync(0xFFFFFFFFu, mem, k);
+            if ((peers >> k) & 1u) msum += v;
+        }
+        if (ok && lane == __ffs(peers) - 1) {  // the lowest lane holds the group's first index
+            atomicAdd(&s_cnt[ty], (ull)__popc(peers));
+            atomicMin(&s_first[ty], (int)i);
+            if (msum) atomicAdd(&s_mem[ty], msum);
+        }
     }
     __syncthreads();
     if (threadIdx.x < 8) {
@@ -896,26 +910,53 @@ __device__ __forceinline__ float ordered_to_float(unsigned u)
     return __uint_as_float(b);
 }
 
+// Per-material benefit (sum of luminance(throughput), in double) and the hit
+// points' bounds.  Lanes of a warp hitting the same material add their sum
+// once; with few enough materials a block first sums into shared memory.
 __global__ void k_cb_reduce(ShadeColumnsDev c, const ull* __restrict__ d_n, double* benefit,
-                            int* present, unsigned* bounds6)
+                            int* present, unsigned* bounds6, int num_materials)
 {
+    extern __shared__ double s_benefit[];
+    const bool staged = num_materials <= kCbSharedMaterials;
+    if (staged)
+        for (int m = threadIdx.x; m < num_materials; m += blockDim.x) s_benefit[m] = 0.0;
+    __syncthreads();
     const int64_t n = (int64_t)*d_n;
+    const int lane = threadIdx.x & 31;
     unsigned mn[3] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu}, mx[3] = {0u, 0u, 0u};
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-         i += (int64_t)gridDim.x * blockDim.x) {
-        const int m = c.mat[i];
+    for (int64_t b = blockIdx.x * (int64_t)blockDim.x; b < n; b += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = b + threadIdx.x;
+        const bool ok = i < n;
+        const int m = ok ? c.mat[i] : -1;
         // luminance, include/render/AdaptiveSampler.h:21-27 (float), summed in double
-        const float l = 0.2126f * c.tr[i] + 0.7152f * c.tg[i] + 0.0722f * c.tb[i];
-        atomicAdd(&benefit[m], (double)l);
-        present[m] = 1;
-        const float p3[3] = {c.px[i], c.py[i], c.pz[i]};
+        const double l = ok ? (double)(0.2126f * c.tr[i] + 0.7152f * c.tg[i] + 0.0722f * c.tb[i]) : 0.0;
+        const unsigned peers = __match_any_sync(0xFFFFFFFFu, m);
+        double sum = 0.0;
+        for (int k = 0; k < 32; ++k) {
+            const double v = __shfl_sync(0xFFFFFFFFu, l, k);
+            if ((peers >> k) & 1u) sum += v;
+        }
+        if (ok && lane == __ffs(peers) - 1) {
+            if (staged)
+                atomicAdd(&s_benefit[m], sum);
+            else
+                atomicAdd(&benefit[m], sum);
+            present[m] = 1;
+        }
+        if (ok) {
+            const float p3[3] = {c.px[i], c.py[i], c.pz[i]};
 #pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            unsigned o = float_to_ordered(p3[k]);
-            mn[k] = min(mn[k], o);
-            mx[k] = max(mx[k], o);
+            for (int k = 0; k < 3; ++k) {
+                unsigned o = float_to_ordered(p3[k]);
+                mn[k] = min(mn[k], o);
+                mx[k] = max(mx[k], o);
+            }
         }
     }
+    __syncthreads();
+    if (staged)
+        for (int m = threadIdx.x; m < num_materials; m += blockDim.x)
+            if (s_benefit[m] != 0.0) atomicAdd(&benefit[m], s_benefit[m]);
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
         for (int off = 16; off > 0; off >>= 1) {
@@ -1248,9 +1289,10 @@ void launch_policy_keys(ShadeColumnsDev c, const ull* d_n, const wf_material* ma
 }
 
 void launch_cb_reduce(ShadeColumnsDev c, const ull* d_n, double* benefit, int* present,
-                      unsigned* bounds6, LaunchCfg cfg, cudaStream_t s)
+                      unsigned* bounds6, int num_materials, LaunchCfg cfg, cudaStream_t s)
 {
-    k_cb_reduce<<<cfg.grid, 256, 0, s>>>(c, d_n, benefit, present, bounds6);
+    const size_t shm = num_materials <= kCbSharedMaterials ? sizeof(double) * (size_t)num_materials : 0;
+    k_cb_reduce<<<cfg.grid, 256, shm, s>>>(c, d_n, benefit, present, bounds6, num_materials);
 }
 
 void launch_cb_keys(ShadeColumnsDev c, const ull* d_n, const wf_material* mats,

@@ -7,13 +7,14 @@
 // exactly the permutation std::stable_sort gives with the reference
 // comparator.
 //
-// One pass per 8-bit digit, three kernels per pass:
+// One pass per 8-bit digit:
 //   hist    — each block counts the digits of its contiguous chunk
-//   scan    — one block turns the [digit][block] counts into offsets
-//   scatter — each block walks its chunk in tiles of 256 keys; a key's rank
-//             among equal digits of its warp comes from __match_any_sync,
-//             warps are combined with a per-digit prefix in shared memory,
-//             so order within a digit follows input order (stable).
+//   scan    — the [digit][block] counts become offsets (multi-block scan)
+//   scatter — each block walks its chunk in tiles of 2048 keys; a key's rank
+//             among equal digits comes from __match_any_sync within a warp
+//             and per-digit prefixes across warps and rounds, so order within
+//             a digit follows input order (stable); the tile is staged
+//             digit-sorted in shared memory and written out in runs.
 // The element count is read from device memory, so a pass can be launched
 // (and graph-captured) before the count is known on the host.
 #include "wf_sort.h"
@@ -52,31 +53,32 @@ __global__ void __launch_bounds__(kTile) k_hist(const uint64_t* __restrict__ key
     hist[(int64_t)threadIdx.x * nb + blockIdx.x] = h[threadIdx.x];
 }
 
-// Exclusive scan of total = 256*nb counts by one block of 1024 threads.
-__global__ void __launch_bounds__(1024) k_scan(uint32_t* __restrict__ hist, int total)
+constexpr int kItems = 8;                   // keys per thread per tile
+constexpr int kTileKeys = kTile * kItems;   // 2048 keys staged per tile
+
+// Exclusive scan of v over the 256 threads of a block (thread = digit).
+__device__ __forceinline__ uint32_t block_exclusive_scan256(uint32_t v, uint32_t* warp_sums)
 {
-    __shared__ uint32_t part[1024];
-    const int t = threadIdx.x;
-    const int per = (total + 1023) / 1024;
-    const int b = t * per, e = min(b + per, total);
-    uint32_t s = 0;
-    for (int i = b; i < e; ++i) s += hist[i];
-    part[t] = s;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t u = __shfl_up_sync(0xFFFFFFFFu, x, o);
+        if (lane >= o) x += u;
+    }
+    if (lane == 31) warp_sums[w] = x;
     __syncthreads();
-    for (int off = 1; off < 1024; off <<= 1) {
-        uint32_t v = t >= off ? part[t - off] : 0u;
-        __syncthreads();
-        part[t] += v;
-        __syncthreads();
-    }
-    uint32_t run = part[t] - s;
-    for (int i = b; i < e; ++i) {
-        uint32_t c = hist[i];
-        hist[i] = run;
-        run += c;
-    }
+    uint32_t before = 0;
+    for (int k = 0; k < w; ++k) before += warp_sums[k];
+    __syncthreads();
+    return before + x - v;
 }
 
+// Scatter of one digit pass.  A tile of 2048 keys is ranked in input order
+// (rounds of 256; within a round by warp, within a warp by __match_any_sync),
+// placed digit-sorted in shared memory, and written out in that order: the
+// keys of one digit leave a tile as one contiguous run, so the global writes
+// coalesce.  Stable: a key's position among equal digits follows its index.
 __global__ void __launch_bounds__(kTile) k_scatter(const uint64_t* __restrict__ kin,
                                                    const uint32_t* __restrict__ vin,
                                                    uint64_t* __restrict__ kout,
@@ -86,52 +88,78 @@ __global__ void __launch_bounds__(kTile) k_scatter(const uint64_t* __restrict__ 
                                                    int nb)
 {
     __shared__ uint32_t running[kDigits];
+    __shared__ uint32_t tile_cnt[kDigits];
+    __shared__ uint32_t tile_start[kDigits];
     __shared__ uint32_t wcnt[kTile / 32][kDigits];
-    __shared__ uint32_t tile_total[kDigits];
+    __shared__ uint32_t warp_sums[kTile / 32];
+    __shared__ uint64_t skey[kTileKeys];
+    __shared__ uint32_t sval[kTileKeys];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const unsigned lt = (1u << lane) - 1u;
     running[tid] = offs[(int64_t)tid * nb + blockIdx.x];
-#pragma unroll
-    for (int w = 0; w < kTile / 32; ++w) wcnt[w][tid] = 0;
-    __syncthreads();
     int64_t start, end;
     chunk_of((int64_t)*d_n, nb, blockIdx.x, start, end);
-    const unsigned lt = (1u << lane) - 1u;
-    for (int64_t base = start; base < end; base += kTile) {
-        const int64_t i = base + tid;
-        const bool valid = i < end;
-        uint64_t key = 0;
-        uint32_t val = 0, digit = 0;
-        unsigned vmask = __ballot_sync(0xFFFFFFFFu, valid);
-        int rank = 0;
-        if (valid) {
-            key = kin[i];
-            val = vin[i];
-            digit = (uint32_t)(key >> shift) & 0xFFu;
-            unsigned peers = __match_any_sync(vmask, digit);
-            rank = __popc(peers & lt);
-            if (rank == 0) wcnt[warp][digit] = __popc(peers);
-        }
-        __syncthreads();
-        {
-            uint32_t acc = 0;
-#pragma unroll
-            for (int w = 0; w < kTile / 32; ++w) {
-                uint32_t c = wcnt[w][tid];
-                wcnt[w][tid] = acc;
-                acc += c;
-            }
-            tile_total[tid] = acc;
-        }
-        __syncthreads();
-        if (valid) {
-            uint32_t pos = running[digit] + wcnt[warp][digit] + (uint32_t)rank;
-            kout[pos] = key;
-            vout[pos] = val;
-        }
-        __syncthreads();
-        running[tid] += tile_total[tid];
+    for (int64_t base = start; base < end; base += kTileKeys) {
+        tile_cnt[tid] = 0;
 #pragma unroll
         for (int w = 0; w < kTile / 32; ++w) wcnt[w][tid] = 0;
+        __syncthreads();
+        uint64_t key[kItems];
+        uint32_t val[kItems], rank[kItems];
+#pragma unroll
+        for (int r = 0; r < kItems; ++r) {
+            const int64_t i = base + (int64_t)r * kTile + tid;
+            const bool valid = i < end;
+            const unsigned vmask = __ballot_sync(0xFFFFFFFFu, valid);
+            uint32_t digit = 0;
+            int wrank = 0;
+            key[r] = 0;
+            val[r] = 0;
+            if (valid) {
+                key[r] = kin[i];
+                val[r] = vin[i];
+                digit = (uint32_t)(key[r] >> shift) & 0xFFu;
+                const unsigned peers = __match_any_sync(vmask, digit);
+                wrank = __popc(peers & lt);
+                if (wrank == 0) wcnt[warp][digit] = __popc(peers);
+            }
+            __syncthreads();
+            uint32_t round_total = 0;
+#pragma unroll
+            for (int w = 0; w < kTile / 32; ++w) {
+                const uint32_t c = wcnt[w][tid];
+                wcnt[w][tid] = round_total;
+                round_total += c;
+            }
+            __syncthreads();
+            rank[r] = valid ? tile_cnt[digit] + wcnt[warp][digit] + (uint32_t)wrank : 0u;
+            __syncthreads();
+            tile_cnt[tid] += round_total;
+#pragma unroll
+            for (int w = 0; w < kTile / 32; ++w) wcnt[w][tid] = 0;
+            __syncthreads();
+        }
+        tile_start[tid] = block_exclusive_scan256(tile_cnt[tid], warp_sums);
+        __syncthreads();
+        const int tile_n = (int)min((int64_t)kTileKeys, end - base);
+#pragma unroll
+        for (int r = 0; r < kItems; ++r) {
+            if (base + (int64_t)r * kTile + tid < end) {
+                const uint32_t pos = tile_start[(uint32_t)(key[r] >> shift) & 0xFFu] + rank[r];
+                skey[pos] = key[r];
+                sval[pos] = val[r];
+            }
+        }
+        __syncthreads();
+        for (int idx = tid; idx < tile_n; idx += kTile) {
+            const uint64_t k = skey[idx];
+            const uint32_t d = (uint32_t)(k >> shift) & 0xFFu;
+            const uint32_t gpos = running[d] + (uint32_t)idx - tile_start[d];
+            kout[gpos] = k;
+            vout[gpos] = sval[idx];
+        }
+        __syncthreads();
+        running[tid] += tile_cnt[tid];
         __syncthreads();
     }
 }
@@ -158,7 +186,7 @@ int radix_blocks_for(int64_t capacity, int num_sms)
     return (int)want;
 }
 
-size_t radix_hist_words(int nb) { return (size_t)kDigits * nb; }
+size_t radix_hist_words(int nb) { return radix_hist_words_for(nb); }
 
 void radix_sort_pairs(RadixSortArgs a, cudaStream_t s)
 {
@@ -168,7 +196,12 @@ void radix_sort_pairs(RadixSortArgs a, cudaStream_t s)
     uint32_t* vout = a.vals_tmp;
     for (int shift = a.begin_bit; shift < a.end_bit; shift += 8) {
         k_hist<<<a.nb, kTile, 0, s>>>(kin, a.d_n, shift, a.hist, a.nb);
-        k_scan<<<1, 1024, 0, s>>>(a.hist, kDigits * a.nb);
+        {   // [digit][block] counts -> offsets (multi-block scan)
+            int* counts = reinterpret_cast<int*>(a.hist);
+            int* block_sums = counts + kDigits * a.nb;
+            int* total = block_sums + ((kDigits * a.nb + 1023) / 1024 + 1);
+            exclusive_scan_i32(counts, kDigits * a.nb, counts, block_sums, total, s);
+        }
         k_scatter<<<a.nb, kTile, 0, s>>>(kin, vin, kout, vout, a.d_n, shift, a.hist, a.nb);
         uint64_t* tk = kin;
         kin = kout;
@@ -189,9 +222,9 @@ void launch_iota(uint32_t* v, const unsigned long long* d_n, int grid, cudaStrea
 namespace {
 
 // Exclusive scan of n ints (three passes: per-block scans of 1024, one block
-// scanning the block totals, then the carries); *total gets the sum.
-__global__ void __launch_bounds__(1024) k_scan_blocks(const int* __restrict__ in, int n, int* __restrict__ out,
-                                                      int* __restrict__ block_sums)
+// scanning the block totals, then the carries); *total gets the sum.  In and
+// out may be the same array (each thread reads its element before writing).
+__global__ void __launch_bounds__(1024) k_scan_blocks(const int* in, int n, int* out, int* __restrict__ block_sums)
 {
     __shared__ int warp_incl[32];
     const int i = blockIdx.x * 1024 + threadIdx.x;

@@ -22,6 +22,12 @@ struct RadixSortArgs {
 };
 
 int radix_blocks_for(int64_t capacity, int num_sms);
+// Scratch of one sort: 256 digit counts per block plus the scan's block
+// totals and its total.
+constexpr size_t radix_hist_words_for(int nb)
+{
+    return (size_t)256 * nb + ((size_t)256 * nb + 1023) / 1024 + 2;
+}
 size_t radix_hist_words(int nb);
 void radix_sort_pairs(RadixSortArgs args, cudaStream_t stream);
 void launch_iota(uint32_t* v, const unsigned long long* d_n, int grid, cudaStream_t stream);

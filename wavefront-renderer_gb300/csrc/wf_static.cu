@@ -31,7 +31,7 @@ constexpr size_t kOffKeysTmp = align_up(kOffKeys + sizeof(uint64_t) * kMaxRays);
 constexpr size_t kOffVals = align_up(kOffKeysTmp + sizeof(uint64_t) * kMaxRays);
 constexpr size_t kOffValsTmp = align_up(kOffVals + sizeof(uint32_t) * kMaxRays);
 constexpr size_t kOffHist = align_up(kOffValsTmp + sizeof(uint32_t) * kMaxRays);
-constexpr size_t kOffCount = align_up(kOffHist + sizeof(uint32_t) * 256 * kMaxSortBlocks);
+constexpr size_t kOffCount = align_up(kOffHist + sizeof(uint32_t) * wf::radix_hist_words_for(kMaxSortBlocks));
 constexpr size_t kScratchBytes = align_up(kOffCount + sizeof(unsigned long long));
 
 // The scratch.  In host code this name is only a host-side stand-in for the
