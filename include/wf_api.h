@@ -299,7 +299,11 @@ typedef struct wf_tuning {
     int32_t speculative_traversal; /* 0 = while-while traversal (default);
                             1 = speculative while-while (lanes postpone their
                             first leaf until every lane of the warp has one) */
-    int32_t reserved[2];
+    int32_t l2_persist;  /* 1 = mark the scene's tree (nodes + triangles, one
+                            range) persisting in L2 for this context's stream,
+                            up to the device's set-aside; the context's
+                            persisting-lines limit is put back at wf_destroy */
+    int32_t reserved[1];
 } wf_tuning;
 int wf_set_tuning(wf_ctx* ctx, const wf_tuning* tuning);
 int wf_get_tuning(const wf_ctx* ctx, wf_tuning* out_tuning);

@@ -377,6 +377,36 @@ int schedule_columns(wf_ctx* c, int policy, const ull* d_n, int64_t n, ShadeColu
     return WF_OK;
 }
 
+void apply_l2_policy(wf_ctx* c, int scene)
+{
+    cudaStreamAttrValue attr{};
+    const ResidentScene* R = (scene >= 0 && scene < (int)c->scenes.size()) ? &c->scenes[scene] : nullptr;
+    const bool on = c->tuning.l2_persist && c->l2_persist_max > 0 && R && R->live && R->tree_base;
+    if (!on) {
+        if (c->l2_window_base) {
+            attr.accessPolicyWindow.base_ptr = nullptr;
+            attr.accessPolicyWindow.num_bytes = 0;
+            cudaStreamSetAttribute(c->stream, cudaStreamAttributeAccessPolicyWindow, &attr);
+            c->l2_window_base = nullptr;
+        }
+        return;
+    }
+    if (c->l2_window_base == R->tree_base) return;
+    if (!c->l2_limit_changed) {
+        cudaDeviceGetLimit(&c->l2_limit_before, cudaLimitPersistingL2CacheSize);
+        c->l2_limit_changed = true;
+    }
+    cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, c->l2_persist_max);
+    const size_t window = std::min(R->tree_bytes, c->l2_window_max);
+    attr.accessPolicyWindow.base_ptr = const_cast<void*>(R->tree_base);
+    attr.accessPolicyWindow.num_bytes = window;
+    attr.accessPolicyWindow.hitRatio = (float)std::min(1.0, (double)c->l2_persist_max / (double)std::max<size_t>(window, 1));
+    attr.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+    attr.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+    cudaStreamSetAttribute(c->stream, cudaStreamAttributeAccessPolicyWindow, &attr);
+    c->l2_window_base = R->tree_base;
+}
+
 int check_device_flag(wf_ctx* c)
 {
     int flag = 0;
@@ -579,9 +609,36 @@ int build_scene(wf_ctx* c, const wf_scene_desc* D, ResidentScene& R)
         auto b1 = std::chrono::steady_clock::now();
         cleanup_tmp();
         if (brc) return set_err(c, WF_ERR_CUDA, "BVH build failed: " + err);
-        A.push_back(bo.tris);
-        if (bo.nodes) A.push_back(bo.nodes);
-        if (bo.wnodes) A.push_back(bo.wnodes);
+        // Tree nodes and triangles in one allocation, nodes first: one
+        // address range the traversal reads, which an L2 persistence window
+        // can cover (wf_tuning::l2_persist).
+        {
+            const size_t node_bytes = (size_t)bo.num_nodes * (bo.wnodes ? sizeof(WideNode) : sizeof(BvhNode));
+            const size_t tri_bytes = 3 * sizeof(float4) * (size_t)ntri;
+            unsigned char* pool = nullptr;
+            if (cudaMalloc(&pool, node_bytes + tri_bytes) != cudaSuccess) {
+                cudaFree(bo.tris);
+                cudaFree(bo.nodes);
+                cudaFree(bo.wnodes);
+                free_scene_res(R);
+                return set_err(c, WF_ERR_OUT_OF_MEMORY, "BVH pool allocation failed");
+            }
+            const void* src_nodes = bo.wnodes ? (const void*)bo.wnodes : (const void*)bo.nodes;
+            cudaMemcpyAsync(pool, src_nodes, node_bytes, cudaMemcpyDeviceToDevice, s);
+            cudaMemcpyAsync(pool + node_bytes, bo.tris, tri_bytes, cudaMemcpyDeviceToDevice, s);
+            cudaStreamSynchronize(s);
+            cudaFree(bo.tris);
+            cudaFree(bo.nodes);
+            cudaFree(bo.wnodes);
+            bo.tris = reinterpret_cast<float4*>(pool + node_bytes);
+            if (bo.wnodes)
+                bo.wnodes = reinterpret_cast<WideNode*>(pool);
+            else
+                bo.nodes = reinterpret_cast<BvhNode*>(pool);
+            A.push_back(pool);
+            R.tree_base = pool;
+            R.tree_bytes = node_bytes + tri_bytes;
+        }
         R.info.bvh_build_ms = std::chrono::duration<double, std::milli>(b1 - b0).count();
         R.info.bvh_depth = bo.max_depth;
     }
@@ -764,6 +821,8 @@ int wf_create(const wf_config* cfg, wf_ctx** out)
     cudaDeviceProp prop;
     cudaGetDeviceProperties(&prop, c->device);
     c->num_sms = prop.multiProcessorCount;
+    c->l2_persist_max = (size_t)std::max(0, prop.persistingL2CacheMaxSize);
+    c->l2_window_max = (size_t)std::max(0, prop.accessPolicyMaxWindowSize);
     bool ok = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) == cudaSuccess;
     for (auto& e : c->ev) ok = ok && cudaEventCreate(&e) == cudaSuccess;
     for (auto& e : c->timer) ok = ok && cudaEventCreate(&e) == cudaSuccess;
@@ -789,6 +848,10 @@ int wf_destroy(wf_ctx* c)
     if (!c) return WF_OK;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->l2_limit_changed) {  // put the persisting-lines limit back as found
+        cudaCtxResetPersistingL2Cache();
+        cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, c->l2_limit_before);
+    }
     drop_graphs(c);
     for (auto& r : c->scenes) free_scene_res(r);
     free_all(c->render_allocs);

@@ -24,6 +24,8 @@ struct ResidentScene {
     std::vector<wf_material> mats;
     std::vector<int64_t> tex_bytes;
     int64_t* d_tex_bytes = nullptr;
+    const void* tree_base = nullptr;  // tree nodes followed by triangles
+    size_t tree_bytes = 0;
 };
 
 // A captured bounce chain (one wave, fixed depth), replayed for every wave.
@@ -117,6 +119,13 @@ struct wf_ctx {
     cudaEvent_t ev[8]{};
     cudaEvent_t timer[2]{};
     wf_tuning tuning{};
+
+    // L2 persistence (wf_tuning::l2_persist): the device's limits, and the
+    // persisting-lines limit this context found, restored at wf_destroy.
+    size_t l2_persist_max = 0, l2_window_max = 0;
+    bool l2_limit_changed = false;
+    size_t l2_limit_before = 0;
+    const void* l2_window_base = nullptr;
 };
 
 namespace wf {
@@ -134,6 +143,9 @@ int reset_cost_trackers(wf_ctx* c, int nmat, int ntex);
 int ensure_job_tables(wf_ctx* c, int jobs, int chunks);
 int sync_scene_table(wf_ctx* c);
 int check_device_flag(wf_ctx* c);
+// Points the context stream's L2 access-policy window at a scene's tree (or
+// clears it) according to wf_tuning::l2_persist.
+void apply_l2_policy(wf_ctx* c, int scene);
 void drop_graphs(wf_ctx* c);
 // Sorts n scheduling columns under a ShadingQueue policy; *perm_out gets the
 // permutation (device).  Materials and texture sizes of one scene.

@@ -411,6 +411,7 @@ int render_single(wf_ctx* c, const wf_render_params* P, wf_render_stats* st)
     rc = upload_jobs(c, table);
     if (rc) return rc;
     WF_CK(c, cudaMemsetAsync(c->arena, 0, sizeof(float) * 3 * (size_t)np, s));
+    apply_l2_policy(c, 0);
     const bool graph = !tracking && use_graph(c, false, P->policy);
     wf_render_stats stats{};
     stats.kernel_launches = kernels_setup;
