@@ -303,7 +303,10 @@ typedef struct wf_tuning {
                             range) persisting in L2 for this context's stream,
                             up to the device's set-aside; the context's
                             persisting-lines limit is put back at wf_destroy */
-    int32_t reserved[1];
+    int32_t ray_sort_bits; /* the render loop's ray sort uses the top bits of
+                            RayQueue::sortKey's 33 (0 = all 33; fewer bits =
+                            fewer 8-bit passes, coarser grouping); the host
+                            entry point always sorts by the full key */
 } wf_tuning;
 int wf_set_tuning(wf_ctx* ctx, const wf_tuning* tuning);
 int wf_get_tuning(const wf_ctx* ctx, wf_tuning* out_tuning);
@@ -316,7 +319,8 @@ int wf_get_tuning(const wf_ctx* ctx, wf_tuning* out_tuning);
  * once untimed and twice
  * timed on the device; then, when params sort rays or shading, the
  * sort-or-skip threshold sort_min_queue over {0, 2^18, 2^20, 2^22, never}
- * with the best launch settings.  Keeps the fastest on the context
+ * and, with the ray sort on, its key width ray_sort_bits over {24, 16}, with
+ * the best launch settings.  Keeps the fastest on the context
  * (bvh_builder is left as it is) and returns it with its time per wave.
  * Images and statistics of the trial renders are discarded. */
 int wf_autotune(wf_ctx* ctx, const wf_render_params* params, wf_tuning* out_tuning, double* out_wave_ms);

@@ -300,6 +300,7 @@ def test_render_is_order_independent(wf, ctx, scene_small, scene_c2small, which)
     try:
         for tune, kw in [(dict(trace_variant=1), {}), (dict(trace_variant=2), {}), (dict(trace_variant=3), {}),
                          (dict(speculative_traversal=1), {}), (dict(l2_persist=1), {}),
+                         (dict(ray_sort_bits=16), dict(ray_sort=True)),
                          (dict(persistent_blocks_per_sm=4), {}), (dict(graph_mode=1), {}),
                          (dict(sort_min_queue=6000), dict(policy=1, ray_sort=True))]:
             ctx.set_tuning(**tune)

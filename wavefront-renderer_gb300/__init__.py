@@ -123,7 +123,7 @@ class WfSceneInfo(C.Structure):
 class WfTuning(C.Structure):
     _fields_ = [("trace_variant", C.c_int32), ("persistent_blocks_per_sm", C.c_int32), ("graph_mode", C.c_int32),
                 ("bvh_builder", C.c_int32), ("sort_min_queue", C.c_int32), ("speculative_traversal", C.c_int32),
-                ("l2_persist", C.c_int32), ("reserved", C.c_int32 * 1)]
+                ("l2_persist", C.c_int32), ("ray_sort_bits", C.c_int32)]
 
 
 class WfJob(C.Structure):
@@ -579,9 +579,9 @@ class Context:
 
     def set_tuning(self, trace_variant: int = 0, persistent_blocks_per_sm: int = 0, graph_mode: int = 0,
                    bvh_builder: int = 0, sort_min_queue: int = 0, speculative_traversal: int = 0,
-                   l2_persist: int = 0) -> None:
+                   l2_persist: int = 0, ray_sort_bits: int = 0) -> None:
         t = WfTuning(trace_variant, persistent_blocks_per_sm, graph_mode, bvh_builder, sort_min_queue,
-                     speculative_traversal, l2_persist)
+                     speculative_traversal, l2_persist, ray_sort_bits)
         _check(load_library().wf_set_tuning(self._h, C.byref(t)), "wf_set_tuning", self)
 
     def autotune(self, params: WfRenderParams) -> tuple[dict, float]:
@@ -597,7 +597,8 @@ class Context:
         _check(load_library().wf_get_tuning(self._h, C.byref(t)), "wf_get_tuning", self)
         return {"trace_variant": t.trace_variant, "persistent_blocks_per_sm": t.persistent_blocks_per_sm,
                 "graph_mode": t.graph_mode, "bvh_builder": t.bvh_builder, "sort_min_queue": t.sort_min_queue,
-                "speculative_traversal": t.speculative_traversal, "l2_persist": t.l2_persist}
+                "speculative_traversal": t.speculative_traversal, "l2_persist": t.l2_persist,
+                "ray_sort_bits": t.ray_sort_bits}
 
     def add_scene(self, desc: WfSceneDesc) -> int:
         sid = C.c_int32()

@@ -334,7 +334,7 @@ int schedule_columns(wf_ctx* c, int policy, const ull* d_n, int64_t n, ShadeColu
         RadixSortArgs a{c->keys, c->vals, c->keys_tmp, c->vals_tmp, c->hist, d_n, c->nb, 0, 33 + bits,
                         &rk, &rv};
         radix_sort_pairs(a, s);
-        c->last_schedule_launches = 2 + 3 * ((33 + bits + 7) / 8);
+        c->last_schedule_launches = 2 + kSortKernelsPerPass * ((33 + bits + 7) / 8);
         *perm_out = rv;
         return WF_OK;
     }
@@ -372,7 +372,7 @@ int schedule_columns(wf_ctx* c, int policy, const ull* d_n, int64_t n, ShadeColu
     RadixSortArgs a{c->keys, c->vals, c->keys_tmp, c->vals_tmp, c->hist, d_n, c->nb, 0, bits + 3,
                     &rk, &rv};
     radix_sort_pairs(a, s);
-    c->last_schedule_launches = 2 + 3 * ((bits + 3 + 7) / 8);
+    c->last_schedule_launches = 2 + kSortKernelsPerPass * ((bits + 3 + 7) / 8);
     *perm_out = rv;
     return WF_OK;
 }

@@ -97,6 +97,16 @@ int upload_wave(wf_ctx* c, const std::vector<WaveChunk>& chunks, int64_t total)
     return WF_OK;
 }
 
+// The render loop's ray sort orders by the top wf_tuning::ray_sort_bits of
+// RayQueue::sortKey's 33 bits (octant, then Morton code of the origin): the
+// order only groups rays, so a coarser key sorts in fewer 8-bit passes.  The
+// host entry point wf_ray_schedule_host always sorts by the full key.
+int ray_key_begin(const wf_ctx* c)
+{
+    const int bits = c->tuning.ray_sort_bits > 0 ? std::min(33, c->tuning.ray_sort_bits) : 33;
+    return 33 - bits;
+}
+
 // Whether the resident scenes carry compressed 8-wide trees; a wave's
 // kernels use one traversal, so the formats must not be mixed.
 int table_wide(wf_ctx* c, bool& wide)
@@ -148,10 +158,11 @@ int wave_host(wf_ctx* c, int64_t total, int max_depth, int policy, bool ray_sort
             launch_ray_keys(c->d_scene_table, c->d_jobs, c->rq[cur], c->counters, c->keys, c->vals, WC, s);
             uint64_t* rk;
             uint32_t* rv;
-            RadixSortArgs a{c->keys, c->vals, c->keys_tmp, c->vals_tmp, c->hist, c->counters, c->nb, 0, 33, &rk, &rv};
+            RadixSortArgs a{c->keys, c->vals,    c->keys_tmp, c->vals_tmp, c->hist, c->counters,
+                            c->nb,   ray_key_begin(c), 33,          &rk,         &rv};
             radix_sort_pairs(a, s);
             launch_gather_rays(c->rq[cur], rv, c->counters, c->rq[1 - cur], WC, s);
-            stats.kernel_launches += 2 + 3 * 5;
+            stats.kernel_launches += 2 + kSortKernelsPerPass * ((33 - ray_key_begin(c) + 7) / 8);
             cur = 1 - cur;
             WF_CK(c, cudaEventRecord(ev[3], s));
             stats.sorted_elements += (uint64_t)count;
@@ -242,10 +253,11 @@ int record_chain(wf_ctx* c, int max_depth, bool ray_sort, bool wide)
             launch_ray_keys(c->d_scene_table, c->d_jobs, c->rq[cur], c->counters, c->keys, c->vals, WC, s);
             uint64_t* rk;
             uint32_t* rv;
-            RadixSortArgs a{c->keys, c->vals, c->keys_tmp, c->vals_tmp, c->hist, c->counters, c->nb, 0, 33, &rk, &rv};
+            RadixSortArgs a{c->keys, c->vals,    c->keys_tmp, c->vals_tmp, c->hist, c->counters,
+                            c->nb,   ray_key_begin(c), 33,          &rk,         &rv};
             radix_sort_pairs(a, s);
             launch_gather_rays(c->rq[cur], rv, c->counters, c->rq[1 - cur], WC, s);
-            kernels += 2 + 3 * 5;
+            kernels += 2 + kSortKernelsPerPass * ((33 - ray_key_begin(c) + 7) / 8);
             cur = 1 - cur;
         }
         cudaMemsetAsync(c->counters + 1, 0, sizeof(ull) * 5, s);
@@ -672,12 +684,15 @@ int wf_autotune(wf_ctx* c, const wf_render_params* P, wf_tuning* out, double* ou
                     best = t;
                 }
             }
-    if (P->policy != WF_POLICY_NONE || P->enable_ray_sort) {  // sort-or-skip threshold
+    if (P->policy != WF_POLICY_NONE || P->enable_ray_sort) {  // sort-or-skip threshold, ray key width
         const int thresholds[5] = {0, 1 << 18, 1 << 20, 1 << 22, INT32_MAX};
+        const int widths[3] = {33, 24, 16};
         const wf_tuning launch = best;
-        for (int th : thresholds) {
+        for (int trial_no = 0; trial_no < 5 + (P->enable_ray_sort ? 2 : 0); ++trial_no) {
             wf_tuning t = launch;
+            const int th = trial_no < 5 ? thresholds[trial_no] : 0;
             t.sort_min_queue = th;
+            t.ray_sort_bits = trial_no < 5 ? 33 : widths[trial_no - 4];
             c->tuning = t;
             double ms = 0.0;
             for (int rep = 0; rep < 3; ++rep) {
@@ -690,7 +705,7 @@ int wf_autotune(wf_ctx* c, const wf_render_params* P, wf_tuning* out, double* ou
                 if (rep > 0) ms += st.ms_total;
             }
             ms *= 0.5;
-            if (th == 0 || ms < best_ms) {  // the launch winner re-timed at 0 sets the bar
+            if (trial_no == 0 || ms < best_ms) {  // the launch winner re-timed at 0 sets the bar
                 best_ms = ms;
                 best = t;
             }

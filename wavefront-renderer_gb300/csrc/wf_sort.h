@@ -21,6 +21,9 @@ struct RadixSortArgs {
     uint32_t** result_vals;
 };
 
+// Kernels per 8-bit pass: digit counts, the three-kernel offset scan, scatter.
+constexpr int kSortKernelsPerPass = 5;
+
 int radix_blocks_for(int64_t capacity, int num_sms);
 // Scratch of one sort: 256 digit counts per block plus the scan's block
 // totals and its total.
