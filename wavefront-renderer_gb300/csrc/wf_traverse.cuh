@@ -135,7 +135,7 @@ struct Traversal {
                 slab2(nd, inv, oi, tmin, best_t, tn0, tn1, h0, h1);
                 const uint32_t c0 = (uint32_t)nd.kids.x, c1 = (uint32_t)nd.kids.y;
                 if (h0 && h1) {
-                    const bool swap = tn1 < tn0;
+                    const bool swap = child_order_swap(nd, tn0, tn1);
                     const uint32_t farc = swap ? c0 : c1;
                     cur = swap ? c1 : c0;
                     if (sp < kStackSize)
@@ -172,7 +172,7 @@ struct Traversal {
                 slab2(nd, inv, oi, tmin, best_t, tn0, tn1, h0, h1);
                 const uint32_t c0 = (uint32_t)nd.kids.x, c1 = (uint32_t)nd.kids.y;
                 if (h0 && h1) {
-                    const bool swap = tn1 < tn0;
+                    const bool swap = child_order_swap(nd, tn0, tn1);
                     const uint32_t farc = swap ? c0 : c1;
                     cur = swap ? c1 : c0;
                     if (sp < kStackSize)
@@ -203,6 +203,26 @@ struct Traversal {
                 return;
             }
         }
+    }
+
+    // Which hit child to visit first: the nearer one (closest hit, and any
+    // hit by default); WF_ANYHIT_ORDER selects other orders for shadow rays
+    // (1 = the first child, 2 = the child with the larger box).
+    __device__ __forceinline__ static bool child_order_swap(const BvhNode& nd, float tn0, float tn1)
+    {
+#if defined(WF_ANYHIT_ORDER) && WF_ANYHIT_ORDER == 1
+        if (kAnyHit) return false;
+#elif defined(WF_ANYHIT_ORDER) && WF_ANYHIT_ORDER == 2
+        if (kAnyHit) {
+            const float a0 = (nd.c0xy.y - nd.c0xy.x) * (nd.c0xy.w - nd.c0xy.z) +
+                             (nd.c0xy.w - nd.c0xy.z) * (nd.cz.y - nd.cz.x) + (nd.cz.y - nd.cz.x) * (nd.c0xy.y - nd.c0xy.x);
+            const float a1 = (nd.c1xy.y - nd.c1xy.x) * (nd.c1xy.w - nd.c1xy.z) +
+                             (nd.c1xy.w - nd.c1xy.z) * (nd.cz.w - nd.cz.z) + (nd.cz.w - nd.cz.z) * (nd.c1xy.y - nd.c1xy.x);
+            return a1 > a0;
+        }
+#endif
+        (void)nd;
+        return tn1 < tn0;
     }
 
     // The triangles of one leaf; true when an any-hit query may stop.
