@@ -402,7 +402,10 @@ __global__ void k_cost_update(CostTrackerDev mat, CostTrackerDev tex, int repeat
 // sample) — the oracle uses the same ones.
 // ---------------------------------------------------------------------------
 template <bool kMulti>
-__global__ void __launch_bounds__(128) k_shade(DeviceScene scene0, DeviceJob job0,
+#ifndef WF_SHADE_MIN_BLOCKS
+#define WF_SHADE_MIN_BLOCKS 6  // 80 registers, 6 resident blocks (91 / 5 unbounded): +2%
+#endif
+__global__ void __launch_bounds__(128, WF_SHADE_MIN_BLOCKS) k_shade(DeviceScene scene0, DeviceJob job0,
                                                const DeviceScene* __restrict__ scenes,
                                                const DeviceJob* __restrict__ jobs, RayQueueDev rq,
                                                HitQueueDev hq, const ull* __restrict__ hq_n,
