@@ -528,7 +528,7 @@ int wf_render_batch(wf_ctx* ctx, const wf_job* jobs, int32_t njobs, float* const
 typedef struct wf_server wf_server;
 typedef struct wf_server_config {
     int64_t hbm_budget_bytes;   /* accumulators + wave buffers              */
-    int64_t max_paths_per_wave; /* 0 = context default                      */
+    int64_t max_paths_per_wave; /* 0 = 2^23 (or the context's, if smaller)  */
     int32_t frame_spp;          /* samples per progressive frame (8)        */
     int32_t reserved[7];
 } wf_server_config;

@@ -569,6 +569,7 @@ namespace {
 // Bytes of the wave buffers per path in flight: two RayQueues (14 columns),
 // two hit queues (5), the shadow queue (2 x 12), sort keys and values (2 x 12)
 // and the policy columns (8).
+constexpr int64_t kServerPathsPerWave = int64_t(1) << 23;
 constexpr int64_t kBytesPerPath = 2 * 14 * 4 + 2 * 5 * 4 + 3 * 12 * 4 + 2 * 12 + 8 * 4;
 
 int finish_job(wf_server* sv, int64_t id, ServedJob& j)
@@ -895,7 +896,12 @@ int wf_server_create(wf_ctx* c, const wf_server_config* cfg, wf_server** out)
     sv->c = c;
     sv->cfg = *cfg;
     if (sv->cfg.frame_spp <= 0) sv->cfg.frame_spp = 8;
-    sv->wave_paths = cfg->max_paths_per_wave > 0 ? cfg->max_paths_per_wave : c->paths_per_wave;
+    // A served wave is a latency unit: every admitted job advances by one
+    // frame's worth of samples per step, so the default stays at 2^23 paths
+    // (a single render's waves default to 2^26, which trades latency for
+    // throughput).
+    sv->wave_paths = cfg->max_paths_per_wave > 0 ? cfg->max_paths_per_wave
+                                                 : std::min<int64_t>(c->paths_per_wave, kServerPathsPerWave);
     sv->wave_bytes = sv->wave_paths * kBytesPerPath;
     const int64_t accum_bytes = cfg->hbm_budget_bytes - sv->wave_bytes;
     if (accum_bytes <= 0) {
