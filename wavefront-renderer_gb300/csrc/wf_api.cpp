@@ -614,7 +614,7 @@ int build_scene(wf_ctx* c, const wf_scene_desc* D, ResidentScene& R)
         // can cover (wf_tuning::l2_persist).
         {
             const size_t node_bytes = (size_t)bo.num_nodes * (bo.wnodes ? sizeof(WideNode) : sizeof(BvhNode));
-            const size_t tri_bytes = tri_block_bytes(ntri);
+            const size_t tri_bytes = 3 * sizeof(float4) * (size_t)ntri;
             unsigned char* pool = nullptr;
             if (cudaMalloc(&pool, node_bytes + tri_bytes) != cudaSuccess) {
                 cudaFree(bo.tris);
@@ -643,12 +643,6 @@ int build_scene(wf_ctx* c, const wf_scene_desc* D, ResidentScene& R)
         R.info.bvh_depth = bo.max_depth;
     }
     S.tris = bo.tris;
-    S.tri_e2z = bo.tris ? reinterpret_cast<const float*>(reinterpret_cast<const unsigned char*>(bo.tris) +
-                                                         tri_e2z_offset(ntri))
-                        : nullptr;
-    S.tri_ids = bo.tris ? reinterpret_cast<const int4*>(reinterpret_cast<const unsigned char*>(bo.tris) +
-                                                        tri_ids_offset(ntri))
-                        : nullptr;
     S.nodes = bo.nodes;
     S.wnodes = bo.wnodes;
     S.num_tris = ntri;
@@ -791,7 +785,7 @@ int build_scene(wf_ctx* c, const wf_scene_desc* D, ResidentScene& R)
     I.num_meshes = D->num_meshes;
     I.num_emissive_meshes = (int32_t)em.size();
     I.bvh_nodes = bo.num_nodes;
-    int64_t bytes = (int64_t)tri_block_bytes(ntri) +
+    int64_t bytes = (int64_t)ntri * 48 +
                     (int64_t)bo.num_nodes * (int64_t)(bo.wnodes ? sizeof(WideNode) : sizeof(BvhNode)) +
                     (int64_t)pool_f.size() * 4 + (int64_t)pool_b.size() * 4;
     I.device_bytes = bytes;

@@ -217,27 +217,18 @@ __global__ void k_emit_single(const float* __restrict__ leaf_box, BvhNode* nodes
     nodes[0] = nd;
 }
 
-// The triangle block (wf_device.cuh, tri_*_offset) in leaf order:
-// e1 = v1 - v0 and e2 = v2 - v0 are the float subtractions the reference's
-// intersectTriangle does, so storing them changes no bit.
 __global__ void k_emit_tris(const float* __restrict__ px, const float* __restrict__ py,
                             const float* __restrict__ pz, const int32_t* __restrict__ idx,
                             const int32_t* __restrict__ tri_geom, const int32_t* __restrict__ tri_prim,
-                            const uint32_t* __restrict__ sorted, int n, float4* __restrict__ block)
+                            const uint32_t* __restrict__ sorted, int n, float4* __restrict__ tris)
 {
-    float4* geo = block;
-    float* e2z = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(block) + tri_e2z_offset(n));
-    int4* ids = reinterpret_cast<int4*>(reinterpret_cast<unsigned char*>(block) + tri_ids_offset(n));
     for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
         int t = (int)sorted[j];
         int a = idx[3 * t], b = idx[3 * t + 1], c = idx[3 * t + 2];
         float x0 = px[a], y0 = py[a], z0 = pz[a];
-        const float e1x = px[b] - x0, e1y = py[b] - y0, e1z = pz[b] - z0;
-        const float e2x = px[c] - x0, e2y = py[c] - y0;
-        geo[2 * (int64_t)j + 0] = make_float4(x0, y0, z0, e1x);
-        geo[2 * (int64_t)j + 1] = make_float4(e1y, e1z, e2x, e2y);
-        e2z[j] = pz[c] - z0;
-        ids[j] = make_int4(t, tri_geom[t], tri_prim[t], 0);
+        tris[3 * (int64_t)j + 0] = make_float4(x0, y0, z0, __int_as_float(t));
+        tris[3 * (int64_t)j + 1] = make_float4(px[b] - x0, py[b] - y0, pz[b] - z0, __int_as_float(tri_geom[t]));
+        tris[3 * (int64_t)j + 2] = make_float4(px[c] - x0, py[c] - y0, pz[c] - z0, __int_as_float(tri_prim[t]));
     }
 }
 
@@ -749,7 +740,7 @@ int build_lbvh(const BvhBuildInput& in, BvhBuildOutput& out, int num_sms, cudaSt
     WF_TRY(cudaMalloc(&flags, sizeof(int) * (size_t)nint));
     WF_TRY(cudaMalloc(&d_depth, sizeof(int)));
     WF_TRY(cudaMalloc(&d_n, sizeof(unsigned long long)));
-    WF_TRY(cudaMalloc((void**)&out.tris, tri_block_bytes(n)));
+    WF_TRY(cudaMalloc(&out.tris, 3 * sizeof(float4) * (size_t)n));
     WF_TRY(cudaMalloc(&out.nodes, sizeof(BvhNode) * (size_t)nint));
     WF_TRY(cudaMemsetAsync(flags, 0, sizeof(int) * (size_t)nint, s));
     WF_TRY(cudaMemsetAsync(d_depth, 0, sizeof(int), s));
@@ -988,7 +979,7 @@ int build_ploc(const BvhBuildInput& in, BvhBuildOutput& out, int num_sms, cudaSt
         out.num_nodes = kept;
         WF_TRY(cudaMemcpyAsync(&h_depth, d_depth, sizeof(int), cudaMemcpyDeviceToHost, s));
     }
-    WF_TRY(cudaMalloc((void**)&out.tris, tri_block_bytes(n)));
+    WF_TRY(cudaMalloc(&out.tris, 3 * sizeof(float4) * (size_t)n));
     k_emit_tris<<<grid, 256, 0, s>>>(in.px, in.py, in.pz, in.idx, in.tri_geom, in.tri_prim, T.final_ids, n,
                                      out.tris);
     WF_TRY(cudaGetLastError());
@@ -1076,7 +1067,7 @@ int build_ploc_wide(const BvhBuildInput& in, BvhBuildOutput& out, int num_sms, c
         err = "wide BVH lost triangles";
         goto fail;
     }
-    WF_TRY(cudaMalloc((void**)&out.tris, tri_block_bytes(n)));
+    WF_TRY(cudaMalloc(&out.tris, 3 * sizeof(float4) * (size_t)n));
     k_emit_tris<<<grid, 256, 0, s>>>(in.px, in.py, in.pz, in.idx, in.tri_geom, in.tri_prim, wide_ids, n, out.tris);
     WF_TRY(cudaGetLastError());
     WF_TRY(cudaStreamSynchronize(s));

@@ -78,20 +78,12 @@ static_assert(sizeof(WideNode) == 80, "WideNode is five 16-byte words");
 constexpr int kWideLeafMax = 3;   // triangles per leaf child
 constexpr int kWideStack = 32;    // node-group stack entries (checked at build)
 
-// Triangles in BVH leaf order, one block per scene:
-//   geo[2n] float4: (v0.x, v0.y, v0.z, e1.x), (e1.y, e1.z, e2.x, e2.y)
-//   e2z[n]  float:  e2.z
-//   ids[n]  int4:   (global triangle index, geomID, primID, 0)
-// with e1 = v1 - v0, e2 = v2 - v0.  A triangle test reads 36 bytes; the ids
-// are read only for an accepted hit.
-__host__ __device__ constexpr size_t tri_e2z_offset(int64_t n) { return (size_t)32 * (size_t)n; }
-__host__ __device__ constexpr size_t tri_ids_offset(int64_t n) { return ((size_t)36 * (size_t)n + 255) / 256 * 256; }
-__host__ __device__ constexpr size_t tri_block_bytes(int64_t n) { return tri_ids_offset(n) + (size_t)16 * (size_t)n; }
-
 struct DeviceScene {
-    const float4* tris;        // triangle block (geo first), see above
-    const float* tri_e2z;
-    const int4* tri_ids;
+    // Triangles in BVH leaf order: 3 float4 each.
+    //   [0] = v0.xyz, w = global triangle index (bits)
+    //   [1] = (v1 - v0).xyz, w = geomID (mesh index)
+    //   [2] = (v2 - v0).xyz, w = primID (index within the mesh)
+    const float4* tris;
     const BvhNode* nodes;      // binary tree, or null when wnodes is set
     const WideNode* wnodes;    // compressed 8-wide tree, or null
     int32_t num_tris;
@@ -369,25 +361,15 @@ struct HitRec {
     bool front;
 };
 
-// v0, e1 = v1 - v0, e2 = v2 - v0 of a leaf-order triangle.
-struct TriGeo {
-    V3 v0, e1, e2;
-};
-__device__ __forceinline__ TriGeo load_tri(const float4* __restrict__ geo, const float* __restrict__ e2z, int lp)
-{
-    const float4 a = __ldg(geo + 2 * (int64_t)lp), b = __ldg(geo + 2 * (int64_t)lp + 1);
-    const float z = __ldg(e2z + lp);
-    return {v3(a.x, a.y, a.z), v3(a.w, b.x, b.y), v3(b.z, b.w, z)};
-}
-
 __device__ __forceinline__ void rebuild_hit(const DeviceScene& S, V3 o, V3 d, int leafpos,
                                             float t, float bu, float bv, HitRec& h)
 {
-    const TriGeo tg = load_tri(S.tris, S.tri_e2z, leafpos);
-    const int4 ids = __ldg(S.tri_ids + leafpos);
-    h.global_tri = ids.x;
-    h.geom = ids.y;
-    h.prim = ids.z;
+    float4 a = __ldg(S.tris + 3 * leafpos + 0);
+    float4 b = __ldg(S.tris + 3 * leafpos + 1);
+    float4 c = __ldg(S.tris + 3 * leafpos + 2);
+    h.global_tri = __float_as_int(a.w);
+    h.geom = __float_as_int(b.w);
+    h.prim = __float_as_int(c.w);
     h.t = t;
     h.p = o + d * t;  // Ray::at
     h.mat = __ldg(S.mesh_material + h.geom);
@@ -404,7 +386,7 @@ __device__ __forceinline__ void rebuild_hit(const DeviceScene& S, V3 o, V3 d, in
         h.u = bu;
         h.v = bv;
     }
-    V3 outward = normalized(cross(tg.e1, tg.e2));
+    V3 outward = normalized(cross(v3(b.x, b.y, b.z), v3(c.x, c.y, c.z)));
     h.front = dot(d, outward) < 0.0f;  // HitRecord::setFaceNormal
     h.n = h.front ? outward : outward * -1.0f;
 }

@@ -1017,7 +1017,8 @@ __global__ void k_hit_columns(const DeviceScene* __restrict__ scenes, const Devi
          k += (int64_t)gridDim.x * blockDim.x) {
         const int ri = hq.ray[k];
         const DeviceScene& S = scenes[jobs[rq.job[ri]].scene];
-        const int m = S.mesh_material[__ldg(&S.tri_ids[hq.tri[k]].y)];
+        const float4 b = __ldg(S.tris + 3 * (int64_t)hq.tri[k] + 1);
+        const int m = S.mesh_material[__float_as_int(b.w)];
         out.mat[k] = m;
         out.tex[k] = S.materials[m].texture_id;
         out.tr[k] = rq.tr[ri];

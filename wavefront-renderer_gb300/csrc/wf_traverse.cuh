@@ -105,7 +105,7 @@ struct Traversal {
     template <class Stk>
     __device__ __forceinline__ void round(const DeviceScene& S, Stk stack)
     {
-        round(S.nodes, S.tris, S.tri_e2z, S.tri_ids, stack);
+        round(S.nodes, S.tris, stack);
     }
 
     // With the top of the tree staged in shared memory: nodes [0, ntop)
@@ -115,14 +115,14 @@ struct Traversal {
     {
         top_nodes = top;
         num_top = ntop;
-        round(S.nodes, S.tris, S.tri_e2z, S.tri_ids, stack);
+        round(S.nodes, S.tris, stack);
     }
 
     // nodes / tris of the ray's scene: from the kernel's parameter bank when
     // every ray shares one scene, else from the scene table.
     template <class Stk>
     __device__ __forceinline__ void round(const BvhNode* __restrict__ nodes, const float4* __restrict__ tris,
-                                          const float* __restrict__ e2z, const int4* __restrict__ ids, Stk stack)
+                                          Stk stack)
     {
         if (!speculative) {
             // While-while: walk interior nodes down to a leaf, then test
@@ -151,7 +151,7 @@ struct Traversal {
             while (cur != kSentinel && (cur & kLeafFlag)) {
                 const uint32_t leaf = cur;
                 cur = stack[--sp];
-                if (test_leaf(tris, e2z, ids, leaf)) {
+                if (test_leaf(tris, leaf)) {
                     cur = kSentinel;
                     return;
                 }
@@ -191,14 +191,14 @@ struct Traversal {
             }
             if (!__any_sync(active, postponed == 0u && cur != kSentinel)) break;
         }
-        if (postponed != 0u && test_leaf(tris, e2z, ids, postponed)) {
+        if (postponed != 0u && test_leaf(tris, postponed)) {
             cur = kSentinel;  // any hit: done
             return;
         }
         while (cur != kSentinel && (cur & kLeafFlag)) {
             const uint32_t leaf = cur;
             cur = stack[--sp];
-            if (test_leaf(tris, e2z, ids, leaf)) {
+            if (test_leaf(tris, leaf)) {
                 cur = kSentinel;
                 return;
             }
@@ -225,34 +225,28 @@ struct Traversal {
         return tn1 < tn0;
     }
 
-    // The triangles of one leaf; true when an any-hit query may stop.  The
-    // global index (for ties at equal t) is read only for accepted hits.
-    __device__ __forceinline__ bool test_leaf(const float4* __restrict__ tris, const float* __restrict__ e2z,
-                                              const int4* __restrict__ ids, uint32_t leaf)
+    // The triangles of one leaf; true when an any-hit query may stop.
+    __device__ __forceinline__ bool test_leaf(const float4* __restrict__ tris, uint32_t leaf)
     {
         const int first = (int)((leaf & ~kLeafFlag) >> 3);
         const int cnt = (int)(leaf & 7u) + 1;
         for (int k = 0; k < cnt; ++k) {
             const int lp = first + k;
-            const TriGeo tg = load_tri(tris, e2z, lp);
+            const float4 a = __ldg(tris + 3 * lp + 0);
+            const float4 b = __ldg(tris + 3 * lp + 1);
+            const float4 c = __ldg(tris + 3 * lp + 2);
             float th, uh, vh;
-            if (intersect_triangle(o, d, tg.v0, tg.e1, tg.e2, tmin, best_t, th, uh, vh)) {
-                if (kAnyHit) {
-                    res.leafpos = lp;
-                    res.t = th;
-                    res.bu = uh;
-                    res.bv = vh;
-                    return true;
-                }
-                const bool closer = th < best_t || res.leafpos < 0;
-                const int g = __ldg(&ids[lp].x);
-                if (closer || g > best_g) {
+            if (intersect_triangle(o, d, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), v3(c.x, c.y, c.z), tmin, best_t, th,
+                                   uh, vh)) {
+                const int g = __float_as_int(a.w);
+                if (kAnyHit || th < best_t || res.leafpos < 0 || g > best_g) {
                     res.leafpos = lp;
                     res.t = th;
                     res.bu = uh;
                     res.bv = vh;
                     best_t = th;
                     best_g = g;
+                    if (kAnyHit) return true;
                 }
             }
         }
@@ -329,10 +323,13 @@ struct WideTraversal {
         while (tri_hits) {
             const int lp = (int)tri_base + __ffs(tri_hits) - 1;
             tri_hits &= tri_hits - 1u;
-            const TriGeo tg = load_tri(S.tris, S.tri_e2z, lp);
+            const float4 a = __ldg(S.tris + 3 * lp + 0);
+            const float4 bq = __ldg(S.tris + 3 * lp + 1);
+            const float4 c = __ldg(S.tris + 3 * lp + 2);
             float th, uh, vh;
-            if (intersect_triangle(o, d, tg.v0, tg.e1, tg.e2, tmin, best_t, th, uh, vh)) {
-                const int g = kAnyHit ? 0 : __ldg(&S.tri_ids[lp].x);
+            if (intersect_triangle(o, d, v3(a.x, a.y, a.z), v3(bq.x, bq.y, bq.z), v3(c.x, c.y, c.z), tmin, best_t,
+                                   th, uh, vh)) {
+                const int g = __float_as_int(a.w);
                 if (kAnyHit || th < best_t || res.leafpos < 0 || g > best_g) {
                     res.leafpos = lp;
                     res.t = th;
