@@ -388,7 +388,7 @@ def main() -> int:
     ap.add_argument("--blocks-per-sm", type=int, default=0)
     ap.add_argument("--ref-rows", type=int, default=256)
     ap.add_argument("--ref-spp", type=int, default=16)
-    ap.add_argument("--bvh", default="ploc", choices=["ploc", "lbvh", "wide"])
+    ap.add_argument("--bvh", default="ploc", choices=["ploc", "lbvh", "wide", "ploc4"])
     ap.add_argument("--autotune", type=int, default=0, help="run wf_autotune on the workload before timing")
     ap.add_argument("--speculative", type=int, default=0, help="1 = speculative while-while traversal")
     ap.add_argument("--adaptive", type=int, default=0, help="the reference's adaptive sampling (threshold 0.05)")
@@ -413,7 +413,7 @@ def main() -> int:
     ctx = pkg.Context(local)
     scene = pkg.HostScene(wl["config"])
     ctx.set_tuning(max(args.trace_variant, 0), args.blocks_per_sm,
-                   bvh_builder={"ploc": 0, "lbvh": 1, "wide": 2}[args.bvh],
+                   bvh_builder={"ploc": 0, "lbvh": 1, "wide": 2, "ploc4": 3}[args.bvh],
                    speculative_traversal=args.speculative, l2_persist=args.l2_persist,
                    ray_sort_bits=args.ray_sort_bits)
     info = ctx.upload(scene.desc)
@@ -472,11 +472,12 @@ def main() -> int:
     achieved = alg_bytes / (trace_ms / 1e3) / 1e9
     peak, peak_kind = measured_peaks()
     # DRAM bytes per closest-hit ray of k_trace_render, measured by ncu over
-    # every launch of a smaller render of the same scene (profiles/); scaled to
-    # this run's average launch by its rays.
+    # every launch of a smaller render of the same scene (profiles/) with the
+    # default tree (binary PLOC); scaled to this run's average launch by its
+    # rays.  Other trees have no measured figure.
     traffic = None
     tp = ROOT / "profiles" / "traffic.json"
-    if tp.exists():
+    if tp.exists() and info.bvh_builder == 0:
         try:
             per_ray = json.loads(tp.read_text())[f"config{wl['config']}"]["dram_bytes_per_closest_ray"]
             traffic = per_ray * closest / max(launches, 1)
@@ -507,7 +508,7 @@ def main() -> int:
         "clocks": clocks,
         "gpu_launches": int(sum(s["kernel_launches"] for s in stats)),
         "bvh_build_ms": info.bvh_build_ms,
-        "bvh": {"builder": ["ploc", "lbvh", "ploc_wide8"][info.bvh_builder], "nodes": info.bvh_nodes,
+        "bvh": {"builder": ["ploc", "lbvh", "ploc_wide8", "ploc4"][info.bvh_builder], "nodes": info.bvh_nodes,
                 "depth": info.bvh_depth},
         "tuning": dict(ctx.get_tuning(), autotuned=bool(args.autotune), autotune_wave_ms=tune_ms),
     }

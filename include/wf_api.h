@@ -288,9 +288,11 @@ typedef struct wf_tuning {
     int32_t bvh_builder; /* scenes uploaded afterwards: 0 = PLOC binary tree
                             (locally-ordered clustering, default), 1 = LBVH
                             binary tree (Karras radix tree), 2 = the PLOC tree
-                            collapsed into compressed 8-wide nodes; a PLOC
-                            tree deeper than its traversal stack falls back
-                            to LBVH */
+                            collapsed into compressed 8-wide nodes, 3 = the
+                            PLOC tree collapsed into 4-wide nodes (full-
+                            precision boxes, 128 bytes each); a PLOC tree
+                            deeper than its traversal stack falls back to
+                            LBVH */
     int32_t sort_min_queue; /* sort-or-skip: the ray sort and the shading
                             policies run on a bounce only when its queue holds
                             at least this many entries (0 = always, as the

@@ -311,6 +311,32 @@ def test_render_is_order_independent(wf, ctx, scene_small, scene_c2small, which)
         ctx.set_tuning()
 
 
+@pytest.mark.parametrize("builder", [2, 3])
+def test_tree_formats_render_the_same_image(wf, ctx, scene_c2small, builder):
+    """The 8-wide and 4-wide trees return the binary tree's hits, so a render
+    over them (plain launches, graph replay, every launch variant) gives the
+    binary tree's image up to float-add order (1e-4 relative, 99.9% of
+    pixels).  A context of its own: the resident scenes of one context share
+    one tree format."""
+    W = H = 48
+    cam = scene_c2small.camera(W, H)
+    ctx.upload(scene_c2small.desc)
+    base, st0 = ctx.render(wf.render_params(W, H, 8, 8, cam, seed=13))
+    other = wf.Context(0)
+    try:
+        other.set_tuning(bvh_builder=builder)
+        info = other.upload(scene_c2small.desc)
+        assert info.bvh_builder == builder
+        for tune in [{}, dict(graph_mode=1), dict(trace_variant=1), dict(trace_variant=2), dict(trace_variant=3)]:
+            other.set_tuning(bvh_builder=builder, **tune)
+            img, st = other.render(wf.render_params(W, H, 8, 8, cam, seed=13))
+            agree = np.isclose(img, base, rtol=1e-4, atol=1e-6).all(axis=2).mean()
+            assert agree >= 0.999, (tune, agree)
+            assert st["closest_rays"] == st0["closest_rays"], tune
+    finally:
+        other.close()
+
+
 def test_autotune_picks_a_valid_tuning(wf, ctx, scene_small):
     ctx.upload(scene_small.desc)
     cam = scene_small.camera(64, 64)
@@ -542,9 +568,9 @@ def test_gpu_live_costs_only_reorder_shading(wf, ctx, scene_c2small, policy):
 
 @pytest.mark.parametrize("which", ["c0", "small", "c2small"])
 def test_bvh_builders_give_identical_hits(wf, orc, ctx, scene0, scene_small, scene_c2small, which):
-    """The binary PLOC tree, the LBVH and the compressed 8-wide PLOC tree
-    return the same closest hits and occlusion bit for bit (and the port's),
-    and each passes the build's structural check."""
+    """The binary PLOC tree, the LBVH, the compressed 8-wide and the 4-wide
+    PLOC trees return the same closest hits and occlusion bit for bit (and the
+    port's), and each passes the build's structural check."""
     scene = {"c0": scene0, "small": scene_small, "c2small": scene_c2small}[which]
     rng = np.random.default_rng(21)
     lo, hi = ([0.0, 0.01, 0.0], [16.0, 0.9, 16.0]) if which == "c2small" else \
@@ -556,7 +582,7 @@ def test_bvh_builders_give_identical_hits(wf, orc, ctx, scene0, scene_small, sce
     want_occ = port.trace_occluded(o, d, maxd)
     infos = []
     try:
-        for builder in (0, 1, 2):
+        for builder in (0, 1, 2, 3):
             ctx.set_tuning(bvh_builder=builder)
             infos.append(ctx.upload(scene.desc))
             got = ctx.trace_closest(o, d)
@@ -565,8 +591,49 @@ def test_bvh_builders_give_identical_hits(wf, orc, ctx, scene0, scene_small, sce
             assert np.array_equal(ctx.trace_occluded(o, d, maxd), want_occ), builder
     finally:
         ctx.set_tuning()
-    assert [i.bvh_builder for i in infos] == [0, 1, 2]
+    assert [i.bvh_builder for i in infos] == [0, 1, 2, 3]
     assert infos[2].bvh_nodes < infos[0].bvh_nodes  # the 8-wide tree has fewer nodes
+    assert infos[3].bvh_nodes < infos[0].bvh_nodes  # so has the 4-wide one
+    assert infos[3].bvh_depth < infos[0].bvh_depth
+
+
+@pytest.mark.parametrize("ntri", [1, 2, 4, 5, 9, 33])
+def test_bvh_builders_on_tiny_scenes(wf, orc, ntri):
+    """Trees of a few triangles — the whole tree one leaf (<= 4 triangles),
+    the first split, a couple of levels — give the port's hits and occlusion
+    under every builder.  A context of its own per format."""
+    rng = np.random.default_rng(100 + ntri)
+    c = rng.uniform(-0.5, 0.5, size=(ntri, 1, 3))
+    v = (c + rng.uniform(-0.3, 0.3, size=(ntri, 3, 3))).reshape(-1, 3).astype(np.float32)
+    idx = np.arange(3 * ntri, dtype=np.int32)
+    mats = [wf.WfMaterial(type=0, albedo=(0.5, 0.5, 0.5), texture_id=-1)]
+    desc, keep = _desc(wf, [(v[:, 0].copy(), v[:, 1].copy(), v[:, 2].copy(), idx, 0)], mats)
+    # rays aimed at points on random triangles (a quarter at random points)
+    n = 4000
+    o = rng.uniform(-1.5, 1.5, size=(n, 3)).astype(np.float32)
+    tv = v.reshape(ntri, 3, 3)[rng.integers(0, ntri, n)]
+    b = rng.dirichlet([1.0, 1.0, 1.0], n)[:, :, None]
+    target = (tv * b).sum(axis=1)
+    target[: n // 4] = rng.uniform(-0.8, 0.8, size=(n // 4, 3))
+    d = (target - o).astype(np.float32)
+    d[:100, 1] = 0.0  # axis-parallel components
+    maxd = rng.uniform(0.01, 4.0, n).astype(np.float32)
+    port = orc.Port(desc)
+    want = port.trace_closest(o, d)
+    want_occ = port.trace_occluded(o, d, maxd)
+    assert (want["prim_id"] >= 0).mean() > 0.3
+    for builder in (0, 1, 2, 3):
+        c2 = wf.Context(0)
+        try:
+            c2.set_tuning(bvh_builder=builder)
+            info = c2.upload(desc)
+            assert info.bvh_builder == builder
+            got = c2.trace_closest(o, d)
+            for k in HIT_KEYS_EXACT:
+                assert np.array_equal(got[k], want[k]), (builder, k)
+            assert np.array_equal(c2.trace_occluded(o, d, maxd), want_occ), builder
+        finally:
+            c2.close()
 
 
 def test_scene_file_renders_like_the_original(wf, ctx, scene_c2small, tmp_path):

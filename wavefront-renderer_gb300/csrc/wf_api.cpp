@@ -425,6 +425,12 @@ int check_device_flag(wf_ctx* c)
 
 namespace {
 
+// Bytes per node of a built tree's format.
+size_t tree_node_bytes(const BvhBuildOutput& b)
+{
+    return b.wnodes ? sizeof(WideNode) : (b.nodes4 ? sizeof(Bvh4Node) : sizeof(BvhNode));
+}
+
 // srgbToLinear, reference src/shading/Texture.cpp:20-27.
 float srgb_to_linear(float s)
 {
@@ -601,6 +607,9 @@ int build_scene(wf_ctx* c, const wf_scene_desc* D, ResidentScene& R)
         } else if (c->tuning.bvh_builder == 2) {
             brc = build_ploc_wide(bi, bo, c->num_sms, s, err);
             R.info.bvh_builder = 2;
+        } else if (c->tuning.bvh_builder == 3) {
+            brc = build_ploc4(bi, bo, c->num_sms, s, err);
+            R.info.bvh_builder = 3;
         }
         if (brc) {  // LBVH on request, or when a PLOC tree is too deep for its stack
             brc = build_lbvh(bi, bo, c->num_sms, s, err);
@@ -613,26 +622,32 @@ int build_scene(wf_ctx* c, const wf_scene_desc* D, ResidentScene& R)
         // address range the traversal reads, which an L2 persistence window
         // can cover (wf_tuning::l2_persist).
         {
-            const size_t node_bytes = (size_t)bo.num_nodes * (bo.wnodes ? sizeof(WideNode) : sizeof(BvhNode));
+            const size_t node_bytes = (size_t)bo.num_nodes * tree_node_bytes(bo);
             const size_t tri_bytes = 3 * sizeof(float4) * (size_t)ntri;
             unsigned char* pool = nullptr;
             if (cudaMalloc(&pool, node_bytes + tri_bytes) != cudaSuccess) {
                 cudaFree(bo.tris);
                 cudaFree(bo.nodes);
                 cudaFree(bo.wnodes);
+                cudaFree(bo.nodes4);
                 free_scene_res(R);
                 return set_err(c, WF_ERR_OUT_OF_MEMORY, "BVH pool allocation failed");
             }
-            const void* src_nodes = bo.wnodes ? (const void*)bo.wnodes : (const void*)bo.nodes;
+            const void* src_nodes = bo.wnodes   ? (const void*)bo.wnodes
+                                    : bo.nodes4 ? (const void*)bo.nodes4
+                                                : (const void*)bo.nodes;
             cudaMemcpyAsync(pool, src_nodes, node_bytes, cudaMemcpyDeviceToDevice, s);
             cudaMemcpyAsync(pool + node_bytes, bo.tris, tri_bytes, cudaMemcpyDeviceToDevice, s);
             cudaStreamSynchronize(s);
             cudaFree(bo.tris);
             cudaFree(bo.nodes);
             cudaFree(bo.wnodes);
+            cudaFree(bo.nodes4);
             bo.tris = reinterpret_cast<float4*>(pool + node_bytes);
             if (bo.wnodes)
                 bo.wnodes = reinterpret_cast<WideNode*>(pool);
+            else if (bo.nodes4)
+                bo.nodes4 = reinterpret_cast<Bvh4Node*>(pool);
             else
                 bo.nodes = reinterpret_cast<BvhNode*>(pool);
             A.push_back(pool);
@@ -645,6 +660,7 @@ int build_scene(wf_ctx* c, const wf_scene_desc* D, ResidentScene& R)
     S.tris = bo.tris;
     S.nodes = bo.nodes;
     S.wnodes = bo.wnodes;
+    S.nodes4 = bo.nodes4;
     S.num_tris = ntri;
     S.num_nodes = bo.num_nodes;
     S.root_is_empty = ntri == 0 ? 1 : 0;
@@ -786,7 +802,7 @@ int build_scene(wf_ctx* c, const wf_scene_desc* D, ResidentScene& R)
     I.num_emissive_meshes = (int32_t)em.size();
     I.bvh_nodes = bo.num_nodes;
     int64_t bytes = (int64_t)ntri * 48 +
-                    (int64_t)bo.num_nodes * (int64_t)(bo.wnodes ? sizeof(WideNode) : sizeof(BvhNode)) +
+                    (int64_t)bo.num_nodes * (int64_t)tree_node_bytes(bo) +
                     (int64_t)pool_f.size() * 4 + (int64_t)pool_b.size() * 4;
     I.device_bytes = bytes;
     return WF_OK;
@@ -1192,7 +1208,7 @@ int wf_set_tuning(wf_ctx* c, const wf_tuning* t)
 {
     if (!c || !t) return WF_ERR_INVALID_ARGUMENT;
     if (t->trace_variant < 0 || t->trace_variant > 3 || t->persistent_blocks_per_sm < 0 ||
-        t->persistent_blocks_per_sm > 32 || t->bvh_builder < 0 || t->bvh_builder > 2)
+        t->persistent_blocks_per_sm > 32 || t->bvh_builder < 0 || t->bvh_builder > 3)
         return set_err(c, WF_ERR_INVALID_ARGUMENT, "tuning out of range");
     c->tuning = *t;
     return WF_OK;

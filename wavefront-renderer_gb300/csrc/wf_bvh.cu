@@ -451,9 +451,11 @@ __global__ void k_ploc_init(int n, const float* __restrict__ leaf_box, float* __
 // pass (items = binary node ids of the level's wide nodes).
 // ---------------------------------------------------------------------------
 
-// Children of each wide node: open the binary subtree greedily, always the
-// child of largest surface area among those with more than kWideLeafMax
-// triangles, until eight children or none left to open.
+// Children of each wide node (kWidth of them at most): open the binary
+// subtree greedily, always the child of largest surface area among those with
+// more than kLeafCnt triangles, until kWidth children or none left to open.
+// kids has 8 entries per item; unused ones are -1.
+template <int kWidth, int kLeafCnt>
 __global__ void k_wide_gather(const int* __restrict__ items, int count, int num_tris, const int* __restrict__ left,
                               const int* __restrict__ right, const int* __restrict__ cnt,
                               const float* __restrict__ nbox, int* __restrict__ kids, int* __restrict__ n_int,
@@ -463,16 +465,16 @@ __global__ void k_wide_gather(const int* __restrict__ items, int count, int num_
         const int b = items[k];
         int ch[8];
         int m = 0;
-        if (cnt[b] <= kWideLeafMax) {  // a whole tree of <= 3 triangles: one leaf child
+        if (cnt[b] <= kLeafCnt) {  // a whole tree small enough for one leaf child
             ch[m++] = b;
         } else {
             ch[m++] = left[b - num_tris];
             ch[m++] = right[b - num_tris];
-            while (m < 8) {
+            while (m < kWidth) {
                 int best = -1;
                 float best_a = -1.0f;
                 for (int i = 0; i < m; ++i) {
-                    if (cnt[ch[i]] <= kWideLeafMax) continue;
+                    if (cnt[ch[i]] <= kLeafCnt) continue;
                     const float* x = nbox + 6 * (int64_t)ch[i];
                     const float dx = x[3] - x[0], dy = x[4] - x[1], dz = x[5] - x[2];
                     const float a = dx * dy + dy * dz + dz * dx;
@@ -491,7 +493,7 @@ __global__ void k_wide_gather(const int* __restrict__ items, int count, int num_
         for (int i = 0; i < 8; ++i) {
             kids[8 * (int64_t)k + i] = i < m ? ch[i] : -1;
             if (i < m) {
-                if (cnt[ch[i]] > kWideLeafMax)
+                if (cnt[ch[i]] > kLeafCnt)
                     ++ni;
                 else
                     nt += cnt[ch[i]];
@@ -604,6 +606,56 @@ __global__ void k_wide_emit(const int* __restrict__ items, int count, int level_
     }
 }
 
+// One level of 4-wide nodes: padded child boxes at full precision, interior
+// children numbered from next_base in the order of the level's items, leaf
+// children over their depth-first triangle range of the PLOC order.
+__global__ void k_four_emit(const int* __restrict__ items, int count, int level_base, int next_base,
+                            const int* __restrict__ kids, const int* __restrict__ int_off, int num_tris,
+                            const int* __restrict__ cnt, const float* __restrict__ nbox,
+                            const int* __restrict__ offset, Bvh4Node* __restrict__ nodes,
+                            int* __restrict__ next_items)
+{
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
+        float pl[6][4];
+        int word[4];
+        int irank = 0;
+        for (int i = 0; i < 4; ++i) {
+            const int c = kids[8 * (int64_t)k + i];
+            float b[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+            if (c < 0) {
+                word[i] = (int)kEmptyChild4;
+            } else {
+                for (int a = 0; a < 6; ++a) b[a] = nbox[6 * (int64_t)c + a];
+                pad_box(b);
+                if (c < num_tris || cnt[c] <= kLeafMax) {
+                    word[i] = (int)(kLeafFlag | ((uint32_t)offset[c] << 3) | (uint32_t)(cnt[c] - 1));
+                } else {
+                    const int slot = int_off[k] + irank++;
+                    word[i] = next_base + slot;
+                    next_items[slot] = c;
+                }
+            }
+            // planes: lo x, hi x, lo y, hi y, lo z, hi z
+            pl[0][i] = b[0];
+            pl[1][i] = b[3];
+            pl[2][i] = b[1];
+            pl[3][i] = b[4];
+            pl[4][i] = b[2];
+            pl[5][i] = b[5];
+        }
+        Bvh4Node nd;
+        nd.lox = make_float4(pl[0][0], pl[0][1], pl[0][2], pl[0][3]);
+        nd.hix = make_float4(pl[1][0], pl[1][1], pl[1][2], pl[1][3]);
+        nd.loy = make_float4(pl[2][0], pl[2][1], pl[2][2], pl[2][3]);
+        nd.hiy = make_float4(pl[3][0], pl[3][1], pl[3][2], pl[3][3]);
+        nd.loz = make_float4(pl[4][0], pl[4][1], pl[4][2], pl[4][3]);
+        nd.hiz = make_float4(pl[5][0], pl[5][1], pl[5][2], pl[5][3]);
+        nd.kids = make_int4(word[0], word[1], word[2], word[3]);
+        nd.pad = make_int4(0, 0, 0, 0);
+        nodes[level_base + k] = nd;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Structural checks of a finished tree before it is used: every child index
 // and triangle range must lie inside the arrays (a failed check rejects the
@@ -656,6 +708,30 @@ __global__ void k_validate_binary(const BvhNode* __restrict__ nodes, int num_nod
     }
 }
 
+// 4-wide nodes: interior children only after their parent (level order, so
+// every walk down the tree ends), leaf ranges inside the triangle array, at
+// least one child per node.
+__global__ void k_validate_four(const Bvh4Node* __restrict__ nodes, int num_nodes, int num_tris, int* __restrict__ bad)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < num_nodes; i += gridDim.x * blockDim.x) {
+        const int kid[4] = {nodes[i].kids.x, nodes[i].kids.y, nodes[i].kids.z, nodes[i].kids.w};
+        bool ok = true;
+        int used = 0;
+        for (int c = 0; c < 4; ++c) {
+            const uint32_t k = (uint32_t)kid[c];
+            if (k == kEmptyChild4) continue;
+            ++used;
+            if (k & kLeafFlag) {
+                const int64_t first = (int64_t)((k & ~kLeafFlag) >> 3), cnt = (int64_t)(k & 7u) + 1;
+                ok = ok && cnt <= kLeafMax && first + cnt <= (int64_t)num_tris;
+            } else {
+                ok = ok && (int)k > i && (int)k < num_nodes;
+            }
+        }
+        if (!ok || used == 0) atomicOr(bad, 1);
+    }
+}
+
 int validate_tree(const BvhBuildOutput& out, int num_tris, int num_sms, cudaStream_t s, std::string& err)
 {
     int* d_bad = nullptr;
@@ -667,6 +743,8 @@ int validate_tree(const BvhBuildOutput& out, int num_tris, int num_sms, cudaStre
     cudaMemsetAsync(d_bad, 0, sizeof(int), s);
     if (out.wnodes)
         k_validate_wide<<<num_sms * 8, 256, 0, s>>>(out.wnodes, out.num_nodes, num_tris, d_bad);
+    else if (out.nodes4)
+        k_validate_four<<<num_sms * 8, 256, 0, s>>>(out.nodes4, out.num_nodes, num_tris, d_bad);
     else if (out.nodes)
         k_validate_binary<<<num_sms * 8, 256, 0, s>>>(out.nodes, out.num_nodes, num_tris, d_bad);
     cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, s);
@@ -1033,7 +1111,7 @@ int build_ploc_wide(const BvhBuildInput& in, BvhBuildOutput& out, int num_sms, c
             goto fail;
         }
         const int g = std::max(1, std::min(grid, (count + 127) / 128));
-        k_wide_gather<<<g, 128, 0, s>>>(items, count, n, T.left, T.right, T.cnt, T.nbox, kids, n_int, n_tri);
+        k_wide_gather<8, kWideLeafMax><<<g, 128, 0, s>>>(items, count, n, T.left, T.right, T.cnt, T.nbox, kids, n_int, n_tri);
         exclusive_scan_i32(n_int, count, int_off, T.block_sums, T.d_total, s);
         exclusive_scan_i32(n_tri, count, tri_off, T.block_sums, T.d_total + 1, s);
         int tot[2] = {0, 0};
@@ -1080,6 +1158,83 @@ fail:
     cudaFree(out.wnodes);
     out.tris = nullptr;
     out.wnodes = nullptr;
+    return -1;
+}
+
+int build_ploc4(const BvhBuildInput& in, BvhBuildOutput& out, int num_sms, cudaStream_t s, std::string& err)
+{
+    const int n = in.num_tris;
+    out.tris = nullptr;
+    out.nodes = nullptr;
+    out.wnodes = nullptr;
+    out.nodes4 = nullptr;
+    out.num_nodes = 0;
+    out.max_depth = 0;
+    if (n <= 0) return 0;
+    BuildScratch B;
+    PlocTree T;
+    const int grid = num_sms * 8;
+    int *keep, *keep_off, *items, *next_items, *kids, *n_int, *n_tri, *int_off;
+    int cap = 1, level_base = 0, count = 1, next_base = 1, levels = 0;
+    if (ploc_tree(in, num_sms, s, err, B, T)) goto fail;
+    // Every 4-wide node stands for a distinct binary node of more than
+    // kLeafMax triangles (or the root): that count bounds the node array.
+    WF_TRY(B.alloc(&keep, (size_t)n));
+    WF_TRY(B.alloc(&keep_off, (size_t)n));
+    if (n > 1) {
+        const int ninternal = T.root - n + 1;
+        k_ploc_keep<<<grid, 256, 0, s>>>(n, T.root, T.cnt, keep);
+        exclusive_scan_i32(keep, ninternal, keep_off, T.block_sums, T.d_total, s);
+        WF_TRY(cudaMemcpyAsync(&cap, T.d_total, sizeof(int), cudaMemcpyDeviceToHost, s));
+        WF_TRY(cudaStreamSynchronize(s));
+        cap = std::max(cap, 1);
+    }
+    WF_TRY(B.alloc(&items, (size_t)cap));
+    WF_TRY(B.alloc(&next_items, (size_t)cap));
+    WF_TRY(B.alloc(&kids, 8 * (size_t)cap));
+    WF_TRY(B.alloc(&n_int, (size_t)cap));
+    WF_TRY(B.alloc(&n_tri, (size_t)cap));
+    WF_TRY(B.alloc(&int_off, (size_t)cap));
+    WF_TRY(cudaMalloc(&out.nodes4, sizeof(Bvh4Node) * (size_t)cap));
+    WF_TRY(cudaMemcpyAsync(items, &T.root, sizeof(int), cudaMemcpyHostToDevice, s));
+    while (count > 0) {
+        ++levels;
+        if (1 + 3 * levels > kStack4) {
+            err = "4-wide BVH deeper than the traversal stack";
+            goto fail;
+        }
+        const int g = std::max(1, std::min(grid, (count + 127) / 128));
+        k_wide_gather<4, kLeafMax><<<g, 128, 0, s>>>(items, count, n, T.left, T.right, T.cnt, T.nbox, kids, n_int,
+                                                      n_tri);
+        exclusive_scan_i32(n_int, count, int_off, T.block_sums, T.d_total, s);
+        int next = 0;
+        WF_TRY(cudaMemcpyAsync(&next, T.d_total, sizeof(int), cudaMemcpyDeviceToHost, s));
+        WF_TRY(cudaStreamSynchronize(s));
+        if ((int64_t)next_base + next > cap) {
+            err = "4-wide BVH larger than its node bound";
+            goto fail;
+        }
+        k_four_emit<<<g, 128, 0, s>>>(items, count, level_base, next_base, kids, int_off, n, T.cnt, T.nbox, T.offset,
+                                      out.nodes4, next_items);
+        std::swap(items, next_items);
+        level_base = next_base;
+        next_base += next;
+        count = next;
+    }
+    WF_TRY(cudaMalloc(&out.tris, 3 * sizeof(float4) * (size_t)n));
+    k_emit_tris<<<grid, 256, 0, s>>>(in.px, in.py, in.pz, in.idx, in.tri_geom, in.tri_prim, T.final_ids, n,
+                                     out.tris);
+    WF_TRY(cudaGetLastError());
+    WF_TRY(cudaStreamSynchronize(s));
+    out.num_nodes = level_base;  // every level written: total nodes
+    out.max_depth = levels;
+    if (validate_tree(out, n, num_sms, s, err)) goto fail;
+    return 0;
+fail:
+    cudaFree(out.tris);
+    cudaFree(out.nodes4);
+    out.tris = nullptr;
+    out.nodes4 = nullptr;
     return -1;
 }
 

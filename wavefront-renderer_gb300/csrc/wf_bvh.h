@@ -25,6 +25,7 @@ struct BvhBuildOutput {
     int num_nodes;
     int max_depth;
     WideNode* wnodes = nullptr;  // compressed 8-wide tree instead of nodes
+    Bvh4Node* nodes4 = nullptr;  // 4-wide tree instead of nodes
 };
 
 // Returns 0 on success, -1 with err set otherwise.
@@ -42,5 +43,12 @@ int build_ploc(const BvhBuildInput& in, BvhBuildOutput& out, int num_sms, cudaSt
 // leaf children.  out.wnodes / out.num_nodes / out.max_depth (wide levels).
 int build_ploc_wide(const BvhBuildInput& in, BvhBuildOutput& out, int num_sms, cudaStream_t s,
                     std::string& err);
+
+// PLOC tree collapsed top-down into 4-wide nodes (Bvh4Node), level by
+// level: each node opens the binary subtree greedily (largest surface area
+// first) up to four children; subtrees of <= kLeafMax triangles stay leaves
+// over the same triangle order as build_ploc.  out.nodes4 / out.num_nodes /
+// out.max_depth (levels).
+int build_ploc4(const BvhBuildInput& in, BvhBuildOutput& out, int num_sms, cudaStream_t s, std::string& err);
 
 }  // namespace wf

@@ -39,7 +39,7 @@ struct CapturedWave {
     int variant = 0;
     const void* key_ptr = nullptr;  // buffers the capture baked in
     int64_t key_cap = 0;
-    bool wide = false;              // compressed 8-wide traversal
+    int tree = kTreeBinary;         // tree format (TreeFormat) of the traversal
     int kernels = 0;                // kernels per replay
 };
 

@@ -78,14 +78,33 @@ static_assert(sizeof(WideNode) == 80, "WideNode is five 16-byte words");
 constexpr int kWideLeafMax = 3;   // triangles per leaf child
 constexpr int kWideStack = 32;    // node-group stack entries (checked at build)
 
+// 4-wide node: the four child boxes at full precision, one 128-byte line.
+// Planes are stored per axis and side for the four children (lox.x = child
+// 0's lower x plane, ...); kids holds the child words of BvhNode's encoding,
+// kEmptyChild4 for an empty slot (whose box is never tested).  Interior
+// children are numbered level by level, so a child's index is always larger
+// than its parent's.
+struct __align__(16) Bvh4Node {
+    float4 lox, hix, loy, hiy, loz, hiz;
+    int4 kids;
+    int4 pad;
+};
+static_assert(sizeof(Bvh4Node) == 128, "Bvh4Node is one 128-byte line");
+constexpr uint32_t kEmptyChild4 = 0xFFFFFFFFu;  // never a leaf word: scenes hold < 2^28 triangles
+constexpr int kStack4 = 96;  // 4-wide traversal stack entries (checked at build: 1 + 3 x levels)
+
+// Tree format of a resident scene; the kernels of one wave use one traversal.
+enum TreeFormat : int { kTreeBinary = 0, kTreeWide8 = 1, kTreeFour = 2 };
+
 struct DeviceScene {
     // Triangles in BVH leaf order: 3 float4 each.
     //   [0] = v0.xyz, w = global triangle index (bits)
     //   [1] = (v1 - v0).xyz, w = geomID (mesh index)
     //   [2] = (v2 - v0).xyz, w = primID (index within the mesh)
     const float4* tris;
-    const BvhNode* nodes;      // binary tree, or null when wnodes is set
+    const BvhNode* nodes;      // binary tree, or null when wnodes / nodes4 is set
     const WideNode* wnodes;    // compressed 8-wide tree, or null
+    const Bvh4Node* nodes4;    // 4-wide tree, or null
     int32_t num_tris;
     int32_t num_nodes;
     int32_t root_is_empty;  // scene without triangles
@@ -122,6 +141,11 @@ struct DeviceScene {
     // Bounds (Scene::computeBounds) for the ray sort
     float bmin[3], bmax[3];
 };
+
+__host__ __device__ __forceinline__ int tree_format(const DeviceScene& S)
+{
+    return S.wnodes ? kTreeWide8 : (S.nodes4 ? kTreeFour : kTreeBinary);
+}
 
 // ---------------------------------------------------------------------------
 // Queues (device SoA).  Names follow the reference's columns

@@ -60,7 +60,7 @@ struct WaveTables {
     DeviceScene scene0;
     DeviceJob job0;
     bool multi;
-    bool wide;  // the scenes carry compressed 8-wide trees
+    int tree;  // tree format of the scenes (TreeFormat)
 };
 void launch_trace_render(const WaveTables& t, RayQueueDev rq, const ull* d_n, HitQueueDev hq, ull* hq_n,
                          float* accum, ull* work, int* err, LaunchCfg cfg, cudaStream_t s);

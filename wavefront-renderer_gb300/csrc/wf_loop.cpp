@@ -107,17 +107,20 @@ int ray_key_begin(const wf_ctx* c)
     return 33 - bits;
 }
 
-// Whether the resident scenes carry compressed 8-wide trees; a wave's
-// kernels use one traversal, so the formats must not be mixed.
-int table_wide(wf_ctx* c, bool& wide)
+// The tree format of the resident scenes (TreeFormat); a wave's kernels use
+// one traversal, so the formats must not be mixed.
+int table_tree(wf_ctx* c, int& tree)
 {
-    int w = 0, b = 0;
-    for (const auto& r : c->scenes)
-        if (r.live && r.S.num_tris > 0) ++(r.S.wnodes ? w : b);
-    if (w && b)
-        return set_err(c, WF_ERR_STATE,
-                       "resident scenes were built with different BVH formats (wf_tuning::bvh_builder)");
-    wide = w > 0;
+    int seen = -1;
+    for (const auto& r : c->scenes) {
+        if (!r.live || r.S.num_tris <= 0) continue;
+        const int f = tree_format(r.S);
+        if (seen >= 0 && f != seen)
+            return set_err(c, WF_ERR_STATE,
+                           "resident scenes were built with different BVH formats (wf_tuning::bvh_builder)");
+        seen = f;
+    }
+    tree = seen < 0 ? kTreeBinary : seen;
     return WF_OK;
 }
 
@@ -130,13 +133,13 @@ int wave_host(wf_ctx* c, int64_t total, int max_depth, int policy, bool ray_sort
 {
     std::vector<double> live_mat, live_tex;  // relativeCost of the live trackers, for the policies
     cudaStream_t s = c->stream;
-    WaveTables T{c->d_scene_table, c->d_jobs, DeviceScene{}, DeviceJob{}, single_job == nullptr, false};
+    WaveTables T{c->d_scene_table, c->d_jobs, DeviceScene{}, DeviceJob{}, single_job == nullptr, kTreeBinary};
     if (single_job) {
         T.job0 = *single_job;
         T.scene0 = c->scenes[single_job->scene].S;
-        T.wide = T.scene0.wnodes != nullptr;
+        T.tree = tree_format(T.scene0);
     } else {
-        int rc = table_wide(c, T.wide);
+        int rc = table_tree(c, T.tree);
         if (rc) return rc;
     }
     const LaunchCfg PC = persist_cfg(c), WC = wide_cfg(c);
@@ -238,13 +241,13 @@ int wave_host(wf_ctx* c, int64_t total, int max_depth, int policy, bool ray_sort
 
 // The launches of one wave with every count on the device: what a graph
 // captures.  Returns the number of kernels.
-int record_chain(wf_ctx* c, int max_depth, bool ray_sort, bool wide)
+int record_chain(wf_ctx* c, int max_depth, bool ray_sort, int tree)
 {
     cudaStream_t s = c->stream;
     const LaunchCfg PC = persist_cfg(c), WC = wide_cfg(c);
     int kernels = 0;
     int cur = 0;
-    const WaveTables T{c->d_scene_table, c->d_jobs, DeviceScene{}, DeviceJob{}, true, wide};
+    const WaveTables T{c->d_scene_table, c->d_jobs, DeviceScene{}, DeviceJob{}, true, tree};
     launch_camera_chunks(c->d_chunks, c->d_wave_header, c->d_jobs, c->rq[cur], WC, s);
     cudaMemcpyAsync(c->counters, c->d_wave_header, sizeof(ull), cudaMemcpyDeviceToDevice, s);
     kernels += 1;
@@ -277,18 +280,18 @@ int record_chain(wf_ctx* c, int max_depth, bool ray_sort, bool wide)
 int wave_graph(wf_ctx* c, int max_depth, bool ray_sort, wf_render_stats& stats)
 {
     cudaStream_t s = c->stream;
-    bool wide = false;
-    int rc = table_wide(c, wide);
+    int tree = kTreeBinary;
+    int rc = table_tree(c, tree);
     if (rc) return rc;
     CapturedWave* g = nullptr;
     for (auto& x : c->graphs)
         if (x.max_depth == max_depth && x.ray_sort == ray_sort && x.variant == c->tuning.trace_variant &&
-            x.key_ptr == c->arena && x.key_cap == c->cap && x.wide == wide)
+            x.key_ptr == c->arena && x.key_cap == c->cap && x.tree == tree)
             g = &x;
     if (!g) {
         cudaGraph_t graph = nullptr;
         WF_CK(c, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-        int k = record_chain(c, max_depth, ray_sort, wide);
+        int k = record_chain(c, max_depth, ray_sort, tree);
         cudaError_t e = cudaStreamEndCapture(s, &graph);
         if (e != cudaSuccess) return set_err(c, WF_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
         CapturedWave w;
@@ -300,7 +303,7 @@ int wave_graph(wf_ctx* c, int max_depth, bool ray_sort, wf_render_stats& stats)
         w.variant = c->tuning.trace_variant;
         w.key_ptr = c->arena;
         w.key_cap = c->cap;
-        w.wide = wide;
+        w.tree = tree;
         w.kernels = k;
         c->graphs.push_back(w);
         g = &c->graphs.back();

@@ -1175,7 +1175,8 @@ void launch_occluded_api(const DeviceScene& S, int64_t n, const float* ox, const
 // variant: 0 = no occupancy hint, 1 = 10 blocks of 128 per SM, 2 = the
 // traversal stack in shared memory (binary trees), 3 = the top 256 nodes of
 // the tree staged in shared memory (binary trees, single-scene waves; else
-// variant 0); the traversal follows the scene's tree (8-wide or binary).
+// variant 0); the traversal follows the scene's tree (binary, 4-wide or
+// compressed 8-wide).
 void launch_trace_render(const WaveTables& t, RayQueueDev rq, const ull* d_n, HitQueueDev hq, ull* hq_n,
                          float* accum, ull* work, int* err, LaunchCfg cfg, cudaStream_t s)
 {
@@ -1188,8 +1189,10 @@ void launch_trace_render(const WaveTables& t, RayQueueDev rq, const ull* d_n, Hi
     k_trace_render<M, 1, Traversal<false>, true><<<cfg.grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, \
                                                                          rq, d_n, hq, hq_n, accum, work, err, \
                                                                          cfg.speculative)
-    if (t.wide) {
+    if (t.tree == kTreeWide8) {
         if (t.multi) { WF_TRACE2(true, WideTraversal<false>); } else { WF_TRACE2(false, WideTraversal<false>); }
+    } else if (t.tree == kTreeFour) {
+        if (t.multi) { WF_TRACE2(true, Traversal4<false>); } else { WF_TRACE2(false, Traversal4<false>); }
     } else if (cfg.variant == 2) {
         if (t.multi) { WF_TRACE_SHARED(true); } else { WF_TRACE_SHARED(false); }
     } else if (cfg.variant == 3 && !t.multi && t.scene0.nodes) {
@@ -1234,8 +1237,10 @@ void launch_occluded_render(const WaveTables& t, ShadowQueueDev sh, const ull* s
     k_occluded_render<M, 1, Traversal<true>, true><<<cfg.grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, \
                                                                            sh, sh_n, accum, work, err, \
                                                                            cfg.speculative)
-    if (t.wide) {
+    if (t.tree == kTreeWide8) {
         if (t.multi) { WF_OCC2(true, WideTraversal<true>); } else { WF_OCC2(false, WideTraversal<true>); }
+    } else if (t.tree == kTreeFour) {
+        if (t.multi) { WF_OCC2(true, Traversal4<true>); } else { WF_OCC2(false, Traversal4<true>); }
     } else if (cfg.variant == 2) {
         if (t.multi) { WF_OCC_SHARED(true); } else { WF_OCC_SHARED(false); }
     } else if (cfg.variant == 3 && !t.multi && t.scene0.nodes) {

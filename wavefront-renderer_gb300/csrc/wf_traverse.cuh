@@ -1,4 +1,5 @@
-// wf_traverse.cuh — BVH2 traversal (closest hit and any hit).
+// wf_traverse.cuh — BVH traversal (closest hit and any hit) over the binary,
+// 4-wide and compressed 8-wide trees.
 //
 // Closest hit follows the brute-force semantics of the reference's
 // Scene::hit / Mesh::hit (src/core/Scene.cpp:120-160, src/geometry/Mesh.cpp
@@ -254,6 +255,99 @@ struct Traversal {
     }
 };
 
+// While-while traversal of the 4-wide tree (Bvh4Node): the four child boxes
+// of a node are slab-tested together; the hit children are ordered by entry
+// distance with a sorting network over keys (distance bits with the slot in
+// the low two bits, misses all ones), the nearest is visited next and the
+// others are pushed farthest first.  Same state, leaf test and acceptance
+// rule as the binary traversal, so the result does not depend on the tree.
+template <bool kAnyHit>
+struct Traversal4 : Traversal<kAnyHit> {
+    static constexpr int kStack = kStack4;
+
+    template <class Stk>
+    __device__ __forceinline__ void round(const DeviceScene& S, Stk stack)
+    {
+        round4(S.nodes4, S.tris, stack);
+    }
+    template <class Stk>
+    __device__ __forceinline__ void round(const DeviceScene& S, Stk stack, const BvhNode*, uint32_t)
+    {
+        round4(S.nodes4, S.tris, stack);
+    }
+
+    __device__ __forceinline__ uint32_t slab_key(float lx, float hx, float ly, float hy, float lz, float hz,
+                                                 int kid, uint32_t slot) const
+    {
+        const float tlx = __fmaf_rn(lx, this->inv.x, -this->oi.x), thx = __fmaf_rn(hx, this->inv.x, -this->oi.x);
+        const float tly = __fmaf_rn(ly, this->inv.y, -this->oi.y), thy = __fmaf_rn(hy, this->inv.y, -this->oi.y);
+        const float tlz = __fmaf_rn(lz, this->inv.z, -this->oi.z), thz = __fmaf_rn(hz, this->inv.z, -this->oi.z);
+        const float tn = fmaxf(fmaxf(fminf(tlx, thx), fminf(tly, thy)), fmaxf(fminf(tlz, thz), this->tmin));
+        const float tf = fminf(fminf(fmaxf(tlx, thx), fmaxf(tly, thy)), fminf(fmaxf(tlz, thz), this->best_t));
+        // tn >= tmin: for tmin >= 0 the bits order like the distances (the
+        // order only steers the walk, never the result)
+        return (tn <= tf && (uint32_t)kid != kEmptyChild4) ? ((__float_as_uint(tn) & ~3u) | slot) : 0xFFFFFFFFu;
+    }
+    __device__ __forceinline__ static void sort2(uint32_t& a, uint32_t& b)
+    {
+        const uint32_t lo = min(a, b), hi = max(a, b);
+        a = lo;
+        b = hi;
+    }
+    __device__ __forceinline__ static uint32_t kid_of(const int4& k, uint32_t key)
+    {
+        const uint32_t s = key & 3u;
+        return (uint32_t)(s == 0u ? k.x : s == 1u ? k.y : s == 2u ? k.z : k.w);
+    }
+    template <class Stk>
+    __device__ __forceinline__ void push(Stk stack, uint32_t e)
+    {
+        stack[this->sp++] = e;
+    }
+
+    template <class Stk>
+    __device__ __forceinline__ void round4(const Bvh4Node* __restrict__ nodes, const float4* __restrict__ tris,
+                                           Stk stack)
+    {
+        while (!(this->cur & kLeafFlag)) {
+            const float4* p = reinterpret_cast<const float4*>(nodes + this->cur);
+            const float4 lx = __ldg(p + 0), hx = __ldg(p + 1), ly = __ldg(p + 2), hy = __ldg(p + 3);
+            const float4 lz = __ldg(p + 4), hz = __ldg(p + 5);
+            const int4 k = __ldg(reinterpret_cast<const int4*>(p + 6));
+            uint32_t k0 = slab_key(lx.x, hx.x, ly.x, hy.x, lz.x, hz.x, k.x, 0u);
+            uint32_t k1 = slab_key(lx.y, hx.y, ly.y, hy.y, lz.y, hz.y, k.y, 1u);
+            uint32_t k2 = slab_key(lx.z, hx.z, ly.z, hy.z, lz.z, hz.z, k.z, 2u);
+            uint32_t k3 = slab_key(lx.w, hx.w, ly.w, hy.w, lz.w, hz.w, k.w, 3u);
+            sort2(k0, k1);
+            sort2(k2, k3);
+            sort2(k0, k2);
+            sort2(k1, k3);
+            sort2(k1, k2);
+            if (k0 == 0xFFFFFFFFu) {
+                this->cur = stack[--this->sp];
+                continue;
+            }
+            this->cur = kid_of(k, k0);
+            const int extra = (k1 != 0xFFFFFFFFu) + (k2 != 0xFFFFFFFFu) + (k3 != 0xFFFFFFFFu);
+            if (this->sp + extra > kStack4) {
+                this->overflow = true;
+                continue;
+            }
+            if (k3 != 0xFFFFFFFFu) push(stack, kid_of(k, k3));
+            if (k2 != 0xFFFFFFFFu) push(stack, kid_of(k, k2));
+            if (k1 != 0xFFFFFFFFu) push(stack, kid_of(k, k1));
+        }
+        while (this->cur != kSentinel && (this->cur & kLeafFlag)) {
+            const uint32_t leaf = this->cur;
+            this->cur = stack[--this->sp];
+            if (this->test_leaf(tris, leaf)) {
+                this->cur = kSentinel;
+                return;
+            }
+        }
+    }
+};
+
 // Traversal of the compressed 8-wide BVH (WideNode), after Ylitie, Karras &
 // Laine (HPG 2017): the stack holds node groups (x = first interior child,
 // y = hit keys << 24 | interior mask); one round descends into the nearest
@@ -421,6 +515,7 @@ __device__ __forceinline__ bool traverse(const DeviceScene& S, V3 o, V3 d, float
                                          TraceResult& res, int* err_flag)
 {
     if (S.wnodes) return traverse_with<WideTraversal<kAnyHit>>(S, o, d, tmin, tmax, res, err_flag);
+    if (S.nodes4) return traverse_with<Traversal4<kAnyHit>>(S, o, d, tmin, tmax, res, err_flag);
     return traverse_with<Traversal<kAnyHit>>(S, o, d, tmin, tmax, res, err_flag);
 }
 
