@@ -24,6 +24,7 @@ struct LaunchCfg {
     int block;
     int variant = 0;   // kernel variant (traversal occupancy hint / stack placement)
     int speculative = 0;  // 1 = speculative while-while traversal
+    int ray_order = 0;    // 1 = hit records at their rays' indices, listed by k_compact_hits
 };
 
 // Camera rays of n = width*height*nspp paths, sample-major.
@@ -66,6 +67,9 @@ void launch_trace_render(const WaveTables& t, RayQueueDev rq, const ull* d_n, Hi
                          float* accum, ull* work, int* err, LaunchCfg cfg, cudaStream_t s);
 void launch_shade(const WaveTables& t, RayQueueDev rq, HitQueueDev hq, const ull* hq_n, ShadowQueueDev sh,
                   ull* sh_n, RayQueueDev next, ull* next_n, float* accum, int* err, LaunchCfg cfg, cudaStream_t s);
+// After a ray-order trace: lists the rays that hit in hq.ray, counting them
+// into *hq_n (zero before the launch).
+void launch_compact_hits(const ull* d_n, HitQueueDev hq, ull* hq_n, LaunchCfg cfg, cudaStream_t s);
 void launch_occluded_render(const WaveTables& t, ShadowQueueDev sh, const ull* sh_n, float* accum, ull* work,
                             int* err, LaunchCfg cfg, cudaStream_t s);
 // tally[0..3] += rays, hits, shadow rays, (rays > 0) of the bounce just run.

@@ -225,7 +225,8 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_trace_render(DeviceScene sc
                                                                   const DeviceJob* __restrict__ jobs,
                                                                   RayQueueDev rq, const ull* __restrict__ d_n,
                                                                   HitQueueDev hq, ull* hq_n, float* accum,
-                                                                  ull* work, int* err, int speculative)
+                                                                  ull* work, int* err, int speculative,
+                                                                  int ray_order)
 {
     const int64_t n = (int64_t)*d_n;
     const int lane = threadIdx.x & 31;
@@ -256,7 +257,18 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_trace_render(DeviceScene sc
         const bool fin = ray >= 0 && tr.done();
         const bool hit = fin && tr.res.leafpos >= 0;
         const unsigned hm = __ballot_sync(0xFFFFFFFFu, hit);
-        if (hm) {
+        if (ray_order) {
+            // hit record at the ray's own index, tri = -1 for a miss (the
+            // hits are counted and listed by k_compact_hits)
+            if (fin) {
+                hq.tri[ray] = hit ? tr.res.leafpos : -1;
+                if (hit) {
+                    hq.t[ray] = tr.res.t;
+                    hq.bu[ray] = tr.res.bu;
+                    hq.bv[ray] = tr.res.bv;
+                }
+            }
+        } else if (hm) {
             ull base = 0;
             const int leader = __ffs(hm) - 1;
             if (lane == leader) base = atomicAdd(hq_n, (ull)__popc(hm));
@@ -324,6 +336,58 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_trace_render(DeviceScene sc
         }
     }
     if (overflow) atomicOr(err, 1);
+}
+
+// The rays that hit, listed in queue order for shading after a ray-order
+// trace (records at the rays' indices, tri = -1 for a miss).  A block takes
+// tiles of kCompactIters x 256 rays, ranks the hits of a tile in ray order
+// (ballots, then one warp scans the 64 warp counts) and reserves the tile's
+// run of the list with one atomic, so the list is sorted within a tile and
+// the tiles follow the blocks' sweep.  Shading in this order keeps the next
+// rays and the shadow rays in queue order too.
+constexpr int kCompactIters = 8;  // 8 x 8 warps = 64 counts: two per lane of the scanning warp
+
+__global__ void __launch_bounds__(256) k_compact_hits(const ull* __restrict__ d_n, HitQueueDev hq, ull* hq_n)
+{
+    __shared__ unsigned offs[kCompactIters * 8];
+    __shared__ ull tile_first;
+    const int64_t n = (int64_t)*d_n;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const unsigned lt = (1u << lane) - 1u;
+    const int64_t tile = 256 * kCompactIters;
+    for (int64_t t0 = (int64_t)blockIdx.x * tile; t0 < n; t0 += (int64_t)gridDim.x * tile) {
+        unsigned masks[kCompactIters];
+#pragma unroll
+        for (int j = 0; j < kCompactIters; ++j) {
+            const int64_t k = t0 + j * 256 + threadIdx.x;
+            masks[j] = __ballot_sync(0xFFFFFFFFu, k < n && hq.tri[k] >= 0);
+            if (lane == 0) offs[j * 8 + warp] = (unsigned)__popc(masks[j]);
+        }
+        __syncthreads();
+        if (warp == 0) {  // exclusive scan of the counts in ray order (j, then warp)
+            const unsigned a = offs[2 * lane], b = offs[2 * lane + 1];
+            unsigned incl = a + b;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const unsigned y = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+                if (lane >= d) incl += y;
+            }
+            const unsigned excl = incl - (a + b);
+            offs[2 * lane] = excl;
+            offs[2 * lane + 1] = excl + a;
+            const unsigned total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+            if (lane == 0) tile_first = total ? atomicAdd(hq_n, (ull)total) : 0ull;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < kCompactIters; ++j) {
+            if ((masks[j] >> lane) & 1u) {
+                const int64_t k = t0 + j * 256 + threadIdx.x;
+                hq.ray[(int64_t)tile_first + offs[j * 8 + warp] + __popc(masks[j] & lt)] = (int32_t)k;
+            }
+        }
+        __syncthreads();  // offs and tile_first are reused by the next tile
+    }
 }
 
 // Adds the cycles of the lanes timing the same item with one atomic per item
@@ -401,17 +465,22 @@ __global__ void k_cost_update(CostTrackerDev mat, CostTrackerDev tex, int repeat
 // roulette and the next ray.  Random streams per (purpose, depth, pixel,
 // sample) — the oracle uses the same ones.
 // ---------------------------------------------------------------------------
-template <bool kMulti>
+constexpr int kShadeWarps = 4;  // k_shade runs 128-thread blocks
 #ifndef WF_SHADE_MIN_BLOCKS
 #define WF_SHADE_MIN_BLOCKS 6  // 80 registers, 6 resident blocks (91 / 5 unbounded): +2%
 #endif
+template <bool kMulti>
 __global__ void __launch_bounds__(128, WF_SHADE_MIN_BLOCKS) k_shade(DeviceScene scene0, DeviceJob job0,
                                                const DeviceScene* __restrict__ scenes,
                                                const DeviceJob* __restrict__ jobs, RayQueueDev rq,
-                                               HitQueueDev hq, const ull* __restrict__ hq_n,
+                                               HitQueueDev hq, const ull* __restrict__ hq_n, int ray_order,
                                                ShadowQueueDev sh, ull* sh_n, RayQueueDev nx,
                                                ull* nx_n, float* accum_base, int* err)
 {
+    // hq.ray lists the rays that hit; their records (tri, t, u, v) sit at the
+    // list position, or with ray_order at the ray's own index.
+    __shared__ unsigned blk_sh[kShadeWarps], blk_nx[kShadeWarps];
+    __shared__ ull blk_first[2];
     const int64_t n = (int64_t)*hq_n;
     WF_BLOCK_LOOP(base, n)
     {
@@ -426,6 +495,7 @@ __global__ void __launch_bounds__(128, WF_SHADE_MIN_BLOCKS) k_shade(DeviceScene 
         unsigned cyc_mat = 0, cyc_tex = 0;
         if (active) {
             const int ri = hq.ray[k];
+            const int64_t hk = ray_order ? (int64_t)ri : k;
             job = kMulti ? rq.job[ri] : 0;
             const DeviceJob& J = kMulti ? jobs[job] : job0;
             const DeviceScene& S = kMulti ? scenes[J.scene] : scene0;
@@ -441,7 +511,7 @@ __global__ void __launch_bounds__(128, WF_SHADE_MIN_BLOCKS) k_shade(DeviceScene 
             sample = rq.sample[ri];
             slot = job_slot(J, pixel, sample);
             HitRec h;
-            rebuild_hit(S, o, d, hq.tri[k], hq.t[k], hq.bu[k], hq.bv[k], h);
+            rebuild_hit(S, o, d, hq.tri[hk], hq.t[hk], hq.bu[hk], hq.bv[hk], h);
             p = h.p;
             const wf_material m = S.materials[h.mat];
             V3 surf = {0, 0, 0};
@@ -608,7 +678,38 @@ __global__ void __launch_bounds__(128, WF_SHADE_MIN_BLOCKS) k_shade(DeviceScene 
             warp_cost_add(job0.cost_sum_mat, job0.cost_cnt_mat, cost_mat, cyc_mat);
             warp_cost_add(job0.cost_sum_tex, job0.cost_cnt_tex, cost_tex, cyc_tex);
         }
-        int64_t pa = warp_append(sh_n, want_area);
+        // One reservation per block and queue: the block's shadow rays (each
+        // warp's area, then directional, then environment rays) and next rays
+        // keep the order of the hits, with one atomic per block and counter.
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        const unsigned lt = (1u << lane) - 1u;
+        const unsigned ma = __ballot_sync(0xFFFFFFFFu, want_area), md = __ballot_sync(0xFFFFFFFFu, want_dir);
+        const unsigned me = __ballot_sync(0xFFFFFFFFu, want_env), mn = __ballot_sync(0xFFFFFFFFu, want_next);
+        if (lane == 0) {
+            blk_sh[warp] = (unsigned)(__popc(ma) + __popc(md) + __popc(me));
+            blk_nx[warp] = (unsigned)__popc(mn);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned ts = 0, tn = 0;
+            for (int w = 0; w < kShadeWarps; ++w) {
+                const unsigned a = blk_sh[w], b = blk_nx[w];
+                blk_sh[w] = ts;
+                blk_nx[w] = tn;
+                ts += a;
+                tn += b;
+            }
+            blk_first[0] = ts ? atomicAdd(sh_n, (ull)ts) : 0ull;
+            blk_first[1] = tn ? atomicAdd(nx_n, (ull)tn) : 0ull;
+        }
+        __syncthreads();
+        const int64_t sh0 = (int64_t)blk_first[0] + blk_sh[warp];
+        const int64_t nx0 = (int64_t)blk_first[1] + blk_nx[warp];
+        __syncthreads();  // the block's words are rewritten by the next iteration
+        const int64_t pa = sh0 + __popc(ma & lt);
+        const int64_t pd = sh0 + __popc(ma) + __popc(md & lt);
+        const int64_t pe = sh0 + __popc(ma) + __popc(md) + __popc(me & lt);
+        const int64_t pn = nx0 + __popc(mn & lt);
         if (want_area) {
             if (pa < sh.capacity) {
                 sh.ox[pa] = p.x; sh.oy[pa] = p.y; sh.oz[pa] = p.z;
@@ -621,8 +722,6 @@ __global__ void __launch_bounds__(128, WF_SHADE_MIN_BLOCKS) k_shade(DeviceScene 
                 atomicOr(err, 4);
             }
         }
-        __syncwarp();
-        int64_t pd = warp_append(sh_n, want_dir);
         if (want_dir) {
             if (pd < sh.capacity) {
                 sh.ox[pd] = p.x; sh.oy[pd] = p.y; sh.oz[pd] = p.z;
@@ -635,8 +734,6 @@ __global__ void __launch_bounds__(128, WF_SHADE_MIN_BLOCKS) k_shade(DeviceScene 
                 atomicOr(err, 4);
             }
         }
-        __syncwarp();
-        int64_t pe = warp_append(sh_n, want_env);
         if (want_env) {
             if (pe < sh.capacity) {
                 sh.ox[pe] = p.x; sh.oy[pe] = p.y; sh.oz[pe] = p.z;
@@ -649,8 +746,6 @@ __global__ void __launch_bounds__(128, WF_SHADE_MIN_BLOCKS) k_shade(DeviceScene 
                 atomicOr(err, 4);
             }
         }
-        __syncwarp();
-        int64_t pn = warp_append(nx_n, want_next);
         if (want_next) {
             if (pn < nx.capacity) {
                 nx.ox[pn] = p.x; nx.oy[pn] = p.y; nx.oz[pn] = p.z;
@@ -1182,13 +1277,13 @@ void launch_trace_render(const WaveTables& t, RayQueueDev rq, const ull* d_n, Hi
 {
 #define WF_TRACE(M, B, T)                                                                                   \
     k_trace_render<M, B, T><<<cfg.grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, d_n, hq, hq_n, \
-                                                     accum, work, err, cfg.speculative)
+                                                     accum, work, err, cfg.speculative, cfg.ray_order)
 #define WF_TRACE2(M, T) \
     if (cfg.variant == 1) WF_TRACE(M, 10, T); else WF_TRACE(M, 1, T)
 #define WF_TRACE_SHARED(M)                                                                                \
     k_trace_render<M, 1, Traversal<false>, true><<<cfg.grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, \
                                                                          rq, d_n, hq, hq_n, accum, work, err, \
-                                                                         cfg.speculative)
+                                                                         cfg.speculative, cfg.ray_order)
     if (t.tree == kTreeWide8) {
         if (t.multi) { WF_TRACE2(true, WideTraversal<false>); } else { WF_TRACE2(false, WideTraversal<false>); }
     } else if (t.tree == kTreeFour) {
@@ -1197,7 +1292,7 @@ void launch_trace_render(const WaveTables& t, RayQueueDev rq, const ull* d_n, Hi
         if (t.multi) { WF_TRACE_SHARED(true); } else { WF_TRACE_SHARED(false); }
     } else if (cfg.variant == 3 && !t.multi && t.scene0.nodes) {
         k_trace_render<false, 1, Traversal<false>, false, true><<<cfg.grid, 128, 0, s>>>(
-            t.scene0, t.job0, t.scenes, t.jobs, rq, d_n, hq, hq_n, accum, work, err, cfg.speculative);
+            t.scene0, t.job0, t.scenes, t.jobs, rq, d_n, hq, hq_n, accum, work, err, cfg.speculative, cfg.ray_order);
     } else {
         if (t.multi) { WF_TRACE2(true, Traversal<false>); } else { WF_TRACE2(false, Traversal<false>); }
     }
@@ -1218,11 +1313,16 @@ void launch_shade(const WaveTables& t, RayQueueDev rq, HitQueueDev hq, const ull
                   ull* sh_n, RayQueueDev next, ull* next_n, float* accum, int* err, LaunchCfg cfg, cudaStream_t s)
 {
     if (t.multi)
-        k_shade<true><<<cfg.grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, hq, hq_n, sh, sh_n, next,
-                                               next_n, accum, err);
+        k_shade<true><<<cfg.grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, hq, hq_n, cfg.ray_order, sh,
+                                               sh_n, next, next_n, accum, err);
     else
-        k_shade<false><<<cfg.grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, hq, hq_n, sh, sh_n, next,
-                                                next_n, accum, err);
+        k_shade<false><<<cfg.grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, hq, hq_n, cfg.ray_order, sh,
+                                                sh_n, next, next_n, accum, err);
+}
+
+void launch_compact_hits(const ull* d_n, HitQueueDev hq, ull* hq_n, LaunchCfg cfg, cudaStream_t s)
+{
+    k_compact_hits<<<cfg.grid, 256, 0, s>>>(d_n, hq, hq_n);
 }
 
 void launch_occluded_render(const WaveTables& t, ShadowQueueDev sh, const ull* sh_n, float* accum, ull* work,
