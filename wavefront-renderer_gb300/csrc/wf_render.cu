@@ -61,6 +61,30 @@ __global__ void k_camera(wf_camera cam, int W, int H, uint32_t s0, uint32_t s1, 
 
 // Camera rays of one wave made of chunks (job, samples) of several jobs: the
 // same arithmetic as k_camera, the job's camera and seed.
+// Queue order of a sample's pixels in the render loop: bands of 4 rows, each
+// walked in 8x4 tiles (a narrower last tile where the width is not a multiple
+// of 8; the last band may hold fewer rows), so a warp's 32 camera rays cover
+// an 8x4 block and its later bounces start from nearby points.  A bijection
+// on [0, W*H); the pixel keys the random streams, so the order changes no path.
+__device__ __forceinline__ int tile_pixel(int q, int W, int H)
+{
+    const int band = q / (4 * W);
+    const int r = q - band * 4 * W;
+    const int hb = min(4, H - 4 * band);
+    const int full = (W / 8) * 8 * hb;
+    int x, y;
+    if (r < full) {
+        const int c = r / (8 * hb), w = r - c * 8 * hb;
+        x = c * 8 + (w & 7);
+        y = 4 * band + (w >> 3);
+    } else {
+        const int wl = W - (W / 8) * 8, w = r - full;
+        x = (W / 8) * 8 + w % wl;
+        y = 4 * band + w / wl;
+    }
+    return y * W + x;
+}
+
 __global__ void k_camera_chunks(const WaveChunk* __restrict__ chunks, const long long* __restrict__ header,
                                 const DeviceJob* __restrict__ jobs, RayQueueDev rq)
 {
@@ -79,7 +103,10 @@ __global__ void k_camera_chunks(const WaveChunk* __restrict__ chunks, const long
         const int64_t local = i - ch.path_offset;
         const int s = (int)(local / np);
         int p = (int)(local - (int64_t)s * np);
-        if (ch.active_count > 0) p = J.active[p];  // generatePrimaryRays' activePixels mask
+        if (ch.active_count > 0)
+            p = J.active[p];  // generatePrimaryRays' activePixels mask
+        else
+            p = tile_pixel(p, J.width, J.height);
         const int x = p % J.width, y = p / J.width;
         const int sample = ch.first_sample + s;
         const wf_camera& cam = J.camera;
