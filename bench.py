@@ -453,11 +453,13 @@ def main() -> int:
         samples_all = world * args.steps * int(ctx.sample_counts(W, H).sum())
 
     # ---- end to end through the C ABI with host buffers ----
+    # the image comes back into page-locked host memory (wf_host_alloc)
+    image_host = pkg.host_array(W * H * 3)
     barrier(dist)
     e2e_rays = 0
     t0 = time.perf_counter()
     for k in range(args.steps):
-        _, st = ctx.render(params(rank * 100000 + 50000 + k))
+        _, st = ctx.render(params(rank * 100000 + 50000 + k), out=image_host)
         e2e_rays += st["closest_rays"] + st["shadow_rays"]
     e2e_s = allreduce_max(dist, time.perf_counter() - t0)
     e2e_value = allreduce_sum(dist, e2e_rays) / e2e_s / 1e6

@@ -25,6 +25,7 @@
 #ifndef WF_API_H
 #define WF_API_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -273,8 +274,8 @@ typedef struct wf_scene_info {
 int wf_scene_get_info(wf_ctx* ctx, wf_scene_info* out_info);
 
 /* Launch tuning of a context (the autotuner's knobs).  trace_variant: 0 = no
- * occupancy hint on the traversal kernels, 1 = 10 blocks of 128 threads per
- * SM, 2 = the traversal stack in shared memory instead of local memory
+ * occupancy hint on the traversal kernels, 1 = 9 blocks of 128 threads per
+ * SM (56 registers, no spills), 2 = the traversal stack in shared memory instead of local memory
  * (binary trees; 32 KB per block), 3 = the top 256 nodes of the tree staged
  * in shared memory (binary trees, single-scene renders).
  * persistent_blocks_per_sm: resident blocks launched per
@@ -452,6 +453,13 @@ int wf_render_accumulate(wf_ctx* ctx, const wf_render_params* params, float* acc
 int wf_render_device(wf_ctx* ctx, const wf_render_params* params, wf_render_stats* stats);
 /* Copies the image of the last wf_render_device (width*height*3 floats). */
 int wf_image_download(wf_ctx* ctx, float* image_rgb, int64_t num_floats);
+
+/* Page-locked host memory (device addition): images and queue mirrors in it
+ * are copied by DMA at full link speed, without staging through the driver's
+ * buffers.  wf_host_alloc returns WF_ERR_OUT_OF_MEMORY (or WF_ERR_NO_DEVICE)
+ * and leaves *out_ptr NULL on failure; wf_host_free(NULL) is a no-op. */
+int wf_host_alloc(size_t bytes, void** out_ptr);
+int wf_host_free(void* ptr);
 
 /* Relative costs (CostTracker::relativeCost) of the live trackers after
  * the last render with enable_cost_tracking: num_materials doubles, then

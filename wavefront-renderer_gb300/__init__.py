@@ -228,6 +228,8 @@ def _declare(lib: C.CDLL) -> None:
         "wf_render_accumulate": ([V, C.POINTER(WfRenderParams), f32p, C.POINTER(WfRenderStats)], C.c_int),
         "wf_render_device": ([V, C.POINTER(WfRenderParams), C.POINTER(WfRenderStats)], C.c_int),
         "wf_image_download": ([V, f32p, C.c_int64], C.c_int),
+        "wf_host_alloc": ([C.c_size_t, C.POINTER(V)], C.c_int),
+        "wf_host_free": ([V], C.c_int),
         "wf_adaptive_sample_counts": ([V, i32p, C.c_int64], C.c_int),
         "wf_autotune": ([V, C.POINTER(WfRenderParams), C.POINTER(WfTuning), C.POINTER(C.c_double)], C.c_int),
         "wf_scene_save": ([C.c_char_p, C.POINTER(WfSceneDesc), f32p, f32p, f32p, C.c_float], C.c_int),
@@ -273,6 +275,19 @@ def header_symbols() -> list[str]:
 
 class WfError(RuntimeError):
     pass
+
+
+def host_array(count: int, dtype=np.float32) -> np.ndarray:
+    """A 1-D numpy array of `count` elements in page-locked host memory
+    (wf_host_alloc); the memory is released when the array is collected."""
+    import weakref
+
+    dt = np.dtype(dtype)
+    p = C.c_void_p()
+    _check(load_library().wf_host_alloc(C.c_size_t(count * dt.itemsize), C.byref(p)), "wf_host_alloc")
+    raw = (C.c_uint8 * (count * dt.itemsize)).from_address(p.value)
+    weakref.finalize(raw, load_library().wf_host_free, C.c_void_p(p.value))
+    return np.frombuffer(raw, dtype=dt, count=count)
 
 
 def _check(rc: int, what: str, ctx=None) -> None:
@@ -631,8 +646,17 @@ class Context:
         _check(load_library().wf_get_stream(self._h, C.byref(s)), "wf_get_stream", self)
         return s.value or 0
 
-    def render(self, params: WfRenderParams, accumulate: bool = False):
-        img = np.zeros(params.width * params.height * 3, dtype=np.float32)
+    def render(self, params: WfRenderParams, accumulate: bool = False, out: np.ndarray | None = None):
+        """wf_render (or wf_render_accumulate) into `out` when given — a
+        contiguous float32 array of width*height*3 values, e.g. a host_array
+        in page-locked memory — else into a new array."""
+        nf = params.width * params.height * 3
+        if out is None:
+            img = np.zeros(nf, dtype=np.float32)
+        else:
+            if out.dtype != np.float32 or out.size != nf or not out.flags.c_contiguous:
+                raise ValueError("out must be a contiguous float32 array of width*height*3 values")
+            img = out.reshape(-1)
         st = WfRenderStats()
         fn = load_library().wf_render_accumulate if accumulate else load_library().wf_render
         _check(fn(self._h, C.byref(params), ptr(img), C.byref(st)), "wf_render", self)

@@ -900,6 +900,29 @@ int wf_destroy(wf_ctx* c)
 
 const char* wf_last_error(const wf_ctx* c) { return c ? c->last_error.c_str() : ""; }
 
+int wf_host_alloc(size_t bytes, void** out)
+{
+    if (!out) return WF_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n <= 0) {
+        cudaGetLastError();
+        return WF_ERR_NO_DEVICE;
+    }
+    if (cudaMallocHost(out, bytes ? bytes : 1) != cudaSuccess) {
+        cudaGetLastError();
+        *out = nullptr;
+        return WF_ERR_OUT_OF_MEMORY;
+    }
+    return WF_OK;
+}
+
+int wf_host_free(void* p)
+{
+    if (!p) return WF_OK;
+    return cudaFreeHost(p) == cudaSuccess ? WF_OK : WF_ERR_INVALID_ARGUMENT;
+}
+
 int wf_camera_make(const float look_from[3], const float look_at[3], const float up[3],
                    float vfov, int32_t w, int32_t h, wf_camera* out)
 {

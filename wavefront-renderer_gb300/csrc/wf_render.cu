@@ -1294,7 +1294,7 @@ void launch_occluded_api(const DeviceScene& S, int64_t n, const float* ox, const
                                                              out, err);
 }
 
-// variant: 0 = no occupancy hint, 1 = 10 blocks of 128 per SM, 2 = the
+// variant: 0 = no occupancy hint, 1 = 9 blocks of 128 per SM, 2 = the
 // traversal stack in shared memory (binary trees), 3 = the top 256 nodes of
 // the tree staged in shared memory (binary trees, single-scene waves; else
 // variant 0); the traversal follows the scene's tree (binary, 4-wide or
@@ -1306,7 +1306,7 @@ void launch_trace_render(const WaveTables& t, RayQueueDev rq, const ull* d_n, Hi
     k_trace_render<M, B, T><<<cfg.grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, d_n, hq, hq_n, \
                                                      accum, work, err, cfg.speculative, cfg.ray_order)
 #define WF_TRACE2(M, T) \
-    if (cfg.variant == 1) WF_TRACE(M, 10, T); else WF_TRACE(M, 1, T)
+    if (cfg.variant == 1) WF_TRACE(M, 9, T); else WF_TRACE(M, 1, T)
 #define WF_TRACE_SHARED(M)                                                                                \
     k_trace_render<M, 1, Traversal<false>, true><<<cfg.grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, \
                                                                          rq, d_n, hq, hq_n, accum, work, err, \
@@ -1359,7 +1359,7 @@ void launch_occluded_render(const WaveTables& t, ShadowQueueDev sh, const ull* s
     k_occluded_render<M, B, T><<<cfg.grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, sh, sh_n, accum, work, \
                                                         err, cfg.speculative)
 #define WF_OCC2(M, T) \
-    if (cfg.variant == 1) WF_OCC(M, 10, T); else WF_OCC(M, 1, T)
+    if (cfg.variant == 1) WF_OCC(M, 9, T); else WF_OCC(M, 1, T)
 #define WF_OCC_SHARED(M)                                                                                     \
     k_occluded_render<M, 1, Traversal<true>, true><<<cfg.grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, \
                                                                            sh, sh_n, accum, work, err, \
