@@ -118,20 +118,20 @@ __global__ void k_camera_chunks(const WaveChunk* __restrict__ chunks, const long
         float u = ((float)x + rng.next()) / (float)(J.width - 1);
         float v = 1.0f - ((float)y + rng.next()) / (float)(J.height - 1);
         V3 d = normalized(tl + hz * u + vt * v - org);
-        rq.ox[i] = org.x;
-        rq.oy[i] = org.y;
-        rq.oz[i] = org.z;
-        rq.dx[i] = d.x;
-        rq.dy[i] = d.y;
-        rq.dz[i] = d.z;
-        rq.tr[i] = 1.0f;
-        rq.tg[i] = 1.0f;
-        rq.tb[i] = 1.0f;
-        rq.pdf[i] = -1.0f;
-        rq.pixel[i] = p;
-        rq.depth[i] = 0;
-        rq.sample[i] = sample;
-        rq.job[i] = ch.job;
+        stq(&rq.ox[i], org.x);
+        stq(&rq.oy[i], org.y);
+        stq(&rq.oz[i], org.z);
+        stq(&rq.dx[i], d.x);
+        stq(&rq.dy[i], d.y);
+        stq(&rq.dz[i], d.z);
+        stq(&rq.tr[i], 1.0f);
+        stq(&rq.tg[i], 1.0f);
+        stq(&rq.tb[i], 1.0f);
+        stq(&rq.pdf[i], -1.0f);
+        stq(&rq.pixel[i], p);
+        stq(&rq.depth[i], 0);
+        stq(&rq.sample[i], sample);
+        stq(&rq.job[i], ch.job);
     }
 }
 
@@ -288,11 +288,11 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_trace_render(DeviceScene sc
             // hit record at the ray's own index, tri = -1 for a miss (the
             // hits are counted and listed by k_compact_hits)
             if (fin) {
-                hq.tri[ray] = hit ? tr.res.leafpos : -1;
+                stq(&hq.tri[ray], hit ? tr.res.leafpos : -1);
                 if (hit) {
-                    hq.t[ray] = tr.res.t;
-                    hq.bu[ray] = tr.res.bu;
-                    hq.bv[ray] = tr.res.bv;
+                    stq(&hq.t[ray], tr.res.t);
+                    stq(&hq.bu[ray], tr.res.bu);
+                    stq(&hq.bv[ray], tr.res.bv);
                 }
             }
         } else if (hm) {
@@ -303,11 +303,11 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_trace_render(DeviceScene sc
             if (hit) {
                 const int64_t pos = (int64_t)base + __popc(hm & lt);
                 if (pos < hq.capacity) {
-                    hq.ray[pos] = (int32_t)ray;
-                    hq.tri[pos] = tr.res.leafpos;
-                    hq.t[pos] = tr.res.t;
-                    hq.bu[pos] = tr.res.bu;
-                    hq.bv[pos] = tr.res.bv;
+                    stq(&hq.ray[pos], (int32_t)ray);
+                    stq(&hq.tri[pos], tr.res.leafpos);
+                    stq(&hq.t[pos], tr.res.t);
+                    stq(&hq.bu[pos], tr.res.bu);
+                    stq(&hq.bv[pos], tr.res.bv);
                 } else {
                     atomicOr(err, 2);
                 }
@@ -315,15 +315,15 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_trace_render(DeviceScene sc
         }
         if (fin && !hit) {
             const DeviceJob& J = kMulti ? jobs[job] : job0;
-            const V3 T = {rq.tr[ray], rq.tg[ray], rq.tb[ray]};
+            const V3 T = {ldq(&rq.tr[ray]), ldq(&rq.tg[ray]), ldq(&rq.tb[ray])};
             V3 c = T * sky_color(*S, tr.d);
             // With environment NEE the bounce that sampled this direction by
             // its BSDF (pdf > 0) shares the estimate: balance-heuristic weight.
             if (J.env_nee && S->env_alias_prob) {
-                const float ip = rq.pdf[ray];
+                const float ip = ldq(&rq.pdf[ray]);
                 if (ip > 0.0f) c = c * mis_balance(ip, env_pdf(*S, normalized(tr.d)));
             }
-            const int32_t slot = job_slot(J, rq.pixel[ray], J.sample_buf ? rq.sample[ray] : 0);
+            const int32_t slot = job_slot(J, ldq(&rq.pixel[ray]), J.sample_buf ? ldq(&rq.sample[ray]) : 0);
             accum_add(job_accum(J, accum), slot, c);
         }
         if (fin) {
@@ -343,11 +343,11 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_trace_render(DeviceScene sc
                 if (idx < n) {
                     ray = idx;
                     if (kMulti) {
-                        job = rq.job[idx];
+                        job = ldq(&rq.job[idx]);
                         S = scenes + jobs[job].scene;
                     }
-                    tr.init(*S, stack, v3(rq.ox[idx], rq.oy[idx], rq.oz[idx]),
-                            v3(rq.dx[idx], rq.dy[idx], rq.dz[idx]), 0.001f, 1e9f);
+                    tr.init(*S, stack, v3(ldq(&rq.ox[idx]), ldq(&rq.oy[idx]), ldq(&rq.oz[idx])),
+                            v3(ldq(&rq.dx[idx]), ldq(&rq.dy[idx]), ldq(&rq.dz[idx])), 0.001f, 1e9f);
                 } else {
                     exhausted = true;
                 }
@@ -387,7 +387,7 @@ __global__ void __launch_bounds__(256) k_compact_hits(const ull* __restrict__ d_
 #pragma unroll
         for (int j = 0; j < kCompactIters; ++j) {
             const int64_t k = t0 + j * 256 + threadIdx.x;
-            masks[j] = __ballot_sync(0xFFFFFFFFu, k < n && hq.tri[k] >= 0);
+            masks[j] = __ballot_sync(0xFFFFFFFFu, k < n && ldq(&hq.tri[k]) >= 0);
             if (lane == 0) offs[j * 8 + warp] = (unsigned)__popc(masks[j]);
         }
         __syncthreads();
@@ -410,7 +410,7 @@ __global__ void __launch_bounds__(256) k_compact_hits(const ull* __restrict__ d_
         for (int j = 0; j < kCompactIters; ++j) {
             if ((masks[j] >> lane) & 1u) {
                 const int64_t k = t0 + j * 256 + threadIdx.x;
-                hq.ray[(int64_t)tile_first + offs[j * 8 + warp] + __popc(masks[j] & lt)] = (int32_t)k;
+                stq(&hq.ray[(int64_t)tile_first + offs[j * 8 + warp] + __popc(masks[j] & lt)], (int32_t)k);
             }
         }
         __syncthreads();  // offs and tile_first are reused by the next tile
@@ -521,24 +521,24 @@ __global__ void __launch_bounds__(128, WF_SHADE_MIN_BLOCKS) k_shade(DeviceScene 
         int cost_mat = -1, cost_tex = -1;
         unsigned cyc_mat = 0, cyc_tex = 0;
         if (active) {
-            const int ri = hq.ray[k];
+            const int ri = ldq(&hq.ray[k]);
             const int64_t hk = ray_order ? (int64_t)ri : k;
-            job = kMulti ? rq.job[ri] : 0;
+            job = kMulti ? ldq(&rq.job[ri]) : 0;
             const DeviceJob& J = kMulti ? jobs[job] : job0;
             const DeviceScene& S = kMulti ? scenes[J.scene] : scene0;
             float* accum = job_accum(J, accum_base);
             const float ff = J.firefly;
             const uint32_t seed_lo = J.seed_lo, seed_hi = J.seed_hi;
-            const V3 o = {rq.ox[ri], rq.oy[ri], rq.oz[ri]};
-            const V3 d = {rq.dx[ri], rq.dy[ri], rq.dz[ri]};
-            const V3 T = {rq.tr[ri], rq.tg[ri], rq.tb[ri]};
-            const float in_pdf = rq.pdf[ri];
-            pixel = rq.pixel[ri];
-            depth = rq.depth[ri];
-            sample = rq.sample[ri];
+            const V3 o = {ldq(&rq.ox[ri]), ldq(&rq.oy[ri]), ldq(&rq.oz[ri])};
+            const V3 d = {ldq(&rq.dx[ri]), ldq(&rq.dy[ri]), ldq(&rq.dz[ri])};
+            const V3 T = {ldq(&rq.tr[ri]), ldq(&rq.tg[ri]), ldq(&rq.tb[ri])};
+            const float in_pdf = ldq(&rq.pdf[ri]);
+            pixel = ldq(&rq.pixel[ri]);
+            depth = ldq(&rq.depth[ri]);
+            sample = ldq(&rq.sample[ri]);
             slot = job_slot(J, pixel, sample);
             HitRec h;
-            rebuild_hit(S, o, d, hq.tri[hk], hq.t[hk], hq.bu[hk], hq.bv[hk], h);
+            rebuild_hit(S, o, d, ldq(&hq.tri[hk]), ldq(&hq.t[hk]), ldq(&hq.bu[hk]), ldq(&hq.bv[hk]), h);
             p = h.p;
             const wf_material m = S.materials[h.mat];
             V3 surf = {0, 0, 0};
@@ -739,50 +739,50 @@ __global__ void __launch_bounds__(128, WF_SHADE_MIN_BLOCKS) k_shade(DeviceScene 
         const int64_t pn = nx0 + __popc(mn & lt);
         if (want_area) {
             if (pa < sh.capacity) {
-                sh.ox[pa] = p.x; sh.oy[pa] = p.y; sh.oz[pa] = p.z;
-                sh.dx[pa] = dir_area.x; sh.dy[pa] = dir_area.y; sh.dz[pa] = dir_area.z;
-                sh.dist[pa] = dist_area;
-                sh.cr[pa] = c_area.x; sh.cg[pa] = c_area.y; sh.cb[pa] = c_area.z;
-                sh.pixel[pa] = slot;
-                sh.job[pa] = job;
+                stq(&sh.ox[pa], p.x); stq(&sh.oy[pa], p.y); stq(&sh.oz[pa], p.z);
+                stq(&sh.dx[pa], dir_area.x); stq(&sh.dy[pa], dir_area.y); stq(&sh.dz[pa], dir_area.z);
+                stq(&sh.dist[pa], dist_area);
+                stq(&sh.cr[pa], c_area.x); stq(&sh.cg[pa], c_area.y); stq(&sh.cb[pa], c_area.z);
+                stq(&sh.pixel[pa], slot);
+                stq(&sh.job[pa], job);
             } else {
                 atomicOr(err, 4);
             }
         }
         if (want_dir) {
             if (pd < sh.capacity) {
-                sh.ox[pd] = p.x; sh.oy[pd] = p.y; sh.oz[pd] = p.z;
-                sh.dx[pd] = dir_sun.x; sh.dy[pd] = dir_sun.y; sh.dz[pd] = dir_sun.z;
-                sh.dist[pd] = 1e6f;
-                sh.cr[pd] = c_sun.x; sh.cg[pd] = c_sun.y; sh.cb[pd] = c_sun.z;
-                sh.pixel[pd] = slot;
-                sh.job[pd] = job;
+                stq(&sh.ox[pd], p.x); stq(&sh.oy[pd], p.y); stq(&sh.oz[pd], p.z);
+                stq(&sh.dx[pd], dir_sun.x); stq(&sh.dy[pd], dir_sun.y); stq(&sh.dz[pd], dir_sun.z);
+                stq(&sh.dist[pd], 1e6f);
+                stq(&sh.cr[pd], c_sun.x); stq(&sh.cg[pd], c_sun.y); stq(&sh.cb[pd], c_sun.z);
+                stq(&sh.pixel[pd], slot);
+                stq(&sh.job[pd], job);
             } else {
                 atomicOr(err, 4);
             }
         }
         if (want_env) {
             if (pe < sh.capacity) {
-                sh.ox[pe] = p.x; sh.oy[pe] = p.y; sh.oz[pe] = p.z;
-                sh.dx[pe] = dir_env.x; sh.dy[pe] = dir_env.y; sh.dz[pe] = dir_env.z;
-                sh.dist[pe] = 1e6f;
-                sh.cr[pe] = c_env.x; sh.cg[pe] = c_env.y; sh.cb[pe] = c_env.z;
-                sh.pixel[pe] = slot;
-                sh.job[pe] = job;
+                stq(&sh.ox[pe], p.x); stq(&sh.oy[pe], p.y); stq(&sh.oz[pe], p.z);
+                stq(&sh.dx[pe], dir_env.x); stq(&sh.dy[pe], dir_env.y); stq(&sh.dz[pe], dir_env.z);
+                stq(&sh.dist[pe], 1e6f);
+                stq(&sh.cr[pe], c_env.x); stq(&sh.cg[pe], c_env.y); stq(&sh.cb[pe], c_env.z);
+                stq(&sh.pixel[pe], slot);
+                stq(&sh.job[pe], job);
             } else {
                 atomicOr(err, 4);
             }
         }
         if (want_next) {
             if (pn < nx.capacity) {
-                nx.ox[pn] = p.x; nx.oy[pn] = p.y; nx.oz[pn] = p.z;
-                nx.dx[pn] = nd.x; nx.dy[pn] = nd.y; nx.dz[pn] = nd.z;
-                nx.tr[pn] = Tn.x; nx.tg[pn] = Tn.y; nx.tb[pn] = Tn.z;
-                nx.pdf[pn] = next_pdf;
-                nx.pixel[pn] = pixel;
-                nx.depth[pn] = depth + 1;
-                nx.sample[pn] = sample;
-                nx.job[pn] = job;
+                stq(&nx.ox[pn], p.x); stq(&nx.oy[pn], p.y); stq(&nx.oz[pn], p.z);
+                stq(&nx.dx[pn], nd.x); stq(&nx.dy[pn], nd.y); stq(&nx.dz[pn], nd.z);
+                stq(&nx.tr[pn], Tn.x); stq(&nx.tg[pn], Tn.y); stq(&nx.tb[pn], Tn.z);
+                stq(&nx.pdf[pn], next_pdf);
+                stq(&nx.pixel[pn], pixel);
+                stq(&nx.depth[pn], depth + 1);
+                stq(&nx.sample[pn], sample);
+                stq(&nx.job[pn], job);
             } else {
                 atomicOr(err, 8);
             }
@@ -829,8 +829,8 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_occluded_render(DeviceScene
     for (;;) {
         if (ray >= 0 && tr.done()) {
             if (tr.res.leafpos < 0)  // sh.pixel holds the slot (job_slot)
-                accum_add(job_accum(kMulti ? jobs[job] : job0, accum), sh.pixel[ray],
-                          v3(sh.cr[ray], sh.cg[ray], sh.cb[ray]));
+                accum_add(job_accum(kMulti ? jobs[job] : job0, accum), ldq(&sh.pixel[ray]),
+                          v3(ldq(&sh.cr[ray]), ldq(&sh.cg[ray]), ldq(&sh.cb[ray])));
             overflow = overflow || tr.overflow;
             ray = -1;
         }
@@ -846,11 +846,11 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_occluded_render(DeviceScene
                 if (idx < n) {
                     ray = idx;
                     if (kMulti) {
-                        job = sh.job[idx];
+                        job = ldq(&sh.job[idx]);
                         S = scenes + jobs[job].scene;
                     }
-                    tr.init(*S, stack, v3(sh.ox[idx], sh.oy[idx], sh.oz[idx]),
-                            v3(sh.dx[idx], sh.dy[idx], sh.dz[idx]), 0.001f, sh.dist[idx] - 0.001f);
+                    tr.init(*S, stack, v3(ldq(&sh.ox[idx]), ldq(&sh.oy[idx]), ldq(&sh.oz[idx])),
+                            v3(ldq(&sh.dx[idx]), ldq(&sh.dy[idx]), ldq(&sh.dz[idx])), 0.001f, ldq(&sh.dist[idx]) - 0.001f);
                 } else {
                     exhausted = true;
                 }
