@@ -23,6 +23,11 @@ struct TraceResult {
     float t, bu, bv;
 };
 
+// Entry / exit distance of a slab test over three axes (an explicit
+// three-operand PTX min / max measured no faster than the nested pair).
+__device__ __forceinline__ float fmax3(float a, float b, float c) { return fmaxf(fmaxf(a, b), c); }
+__device__ __forceinline__ float fmin3(float a, float b, float c) { return fminf(fminf(a, b), c); }
+
 // Slab test of both children of a node; FMA form t = lo*inv - o*inv (the
 // padded boxes absorb the rounding difference).
 __device__ __forceinline__ void slab2(const BvhNode& nd, V3 inv, V3 oi, float tmin, float tmax,
@@ -34,10 +39,10 @@ __device__ __forceinline__ void slab2(const BvhNode& nd, V3 inv, V3 oi, float tm
     float lx1 = __fmaf_rn(nd.c1xy.x, inv.x, -oi.x), hx1 = __fmaf_rn(nd.c1xy.y, inv.x, -oi.x);
     float ly1 = __fmaf_rn(nd.c1xy.z, inv.y, -oi.y), hy1 = __fmaf_rn(nd.c1xy.w, inv.y, -oi.y);
     float lz1 = __fmaf_rn(nd.cz.z, inv.z, -oi.z), hz1 = __fmaf_rn(nd.cz.w, inv.z, -oi.z);
-    tn0 = fmaxf(fmaxf(fminf(lx0, hx0), fminf(ly0, hy0)), fmaxf(fminf(lz0, hz0), tmin));
-    float tf0 = fminf(fminf(fmaxf(lx0, hx0), fmaxf(ly0, hy0)), fminf(fmaxf(lz0, hz0), tmax));
-    tn1 = fmaxf(fmaxf(fminf(lx1, hx1), fminf(ly1, hy1)), fmaxf(fminf(lz1, hz1), tmin));
-    float tf1 = fminf(fminf(fmaxf(lx1, hx1), fmaxf(ly1, hy1)), fminf(fmaxf(lz1, hz1), tmax));
+    tn0 = fmax3(fminf(lx0, hx0), fminf(ly0, hy0), fmaxf(fminf(lz0, hz0), tmin));
+    float tf0 = fmin3(fmaxf(lx0, hx0), fmaxf(ly0, hy0), fminf(fmaxf(lz0, hz0), tmax));
+    tn1 = fmax3(fminf(lx1, hx1), fminf(ly1, hy1), fmaxf(fminf(lz1, hz1), tmin));
+    float tf1 = fmin3(fmaxf(lx1, hx1), fmaxf(ly1, hy1), fminf(fmaxf(lz1, hz1), tmax));
     h0 = tn0 <= tf0;
     h1 = tn1 <= tf1;
 }
@@ -76,6 +81,7 @@ struct Traversal {
     float tmin, best_t;
     int best_g;
     uint32_t cur;
+    uint32_t top;  // the entry the next pop returns (binary traversal)
     int sp;
     bool overflow;
     bool speculative = false;
@@ -98,11 +104,36 @@ struct Traversal {
         res.leafpos = -1;
         sp = 0;
         stack[sp++] = kSentinel;
+        top = kSentinel;
         cur = S.root_is_empty ? kSentinel : 0u;
         overflow = false;
     }
     __device__ __forceinline__ bool done() const { return cur == kSentinel; }
     __device__ __forceinline__ void idle() { cur = kSentinel; }
+
+    // Binary-traversal stack with its top entry in a register: entries
+    // 0 .. sp-2 are in memory, entry sp-1 is `top`.  A pop returns the
+    // register at once and reloads `top` for the pop after it, so the next
+    // node fetch never waits on a local-memory load.
+    template <class Stk>
+    __device__ __forceinline__ void push(Stk stack, uint32_t e)
+    {
+        if (sp < kStackSize) {
+            stack[sp - 1] = top;
+            top = e;
+            ++sp;
+        } else {
+            overflow = true;
+        }
+    }
+    template <class Stk>
+    __device__ __forceinline__ uint32_t pop(Stk stack)
+    {
+        const uint32_t r = top;
+        --sp;
+        top = sp > 0 ? stack[sp - 1] : kSentinel;
+        return r;
+    }
     template <class Stk>
     __device__ __forceinline__ void round(const DeviceScene& S, Stk stack)
     {
@@ -112,9 +143,9 @@ struct Traversal {
     // With the top of the tree staged in shared memory: nodes [0, ntop)
     // (the root and the last clustering passes' nodes) come from `top`.
     template <class Stk>
-    __device__ __forceinline__ void round(const DeviceScene& S, Stk stack, const BvhNode* top, uint32_t ntop)
+    __device__ __forceinline__ void round(const DeviceScene& S, Stk stack, const BvhNode* staged, uint32_t ntop)
     {
-        top_nodes = top;
+        top_nodes = staged;
         num_top = ntop;
         round(S.nodes, S.tris, stack);
     }
@@ -139,19 +170,16 @@ struct Traversal {
                     const bool swap = child_order_swap(nd, tn0, tn1);
                     const uint32_t farc = swap ? c0 : c1;
                     cur = swap ? c1 : c0;
-                    if (sp < kStackSize)
-                        stack[sp++] = farc;
-                    else
-                        overflow = true;
+                    push(stack, farc);
                 } else if (h0 || h1) {
                     cur = h0 ? c0 : c1;
                 } else {
-                    cur = stack[--sp];
+                    cur = pop(stack);
                 }
             }
             while (cur != kSentinel && (cur & kLeafFlag)) {
                 const uint32_t leaf = cur;
-                cur = stack[--sp];
+                cur = pop(stack);
                 if (test_leaf(tris, leaf)) {
                     cur = kSentinel;
                     return;
@@ -176,19 +204,16 @@ struct Traversal {
                     const bool swap = child_order_swap(nd, tn0, tn1);
                     const uint32_t farc = swap ? c0 : c1;
                     cur = swap ? c1 : c0;
-                    if (sp < kStackSize)
-                        stack[sp++] = farc;
-                    else
-                        overflow = true;
+                    push(stack, farc);
                 } else if (h0 || h1) {
                     cur = h0 ? c0 : c1;
                 } else {
-                    cur = stack[--sp];
+                    cur = pop(stack);
                 }
             }
             if (postponed == 0u && cur != kSentinel && (cur & kLeafFlag)) {
                 postponed = cur;
-                cur = stack[--sp];
+                cur = pop(stack);
             }
             if (!__any_sync(active, postponed == 0u && cur != kSentinel)) break;
         }
@@ -198,7 +223,7 @@ struct Traversal {
         }
         while (cur != kSentinel && (cur & kLeafFlag)) {
             const uint32_t leaf = cur;
-            cur = stack[--sp];
+            cur = pop(stack);
             if (test_leaf(tris, leaf)) {
                 cur = kSentinel;
                 return;
@@ -282,8 +307,8 @@ struct Traversal4 : Traversal<kAnyHit> {
         const float tlx = __fmaf_rn(lx, this->inv.x, -this->oi.x), thx = __fmaf_rn(hx, this->inv.x, -this->oi.x);
         const float tly = __fmaf_rn(ly, this->inv.y, -this->oi.y), thy = __fmaf_rn(hy, this->inv.y, -this->oi.y);
         const float tlz = __fmaf_rn(lz, this->inv.z, -this->oi.z), thz = __fmaf_rn(hz, this->inv.z, -this->oi.z);
-        const float tn = fmaxf(fmaxf(fminf(tlx, thx), fminf(tly, thy)), fmaxf(fminf(tlz, thz), this->tmin));
-        const float tf = fminf(fminf(fmaxf(tlx, thx), fmaxf(tly, thy)), fminf(fmaxf(tlz, thz), this->best_t));
+        const float tn = fmax3(fminf(tlx, thx), fminf(tly, thy), fmaxf(fminf(tlz, thz), this->tmin));
+        const float tf = fmin3(fmaxf(tlx, thx), fmaxf(tly, thy), fminf(fmaxf(tlz, thz), this->best_t));
         // tn >= tmin: for tmin >= 0 the bits order like the distances (the
         // order only steers the walk, never the result)
         return (tn <= tf && (uint32_t)kid != kEmptyChild4) ? ((__float_as_uint(tn) & ~3u) | slot) : 0xFFFFFFFFu;
@@ -479,8 +504,8 @@ struct WideTraversal {
             const float tlx = __fmaf_rn(lx, inv.x, -oi.x), thx = __fmaf_rn(hx, inv.x, -oi.x);
             const float tly = __fmaf_rn(ly, inv.y, -oi.y), thy = __fmaf_rn(hy, inv.y, -oi.y);
             const float tlz = __fmaf_rn(lz, inv.z, -oi.z), thz = __fmaf_rn(hz, inv.z, -oi.z);
-            const float tn = fmaxf(fmaxf(fminf(tlx, thx), fminf(tly, thy)), fmaxf(fminf(tlz, thz), tmin));
-            const float tf = fminf(fminf(fmaxf(tlx, thx), fmaxf(tly, thy)), fminf(fmaxf(tlz, thz), best_t));
+            const float tn = fmax3(fminf(tlx, thx), fminf(tly, thy), fmaxf(fminf(tlz, thz), tmin));
+            const float tf = fmin3(fmaxf(tlx, thx), fmaxf(tly, thy), fminf(fmaxf(tlz, thz), best_t));
             if (m != 0u && tn <= tf) {
                 if ((m & 0x1Fu) >= 24u)
                     hits_i |= 1u << (24u + ((uint32_t)s ^ octinv));
