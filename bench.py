@@ -258,12 +258,13 @@ def run_batched(args) -> int:
     pkg = load_pkg()
     ctx = pkg.Context(local)
     jobs = c3_jobs(pkg, ctx, args.jobs, seed=2026)
-    ctx.set_tuning(graph_mode=0)
+    tv = max(args.trace_variant, 0)
+    ctx.set_tuning(tv, graph_mode=0)
     ctx.render_batch(jobs[:16], want_images=False)  # warm-up (captures the graph)
-    ctx.set_tuning(graph_mode=2)
+    ctx.set_tuning(tv, graph_mode=2)
     ctx.render_batch(jobs[:4], want_images=False)
     # plain loop: one job per render, host round trip per bounce
-    ctx.set_tuning(graph_mode=2)
+    ctx.set_tuning(tv, graph_mode=2)
     ctx.timer_begin()
     plain_rays = 0
     for j in jobs:
@@ -271,7 +272,7 @@ def run_batched(args) -> int:
         plain_rays += st["closest_rays"] + st["shadow_rays"]
     plain_ms = ctx.timer_end()
     # batched: one call, waves shared by all jobs, graph replay
-    ctx.set_tuning(graph_mode=0)
+    ctx.set_tuning(tv, graph_mode=0)
     ctx.timer_begin()
     _, st = ctx.render_batch(jobs, want_images=False)
     ms = ctx.timer_end()
@@ -309,6 +310,7 @@ def run_serving(args) -> int:
     for k in range(16):
         hs = pkg.HostScene(3, seed=k)
         scenes.append((ctx.add_scene(hs.desc), hs))
+    ctx.set_tuning(max(args.trace_variant, 0))
     srv = pkg.Server(ctx, hbm_budget_bytes=int(args.budget_gb * (1 << 30)), frame_spp=8)
     # warm-up: one small job per scene kind
     for sid, hs in scenes[:3]:
@@ -339,7 +341,11 @@ def run_serving(args) -> int:
             ids.append(srv.submit(arrivals[k][1]))
             k += 1
         if now > t_end:
-            break
+            # after the last arrival, optionally keep serving until every
+            # submitted job is done (so the latency percentiles cover all jobs)
+            terminal = (pkg.JOB_DONE, pkg.JOB_REJECTED, pkg.JOB_CANCELLED)
+            if now > t_end + args.drain or all(srv.status(i)["state"] in terminal for i in ids):
+                break
         info = srv.step()
         rays += info["rays_traced"]
         dev_ms += info["step_ms"]
@@ -351,7 +357,7 @@ def run_serving(args) -> int:
         "metric": METRIC, "value": rays / wall / 1e6, "unit": "Mrays/s", "n_gpus": world, "steps": 1,
         "warmup": 1, "ms_per_step": wall * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "c4_serving_poisson", "rate_per_s": lam, "duration_s": t_end,
+        "config": {"workload": "c4_serving_poisson", "rate_per_s": lam, "duration_s": t_end, "drain_s": args.drain,
                    "hbm_budget_gb": args.budget_gb, "frame_spp": 8,
                    "scenes": "config 0, config 1 (1.31 M tris), 16 config-3 variants"},
         "device_busy_mrays_per_s": rays / (dev_ms / 1e3) / 1e6 if dev_ms else None,
@@ -378,6 +384,8 @@ def main() -> int:
     ap.add_argument("--duration", type=float, default=20.0, help="config 4: seconds of arrivals")
     ap.add_argument("--rate", type=float, default=200.0, help="config 4: arrivals per second")
     ap.add_argument("--budget-gb", type=float, default=60.0, help="config 4: HBM budget")
+    ap.add_argument("--drain", type=float, default=0.0,
+                    help="config 4: seconds to keep serving after the last arrival until all jobs are done")
     ap.add_argument("--policy", default="none", choices=["none", "material", "texture", "costBenefit"])
     ap.add_argument("--ray-sort", type=int, default=0)
     ap.add_argument("--env-nee", type=int, default=0, help="environment NEE + MIS (same mean, lower variance)")
