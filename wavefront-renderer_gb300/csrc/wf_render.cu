@@ -1336,15 +1336,32 @@ void launch_camera_chunks(const WaveChunk* chunks, const long long* header, cons
 
 void launch_tally(const ull* counters, ull* tally, cudaStream_t s) { k_tally<<<1, 1, 0, s>>>(counters, tally); }
 
+int shade_blocks_per_sm()
+{
+    int a = 0, b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_shade<false>, 128, 0) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_shade<true>, 128, 0) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    const int m = a < b ? a : b;
+    return m > 0 ? m : 1;
+}
+
+// k_shade walks the hit list with a block-stride loop, every block taking an
+// equal share; its grid is therefore one full wave of resident blocks.  A grid
+// that is not a multiple of them (16 blocks per SM against 6 resident: 2.67
+// waves) leaves a partial last wave whose blocks start late and end late.
 void launch_shade(const WaveTables& t, RayQueueDev rq, HitQueueDev hq, const ull* hq_n, ShadowQueueDev sh,
                   ull* sh_n, RayQueueDev next, ull* next_n, float* accum, int* err, LaunchCfg cfg, cudaStream_t s)
 {
+    const int grid = cfg.shade_grid > 0 ? cfg.shade_grid : cfg.grid;
     if (t.multi)
-        k_shade<true><<<cfg.grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, hq, hq_n, cfg.ray_order, sh,
-                                               sh_n, next, next_n, accum, err);
+        k_shade<true><<<grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, hq, hq_n, cfg.ray_order, sh,
+                                           sh_n, next, next_n, accum, err);
     else
-        k_shade<false><<<cfg.grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, hq, hq_n, cfg.ray_order, sh,
-                                                sh_n, next, next_n, accum, err);
+        k_shade<false><<<grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, hq, hq_n, cfg.ray_order, sh,
+                                            sh_n, next, next_n, accum, err);
 }
 
 void launch_compact_hits(const ull* d_n, HitQueueDev hq, ull* hq_n, LaunchCfg cfg, cudaStream_t s)
