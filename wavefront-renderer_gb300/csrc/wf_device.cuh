@@ -535,28 +535,26 @@ __device__ __forceinline__ V3 cosine_sample_hemisphere(V3 n, Stream& rng)
     return normalized(tangent * x + n * y + bitangent * z);
 }
 
-// Material::scatter, src/shading/Material.cpp:165-266.
-__device__ __forceinline__ bool scatter(const DeviceScene& S, const wf_material& m, V3 in_dir,
-                                        const HitRec& h, Stream& rng, V3& att, V3& out_dir,
-                                        float& pdf)
+// Material::scatter, src/shading/Material.cpp:165-266.  The diffuse and
+// plastic cases share one cosine-lobe sampler and the metal and plastic
+// cases one fuzzy-mirror sampler (one inlined copy of each in k_shade); the
+// operations and the order of the random draws are the reference's.
+__device__ __forceinline__ bool scatter(const wf_material& m, V3 surf, V3 in_dir, const HitRec& h, Stream& rng,
+                                        V3& att, V3& out_dir, float& pdf)
 {
-    V3 surf = surface_color(S, m, h);
+    bool cosine_lobe = false;  // else the fuzzy mirror around `mirror`
+    bool must_leave = false;   // metal: absorbed when the fuzzed ray points into the surface
+    V3 mirror = {0.0f, 0.0f, 0.0f};
     switch (m.type) {
-    case WF_MATERIAL_DIFFUSE: {
-        V3 d = cosine_sample_hemisphere(h.n, rng);
-        out_dir = d;
+    case WF_MATERIAL_DIFFUSE:
+        cosine_lobe = true;
         att = surf;
-        pdf = fmaxf(0.0f, dot(h.n, d)) / kPi;
-        return true;
-    }
-    case WF_MATERIAL_METAL: {
-        V3 r = reflect(in_dir, h.n);
-        V3 fuzz = random_in_unit_sphere(rng) * m.roughness;
-        out_dir = normalized(r + fuzz);
+        break;
+    case WF_MATERIAL_METAL:
+        mirror = reflect(in_dir, h.n);
+        must_leave = true;
         att = surf;
-        pdf = -1.0f;
-        return dot(out_dir, h.n) > 0.0f;
-    }
+        break;
     case WF_MATERIAL_EMISSIVE:
     case WF_MATERIAL_SPOTLIGHT:
         att = surf * m.emission;
@@ -580,23 +578,28 @@ __device__ __forceinline__ bool scatter(const DeviceScene& S, const wf_material&
         float c = fmaxf(0.0f, dot(in_dir * -1.0f, h.n));
         float refl = schlick(c, 1.5f);
         if (rng.next() < refl) {
-            V3 r = reflect(normalized(in_dir), h.n);
-            V3 fuzz = random_in_unit_sphere(rng) * m.roughness;
-            out_dir = normalized(r + fuzz);
+            mirror = reflect(normalized(in_dir), h.n);
             att = v3(1.0f, 1.0f, 1.0f);
-            pdf = -1.0f;
         } else {
-            V3 d = cosine_sample_hemisphere(h.n, rng);
-            out_dir = d;
+            cosine_lobe = true;
             att = surf;
-            pdf = fmaxf(0.0f, dot(h.n, d)) / kPi;
         }
-        return true;
+        break;
     }
     default:
         pdf = -1.0f;
         return false;
     }
+    if (cosine_lobe) {
+        V3 d = cosine_sample_hemisphere(h.n, rng);
+        out_dir = d;
+        pdf = fmaxf(0.0f, dot(h.n, d)) / kPi;
+        return true;
+    }
+    V3 fuzz = random_in_unit_sphere(rng) * m.roughness;
+    out_dir = normalized(mirror + fuzz);
+    pdf = -1.0f;
+    return must_leave ? dot(out_dir, h.n) > 0.0f : true;
 }
 
 // MIS helpers, include/shading/MIS.h:6-32.

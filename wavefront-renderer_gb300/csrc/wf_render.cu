@@ -496,7 +496,9 @@ constexpr int kShadeWarps = 4;  // k_shade runs 128-thread blocks
 #ifndef WF_SHADE_MIN_BLOCKS
 #define WF_SHADE_MIN_BLOCKS 6  // 80 registers, 6 resident blocks (91 / 5 unbounded): +2%
 #endif
-template <bool kMulti>
+// kTimed: the live CostTracker times a quarter of the hits (single-job
+// renders only); the other instances carry no clock reads.
+template <bool kMulti, bool kTimed>
 __global__ void __launch_bounds__(128, WF_SHADE_MIN_BLOCKS) k_shade(DeviceScene scene0, DeviceJob job0,
                                                const DeviceScene* __restrict__ scenes,
                                                const DeviceJob* __restrict__ jobs, RayQueueDev rq,
@@ -541,24 +543,29 @@ __global__ void __launch_bounds__(128, WF_SHADE_MIN_BLOCKS) k_shade(DeviceScene 
             rebuild_hit(S, o, d, ldq(&hq.tri[hk]), ldq(&hq.t[hk]), ldq(&hq.bu[hk]), ldq(&hq.bv[hk]), h);
             p = h.p;
             const wf_material m = S.materials[h.mat];
-            V3 surf = {0, 0, 0};
-            bool have_surf = false;
             // Live cost tracking (.cpp:612-625): a quarter of the hits time
             // their surface colour lookup (textured materials) and their
             // scatter with the SM clock.
             bool timed = false;
-            if (!kMulti && J.cost_sum_mat) {
+            if (kTimed && !kMulti && J.cost_sum_mat) {
                 Stream cs(seed_lo, seed_hi, kPurposeCostSample, (uint32_t)depth, (uint32_t)pixel,
                           (uint32_t)sample);
                 timed = cs.next() < 0.25f;
             }
-            if (timed && m.texture_id >= 0) {
-                const long long t0 = clock64();
-                surf = surface_color(S, m, h);
-                const long long t1 = clock64();
-                have_surf = true;
-                cost_tex = m.texture_id;
-                cyc_tex = (unsigned)min(t1 - t0, (long long)(1 << 26));
+            // Material::getSurfaceColor, evaluated once per hit: scatter
+            // (which starts with it, Material.cpp:165-169) and every NEE term
+            // use the same value of this pure lookup.  A timed hit charges
+            // its cycles to the texture and, as part of scatter, to the
+            // material, as the reference's two timers do.
+            const long long tc0 = timed ? clock64() : 0;
+            const V3 surf = surface_color(S, m, h);
+            unsigned cyc_surf = 0;
+            if (timed) {
+                cyc_surf = (unsigned)min(clock64() - tc0, (long long)(1 << 26));
+                if (m.texture_id >= 0) {
+                    cost_tex = m.texture_id;
+                    cyc_tex = cyc_surf;
+                }
             }
             // Emission with MIS (.cpp:629-658)
             V3 Le = emitted(m, h.n, d * -1.0f);
@@ -604,8 +611,6 @@ __global__ void __launch_bounds__(128, WF_SHADE_MIN_BLOCKS) k_shade(DeviceScene 
                     const float cos_s = dot(h.n, dl);
                     const float cos_l = dot(dl * -1.0f, ln);
                     if (cos_s > 0.0f && cos_l > 0.0f) {
-                        surf = surface_color(S, m, h);
-                        have_surf = true;
                         const float g = (cos_s * cos_l) / (dist * dist);
                         const V3 brdf = surf * (1.0f / kPi);
                         const float lp = area_to_angle(S.light_area_pdf, dist, cos_l);
@@ -625,8 +630,6 @@ __global__ void __launch_bounds__(128, WF_SHADE_MIN_BLOCKS) k_shade(DeviceScene 
                                  S.directional.direction[2]) * -1.0f;
                 const float cos_s = dot(h.n, to);
                 if (cos_s > 0.0f) {
-                    if (!have_surf) surf = surface_color(S, m, h);
-                    have_surf = true;
                     const V3 brdf = surf * (1.0f / kPi);
                     const V3 col = {S.directional.color[0], S.directional.color[1], S.directional.color[2]};
                     const V3 direct = T * brdf * col * S.directional.intensity * cos_s;
@@ -655,8 +658,6 @@ __global__ void __launch_bounds__(128, WF_SHADE_MIN_BLOCKS) k_shade(DeviceScene 
                 const float cos_s = dot(h.n, wi);
                 const float pe = env_pdf(S, wi);
                 if (cos_s > 0.0f && pe > 0.0f) {
-                    if (!have_surf) surf = surface_color(S, m, h);
-                    have_surf = true;
                     float kd = 1.0f;
                     if (m.type == WF_MATERIAL_PLASTIC)
                         kd = 1.0f - schlick(fmaxf(0.0f, dot(d * -1.0f, h.n)), 1.5f);
@@ -672,10 +673,10 @@ __global__ void __launch_bounds__(128, WF_SHADE_MIN_BLOCKS) k_shade(DeviceScene 
             V3 att;
             float spdf;
             const long long ts0 = timed ? clock64() : 0;
-            const bool scattered = scatter(S, m, d, h, sr, att, nd, spdf);
+            const bool scattered = scatter(m, surf, d, h, sr, att, nd, spdf);
             if (timed) {
                 cost_mat = h.mat;
-                cyc_mat = (unsigned)min(clock64() - ts0, (long long)(1 << 26));
+                cyc_mat = (unsigned)min(clock64() - ts0 + (long long)cyc_surf, (long long)(1 << 26));
             }
             if (scattered) {
                 Tn = T * att;
@@ -701,7 +702,7 @@ __global__ void __launch_bounds__(128, WF_SHADE_MIN_BLOCKS) k_shade(DeviceScene 
             }
         }
         __syncwarp();
-        if (!kMulti && job0.cost_sum_mat) {
+        if (kTimed && !kMulti && job0.cost_sum_mat) {
             warp_cost_add(job0.cost_sum_mat, job0.cost_cnt_mat, cost_mat, cyc_mat);
             warp_cost_add(job0.cost_sum_tex, job0.cost_cnt_tex, cost_tex, cyc_tex);
         }
@@ -1338,13 +1339,15 @@ void launch_tally(const ull* counters, ull* tally, cudaStream_t s) { k_tally<<<1
 
 int shade_blocks_per_sm()
 {
-    int a = 0, b = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_shade<false>, 128, 0) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_shade<true>, 128, 0) != cudaSuccess) {
+    int a = 0, b = 0, c = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_shade<false, false>, 128, 0) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_shade<true, false>, 128, 0) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_shade<false, true>, 128, 0) != cudaSuccess) {
         cudaGetLastError();
         return 0;
     }
-    const int m = a < b ? a : b;
+    int m = a < b ? a : b;
+    m = m < c ? m : c;
     return m > 0 ? m : 1;
 }
 
@@ -1357,11 +1360,14 @@ void launch_shade(const WaveTables& t, RayQueueDev rq, HitQueueDev hq, const ull
 {
     const int grid = cfg.shade_grid > 0 ? cfg.shade_grid : cfg.grid;
     if (t.multi)
-        k_shade<true><<<grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, hq, hq_n, cfg.ray_order, sh,
-                                           sh_n, next, next_n, accum, err);
+        k_shade<true, false><<<grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, hq, hq_n, cfg.ray_order,
+                                                  sh, sh_n, next, next_n, accum, err);
+    else if (t.job0.cost_sum_mat)
+        k_shade<false, true><<<grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, hq, hq_n, cfg.ray_order,
+                                                  sh, sh_n, next, next_n, accum, err);
     else
-        k_shade<false><<<grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, hq, hq_n, cfg.ray_order, sh,
-                                            sh_n, next, next_n, accum, err);
+        k_shade<false, false><<<grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, hq, hq_n, cfg.ray_order,
+                                                   sh, sh_n, next, next_n, accum, err);
 }
 
 void launch_compact_hits(const ull* d_n, HitQueueDev hq, ull* hq_n, LaunchCfg cfg, cudaStream_t s)
