@@ -476,12 +476,14 @@ def test_gpu_env_nee_matches_oracle_paths(wf, orc, ctx, scene_c2small):
 
 # ------------------------------------------------ adaptive sampling --------
 
-@pytest.mark.parametrize("spw", [0, 4])
+@pytest.mark.parametrize("spw", [0, 4, 16])
 def test_gpu_adaptive_matches_oracle(wf, orc, ctx, scene0, spw):
     """AdaptiveSampler on the GPU: each pixel's sample count and image equal
     the port's (same random streams; the Welford inputs differ only by the
     order of float additions, so a stop may move by one check on a few
-    pixels).  Tolerance: counts equal on 99% of pixels, image within 1e-3
+    pixels).  spw 0 runs samples 0-31 as one wave and then waves of 16 (the
+    per-sample slots of a 32-slot buffer used from slot 16 on alternate
+    waves); 4 and 16 run fixed waves.  Tolerance: counts equal on 99% of pixels, image within 1e-3
     relative + 1e-4 on 98%."""
     ctx.upload(scene0.desc)
     port = orc.Port(scene0.desc)

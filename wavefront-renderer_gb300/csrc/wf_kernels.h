@@ -129,10 +129,13 @@ void launch_permute_hits(HitQueueDev in, const uint32_t* perm, const ull* d_n, H
 void launch_finalize(const float* accum, int64_t nfloats, float spp, float* image, cudaStream_t s);
 
 // Adaptive sampling: fold a wave's per-sample sums into the pixel sums and
-// Welford statistics; mark converged pixels; list the active ones in index
-// order; divide by per-pixel sample counts; fill an int array (or iota).
-void launch_adaptive_fold(float* sample_buf, int64_t np, int nspp, float* accum, float* mean, float* m2,
-                          int32_t* count, const int32_t* active, int32_t n_active, cudaStream_t s);
+// Welford statistics (the wave's samples sit in slots slot0, slot0+1, ...
+// modulo wave_spp of the per-sample buffer); mark converged pixels; list the
+// active ones in index order; divide by per-pixel sample counts; fill an int
+// array (or iota).
+void launch_adaptive_fold(float* sample_buf, int64_t np, int nspp, int slot0, int wave_spp, float* accum,
+                          float* mean, float* m2, int32_t* count, const int32_t* active, int32_t n_active,
+                          cudaStream_t s);
 void launch_adaptive_check(const float* mean, const float* m2, const int32_t* count, const int32_t* active,
                            int32_t n_active, float threshold, int32_t* flag, cudaStream_t s);
 void launch_compact_active(const int32_t* flag, int64_t np, int32_t* pos, int32_t* block_sums, int32_t* out,

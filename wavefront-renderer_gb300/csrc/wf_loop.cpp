@@ -387,9 +387,9 @@ int render_single(wf_ctx* c, const wf_render_params* P, wf_render_stats* st)
     int spw = P->spp_per_wave > 0 ? P->spp_per_wave : (int)std::max<int64_t>(1, c->paths_per_wave / np);
     spw = std::max(1, std::min(spw, P->samples_per_pixel));
     const bool adaptive = P->enable_adaptive_sampling != 0;
-    if (adaptive) {  // waves end on the convergence checks (every 16th sample)
+    if (adaptive) {  // waves end on the convergence checks: sample 32, then every 16th
         int p2 = 1;
-        while (p2 * 2 <= std::min(spw, 16)) p2 *= 2;
+        while (p2 * 2 <= std::min(spw, 32) && np * (p2 * 2) <= (int64_t)INT32_MAX) p2 *= 2;
         spw = p2;
     }
     int rc = ensure_render_buffers(c, np * spw);
@@ -460,8 +460,12 @@ int render_single(wf_ctx* c, const wf_render_params* P, wf_render_stats* st)
     int32_t n_active = (int32_t)np;
     int samples_run = P->samples_per_pixel;
     WF_CK(c, cudaEventRecord(c->ev[0], s));
-    for (int s0 = 0; s0 < P->samples_per_pixel; s0 += spw) {
-        const int nspp = std::min(spw, P->samples_per_pixel - s0);
+    for (int s0 = 0, nspp = 0; s0 < P->samples_per_pixel; s0 += nspp) {
+        nspp = std::min(spw, P->samples_per_pixel - s0);
+        if (adaptive) {  // no wave crosses a check (AdaptiveSampler: from 32 samples, every 16)
+            const int next_check = s0 < 32 ? 32 : (s0 / 16 + 1) * 16;
+            nspp = std::min(nspp, next_check - s0);
+        }
         const int64_t pix = adaptive ? (int64_t)n_active : np;
         std::vector<WaveChunk> ch(1);
         ch[0] = WaveChunk{0, P->first_sample + s0, nspp, adaptive ? n_active : 0, 0};
@@ -472,8 +476,8 @@ int render_single(wf_ctx* c, const wf_render_params* P, wf_render_stats* st)
                                P->rel_cost_material, P->rel_cost_texture, &table[0], stats, tracking, nspp);
         if (rc) return rc;
         if (adaptive) {  // renderScene's per-sample adaptive block (.cpp:270-294)
-            launch_adaptive_fold(c->ad_buf, np, nspp, c->arena, c->ad_mean, c->ad_m2, c->ad_count, c->ad_active,
-                                 n_active, s);
+            launch_adaptive_fold(c->ad_buf, np, nspp, s0 % spw, spw, c->arena, c->ad_mean, c->ad_m2, c->ad_count,
+                                 c->ad_active, n_active, s);
             stats.kernel_launches += 1;
             if ((s0 + nspp) % 16 == 0) {
                 launch_adaptive_check(c->ad_mean, c->ad_m2, c->ad_count, c->ad_active, n_active,

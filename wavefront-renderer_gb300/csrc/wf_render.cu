@@ -1184,9 +1184,9 @@ __global__ void k_finalize(const float* accum, int64_t n, float spp, float* imag
 // After a wave: every sample of every active pixel, in sample order, is added
 // to the pixel sum and luminance(sum after - sum before) goes to Welford's
 // update (AdaptiveSampler::addSample, :41-53); the slot is cleared.
-__global__ void k_adaptive_fold(float* __restrict__ sample_buf, int64_t np, int nspp, float* __restrict__ accum,
-                                float* __restrict__ mean, float* __restrict__ m2, int32_t* __restrict__ count,
-                                const int32_t* __restrict__ active, int32_t n_active)
+__global__ void k_adaptive_fold(float* __restrict__ sample_buf, int64_t np, int nspp, int slot0, int wave_spp,
+                                float* __restrict__ accum, float* __restrict__ mean, float* __restrict__ m2,
+                                int32_t* __restrict__ count, const int32_t* __restrict__ active, int32_t n_active)
 {
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n_active;
          r += (int64_t)gridDim.x * blockDim.x) {
@@ -1195,7 +1195,7 @@ __global__ void k_adaptive_fold(float* __restrict__ sample_buf, int64_t np, int 
         float mu = mean[p], M2 = m2[p];
         int n = count[p];
         for (int k = 0; k < nspp; ++k) {
-            float* b = sample_buf + 3 * ((int64_t)k * np + p);
+            float* b = sample_buf + 3 * ((int64_t)((slot0 + k) % wave_spp) * np + p);
             const float nr = ar + b[0], ng = ag + b[1], nb = ab + b[2];
             b[0] = 0.0f;
             b[1] = 0.0f;
@@ -1482,12 +1482,13 @@ void launch_cost_update(const CostTrackerDev& mat, const CostTrackerDev& tex, in
     k_cost_update<<<2, 32, 0, s>>>(mat, tex, repeat);
 }
 
-void launch_adaptive_fold(float* sample_buf, int64_t np, int nspp, float* accum, float* mean, float* m2,
-                          int32_t* count, const int32_t* active, int32_t n_active, cudaStream_t s)
+void launch_adaptive_fold(float* sample_buf, int64_t np, int nspp, int slot0, int wave_spp, float* accum,
+                          float* mean, float* m2, int32_t* count, const int32_t* active, int32_t n_active,
+                          cudaStream_t s)
 {
     if (n_active <= 0) return;
-    k_adaptive_fold<<<grid_for(n_active, 256, 65535), 256, 0, s>>>(sample_buf, np, nspp, accum, mean, m2, count,
-                                                                   active, n_active);
+    k_adaptive_fold<<<grid_for(n_active, 256, 65535), 256, 0, s>>>(sample_buf, np, nspp, slot0, wave_spp, accum,
+                                                                   mean, m2, count, active, n_active);
 }
 
 void launch_adaptive_check(const float* mean, const float* m2, const int32_t* count, const int32_t* active,
