@@ -25,12 +25,14 @@ struct LaunchCfg {
     int variant = 0;   // kernel variant (traversal occupancy hint / stack placement)
     int speculative = 0;  // 1 = speculative while-while traversal
     int ray_order = 0;    // 1 = hit records at their rays' indices, listed by k_compact_hits
-    int shade_grid = 0;   // k_shade's grid (one full wave of resident blocks); 0 = grid
+    int shade_grid = 0;        // k_shade's grid (one full wave of resident blocks); 0 = grid
+    int shade_grid_other = 0;  // the same for its multi-job and cost-timed forms
 };
 
-// Resident blocks of 128 threads per SM of k_shade (the smaller of its
-// single-job and multi-job forms), from the occupancy calculator.
-int shade_blocks_per_sm();
+// Resident blocks of 128 threads per SM of k_shade from the occupancy
+// calculator: the plain single-job form (plain = true) or the smaller of the
+// multi-job and cost-timed forms.
+int shade_blocks_per_sm(bool plain);
 
 // Camera rays of n = width*height*nspp paths, sample-major.
 void launch_camera(const wf_camera& cam, int width, int height, uint32_t seed_lo, uint32_t seed_hi,

@@ -493,13 +493,20 @@ __global__ void k_cost_update(CostTrackerDev mat, CostTrackerDev tex, int repeat
 // sample) — the oracle uses the same ones.
 // ---------------------------------------------------------------------------
 constexpr int kShadeWarps = 4;  // k_shade runs 128-thread blocks
+// Resident blocks of k_shade per SM: the multi-job and cost-timed instances,
+// and the plain single-job instance, each bounded where it still compiles
+// without spills.
 #ifndef WF_SHADE_MIN_BLOCKS
-#define WF_SHADE_MIN_BLOCKS 6  // 80 registers, 6 resident blocks (91 / 5 unbounded): +2%
+#define WF_SHADE_MIN_BLOCKS 7
+#endif
+#ifndef WF_SHADE_MIN_BLOCKS_PLAIN
+#define WF_SHADE_MIN_BLOCKS_PLAIN 8
 #endif
 // kTimed: the live CostTracker times a quarter of the hits (single-job
 // renders only); the other instances carry no clock reads.
 template <bool kMulti, bool kTimed>
-__global__ void __launch_bounds__(128, WF_SHADE_MIN_BLOCKS) k_shade(DeviceScene scene0, DeviceJob job0,
+__global__ void __launch_bounds__(128, (kMulti || kTimed) ? WF_SHADE_MIN_BLOCKS : WF_SHADE_MIN_BLOCKS_PLAIN)
+    k_shade(DeviceScene scene0, DeviceJob job0,
                                                const DeviceScene* __restrict__ scenes,
                                                const DeviceJob* __restrict__ jobs, RayQueueDev rq,
                                                HitQueueDev hq, const ull* __restrict__ hq_n, int ray_order,
@@ -1337,17 +1344,17 @@ void launch_camera_chunks(const WaveChunk* chunks, const long long* header, cons
 
 void launch_tally(const ull* counters, ull* tally, cudaStream_t s) { k_tally<<<1, 1, 0, s>>>(counters, tally); }
 
-int shade_blocks_per_sm()
+int shade_blocks_per_sm(bool plain)
 {
-    int a = 0, b = 0, c = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_shade<false, false>, 128, 0) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_shade<true, false>, 128, 0) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_shade<false, true>, 128, 0) != cudaSuccess) {
+    int a = 0, b = 0;
+    cudaError_t e = plain ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_shade<false, false>, 128, 0)
+                          : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_shade<true, false>, 128, 0);
+    if (e == cudaSuccess && !plain) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_shade<false, true>, 128, 0);
+    if (e != cudaSuccess) {
         cudaGetLastError();
         return 0;
     }
-    int m = a < b ? a : b;
-    m = m < c ? m : c;
+    const int m = (!plain && b < a) ? b : a;
     return m > 0 ? m : 1;
 }
 
@@ -1358,7 +1365,8 @@ int shade_blocks_per_sm()
 void launch_shade(const WaveTables& t, RayQueueDev rq, HitQueueDev hq, const ull* hq_n, ShadowQueueDev sh,
                   ull* sh_n, RayQueueDev next, ull* next_n, float* accum, int* err, LaunchCfg cfg, cudaStream_t s)
 {
-    const int grid = cfg.shade_grid > 0 ? cfg.shade_grid : cfg.grid;
+    const int plain_grid = cfg.shade_grid > 0 ? cfg.shade_grid : cfg.grid;
+    const int grid = cfg.shade_grid_other > 0 ? cfg.shade_grid_other : cfg.grid;
     if (t.multi)
         k_shade<true, false><<<grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, hq, hq_n, cfg.ray_order,
                                                   sh, sh_n, next, next_n, accum, err);
@@ -1366,7 +1374,7 @@ void launch_shade(const WaveTables& t, RayQueueDev rq, HitQueueDev hq, const ull
         k_shade<false, true><<<grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, hq, hq_n, cfg.ray_order,
                                                   sh, sh_n, next, next_n, accum, err);
     else
-        k_shade<false, false><<<grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, hq, hq_n, cfg.ray_order,
+        k_shade<false, false><<<plain_grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, hq, hq_n, cfg.ray_order,
                                                    sh, sh_n, next, next_n, accum, err);
 }
 
