@@ -55,6 +55,12 @@ METRIC = "Mrays/s (closest-hit + shadow rays) at equal MSE vs FP64 oracle"
 BYTES_RAY = 24
 BYTES_HIT = 20
 BYTES_MISS = 16 + 24
+# The whole bounce loop's compulsory inter-kernel state, per closest-hit ray
+# (ray state written and read 2 x 48 B, hit record written and read 2 x 20 B,
+# accumulator read-modify-write 24 B) and per shadow ray (2 x 44 B + 24 B),
+# reported beside the kernel figure over the whole step.
+PIPE_BYTES_CLOSEST = 160
+PIPE_BYTES_SHADOW = 112
 
 
 def load_pkg():
@@ -480,6 +486,9 @@ def main() -> int:
     launches = sum(s["bounces"] for s in stats)
     alg_bytes = closest * BYTES_RAY + hits * BYTES_HIT + misses * BYTES_MISS
     achieved = alg_bytes / (trace_ms / 1e3) / 1e9
+    shadow = sum(s["shadow_rays"] for s in stats)
+    step_ms = sum(s["ms_total"] for s in stats)
+    pipe_achieved = (closest * PIPE_BYTES_CLOSEST + shadow * PIPE_BYTES_SHADOW) / (step_ms / 1e3) / 1e9
     peak, peak_kind = measured_peaks()
     # DRAM bytes per closest-hit ray of k_trace_render, measured by ncu over
     # every launch of a smaller render of the same scene (profiles/) with the
@@ -512,7 +521,11 @@ def main() -> int:
                      "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
                      "traffic": traffic, "launches": launches,
                      "alg_bytes_per_launch": alg_bytes / max(launches, 1),
-                     "avg_launch_ms": trace_ms / max(launches, 1)},
+                     "avg_launch_ms": trace_ms / max(launches, 1),
+                     "pipeline_model": {
+                         "bytes_per_closest_ray": PIPE_BYTES_CLOSEST, "bytes_per_shadow_ray": PIPE_BYTES_SHADOW,
+                         "achieved": pipe_achieved, "frac": pipe_achieved / peak,
+                         "over": "the whole step (all kernels of the bounce loop)"}},
         "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": 128,
                 "d2h_bytes_per_step": W * H * 3 * 4},
         "clocks": clocks,
