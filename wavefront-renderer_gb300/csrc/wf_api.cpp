@@ -898,6 +898,8 @@ int wf_destroy(wf_ctx* c)
         if (e) cudaEventDestroy(e);
     for (auto& e : c->timer)
         if (e) cudaEventDestroy(e);
+    for (auto& e : c->stage_ev)
+        if (e) cudaEventDestroy(e);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return WF_OK;

@@ -123,6 +123,7 @@ struct wf_ctx {
 
     cudaEvent_t ev[8]{};
     cudaEvent_t timer[2]{};
+    std::vector<cudaEvent_t> stage_ev;  // per-bounce stage events of the device-counted chain
     wf_tuning tuning{};
 
     // L2 persistence (wf_tuning::l2_persist): the device's limits, and the

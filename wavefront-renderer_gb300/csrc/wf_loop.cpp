@@ -338,6 +338,91 @@ int wave_graph(wf_ctx* c, int max_depth, bool ray_sort, wf_render_stats& stats)
 
 int zero_tally(wf_ctx* c) { WF_CK(c, cudaMemsetAsync(c->tally, 0, sizeof(ull) * 8, c->stream)); return WF_OK; }
 
+int read_tally(wf_ctx* c, wf_render_stats& stats);
+
+// One wave of a single job without a shading policy, every count on the
+// device and the bounces issued back to back: no host round trip between
+// bounces (wave_host waits for each bounce's counts), with the single-job
+// kernels (wave_graph captures the multi-job ones).  All max_depth bounces
+// are issued; a bounce whose queue is empty costs only its empty launches.
+// Stage times come from per-bounce events read once the wave is done.
+int wave_chain(wf_ctx* c, int max_depth, bool ray_sort, const DeviceJob& job, wf_render_stats& stats,
+               bool track_costs, int cost_records)
+{
+    cudaStream_t s = c->stream;
+    WaveTables T{c->d_scene_table, c->d_jobs, c->scenes[job.scene].S, job, false, kTreeBinary};
+    T.tree = tree_format(T.scene0);
+    LaunchCfg PC = persist_cfg(c);
+    PC.ray_order = hits_in_ray_order(WF_POLICY_NONE);
+    const LaunchCfg WC = wide_cfg(c);
+    const size_t nev = (size_t)5 * (size_t)max_depth;
+    while (c->stage_ev.size() < nev) {
+        cudaEvent_t e = nullptr;
+        WF_CK(c, cudaEventCreate(&e));
+        c->stage_ev.push_back(e);
+    }
+    int rc = zero_tally(c);
+    if (rc) return rc;
+    int cur = 0;
+    int64_t kernels = 0;
+    launch_camera_chunks(c->d_chunks, c->d_wave_header, c->d_jobs, c->rq[cur], WC, s);
+    WF_CK(c, cudaMemcpyAsync(c->counters, c->d_wave_header, sizeof(ull), cudaMemcpyDeviceToDevice, s));
+    kernels += 1;
+    for (int depth = 0; depth < max_depth; ++depth) {
+        cudaEvent_t* E = c->stage_ev.data() + 5 * depth;
+        if (ray_sort) {
+            WF_CK(c, cudaEventRecord(E[0], s));
+            launch_ray_keys(c->d_scene_table, c->d_jobs, c->rq[cur], c->counters, c->keys, c->vals, WC, s);
+            uint64_t* rk;
+            uint32_t* rv;
+            RadixSortArgs a{c->keys, c->vals,    c->keys_tmp, c->vals_tmp, c->hist, c->counters,
+                            c->nb,   ray_key_begin(c), 33,          &rk,         &rv};
+            radix_sort_pairs(a, s);
+            launch_gather_rays(c->rq[cur], rv, c->counters, c->rq[1 - cur], WC, s);
+            kernels += 2 + kSortKernelsPerPass * ((33 - ray_key_begin(c) + 7) / 8);
+            cur = 1 - cur;
+            WF_CK(c, cudaEventRecord(E[1], s));
+        }
+        WF_CK(c, cudaMemsetAsync(c->counters + 1, 0, sizeof(ull) * 5, s));
+        WF_CK(c, cudaEventRecord(E[2], s));
+        launch_trace_render(T, c->rq[cur], c->counters, c->hq[0], c->counters + 1, c->arena, c->counters + 4,
+                            c->err_flag, PC, s);
+        launch_compact_hits(c->counters, c->hq[0], c->counters + 1, WC, s);
+        WF_CK(c, cudaEventRecord(E[3], s));
+        launch_shade(T, c->rq[cur], c->hq[0], c->counters + 1, c->sh, c->counters + 2, c->rq[1 - cur],
+                     c->counters + 3, c->arena, c->err_flag, PC, s);
+        if (track_costs) {  // the tracker merge at the end of shadeAll (.cpp:800-844)
+            launch_cost_update(c->ct_mat, c->ct_tex, cost_records, s);
+            kernels += 1;
+        }
+        launch_occluded_render(T, c->sh, c->counters + 2, c->arena, c->counters + 5, c->err_flag, PC, s);
+        WF_CK(c, cudaEventRecord(E[4], s));
+        launch_tally(c->counters, c->tally, s);
+        WF_CK(c, cudaMemcpyAsync(c->counters, c->counters + 3, sizeof(ull), cudaMemcpyDeviceToDevice, s));
+        kernels += 5;
+        cur = 1 - cur;
+    }
+    const uint64_t rays_before = stats.closest_rays;
+    rc = read_tally(c, stats);  // waits for the wave
+    if (rc) return rc;
+    float ms = 0.0f;
+    for (int depth = 0; depth < max_depth; ++depth) {
+        cudaEvent_t* E = c->stage_ev.data() + 5 * depth;
+        if (ray_sort) {
+            WF_CK(c, cudaEventElapsedTime(&ms, E[0], E[1]));
+            stats.ms_ray_sort += ms;
+        }
+        WF_CK(c, cudaEventElapsedTime(&ms, E[2], E[3]));
+        stats.ms_intersect += ms;
+        WF_CK(c, cudaEventElapsedTime(&ms, E[3], E[4]));
+        stats.ms_shade += ms;
+    }
+    if (ray_sort) stats.sorted_elements += stats.closest_rays - rays_before;  // every bounce sorts its queue
+    stats.waves++;
+    stats.kernel_launches += kernels;
+    return WF_OK;
+}
+
 int read_tally(wf_ctx* c, wf_render_stats& stats)
 {
     ull t[4];
@@ -450,6 +535,10 @@ int render_single(wf_ctx* c, const wf_render_params* P, wf_render_stats* st)
     WF_CK(c, cudaMemsetAsync(c->arena, 0, sizeof(float) * 3 * (size_t)np, s));
     apply_l2_policy(c, 0);
     const bool graph = !tracking && use_graph(c, false, P->policy);
+    // without a policy (and without a sort-or-skip threshold, a host decision)
+    // the bounces need no host round trip
+    const bool chain = !graph && P->policy == WF_POLICY_NONE &&
+                       !(P->enable_ray_sort && c->tuning.sort_min_queue > 0);
     wf_render_stats stats{};
     stats.kernel_launches = kernels_setup;
     if (graph) {
@@ -471,9 +560,13 @@ int render_single(wf_ctx* c, const wf_render_params* P, wf_render_stats* st)
         ch[0] = WaveChunk{0, P->first_sample + s0, nspp, adaptive ? n_active : 0, 0};
         rc = upload_wave(c, ch, pix * nspp);
         if (rc) return rc;
-        rc = graph ? wave_graph(c, P->max_depth, P->enable_ray_sort != 0, stats)
-                   : wave_host(c, pix * nspp, P->max_depth, P->policy, P->enable_ray_sort != 0, 0,
-                               P->rel_cost_material, P->rel_cost_texture, &table[0], stats, tracking, nspp);
+        if (graph)
+            rc = wave_graph(c, P->max_depth, P->enable_ray_sort != 0, stats);
+        else if (chain)
+            rc = wave_chain(c, P->max_depth, P->enable_ray_sort != 0, table[0], stats, tracking, nspp);
+        else
+            rc = wave_host(c, pix * nspp, P->max_depth, P->policy, P->enable_ray_sort != 0, 0, P->rel_cost_material,
+                           P->rel_cost_texture, &table[0], stats, tracking, nspp);
         if (rc) return rc;
         if (adaptive) {  // renderScene's per-sample adaptive block (.cpp:270-294)
             launch_adaptive_fold(c->ad_buf, np, nspp, s0 % spw, spw, c->arena, c->ad_mean, c->ad_m2, c->ad_count,
