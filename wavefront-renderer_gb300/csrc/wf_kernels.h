@@ -76,7 +76,8 @@ void launch_shade(const WaveTables& t, RayQueueDev rq, HitQueueDev hq, const ull
                   ull* sh_n, RayQueueDev next, ull* next_n, float* accum, int* err, LaunchCfg cfg, cudaStream_t s);
 // After a ray-order trace: lists the rays that hit in hq.ray, counting them
 // into *hq_n (zero before the launch).
-void launch_compact_hits(const ull* d_n, HitQueueDev hq, ull* hq_n, LaunchCfg cfg, cudaStream_t s);
+void launch_compact_hits(const WaveTables& t, RayQueueDev rq, const ull* d_n, HitQueueDev hq, ull* hq_n,
+                         float* accum, LaunchCfg cfg, cudaStream_t s);
 void launch_occluded_render(const WaveTables& t, ShadowQueueDev sh, const ull* sh_n, float* accum, ull* work,
                             int* err, LaunchCfg cfg, cudaStream_t s);
 // tally[0..3] += rays, hits, shadow rays, (rays > 0) of the bounce just run.

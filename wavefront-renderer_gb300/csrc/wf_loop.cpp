@@ -187,7 +187,7 @@ int wave_host(wf_ctx* c, int64_t total, int max_depth, int policy, bool ray_sort
         launch_trace_render(T, c->rq[cur], c->counters, c->hq[0], c->counters + 1, c->arena, c->counters + 4,
                             c->err_flag, PC, s);
         if (PC.ray_order) {
-            launch_compact_hits(c->counters, c->hq[0], c->counters + 1, WC, s);
+            launch_compact_hits(T, c->rq[cur], c->counters, c->hq[0], c->counters + 1, c->arena, WC, s);
             stats.kernel_launches += 1;
         }
         WF_CK(c, cudaEventRecord(ev[5], s));
@@ -285,7 +285,7 @@ int record_chain(wf_ctx* c, int max_depth, bool ray_sort, int tree)
         launch_trace_render(T, c->rq[cur], c->counters, c->hq[0], c->counters + 1, c->arena, c->counters + 4,
                             c->err_flag, PC, s);
         if (PC.ray_order) {
-            launch_compact_hits(c->counters, c->hq[0], c->counters + 1, WC, s);
+            launch_compact_hits(T, c->rq[cur], c->counters, c->hq[0], c->counters + 1, c->arena, WC, s);
             kernels += 1;
         }
         launch_shade(T, c->rq[cur], c->hq[0], c->counters + 1, c->sh, c->counters + 2, c->rq[1 - cur], c->counters + 3,
@@ -387,7 +387,7 @@ int wave_chain(wf_ctx* c, int max_depth, bool ray_sort, const DeviceJob& job, wf
         WF_CK(c, cudaEventRecord(E[2], s));
         launch_trace_render(T, c->rq[cur], c->counters, c->hq[0], c->counters + 1, c->arena, c->counters + 4,
                             c->err_flag, PC, s);
-        launch_compact_hits(c->counters, c->hq[0], c->counters + 1, WC, s);
+        launch_compact_hits(T, c->rq[cur], c->counters, c->hq[0], c->counters + 1, c->arena, WC, s);
         WF_CK(c, cudaEventRecord(E[3], s));
         launch_shade(T, c->rq[cur], c->hq[0], c->counters + 1, c->sh, c->counters + 2, c->rq[1 - cur],
                      c->counters + 3, c->arena, c->err_flag, PC, s);

@@ -313,7 +313,7 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_trace_render(DeviceScene sc
                 }
             }
         }
-        if (fin && !hit) {
+        if (fin && !hit && ray_order != 2) {  // (2: k_compact_hits shades the misses)
             const DeviceJob& J = kMulti ? jobs[job] : job0;
             const V3 T = {ldq(&rq.tr[ray]), ldq(&rq.tg[ray]), ldq(&rq.tb[ray])};
             V3 c = T * sky_color(*S, tr.d);
@@ -365,6 +365,29 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_trace_render(DeviceScene sc
     if (overflow) atomicOr(err, 1);
 }
 
+// A ray that left the scene (the miss loop of renderScene, .cpp:256-265):
+// throughput x sky (or environment map) added to its pixel, with the
+// balance-heuristic weight against environment NEE when the job samples it.
+template <bool kMulti>
+__device__ __forceinline__ void shade_miss(const DeviceScene& scene0, const DeviceJob& job0,
+                                           const DeviceScene* __restrict__ scenes,
+                                           const DeviceJob* __restrict__ jobs, const RayQueueDev& rq, int64_t ray,
+                                           float* accum)
+{
+    const int job = kMulti ? ldq(&rq.job[ray]) : 0;
+    const DeviceJob& J = kMulti ? jobs[job] : job0;
+    const DeviceScene& S = kMulti ? scenes[J.scene] : scene0;
+    const V3 d = {ldq(&rq.dx[ray]), ldq(&rq.dy[ray]), ldq(&rq.dz[ray])};
+    const V3 T = {ldq(&rq.tr[ray]), ldq(&rq.tg[ray]), ldq(&rq.tb[ray])};
+    V3 c = T * sky_color(S, d);
+    if (J.env_nee && S.env_alias_prob) {
+        const float ip = ldq(&rq.pdf[ray]);
+        if (ip > 0.0f) c = c * mis_balance(ip, env_pdf(S, normalized(d)));
+    }
+    const int32_t slot = job_slot(J, ldq(&rq.pixel[ray]), J.sample_buf ? ldq(&rq.sample[ray]) : 0);
+    accum_add(job_accum(J, accum), slot, c);
+}
+
 // The rays that hit, listed in queue order for shading after a ray-order
 // trace (records at the rays' indices, tri = -1 for a miss).  A block takes
 // tiles of kCompactIters x 256 rays, ranks the hits of a tile in ray order
@@ -374,7 +397,12 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_trace_render(DeviceScene sc
 // rays and the shadow rays in queue order too.
 constexpr int kCompactIters = 8;  // 8 x 8 warps = 64 counts: two per lane of the scanning warp
 
-__global__ void __launch_bounds__(256) k_compact_hits(const ull* __restrict__ d_n, HitQueueDev hq, ull* hq_n)
+template <bool kMulti, bool kMisses>
+__global__ void __launch_bounds__(256) k_compact_hits(DeviceScene scene0, DeviceJob job0,
+                                                      const DeviceScene* __restrict__ scenes,
+                                                      const DeviceJob* __restrict__ jobs, RayQueueDev rq,
+                                                      const ull* __restrict__ d_n, HitQueueDev hq, ull* hq_n,
+                                                      float* accum)
 {
     __shared__ unsigned offs[kCompactIters * 8];
     __shared__ ull tile_first;
@@ -387,8 +415,10 @@ __global__ void __launch_bounds__(256) k_compact_hits(const ull* __restrict__ d_
 #pragma unroll
         for (int j = 0; j < kCompactIters; ++j) {
             const int64_t k = t0 + j * 256 + threadIdx.x;
-            masks[j] = __ballot_sync(0xFFFFFFFFu, k < n && ldq(&hq.tri[k]) >= 0);
+            const int32_t tri = k < n ? ldq(&hq.tri[k]) : 0;
+            masks[j] = __ballot_sync(0xFFFFFFFFu, k < n && tri >= 0);
             if (lane == 0) offs[j * 8 + warp] = (unsigned)__popc(masks[j]);
+            if (kMisses && tri < 0) shade_miss<kMulti>(scene0, job0, scenes, jobs, rq, k, accum);
         }
         __syncthreads();
         if (warp == 0) {  // exclusive scan of the counts in ray order (j, then warp)
@@ -1307,9 +1337,22 @@ void launch_occluded_api(const DeviceScene& S, int64_t n, const float* ox, const
 // the tree staged in shared memory (binary trees, single-scene waves; else
 // variant 0); the traversal follows the scene's tree (binary, 4-wide or
 // compressed 8-wide).
+// Where a ray-order bounce shades its misses: an environment-map lookup
+// (atan2, asin, a texel fetch) evaluated by finished lanes inside the
+// traversal loop stalls their warp, so for a single-job render of a scene
+// with a map the compaction pass shades the misses in ray order (lattice
+// scene +1.3%); the gradient sky stays in the traversal kernel, where it is
+// cheaper than a second pass over the ray columns (Cornell box, dense mesh,
+// batched jobs measured 1-5% slower with the move).
+static bool misses_in_compaction(const WaveTables& t, bool ray_order)
+{
+    return ray_order && !t.multi && t.scene0.env_rgb != nullptr;
+}
+
 void launch_trace_render(const WaveTables& t, RayQueueDev rq, const ull* d_n, HitQueueDev hq, ull* hq_n,
                          float* accum, ull* work, int* err, LaunchCfg cfg, cudaStream_t s)
 {
+    if (misses_in_compaction(t, cfg.ray_order != 0)) cfg.ray_order = 2;
 #define WF_TRACE(M, B, T)                                                                                   \
     k_trace_render<M, B, T><<<cfg.grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, d_n, hq, hq_n, \
                                                      accum, work, err, cfg.speculative, cfg.ray_order)
@@ -1378,9 +1421,19 @@ void launch_shade(const WaveTables& t, RayQueueDev rq, HitQueueDev hq, const ull
                                                    sh, sh_n, next, next_n, accum, err);
 }
 
-void launch_compact_hits(const ull* d_n, HitQueueDev hq, ull* hq_n, LaunchCfg cfg, cudaStream_t s)
+void launch_compact_hits(const WaveTables& t, RayQueueDev rq, const ull* d_n, HitQueueDev hq, ull* hq_n,
+                         float* accum, LaunchCfg cfg, cudaStream_t s)
 {
-    k_compact_hits<<<cfg.grid, 256, 0, s>>>(d_n, hq, hq_n);
+    // only ray-order bounces compact; misses move here for single-job scenes with a map
+    if (t.multi)
+        k_compact_hits<true, false><<<cfg.grid, 256, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, d_n, hq, hq_n,
+                                                              accum);
+    else if (misses_in_compaction(t, true))
+        k_compact_hits<false, true><<<cfg.grid, 256, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, d_n, hq, hq_n,
+                                                              accum);
+    else
+        k_compact_hits<false, false><<<cfg.grid, 256, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, d_n, hq, hq_n,
+                                                               accum);
 }
 
 void launch_occluded_render(const WaveTables& t, ShadowQueueDev sh, const ull* sh_n, float* accum, ull* work,
