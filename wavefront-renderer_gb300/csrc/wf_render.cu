@@ -240,6 +240,17 @@ __device__ __forceinline__ void accum_add(float* accum, int32_t slot, V3 c)
 // loop (.cpp:256-265): misses add throughput * sky to their pixel, hits are
 // appended to the hit queue with one atomic per warp.
 //
+// Dynamic fetch refills a warp's idle lanes only once at least half of them
+// are idle (or all are): the refilled lanes then take one run of consecutive
+// queue entries — neighbouring paths of the ray-ordered queue, which traverse
+// alike — instead of a lane or two at a time from wherever the global counter
+// has moved.  Against refilling every idle lane every round: lattice scene
+// +4.9%, dense mesh +0.1%, batched jobs +0.7%; 20 and more idle lanes starve
+// the dense mesh (-0.9% at 20, -24% at 32).
+#ifndef WF_REFILL_MIN
+#define WF_REFILL_MIN 16
+#endif
+
 // Persistent threads with dynamic ray fetch (Aila & Laine 2009): between
 // traversal rounds, lanes whose ray has finished emit its result and take a
 // new ray from a global counter, so a warp is not held by its slowest ray.
@@ -333,7 +344,7 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_trace_render(DeviceScene sc
         // 2. lanes without a ray take new ones
         const bool need = ray < 0 && !exhausted;
         const unsigned nm = __ballot_sync(0xFFFFFFFFu, need);
-        if (nm) {
+        if (nm && (__popc(nm) >= WF_REFILL_MIN || __all_sync(0xFFFFFFFFu, ray < 0))) {
             ull base = 0;
             const int leader = __ffs(nm) - 1;
             if (lane == leader) base = atomicAdd(work, (ull)__popc(nm));
@@ -874,7 +885,7 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_occluded_render(DeviceScene
         }
         const bool need = ray < 0 && !exhausted;
         const unsigned nm = __ballot_sync(0xFFFFFFFFu, need);
-        if (nm) {
+        if (nm && (__popc(nm) >= WF_REFILL_MIN || __all_sync(0xFFFFFFFFu, ray < 0))) {
             ull base = 0;
             const int leader = __ffs(nm) - 1;
             if (lane == leader) base = atomicAdd(work, (ull)__popc(nm));
