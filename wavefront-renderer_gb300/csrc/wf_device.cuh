@@ -260,7 +260,8 @@ __device__ __forceinline__ int32_t job_slot(const DeviceJob& J, int32_t pixel, i
 }
 
 // One slice of a wave: samples [first_sample, first_sample + nspp) of every
-// pixel of a job, as paths [path_offset, path_offset + width*height*nspp).
+// pixel of a job, as paths [path_offset, path_offset + width*height*nspp),
+// pixel-major (a pixel's nspp samples are consecutive paths).
 struct WaveChunk {
     int32_t job;
     int32_t first_sample;

@@ -61,11 +61,16 @@ __global__ void k_camera(wf_camera cam, int W, int H, uint32_t s0, uint32_t s1, 
 
 // Camera rays of one wave made of chunks (job, samples) of several jobs: the
 // same arithmetic as k_camera, the job's camera and seed.
-// Queue order of a sample's pixels in the render loop: bands of 4 rows, each
-// walked in 8x4 tiles (a narrower last tile where the width is not a multiple
-// of 8; the last band may hold fewer rows), so a warp's 32 camera rays cover
-// an 8x4 block and its later bounces start from nearby points.  A bijection
-// on [0, W*H); the pixel keys the random streams, so the order changes no path.
+// Queue order of a chunk: pixel-major — a pixel's samples are consecutive
+// paths, so a warp traces the samples of one pixel (or of 32 / nspp pixels)
+// and, as its paths bounce, starts them from nearly the same point; the
+// ray-ordered queues keep that grouping through later bounces.  Against
+// sample-major order (all pixels of sample 0, then sample 1, ...): lattice
+// scene +19.7%, dense mesh +2.3%, 4-sample groups half of that.  Pixels
+// follow bands of 4 rows, each walked in 8x4 tiles (a narrower last tile
+// where the width is not a multiple of 8; the last band may hold fewer rows).
+// A bijection on the chunk's paths; the pixel and sample key the random
+// streams, so the order changes no path.
 __device__ __forceinline__ int tile_pixel(int q, int W, int H)
 {
     const int band = q / (4 * W);
@@ -101,8 +106,9 @@ __global__ void k_camera_chunks(const WaveChunk* __restrict__ chunks, const long
         const DeviceJob& J = jobs[ch.job];
         const int64_t np = ch.active_count > 0 ? ch.active_count : (int64_t)J.width * J.height;
         const int64_t local = i - ch.path_offset;
-        const int s = (int)(local / np);
-        int p = (int)(local - (int64_t)s * np);
+        const int64_t pi = local / ch.nspp;
+        const int s = (int)(local - pi * ch.nspp);
+        int p = (int)pi;
         if (ch.active_count > 0)
             p = J.active[p];  // generatePrimaryRays' activePixels mask
         else
