@@ -510,7 +510,7 @@ def main() -> int:
         "config": {"workload": wl["name"], "policy": args.policy, "ray_sort": bool(args.ray_sort),
                    "env_nee": bool(args.env_nee), "adaptive": bool(args.adaptive), "cost_aware_rr": bool(args.cost_rr),
                    "triangles": info.num_triangles, "spp_per_wave": args.spp_per_wave or "auto",
-                   "l2": f"inputs larger than L2 (ray queues {W * H * min(wl['spp'], max(1, (1 << 26) // (W * H))) * 112 / 1e9:.1f} GB "
+                   "l2": f"inputs larger than L2 (ray queues {W * H * min(wl['spp'], max(1, (1 << 27) // (W * H))) * 112 / 1e9:.1f} GB "
                          f"per wave; BVH + triangles {info.num_triangles * 68 / 1e6:.0f} MB)",
                    "parallelism": f"replicas x{world}"},
         "samples_per_s": samples_all / (ms_max / 1e3),

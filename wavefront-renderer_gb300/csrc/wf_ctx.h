@@ -13,10 +13,12 @@
 
 namespace wf {
 
-// Paths in flight per wave: 2^26 (67 M paths, ~28 GB of queues at 424 B per
-// path) holds all 64 samples of a 1024^2 render in one wave, so the bounce
-// tails stay wide (2^23 measured 30% slower on the dense-mesh workload).
-constexpr int64_t kDefaultPathsPerWave = int64_t(1) << 26;
+// Paths in flight per wave: 2^27 (134 M paths, ~57 GB of queues at 424 B per
+// path) holds all 64 samples of a 1024^2 render, or all 32 of a 2048^2
+// render, in one wave, so the bounce tails stay wide and a warp traces the
+// samples of one pixel (2^23 measured 30% slower on the dense-mesh workload;
+// 2^27 against 2^26 on the 2048^2 lattice: +1.1%).
+constexpr int64_t kDefaultPathsPerWave = int64_t(1) << 27;
 
 // A scene kept on the device: BVH, triangles, materials, textures, lights.
 struct ResidentScene {
