@@ -296,13 +296,17 @@ def test_render_is_order_independent(wf, ctx, scene_small, scene_c2small, which)
         agree = np.isclose(img, base, rtol=1e-4, atol=1e-6).all(axis=2).mean()
         assert agree >= 0.999, (kw, agree)
     # launch tuning: occupancy variant, shared-memory stack, grid size,
-    # graph replay and the sort-or-skip threshold change no pixel beyond that
+    # graph replay and the sort-or-skip threshold change no pixel beyond that.
+    # The base render issues its bounces back to back with device-side counts;
+    # a sort-or-skip threshold sends policy none through the loop that waits
+    # for each bounce's counts on the host, graph_mode=1 through graph replay.
     try:
         for tune, kw in [(dict(trace_variant=1), {}), (dict(trace_variant=2), {}), (dict(trace_variant=3), {}),
                          (dict(speculative_traversal=1), {}), (dict(l2_persist=1), {}),
                          (dict(ray_sort_bits=16), dict(ray_sort=True)),
                          (dict(persistent_blocks_per_sm=4), {}), (dict(graph_mode=1), {}),
-                         (dict(sort_min_queue=6000), dict(policy=1, ray_sort=True))]:
+                         (dict(sort_min_queue=6000), dict(policy=1, ray_sort=True)),
+                         (dict(sort_min_queue=6000), dict(ray_sort=True))]:
             ctx.set_tuning(**tune)
             img, _ = ctx.render(wf.render_params(W, H, 8, 12, cam, seed=5, **kw))
             agree = np.isclose(img, base, rtol=1e-4, atol=1e-6).all(axis=2).mean()
