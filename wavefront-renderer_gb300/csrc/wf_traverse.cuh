@@ -73,7 +73,7 @@ struct SharedStack32 {
     __device__ __forceinline__ uint32_t& operator[](int i) const { return p[i * 128]; }
 };
 
-template <bool kAnyHit>
+template <bool kAnyHit, bool kFarFirst = false>
 struct Traversal {
     using Entry = uint32_t;
     static constexpr int kStack = kStackSize;
@@ -231,9 +231,13 @@ struct Traversal {
         }
     }
 
-    // Which hit child to visit first: the nearer one (closest hit, and any
-    // hit by default); WF_ANYHIT_ORDER selects other orders for shadow rays
-    // (1 = the first child, 2 = the child with the larger box).
+    // Which hit child to visit first: the nearer one for closest hit; for
+    // any hit (shadow rays) the nearer one, or with kFarFirst the farther
+    // one, which reaches the occluders between the surface and the light
+    // before the geometry around the ray's own origin, where a shadow ray
+    // leaving its surface finds nothing.  WF_ANYHIT_ORDER selects other
+    // orders for shadow rays (1 = the first child, 2 = the child with the
+    // larger box).
     __device__ __forceinline__ static bool child_order_swap(const BvhNode& nd, float tn0, float tn1)
     {
 #if defined(WF_ANYHIT_ORDER) && WF_ANYHIT_ORDER == 1
@@ -248,6 +252,7 @@ struct Traversal {
         }
 #endif
         (void)nd;
+        if (kAnyHit && kFarFirst) return !(tn1 < tn0);
         return tn1 < tn0;
     }
 
