@@ -561,8 +561,13 @@ constexpr int kShadeWarps = 4;  // k_shade runs 128-thread blocks
 #define WF_SHADE_MIN_BLOCKS_PLAIN 8
 #endif
 // kTimed: the live CostTracker times a quarter of the hits (single-job
-// renders only); the other instances carry no clock reads.
-template <bool kMulti, bool kTimed>
+// renders only); the other instances carry no clock reads.  kLean: a
+// single-job render of a scene without an environment map, textures or a
+// directional light runs an instance without the environment-NEE block (two
+// map lookups), the texture lookups and the directional NEE — a smaller
+// kernel that waits less on the instruction cache (dense mesh +0.9%,
+// Cornell box +1.7% for the environment block alone).
+template <bool kMulti, bool kTimed, bool kLean = false>
 __global__ void __launch_bounds__(128, (kMulti || kTimed) ? WF_SHADE_MIN_BLOCKS : WF_SHADE_MIN_BLOCKS_PLAIN)
     k_shade(DeviceScene scene0, DeviceJob job0,
                                                const DeviceScene* __restrict__ scenes,
@@ -623,7 +628,7 @@ __global__ void __launch_bounds__(128, (kMulti || kTimed) ? WF_SHADE_MIN_BLOCKS 
             // its cycles to the texture and, as part of scatter, to the
             // material, as the reference's two timers do.
             const long long tc0 = timed ? clock64() : 0;
-            const V3 surf = surface_color(S, m, h);
+            const V3 surf = kLean ? v3(m.albedo[0], m.albedo[1], m.albedo[2]) : surface_color(S, m, h);
             unsigned cyc_surf = 0;
             if (timed) {
                 cyc_surf = (unsigned)min(clock64() - tc0, (long long)(1 << 26));
@@ -690,7 +695,7 @@ __global__ void __launch_bounds__(128, (kMulti || kTimed) ? WF_SHADE_MIN_BLOCKS 
                 }
             }
             // Directional NEE (.cpp:712-737)
-            if (S.directional.intensity > 0.0f) {
+            if (!kLean && S.directional.intensity > 0.0f) {
                 const V3 to = v3(S.directional.direction[0], S.directional.direction[1],
                                  S.directional.direction[2]) * -1.0f;
                 const float cos_s = dot(h.n, to);
@@ -711,7 +716,7 @@ __global__ void __launch_bounds__(128, (kMulti || kTimed) ? WF_SHADE_MIN_BLOCKS 
             // its NEE carries that factor.  The last depth gets none: the ray
             // it would share with is never traced (.cpp:154), so the mean stays
             // the miss-only estimator's.
-            if (J.env_nee && S.env_alias_prob && depth + 1 < J.max_depth &&
+            if (!kLean && J.env_nee && S.env_alias_prob && depth + 1 < J.max_depth &&
                 (m.type == WF_MATERIAL_DIFFUSE || m.type == WF_MATERIAL_PLASTIC)) {
                 Stream er(seed_lo, seed_hi, kPurposeEnvironment, (uint32_t)depth, (uint32_t)pixel,
                           (uint32_t)sample);
@@ -1420,6 +1425,11 @@ int shade_blocks_per_sm(bool plain)
     int a = 0, b = 0;
     cudaError_t e = plain ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_shade<false, false>, 128, 0)
                           : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_shade<true, false>, 128, 0);
+    if (e == cudaSuccess && plain) {  // the lean instance shares the plain grid
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_shade<false, false, true>, 128, 0);
+        if (e == cudaSuccess && b < a) a = b;
+        b = 0;
+    }
     if (e == cudaSuccess && !plain) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_shade<false, true>, 128, 0);
     if (e != cudaSuccess) {
         cudaGetLastError();
@@ -1444,6 +1454,9 @@ void launch_shade(const WaveTables& t, RayQueueDev rq, HitQueueDev hq, const ull
     else if (t.job0.cost_sum_mat)
         k_shade<false, true><<<grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, hq, hq_n, cfg.ray_order,
                                                   sh, sh_n, next, next_n, accum, err);
+    else if (!t.scene0.env_alias_prob && t.scene0.num_textures == 0 && !(t.scene0.directional.intensity > 0.0f))
+        k_shade<false, false, true><<<plain_grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, hq, hq_n,
+                                                                cfg.ray_order, sh, sh_n, next, next_n, accum, err);
     else
         k_shade<false, false><<<plain_grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, hq, hq_n, cfg.ray_order,
                                                    sh, sh_n, next, next_n, accum, err);
