@@ -459,6 +459,40 @@ def test_gpu_env_nee_matches_analytic_irradiance(wf, orc, ctx):
     assert np.all(np.abs(m - sky.expected) <= 4 * se + 1e-3 * sky.expected), (m, se, sky.expected)
 
 
+def test_render_matches_oracle_plastic_spotlight(wf, orc, ctx):
+    """The plastic lobes (Schlick-chosen fuzzy mirror or cosine lobe) and the
+    spotlight's cone (full inside the falloff angle, smoothstep to the outer
+    angle, dark beyond) against the port on the same random streams: the
+    Cornell box with its white box turned plastic (roughness 0.2) and its
+    ceiling light a spotlight (falloff 35, outer 65 degrees); without an
+    environment map, textures or a directional light it runs the lean
+    shading instance.  Tolerance as for the other path-level checks."""
+    scene = wf.HostScene(0)  # a copy of its own: the materials are edited in place
+    mats = scene.desc.materials
+    kinds = [mats[i].type for i in range(scene.desc.num_materials)]
+    light = kinds.index(wf.MATERIAL_EMISSIVE)
+    mats[light].type = wf.MATERIAL_SPOTLIGHT
+    mats[light].spot_falloff_deg = 35.0
+    mats[light].spot_outer_deg = 65.0
+    box = scene.desc.num_materials - 1  # the white Lambert box
+    assert kinds[box] == wf.MATERIAL_DIFFUSE
+    mats[box].type = wf.MATERIAL_PLASTIC
+    mats[box].roughness = 0.2
+    ctx.upload(scene.desc)
+    port = orc.Port(scene.desc)
+    W = H = 64
+    spp = 8
+    cam = scene.camera(W, H)
+    p = wf.render_params(W, H, spp, 8, cam, seed=41)
+    img, st = ctx.render(p)
+    acc, cnt = port.render_window(p, 0, 0, W, H)
+    ref = acc / spp
+    assert ref.mean() > 0.0
+    agree = np.isclose(img, ref, rtol=1e-3, atol=1e-4).all(axis=2).mean()
+    assert agree >= 0.98, agree
+    assert _mean_close(img, ref, 0.01)
+
+
 def test_gpu_env_nee_matches_oracle_paths(wf, orc, ctx, scene_c2small):
     """Environment NEE on the textured 16 x 16 lattice: the GPU's paths are
     the port's (same alias table, same random streams); tolerance as for the
