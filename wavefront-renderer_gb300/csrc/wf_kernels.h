@@ -82,6 +82,9 @@ void launch_occluded_render(const WaveTables& t, ShadowQueueDev sh, const ull* s
                             int* err, LaunchCfg cfg, cudaStream_t s);
 // tally[0..3] += rays, hits, shadow rays, (rays > 0) of the bounce just run.
 void launch_tally(const ull* counters, ull* tally, cudaStream_t s);
+// Tally, next ray count and zeroed bounce counters in one launch (the end
+// of a bounce of a device-counted chain).
+void launch_bounce_end(ull* counters, ull* tally, cudaStream_t s);
 
 // RayQueue::sortKey over the queue (each ray's scene bounds), (key, index)
 // pairs for the radix sort.

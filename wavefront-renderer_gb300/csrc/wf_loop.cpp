@@ -367,6 +367,7 @@ int wave_chain(wf_ctx* c, int max_depth, bool ray_sort, const DeviceJob& job, wf
     int64_t kernels = 0;
     launch_camera_chunks(c->d_chunks, c->d_wave_header, c->d_jobs, c->rq[cur], WC, s);
     WF_CK(c, cudaMemcpyAsync(c->counters, c->d_wave_header, sizeof(ull), cudaMemcpyDeviceToDevice, s));
+    WF_CK(c, cudaMemsetAsync(c->counters + 1, 0, sizeof(ull) * 5, s));  // later bounces: k_bounce_end
     kernels += 1;
     for (int depth = 0; depth < max_depth; ++depth) {
         cudaEvent_t* E = c->stage_ev.data() + 5 * depth;
@@ -383,7 +384,6 @@ int wave_chain(wf_ctx* c, int max_depth, bool ray_sort, const DeviceJob& job, wf
             cur = 1 - cur;
             WF_CK(c, cudaEventRecord(E[1], s));
         }
-        WF_CK(c, cudaMemsetAsync(c->counters + 1, 0, sizeof(ull) * 5, s));
         WF_CK(c, cudaEventRecord(E[2], s));
         launch_trace_render(T, c->rq[cur], c->counters, c->hq[0], c->counters + 1, c->arena, c->counters + 4,
                             c->err_flag, PC, s);
@@ -397,8 +397,7 @@ int wave_chain(wf_ctx* c, int max_depth, bool ray_sort, const DeviceJob& job, wf
         }
         launch_occluded_render(T, c->sh, c->counters + 2, c->arena, c->counters + 5, c->err_flag, PC, s);
         WF_CK(c, cudaEventRecord(E[4], s));
-        launch_tally(c->counters, c->tally, s);
-        WF_CK(c, cudaMemcpyAsync(c->counters, c->counters + 3, sizeof(ull), cudaMemcpyDeviceToDevice, s));
+        launch_bounce_end(c->counters, c->tally, s);
         kernels += 5;
         cur = 1 - cur;
     }

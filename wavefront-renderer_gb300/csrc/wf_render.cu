@@ -143,6 +143,19 @@ __global__ void k_camera_chunks(const WaveChunk* __restrict__ chunks, const long
 
 // Per-bounce counters accumulated on the device (so a captured bounce chain
 // needs no host round trip): tally[0] += rays, [1] += hits, [2] += shadow rays.
+// End of a bounce in a device-counted chain: the tally above, the next
+// bounce's ray count (counters[0] = counters[3]) and its zeroed counters
+// [1..5], in one launch instead of a kernel, a copy and a memset.
+__global__ void k_bounce_end(ull* __restrict__ counters, ull* tally)
+{
+    tally[0] += counters[0];
+    tally[1] += counters[1];
+    tally[2] += counters[2];
+    tally[3] += counters[0] ? 1ull : 0ull;
+    counters[0] = counters[3];
+    for (int k = 1; k <= 5; ++k) counters[k] = 0ull;
+}
+
 __global__ void k_tally(const ull* __restrict__ counters, ull* tally)
 {
     tally[0] += counters[0];
@@ -1419,6 +1432,8 @@ void launch_camera_chunks(const WaveChunk* chunks, const long long* header, cons
 }
 
 void launch_tally(const ull* counters, ull* tally, cudaStream_t s) { k_tally<<<1, 1, 0, s>>>(counters, tally); }
+
+void launch_bounce_end(ull* counters, ull* tally, cudaStream_t s) { k_bounce_end<<<1, 1, 0, s>>>(counters, tally); }
 
 int shade_blocks_per_sm(bool plain)
 {
