@@ -80,10 +80,9 @@ void launch_compact_hits(const WaveTables& t, RayQueueDev rq, const ull* d_n, Hi
                          float* accum, LaunchCfg cfg, cudaStream_t s);
 void launch_occluded_render(const WaveTables& t, ShadowQueueDev sh, const ull* sh_n, float* accum, ull* work,
                             int* err, LaunchCfg cfg, cudaStream_t s);
-// tally[0..3] += rays, hits, shadow rays, (rays > 0) of the bounce just run.
-void launch_tally(const ull* counters, ull* tally, cudaStream_t s);
-// Tally, next ray count and zeroed bounce counters in one launch (the end
-// of a bounce of a device-counted chain).
+// End of a bounce of a device-counted chain: tally[0..3] += rays, hits,
+// shadow rays, (rays > 0) of the bounce just run; the next bounce's ray
+// count into counters[0]; counters[1..5] zeroed.
 void launch_bounce_end(ull* counters, ull* tally, cudaStream_t s);
 
 // RayQueue::sortKey over the queue (each ray's scene bounds), (key, index)

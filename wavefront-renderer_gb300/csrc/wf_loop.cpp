@@ -268,6 +268,7 @@ int record_chain(wf_ctx* c, int max_depth, bool ray_sort, int tree)
     const WaveTables T{c->d_scene_table, c->d_jobs, DeviceScene{}, DeviceJob{}, true, tree};
     launch_camera_chunks(c->d_chunks, c->d_wave_header, c->d_jobs, c->rq[cur], WC, s);
     cudaMemcpyAsync(c->counters, c->d_wave_header, sizeof(ull), cudaMemcpyDeviceToDevice, s);
+    cudaMemsetAsync(c->counters + 1, 0, sizeof(ull) * 5, s);  // later bounces: k_bounce_end
     kernels += 1;
     for (int depth = 0; depth < max_depth; ++depth) {
         if (ray_sort) {
@@ -281,7 +282,6 @@ int record_chain(wf_ctx* c, int max_depth, bool ray_sort, int tree)
             kernels += 2 + kSortKernelsPerPass * ((33 - ray_key_begin(c) + 7) / 8);
             cur = 1 - cur;
         }
-        cudaMemsetAsync(c->counters + 1, 0, sizeof(ull) * 5, s);
         launch_trace_render(T, c->rq[cur], c->counters, c->hq[0], c->counters + 1, c->arena, c->counters + 4,
                             c->err_flag, PC, s);
         if (PC.ray_order) {
@@ -291,8 +291,7 @@ int record_chain(wf_ctx* c, int max_depth, bool ray_sort, int tree)
         launch_shade(T, c->rq[cur], c->hq[0], c->counters + 1, c->sh, c->counters + 2, c->rq[1 - cur], c->counters + 3,
                      c->arena, c->err_flag, PC, s);
         launch_occluded_render(T, c->sh, c->counters + 2, c->arena, c->counters + 5, c->err_flag, PC, s);
-        launch_tally(c->counters, c->tally, s);
-        cudaMemcpyAsync(c->counters, c->counters + 3, sizeof(ull), cudaMemcpyDeviceToDevice, s);
+        launch_bounce_end(c->counters, c->tally, s);
         kernels += 4;
         cur = 1 - cur;
     }

@@ -141,11 +141,12 @@ __global__ void k_camera_chunks(const WaveChunk* __restrict__ chunks, const long
     }
 }
 
-// Per-bounce counters accumulated on the device (so a captured bounce chain
-// needs no host round trip): tally[0] += rays, [1] += hits, [2] += shadow rays.
-// End of a bounce in a device-counted chain: the tally above, the next
-// bounce's ray count (counters[0] = counters[3]) and its zeroed counters
-// [1..5], in one launch instead of a kernel, a copy and a memset.
+// End of a bounce in a device-counted chain (no host round trip, or a
+// captured graph): the per-bounce counters accumulated on the device
+// (tally[0] += rays, [1] += hits, [2] += shadow rays, [3] += bounces that
+// had rays), the next bounce's ray count (counters[0] = counters[3]) and its
+// zeroed counters [1..5], in one launch instead of a kernel, a copy and a
+// memset (Cornell box +3.3%).
 __global__ void k_bounce_end(ull* __restrict__ counters, ull* tally)
 {
     tally[0] += counters[0];
@@ -154,14 +155,6 @@ __global__ void k_bounce_end(ull* __restrict__ counters, ull* tally)
     tally[3] += counters[0] ? 1ull : 0ull;
     counters[0] = counters[3];
     for (int k = 1; k <= 5; ++k) counters[k] = 0ull;
-}
-
-__global__ void k_tally(const ull* __restrict__ counters, ull* tally)
-{
-    tally[0] += counters[0];
-    tally[1] += counters[1];
-    tally[2] += counters[2];
-    tally[3] += counters[0] ? 1ull : 0ull;
 }
 
 // ---------------------------------------------------------------------------
@@ -1430,8 +1423,6 @@ void launch_camera_chunks(const WaveChunk* chunks, const long long* header, cons
 {
     k_camera_chunks<<<cfg.grid, 256, 0, s>>>(chunks, header, jobs, rq);
 }
-
-void launch_tally(const ull* counters, ull* tally, cudaStream_t s) { k_tally<<<1, 1, 0, s>>>(counters, tally); }
 
 void launch_bounce_end(ull* counters, ull* tally, cudaStream_t s) { k_bounce_end<<<1, 1, 0, s>>>(counters, tally); }
 
