@@ -274,7 +274,9 @@ typedef struct wf_scene_info {
 int wf_scene_get_info(wf_ctx* ctx, wf_scene_info* out_info);
 
 /* Launch tuning of a context (the autotuner's knobs).  trace_variant: 0 = no
- * occupancy hint on the traversal kernels, 1 = 9 blocks of 128 threads per
+ * occupancy hint on the traversal kernels (the closest-hit kernel of a
+ * single-job render whose binary tree and triangles exceed L2 runs as 1),
+ * 1 = 9 blocks of 128 threads per
  * SM (56 registers, no spills), 2 = the traversal stack in shared memory instead of local memory
  * (binary trees; 32 KB per block), 3 = the top 256 nodes of the tree staged
  * in shared memory (binary trees, single-scene renders).

@@ -40,6 +40,7 @@ LaunchCfg persist_cfg(const wf_ctx* c)
 {
     int per_sm = c->tuning.persistent_blocks_per_sm > 0 ? c->tuning.persistent_blocks_per_sm : 16;
     LaunchCfg cfg{c->num_sms * per_sm, 128, c->tuning.trace_variant, c->tuning.speculative_traversal};
+    cfg.l2_bytes = c->l2_bytes;
     cfg.shade_grid = c->num_sms * c->shade_per_sm;
     cfg.shade_grid_other = c->num_sms * c->shade_per_sm_other;
     return cfg;
@@ -840,6 +841,7 @@ int wf_create(const wf_config* cfg, wf_ctx** out)
     cudaDeviceProp prop;
     cudaGetDeviceProperties(&prop, c->device);
     c->num_sms = prop.multiProcessorCount;
+    c->l2_bytes = prop.l2CacheSize;
     c->shade_per_sm = shade_blocks_per_sm(true);
     c->shade_per_sm_other = shade_blocks_per_sm(false);
     c->l2_persist_max = (size_t)std::max(0, prop.persistingL2CacheMaxSize);

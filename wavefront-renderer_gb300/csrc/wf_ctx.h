@@ -51,6 +51,7 @@ struct wf_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
     int num_sms = 1;
+    int64_t l2_bytes = 0;  // L2 cache size of the device
     int shade_per_sm = 0;        // k_shade's resident blocks per SM (0 = unknown: use the persistent grid)
     int shade_per_sm_other = 0;  // the same for its multi-job and cost-timed forms
     std::string last_error;

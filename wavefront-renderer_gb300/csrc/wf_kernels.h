@@ -23,6 +23,7 @@ struct LaunchCfg {
     int grid;
     int block;
     int variant = 0;   // kernel variant (traversal occupancy hint / stack placement)
+    int64_t l2_bytes = 0;  // the device's L2 size (variant 0 of a larger scene runs at 9 blocks per SM)
     int speculative = 0;  // 1 = speculative while-while traversal
     int ray_order = 0;    // 1 = hit records at their rays' indices, listed by k_compact_hits
     int shade_grid = 0;        // k_shade's grid (one full wave of resident blocks); 0 = grid

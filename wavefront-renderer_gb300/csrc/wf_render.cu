@@ -1392,6 +1392,13 @@ void launch_trace_render(const WaveTables& t, RayQueueDev rq, const ull* d_n, Hi
                          float* accum, ull* work, int* err, LaunchCfg cfg, cudaStream_t s)
 {
     if (misses_in_compaction(t, cfg.ray_order != 0)) cfg.ray_order = 2;
+    // A single scene whose binary tree and triangles exceed L2 waits on DRAM:
+    // 9 resident blocks (56 registers) hide more of that latency than 8 (64
+    // registers), which an L2-resident scene prefers (lattice +0.9%, dense
+    // mesh -0.6% at 9).
+    if (cfg.variant == 0 && !t.multi && t.tree == kTreeBinary && cfg.l2_bytes > 0 &&
+        (int64_t)t.scene0.num_nodes * (int64_t)sizeof(BvhNode) + (int64_t)t.scene0.num_tris * 48 > cfg.l2_bytes)
+        cfg.variant = 1;
 #define WF_TRACE(M, B, T)                                                                                   \
     k_trace_render<M, B, T><<<cfg.grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, d_n, hq, hq_n, \
                                                      accum, work, err, cfg.speculative, cfg.ray_order)
