@@ -38,11 +38,11 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 
 WORKLOADS = {
-    "c1": dict(config=1, width=1024, height=1024, spp=64, depth=12,
+    "c1": dict(config=1, width=1024, height=1024, spp=64, depth=12, triangles=1310732,
                name="c1_icosphere_1310720tri_1024x1024_64spp_depth12"),
-    "c0": dict(config=0, width=256, height=256, spp=16, depth=8,
+    "c0": dict(config=0, width=256, height=256, spp=16, depth=8, triangles=36,
                name="c0_cornell_36tri_256x256_16spp_depth8"),
-    "c2": dict(config=2, width=2048, height=2048, spp=32, depth=8,
+    "c2": dict(config=2, width=2048, height=2048, spp=32, depth=8, triangles=15127922,
                name="c2_lattice_4096meshes_15127922tri_256mat_64tex_hdri_2048x2048_32spp_depth8"),
 }
 METRIC = "Mrays/s (closest-hit + shadow rays) at equal MSE vs FP64 oracle"
@@ -187,41 +187,67 @@ def barrier(dist):
 
 _CPU_SCENES: dict = {}
 
+# The CPU legs (the GPU arm's cpu_baseline and --impl reference) time the same
+# bounded sample of the workload: a centred band of REF_ROWS rows of the full
+# image at REF_SPP samples per pixel.
+REF_ROWS = 256
+REF_SPP = 16
 
-def cpu_sample(pkg, wl, threads: int, rows: int, spp: int, seed: int):
-    """The oracle port over a centred band of the workload (rank 0 only).
-    The scene and the port's BVH are built once per workload, untimed."""
+
+def _oracle():
+    """The CPU oracle (oracle/oracle.py): the reference's loop restated in C++,
+    with its own copy of the procedural scene generator; it loads no GPU
+    library."""
     sys.path.insert(0, str(ROOT / "oracle"))
     import oracle
 
+    return oracle
+
+
+def cpu_sample(wl, threads: int, rows: int, spp: int, seed: int):
+    """The oracle port over a centred band of the workload (rank 0 only).
+    The scene and the port's BVH are built once per workload, untimed."""
+    oracle = _oracle()
     if wl["config"] not in _CPU_SCENES:
-        sc = pkg.HostScene(wl["config"])
+        sc = oracle.HostScene(wl["config"])
         _CPU_SCENES[wl["config"]] = (sc, oracle.Port(sc.desc))
     scene, port = _CPU_SCENES[wl["config"]]
     W, H = wl["width"], wl["height"]
     cam = scene.camera(W, H)
-    p = pkg.render_params(W, H, spp, wl["depth"], cam, seed=seed)
+    p = oracle.render_params(W, H, spp, wl["depth"], cam, seed=seed)
     y0 = (H - rows) // 2
     t0 = time.perf_counter()
     _, cnt = port.render_window(p, 0, y0, W, rows, threads)
     dt = time.perf_counter() - t0
     rays = cnt["closest_rays"] + cnt["shadow_rays"]
-    return rays, dt, f"{W}x{rows} px centre band x {spp} spp of {wl['name']} ({W * rows * spp} paths)"
+    return rays, dt, (f"{W}x{rows} px centre band x {spp} spp of {wl['name']} ({W * rows * spp} paths); "
+                      f"the oracle port of the reference loop on {threads} host threads")
+
+
+def workload_config(wl, args, world: int) -> dict:
+    """The `config` object of both arms' lines (identical by construction)."""
+    W, H = wl["width"], wl["height"]
+    wave_paths = W * H * min(wl["spp"], max(1, (1 << 27) // (W * H)))
+    return {"workload": wl["name"], "policy": args.policy, "ray_sort": bool(args.ray_sort),
+            "env_nee": bool(args.env_nee), "adaptive": bool(args.adaptive), "cost_aware_rr": bool(args.cost_rr),
+            "triangles": wl["triangles"],
+            "l2": f"inputs larger than L2 (ray queues {wave_paths * 112 / 1e9:.1f} GB per wave; "
+                  f"BVH + triangles {wl['triangles'] * 68 / 1e6:.0f} MB)",
+            "parallelism": f"replicas x{world}"}
 
 
 def run_reference(args, wl):
     world, rank, local, dist = dist_init()
     if rank != 0:
         return 0
-    pkg = load_pkg()
     threads = os.cpu_count() or 1
     rows, spp = args.ref_rows, args.ref_spp
     for _ in range(args.warmup):
-        cpu_sample(pkg, wl, threads, rows, spp, seed=17)
+        cpu_sample(wl, threads, rows, spp, seed=17)
     total_rays, total_s = 0, 0.0
     sample = ""
     for k in range(args.steps):
-        rays, dt, sample = cpu_sample(pkg, wl, threads, rows, spp, seed=100 + k)
+        rays, dt, sample = cpu_sample(wl, threads, rows, spp, seed=100 + k)
         total_rays += rays
         total_s += dt
     value = total_rays / total_s / 1e6
@@ -229,9 +255,10 @@ def run_reference(args, wl):
         "impl": "reference", "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * total_s / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": wl["name"], "policy": "none", "sample": sample},
+        "config": workload_config(wl, args, world),
         "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": threads, "kind": "port",
-                         "sample": sample + "; oracle port of the reference loop (Embree/TBB absent on the host)"},
+                         "sample": sample + " (Embree and TBB, which the reference's own build needs, are absent "
+                                            "on the GPU host)"},
         "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -400,8 +427,8 @@ def main() -> int:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--trace-variant", type=int, default=-1)
     ap.add_argument("--blocks-per-sm", type=int, default=0)
-    ap.add_argument("--ref-rows", type=int, default=256)
-    ap.add_argument("--ref-spp", type=int, default=16)
+    ap.add_argument("--ref-rows", type=int, default=REF_ROWS, help="CPU legs: rows of the timed band")
+    ap.add_argument("--ref-spp", type=int, default=REF_SPP, help="CPU legs: samples per pixel of the timed band")
     ap.add_argument("--bvh", default="ploc", choices=["ploc", "lbvh", "wide", "ploc4"])
     ap.add_argument("--autotune", type=int, default=0, help="run wf_autotune on the workload before timing")
     ap.add_argument("--speculative", type=int, default=0, help="1 = speculative while-while traversal")
@@ -411,6 +438,10 @@ def main() -> int:
     ap.add_argument("--cost-rr", type=int, default=0, help="cost-aware RR fed by the live device CostTracker")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 0)
+    if args.impl == "reference" and args.workload in ("c3", "c4"):
+        print(json.dumps({"impl": "reference", "unavailable": "the reference has no batched or served form: its "
+                          "loop renders one scene per call (src/render/WavefrontRenderer.cpp:94-399)"}), flush=True)
+        return 0
     if args.workload == "c3":
         return run_batched(args)
     if args.workload == "c4":
@@ -507,12 +538,8 @@ def main() -> int:
         "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": wl["name"], "policy": args.policy, "ray_sort": bool(args.ray_sort),
-                   "env_nee": bool(args.env_nee), "adaptive": bool(args.adaptive), "cost_aware_rr": bool(args.cost_rr),
-                   "triangles": info.num_triangles, "spp_per_wave": args.spp_per_wave or "auto",
-                   "l2": f"inputs larger than L2 (ray queues {W * H * min(wl['spp'], max(1, (1 << 27) // (W * H))) * 112 / 1e9:.1f} GB "
-                         f"per wave; BVH + triangles {info.num_triangles * 68 / 1e6:.0f} MB)",
-                   "parallelism": f"replicas x{world}"},
+        "config": workload_config(wl, args, world),
+        "spp_per_wave": args.spp_per_wave or "auto",
         "samples_per_s": samples_all / (ms_max / 1e3),
         "closest_rays_per_step": stats[0]["closest_rays"], "shadow_rays_per_step": stats[0]["shadow_rays"],
         "stage_ms_per_step": {k: sum(s[k] for s in stats) / args.steps for k in
@@ -536,10 +563,14 @@ def main() -> int:
         "tuning": dict(ctx.get_tuning(), autotuned=bool(args.autotune), autotune_wave_ms=tune_ms),
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        rays, dt, sample = cpu_sample(pkg, wl, os.cpu_count() or 1, rows=wl["height"], spp=wl.get("cpu_spp", 32),
-                                      seed=7)
-        line["cpu_baseline"] = {"value": rays / dt / 1e6, "unit": "Mrays/s", "cores": os.cpu_count() or 1,
-                                "kind": "port", "sample": sample}
+        # the same band as --impl reference, repeated for >= 10 s of CPU work
+        threads = os.cpu_count() or 1
+        rays, dt, k = 0, 0.0, 0
+        while dt < 10.0 and k < 16:
+            r, t, sample = cpu_sample(wl, threads, args.ref_rows, args.ref_spp, seed=100 + k)
+            rays, dt, k = rays + r, dt + t, k + 1
+        line["cpu_baseline"] = {"value": rays / dt / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "port",
+                                "sample": f"{k} runs of the {sample}"}
     if rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()

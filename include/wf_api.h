@@ -382,8 +382,10 @@ int wf_generate_primary_host(wf_ctx* ctx, const wf_camera* camera, int32_t width
 
 /* RayQueue sort for callers that cannot allocate device memory.  This entry
  * point has no counterpart in the reference.  It computes the same keys and
- * permutation as wf_ray_schedule_host, but takes DEVICE pointers (inputs and
- * outputs owned by the caller), needs no context, and calls no cudaMalloc,
+ * permutation as wf_ray_schedule_host, but the ray columns and the outputs
+ * are DEVICE pointers owned by the caller, while bounds_min / bounds_max are
+ * HOST arrays of 3 floats read during the call.  It needs no context and calls
+ * no cudaMalloc,
  * cudaFree or other allocating routine: its scratch is one file-scope device
  * array sized for WF_STATIC_SCHEDULE_MAX_RAYS rays (~25 MB, held by every GPU
  * that loads the library until the process exits).  Callers it is for: code
@@ -397,7 +399,11 @@ int wf_generate_primary_host(wf_ctx* ctx, const wf_camera* camera, int32_t width
  *    calls whose GPU work overlaps (other streams, other host threads) race.
  *    Serialise them on one stream.
  *  - n > WF_STATIC_SCHEDULE_MAX_RAYS returns WF_ERR_CAPACITY and enqueues
- *    nothing.  out_keys may be NULL. */
+ *    nothing.  out_keys may be NULL.
+ *  - A launch error already pending on the calling thread (left by earlier,
+ *    unrelated work) is not cleared: the call returns WF_ERR_CUDA and
+ *    enqueues nothing.  WF_ERR_CUDA after work was enqueued means one of this
+ *    call's own launches failed. */
 #define WF_STATIC_SCHEDULE_MAX_RAYS (1 << 20)
 int wf_ray_schedule_static(void* stream, int64_t n, const float* origins_x, const float* origins_y,
                            const float* origins_z, const float* dirs_x, const float* dirs_y,

@@ -24,25 +24,29 @@ HERE = Path(__file__).resolve().parent
 ROOT = HERE.parent
 PORT_LIB = HERE / "build" / "liboracle.so"
 REF_LIB = HERE / "_ref" / "libwfref.so"
-REF_SRC = Path(os.environ.get("WF_REFERENCE_DIR", "/root/reference"))
+# The reference checkout: WF_REFERENCE_DIR, else a `reference` directory
+# beside this repository.  Only the development machine has one.
+REF_SRC = Path(os.environ.get("WF_REFERENCE_DIR", str(ROOT.parent / "reference")))
 
 
-def _wf():
-    """The binding module (for its ctypes structs), shared with the caller."""
+def _abi():
+    """include/wf_abi.py: the ABI's ctypes structs, shared with the product's
+    binding.  It is pure Python: importing it loads no library."""
     import sys
 
-    if "wavefront_gb300" in sys.modules:
-        return sys.modules["wavefront_gb300"]
-    spec = importlib.util.spec_from_file_location("wavefront_gb300", ROOT / "wavefront-renderer_gb300" / "__init__.py")
+    if "wf_abi" in sys.modules:
+        return sys.modules["wf_abi"]
+    spec = importlib.util.spec_from_file_location("wf_abi", ROOT / "include" / "wf_abi.py")
     m = importlib.util.module_from_spec(spec)
-    sys.modules["wavefront_gb300"] = m
+    sys.modules["wf_abi"] = m
     spec.loader.exec_module(m)
     return m
 
 
-wf = _wf()
+wf = _abi()
 f32p, i32p, u8p, f64p, i64p, u64p = wf.f32p, wf.i32p, wf.u8p, wf.f64p, wf.i64p, wf.u64p
 ptr = wf.ptr
+render_params = wf.render_params
 
 
 def build_port() -> Path:
@@ -53,7 +57,7 @@ def build_port() -> Path:
 def build_ref() -> Path | None:
     if not (REF_SRC / "src" / "render" / "WavefrontRenderer.cpp").exists():
         return None
-    subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REF={REF_SRC}"], check=True)
+    subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REF={REF_SRC.resolve()}"], check=True)
     return REF_LIB
 
 
@@ -69,7 +73,8 @@ def port_lib() -> C.CDLL:
     global _port
     if _port is not None:
         return _port
-    if not PORT_LIB.exists() or PORT_LIB.stat().st_mtime < (HERE / "wf_oracle.cpp").stat().st_mtime:
+    sources = [HERE / "wf_oracle.cpp", ROOT / "wavefront-renderer_gb300" / "csrc" / "wf_scenes.cpp"]
+    if not PORT_LIB.exists() or PORT_LIB.stat().st_mtime < max(p.stat().st_mtime for p in sources):
         build_port()
     lib = C.CDLL(str(PORT_LIB))
     V = C.c_void_p
@@ -94,6 +99,11 @@ def port_lib() -> C.CDLL:
         "orc_render_window_counts": ([V, C.POINTER(wf.WfRenderParams), C.c_int32, C.c_int32, C.c_int32,
                                       C.c_int32, C.c_int32, f32p, i32p, C.POINTER(OrcCounters)], None),
         "orc_cost_tracker_relative": ([C.c_int32, C.c_int64, i32p, f64p, f64p], None),
+        "wf_camera_make": ([f32p, f32p, f32p, C.c_float, C.c_int32, C.c_int32, C.POINTER(wf.WfCamera)], C.c_int),
+        "wf_host_scene_generate": ([C.c_int32, C.c_uint64, C.POINTER(V)], C.c_int),
+        "wf_host_scene_describe": ([V, C.POINTER(wf.WfSceneDesc)], C.c_int),
+        "wf_host_scene_camera": ([V, C.c_int32, C.c_int32, C.POINTER(wf.WfCamera)], C.c_int),
+        "wf_host_scene_free": ([V], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -101,6 +111,43 @@ def port_lib() -> C.CDLL:
         fn.restype = res
     _port = lib
     return lib
+
+
+class HostScene:
+    """A procedural workload built by the generator compiled into
+    liboracle.so (the same source as the GPU library's wf_host_scene_*):
+    0 Cornell box, 1 icosphere scene, 2 lattice, 3 Cornell variants, 100/102
+    small variants, 104 Cornell box under a directional light."""
+
+    def __init__(self, config: int, seed: int = 1):
+        lib = port_lib()
+        self._lib = lib
+        self._h = C.c_void_p()
+        if lib.wf_host_scene_generate(config, seed, C.byref(self._h)) != 0:
+            raise RuntimeError(f"scene generator: config {config} failed")
+        self.desc = wf.WfSceneDesc()
+        lib.wf_host_scene_describe(self._h, C.byref(self.desc))
+        self.config = config
+
+    def camera(self, width: int, height: int):
+        cam = wf.WfCamera()
+        if self._lib.wf_host_scene_camera(self._h, width, height, C.byref(cam)) != 0:
+            raise RuntimeError("scene camera failed")
+        return cam
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            self._lib.wf_host_scene_free(self._h)
+            self._h = None
+
+
+def camera_make(look_from, look_at, up, vfov, width, height):
+    """Camera::Camera (include/core/Camera.h:13-33) as the oracle restates it."""
+    cam = wf.WfCamera()
+    a = [np.asarray(v, dtype=np.float32) for v in (look_from, look_at, up)]
+    if port_lib().wf_camera_make(ptr(a[0]), ptr(a[1]), ptr(a[2]), vfov, width, height, C.byref(cam)) != 0:
+        raise RuntimeError("camera_make failed")
+    return cam
 
 
 def _cols(a: np.ndarray) -> list:
@@ -274,6 +321,7 @@ def ref_lib() -> C.CDLL:
         "ref_render": ([V, f32p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_float, C.c_char_p, f32p],
                        None),
         "ref_render_adaptive": ([V, f32p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_float, f32p], None),
+        "ref_front_face_stats": ([C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)], None),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -336,6 +384,14 @@ class Ref:
         cam12 = np.ascontiguousarray(cam12, np.float32)
         self.lib.ref_render_adaptive(self.h, ptr(cam12), w, h, spp, max_depth, threshold, ptr(img))
         return img.reshape(h, w, 3)
+
+
+def ref_front_face_stats() -> tuple[int, int]:
+    """(unresolved, ambiguous) rebuilt-record frontFace lookups of the last
+    reference render (shims/core/HitRecord.h); unresolved must be 0."""
+    a, b = C.c_longlong(), C.c_longlong()
+    ref_lib().ref_front_face_stats(C.byref(a), C.byref(b))
+    return a.value, b.value
 
 
 def write_pfm(path, rgb: np.ndarray) -> None:

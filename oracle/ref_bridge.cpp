@@ -306,6 +306,7 @@ void ref_render(void* sp, const float c12[12], int w, int h, int spp, int max_de
     if (env_path) r.environmentMapPath = env_path;
     void (*old_term)(int) = std::signal(SIGTERM, SIG_DFL);
     void (*old_int)(int) = std::signal(SIGINT, SIG_DFL);
+    wfshim::set_render_scene(s);
     {
         Silence q;
         r.renderScene(*s, cam, img);
@@ -335,6 +336,7 @@ void ref_render_adaptive(void* sp, const float c12[12], int w, int h, int spp, i
     r.enableSampleLogging = true;
     void (*old_term)(int) = std::signal(SIGTERM, SIG_DFL);
     void (*old_int)(int) = std::signal(SIGINT, SIG_DFL);
+    wfshim::set_render_scene(s);
     {
         Silence q;
         r.renderScene(*s, cam, img);
@@ -346,6 +348,14 @@ void ref_render_adaptive(void* sp, const float c12[12], int w, int h, int spp, i
         image_out[3 * i + 1] = img.pixels[i].y;
         image_out[3 * i + 2] = img.pixels[i].z;
     }
+}
+
+// Rebuilt hit records whose frontFace the shim could not resolve, and those
+// settled by the hit point (shims/core/HitRecord.h), over the last render.
+void ref_front_face_stats(long long* unresolved, long long* ambiguous)
+{
+    *unresolved = wfshim::front_face_unresolved();
+    *ambiguous = wfshim::front_face_ambiguous();
 }
 
 }  // extern "C"

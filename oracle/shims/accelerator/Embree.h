@@ -13,6 +13,16 @@
 
 struct Scene;
 
+namespace wfshim {
+// The scene whose rebuilt hit records resolve frontFace (core/HitRecord.h shim);
+// set by the bridge before WavefrontRenderer::renderScene.
+void set_render_scene(const Scene* scene);
+// Rebuilt records whose triangle could not be found (0 in a correct run), and
+// those whose candidate triangles disagreed and were settled by the hit point.
+long long front_face_unresolved();
+long long front_face_ambiguous();
+}  // namespace wfshim
+
 class EmbreeAccelerator
 {
   public:

@@ -5,6 +5,7 @@
 #include <geometry/Triangle.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <numeric>
@@ -255,3 +256,80 @@ bool EmbreeAccelerator::occluded(const Point3& origin, const Vec3& direction, fl
     }
     return false;
 }
+
+// frontFace of a HitRecord rebuilt by ShadingQueue::getHitRecord (see
+// shims/core/HitRecord.h).  The record keeps its material, its triangle index
+// within the mesh and the face-forwarded geometric normal that fill()
+// computed; the meshes with that material that own such a triangle are the
+// candidates, and the one whose outward normal equals the record's normal
+// (frontFace true) or its negation (false) answers.  Candidates that agree
+// need no further test; if they disagree, the triangle whose plane holds the
+// hit point decides.
+namespace wfshim {
+namespace {
+std::atomic<const Scene*> g_render_scene{nullptr};
+std::vector<std::vector<int>> g_meshes_of_material;
+std::atomic<long long> g_unresolved{0}, g_ambiguous{0};
+
+inline bool same(const Vec3& a, const Vec3& b) { return a.x == b.x && a.y == b.y && a.z == b.z; }
+}  // namespace
+
+void set_render_scene(const Scene* scene)
+{
+    g_meshes_of_material.clear();
+    if (scene) {
+        g_meshes_of_material.resize(scene->materials.size());
+        for (int m = 0; m < (int)scene->meshes.size(); ++m) {
+            int mat = scene->meshes[m].materialID;
+            if (mat >= 0 && mat < (int)g_meshes_of_material.size()) g_meshes_of_material[mat].push_back(m);
+        }
+    }
+    g_unresolved = 0;
+    g_ambiguous = 0;
+    g_render_scene = scene;
+}
+
+long long front_face_unresolved() { return g_unresolved.load(); }
+long long front_face_ambiguous() { return g_ambiguous.load(); }
+
+bool rebuilt_front_face(const HitRecord& r)
+{
+    const Scene* s = g_render_scene.load();
+    if (!s || r.materialID < 0 || r.materialID >= (int)g_meshes_of_material.size()) {
+        ++g_unresolved;
+        return true;
+    }
+    int yes = 0, no = 0;
+    bool best_answer = true;
+    float best_dist = INFINITY;
+    for (int m : g_meshes_of_material[r.materialID]) {
+        const Mesh& mesh = s->meshes[m];
+        if (r.triangleIndex < 0 || r.triangleIndex >= mesh.triangleCount()) continue;
+        const Point3& v0 = mesh.vertexPositions[mesh.triangleIndices[3 * r.triangleIndex + 0]];
+        const Point3& v1 = mesh.vertexPositions[mesh.triangleIndices[3 * r.triangleIndex + 1]];
+        const Point3& v2 = mesh.vertexPositions[mesh.triangleIndices[3 * r.triangleIndex + 2]];
+        Vec3 edge1 = v1 - v0;
+        Vec3 edge2 = v2 - v0;
+        Vec3 outward = edge1.cross(edge2).normalized();
+        bool answer;
+        if (same(r.normal, outward))
+            answer = true;
+        else if (same(r.normal, outward * -1.0f))
+            answer = false;
+        else
+            continue;
+        (answer ? yes : no)++;
+        float dist = std::fabs((r.point - v0).dot(outward));
+        if (dist < best_dist) {
+            best_dist = dist;
+            best_answer = answer;
+        }
+    }
+    if (yes + no == 0) {
+        ++g_unresolved;
+        return true;
+    }
+    if (yes && no) ++g_ambiguous;
+    return yes && !no ? true : (no && !yes ? false : best_answer);
+}
+}  // namespace wfshim

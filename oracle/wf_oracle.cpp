@@ -1024,6 +1024,39 @@ void orc_scene_bounds(const orc_scene* s, float bmin[3], float bmax[3])
 
 float orc_scene_total_emissive_area(const orc_scene* s) { return s->total_emissive_area; }
 
+// Camera::Camera, include/core/Camera.h:13-33, float arithmetic in the
+// reference's order.  It carries the ABI's name because the procedural scene
+// generator compiled into this library (wavefront-renderer_gb300/csrc/
+// wf_scenes.cpp: the workload definition, shared so that the oracle and the
+// GPU render identical scenes) calls it for a scene's default camera; the
+// library is linked -Bsymbolic, so that call stays inside it.
+int wf_camera_make(const float look_from[3], const float look_at[3], const float up[3], float vfov, int32_t w,
+                   int32_t h, wf_camera* out)
+{
+    if (!look_from || !look_at || !up || !out || w <= 0 || h <= 0) return WF_ERR_INVALID_ARGUMENT;
+    float aspect = static_cast<float>(w) / h;
+    float theta = vfov * 3.14159265f / 180.0f;
+    float view_h = 2.0f * std::tan(theta / 2.0f);
+    float view_w = aspect * view_h;
+    V3 from{look_from[0], look_from[1], look_from[2]};
+    V3 at{look_at[0], look_at[1], look_at[2]};
+    V3 upd{up[0], up[1], up[2]};
+    V3 forward = normalized(from - at);
+    V3 right = normalized(cross(upd, forward));
+    V3 camera_up = cross(forward, right);
+    V3 horizontal = right * view_w;
+    V3 vertical = camera_up * view_h;
+    V3 top_left = from - horizontal / 2.0f - vertical / 2.0f - forward;
+    const V3 fields[4] = {from, top_left, horizontal, vertical};
+    float* dst[4] = {out->origin, out->top_left, out->horizontal, out->vertical};
+    for (int k = 0; k < 4; ++k) {
+        dst[k][0] = fields[k].x;
+        dst[k][1] = fields[k].y;
+        dst[k][2] = fields[k].z;
+    }
+    return WF_OK;
+}
+
 void orc_camera_get_ray(const wf_camera* cam, float u, float v, float origin[3], float dir[3])
 {
     V3 o, d;

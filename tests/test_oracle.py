@@ -16,6 +16,24 @@ from conftest import GOLDEN, rays_in_box
 from test_gpu_parity import _desc
 
 
+# The oracle's tests load no GPU library: the ABI's structs come from
+# include/wf_abi.py and the workload scenes from the generator compiled into
+# liboracle.so.
+@pytest.fixture(scope="module")
+def wf(orc):
+    return orc.wf
+
+
+@pytest.fixture(scope="module")
+def scene0(orc):
+    return orc.HostScene(0)
+
+
+@pytest.fixture(scope="module")
+def scene_small(orc):
+    return orc.HostScene(100, seed=3)
+
+
 def _tri_scene(wf, v0, v1, v2):
     x, y, z = (np.array(a, np.float32) for a in zip(v0, v1, v2))
     return _desc(wf, [(x, y, z, np.array([0, 1, 2], np.int32), 0)],
@@ -258,21 +276,15 @@ def test_port_render_statistics_match_reference_live(wf, orc, scene0):
     assert abs(np.median(P.var(0) / (R.var(0) + 1e-30)) - 1.0) < 0.2
 
 
-def _c102_no_glass(wf, orc, tmp_path):
-    """Config 102 (16 x 16 textured meshes under an HDRI) with its glass
-    materials made Lambertian and the HDRI clipped at 2.0 (keeps the variance
-    small).  Glass is left out: ShadingQueue::getHitRecord
-    (include/scheduling/ShadingQueue.h:144-158) never sets HitRecord::frontFace
-    (include/core/HitRecord.h:15, no initialiser), so the reference's
-    dielectric reads an indeterminate value and its mean changes with the
-    worker count.  The port follows the value the intersection computed."""
-    import ctypes as C
-    hs = wf.HostScene(102)
+def _c102_clipped(wf, orc, tmp_path):
+    """Config 102 (16 x 16 textured, metal and glass meshes under an HDRI)
+    with the HDRI clipped at 2.0 (keeps the variance small).  Glass stays in:
+    the reference reads HitRecord::frontFace uninitialised after
+    ShadingQueue::getHitRecord (include/scheduling/ShadingQueue.h:144-158),
+    and the shim (oracle/shims/core/HitRecord.h) gives it the value the
+    intersection computed, which is what the port and the GPU carry."""
+    hs = orc.HostScene(102)
     d = hs.desc
-    mats = (wf.WfMaterial * d.num_materials).from_address(C.addressof(d.materials.contents))
-    for m in mats:
-        if m.type == 4:
-            m.type = 0
     env = np.minimum(orc.scene_environment(d), 2.0).astype(np.float32)
     np.ctypeslib.as_array(d.environment.rgb, shape=(env.size,))[:] = env.ravel()
     path = tmp_path / "env.pfm"
@@ -287,7 +299,7 @@ def test_port_textured_hdri_statistics_match_reference_live(wf, orc, tmp_path):
     standard errors)."""
     if not orc.ref_available():
         pytest.skip("reference checkout not present")
-    hs, d, env_path = _c102_no_glass(wf, orc, tmp_path)
+    hs, d, env_path = _c102_clipped(wf, orc, tmp_path)
     port, ref = orc.Port(d), orc.Ref(d, True)
     W = H = 32
     spp, N = 64, 12
@@ -314,7 +326,7 @@ def test_port_env_nee_matches_analytic_irradiance(wf, orc, clip):
     independent runs (plus 1e-3 relative for the finite plane)."""
     from conftest import PlaneUnderSky
 
-    hs = wf.HostScene(102)  # owns the map scene_environment copies
+    hs = orc.HostScene(102)  # owns the map scene_environment copies
     env = orc.scene_environment(hs.desc)
     if clip is not None:
         env = np.minimum(env, clip)
@@ -322,7 +334,7 @@ def test_port_env_nee_matches_analytic_irradiance(wf, orc, clip):
     port = orc.Port(sky.desc)
     W = H = 32
     spp, N = 256, 8
-    cam = sky.camera(wf, W, H)
+    cam = sky.camera(orc, W, H)
     X = np.array([port.render_window(wf.render_params(W, H, spp, 2, cam, seed=900 + k, env_nee=True),
                                      0, 0, W, H)[0] / spp for k in range(N)], np.float64)
     per_run = X.mean(axis=(1, 2))
@@ -338,11 +350,11 @@ def test_port_env_nee_matches_analytic_irradiance(wf, orc, clip):
 
 def test_port_env_nee_mean_matches_reference_live(wf, orc, tmp_path):
     """With environment NEE on, the port's per-pixel means still agree with
-    the reference's miss-only renderScene (config 102 without glass, HDRI
+    the reference's miss-only renderScene (config 102 with its glass, HDRI
     clipped at 2.0 so both estimators are well behaved)."""
     if not orc.ref_available():
         pytest.skip("reference checkout not present")
-    hs, d, env_path = _c102_no_glass(wf, orc, tmp_path)
+    hs, d, env_path = _c102_clipped(wf, orc, tmp_path)
     port, ref = orc.Port(d), orc.Ref(d, True)
     W = H = 32
     spp, N = 64, 12

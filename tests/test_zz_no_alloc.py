@@ -49,7 +49,43 @@ def test_static_schedule_matches_allocating_entry_point(wf):
         torch.cuda.synchronize()
         assert np.array_equal(perm.cpu().numpy(), want_perm)
         assert np.array_equal(keys.cpu().numpy().view(np.uint64), want_keys)
+    # Its defining property: once the library's module is loaded (the calls
+    # above), a call takes no device memory, so the device's free memory is
+    # the same before and after it.
+    free_before = torch.cuda.mem_get_info()[0]
+    rc = lib.wf_ray_schedule_static(None, n, *[c.data_ptr() for c in cols], wf.ptr(bmin), wf.ptr(bmax),
+                                    perm.data_ptr(), None)
+    torch.cuda.synchronize()
+    assert rc == wf.WF_OK
+    assert torch.cuda.mem_get_info()[0] == free_before
+    assert np.array_equal(perm.cpu().numpy(), want_perm)
     ctx.close()
+
+
+def test_static_schedule_matches_the_reference_golden_permutation(wf):
+    """RayQueue::schedule's permutation and keys as the reference's own code
+    computed them (tests/golden/ray_schedule.npz, include/scheduling/
+    RayQueue.h:135-179), through the allocation-free entry point."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device visible to torch")
+    from conftest import GOLDEN
+
+    g = np.load(GOLDEN / "ray_schedule.npz")
+    lib = wf.load_library()
+    n = len(g["perm"])
+    cols = [torch.from_numpy(np.ascontiguousarray(g[a][:, k])).cuda() for a in ("o", "d") for k in range(3)]
+    perm = torch.full((n,), -1, dtype=torch.int32, device="cuda")
+    keys = torch.zeros((n,), dtype=torch.int64, device="cuda")
+    bmin = np.ascontiguousarray(g["bmin"], np.float32)
+    bmax = np.ascontiguousarray(g["bmax"], np.float32)
+    torch.cuda.synchronize()
+    rc = lib.wf_ray_schedule_static(None, n, *[c.data_ptr() for c in cols], wf.ptr(bmin), wf.ptr(bmax),
+                                    perm.data_ptr(), keys.data_ptr())
+    torch.cuda.synchronize()
+    assert rc == wf.WF_OK
+    assert np.array_equal(perm.cpu().numpy(), g["perm"])
+    assert np.array_equal(keys.cpu().numpy().view(np.uint64), g["keys"])
 
 
 def test_static_schedule_rejects_sizes_beyond_its_scratch(wf):

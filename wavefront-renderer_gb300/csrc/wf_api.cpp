@@ -39,7 +39,9 @@ void free_all(std::vector<void*>& v)
 LaunchCfg persist_cfg(const wf_ctx* c)
 {
     int per_sm = c->tuning.persistent_blocks_per_sm > 0 ? c->tuning.persistent_blocks_per_sm : 16;
-    LaunchCfg cfg{c->num_sms * per_sm, 128, c->tuning.trace_variant, c->tuning.speculative_traversal};
+    LaunchCfg cfg{c->num_sms * per_sm, 128};
+    cfg.variant = c->tuning.trace_variant;
+    cfg.speculative = c->tuning.speculative_traversal;
     cfg.l2_bytes = c->l2_bytes;
     cfg.shade_grid = c->num_sms * c->shade_per_sm;
     cfg.shade_grid_other = c->num_sms * c->shade_per_sm_other;

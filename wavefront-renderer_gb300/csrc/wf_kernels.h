@@ -19,6 +19,7 @@ struct ShadeParams {
     const float* rel_cost_material;  // device, float(relativeCost) per material, or null
 };
 
+// Build it as LaunchCfg{grid, block} and assign the other members by name.
 struct LaunchCfg {
     int grid;
     int block;

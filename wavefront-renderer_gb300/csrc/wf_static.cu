@@ -87,6 +87,9 @@ extern "C" int wf_ray_schedule_static(void* stream, int64_t n, const float* ox, 
     if (n < 0 || !bounds_min || !bounds_max) return WF_ERR_INVALID_ARGUMENT;
     if (n > kMaxRays) return WF_ERR_CAPACITY;  // beyond the static scratch
     if (n > 0 && (!ox || !oy || !oz || !dx || !dy || !dz || !out_sorted_indices)) return WF_ERR_INVALID_ARGUMENT;
+    // An error left pending by earlier work on this thread stays the caller's:
+    // report it without clearing it, and enqueue nothing.
+    if (cudaPeekAtLastError() != cudaSuccess) return WF_ERR_CUDA;
     DeviceSetup* dev = nullptr;
     int rc = setup_current_device(&dev);
     if (rc != WF_OK) return rc;
@@ -105,6 +108,7 @@ extern "C" int wf_ray_schedule_static(void* stream, int64_t n, const float* ox, 
     k_store_count<<<1, 1, 0, s>>>(count, (unsigned long long)n);
     wf::launch_ray_keys_raw(n, ox, oy, oz, dx, dy, dz, bounds_min, bounds_max, keys, vals,
                             wf::LaunchCfg{dev->num_sms * 8, 256}, s);
+    if (cudaGetLastError() != cudaSuccess) return WF_ERR_CUDA;
     if (out_keys && cudaMemcpyAsync(out_keys, keys, sizeof(uint64_t) * (size_t)n, cudaMemcpyDeviceToDevice, s) !=
                         cudaSuccess)
         return WF_ERR_CUDA;
@@ -112,6 +116,7 @@ extern "C" int wf_ray_schedule_static(void* stream, int64_t n, const float* ox, 
     uint32_t* rv = nullptr;
     wf::RadixSortArgs a{keys, vals, keys_tmp, vals_tmp, hist, count, nb, 0, 33, &rk, &rv};
     wf::radix_sort_pairs(a, s);
+    if (cudaGetLastError() != cudaSuccess) return WF_ERR_CUDA;
     int grid = (int)((n + 255) / 256);
     if (grid > dev->num_sms * 8) grid = dev->num_sms * 8;
     k_emit_permutation<<<grid, 256, 0, s>>>(rv, out_sorted_indices, n);
