@@ -265,6 +265,26 @@ def run_reference(args, wl):
     return 0
 
 
+def image_mse(img, wl, spp):
+    """MSE of the fixture window of a rendered image against the reference's
+    FP64 mean of that window (tests/golden/c<config>_fp64_crop.npz), and what
+    the per-sample variance predicts for it: sigma^2 (1/spp + 1/oracle_spp)."""
+    p = ROOT / "tests" / "golden" / f"c{wl['config']}_fp64_crop.npz"
+    if not p.exists():
+        return None
+    g = np.load(p)
+    if tuple(int(v) for v in g["image_size"]) != (wl["width"], wl["height"]) or int(g["max_depth"]) != wl["depth"]:
+        return None
+    x0, y0, w, h = (int(v) for v in g["window"])
+    win = img[y0:y0 + h, x0:x0 + w].astype(np.float64)
+    mean = g["mean"].astype(np.float64)
+    exp = float((g["sigma"].astype(np.float64) ** 2 * (1.0 / spp + 1.0 / float(g["spp"]))).mean())
+    mse = float(((win - mean) ** 2).mean())
+    return {"value": mse, "expected": exp, "ratio": mse / exp, "window": [x0, y0, w, h], "spp": spp,
+            "oracle": f"the reference's renderScene, FP64 mean over {int(g['spp'])} spp of the window",
+            "image": "the last end-to-end step's image"}
+
+
 def percentile(xs, q):
     return float(np.percentile(np.asarray(xs, dtype=np.float64), q)) if len(xs) else None
 
@@ -283,58 +303,89 @@ def c3_jobs(pkg, ctx, n, seed):
     return jobs
 
 
-def run_batched(args) -> int:
-    """Batched small renders (config 3): all jobs' rays share waves, the
-    bounce chain replays a captured CUDA graph; against the plain loop (each
-    job rendered alone, one host round trip per bounce)."""
-    world, rank, local, dist = dist_init()
-    pkg = load_pkg()
-    ctx = pkg.Context(local)
-    jobs = c3_jobs(pkg, ctx, args.jobs, seed=2026)
-    tv = max(args.trace_variant, 0)
+def batched_block(pkg, ctx, n_jobs: int, trace_variant: int) -> dict:
+    """Config 3: n_jobs jobs rendered in one call (all jobs' rays share
+    waves, the bounce chain replays a captured CUDA graph) against the plain
+    loop: each job rendered alone, its bounces issued back to back with
+    device-side counts (the single-job render's form; no graph).  Also the
+    jobs one at a time with graph replay, for reference."""
+    tv = max(trace_variant, 0)
+    jobs = c3_jobs(pkg, ctx, n_jobs, seed=2026)
+    paths = sum(j.width * j.height * j.samples_per_pixel for j in jobs)
+
+    def one_by_one(graph_mode):
+        ctx.set_tuning(tv, graph_mode=graph_mode)
+        ctx.timer_begin()
+        rays = 0
+        for j in jobs:
+            _, st = ctx.render_batch([j], want_images=False)
+            rays += st["closest_rays"] + st["shadow_rays"]
+        return rays, ctx.timer_end()
+
+    # warm-up: both single-job forms and the batched graph capture
+    for gm in (2, 0):
+        ctx.set_tuning(tv, graph_mode=gm)
+        for j in jobs[:8]:
+            ctx.render_batch([j], want_images=False)
     ctx.set_tuning(tv, graph_mode=0)
-    ctx.render_batch(jobs[:16], want_images=False)  # warm-up (captures the graph)
-    ctx.set_tuning(tv, graph_mode=2)
-    ctx.render_batch(jobs[:4], want_images=False)
-    # plain loop: one job per render, host round trip per bounce
-    ctx.set_tuning(tv, graph_mode=2)
-    ctx.timer_begin()
-    plain_rays = 0
-    for j in jobs:
-        _, st = ctx.render_batch([j], want_images=False)
-        plain_rays += st["closest_rays"] + st["shadow_rays"]
-    plain_ms = ctx.timer_end()
-    # batched: one call, waves shared by all jobs, graph replay
+    ctx.render_batch(jobs[:32], want_images=False)
+    plain_rays, plain_ms = one_by_one(2)
+    graph_rays, graph_ms = one_by_one(0)
     ctx.set_tuning(tv, graph_mode=0)
     ctx.timer_begin()
     _, st = ctx.render_batch(jobs, want_images=False)
     ms = ctx.timer_end()
+    ctx.set_tuning(tv)
     rays = st["closest_rays"] + st["shadow_rays"]
     value = rays / ms / 1e3
     plain = plain_rays / plain_ms / 1e3
-    paths = sum(j.width * j.height * j.samples_per_pixel for j in jobs)
+    return {"workload": f"c3_batched_{len(jobs)}_jobs_cornell_variants_64-256px_4-64spp_depth8",
+            "value": value, "unit": "Mrays/s", "ms": ms, "paths": paths, "waves": st["waves"],
+            "samples_per_s": paths / (ms / 1e3), "gpu_launches": st["kernel_launches"],
+            "form": "all jobs in shared waves, bounce chain replayed from a CUDA graph",
+            "plain_loop": {"value": plain, "unit": "Mrays/s", "ms": plain_ms,
+                           "form": "one job per render, bounces issued back to back with device-side counts"},
+            "one_job_per_call_graph_replay": {"value": graph_rays / graph_ms / 1e3, "unit": "Mrays/s",
+                                              "ms": graph_ms},
+            "speedup_vs_plain_loop": value / plain}
+
+
+def run_batched(args) -> int:
+    world, rank, local, dist = dist_init()
+    pkg = load_pkg()
+    ctx = pkg.Context(local)
+    b = batched_block(pkg, ctx, args.jobs, args.trace_variant)
     line = {
-        "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": 1, "warmup": 1,
-        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic",
-        "config": {"workload": f"c3_batched_{len(jobs)}_jobs_cornell_variants_depth8", "paths": paths,
-                   "form": "batched waves + CUDA graph bounce chain"},
-        "plain_loop": {"value": plain, "unit": "Mrays/s", "ms": plain_ms, "form": "one job per render"},
-        "speedup_vs_plain_loop": value / plain,
-        "samples_per_s": paths / (ms / 1e3), "waves": st["waves"], "gpu_launches": st["kernel_launches"],
+        "metric": METRIC, "value": b["value"], "unit": "Mrays/s", "n_gpus": world, "steps": 1, "warmup": 1,
+        "ms_per_step": b["ms"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic", "config": {"workload": b["workload"], "paths": b["paths"], "form": b["form"]},
+        "plain_loop": b["plain_loop"], "speedup_vs_plain_loop": b["speedup_vs_plain_loop"],
+        "samples_per_s": b["samples_per_s"], "waves": b["waves"], "gpu_launches": b["gpu_launches"],
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
     return 0
 
 
-def run_serving(args) -> int:
-    """Serving workload (config 4): Poisson arrivals over resident scenes of
-    configs 0, 1 and 3; admission by an HBM budget; progressive frames every
-    8 spp.  Reports Mrays/s and p50/p99 time-to-first-frame / to-complete."""
-    world, rank, local, dist = dist_init()
-    pkg = load_pkg()
-    ctx = pkg.Context(local)
+def _c0_oracle():
+    p = ROOT / "tests" / "golden" / "c0_fp64.npz"
+    if not p.exists():
+        return None
+    g = np.load(p)
+    return {k: g[k] for k in ("mean", "sigma", "spp")}
+
+
+def serving_block(pkg, ctx, duration: float, rate: float, budget_gb: float, drain: float,
+                  trace_variant: int) -> dict:
+    """Config 4: Poisson arrivals over resident scenes of configs 0, 1 and
+    16 config-3 variants; admission by an HBM budget; progressive frames every
+    8 spp.  Time to first frame (TTFF) and to completion (TTC) are taken over
+    every submitted job: a job without a frame (or not done) when the run ends
+    counts at the end time (censored), and the censored counts are given.
+    Jobs on the config-0 scene are 256 x 256 at depth 8, so each has an FP64
+    oracle (the reference's 16384-spp mean); their final images give a
+    per-job MSE.  Other jobs: resolution log-uniform in [128^2, 1024^2],
+    spp from {8, 32, 128}, depth 4-12."""
     rng = np.random.default_rng(4242)
     scenes = []
     for cfg in (0, 1):
@@ -343,64 +394,99 @@ def run_serving(args) -> int:
     for k in range(16):
         hs = pkg.HostScene(3, seed=k)
         scenes.append((ctx.add_scene(hs.desc), hs))
-    ctx.set_tuning(max(args.trace_variant, 0))
-    srv = pkg.Server(ctx, hbm_budget_bytes=int(args.budget_gb * (1 << 30)), frame_spp=8)
-    # warm-up: one small job per scene kind
-    for sid, hs in scenes[:3]:
+    ctx.set_tuning(max(trace_variant, 0))
+    srv = pkg.Server(ctx, hbm_budget_bytes=int(budget_gb * (1 << 30)), frame_spp=8)
+    for sid, hs in scenes[:3]:  # warm-up: one small job per scene kind
         srv.submit(pkg.make_job(sid, 64, 64, 8, 8, hs.camera(64, 64), seed=1))
-    for _ in range(10):
+    for _ in range(20):
         if srv.step()["running"] == 0:
             break
-    t_end = args.duration
-    lam = args.rate
     arrivals = []
     t = 0.0
-    while t < t_end:
-        t += rng.exponential(1.0 / lam)
+    while t < duration:
+        t += rng.exponential(1.0 / rate)
         side = int(round(np.exp(rng.uniform(np.log(128), np.log(1024)))))
         spp = int(rng.choice([8, 32, 128]))
         depth = int(rng.integers(4, 13))
         kind = int(rng.integers(0, 3))
+        if kind == 0:
+            side, depth = 256, 8
         sid, hs = scenes[kind] if kind < 2 else scenes[2 + int(rng.integers(0, 16))]
-        arrivals.append((t, pkg.make_job(sid, side, side, spp, depth, hs.camera(side, side),
-                                         seed=int(rng.integers(1, 2**31)))))
-    ids = []
+        arrivals.append((t, kind, pkg.make_job(sid, side, side, spp, depth, hs.camera(side, side),
+                                               seed=int(rng.integers(1, 2**31)))))
+    ids, kinds = [], []
     rays, dev_ms = 0, 0.0
     base = srv.clock()
     k = 0
+    terminal = (pkg.JOB_DONE, pkg.JOB_REJECTED, pkg.JOB_CANCELLED)
     while True:
         now = srv.clock() - base
         while k < len(arrivals) and arrivals[k][0] <= now:
-            ids.append(srv.submit(arrivals[k][1]))
+            ids.append(srv.submit(arrivals[k][2]))
+            kinds.append(arrivals[k][1])
             k += 1
-        if now > t_end:
-            # after the last arrival, optionally keep serving until every
-            # submitted job is done (so the latency percentiles cover all jobs)
-            terminal = (pkg.JOB_DONE, pkg.JOB_REJECTED, pkg.JOB_CANCELLED)
-            if now > t_end + args.drain or all(srv.status(i)["state"] in terminal for i in ids):
+        if now > duration:
+            if now > duration + drain or all(srv.status(i)["state"] in terminal for i in ids):
                 break
         info = srv.step()
         rays += info["rays_traced"]
         dev_ms += info["step_ms"]
     wall = srv.clock() - base
+    t_end = base + wall
     st = [srv.status(i) for i in ids]
-    ttff = [s["t_first_frame"] - s["t_submit"] for s in st if s["t_first_frame"] >= 0]
-    ttc = [s["t_done"] - s["t_submit"] for s in st if s["state"] == pkg.JOB_DONE]
-    line = {
-        "metric": METRIC, "value": rays / wall / 1e6, "unit": "Mrays/s", "n_gpus": world, "steps": 1,
-        "warmup": 1, "ms_per_step": wall * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "c4_serving_poisson", "rate_per_s": lam, "duration_s": t_end, "drain_s": args.drain,
-                   "hbm_budget_gb": args.budget_gb, "frame_spp": 8,
-                   "scenes": "config 0, config 1 (1.31 M tris), 16 config-3 variants"},
-        "device_busy_mrays_per_s": rays / (dev_ms / 1e3) / 1e6 if dev_ms else None,
-        "submitted": len(ids), "completed": len(ttc), "with_first_frame": len(ttff),
-        "rejected": sum(1 for s in st if s["state"] == pkg.JOB_REJECTED),
-        "queued_at_end": sum(1 for s in st if s["state"] == pkg.JOB_QUEUED),
-        "ttff_s": {"p50": percentile(ttff, 50), "p99": percentile(ttff, 99)},
-        "ttc_s": {"p50": percentile(ttc, 50), "p99": percentile(ttc, 99)},
-    }
+    ttff = [(s["t_first_frame"] if s["t_first_frame"] >= 0 else t_end) - s["t_submit"] for s in st]
+    ttc = [(s["t_done"] if s["state"] == pkg.JOB_DONE else t_end) - s["t_submit"] for s in st]
+    done_ttc = [s["t_done"] - s["t_submit"] for s in st if s["state"] == pkg.JOB_DONE]
+    g = _c0_oracle()
+    mses = []
+    if g is not None:
+        for jid, kind, s, arr in zip(ids, kinds, st, arrivals):
+            if kind == 0 and s["state"] == pkg.JOB_DONE:
+                img = srv.image(jid, 256, 256).astype(np.float64)
+                spp = arr[2].samples_per_pixel
+                mse = float(((img - g["mean"]) ** 2).mean())
+                exp = float((g["sigma"].astype(np.float64) ** 2 * (1.0 / spp + 1.0 / float(g["spp"]))).mean())
+                mses.append((mse / exp, spp))
     srv.close()
+    ratio = [m for m, _ in mses]
+    return {
+        "workload": "c4_serving_poisson", "rate_per_s": rate, "duration_s": duration, "drain_s": drain,
+        "hbm_budget_gb": budget_gb, "frame_spp": 8,
+        "scenes": "config 0 (jobs 256^2, depth 8), config 1 (1.31 M tris), 16 config-3 variants",
+        "value": rays / wall / 1e6, "unit": "Mrays/s", "wall_s": wall,
+        "device_busy_mrays_per_s": rays / (dev_ms / 1e3) / 1e6 if dev_ms else None,
+        "submitted": len(ids), "completed": len(done_ttc),
+        "with_first_frame": sum(1 for s in st if s["t_first_frame"] >= 0),
+        "rejected": sum(1 for s in st if s["state"] == pkg.JOB_REJECTED),
+        "censored_ttff": sum(1 for s in st if s["t_first_frame"] < 0),
+        "censored_ttc": sum(1 for s in st if s["state"] != pkg.JOB_DONE),
+        "ttff_s": {"p50": percentile(ttff, 50), "p99": percentile(ttff, 99),
+                   "over": "all submitted jobs; jobs without a frame count at the end time"},
+        "ttc_s": {"p50": percentile(ttc, 50), "p99": percentile(ttc, 99),
+                  "over": "all submitted jobs; unfinished jobs count at the end time"},
+        "ttc_completed_only_s": {"p50": percentile(done_ttc, 50), "p99": percentile(done_ttc, 99)},
+        "c0_job_mse": {"jobs": len(mses),
+                       "mse_over_expected_median": float(np.median(ratio)) if ratio else None,
+                       "mse_over_expected_max": float(np.max(ratio)) if ratio else None,
+                       "oracle": "the reference's 16384-spp FP64 mean of config 0 at 256^2 (tests/golden/c0_fp64.npz)",
+                       "expected": "sigma^2 (1/spp + 1/16384) per pixel, from the oracle's per-sample variance"},
+    }
+
+
+def run_serving(args) -> int:
+    world, rank, local, dist = dist_init()
+    pkg = load_pkg()
+    ctx = pkg.Context(local)
+    b = serving_block(pkg, ctx, args.duration, args.rate, args.budget_gb, args.drain, args.trace_variant)
+    line = {
+        "metric": METRIC, "value": b["value"], "unit": "Mrays/s", "n_gpus": world, "steps": 1,
+        "warmup": 1, "ms_per_step": b["wall_s"] * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {k: b[k] for k in ("workload", "rate_per_s", "duration_s", "drain_s", "hbm_budget_gb",
+                                     "frame_spp", "scenes")},
+        **{k: v for k, v in b.items() if k not in ("value", "unit", "workload", "rate_per_s", "duration_s",
+                                                   "drain_s", "hbm_budget_gb", "frame_spp", "scenes")},
+    }
     if rank == 0:
         print(json.dumps(line), flush=True)
     return 0
@@ -424,6 +510,7 @@ def main() -> int:
     ap.add_argument("--env-nee", type=int, default=0, help="environment NEE + MIS (same mean, lower variance)")
     ap.add_argument("--spp-per-wave", type=int, default=0)
     ap.add_argument("--spp", type=int, default=0, help="override the workload's spp (profiling runs only)")
+    ap.add_argument("--res", type=int, default=0, help="override the workload's resolution (profiling runs only)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--trace-variant", type=int, default=-1)
     ap.add_argument("--blocks-per-sm", type=int, default=0)
@@ -436,6 +523,10 @@ def main() -> int:
     ap.add_argument("--l2-persist", type=int, default=0, help="mark the tree persisting in L2")
     ap.add_argument("--ray-sort-bits", type=int, default=0, help="key bits of the loop's ray sort (0 = 33)")
     ap.add_argument("--cost-rr", type=int, default=0, help="cost-aware RR fed by the live device CostTracker")
+    ap.add_argument("--batched-jobs", type=int, default=512,
+                    help="config-3 jobs of the batched block of the default line (0 = skip)")
+    ap.add_argument("--serve-seconds", type=float, default=10.0,
+                    help="seconds of config-4 arrivals in the serving block of the default line (0 = skip)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 0)
     if args.impl == "reference" and args.workload in ("c3", "c4"):
@@ -450,6 +541,10 @@ def main() -> int:
     if args.spp > 0:
         wl["spp"] = args.spp
         wl["name"] = wl["name"].replace(f"_{WORKLOADS[args.workload]['spp']}spp", f"_{args.spp}spp")
+    if args.res > 0:
+        r0 = WORKLOADS[args.workload]["width"]
+        wl["width"] = wl["height"] = args.res
+        wl["name"] = wl["name"].replace(f"_{r0}x{r0}_", f"_{args.res}x{args.res}_")
     if args.impl == "reference":
         return run_reference(args, wl)
 
@@ -508,6 +603,7 @@ def main() -> int:
         e2e_rays += st["closest_rays"] + st["shadow_rays"]
     e2e_s = allreduce_max(dist, time.perf_counter() - t0)
     e2e_value = allreduce_sum(dist, e2e_rays) / e2e_s / 1e6
+    mse = image_mse(np.asarray(image_host).reshape(H, W, 3), wl, wl["spp"])
 
     # ---- roofline of the closest-hit kernel ----
     closest = sum(s["closest_rays"] for s in stats)
@@ -562,6 +658,16 @@ def main() -> int:
                 "depth": info.bvh_depth},
         "tuning": dict(ctx.get_tuning(), autotuned=bool(args.autotune), autotune_wave_ms=tune_ms),
     }
+    if mse is not None:
+        line["mse"] = mse
+    # the systems forms beside the plain loop (config 3 batched, config 4
+    # served), one GPU, after the timed region of the headline workload
+    if world == 1 and args.workload == "c1" and args.policy == "none" and not args.adaptive:
+        if args.batched_jobs > 0:
+            line["batched"] = batched_block(pkg, ctx, args.batched_jobs, args.trace_variant)
+        if args.serve_seconds > 0:
+            line["serving"] = serving_block(pkg, ctx, args.serve_seconds, args.rate, args.budget_gb, 0.0,
+                                            args.trace_variant)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         # the same band as --impl reference, repeated for >= 10 s of CPU work
         threads = os.cpu_count() or 1

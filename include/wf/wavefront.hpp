@@ -268,6 +268,127 @@ inline void intersectAll(Context& ctx, const RayQueue& in, ShadingQueue& hits, R
     }
 }
 
+// ---- queues in device memory (the stage-level entry points) ---------------
+
+namespace detail {
+template <class H, int (*Free)(H*)>
+class DeviceHandle {
+  public:
+    DeviceHandle() = default;
+    DeviceHandle(const DeviceHandle&) = delete;
+    DeviceHandle& operator=(const DeviceHandle&) = delete;
+    DeviceHandle(DeviceHandle&& o) noexcept : h_(std::exchange(o.h_, nullptr)), ctx_(o.ctx_) {}
+    DeviceHandle& operator=(DeviceHandle&& o) noexcept
+    {
+        if (this != &o) {
+            if (h_) Free(h_);
+            h_ = std::exchange(o.h_, nullptr);
+            ctx_ = o.ctx_;
+        }
+        return *this;
+    }
+    ~DeviceHandle()
+    {
+        if (h_) Free(h_);
+    }
+    H* handle() const { return h_; }
+
+  protected:
+    H* h_ = nullptr;
+    wf_ctx* ctx_ = nullptr;
+};
+}  // namespace detail
+
+// RayQueue kept on the GPU: schedule / materialize run there; upload and
+// download move it to and from the host mirror above.
+class DeviceRayQueue : public detail::DeviceHandle<wf_ray_queue, wf_ray_queue_free> {
+  public:
+    DeviceRayQueue(Context& ctx, int64_t capacity)
+    {
+        ctx_ = ctx.handle();
+        check(wf_ray_queue_alloc(ctx_, capacity, &h_), ctx_, "wf_ray_queue_alloc");
+    }
+    int64_t size() const
+    {
+        int64_t n = 0;
+        check(wf_ray_queue_size(h_, &n), ctx_, "wf_ray_queue_size");
+        return n;
+    }
+    // RayQueue::schedule (sortedIndices stay on the device; `sorted` gets a copy if given)
+    void schedule(const float sceneMin[3], const float sceneMax[3], std::vector<int>* sorted = nullptr)
+    {
+        if (sorted) sorted->assign((size_t)size(), 0);
+        check(wf_ray_queue_schedule(h_, sceneMin, sceneMax, sorted ? sorted->data() : nullptr), ctx_,
+              "wf_ray_queue_schedule");
+    }
+    void materialize() { check(wf_ray_queue_materialize(h_), ctx_, "wf_ray_queue_materialize"); }
+    void upload(const RayQueue& q)
+    {
+        wf_ray_columns c{const_cast<float*>(q.originsX.data()), const_cast<float*>(q.originsY.data()),
+                         const_cast<float*>(q.originsZ.data()), const_cast<float*>(q.dirsX.data()),
+                         const_cast<float*>(q.dirsY.data()), const_cast<float*>(q.dirsZ.data()),
+                         const_cast<float*>(q.throughputsR.data()), const_cast<float*>(q.throughputsG.data()),
+                         const_cast<float*>(q.throughputsB.data()), const_cast<float*>(q.pdfs.data()),
+                         const_cast<int*>(q.pixelIndices.data()), const_cast<int*>(q.depths.data()), nullptr};
+        check(wf_ray_queue_upload(h_, &c, q.size()), ctx_, "wf_ray_queue_upload");
+    }
+    RayQueue download() const
+    {
+        const int64_t n = size();
+        RayQueue q;
+        for (auto* v : {&q.originsX, &q.originsY, &q.originsZ, &q.dirsX, &q.dirsY, &q.dirsZ, &q.throughputsR,
+                        &q.throughputsG, &q.throughputsB, &q.pdfs, &q.accumLightR, &q.accumLightG, &q.accumLightB})
+            v->assign((size_t)n, 0.0f);
+        q.pixelIndices.assign((size_t)n, 0);
+        q.depths.assign((size_t)n, 0);
+        q.alive.assign((size_t)n, true);
+        wf_ray_columns c{q.originsX.data(), q.originsY.data(), q.originsZ.data(), q.dirsX.data(), q.dirsY.data(),
+                         q.dirsZ.data(), q.throughputsR.data(), q.throughputsG.data(), q.throughputsB.data(),
+                         q.pdfs.data(), q.pixelIndices.data(), q.depths.data(), nullptr};
+        int64_t got = 0;
+        check(wf_ray_queue_download(h_, &c, n, &got), ctx_, "wf_ray_queue_download");
+        return q;
+    }
+};
+
+// ShadingQueue kept on the GPU (its entries index the ray queue they were
+// intersected from, which must stay unchanged until they are shaded).
+class DeviceShadingQueue : public detail::DeviceHandle<wf_shading_queue, wf_shading_queue_free> {
+  public:
+    DeviceShadingQueue(Context& ctx, int64_t capacity, SchedulingPolicy p = SchedulingPolicy::None) : policy(p)
+    {
+        ctx_ = ctx.handle();
+        check(wf_shading_queue_alloc(ctx_, capacity, &h_), ctx_, "wf_shading_queue_alloc");
+    }
+    int64_t size() const
+    {
+        int64_t n = 0;
+        check(wf_shading_queue_size(h_, &n), ctx_, "wf_shading_queue_size");
+        return n;
+    }
+    // ShadingQueue::schedule with frozen relative costs (null = no tracker)
+    void schedule(const std::vector<double>* relCostMaterial = nullptr,
+                  const std::vector<double>* relCostTexture = nullptr, std::vector<int>* sorted = nullptr)
+    {
+        if (sorted) sorted->assign((size_t)size(), 0);
+        check(wf_shading_queue_schedule(h_, (int32_t)policy, relCostMaterial ? relCostMaterial->data() : nullptr,
+                                        relCostTexture ? relCostTexture->data() : nullptr,
+                                        sorted ? sorted->data() : nullptr),
+              ctx_, "wf_shading_queue_schedule");
+    }
+    void materialize() { check(wf_shading_queue_materialize(h_), ctx_, "wf_shading_queue_materialize"); }
+    SchedulingPolicy policy;
+};
+
+class DeviceShadowQueue : public detail::DeviceHandle<wf_shadow_queue, wf_shadow_queue_free> {
+  public:
+    DeviceShadowQueue(Context& ctx, int64_t capacity)
+    {
+        ctx_ = ctx.handle();
+        check(wf_shadow_queue_alloc(ctx_, capacity, &h_), ctx_, "wf_shadow_queue_alloc");
+    }
+};
+
 // include/render/WavefrontRenderer.h:16-56, with the reference's defaults:
 // adaptive sampling on (threshold 0.05), cost-aware RR on with costs from the
 // live device CostTracker, ray sort on.  Frozen relative costs (for
@@ -323,6 +444,61 @@ class WavefrontRenderer {
         pixels.assign((size_t)width * height * 3, 0.0f);
         check(wf_render(ctx.handle(), &p, pixels.data(), &lastStats), ctx.handle(), "wf_render");
         return lastStats.ms_shade;
+    }
+
+    // renderScene's loop (WavefrontRenderer.cpp:141-268) written out stage by
+    // stage over queues that stay on the GPU, in the reference's order: one
+    // sample of every pixel per pass; per bounce the optional ray sort,
+    // intersectAll, the ShadingQueue's schedule + materialize, shadeAll with
+    // its occluded() calls, the miss loop, currentQueue = nextQueue.  With
+    // the same parameters it renders renderScene's image (adaptive sampling
+    // and the live cost tracker are renderScene's; here frozen relative costs
+    // or none).  sceneMin / sceneMax: the scene bounds the ray sort uses.
+    double renderSceneStaged(Context& ctx, const wf_camera& camera, int width, int height, std::vector<float>& pixels,
+                             const float sceneMin[3], const float sceneMax[3])
+    {
+        wf_render_params p{};
+        p.width = width;
+        p.height = height;
+        p.samples_per_pixel = samplesPerPixel;
+        p.max_depth = maxDepth;
+        p.rr_min_depth = rrMinDepth;
+        p.policy = (int32_t)policy;
+        p.enable_cost_aware_rr = enableCostAwareRR && !relativeCostMaterial.empty() ? 1 : 0;
+        p.firefly_threshold = fireflyThreshold;
+        p.seed_lo = (uint32_t)seed;
+        p.seed_hi = (uint32_t)(seed >> 32);
+        p.enable_env_nee = envNEE ? 1 : 0;
+        p.rel_cost_material = relativeCostMaterial.empty() ? nullptr : relativeCostMaterial.data();
+        p.rel_cost_texture = relativeCostTexture.empty() ? nullptr : relativeCostTexture.data();
+        p.camera = camera;
+        wf_ctx* h = ctx.handle();
+        check(wf_stage_begin(h, &p), h, "wf_stage_begin");
+        const int64_t n = (int64_t)width * height;
+        DeviceRayQueue current(ctx, n), next(ctx, n), misses(ctx, n);
+        DeviceShadingQueue hits(ctx, n, policy);
+        DeviceShadowQueue shadows(ctx, 3 * n);
+        const std::vector<double>* rcm = relativeCostMaterial.empty() ? nullptr : &relativeCostMaterial;
+        const std::vector<double>* rct = relativeCostTexture.empty() ? nullptr : &relativeCostTexture;
+        for (int sample = 0; sample < samplesPerPixel; ++sample) {
+            check(wf_generate_primary(h, sample, 1, current.handle()), h, "wf_generate_primary");
+            for (int depth = 0; depth < maxDepth && current.size() > 0; ++depth) {
+                if (enableRaySort) {
+                    current.schedule(sceneMin, sceneMax);
+                    current.materialize();
+                }
+                check(wf_intersect(h, current.handle(), hits.handle(), misses.handle()), h, "wf_intersect");
+                hits.schedule(rcm, rct);
+                hits.materialize();
+                check(wf_shade(h, hits.handle(), next.handle(), shadows.handle()), h, "wf_shade");
+                check(wf_trace_occluded(h, shadows.handle()), h, "wf_trace_occluded");
+                check(wf_miss(h, misses.handle()), h, "wf_miss");
+                std::swap(current, next);
+            }
+        }
+        pixels.assign((size_t)n * 3, 0.0f);
+        check(wf_stage_image(h, pixels.data(), (int64_t)pixels.size()), h, "wf_stage_image");
+        return 0.0;
     }
 
     // AdaptiveSampler::getSampleCount of every pixel of the last render.

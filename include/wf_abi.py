@@ -157,6 +157,33 @@ class WfHitColumns(C.Structure):
                 ("u", f32p), ("v", f32p), ("material_id", i32p), ("texture_id", i32p)]
 
 
+class WfRayColumns(C.Structure):
+    _fields_ = [("origins_x", f32p), ("origins_y", f32p), ("origins_z", f32p), ("dirs_x", f32p), ("dirs_y", f32p),
+                ("dirs_z", f32p), ("throughputs_r", f32p), ("throughputs_g", f32p), ("throughputs_b", f32p),
+                ("pdfs", f32p), ("pixel_indices", i32p), ("depths", i32p), ("sample_indices", i32p)]
+
+
+RAY_FIELDS = {"origins_x": np.float32, "origins_y": np.float32, "origins_z": np.float32, "dirs_x": np.float32,
+              "dirs_y": np.float32, "dirs_z": np.float32, "throughputs_r": np.float32, "throughputs_g": np.float32,
+              "throughputs_b": np.float32, "pdfs": np.float32, "pixel_indices": np.int32, "depths": np.int32,
+              "sample_indices": np.int32}
+
+
+def make_ray_columns(n: int, given: dict | None = None):
+    """Host columns of n rays (RAY_FIELDS) and the WfRayColumns pointing at
+    them; `given` supplies arrays for some columns (others are zero), or,
+    with given is not None, only those columns are pointed at."""
+    cols = {}
+    for k, t in RAY_FIELDS.items():
+        if given is None:
+            cols[k] = np.zeros(n, dtype=t)
+        elif k in given:
+            cols[k] = np.ascontiguousarray(given[k], dtype=t)
+    ct = {np.int32: C.c_int32, np.float32: C.c_float}
+    rc = WfRayColumns(**{k: ptr(v, ct[RAY_FIELDS[k]]) for k, v in cols.items()})
+    return cols, rc
+
+
 HIT_FIELDS = {"geom_id": np.int32, "prim_id": np.int32, "distance": np.float32, "bary_u": np.float32,
               "bary_v": np.float32, "point_x": np.float32, "point_y": np.float32, "point_z": np.float32,
               "normal_x": np.float32, "normal_y": np.float32, "normal_z": np.float32,

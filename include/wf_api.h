@@ -287,7 +287,10 @@ typedef struct wf_tuning {
     int32_t trace_variant;
     int32_t persistent_blocks_per_sm;
     int32_t graph_mode;  /* 0 = graphs for batches and the server, 1 = also for
-                            single renders, 2 = never (policy != none never) */
+                            single renders, 2 = never (policy != none never);
+                            without a graph a batch of one job issues its
+                            bounces with device-side counts, as a single
+                            render does */
     int32_t bvh_builder; /* scenes uploaded afterwards: 0 = PLOC binary tree
                             (locally-ordered clustering, default), 1 = LBVH
                             binary tree (Karras radix tree), 2 = the PLOC tree
@@ -497,6 +500,151 @@ int wf_get_stream(wf_ctx* ctx, void** out_stream);
  * elapsed device time in milliseconds. */
 int wf_timer_begin(wf_ctx* ctx);
 int wf_timer_end(wf_ctx* ctx, double* out_ms);
+
+/* ---- per-bounce stages on device-resident queues ------------------------------
+ *
+ * The reference's loop body (WavefrontRenderer::renderScene, src/render/
+ * WavefrontRenderer.cpp:141-268) as separate calls on queues that live in
+ * device memory, so a caller can drive its own loop, stage by stage, with no
+ * host copy between stages:
+ *
+ *   wf_stage_begin(ctx, &params)                 renderScene's setup (:94-140)
+ *   for sample: wf_generate_primary(...)         generatePrimaryRays (:401-457)
+ *     for depth:
+ *       wf_ray_queue_schedule / _materialize     RayQueue::schedule / materialize (:159-168)
+ *       wf_intersect(rays, hits, misses)         intersectAll (:459-567)
+ *       wf_shading_queue_schedule / _materialize ShadingQueue::schedule / materialize (:183-185)
+ *       wf_shade(hits, next, shadows)            shadeAll (:569-877), emission into the sums
+ *       wf_trace_occluded(shadows)               shadeAll's occluded() calls (:676, :720)
+ *       wf_miss(misses)                          the miss loop (:256-265)
+ *       swap rays <-> next                       currentQueue = nextQueue (:267)
+ *   wf_stage_image(ctx, image)                   writeAveragedImage (:127-137)
+ *
+ * Queue sizes live on the device: stages chain on the context's stream
+ * without waiting; only the calls marked "waits" synchronise.  Paths draw the
+ * same random numbers as in wf_render (streams keyed by pixel, sample, depth),
+ * so a loop driven this way renders wf_render's image up to the order of
+ * float additions into the pixel sums.  The stages share the context's
+ * scratch with the full-render entry points: do not interleave them with
+ * wf_render* between wf_stage_begin and wf_stage_image.
+ *
+ * Device layout differences, stated:
+ *  - a wf_shading_queue holds, per hit, the ray's index in the ray queue it
+ *    came from plus (leaf triangle, t, barycentrics); the other 20 of the
+ *    reference's 24 columns are rebuilt from the scene when read (shading,
+ *    scheduling, wf_shading_queue_download).  The ray queue given to
+ *    wf_intersect must stay unchanged until the hits are shaded.
+ *  - misses go to a wf_ray_queue as copies of the missed rays, as in the
+ *    reference; wf_intersect with misses == NULL adds their sky terms at once.
+ *  - shadow rays are a queue of their own (origin, direction, max distance,
+ *    the unoccluded contribution, pixel): the reference calls occluded()
+ *    inline; the contribution is added when the ray is found unoccluded. */
+
+typedef struct wf_ray_queue wf_ray_queue;         /* RayQueue, RayQueue.h:63-245 */
+typedef struct wf_shading_queue wf_shading_queue; /* ShadingQueue, ShadingQueue.h:27-551 */
+typedef struct wf_shadow_queue wf_shadow_queue;   /* shadow rays of one bounce */
+
+/* Host SoA view of a RayQueue (RayQueue.h:65-90: originsX/Y/Z, dirsX/Y/Z,
+ * throughputsR/G/B, pixelIndices, depths, pdfs; sampleIndices is a device
+ * addition).  accumLight is always 0 and alive always true in the reference's
+ * loop, so neither is stored.  NULL columns are skipped (download) or
+ * defaulted (upload: throughput 1, depth 0, pdf -1, sample 0). */
+typedef struct wf_ray_columns {
+    float* origins_x;
+    float* origins_y;
+    float* origins_z;
+    float* dirs_x;
+    float* dirs_y;
+    float* dirs_z;
+    float* throughputs_r;
+    float* throughputs_g;
+    float* throughputs_b;
+    float* pdfs;
+    int32_t* pixel_indices;
+    int32_t* depths;
+    int32_t* sample_indices;
+} wf_ray_columns;
+
+/* Queues of `capacity` entries on the context's device.  A shadow queue
+ * needs up to 3 entries per hit (area light, directional light, environment
+ * map).  Freed queues must not be in use by queued work. */
+int wf_ray_queue_alloc(wf_ctx* ctx, int64_t capacity, wf_ray_queue** out);
+int wf_ray_queue_free(wf_ray_queue* q);
+int wf_shading_queue_alloc(wf_ctx* ctx, int64_t capacity, wf_shading_queue** out);
+int wf_shading_queue_free(wf_shading_queue* q);
+int wf_shadow_queue_alloc(wf_ctx* ctx, int64_t capacity, wf_shadow_queue** out);
+int wf_shadow_queue_free(wf_shadow_queue* q);
+
+/* Entries in a queue (waits). */
+int wf_ray_queue_size(wf_ray_queue* q, int64_t* n);
+int wf_shading_queue_size(wf_shading_queue* q, int64_t* n);
+int wf_shadow_queue_size(wf_shadow_queue* q, int64_t* n);
+
+/* RayQueue::add / addPrimary for n rays from host columns (replaces the
+ * queue's contents); wf_ray_queue_download copies up to `capacity` entries
+ * back in queue order and returns the count (waits). */
+int wf_ray_queue_upload(wf_ray_queue* q, const wf_ray_columns* host, int64_t n);
+int wf_ray_queue_download(wf_ray_queue* q, wf_ray_columns* host, int64_t capacity, int64_t* n);
+
+/* The ShadingQueue's columns in queue order (waits): hit columns as
+ * wf_trace_closest_host writes them (HitRecord + geomID) and the ray columns
+ * of each hit's ray (origins, dirs, throughputs, pixel, depth, pdf). */
+int wf_shading_queue_download(wf_shading_queue* q, wf_hit_columns* hits, wf_ray_columns* rays,
+                              int64_t capacity, int64_t* n);
+
+/* The render the stages serve: its parameters (the reference's public
+ * WavefrontRenderer fields and the camera; adaptive sampling and live cost
+ * tracking are not used here) and zeroed per-pixel sums.  Needs an uploaded
+ * scene. */
+int wf_stage_begin(wf_ctx* ctx, const wf_render_params* params);
+
+/* generatePrimaryRays for samples [first_sample, first_sample + nspp) of
+ * every pixel, pixel-major (a pixel's samples are consecutive), throughput 1,
+ * depth 0, pdf -1.  Replaces the queue's contents.  Capacity must hold
+ * width * height * nspp rays. */
+int wf_generate_primary(wf_ctx* ctx, int32_t first_sample, int32_t nspp, wf_ray_queue* out);
+
+/* RayQueue::schedule (RayQueue.h:165-179): sortedIndices = the stable sort of
+ * sortKey (octant << 30 | Morton code of the origin in [bounds_min,
+ * bounds_max], host arrays of 3 floats), kept in the queue; if not NULL,
+ * sorted_indices_host receives it (waits).  Reads the queue's size (waits).
+ * RayQueue::materialize (:182-215) gathers every column by it and resets it
+ * to the identity. */
+int wf_ray_queue_schedule(wf_ray_queue* q, const float bounds_min[3], const float bounds_max[3],
+                          int32_t* sorted_indices_host);
+int wf_ray_queue_materialize(wf_ray_queue* q);
+
+/* intersectAll: closest hit of every ray of `rays` (t in [0.001, 1e9]); the
+ * hits fill `hits` in ray order, the misses `misses` (or, with misses ==
+ * NULL, their sky / environment terms go into the sums at once). */
+int wf_intersect(wf_ctx* ctx, wf_ray_queue* rays, wf_shading_queue* hits, wf_ray_queue* misses);
+
+/* ShadingQueue::schedule (ShadingQueue.h:90-141, 277-329, 437-550) under
+ * `policy` with frozen CostTracker::relativeCost vectors (NULL = no tracker):
+ * sortedIndices kept in the queue, copied to sorted_indices_host if not NULL.
+ * Reads the hit count (waits).  ShadingQueue::materialize (:233-275) puts the
+ * queue in that order and resets sortedIndices to the identity. */
+int wf_shading_queue_schedule(wf_shading_queue* q, int32_t policy, const double* rel_cost_material,
+                              const double* rel_cost_texture, int32_t* sorted_indices_host);
+int wf_shading_queue_materialize(wf_shading_queue* q);
+
+/* shadeAll for every hit of `hits`: emission with MIS into the sums,
+ * area / directional (/ environment) NEE as shadow rays, Material::scatter,
+ * Russian roulette, next rays.  Replaces the contents of `next` and
+ * `shadows`. */
+int wf_shade(wf_ctx* ctx, wf_shading_queue* hits, wf_ray_queue* next, wf_shadow_queue* shadows);
+
+/* The occluded() test of every shadow ray; the contribution of an
+ * unoccluded one goes into the sums. */
+int wf_trace_occluded(wf_ctx* ctx, wf_shadow_queue* shadows);
+
+/* The miss loop: throughput x getSkyColor (or the environment map) of every
+ * ray of `misses` into the sums. */
+int wf_miss(wf_ctx* ctx, wf_ray_queue* misses);
+
+/* writeAveragedImage: sums / samples_per_pixel into image_rgb (host,
+ * width*height*3 floats); also reports a tripped device check (waits). */
+int wf_stage_image(wf_ctx* ctx, float* image_rgb, int64_t num_floats);
 
 /* ---- resident scenes, jobs, batches ------------------------------------------ */
 

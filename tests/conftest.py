@@ -22,6 +22,27 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300)")
 
 
+# Figures the parity tests measure (disagreeing-pixel fractions, MSE against
+# the FP64 oracle, ...), keyed by test.  With WF_PARITY_REPORT=<path> they are
+# written there as JSON when the session ends.
+PARITY_REPORT: dict = {}
+
+
+def report(name: str, **figures) -> None:
+    PARITY_REPORT[name] = {k: (float(v) if isinstance(v, (np.floating, np.integer)) else v)
+                           for k, v in figures.items()}
+
+
+def pytest_sessionfinish(session, exitstatus):
+    import json
+    import os
+
+    path = os.environ.get("WF_PARITY_REPORT")
+    if path and PARITY_REPORT:
+        Path(path).parent.mkdir(parents=True, exist_ok=True)
+        Path(path).write_text(json.dumps(PARITY_REPORT, indent=1, sort_keys=True))
+
+
 def _load(name, path):
     if name in sys.modules:
         return sys.modules[name]
@@ -82,34 +103,42 @@ def rays_in_box(rng, n, lo, hi):
 
 def fp64_band(img, spp, golden, block=8):
     """Check (c): an image rendered with `spp` samples against the
-    reference's FP64 per-pixel mean (`golden["mean"]`) and per-sample standard
-    deviation (`golden["sigma"]`) over 16384 spp.
+    reference's FP64 per-pixel mean (`golden["mean"]`, over `golden["spp"]`
+    samples) and per-sample standard deviation (`golden["sigma"]`).
 
     Per-pixel samples are heavy-tailed here (rare paths clamped at the
     firefly threshold of 10), so the 3-sigma band is applied to block means of
-    block x block pixels (block*block*spp samples each):
+    block x block pixels (block*block*spp samples each).  The variance of a
+    difference counts both sides: sigma^2/spp for the image and
+    sigma^2/golden_spp for the oracle's own mean.
       * bias: the mean of the block z-scores is within 3 standard errors of 0;
       * variance: their standard deviation is 1 +- 0.15;
       * tail: |z| > 3 on fewer than 3% of blocks (a normal tail gives 0.27%);
-      * MSE against the FP64 mean is within 20% of sum(sigma^2)/spp;
-      * channel means within 1%.
+      * MSE against the FP64 mean is within 20% of what the variance predicts;
+      * each channel's image mean is within 4 standard errors of the oracle's.
     Returns the figures (MSE included) for reporting."""
     H, W, _ = img.shape
+    gspp = float(golden["spp"]) if "spp" in golden else 16384.0
     mean, sigma = golden["mean"].astype(np.float64), golden["sigma"].astype(np.float64)
+    pix_var = sigma ** 2 * (1.0 / spp + 1.0 / gspp)
     bm = mean.reshape(H // block, block, W // block, block, 3).mean((1, 3))
     bx = img.astype(np.float64).reshape(H // block, block, W // block, block, 3).mean((1, 3))
-    bv = (sigma ** 2 / spp).reshape(H // block, block, W // block, block, 3).sum((1, 3)) / block ** 4
-    z = (bx - bm) / np.sqrt(np.maximum(bv, 1e-12))
+    bv = pix_var.reshape(H // block, block, W // block, block, 3).sum((1, 3)) / block ** 4
+    live = bv > 1e-14  # blocks that see only a constant sky have no variance
+    z = (bx - bm)[live] / np.sqrt(bv[live])
     mse = float(((img - mean) ** 2).mean())
-    expected = float((sigma ** 2 / spp).mean())
+    expected = float(pix_var.mean())
+    ch_se = np.sqrt(pix_var.sum((0, 1))) / (H * W)
+    ch_diff = img.astype(np.float64).mean((0, 1)) - mean.mean((0, 1))
     out = {"mse": mse, "expected_mse": expected, "z_mean": float(z.mean()), "z_std": float(z.std()),
-           "tail_frac": float((np.abs(z) > 3).mean()),
-           "channel_rel": (img.mean((0, 1)) / mean.mean((0, 1)) - 1).tolist()}
+           "tail_frac": float((np.abs(z) > 3).mean()), "blocks": int(z.size),
+           "channel_rel": (ch_diff / mean.mean((0, 1))).tolist(), "channel_z": (ch_diff / ch_se).tolist(),
+           "spp": spp, "oracle_spp": gspp}
     assert abs(out["z_mean"]) < 3.0 / np.sqrt(z.size), out
     assert abs(out["z_std"] - 1.0) < 0.15, out
     assert out["tail_frac"] < 0.03, out
     assert mse < 1.2 * expected, out
-    assert max(abs(c) for c in out["channel_rel"]) < 0.01, out
+    assert max(abs(c) for c in out["channel_z"]) < 4.0, out
     return out
 
 

@@ -124,6 +124,39 @@ int main()
         // 32 samples) and cost-aware RR fed by the live tracker
         const std::vector<int32_t> counts = r.sampleCounts(ctx, 16, 16);
         EXPECT(counts.size() == 256 && counts[0] == 8 && counts[255] == 8);
+        // the same loop stage by stage on device-resident queues: renderScene's
+        // image up to the order of float additions (1e-4 relative on 99% of
+        // pixels), policy and ray sort included
+        wf::WavefrontRenderer a(4, 8, wf::SchedulingPolicy::MaterialAware);
+        a.enableAdaptiveSampling = false;
+        a.enableCostAwareRR = false;
+        a.relativeCostMaterial.assign((size_t)desc.num_materials, 1.0);
+        a.relativeCostTexture.assign(1, 1.0);
+        std::vector<float> whole, staged;
+        a.renderScene(ctx, cam, 16, 16, whole);
+        wf_scene_info info{};
+        wf_scene_get_info(ctx.handle(), &info);
+        a.renderSceneStaged(ctx, cam, 16, 16, staged, info.bounds_min, info.bounds_max);
+        int close = 0;
+        for (size_t i = 0; i < whole.size(); i += 3) {
+            bool ok = true;
+            for (int k = 0; k < 3; ++k)
+                ok = ok && std::fabs(whole[i + k] - staged[i + k]) <= 1e-6f + 1e-4f * std::fabs(whole[i + k]);
+            close += ok ? 1 : 0;
+        }
+        EXPECT(close >= 253);  // 99% of 256 pixels
+        // RayQueue round trip through the device queue, schedule on the device
+        wf::DeviceRayQueue dq(ctx, 256);
+        dq.upload(prim);
+        std::vector<int> sorted;
+        dq.schedule(info.bounds_min, info.bounds_max, &sorted);
+        wf::RayQueue hostSorted = prim;
+        hostSorted.schedule(ctx, info.bounds_min, info.bounds_max);
+        EXPECT(sorted == hostSorted.sortedIndices);
+        dq.materialize();
+        wf::RayQueue back = dq.download();
+        hostSorted.materialize();
+        EXPECT(back.pixelIndices == hostSorted.pixelIndices && back.dirsX == hostSorted.dirsX);
         wf_host_scene_free(hs);
     }
     std::printf("%s (%d failures)\n", failures ? "FAIL" : "OK", failures);

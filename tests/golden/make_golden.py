@@ -10,9 +10,25 @@ read the committed .npz files).
                                              (the reference's renderScene,
                                              256 batches x 64 spp; ~1 h on 8
                                              cores, resumable)
+  python tests/golden/make_golden.py hits1   dense-mesh scene (config 1):
+                                             closest hits and occlusion
+  python tests/golden/make_golden.py hits2   lattice scene (config 2), same
+  python tests/golden/make_golden.py crop1   FP64 mean of a 128 x 128 window
+                                             of the 1024^2 dense-mesh render
+                                             (16384 spp, depth 12; ~30 min)
+  python tests/golden/make_golden.py crop2   FP64 mean of a 128 x 128 window
+                                             of the 2048^2 lattice render
+                                             (8192 spp, depth 8, HDRI)
+  python tests/golden/make_golden.py fp104   FP64 mean of config 104 (config 0
+                                             with a directional light and a
+                                             glass box), 128 x 128, 16384 spp
 
-Inputs are seeded; the workload scene comes from the product's procedural
-generator (wf_host_scene_generate), fed identically to the reference.
+Inputs are seeded; the workload scenes come from the procedural generator
+compiled into the oracle (the same source as the GPU library's), fed
+identically to the reference.  A window of a W x H render is rendered by the
+reference with the camera moved onto that window (Camera's public
+topLeftCorner / horizontal / vertical, include/core/Camera.h:8-11), which
+gives pixel (x0 + i, y0 + j) of the full image the same ray formula.
 """
 from __future__ import annotations
 
@@ -32,7 +48,7 @@ wf = O.wf
 
 
 def small() -> None:
-    scene = wf.HostScene(0)
+    scene = O.HostScene(0)
     ref = O.Ref(scene.desc, True)
     # Camera (Camera::Camera) and Camera::getRay on a grid of (u, v)
     cam12 = O.ref_camera([0, 0.275, 0.8], [0, 0.275, 0], [0, 1, 0], 40.0, 256, 256)
@@ -95,7 +111,7 @@ def fp64(batches: int = 256, spp: int = 64, threads: int = 8) -> None:
     (adaptive sampling and cost-aware RR off, policy none, firefly 10)."""
     W = H = 256
     out = HERE / "c0_fp64.npz"
-    scene = wf.HostScene(0)
+    scene = O.HostScene(0)
     ref = O.Ref(scene.desc, True)
     cam12 = scene.camera(W, H).as_array()
     s1 = np.zeros((H, W, 3), np.float64)
@@ -123,11 +139,129 @@ def fp64(batches: int = 256, spp: int = 64, threads: int = 8) -> None:
     print("written", out, "spp", done * spp)
 
 
+def crop_camera(cam12: np.ndarray, W: int, H: int, x0: int, y0: int, w: int, h: int) -> np.ndarray:
+    """The camera whose w x h image is pixels [x0, x0 + w) x [y0, y0 + h) of
+    the W x H image of `cam12` (origin, topLeftCorner, horizontal, vertical):
+    the reference's pixel (x, y) uses u = (x + a) / (W - 1) and
+    v = 1 - (y + b) / (H - 1) (src/render/WavefrontRenderer.cpp:401-457)."""
+    o, tl, hor, ver = np.asarray(cam12, np.float32).reshape(4, 3)
+    tl2 = tl + hor * np.float32(x0 / (W - 1)) + ver * np.float32(1.0 - (y0 + h - 1) / (H - 1))
+    return np.concatenate([o, tl2, hor * np.float32((w - 1) / (W - 1)),
+                           ver * np.float32((h - 1) / (H - 1))]).astype(np.float32)
+
+
+def hits(config: int, n: int = 8192, brute_n: int = 128) -> None:
+    """Closest hits (EmbreeAccelerator::intersect4 mapping) and occlusion of
+    a workload scene from the reference's code: a quarter camera rays through
+    random image positions, a quarter secondary rays leaving first hits in
+    random directions, a quarter aimed at triangle vertices and a quarter at
+    edge midpoints (shared edges) from random points inside the scene bounds.
+    `brute_n` of them also through Scene::hit's brute force."""
+    scene = O.HostScene(config)
+    ref = O.Ref(scene.desc, True)
+    rng = np.random.default_rng(20261204 + config)
+    W = H = {1: 1024, 2: 2048}[config]
+    cam12 = scene.camera(W, H).as_array()
+    q = n // 4
+    uv = rng.uniform(0, 1, size=(2 * q, 2)).astype(np.float32)
+    ro, rd = map(np.array, zip(*[O.ref_camera_get_ray(cam12, float(u), float(v)) for u, v in uv]))
+    first = ref.trace(ro[q:], rd[q:], mode=1)
+    hitmask = first["prim_id"] >= 0
+    pts = np.stack([first["point_x"], first["point_y"], first["point_z"]], 1)
+    sd = rng.normal(size=(q, 3))
+    sd = (sd / np.linalg.norm(sd, axis=1, keepdims=True)).astype(np.float32)
+    so = np.where(hitmask[:, None], pts, ro[q:]).astype(np.float32)
+    # rays at vertices and edge midpoints of random triangles
+    d = scene.desc
+    ni = d.num_indices
+    idx = np.ctypeslib.as_array(d.indices, (ni,))
+    P = np.stack([np.ctypeslib.as_array(a, (d.num_vertices,)) for a in (d.positions_x, d.positions_y, d.positions_z)], 1)
+    bmin, bmax = ref.bounds()
+    tri = rng.integers(0, ni // 3, 2 * q)
+    corner = rng.integers(0, 3, 2 * q)
+    a = P[idx[3 * tri + corner]]
+    b = P[idx[3 * tri + (corner + 1) % 3]]
+    target = np.concatenate([a[:q], 0.5 * (a[q:] + b[q:])]).astype(np.float32)
+    org = rng.uniform(bmin, bmax, size=(2 * q, 3)).astype(np.float32)
+    td = target - org
+    td = (td / np.linalg.norm(td, axis=1, keepdims=True)).astype(np.float32)
+    o = np.concatenate([ro[:q], so, org]).astype(np.float32)
+    dd = np.concatenate([rd[:q], sd, td]).astype(np.float32)
+    h4 = ref.trace(o, dd, mode=1)
+    sel = rng.choice(n, brute_n, replace=False)
+    brute = O.Ref(scene.desc, False).trace(o[sel], dd[sel], mode=0)
+    for k in ("prim_id", "distance", "material_id"):
+        assert np.array_equal(brute[k], h4[k][sel]), k
+    np.savez_compressed(HERE / f"c{config}_hits.npz", o=o, d=dd, **{f"i4_{k}": v for k, v in h4.items()})
+    # occlusion: maxd below and above the closest hit distance
+    t = np.where(h4["prim_id"] >= 0, h4["distance"], 1e3).astype(np.float32)
+    maxd = (t * rng.choice([0.5, 0.999, 1.001, 2.0], n)).astype(np.float32)
+    occ = ref.occluded(o, dd, maxd)
+    np.savez_compressed(HERE / f"c{config}_occluded.npz", o=o, d=dd, maxd=maxd, occluded=occ)
+    print(f"config {config}: {int((h4['prim_id'] >= 0).sum())} of {n} rays hit, {int(occ.sum())} occluded")
+
+
+def fp64_window(name: str, config: int, W: int, H: int, window, depth: int, batches: int, batch_spp: int,
+                threads: int = 8) -> None:
+    """Per-pixel FP64 mean and per-sample standard deviation of a window of
+    the W x H render of `config` from the reference's renderScene: batch b
+    renders `batch_spp` samples with seed b (adaptive sampling and cost-aware
+    RR off, policy none, firefly 10).  Resumable."""
+    x0, y0, w, h = window
+    scene = O.HostScene(config)
+    ref = O.Ref(scene.desc, True)
+    cam12 = crop_camera(scene.camera(W, H).as_array(), W, H, x0, y0, w, h)
+    env = O.scene_environment(scene.desc)
+    env_path = None
+    if env is not None:
+        env_path = HERE / f"{name}.env.partial.pfm"
+        O.write_pfm(env_path, env)
+    out = HERE / f"{name}.npz"
+    part = HERE / f"{name}.partial.npz"
+    s1 = np.zeros((h, w, 3), np.float64)
+    s2 = np.zeros((h, w, 3), np.float64)
+    done = 0
+    if part.exists():
+        z = np.load(part)
+        s1, s2, done = z["s1"], z["s2"], int(z["done"])
+    t0 = time.time()
+    unresolved = 0
+    for b in range(done, batches):
+        img = ref.render(cam12, w, h, batch_spp, depth, policy=0, ray_sort=False, firefly=10.0, seed=1 + b,
+                         threads=threads, env_path=env_path)
+        unresolved += O.ref_front_face_stats()[0]
+        s1 += img
+        s2 += img.astype(np.float64) ** 2
+        done = b + 1
+        if done % 8 == 0 or done == batches:
+            np.savez(part, s1=s1, s2=s2, done=done)
+            print(f"{name}: batch {done}/{batches} {time.time() - t0:.0f}s", flush=True)
+    assert unresolved == 0, "frontFace of a rebuilt hit record not resolved"
+    mean = s1 / done
+    var_batch = np.maximum(s2 / done - mean ** 2, 0.0) * done / max(done - 1, 1)
+    sigma_sample = np.sqrt(var_batch * batch_spp)
+    np.savez_compressed(out, mean=mean.astype(np.float32), sigma=sigma_sample.astype(np.float32),
+                        spp=np.int64(done * batch_spp), batches=np.int64(done), batch_spp=np.int64(batch_spp),
+                        cam12=cam12, window=np.array(window, np.int64), image_size=np.array([W, H], np.int64),
+                        max_depth=np.int64(depth), config=np.int64(config))
+    if env_path is not None:
+        env_path.unlink()
+    print("written", out, "spp", done * batch_spp)
+
+
 if __name__ == "__main__":
     what = sys.argv[1] if len(sys.argv) > 1 else "small"
     if what == "small":
         small()
     elif what == "fp64":
         fp64(batches=int(sys.argv[2]) if len(sys.argv) > 2 else 256)
+    elif what in ("hits1", "hits2"):
+        hits(int(what[-1]))
+    elif what == "crop1":
+        fp64_window("c1_fp64_crop", 1, 1024, 1024, (256, 384, 128, 128), 12, 256, 64)
+    elif what == "crop2":
+        fp64_window("c2_fp64_crop", 2, 2048, 2048, (960, 1536, 128, 128), 8, 256, 32)
+    elif what == "fp104":
+        fp64_window("c104_fp64", 104, 128, 128, (0, 0, 128, 128), 8, 256, 64)
     else:
         raise SystemExit(__doc__)

@@ -240,7 +240,66 @@ def test_golden_fp64_port_render(wf, orc, scene0):
     fp64_band(acc / spp, spp, g)
 
 
+@pytest.mark.parametrize("config", [1, 2])
+def test_golden_workload_window_port_render(wf, orc, config):
+    """The port renders the benchmarked workload's fixture window (config 1:
+    1024^2 at 64 spp, depth 12; config 2: 2048^2 at 32 spp, depth 8) inside
+    the band of the reference's FP64 mean of that window, and agrees with the
+    hit fixtures of the same scene bit for bit."""
+    from conftest import fp64_band
+    g = np.load(GOLDEN / f"c{config}_fp64_crop.npz")
+    sc = orc.HostScene(config)
+    port = orc.Port(sc.desc)
+    h = np.load(GOLDEN / f"c{config}_hits.npz")
+    got = port.trace_closest(h["o"], h["d"])
+    for k in ("prim_id", "material_id", "texture_id", "distance", "point_x", "normal_z", "front_face", "u", "v"):
+        assert np.array_equal(got[k], h["i4_" + k]), k
+    z = np.load(GOLDEN / f"c{config}_occluded.npz")
+    assert np.array_equal(port.trace_occluded(z["o"], z["d"], z["maxd"]), z["occluded"])
+    W, H = (int(v) for v in g["image_size"])
+    x0, y0, w, hh = (int(v) for v in g["window"])
+    spp = {1: 64, 2: 32}[config]
+    p = wf.render_params(W, H, spp, int(g["max_depth"]), sc.camera(W, H), seed=5150)
+    acc, _ = port.render_window(p, x0, y0, w, hh)
+    fp64_band(acc / spp, spp, g)
+
+
+def test_golden_directional_port_render(wf, orc):
+    """Config 104 (directional light, metal and glass boxes): the port's
+    render at 64 spp inside the band of the reference's FP64 mean."""
+    from conftest import fp64_band
+    g = np.load(GOLDEN / "c104_fp64.npz")
+    sc = orc.HostScene(104)
+    port = orc.Port(sc.desc)
+    W = H = 128
+    spp = 64
+    p = wf.render_params(W, H, spp, 8, sc.camera(W, H), seed=8080)
+    acc, _ = port.render_window(p, 0, 0, W, H)
+    fp64_band(acc / spp, spp, g)
+
+
 # ------------------------------------------------- live reference (x86 dev) ---
+
+def test_port_directional_statistics_match_reference_live(wf, orc):
+    """Config 104: the reference's directional NEE (WavefrontRenderer.cpp
+    :712-737) and the port's agree pixel by pixel in distribution (24 runs
+    each, |z| > 3 on < 1.5% of pixel channels)."""
+    if not orc.ref_available():
+        pytest.skip("reference checkout not present")
+    sc = orc.HostScene(104)
+    ref = orc.Ref(sc.desc, True)
+    port = orc.Port(sc.desc)
+    W = H = 32
+    spp, N = 32, 24
+    cam = sc.camera(W, H)
+    P = np.array([port.render_window(wf.render_params(W, H, spp, 8, cam, seed=900 + k), 0, 0, W, H)[0] / spp
+                  for k in range(N)], np.float64)
+    R = np.array([ref.render(cam.as_array(), W, H, spp, 8, seed=700 + k) for k in range(N)], np.float64)
+    assert orc.ref_front_face_stats()[0] == 0
+    z = (P.mean(0) - R.mean(0)) / np.sqrt(P.var(0, ddof=1) / N + R.var(0, ddof=1) / N + 1e-30)
+    assert (np.abs(z) > 3).mean() < 0.015
+    assert abs(np.median(P.var(0) / (R.var(0) + 1e-30)) - 1.0) < 0.2
+
 
 def test_port_equals_reference_live(wf, orc, scene_small):
     if not orc.ref_available():

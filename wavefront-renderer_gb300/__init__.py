@@ -113,6 +113,30 @@ def _declare(lib: C.CDLL) -> None:
         "wf_host_scene_describe": ([V, C.POINTER(WfSceneDesc)], C.c_int),
         "wf_host_scene_camera": ([V, C.c_int32, C.c_int32, C.POINTER(WfCamera)], C.c_int),
         "wf_host_scene_free": ([V], C.c_int),
+        "wf_ray_queue_alloc": ([V, C.c_int64, C.POINTER(V)], C.c_int),
+        "wf_ray_queue_free": ([V], C.c_int),
+        "wf_shading_queue_alloc": ([V, C.c_int64, C.POINTER(V)], C.c_int),
+        "wf_shading_queue_free": ([V], C.c_int),
+        "wf_shadow_queue_alloc": ([V, C.c_int64, C.POINTER(V)], C.c_int),
+        "wf_shadow_queue_free": ([V], C.c_int),
+        "wf_ray_queue_size": ([V, C.POINTER(C.c_int64)], C.c_int),
+        "wf_shading_queue_size": ([V, C.POINTER(C.c_int64)], C.c_int),
+        "wf_shadow_queue_size": ([V, C.POINTER(C.c_int64)], C.c_int),
+        "wf_ray_queue_upload": ([V, C.POINTER(WfRayColumns), C.c_int64], C.c_int),
+        "wf_ray_queue_download": ([V, C.POINTER(WfRayColumns), C.c_int64, C.POINTER(C.c_int64)], C.c_int),
+        "wf_shading_queue_download": ([V, C.POINTER(WfHitColumns), C.POINTER(WfRayColumns), C.c_int64,
+                                       C.POINTER(C.c_int64)], C.c_int),
+        "wf_stage_begin": ([V, C.POINTER(WfRenderParams)], C.c_int),
+        "wf_generate_primary": ([V, C.c_int32, C.c_int32, V], C.c_int),
+        "wf_ray_queue_schedule": ([V, f32p, f32p, i32p], C.c_int),
+        "wf_ray_queue_materialize": ([V], C.c_int),
+        "wf_intersect": ([V, V, V, V], C.c_int),
+        "wf_shading_queue_schedule": ([V, C.c_int32, f64p, f64p, i32p], C.c_int),
+        "wf_shading_queue_materialize": ([V], C.c_int),
+        "wf_shade": ([V, V, V, V], C.c_int),
+        "wf_trace_occluded": ([V, V], C.c_int),
+        "wf_miss": ([V, V], C.c_int),
+        "wf_stage_image": ([V, f32p, C.c_int64], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -270,6 +294,106 @@ class Server:
 
     def clock(self) -> float:
         return load_library().wf_server_clock(self._h)
+
+
+class _DeviceQueue:
+    """A queue in device memory (wf_*_queue_alloc); freed by close()."""
+
+    _kind = ""
+
+    def __init__(self, ctx: "Context", capacity: int):
+        self.ctx = ctx
+        self.capacity = int(capacity)
+        self._h = C.c_void_p()
+        _check(getattr(load_library(), f"wf_{self._kind}_queue_alloc")(ctx._h, self.capacity, C.byref(self._h)),
+               f"wf_{self._kind}_queue_alloc", ctx)
+
+    def close(self):
+        if self._h:
+            getattr(load_library(), f"wf_{self._kind}_queue_free")(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def size(self) -> int:
+        n = C.c_int64()
+        _check(getattr(load_library(), f"wf_{self._kind}_queue_size")(self._h, C.byref(n)),
+               f"wf_{self._kind}_queue_size", self.ctx)
+        return n.value
+
+
+class RayQueue(_DeviceQueue):
+    """A RayQueue in device memory (RayQueue.h:63-245)."""
+
+    _kind = "ray"
+
+    def upload(self, cols: dict) -> None:
+        """cols: RAY_FIELDS arrays (origins, directions and pixel indices
+        required; the others default as RayQueue::addPrimary sets them)."""
+        n = len(cols["origins_x"])
+        keep, rc = make_ray_columns(n, cols)
+        _check(load_library().wf_ray_queue_upload(self._h, C.byref(rc), n), "wf_ray_queue_upload", self.ctx)
+
+    def download(self) -> dict:
+        n = self.size()
+        cols, rc = make_ray_columns(n)
+        got = C.c_int64()
+        _check(load_library().wf_ray_queue_download(self._h, C.byref(rc), n, C.byref(got)), "wf_ray_queue_download",
+               self.ctx)
+        return {k: v[:got.value] for k, v in cols.items()}
+
+    def schedule(self, bounds_min, bounds_max) -> np.ndarray:
+        """RayQueue::schedule: the permutation (sortedIndices), also kept in
+        the queue for materialize()."""
+        n = self.size()
+        perm = np.zeros(max(n, 1), np.int32)
+        bmin = np.ascontiguousarray(bounds_min, np.float32)
+        bmax = np.ascontiguousarray(bounds_max, np.float32)
+        _check(load_library().wf_ray_queue_schedule(self._h, ptr(bmin), ptr(bmax), ptr(perm, C.c_int32)),
+               "wf_ray_queue_schedule", self.ctx)
+        return perm[:n]
+
+    def materialize(self) -> None:
+        _check(load_library().wf_ray_queue_materialize(self._h), "wf_ray_queue_materialize", self.ctx)
+
+
+class ShadingQueue(_DeviceQueue):
+    """A ShadingQueue in device memory (ShadingQueue.h:27-551)."""
+
+    _kind = "shading"
+
+    def download(self) -> tuple[dict, dict]:
+        """The queue's hit columns (HIT_FIELDS) and its rays' columns
+        (RAY_FIELDS), in queue order."""
+        n = self.size()
+        hits, hc = make_hit_columns(n)
+        rays, rc = make_ray_columns(n)
+        got = C.c_int64()
+        _check(load_library().wf_shading_queue_download(self._h, C.byref(hc), C.byref(rc), n, C.byref(got)),
+               "wf_shading_queue_download", self.ctx)
+        return hits, rays
+
+    def schedule(self, policy: int, rel_cost_material=None, rel_cost_texture=None) -> np.ndarray:
+        n = self.size()
+        perm = np.zeros(max(n, 1), np.int32)
+        rcm = None if rel_cost_material is None else np.ascontiguousarray(rel_cost_material, np.float64)
+        rct = None if rel_cost_texture is None else np.ascontiguousarray(rel_cost_texture, np.float64)
+        _check(load_library().wf_shading_queue_schedule(self._h, policy, ptr(rcm, C.c_double), ptr(rct, C.c_double),
+                                                        ptr(perm, C.c_int32)), "wf_shading_queue_schedule", self.ctx)
+        return perm[:n]
+
+    def materialize(self) -> None:
+        _check(load_library().wf_shading_queue_materialize(self._h), "wf_shading_queue_materialize", self.ctx)
+
+
+class ShadowQueue(_DeviceQueue):
+    """The shadow rays of one bounce, in device memory."""
+
+    _kind = "shadow"
 
 
 class Context:
@@ -460,6 +584,33 @@ class Context:
         s = C.c_void_p()
         _check(load_library().wf_get_stream(self._h, C.byref(s)), "wf_get_stream", self)
         return s.value or 0
+
+    # ---- per-bounce stages on device-resident queues ----
+    def stage_begin(self, params: WfRenderParams) -> None:
+        self._stage = params
+        _check(load_library().wf_stage_begin(self._h, C.byref(params)), "wf_stage_begin", self)
+
+    def generate_primary(self, first_sample: int, nspp: int, out: RayQueue) -> None:
+        _check(load_library().wf_generate_primary(self._h, first_sample, nspp, out._h), "wf_generate_primary", self)
+
+    def intersect(self, rays: RayQueue, hits: ShadingQueue, misses: RayQueue | None = None) -> None:
+        _check(load_library().wf_intersect(self._h, rays._h, hits._h, misses._h if misses else None),
+               "wf_intersect", self)
+
+    def shade(self, hits: ShadingQueue, next_rays: RayQueue, shadows: ShadowQueue) -> None:
+        _check(load_library().wf_shade(self._h, hits._h, next_rays._h, shadows._h), "wf_shade", self)
+
+    def occluded(self, shadows: ShadowQueue) -> None:
+        _check(load_library().wf_trace_occluded(self._h, shadows._h), "wf_trace_occluded", self)
+
+    def miss(self, misses: RayQueue) -> None:
+        _check(load_library().wf_miss(self._h, misses._h), "wf_miss", self)
+
+    def stage_image(self) -> np.ndarray:
+        p = self._stage
+        img = np.zeros(p.width * p.height * 3, np.float32)
+        _check(load_library().wf_stage_image(self._h, ptr(img), img.size), "wf_stage_image", self)
+        return img.reshape(p.height, p.width, 3)
 
     def render(self, params: WfRenderParams, accumulate: bool = False, out: np.ndarray | None = None):
         """wf_render (or wf_render_accumulate) into `out` when given — a

@@ -28,7 +28,8 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-prec-div=true",
               "-I", str(ROOT / "include")]
 CXX_FLAGS = ["-O2", "-fPIC", "-std=c++17", "-ffp-contract=off", "-I", str(ROOT / "include")]
 
-CUDA_SOURCES = ["wf_sort.cu", "wf_bvh.cu", "wf_render.cu", "wf_api.cpp", "wf_loop.cpp", "wf_static.cu"]
+CUDA_SOURCES = ["wf_sort.cu", "wf_bvh.cu", "wf_render.cu", "wf_api.cpp", "wf_loop.cpp", "wf_stages.cpp",
+                "wf_static.cu"]
 HOST_SOURCES = ["wf_scenes.cpp", "wf_scene_io.cpp"]
 
 

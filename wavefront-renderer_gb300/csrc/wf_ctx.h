@@ -135,6 +135,14 @@ struct wf_ctx {
     bool l2_limit_changed = false;
     size_t l2_limit_before = 0;
     const void* l2_window_base = nullptr;
+
+    // The render served by the per-bounce stage entry points (wf_stage_begin):
+    // its parameters, its device job (slot 0 of the job table, scene 0) and
+    // its pixel sums at offset 0 of the arena.
+    bool stage_live = false;
+    wf_render_params stage_params{};
+    wf::DeviceJob stage_job{};
+    int64_t stage_pixels = 0;
 };
 
 namespace wf {
@@ -152,6 +160,13 @@ int reset_cost_trackers(wf_ctx* c, int nmat, int ntex);
 int ensure_job_tables(wf_ctx* c, int jobs, int chunks);
 int sync_scene_table(wf_ctx* c);
 int check_device_flag(wf_ctx* c);
+// Job setup shared by the render loop and the per-bounce stage entry points
+// (wf_loop.cpp): a job's limits; its device form (accumulator at
+// accum_offset floats); the job table; a wave's chunks and header.
+int validate_job(wf_ctx* c, const wf_job& j);
+int make_device_job(wf_ctx* c, const wf_job& j, int64_t accum_offset, DeviceJob& dj);
+int upload_jobs(wf_ctx* c, const std::vector<DeviceJob>& jobs);
+int upload_wave(wf_ctx* c, const std::vector<WaveChunk>& chunks, int64_t total);
 // Points the context stream's L2 access-policy window at a scene's tree (or
 // clears it) according to wf_tuning::l2_persist.
 void apply_l2_policy(wf_ctx* c, int scene);

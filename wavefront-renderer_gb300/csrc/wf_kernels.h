@@ -132,6 +132,23 @@ void launch_hit_columns(const DeviceScene* scenes, const DeviceJob* jobs, RayQue
 void launch_permute_hits(HitQueueDev in, const uint32_t* perm, const ull* d_n, HitQueueDev out,
                          LaunchCfg cfg, cudaStream_t s);
 
+// Per-bounce stages on caller-held queues.  After a trace with ray_order 2
+// (records at the rays' indices, misses left alone): the hits listed in
+// hq.ray (k_compact_hits) and the misses in miss_list; the counts must be
+// zero before the launch.
+void launch_split_hits(const WaveTables& t, RayQueueDev rq, const ull* d_n, HitQueueDev hq, ull* hq_n,
+                       uint32_t* miss_list, ull* miss_n, LaunchCfg cfg, cudaStream_t s);
+// The miss loop over a queue of missed rays (single job t.job0 on t.scene0).
+void launch_miss_queue(const WaveTables& t, RayQueueDev misses, const ull* d_n, float* accum, LaunchCfg cfg,
+                       cudaStream_t s);
+// out[i] = in[perm ? perm[i] : i] in list layout (records at list positions);
+// at_ray: in's records sit at their rays' indices.
+void launch_materialize_hits(HitQueueDev in, bool at_ray, const uint32_t* perm, const ull* d_n, HitQueueDev out,
+                             LaunchCfg cfg, cudaStream_t s);
+// The ShadingQueue's columns of every entry (HitRecord + the ray's columns).
+void launch_shading_columns(const DeviceScene& S, RayQueueDev rq, HitQueueDev hq, bool at_ray, const ull* d_n,
+                            HitColumnsDev out, RayQueueDev rays_out, LaunchCfg cfg, cudaStream_t s);
+
 // image = accum / spp.
 void launch_finalize(const float* accum, int64_t nfloats, float spp, float* image, cudaStream_t s);
 

@@ -30,7 +30,7 @@
 
 using namespace wf;
 
-namespace {
+namespace wf {
 
 int validate_job(wf_ctx* c, const wf_job& j)
 {
@@ -96,6 +96,10 @@ int upload_wave(wf_ctx* c, const std::vector<WaveChunk>& chunks, int64_t total)
     WF_CK(c, cudaStreamSynchronize(c->stream));
     return WF_OK;
 }
+
+}  // namespace wf
+
+namespace {
 
 // The render loop's ray sort orders by the top wf_tuning::ray_sort_bits of
 // RayQueue::sortKey's 33 bits (octant, then Morton code of the origin): the
@@ -975,9 +979,15 @@ int wf_render_batch(wf_ctx* c, const wf_job* jobs, int32_t njobs, float* const* 
         }
         if (chunks.empty()) return set_err(c, WF_ERR_CAPACITY, "no job fits a wave");
         if ((rc = upload_wave(c, chunks, total))) return rc;
-        rc = graph ? wave_graph(c, max_depth, false, stats)
-                   : wave_host(c, total, wave_depth, WF_POLICY_NONE, false, 0, nullptr, nullptr,
-                               njobs == 1 ? &table[0] : nullptr, stats);
+        // without graph replay a lone job issues its bounces back to back with
+        // device-side counts (the single-job render's chain); several jobs in
+        // one wave take the host loop
+        if (graph)
+            rc = wave_graph(c, max_depth, false, stats);
+        else if (njobs == 1)
+            rc = wave_chain(c, wave_depth, false, table[0], stats, false, 0);
+        else
+            rc = wave_host(c, total, wave_depth, WF_POLICY_NONE, false, 0, nullptr, nullptr, nullptr, stats);
         if (rc) return rc;
         while (next < njobs && done[next] >= jobs[next].samples_per_pixel) ++next;
     }

@@ -1245,6 +1245,103 @@ __global__ void k_permute_hits(HitQueueDev in, const uint32_t* __restrict__ perm
     }
 }
 
+// ---------------------------------------------------------------------------
+// Per-bounce stages on caller-held queues (the wf_intersect / wf_miss /
+// wf_shading_queue_* entry points).
+// ---------------------------------------------------------------------------
+
+// The rays of a ray-order trace that missed (record tri < 0), listed with one
+// atomic per warp.
+__global__ void k_list_misses(const int32_t* __restrict__ tri, const ull* __restrict__ d_n, uint32_t* list,
+                              ull* list_n)
+{
+    const int64_t n = (int64_t)*d_n;
+    const int lane = threadIdx.x & 31;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += stride) {
+        const int64_t i = base + threadIdx.x;
+        const bool miss = i < n && tri[i] < 0;
+        const unsigned m = __ballot_sync(0xFFFFFFFFu, miss);
+        if (!m) continue;
+        ull first = 0;
+        if (lane == 0) first = atomicAdd(list_n, (ull)__popc(m));
+        first = __shfl_sync(0xFFFFFFFFu, first, 0);
+        if (miss) list[first + __popc(m & ((1u << lane) - 1u))] = (uint32_t)i;
+    }
+}
+
+// The miss loop over a queue of missed rays (renderScene, .cpp:256-265).
+__global__ void k_miss_queue(DeviceScene scene0, DeviceJob job0, RayQueueDev rq, const ull* __restrict__ d_n,
+                             float* accum)
+{
+    const int64_t n = (int64_t)*d_n;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        shade_miss<false>(scene0, job0, nullptr, nullptr, rq, i, accum);
+}
+
+// A hit queue in list order: entry i of `out` is entry perm[i] (or i) of `in`,
+// whose record sits at the entry's position or, with at_ray, at its ray's
+// index.  ShadingQueue::materialize for the compact queue.
+__global__ void k_materialize_hits(HitQueueDev in, int at_ray, const uint32_t* __restrict__ perm,
+                                   const ull* __restrict__ d_n, HitQueueDev out)
+{
+    const int64_t n = (int64_t)*d_n;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t j = perm ? (int64_t)perm[i] : i;
+        const int32_t ray = in.ray[j];
+        const int64_t r = at_ray ? (int64_t)ray : j;
+        out.ray[i] = ray;
+        out.tri[i] = in.tri[r];
+        out.t[i] = in.t[r];
+        out.bu[i] = in.bu[r];
+        out.bv[i] = in.bv[r];
+    }
+}
+
+// The 24 columns of a ShadingQueue, in queue order: the HitRecord rebuilt from
+// the triangle (as the traversal's epilogue builds it) and the ray's columns.
+__global__ void k_shading_columns(DeviceScene S, RayQueueDev rq, HitQueueDev hq, int at_ray,
+                                  const ull* __restrict__ d_n, HitColumnsDev out, RayQueueDev ro)
+{
+    const int64_t n = (int64_t)*d_n;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t ray = hq.ray[i];
+        const int64_t r = at_ray ? (int64_t)ray : i;
+        const V3 o = {rq.ox[ray], rq.oy[ray], rq.oz[ray]}, d = {rq.dx[ray], rq.dy[ray], rq.dz[ray]};
+        HitRec h;
+        rebuild_hit(S, o, d, hq.tri[r], hq.t[r], hq.bu[r], hq.bv[r], h);
+        out.geom[i] = h.geom;
+        out.prim[i] = h.prim;
+        out.t[i] = h.t;
+        out.bu[i] = hq.bu[r];
+        out.bv[i] = hq.bv[r];
+        out.px[i] = h.p.x;
+        out.py[i] = h.p.y;
+        out.pz[i] = h.p.z;
+        out.nx[i] = h.n.x;
+        out.ny[i] = h.n.y;
+        out.nz[i] = h.n.z;
+        out.front[i] = h.front ? 1 : 0;
+        out.u[i] = h.u;
+        out.v[i] = h.v;
+        out.mat[i] = h.mat;
+        out.tex[i] = h.tex;
+        ro.ox[i] = o.x;
+        ro.oy[i] = o.y;
+        ro.oz[i] = o.z;
+        ro.dx[i] = d.x;
+        ro.dy[i] = d.y;
+        ro.dz[i] = d.z;
+        ro.tr[i] = rq.tr[ray];
+        ro.tg[i] = rq.tg[ray];
+        ro.tb[i] = rq.tb[ray];
+        ro.pdf[i] = rq.pdf[ray];
+        ro.pixel[i] = rq.pixel[ray];
+        ro.depth[i] = rq.depth[ray];
+        ro.sample[i] = rq.sample[ray];
+    }
+}
+
 __global__ void k_finalize(const float* accum, int64_t n, float spp, float* image)
 {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
@@ -1632,6 +1729,32 @@ void launch_finalize_counts(const float* accum, const int32_t* count, int64_t np
 void launch_fill_i32(int32_t* a, int64_t n, int32_t v, bool identity, cudaStream_t s)
 {
     k_fill_i32<<<grid_for(n, 256, 65535), 256, 0, s>>>(a, n, v, identity ? 1 : 0);
+}
+
+void launch_split_hits(const WaveTables& t, RayQueueDev rq, const ull* d_n, HitQueueDev hq, ull* hq_n,
+                       uint32_t* miss_list, ull* miss_n, LaunchCfg cfg, cudaStream_t s)
+{
+    k_compact_hits<false, false><<<cfg.grid, 256, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, d_n, hq, hq_n,
+                                                           nullptr);
+    k_list_misses<<<cfg.grid, 256, 0, s>>>(hq.tri, d_n, miss_list, miss_n);
+}
+
+void launch_miss_queue(const WaveTables& t, RayQueueDev misses, const ull* d_n, float* accum, LaunchCfg cfg,
+                       cudaStream_t s)
+{
+    k_miss_queue<<<cfg.grid, 256, 0, s>>>(t.scene0, t.job0, misses, d_n, accum);
+}
+
+void launch_materialize_hits(HitQueueDev in, bool at_ray, const uint32_t* perm, const ull* d_n, HitQueueDev out,
+                             LaunchCfg cfg, cudaStream_t s)
+{
+    k_materialize_hits<<<cfg.grid, 256, 0, s>>>(in, at_ray ? 1 : 0, perm, d_n, out);
+}
+
+void launch_shading_columns(const DeviceScene& S, RayQueueDev rq, HitQueueDev hq, bool at_ray, const ull* d_n,
+                            HitColumnsDev out, RayQueueDev rays_out, LaunchCfg cfg, cudaStream_t s)
+{
+    k_shading_columns<<<cfg.grid, 256, 0, s>>>(S, rq, hq, at_ray ? 1 : 0, d_n, out, rays_out);
 }
 
 }  // namespace wf

@@ -157,6 +157,23 @@ void build_config0(wf_host_scene& s)
     set_camera(s);
 }
 
+// Config 104: config 0 lit also by a directional light (the reference's
+// DirectionalLight, include/core/Scene.h:57-62), with the short box made of
+// glass, so the directional NEE of WavefrontRenderer.cpp:712-737 runs on
+// Lambert, metal and glass hits.  The light comes in through the room's open
+// front, from above and in front of the camera: direction normalize(0.35,
+// -0.6, -1), warm white (1, 0.9, 0.75), intensity 1.5.
+void build_config104(wf_host_scene& s)
+{
+    add_room(s);
+    s.mats.push_back(metal(0.8f, 0.8f, 0.8f, 0.3f));  // 4 tall box, metal
+    s.mats.push_back(glass(1.5f));                     // 5 short box, glass
+    add_box(s, 4, {-0.19f, 0.0f, -0.42f}, {-0.025f, 0.33f, -0.255f}, 0.96592583f, 0.25881905f);
+    add_box(s, 5, {0.0325f, 0.0f, -0.2225f}, {0.1975f, 0.165f, -0.0575f}, 0.95105652f, -0.30901699f);
+    s.dir = wf_directional_light{{0.28745555f, -0.49278094f, -0.82130156f}, {1.0f, 0.9f, 0.75f}, 1.5f};
+    set_camera(s);
+}
+
 // --- seeded value noise / FBM (only +, -, *, floor) -----------------------
 uint32_t hash3(int x, int y, int z, uint32_t seed)
 {
@@ -611,6 +628,9 @@ int wf_host_scene_generate(int32_t config, uint64_t seed, wf_host_scene** out)
         break;
     case 100:  // small variant of config 1 (subdivision 4) for fast tests
         build_config1(*s, seed, 4);
+        break;
+    case 104:  // config 0 with a directional light and a glass box
+        build_config104(*s);
         break;
     default:
         delete s;
