@@ -47,20 +47,24 @@ WORKLOADS = {
 }
 METRIC = "Mrays/s (closest-hit + shadow rays) at equal MSE vs FP64 oracle"
 
-# Algorithmic bytes of the closest-hit kernel (k_trace_render) per ray:
-# read origin + direction (24 B); a hit writes its hit record (ray index,
-# leaf triangle, t, u, v: 20 B); a miss reads throughput + pixel (16 B) and
-# read-modify-writes its pixel's RGB sum (24 B).  BVH and triangle fetches are
-# scene-dependent and excluded (ncu DRAM bytes are reported beside).
+# Algorithmic bytes per unit of work (the fixed per-unit model of the path):
+# per closest-hit ray the compulsory inter-kernel state it moves — ray state
+# written and read (2 x 48 B), hit record written and read (2 x 20 B) and the
+# accumulator read-modify-write of an emission or miss (24 B): 160 B; per
+# shadow ray 2 x 44 B + 24 B = 112 B.  BVH and triangle fetches depend on the
+# scene and are excluded (ncu's DRAM bytes are reported beside as `traffic`).
+# The roofline of the dominant kernel (k_trace_render, the closest-hit
+# traversal) is 160 B x its rays / its measured time; the whole step's figure
+# applies both per-unit numbers to the step time.
+PIPE_BYTES_CLOSEST = 160
+PIPE_BYTES_SHADOW = 112
+# The closest-hit kernel's own reads and writes per ray (a narrower model,
+# reported beside): origin + direction read (24 B); a hit writes its record
+# (ray index, leaf triangle, t, u, v: 20 B); a miss reads throughput + pixel
+# (16 B) and read-modify-writes its pixel's RGB sum (24 B).
 BYTES_RAY = 24
 BYTES_HIT = 20
 BYTES_MISS = 16 + 24
-# The whole bounce loop's compulsory inter-kernel state, per closest-hit ray
-# (ray state written and read 2 x 48 B, hit record written and read 2 x 20 B,
-# accumulator read-modify-write 24 B) and per shadow ray (2 x 44 B + 24 B),
-# reported beside the kernel figure over the whole step.
-PIPE_BYTES_CLOSEST = 160
-PIPE_BYTES_SHADOW = 112
 
 
 def load_pkg():
@@ -611,8 +615,10 @@ def main() -> int:
     misses = sum(s["misses"] for s in stats)
     trace_ms = sum(s["ms_intersect"] for s in stats)
     launches = sum(s["bounces"] for s in stats)
-    alg_bytes = closest * BYTES_RAY + hits * BYTES_HIT + misses * BYTES_MISS
+    alg_bytes = closest * PIPE_BYTES_CLOSEST
     achieved = alg_bytes / (trace_ms / 1e3) / 1e9
+    io_bytes = closest * BYTES_RAY + hits * BYTES_HIT + misses * BYTES_MISS
+    io_achieved = io_bytes / (trace_ms / 1e3) / 1e9
     shadow = sum(s["shadow_rays"] for s in stats)
     step_ms = sum(s["ms_total"] for s in stats)
     pipe_achieved = (closest * PIPE_BYTES_CLOSEST + shadow * PIPE_BYTES_SHADOW) / (step_ms / 1e3) / 1e9
@@ -644,7 +650,12 @@ def main() -> int:
                      "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
                      "traffic": traffic, "launches": launches,
                      "alg_bytes_per_launch": alg_bytes / max(launches, 1),
+                     "alg_bytes_per_unit": {"closest_hit_ray": PIPE_BYTES_CLOSEST},
                      "avg_launch_ms": trace_ms / max(launches, 1),
+                     "kernel_io_model": {
+                         "bytes": "24 B ray read + 20 B hit record or 40 B miss (sky + accumulator)",
+                         "bytes_per_launch": io_bytes / max(launches, 1), "achieved": io_achieved,
+                         "frac": io_achieved / peak},
                      "pipeline_model": {
                          "bytes_per_closest_ray": PIPE_BYTES_CLOSEST, "bytes_per_shadow_ray": PIPE_BYTES_SHADOW,
                          "achieved": pipe_achieved, "frac": pipe_achieved / peak,

@@ -32,7 +32,7 @@ def _staged_render(wf, ctx, p, *, misses=True, policy=0, ray_sort=False, bounds=
     hits = wf.ShadingQueue(ctx, cap)
     shadows = wf.ShadowQueue(ctx, 3 * cap)
     ctx.stage_begin(p)
-    ctx.generate_primary(0, spp, rays)
+    ctx.stage_generate_primary(0, spp, rays)
     counts = []
     try:
         for depth in range(p.max_depth):

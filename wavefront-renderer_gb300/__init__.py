@@ -590,7 +590,7 @@ class Context:
         self._stage = params
         _check(load_library().wf_stage_begin(self._h, C.byref(params)), "wf_stage_begin", self)
 
-    def generate_primary(self, first_sample: int, nspp: int, out: RayQueue) -> None:
+    def stage_generate_primary(self, first_sample: int, nspp: int, out: RayQueue) -> None:
         _check(load_library().wf_generate_primary(self._h, first_sample, nspp, out._h), "wf_generate_primary", self)
 
     def intersect(self, rays: RayQueue, hits: ShadingQueue, misses: RayQueue | None = None) -> None:
