@@ -504,6 +504,149 @@ __global__ void k_wide_gather(const int* __restrict__ items, int count, int num_
     }
 }
 
+// SAH-optimal collapse (Ylitie, Karras & Laine, HPG 2017, section 4.1).  For
+// every interior binary node n and i = 1 .. kWidth-1, cost[n][i-1] is the
+// least SAH cost of representing n's subtree by at most i roots, each a wide
+// node or a leaf child of at most kLeafCnt triangles:
+//   C(n, 1) = min(leaf: A(n) c_prim N(n) if N(n) <= kLeafCnt,
+//                 node: A(n) c_node + D(n, kWidth))
+//   C(n, i) = min(C(n, i - 1), D(n, i)),   D(n, j) = min_a C(l, a) + C(r, j - a)
+// (a single triangle costs A c_prim for every i).  choice[n][i-1] records the
+// minimiser: kChoiceLeaf / kChoiceNode for i = 1, kChoiceFewer for C(n, i-1),
+// else the number of roots given to the left child; choice[n][kWidth-1] is
+// the split of D(n, kWidth), the children of n as a wide node.  The passes of
+// the clustering create parents after their children, so one launch per pass
+// in creation order sees its children's costs.
+constexpr float kSahNode = 1.0f, kSahPrim = 0.3f;
+constexpr uint8_t kChoiceLeaf = 0xF0, kChoiceNode = 0xF1, kChoiceFewer = 0xF2;
+
+__device__ __forceinline__ float box_area(const float* x)
+{
+    const float dx = x[3] - x[0], dy = x[4] - x[1], dz = x[5] - x[2];
+    return dx * dy + dy * dz + dz * dx;
+}
+
+template <int kWidth, int kLeafCnt>
+__global__ void k_wide_sah(int first_id, int count, int num_tris, const int* __restrict__ left,
+                           const int* __restrict__ right, const int* __restrict__ cnt,
+                           const float* __restrict__ nbox, float* __restrict__ cost, uint8_t* __restrict__ choice)
+{
+    constexpr int kC = kWidth - 1;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
+        const int id = first_id + k;
+        const int64_t in = id - num_tris;
+        const int kid[2] = {left[in], right[in]};
+        float c[2][kC];
+        for (int h = 0; h < 2; ++h) {
+            if (kid[h] < num_tris) {
+                const float a = box_area(nbox + 6 * (int64_t)kid[h]) * kSahPrim;
+                for (int i = 0; i < kC; ++i) c[h][i] = a;
+            } else {
+                const float* src = cost + (int64_t)(kid[h] - num_tris) * kC;
+                for (int i = 0; i < kC; ++i) c[h][i] = src[i];
+            }
+        }
+        float D[kWidth + 1];
+        uint8_t Dk[kWidth + 1];
+        for (int j = 2; j <= kWidth; ++j) {
+            float best = INFINITY;
+            int bk = 1;
+            for (int a = 1; a < j; ++a) {
+                const float v = c[0][a - 1] + c[1][j - a - 1];
+                if (v < best) {
+                    best = v;
+                    bk = a;
+                }
+            }
+            D[j] = best;
+            Dk[j] = (uint8_t)bk;
+        }
+        const float A = box_area(nbox + 6 * (int64_t)id);
+        const int N = cnt[id];
+        const float c_leaf = N <= kLeafCnt ? A * kSahPrim * (float)N : INFINITY;
+        const float c_node = A * kSahNode + D[kWidth];
+        float* dst = cost + in * kC;
+        uint8_t* ch = choice + in * kWidth;
+        float cur = fminf(c_leaf, c_node);
+        dst[0] = cur;
+        ch[0] = c_leaf <= c_node ? kChoiceLeaf : kChoiceNode;
+        for (int i = 2; i <= kC; ++i) {
+            if (D[i] < cur) {
+                cur = D[i];
+                ch[i - 1] = Dk[i];
+            } else {
+                ch[i - 1] = kChoiceFewer;
+            }
+            dst[i - 1] = cur;
+        }
+        ch[kWidth - 1] = Dk[kWidth];
+    }
+}
+
+// Children of each wide node from the SAH choices: the node's kWidth slots
+// are split between its binary children, recursively, down to roots of one
+// slot (a subtree of <= kLeafCnt triangles becomes a leaf child, a larger one
+// an interior child); same outputs as k_wide_gather.
+template <int kWidth, int kLeafCnt>
+__global__ void k_wide_gather_sah(const int* __restrict__ items, int count, int num_tris,
+                                  const int* __restrict__ left, const int* __restrict__ right,
+                                  const int* __restrict__ cnt, const uint8_t* __restrict__ choice,
+                                  int* __restrict__ kids, int* __restrict__ n_int, int* __restrict__ n_tri)
+{
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
+        const int b = items[k];
+        int ch[8];
+        int m = 0;
+        if (b < num_tris || cnt[b] <= kLeafCnt) {
+            ch[m++] = b;
+        } else {
+            int sn[2 * kWidth], ss[2 * kWidth];
+            int sp = 0;
+            const int64_t bi = b - num_tris;
+            const int a = choice[bi * kWidth + kWidth - 1];
+            sn[sp] = right[bi];
+            ss[sp++] = kWidth - a;
+            sn[sp] = left[bi];
+            ss[sp++] = a;
+            while (sp > 0 && m < kWidth) {
+                --sp;
+                const int x = sn[sp];
+                int j = ss[sp];
+                if (x < num_tris || j <= 1) {
+                    ch[m++] = x;
+                    continue;
+                }
+                const int64_t xi = x - num_tris;
+                uint8_t c = choice[xi * kWidth + j - 1];
+                while (c == kChoiceFewer && j > 1) {
+                    --j;
+                    c = choice[xi * kWidth + j - 1];
+                }
+                if (j <= 1 || c >= kChoiceLeaf || sp + 2 > 2 * kWidth) {
+                    ch[m++] = x;
+                    continue;
+                }
+                sn[sp] = right[xi];
+                ss[sp++] = j - c;
+                sn[sp] = left[xi];
+                ss[sp++] = c;
+            }
+        }
+        int ni = 0, nt = 0;
+        for (int i = 0; i < 8; ++i) {
+            kids[8 * (int64_t)k + i] = i < m ? ch[i] : -1;
+            if (i < m) {
+                if (cnt[ch[i]] > kLeafCnt)
+                    ++ni;
+                else
+                    nt += cnt[ch[i]];
+            }
+        }
+        n_int[k] = ni;
+        n_tri[k] = nt;
+    }
+}
+
 // Smallest power-of-two step 2^e (e in [-126, 127]) with lo + 255 * 2^e >= hi.
 __device__ __forceinline__ int wide_exponent(float lo, float hi)
 {
@@ -929,6 +1072,7 @@ struct BuildScratch {
 // triangles); depth from the root.
 struct PlocTree {
     int n = 0, root = 0;
+    std::vector<std::pair<int, int>> iters;  // (first node id, nodes) of each clustering pass
     float* nbox = nullptr;
     int *cnt = nullptr, *left = nullptr, *right = nullptr, *offset = nullptr, *depth = nullptr;
     int *block_sums = nullptr, *d_total = nullptr;
@@ -1008,6 +1152,7 @@ int ploc_tree(const BvhBuildInput& in, int num_sms, cudaStream_t s, std::string&
         cur_n = tot[1];
     }
     T.root = n == 1 ? 0 : next_id - 1;
+    T.iters = iters;
     k_ploc_root<<<1, 1, 0, s>>>(T.root, T.offset, T.depth);
     for (auto it = iters.rbegin(); it != iters.rend(); ++it)
         k_ploc_topdown<<<std::max(1, std::min(grid, (it->second + 255) / 256)), 256, 0, s>>>(
@@ -1091,6 +1236,8 @@ int build_ploc_wide(const BvhBuildInput& in, BvhBuildOutput& out, int num_sms, c
     const int grid = num_sms * 8;
     int *items, *next_items, *kids, *n_int, *n_tri, *int_off, *tri_off;
     uint32_t* wide_ids;
+    float* sah_cost = nullptr;
+    uint8_t* sah_choice = nullptr;
     int64_t cap_items = std::max(16, n / 2 + 16);
     int64_t cap_nodes = std::max<int64_t>(16, n / 4 + 16);
     int level_base = 0, count = 1, next_base = 1, tri_base = 0, levels = 0;
@@ -1104,6 +1251,13 @@ int build_ploc_wide(const BvhBuildInput& in, BvhBuildOutput& out, int num_sms, c
     WF_TRY(B.alloc(&tri_off, (size_t)cap_items));
     WF_TRY(B.alloc(&wide_ids, (size_t)n));
     WF_TRY(cudaMalloc(&out.wnodes, sizeof(WideNode) * (size_t)cap_nodes));
+    if (n > 1) {  // SAH costs and choices of every interior binary node, pass by pass
+        WF_TRY(B.alloc(&sah_cost, 7 * (size_t)(n - 1)));
+        WF_TRY(B.alloc(&sah_choice, 8 * (size_t)(n - 1)));
+        for (const auto& it : T.iters)
+            k_wide_sah<8, kWideLeafMax><<<std::max(1, std::min(grid, (it.second + 127) / 128)), 128, 0, s>>>(
+                it.first, it.second, n, T.left, T.right, T.cnt, T.nbox, sah_cost, sah_choice);
+    }
     WF_TRY(cudaMemcpyAsync(items, &T.root, sizeof(int), cudaMemcpyHostToDevice, s));
     while (count > 0) {
         if (++levels > kWideStack) {
@@ -1111,7 +1265,12 @@ int build_ploc_wide(const BvhBuildInput& in, BvhBuildOutput& out, int num_sms, c
             goto fail;
         }
         const int g = std::max(1, std::min(grid, (count + 127) / 128));
-        k_wide_gather<8, kWideLeafMax><<<g, 128, 0, s>>>(items, count, n, T.left, T.right, T.cnt, T.nbox, kids, n_int, n_tri);
+        if (n > 1)
+            k_wide_gather_sah<8, kWideLeafMax><<<g, 128, 0, s>>>(items, count, n, T.left, T.right, T.cnt, sah_choice,
+                                                                 kids, n_int, n_tri);
+        else
+            k_wide_gather<8, kWideLeafMax><<<g, 128, 0, s>>>(items, count, n, T.left, T.right, T.cnt, T.nbox, kids,
+                                                             n_int, n_tri);
         exclusive_scan_i32(n_int, count, int_off, T.block_sums, T.d_total, s);
         exclusive_scan_i32(n_tri, count, tri_off, T.block_sums, T.d_total + 1, s);
         int tot[2] = {0, 0};

@@ -218,8 +218,6 @@ __global__ void __launch_bounds__(128) k_occluded_api(DeviceScene S, int64_t n, 
     }
 }
 
-constexpr int kTopNodes = 256;  // 16 KB of the tree's top staged per block
-
 // Speculation switch of the binary traversal (the wide one has none).
 template <class Tr>
 __device__ __forceinline__ void set_speculative(Tr& tr, bool on)
@@ -238,17 +236,6 @@ __device__ __forceinline__ void set_speculative(Tr& tr, bool on)
 // its own: as a launch argument the choice cost the dense mesh 0.7%).
 constexpr int kFarFirstTriangles = 4096;
 using TraversalFar = Traversal<true, true>;
-
-// The traversal stack of a thread: its local array, or its column of the
-// block's shared array.
-template <bool kShared, class E>
-__device__ __forceinline__ auto pick_stack(E* local, uint32_t* shared)
-{
-    if constexpr (kShared)
-        return SharedStack32{shared + threadIdx.x};
-    else
-        return local;
-}
 
 __device__ __forceinline__ void accum_add(float* accum, int32_t slot, V3 c)
 {
@@ -280,7 +267,7 @@ __device__ __forceinline__ void accum_add(float* accum, int32_t slot, V3 c)
 // ---------------------------------------------------------------------------
 // kMulti = false: every ray belongs to job0 on scene0 (passed by value, read
 // from the constant bank); true: each ray looks its job and scene up.
-template <bool kMulti, int kMinBlocks, class Tr, bool kSharedStack = false, bool kTopStage = false>
+template <bool kMulti, int kMinBlocks, class Tr>
 __global__ void __launch_bounds__(128, kMinBlocks) k_trace_render(DeviceScene scene0, DeviceJob job0,
                                                                   const DeviceScene* __restrict__ scenes,
                                                                   const DeviceJob* __restrict__ jobs,
@@ -293,21 +280,9 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_trace_render(DeviceScene sc
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     Tr tr;
-    typename Tr::Entry local_stack[kSharedStack ? 1 : Tr::kStack];
-    __shared__ uint32_t shared_stack[kSharedStack ? kStackSize * 128 : 1];
-    const auto stack = pick_stack<kSharedStack>(local_stack, shared_stack);
+    typename Tr::Entry stack[Tr::kStack];
     const DeviceScene* S = kMulti ? scenes : &scene0;
     set_speculative(tr, speculative != 0);
-    // top of the single scene's tree in shared memory (node staging)
-    __shared__ BvhNode top_nodes[kTopStage ? kTopNodes : 1];
-    uint32_t num_top = 0;
-    if constexpr (kTopStage) {
-        num_top = (uint32_t)min(kTopNodes, scene0.num_nodes);
-        const float4* src = reinterpret_cast<const float4*>(scene0.nodes);
-        float4* dst = reinterpret_cast<float4*>(top_nodes);
-        for (uint32_t i = threadIdx.x; i < 4u * num_top; i += blockDim.x) dst[i] = __ldg(src + i);
-        __syncthreads();
-    }
     int job = 0;
     int64_t ray = -1;
     bool exhausted = false;
@@ -390,10 +365,7 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_trace_render(DeviceScene sc
         if (__all_sync(0xFFFFFFFFu, ray < 0)) break;
         // 3. one traversal round
         if (ray >= 0 && !tr.done()) {
-            if constexpr (kTopStage)
-                tr.round(*S, stack, top_nodes, num_top);
-            else
-                tr.round(*S, stack);
+            tr.round(*S, stack);
         }
     }
     if (overflow) atomicOr(err, 1);
@@ -870,7 +842,7 @@ __global__ void __launch_bounds__(128, (kMulti || kTimed) ? WF_SHADE_MIN_BLOCKS 
 // Shadow rays (EmbreeAccelerator::occluded): unblocked contributions are
 // added to their pixel.  Same persistent, dynamic-fetch structure as
 // k_trace_render.
-template <bool kMulti, int kMinBlocks, class Tr, bool kSharedStack = false, bool kTopStage = false>
+template <bool kMulti, int kMinBlocks, class Tr>
 __global__ void __launch_bounds__(128, kMinBlocks) k_occluded_render(DeviceScene scene0, DeviceJob job0,
                                                                      const DeviceScene* __restrict__ scenes,
                                                                      const DeviceJob* __restrict__ jobs,
@@ -883,21 +855,9 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_occluded_render(DeviceScene
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     Tr tr;
-    typename Tr::Entry local_stack[kSharedStack ? 1 : Tr::kStack];
-    __shared__ uint32_t shared_stack[kSharedStack ? kStackSize * 128 : 1];
-    const auto stack = pick_stack<kSharedStack>(local_stack, shared_stack);
+    typename Tr::Entry stack[Tr::kStack];
     const DeviceScene* S = kMulti ? scenes : &scene0;
     set_speculative(tr, speculative != 0);
-    // top of the single scene's tree in shared memory (node staging)
-    __shared__ BvhNode top_nodes[kTopStage ? kTopNodes : 1];
-    uint32_t num_top = 0;
-    if constexpr (kTopStage) {
-        num_top = (uint32_t)min(kTopNodes, scene0.num_nodes);
-        const float4* src = reinterpret_cast<const float4*>(scene0.nodes);
-        float4* dst = reinterpret_cast<float4*>(top_nodes);
-        for (uint32_t i = threadIdx.x; i < 4u * num_top; i += blockDim.x) dst[i] = __ldg(src + i);
-        __syncthreads();
-    }
     int job = 0;
     int64_t ray = -1;
     bool exhausted = false;
@@ -935,10 +895,7 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_occluded_render(DeviceScene
         }
         if (__all_sync(0xFFFFFFFFu, ray < 0)) break;
         if (ray >= 0 && !tr.done()) {
-            if constexpr (kTopStage)
-                tr.round(*S, stack, top_nodes, num_top);
-            else
-                tr.round(*S, stack);
+            tr.round(*S, stack);
         }
     }
     if (overflow) atomicOr(err, 1);

@@ -422,27 +422,34 @@ struct WideTraversal {
     __device__ __forceinline__ bool done() const { return fin; }
     __device__ __forceinline__ void idle() { fin = true; }
 
+    // One round walks interior nodes (the nearest remaining hit child of the
+    // current group, popping groups as they empty) until a node hits leaf
+    // children, then tests those triangles: like the binary while-while
+    // round, it ends at a leaf, so the persistent kernel's per-round work
+    // (result ballots, refills) is paid once per leaf visit, not per node.
     __device__ __forceinline__ void round(const DeviceScene& S, uint2* stack)
     {
         uint32_t tri_base = 0, tri_hits = 0;
-        if (ng.y > 0x00FFFFFFu) {
-            const uint32_t b = 31u - (uint32_t)__clz(ng.y);
-            ng.y &= ~(1u << b);
-            const uint32_t slot = (b - 24u) ^ octinv;
-            const uint32_t node = ng.x + (uint32_t)__popc(ng.y & ((1u << slot) - 1u) & 0xFFu);
+        for (;;) {
             if (ng.y > 0x00FFFFFFu) {
-                if (sp < kStack)
-                    stack[sp++] = ng;
-                else
-                    overflow = true;
+                const uint32_t b = 31u - (uint32_t)__clz(ng.y);
+                ng.y &= ~(1u << b);
+                const uint32_t slot = (b - 24u) ^ octinv;
+                const uint32_t node = ng.x + (uint32_t)__popc(ng.y & ((1u << slot) - 1u) & 0xFFu);
+                if (ng.y > 0x00FFFFFFu) {
+                    if (sp < kStack)
+                        stack[sp++] = ng;
+                    else
+                        overflow = true;
+                }
+                intersect_node(S.wnodes + node, tri_base, tri_hits);
+                if (tri_hits) break;
+            } else if (sp > 0) {
+                ng = stack[--sp];
+            } else {
+                fin = true;
+                return;
             }
-            intersect_node(S.wnodes + node, tri_base, tri_hits);
-        } else if (sp > 0) {
-            ng = stack[--sp];
-            return;
-        } else {
-            fin = true;
-            return;
         }
         while (tri_hits) {
             const int lp = (int)tri_base + __ffs(tri_hits) - 1;
@@ -495,7 +502,9 @@ struct WideTraversal {
         const uint32_t hiz[2] = {__float_as_uint(w4.z), __float_as_uint(w4.w)};
         const uint32_t meta[2] = {meta0, meta1};
         uint32_t hits_i = 0, hits_t = 0;
-#pragma unroll
+        // two slots per iteration: 64 registers (8 resident blocks) instead of
+        // 96 with all eight unrolled
+#pragma unroll 2
         for (int s = 0; s < 8; ++s) {
             const int wd = s >> 2;
             const uint32_t sh = 8u * (uint32_t)(s & 3);
