@@ -524,7 +524,6 @@ def main() -> int:
     ap.add_argument("--autotune", type=int, default=0, help="run wf_autotune on the workload before timing")
     ap.add_argument("--speculative", type=int, default=0, help="1 = speculative while-while traversal")
     ap.add_argument("--adaptive", type=int, default=0, help="the reference's adaptive sampling (threshold 0.05)")
-    ap.add_argument("--l2-persist", type=int, default=0, help="mark the tree persisting in L2")
     ap.add_argument("--ray-sort-bits", type=int, default=0, help="key bits of the loop's ray sort (0 = 33)")
     ap.add_argument("--cost-rr", type=int, default=0, help="cost-aware RR fed by the live device CostTracker")
     ap.add_argument("--batched-jobs", type=int, default=512,
@@ -558,7 +557,7 @@ def main() -> int:
     scene = pkg.HostScene(wl["config"])
     ctx.set_tuning(max(args.trace_variant, 0), args.blocks_per_sm,
                    bvh_builder={"ploc": 0, "lbvh": 1, "wide": 2, "ploc4": 3}[args.bvh],
-                   speculative_traversal=args.speculative, l2_persist=args.l2_persist,
+                   speculative_traversal=args.speculative,
                    ray_sort_bits=args.ray_sort_bits)
     info = ctx.upload(scene.desc)
     W, H = wl["width"], wl["height"]

@@ -276,10 +276,7 @@ int wf_scene_get_info(wf_ctx* ctx, wf_scene_info* out_info);
 /* Launch tuning of a context (the autotuner's knobs).  trace_variant: 0 = no
  * occupancy hint on the traversal kernels (the closest-hit kernel of a
  * single-job render whose binary tree and triangles exceed L2 runs as 1),
- * 1 = 9 blocks of 128 threads per
- * SM (56 registers, no spills), 2 = the traversal stack in shared memory instead of local memory
- * (binary trees; 32 KB per block), 3 = the top 256 nodes of the tree staged
- * in shared memory (binary trees, single-scene renders).
+ * 1 = 9 blocks of 128 threads per SM (56 registers, no spills).
  * persistent_blocks_per_sm: resident blocks launched per
  * SM by the persistent traversal kernels (0 = 16).  graph_mode: whether a
  * wave's bounce chain is captured once as a CUDA graph and replayed. */
@@ -307,10 +304,7 @@ typedef struct wf_tuning {
     int32_t speculative_traversal; /* 0 = while-while traversal (default);
                             1 = speculative while-while (lanes postpone their
                             first leaf until every lane of the warp has one) */
-    int32_t l2_persist;  /* 1 = mark the scene's tree (nodes + triangles, one
-                            range) persisting in L2 for this context's stream,
-                            up to the device's set-aside; the context's
-                            persisting-lines limit is put back at wf_destroy */
+    int32_t reserved;    /* must be 0 */
     int32_t ray_sort_bits; /* the render loop's ray sort uses the top bits of
                             RayQueue::sortKey's 33 (0 = all 33; fewer bits =
                             fewer 8-bit passes, coarser grouping); the host
@@ -321,8 +315,8 @@ int wf_get_tuning(const wf_ctx* ctx, wf_tuning* out_tuning);
 
 /* Autotuner (no reference counterpart): renders one wave of `params` on the
  * current scene (samples capped at one wave, adaptive sampling and cost
- * tracking off) under every combination of trace_variant {0, 1, 2, 3}
- * (block occupancy, stack placement, node staging), persistent_blocks_per_sm
+ * tracking off) under every combination of trace_variant {0, 1}
+ * (block occupancy), persistent_blocks_per_sm
  * {4, 8, 12, 16, 24}, graph_mode {2, 1} and speculative_traversal {0, 1}, each
  * once untimed and twice
  * timed on the device; then, when params sort rays or shading, the

@@ -383,36 +383,6 @@ int schedule_columns(wf_ctx* c, int policy, const ull* d_n, int64_t n, ShadeColu
     return WF_OK;
 }
 
-void apply_l2_policy(wf_ctx* c, int scene)
-{
-    cudaStreamAttrValue attr{};
-    const ResidentScene* R = (scene >= 0 && scene < (int)c->scenes.size()) ? &c->scenes[scene] : nullptr;
-    const bool on = c->tuning.l2_persist && c->l2_persist_max > 0 && R && R->live && R->tree_base;
-    if (!on) {
-        if (c->l2_window_base) {
-            attr.accessPolicyWindow.base_ptr = nullptr;
-            attr.accessPolicyWindow.num_bytes = 0;
-            cudaStreamSetAttribute(c->stream, cudaStreamAttributeAccessPolicyWindow, &attr);
-            c->l2_window_base = nullptr;
-        }
-        return;
-    }
-    if (c->l2_window_base == R->tree_base) return;
-    if (!c->l2_limit_changed) {
-        cudaDeviceGetLimit(&c->l2_limit_before, cudaLimitPersistingL2CacheSize);
-        c->l2_limit_changed = true;
-    }
-    cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, c->l2_persist_max);
-    const size_t window = std::min(R->tree_bytes, c->l2_window_max);
-    attr.accessPolicyWindow.base_ptr = const_cast<void*>(R->tree_base);
-    attr.accessPolicyWindow.num_bytes = window;
-    attr.accessPolicyWindow.hitRatio = (float)std::min(1.0, (double)c->l2_persist_max / (double)std::max<size_t>(window, 1));
-    attr.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
-    attr.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
-    cudaStreamSetAttribute(c->stream, cudaStreamAttributeAccessPolicyWindow, &attr);
-    c->l2_window_base = R->tree_base;
-}
-
 int check_device_flag(wf_ctx* c)
 {
     int flag = 0;
@@ -625,8 +595,7 @@ int build_scene(wf_ctx* c, const wf_scene_desc* D, ResidentScene& R)
         cleanup_tmp();
         if (brc) return set_err(c, WF_ERR_CUDA, "BVH build failed: " + err);
         // Tree nodes and triangles in one allocation, nodes first: one
-        // address range the traversal reads, which an L2 persistence window
-        // can cover (wf_tuning::l2_persist).
+        // address range the traversal reads.
         {
             const size_t node_bytes = (size_t)bo.num_nodes * tree_node_bytes(bo);
             const size_t tri_bytes = 3 * sizeof(float4) * (size_t)ntri;
@@ -846,8 +815,6 @@ int wf_create(const wf_config* cfg, wf_ctx** out)
     c->l2_bytes = prop.l2CacheSize;
     c->shade_per_sm = shade_blocks_per_sm(true);
     c->shade_per_sm_other = shade_blocks_per_sm(false);
-    c->l2_persist_max = (size_t)std::max(0, prop.persistingL2CacheMaxSize);
-    c->l2_window_max = (size_t)std::max(0, prop.accessPolicyMaxWindowSize);
     bool ok = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) == cudaSuccess;
     for (auto& e : c->ev) ok = ok && cudaEventCreate(&e) == cudaSuccess;
     for (auto& e : c->timer) ok = ok && cudaEventCreate(&e) == cudaSuccess;
@@ -873,10 +840,6 @@ int wf_destroy(wf_ctx* c)
     if (!c) return WF_OK;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
-    if (c->l2_limit_changed) {  // put the persisting-lines limit back as found
-        cudaCtxResetPersistingL2Cache();
-        cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, c->l2_limit_before);
-    }
     drop_graphs(c);
     for (auto& r : c->scenes) free_scene_res(r);
     free_all(c->render_allocs);
@@ -1241,7 +1204,7 @@ int wf_get_stream(wf_ctx* c, void** out)
 int wf_set_tuning(wf_ctx* c, const wf_tuning* t)
 {
     if (!c || !t) return WF_ERR_INVALID_ARGUMENT;
-    if (t->trace_variant < 0 || t->trace_variant > 3 || t->persistent_blocks_per_sm < 0 ||
+    if (t->trace_variant < 0 || t->trace_variant > 1 || t->persistent_blocks_per_sm < 0 ||
         t->persistent_blocks_per_sm > 32 || t->bvh_builder < 0 || t->bvh_builder > 3)
         return set_err(c, WF_ERR_INVALID_ARGUMENT, "tuning out of range");
     c->tuning = *t;

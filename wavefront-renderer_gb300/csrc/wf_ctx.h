@@ -129,12 +129,6 @@ struct wf_ctx {
     std::vector<cudaEvent_t> stage_ev;  // per-bounce stage events of the device-counted chain
     wf_tuning tuning{};
 
-    // L2 persistence (wf_tuning::l2_persist): the device's limits, and the
-    // persisting-lines limit this context found, restored at wf_destroy.
-    size_t l2_persist_max = 0, l2_window_max = 0;
-    bool l2_limit_changed = false;
-    size_t l2_limit_before = 0;
-    const void* l2_window_base = nullptr;
 
     // The render served by the per-bounce stage entry points (wf_stage_begin):
     // its parameters, its device job (slot 0 of the job table, scene 0) and
@@ -167,9 +161,6 @@ int validate_job(wf_ctx* c, const wf_job& j);
 int make_device_job(wf_ctx* c, const wf_job& j, int64_t accum_offset, DeviceJob& dj);
 int upload_jobs(wf_ctx* c, const std::vector<DeviceJob>& jobs);
 int upload_wave(wf_ctx* c, const std::vector<WaveChunk>& chunks, int64_t total);
-// Points the context stream's L2 access-policy window at a scene's tree (or
-// clears it) according to wf_tuning::l2_persist.
-void apply_l2_policy(wf_ctx* c, int scene);
 void drop_graphs(wf_ctx* c);
 // Sorts n scheduling columns under a ShadingQueue policy; *perm_out gets the
 // permutation (device).  Materials and texture sizes of one scene.

@@ -535,7 +535,6 @@ int render_single(wf_ctx* c, const wf_render_params* P, wf_render_stats* st)
     rc = upload_jobs(c, table);
     if (rc) return rc;
     WF_CK(c, cudaMemsetAsync(c->arena, 0, sizeof(float) * 3 * (size_t)np, s));
-    apply_l2_policy(c, 0);
     const bool graph = !tracking && use_graph(c, false, P->policy);
     // without a policy (and without a sort-or-skip threshold, a host decision)
     // the bounces need no host round trip
@@ -779,7 +778,7 @@ int wf_autotune(wf_ctx* c, const wf_render_params* P, wf_tuning* out, double* ou
     const wf_tuning base = c->tuning;
     wf_tuning best = base;
     double best_ms = -1.0;
-    const int variants[4] = {0, 1, 2, 3};
+    const int variants[2] = {0, 1};
     const int blocks[5] = {4, 8, 12, 16, 24};
     const int graphs[2] = {2, 1};
     const int specs[2] = {0, 1};

@@ -1425,11 +1425,11 @@ void launch_occluded_api(const DeviceScene& S, int64_t n, const float* ox, const
                                                              out, err);
 }
 
-// variant: 0 = no occupancy hint, 1 = 9 blocks of 128 per SM, 2 = the
-// traversal stack in shared memory (binary trees), 3 = the top 256 nodes of
-// the tree staged in shared memory (binary trees, single-scene waves; else
-// variant 0); the traversal follows the scene's tree (binary, 4-wide or
-// compressed 8-wide).
+// variant: 0 = no occupancy hint, 1 = 9 blocks of 128 per SM; the traversal
+// follows the scene's tree (binary, 4-wide or compressed 8-wide).  (The
+// traversal stack in shared memory, -10%, the top 256 nodes staged in shared
+// memory, -8% / -10%, and an L2 persistence window over the tree, -4%,
+// measured slower than these on both workloads and were taken out.)
 // Where a ray-order bounce shades its misses: an environment-map lookup
 // (atan2, asin, a texel fetch) evaluated by finished lanes inside the
 // traversal loop stalls their warp, so for a single-job render of a scene
@@ -1458,23 +1458,13 @@ void launch_trace_render(const WaveTables& t, RayQueueDev rq, const ull* d_n, Hi
                                                      accum, work, err, cfg.speculative, cfg.ray_order)
 #define WF_TRACE2(M, T) \
     if (cfg.variant == 1) WF_TRACE(M, 9, T); else WF_TRACE(M, 1, T)
-#define WF_TRACE_SHARED(M)                                                                                \
-    k_trace_render<M, 1, Traversal<false>, true><<<cfg.grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, \
-                                                                         rq, d_n, hq, hq_n, accum, work, err, \
-                                                                         cfg.speculative, cfg.ray_order)
     if (t.tree == kTreeWide8) {
         if (t.multi) { WF_TRACE2(true, WideTraversal<false>); } else { WF_TRACE2(false, WideTraversal<false>); }
     } else if (t.tree == kTreeFour) {
         if (t.multi) { WF_TRACE2(true, Traversal4<false>); } else { WF_TRACE2(false, Traversal4<false>); }
-    } else if (cfg.variant == 2) {
-        if (t.multi) { WF_TRACE_SHARED(true); } else { WF_TRACE_SHARED(false); }
-    } else if (cfg.variant == 3 && !t.multi && t.scene0.nodes) {
-        k_trace_render<false, 1, Traversal<false>, false, true><<<cfg.grid, 128, 0, s>>>(
-            t.scene0, t.job0, t.scenes, t.jobs, rq, d_n, hq, hq_n, accum, work, err, cfg.speculative, cfg.ray_order);
     } else {
         if (t.multi) { WF_TRACE2(true, Traversal<false>); } else { WF_TRACE2(false, Traversal<false>); }
     }
-#undef WF_TRACE_SHARED
 #undef WF_TRACE2
 #undef WF_TRACE
 }
@@ -1553,25 +1543,15 @@ void launch_occluded_render(const WaveTables& t, ShadowQueueDev sh, const ull* s
                                                         err, cfg.speculative)
 #define WF_OCC2(M, T) \
     if (cfg.variant == 1) WF_OCC(M, 9, T); else WF_OCC(M, 1, T)
-#define WF_OCC_SHARED(M)                                                                                     \
-    k_occluded_render<M, 1, Traversal<true>, true><<<cfg.grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, \
-                                                                           sh, sh_n, accum, work, err, \
-                                                                           cfg.speculative)
     if (t.tree == kTreeWide8) {
         if (t.multi) { WF_OCC2(true, WideTraversal<true>); } else { WF_OCC2(false, WideTraversal<true>); }
     } else if (t.tree == kTreeFour) {
         if (t.multi) { WF_OCC2(true, Traversal4<true>); } else { WF_OCC2(false, Traversal4<true>); }
-    } else if (cfg.variant == 2) {
-        if (t.multi) { WF_OCC_SHARED(true); } else { WF_OCC_SHARED(false); }
-    } else if (cfg.variant == 3 && !t.multi && t.scene0.nodes) {
-        k_occluded_render<false, 1, Traversal<true>, false, true><<<cfg.grid, 128, 0, s>>>(
-            t.scene0, t.job0, t.scenes, t.jobs, sh, sh_n, accum, work, err, cfg.speculative);
     } else if (far_first) {
         WF_OCC2(false, TraversalFar);
     } else {
         if (t.multi) { WF_OCC2(true, Traversal<true>); } else { WF_OCC2(false, Traversal<true>); }
     }
-#undef WF_OCC_SHARED
 #undef WF_OCC2
 #undef WF_OCC
 }

@@ -66,13 +66,6 @@ constexpr uint32_t kSentinel = 0xFFFFFFFFu;
 // interior nodes down to a leaf, then leaves until it pops an interior node or
 // the stack's sentinel, so the lanes of a warp reconverge after every round
 // and a persistent kernel can hand a finished lane a new ray between rounds.
-// A traversal stack kept in shared memory, entry i of thread t at
-// base[i * 128 + t] (one 128-thread block, no bank conflicts between lanes).
-struct SharedStack32 {
-    uint32_t* p;  // shared array + threadIdx.x
-    __device__ __forceinline__ uint32_t& operator[](int i) const { return p[i * 128]; }
-};
-
 template <bool kAnyHit, bool kFarFirst = false>
 struct Traversal {
     using Entry = uint32_t;
@@ -85,8 +78,6 @@ struct Traversal {
     int sp;
     bool overflow;
     bool speculative = false;
-    const BvhNode* top_nodes = nullptr;  // staged top of the tree (shared memory)
-    uint32_t num_top = 0;
     TraceResult res;
 
     // The stack lives outside the struct (a dynamically indexed array would
@@ -140,16 +131,6 @@ struct Traversal {
         round(S.nodes, S.tris, stack);
     }
 
-    // With the top of the tree staged in shared memory: nodes [0, ntop)
-    // (the root and the last clustering passes' nodes) come from `top`.
-    template <class Stk>
-    __device__ __forceinline__ void round(const DeviceScene& S, Stk stack, const BvhNode* staged, uint32_t ntop)
-    {
-        top_nodes = staged;
-        num_top = ntop;
-        round(S.nodes, S.tris, stack);
-    }
-
     // nodes / tris of the ray's scene: from the kernel's parameter bank when
     // every ray shares one scene, else from the scene table.
     template <class Stk>
@@ -161,7 +142,7 @@ struct Traversal {
             // leaves until an interior node or the sentinel comes off the
             // stack.
             while (!(cur & kLeafFlag)) {
-                const BvhNode nd = cur < num_top ? top_nodes[cur] : load_node(nodes, cur);
+                const BvhNode nd = load_node(nodes, cur);
                 float tn0, tn1;
                 bool h0, h1;
                 slab2(nd, inv, oi, tmin, best_t, tn0, tn1, h0, h1);
@@ -195,7 +176,7 @@ struct Traversal {
         uint32_t postponed = 0u;  // leaf words always carry kLeafFlag, so 0 = none
         for (;;) {
             if (cur != kSentinel && !(cur & kLeafFlag)) {
-                const BvhNode nd = cur < num_top ? top_nodes[cur] : load_node(nodes, cur);
+                const BvhNode nd = load_node(nodes, cur);
                 float tn0, tn1;
                 bool h0, h1;
                 slab2(nd, inv, oi, tmin, best_t, tn0, tn1, h0, h1);
@@ -297,11 +278,6 @@ struct Traversal4 : Traversal<kAnyHit> {
 
     template <class Stk>
     __device__ __forceinline__ void round(const DeviceScene& S, Stk stack)
-    {
-        round4(S.nodes4, S.tris, stack);
-    }
-    template <class Stk>
-    __device__ __forceinline__ void round(const DeviceScene& S, Stk stack, const BvhNode*, uint32_t)
     {
         round4(S.nodes4, S.tris, stack);
     }
