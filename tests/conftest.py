@@ -113,8 +113,9 @@ def fp64_band(img, spp, golden, block=8):
     counts both sides: sigma^2/spp for the image and sigma^2/golden_spp for
     the oracle's own mean.  A block where the render drew a rare path that the
     oracle's variance estimate never saw gets an enormous z without any bias,
-    so the mean and spread of the z-scores are taken winsorized at |z| = 10
-    (the number of such blocks is reported):
+    so the mean and spread of the z-scores are taken winsorized at |z| = 5
+    (a normal z passes 5 with probability 6e-7; the number of blocks beyond is
+    reported, and the tail check below still counts them):
       * bias: the mean block z-score is within 3 standard errors of 0;
       * spread: their standard deviation is 1 +- 0.15;
       * tail: |z| > 3 on fewer than 3% of blocks (a normal tail gives 0.27%);
@@ -130,13 +131,13 @@ def fp64_band(img, spp, golden, block=8):
     bv = pix_var.reshape(H // block, block, W // block, block, 3).sum((1, 3)) / block ** 4
     live = bv > 1e-14  # blocks that see only a constant sky have no variance
     z = (bx - bm)[live] / np.sqrt(bv[live])
-    zw = np.clip(z, -10.0, 10.0)
+    zw = np.clip(z, -5.0, 5.0)
     mse = float(((img - mean) ** 2).mean())
     expected = float(pix_var.mean())
     ch_se = np.sqrt(pix_var.sum((0, 1))) / (H * W)
     ch_diff = img.astype(np.float64).mean((0, 1)) - mean.mean((0, 1))
     out = {"mse": mse, "expected_mse": expected, "z_mean": float(zw.mean()), "z_std": float(zw.std()),
-           "z_beyond_10": int((np.abs(z) > 10).sum()), "z_max_abs": float(np.abs(z).max()),
+           "z_beyond_5": int((np.abs(z) > 5).sum()), "z_max_abs": float(np.abs(z).max()),
            "tail_frac": float((np.abs(z) > 3).mean()), "blocks": int(z.size),
            "channel_rel": (ch_diff / mean.mean((0, 1))).tolist(), "channel_z": (ch_diff / ch_se).tolist(),
            "spp": spp, "oracle_spp": gspp}
