@@ -563,8 +563,10 @@ __global__ void k_wide_sah(int first_id, int count, int num_tris, const int* __r
         }
         const float A = box_area(nbox + 6 * (int64_t)id);
         const int N = cnt[id];
+        // a subtree of <= kLeafCnt triangles is always one leaf child when it
+        // takes one slot (the emit kernels make it one)
         const float c_leaf = N <= kLeafCnt ? A * kSahPrim * (float)N : INFINITY;
-        const float c_node = A * kSahNode + D[kWidth];
+        const float c_node = N <= kLeafCnt ? INFINITY : A * kSahNode + D[kWidth];
         float* dst = cost + in * kC;
         uint8_t* ch = choice + in * kWidth;
         float cur = fminf(c_leaf, c_node);
@@ -1334,8 +1336,17 @@ int build_ploc4(const BvhBuildInput& in, BvhBuildOutput& out, int num_sms, cudaS
     PlocTree T;
     const int grid = num_sms * 8;
     int *keep, *keep_off, *items, *next_items, *kids, *n_int, *n_tri, *int_off;
+    float* sah_cost = nullptr;
+    uint8_t* sah_choice = nullptr;
     int cap = 1, level_base = 0, count = 1, next_base = 1, levels = 0;
     if (ploc_tree(in, num_sms, s, err, B, T)) goto fail;
+    if (n > 1) {  // SAH costs and choices for 4-wide nodes, pass by pass
+        WF_TRY(B.alloc(&sah_cost, 3 * (size_t)(n - 1)));
+        WF_TRY(B.alloc(&sah_choice, 4 * (size_t)(n - 1)));
+        for (const auto& it : T.iters)
+            k_wide_sah<4, kLeafMax><<<std::max(1, std::min(grid, (it.second + 127) / 128)), 128, 0, s>>>(
+                it.first, it.second, n, T.left, T.right, T.cnt, T.nbox, sah_cost, sah_choice);
+    }
     // Every 4-wide node stands for a distinct binary node of more than
     // kLeafMax triangles (or the root): that count bounds the node array.
     WF_TRY(B.alloc(&keep, (size_t)n));
@@ -1363,8 +1374,12 @@ int build_ploc4(const BvhBuildInput& in, BvhBuildOutput& out, int num_sms, cudaS
             goto fail;
         }
         const int g = std::max(1, std::min(grid, (count + 127) / 128));
-        k_wide_gather<4, kLeafMax><<<g, 128, 0, s>>>(items, count, n, T.left, T.right, T.cnt, T.nbox, kids, n_int,
-                                                      n_tri);
+        if (n > 1)
+            k_wide_gather_sah<4, kLeafMax><<<g, 128, 0, s>>>(items, count, n, T.left, T.right, T.cnt, sah_choice, kids,
+                                                             n_int, n_tri);
+        else
+            k_wide_gather<4, kLeafMax><<<g, 128, 0, s>>>(items, count, n, T.left, T.right, T.cnt, T.nbox, kids, n_int,
+                                                          n_tri);
         exclusive_scan_i32(n_int, count, int_off, T.block_sums, T.d_total, s);
         int next = 0;
         WF_TRY(cudaMemcpyAsync(&next, T.d_total, sizeof(int), cudaMemcpyDeviceToHost, s));

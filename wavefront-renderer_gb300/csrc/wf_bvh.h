@@ -45,8 +45,8 @@ int build_ploc_wide(const BvhBuildInput& in, BvhBuildOutput& out, int num_sms, c
                     std::string& err);
 
 // PLOC tree collapsed top-down into 4-wide nodes (Bvh4Node), level by
-// level: each node opens the binary subtree greedily (largest surface area
-// first) up to four children; subtrees of <= kLeafMax triangles stay leaves
+// level, with the SAH-optimal choice of each node's (up to four) children
+// (the 8-wide build's dynamic programming); subtrees of <= kLeafMax triangles stay leaves
 // over the same triangle order as build_ploc.  out.nodes4 / out.num_nodes /
 // out.max_depth (levels).
 int build_ploc4(const BvhBuildInput& in, BvhBuildOutput& out, int num_sms, cudaStream_t s, std::string& err);

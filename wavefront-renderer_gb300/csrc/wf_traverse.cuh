@@ -305,10 +305,15 @@ struct Traversal4 : Traversal<kAnyHit> {
         const uint32_t s = key & 3u;
         return (uint32_t)(s == 0u ? k.x : s == 1u ? k.y : s == 2u ? k.z : k.w);
     }
+    // The binary traversal's stack discipline: entry sp-1 lives in `top`, so
+    // a pop hands the next node over at once and reloads the register from
+    // memory for the pop after it.
     template <class Stk>
     __device__ __forceinline__ void push(Stk stack, uint32_t e)
     {
-        stack[this->sp++] = e;
+        stack[this->sp - 1] = this->top;
+        this->top = e;
+        ++this->sp;
     }
 
     template <class Stk>
@@ -330,7 +335,7 @@ struct Traversal4 : Traversal<kAnyHit> {
             sort2(k1, k3);
             sort2(k1, k2);
             if (k0 == 0xFFFFFFFFu) {
-                this->cur = stack[--this->sp];
+                this->cur = this->pop(stack);
                 continue;
             }
             this->cur = kid_of(k, k0);
@@ -345,7 +350,7 @@ struct Traversal4 : Traversal<kAnyHit> {
         }
         while (this->cur != kSentinel && (this->cur & kLeafFlag)) {
             const uint32_t leaf = this->cur;
-            this->cur = stack[--this->sp];
+            this->cur = this->pop(stack);
             if (this->test_leaf(tris, leaf)) {
                 this->cur = kSentinel;
                 return;
