@@ -30,8 +30,16 @@ pytestmark = pytest.mark.gpu
 HIT_FIELDS = ("prim_id", "material_id", "texture_id", "distance", "point_x", "point_y", "point_z", "normal_x",
               "normal_y", "normal_z", "front_face", "u", "v")
 
-WORKLOAD = {1: dict(size=1024, spp=64, depth=12, windows=[(256, 384), (480, 560)]),
-            2: dict(size=2048, spp=32, depth=8, windows=[(960, 1536), (1024, 1200)])}
+# The lattice's estimator is heavy-tailed: sky misses that find the HDRI's
+# sun lobe (1e4 times the sky, unclamped as in the reference's miss loop) are
+# rare and huge, so its block z-scores have a heavier tail and spread than a
+# normal's even when nothing is biased.  Measured on the port (pinned to the
+# reference) over 13 seeds of this window at 32 spp (12 on an x86 host, seed
+# 4242 on the GPU host): |z| > 3 on 0.9-3.3% of blocks, winsorized z spread
+# 0.86-1.12; the band for it allows 5% and +-0.2.
+WORKLOAD = {1: dict(size=1024, spp=64, depth=12, windows=[(256, 384), (480, 560)], band={}),
+            2: dict(size=2048, spp=32, depth=8, windows=[(960, 1536), (1024, 1200)],
+                    band=dict(tail_max=0.05, std_tol=0.2))}
 
 
 @pytest.fixture(scope="module")
@@ -93,11 +101,11 @@ def test_gpu_workload_render_matches_reference_and_port(wf, orc, ctx, scenes, co
                                          "channel_rel": (got.mean((0, 1)) / ref.mean((0, 1)) - 1).tolist()}
     band, band_error = None, None
     try:
-        band = fp64_band(img[y0:y0 + ch, x0:x0 + cw], spp, g)
+        band = fp64_band(img[y0:y0 + ch, x0:x0 + cw], spp, g, **w["band"])
     except AssertionError as e:
         band_error = str(e)
     try:
-        port_band = fp64_band(port_window, spp, g)
+        port_band = fp64_band(port_window, spp, g, **w["band"])
     except AssertionError as e:
         port_band = {"failed": str(e)}
     report(f"render_config{config}", image=f"{W}x{H}x{spp}spp depth {w['depth']}", fp64_window=band or band_error,
