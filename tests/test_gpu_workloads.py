@@ -69,12 +69,16 @@ def test_gpu_workload_hits_match_reference_fixture(wf, ctx, scenes, config):
     assert np.array_equal(occ, z["occluded"])
 
 
-@pytest.mark.parametrize("config", [1, 2])
-def test_gpu_workload_render_matches_reference_and_port(wf, orc, ctx, scenes, config):
-    """The benchmarked render: its paths equal to the port's on the fixture
-    window and a second window (the port renders the same pixels with the same
-    random streams), and its fixture window inside the band of the reference's
-    FP64 mean.  Every figure is reported before anything is asserted."""
+@pytest.mark.parametrize("config,policy", [(1, "none"), (1, "material"), (2, "none"), (2, "material"),
+                                           (2, "texture"), (2, "costBenefit")])
+def test_gpu_workload_render_matches_reference_and_port(wf, orc, ctx, scenes, config, policy):
+    """The benchmarked render, under each scheduling policy its workload
+    compares (dense mesh: none and material; lattice: all four): its paths
+    equal to the port's on the fixture window and a second window (the port
+    renders the same pixels with the same random streams; a policy only
+    reorders the work), and its fixture window inside the band of the
+    reference's FP64 mean.  Every figure is reported before anything is
+    asserted."""
     w = WORKLOAD[config]
     g = np.load(GOLDEN / f"c{config}_fp64_crop.npz")
     assert int(g["max_depth"]) == w["depth"] and int(g["image_size"][0]) == w["size"]
@@ -82,7 +86,7 @@ def test_gpu_workload_render_matches_reference_and_port(wf, orc, ctx, scenes, co
     ctx.upload(sc.desc)
     W = H = w["size"]
     spp = w["spp"]
-    p = wf.render_params(W, H, spp, w["depth"], sc.camera(W, H), seed=4242)
+    p = wf.render_params(W, H, spp, w["depth"], sc.camera(W, H), seed=4242, policy=wf.POLICIES[policy])
     img, st = ctx.render(p)
     assert np.isfinite(img).all()
     x0, y0, cw, ch = (int(v) for v in g["window"])
@@ -108,7 +112,7 @@ def test_gpu_workload_render_matches_reference_and_port(wf, orc, ctx, scenes, co
         port_band = fp64_band(port_window, spp, g, **w["band"])
     except AssertionError as e:
         port_band = {"failed": str(e)}
-    report(f"render_config{config}", image=f"{W}x{H}x{spp}spp depth {w['depth']}", fp64_window=band or band_error,
+    report(f"render_config{config}_{policy}", image=f"{W}x{H}x{spp}spp depth {w['depth']}", fp64_window=band or band_error,
            port_same_seed_fp64_window=port_band, port_windows=paths, closest_rays=st["closest_rays"],
            shadow_rays=st["shadow_rays"])
     for k, v in paths.items():
