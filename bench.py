@@ -389,7 +389,8 @@ def serving_block(pkg, ctx, duration: float, rate: float, budget_gb: float, drai
     Jobs on the config-0 scene are 256 x 256 at depth 8, so each has an FP64
     oracle (the reference's 16384-spp mean); their final images give a
     per-job MSE.  Other jobs: resolution log-uniform in [128^2, 1024^2],
-    spp from {8, 32, 128}, depth 4-12."""
+    spp from {8, 32, 128}, depth 4-12.  Beside it, the plain loop on the same
+    stream: its first jobs rendered one per call."""
     rng = np.random.default_rng(4242)
     scenes = []
     for cfg in (0, 1):
@@ -452,6 +453,25 @@ def serving_block(pkg, ctx, duration: float, rate: float, budget_gb: float, drai
                 exp = float((g["sigma"].astype(np.float64) ** 2 * (1.0 / spp + 1.0 / float(g["spp"]))).mean())
                 mses.append((mse / exp, spp))
     srv.close()
+    # the plain loop on the same stream: the first arrivals rendered one job per
+    # call in the fastest single-job form (bounces back to back with
+    # device-side counts), up to ~1.5 G paths
+    ctx.set_tuning(max(trace_variant, 0), graph_mode=2)
+    plain_jobs, plain_paths = [], 0
+    for _, _, job in arrivals:
+        if plain_paths > 1.5e9 or len(plain_jobs) >= 256:
+            break
+        plain_jobs.append(job)
+        plain_paths += job.width * job.height * job.samples_per_pixel
+    ctx.render_batch(plain_jobs[:2], want_images=False)  # warm-up
+    ctx.timer_begin()
+    plain_rays = 0
+    for job in plain_jobs:
+        _, pst = ctx.render_batch([job], want_images=False)
+        plain_rays += pst["closest_rays"] + pst["shadow_rays"]
+    plain_ms = ctx.timer_end()
+    ctx.set_tuning(max(trace_variant, 0))
+    plain = plain_rays / plain_ms / 1e3
     ratio = [m for m, _ in mses]
     return {
         "workload": "c4_serving_poisson", "rate_per_s": rate, "duration_s": duration, "drain_s": drain,
@@ -459,6 +479,9 @@ def serving_block(pkg, ctx, duration: float, rate: float, budget_gb: float, drai
         "scenes": "config 0 (jobs 256^2, depth 8), config 1 (1.31 M tris), 16 config-3 variants",
         "value": rays / wall / 1e6, "unit": "Mrays/s", "wall_s": wall,
         "device_busy_mrays_per_s": rays / (dev_ms / 1e3) / 1e6 if dev_ms else None,
+        "plain_loop": {"value": plain, "unit": "Mrays/s", "jobs": len(plain_jobs), "paths": plain_paths,
+                       "form": "the stream's first jobs one per call, bounces back to back with device-side counts"},
+        "speedup_vs_plain_loop": (rays / wall / 1e6) / plain if plain > 0 else None,
         "submitted": len(ids), "completed": len(done_ttc),
         "with_first_frame": sum(1 for s in st if s["t_first_frame"] >= 0),
         "rejected": sum(1 for s in st if s["state"] == pkg.JOB_REJECTED),
