@@ -276,7 +276,11 @@ int wf_scene_get_info(wf_ctx* ctx, wf_scene_info* out_info);
 /* Launch tuning of a context (the autotuner's knobs).  trace_variant: 0 = no
  * occupancy hint on the traversal kernels (the closest-hit kernel of a
  * single-job render whose binary tree and triangles exceed L2 runs as 1),
- * 1 = 9 blocks of 128 threads per SM (56 registers, no spills).
+ * 1 = 9 blocks of 128 threads per SM (56 registers, no spills), 2 = the
+ * traversal stack's bottom 6 entries in shared memory and the rest in local
+ * memory (stack placement; binary trees, 3 KB per block), 3 = the binary
+ * tree's top 31 nodes staged in shared memory once per block (node staging;
+ * single-scene renders, else 0).  Variants 2 and 3 run 8 blocks per SM.
  * persistent_blocks_per_sm: resident blocks launched per
  * SM by the persistent traversal kernels (0 = 16).  graph_mode: whether a
  * wave's bounce chain is captured once as a CUDA graph and replayed. */
@@ -315,8 +319,8 @@ int wf_get_tuning(const wf_ctx* ctx, wf_tuning* out_tuning);
 
 /* Autotuner (no reference counterpart): renders one wave of `params` on the
  * current scene (samples capped at one wave, adaptive sampling and cost
- * tracking off) under every combination of trace_variant {0, 1}
- * (block occupancy), persistent_blocks_per_sm
+ * tracking off) under every combination of trace_variant {0, 1, 2, 3}
+ * (block occupancy, stack placement, node staging), persistent_blocks_per_sm
  * {4, 8, 12, 16, 24}, graph_mode {2, 1} and speculative_traversal {0, 1}, each
  * once untimed and twice
  * timed on the device; then, when params sort rays or shading, the

@@ -35,9 +35,16 @@ def _same(a, b):
     return np.isclose(a, b, rtol=1e-4, atol=1e-6).all(axis=2).mean()
 
 
-def test_batch_job_equals_job_alone(wf, ctx):
-    jobs, hosts = _jobs(wf, ctx, 12)
-    imgs, st = ctx.render_batch(jobs)
+@pytest.mark.parametrize("variant", [0, 2])
+def test_batch_job_equals_job_alone(wf, ctx, variant):
+    """Variant 2 runs the multi-job traversal with its stack's bottom entries
+    in shared memory."""
+    ctx.set_tuning(trace_variant=variant)
+    try:
+        jobs, hosts = _jobs(wf, ctx, 12)
+        imgs, st = ctx.render_batch(jobs)
+    finally:
+        ctx.set_tuning()
     assert st["closest_rays"] > 0 and st["waves"] >= 1
     for j, hs, img in zip(jobs, hosts, imgs):
         ctx.upload(hs.desc)  # slot 0: the single-scene path

@@ -295,13 +295,15 @@ def test_render_is_order_independent(wf, ctx, scene_small, scene_c2small, which)
         img, _ = ctx.render(wf.render_params(W, H, 8, 12, cam, seed=5, **kw))
         agree = np.isclose(img, base, rtol=1e-4, atol=1e-6).all(axis=2).mean()
         assert agree >= 0.999, (kw, agree)
-    # launch tuning: occupancy variant, speculative traversal, grid size,
-    # graph replay and the sort-or-skip threshold change no pixel beyond that.
+    # launch tuning: occupancy variant, stack placement in shared memory, top
+    # nodes staged in shared memory, speculative traversal, grid size, graph
+    # replay and the sort-or-skip threshold change no pixel beyond that.
     # The base render issues its bounces back to back with device-side counts;
     # a sort-or-skip threshold sends policy none through the loop that waits
     # for each bounce's counts on the host, graph_mode=1 through graph replay.
     try:
-        for tune, kw in [(dict(trace_variant=1), {}), (dict(speculative_traversal=1), {}),
+        for tune, kw in [(dict(trace_variant=1), {}), (dict(trace_variant=2), {}), (dict(trace_variant=3), {}),
+                         (dict(trace_variant=2, speculative_traversal=1), {}), (dict(speculative_traversal=1), {}),
                          (dict(ray_sort_bits=16), dict(ray_sort=True)),
                          (dict(persistent_blocks_per_sm=4), {}), (dict(graph_mode=1), {}),
                          (dict(sort_min_queue=6000), dict(policy=1, ray_sort=True)),
@@ -347,7 +349,7 @@ def test_autotune_picks_a_valid_tuning(wf, ctx, scene_small):
     try:
         tuning, ms = ctx.autotune(p)
         assert ms > 0
-        assert tuning["trace_variant"] in (0, 1) and tuning["persistent_blocks_per_sm"] in (4, 8, 12, 16, 24)
+        assert tuning["trace_variant"] in (0, 1, 2, 3) and tuning["persistent_blocks_per_sm"] in (4, 8, 12, 16, 24)
         assert tuning["sort_min_queue"] in (0, 1 << 18, 1 << 20, 1 << 22, 2**31 - 1)
         assert ctx.get_tuning() == tuning
         img, _ = ctx.render(p)

@@ -1204,7 +1204,7 @@ int wf_get_stream(wf_ctx* c, void** out)
 int wf_set_tuning(wf_ctx* c, const wf_tuning* t)
 {
     if (!c || !t) return WF_ERR_INVALID_ARGUMENT;
-    if (t->trace_variant < 0 || t->trace_variant > 1 || t->persistent_blocks_per_sm < 0 ||
+    if (t->trace_variant < 0 || t->trace_variant > 3 || t->persistent_blocks_per_sm < 0 ||
         t->persistent_blocks_per_sm > 32 || t->bvh_builder < 0 || t->bvh_builder > 3)
         return set_err(c, WF_ERR_INVALID_ARGUMENT, "tuning out of range");
     c->tuning = *t;

@@ -47,29 +47,75 @@ __device__ __forceinline__ void slab2(const BvhNode& nd, V3 inv, V3 oi, float tm
     h1 = tn1 <= tf1;
 }
 
+// Two float4 in one 32-byte read-only load (sm_100 and later); p must be
+// 32-byte aligned.
+__device__ __forceinline__ void ldg_v8(const float4* p, float4& a, float4& b)
+{
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+        : "l"(p));
+}
+
+// A node in two 32-byte loads: the tree starts its allocation (aligned to 256
+// bytes) and nodes are 64 bytes.
 __device__ __forceinline__ BvhNode load_node(const BvhNode* nodes, uint32_t i)
 {
     const float4* p = reinterpret_cast<const float4*>(nodes + i);
     BvhNode nd;
-    nd.c0xy = __ldg(p + 0);
-    nd.c1xy = __ldg(p + 1);
-    nd.cz = __ldg(p + 2);
-    float4 k = __ldg(p + 3);
+    float4 k;
+    ldg_v8(p, nd.c0xy, nd.c1xy);
+    ldg_v8(p + 2, nd.cz, k);
     nd.kids = make_int4(__float_as_int(k.x), __float_as_int(k.y), 0, 0);
     return nd;
 }
 
 constexpr uint32_t kSentinel = 0xFFFFFFFFu;
 
+// Traversal-stack placement in shared memory (the binary traversal's
+// stack-placement choice, wf_tuning::trace_variant 2): entries
+// [0, kSharedStack) of thread t live in shared memory at sh[i * 128] (one
+// 128-thread block; the lanes of a warp hit 32 distinct banks), deeper
+// entries in the thread's local array.  Six entries are 3 KB per block, which
+// eight resident blocks fit into the shared-memory share the driver already
+// sets aside for kernels that declare none.
+constexpr int kSharedStack = 6;
+struct SplitStack {
+    uint32_t* sh;   // shared array + threadIdx.x
+    uint32_t* loc;  // local array of kStackSize entries (the first kSharedStack unused)
+    struct Ref {
+        const SplitStack& s;
+        int i;
+        __device__ __forceinline__ operator uint32_t() const { return i < kSharedStack ? s.sh[i * 128] : s.loc[i]; }
+        __device__ __forceinline__ Ref& operator=(uint32_t v)
+        {
+            if (i < kSharedStack)
+                s.sh[i * 128] = v;
+            else
+                s.loc[i] = v;
+            return *this;
+        }
+    };
+    __device__ __forceinline__ Ref operator[](int i) const { return Ref{*this, i}; }
+};
+
+// Top-of-tree staging (wf_tuning::trace_variant 3): the first kTopNodes
+// nodes of a binary tree — numbered in reverse creation order, so the root
+// and the last clustering passes' nodes — are copied into shared memory once
+// per block and read from there (31 x 64 B per block).
+constexpr int kTopNodes = 31;
+
 // Resumable while-while traversal (Aila & Laine, "Understanding the
 // efficiency of ray traversal on GPUs", HPG 2009).  One call of round() walks
 // interior nodes down to a leaf, then leaves until it pops an interior node or
 // the stack's sentinel, so the lanes of a warp reconverge after every round
 // and a persistent kernel can hand a finished lane a new ray between rounds.
-template <bool kAnyHit, bool kFarFirst = false>
+template <bool kAnyHit, bool kFarFirst = false, bool kStagedTop = false>
 struct Traversal {
     using Entry = uint32_t;
     static constexpr int kStack = kStackSize;
+    static constexpr bool kStaged = kStagedTop;
+    const BvhNode* staged = nullptr;  // kStagedTop: nodes [0, num_staged) in shared memory
+    uint32_t num_staged = 0;
     V3 o, d, inv, oi;
     float tmin, best_t;
     int best_g;
@@ -101,6 +147,14 @@ struct Traversal {
     }
     __device__ __forceinline__ bool done() const { return cur == kSentinel; }
     __device__ __forceinline__ void idle() { cur = kSentinel; }
+
+    __device__ __forceinline__ BvhNode fetch(const BvhNode* nodes, uint32_t i) const
+    {
+        if constexpr (kStagedTop) {
+            if (i < num_staged) return staged[i];
+        }
+        return load_node(nodes, i);
+    }
 
     // Binary-traversal stack with its top entry in a register: entries
     // 0 .. sp-2 are in memory, entry sp-1 is `top`.  A pop returns the
@@ -142,7 +196,7 @@ struct Traversal {
             // leaves until an interior node or the sentinel comes off the
             // stack.
             while (!(cur & kLeafFlag)) {
-                const BvhNode nd = load_node(nodes, cur);
+                const BvhNode nd = fetch(nodes, cur);
                 float tn0, tn1;
                 bool h0, h1;
                 slab2(nd, inv, oi, tmin, best_t, tn0, tn1, h0, h1);
@@ -176,7 +230,7 @@ struct Traversal {
         uint32_t postponed = 0u;  // leaf words always carry kLeafFlag, so 0 = none
         for (;;) {
             if (cur != kSentinel && !(cur & kLeafFlag)) {
-                const BvhNode nd = load_node(nodes, cur);
+                const BvhNode nd = fetch(nodes, cur);
                 float tn0, tn1;
                 bool h0, h1;
                 slab2(nd, inv, oi, tmin, best_t, tn0, tn1, h0, h1);
