@@ -683,16 +683,25 @@ int wf_render_batch(wf_ctx* ctx, const wf_job* jobs, int32_t njobs, float* const
 
 /* ---- serving loop ------------------------------------------------------------- */
 
-/* A render service on one context: jobs are admitted while their
- * accumulators fit the HBM budget (beside the fixed wave buffers), every step
- * runs one wave over the admitted jobs (up to frame_spp samples of each), a
- * job's progressive frame is ready every frame_spp samples.  Times are
- * seconds on the server's monotonic clock.  No counterpart in the reference
+/* A render service on one context.  Jobs are admitted in arrival order while
+ * their pixel sums fit the HBM budget.  The server owns a streaming wave: a
+ * ray queue of max_paths_per_wave paths that every step advances by 8 bounce
+ * iterations, replacing the paths that ended by camera rays of the next
+ * frames (frame_spp samples of every pixel of one job, appended round robin
+ * over the running jobs, first frames ahead of the others).  A frame's sums
+ * join its job's once every one of its paths has ended (max_depth iterations
+ * after its last one started), so a progressive image is always the average
+ * of whole frames.  Budget = the queue (276 B per path) + the jobs' sums + a
+ * share for frame sums (an eighth of the rest, at least 6 floats per queued
+ * path).  The queue keeps paths between steps: the server's buffers are its
+ * own, apart from the context's.  Times are seconds on the server's monotonic
+ * clock.  No counterpart in the reference
  * (it renders one image per process; its GUI polls a preview file). */
 typedef struct wf_server wf_server;
 typedef struct wf_server_config {
-    int64_t hbm_budget_bytes;   /* accumulators + wave buffers              */
-    int64_t max_paths_per_wave; /* 0 = 2^23 (or the context's, if smaller)  */
+    int64_t hbm_budget_bytes;   /* queue + job sums + frame sums            */
+    int64_t max_paths_per_wave; /* queue capacity; 0 = 2^24 (or the
+                                   context's wave size, if smaller)         */
     int32_t frame_spp;          /* samples per progressive frame (8)        */
     int32_t reserved[7];
 } wf_server_config;
@@ -717,10 +726,10 @@ typedef struct wf_server_step_info {
     int32_t queued;
     int32_t running;
     int32_t completed_this_step;
-    int32_t jobs_in_wave;
-    int64_t paths_in_wave;
+    int32_t jobs_in_wave;       /* jobs with frames still running           */
+    int64_t paths_in_wave;      /* paths started in this step               */
     uint64_t rays_traced;       /* closest + shadow rays of this step       */
-    double step_ms;             /* device time of the wave                  */
+    double step_ms;             /* device time of the step's iterations     */
     int64_t budget_used_bytes;
 } wf_server_step_info;
 int wf_server_create(wf_ctx* ctx, const wf_server_config* config, wf_server** out_server);

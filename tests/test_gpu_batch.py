@@ -112,8 +112,10 @@ def test_server_admission_respects_budget(wf, ctx):
     for j in jobs:
         j.width, j.height, j.samples_per_pixel = 64, 64, 8
     wave = 1 << 14
-    per_path = 2 * 14 * 4 + 2 * 5 * 4 + 3 * 12 * 4 + 2 * 12 + 8 * 4
-    budget = wave * per_path + 2 * 64 * 64 * 3 * 4  # room for two accumulators
+    # the streaming queue (two RayQueues, a hit queue, the shadow queue), then
+    # the sums: two jobs' and the frame share (6 floats per queued path here)
+    per_path = 2 * 14 * 4 + 5 * 4 + 3 * 12 * 4
+    budget = wave * per_path + 4 * (2 * 64 * 64 * 3 + 6 * wave)
     srv = wf.Server(ctx, hbm_budget_bytes=budget, frame_spp=8, max_paths_per_wave=wave)
     ids = [srv.submit(j) for j in jobs]
     big = wf.make_job(jobs[0].scene_id, 512, 512, 4, 8, jobs[0].camera)
@@ -129,6 +131,40 @@ def test_server_admission_respects_budget(wf, ctx):
     assert max_running <= 2
     assert all(srv.status(i)["state"] == wf.JOB_DONE for i in ids)
     srv.close()
+
+
+def test_server_streams_frames_larger_than_its_queue(wf, ctx, scene_small):
+    """A job whose frames hold more paths than the streaming queue (64 x 64
+    x 4 spp = 16384 paths through a queue of 4096): paths that end are
+    replaced by new camera rays bounce by bounce.  Every progressive image is
+    the job's first k frames exactly (equal to a render of its first
+    k * frame_spp samples, same random streams), and the final image equals
+    the job rendered alone."""
+    sid = ctx.add_scene(scene_small.desc)
+    cam = scene_small.camera(64, 64)
+    job = wf.make_job(sid, 64, 64, 16, 8, cam, seed=77)
+    srv = wf.Server(ctx, hbm_budget_bytes=64 << 20, frame_spp=4, max_paths_per_wave=4096)
+    jid = srv.submit(job)
+    seen = {}
+    for _ in range(400):
+        info = srv.step()
+        assert info["paths_in_wave"] <= 8 * 4096
+        st = srv.status(jid)
+        if st["state"] == wf.JOB_RUNNING and st["samples_done"] > 0 and st["samples_done"] not in seen:
+            seen[st["samples_done"]] = srv.image(jid, 64, 64).copy()
+        if st["state"] == wf.JOB_DONE:
+            break
+    st = srv.status(jid)
+    assert st["state"] == wf.JOB_DONE and st["frames"] == 4
+    assert seen, "no progressive frame observed"
+    final = srv.image(jid, 64, 64)
+    srv.close()
+    ctx.upload(scene_small.desc)
+    for spp, img in seen.items():
+        ref, _ = ctx.render(wf.render_params(64, 64, spp, 8, cam, seed=77))
+        assert _same(img, ref) >= 0.999, spp
+    alone, _ = ctx.render(wf.render_params(64, 64, 16, 8, cam, seed=77))
+    assert _same(final, alone) >= 0.999
 
 
 def test_server_cancel(wf, ctx):

@@ -249,8 +249,10 @@ def camera_make(look_from, look_at, up, vfov, width, height) -> WfCamera:
 
 
 class Server:
-    """The serving loop (wf_server_*): admission by HBM budget, one shared
-    wave per step, progressive frames every frame_spp samples."""
+    """The serving loop (wf_server_*): admission by HBM budget, a streaming
+    wave (a fixed-capacity ray queue refilled with new camera rays as paths
+    end, 8 bounce iterations per step), progressive frames every frame_spp
+    samples."""
 
     def __init__(self, ctx: "Context", hbm_budget_bytes: int, frame_spp: int = 8, max_paths_per_wave: int = 0):
         self.ctx = ctx

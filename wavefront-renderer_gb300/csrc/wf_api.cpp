@@ -43,6 +43,8 @@ LaunchCfg persist_cfg(const wf_ctx* c)
     cfg.variant = c->tuning.trace_variant;
     cfg.speculative = c->tuning.speculative_traversal;
     cfg.l2_bytes = c->l2_bytes;
+    for (const auto& r : c->scenes)
+        if (r.live) cfg.max_scene_bytes = std::max<int64_t>(cfg.max_scene_bytes, (int64_t)r.tree_bytes);
     cfg.shade_grid = c->num_sms * c->shade_per_sm;
     cfg.shade_grid_other = c->num_sms * c->shade_per_sm_other;
     return cfg;

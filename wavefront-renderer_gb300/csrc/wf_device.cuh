@@ -270,6 +270,20 @@ struct WaveChunk {
     int64_t path_offset;
 };
 
+// A streaming wave (path regeneration): the queue keeps a fixed capacity and,
+// after every bounce, the paths that ended are replaced by new camera rays
+// taken in order from an append-only list of chunks (absolute path offsets).
+// The host appends chunks (total, nchunks); the device advances the cursor.
+struct StreamState {
+    int64_t cursor;        // paths generated so far
+    int64_t total;         // paths appended to the chunk list
+    int64_t refill_first;  // this bounce's refill: first path,
+    int64_t refill_base;   //   queue position of its first ray,
+    int64_t refill_count;  //   and number of rays
+    int32_t nchunks;       // chunks in the device list (the first may be partly generated)
+    int32_t pad;
+};
+
 // ---------------------------------------------------------------------------
 // Small vector helpers (reference include/math/Vec3.h semantics).
 // ---------------------------------------------------------------------------

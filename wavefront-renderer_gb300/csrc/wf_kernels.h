@@ -25,6 +25,7 @@ struct LaunchCfg {
     int block;
     int variant = 0;   // kernel variant (traversal occupancy hint / stack placement)
     int64_t l2_bytes = 0;  // the device's L2 size (variant 0 of a larger scene runs at 9 blocks per SM)
+    int64_t max_scene_bytes = 0;  // largest resident tree + triangles (variant 0 of multi-job waves)
     int speculative = 0;  // 1 = speculative while-while traversal
     int ray_order = 0;    // 1 = hit records at their rays' indices, listed by k_compact_hits
     int shade_grid = 0;        // k_shade's grid (one full wave of resident blocks); 0 = grid
@@ -86,6 +87,16 @@ void launch_occluded_render(const WaveTables& t, ShadowQueueDev sh, const ull* s
 // shadow rays, (rays > 0) of the bounce just run; the next bounce's ray
 // count into counters[0]; counters[1..5] zeroed.
 void launch_bounce_end(ull* counters, ull* tally, cudaStream_t s);
+
+// Streaming waves: after a bounce's shading, plan the refill (one thread:
+// new rays = min(capacity - next rays, paths left), cursor advanced,
+// counters[3] raised by them, log[iter] = the cursor after it), then write
+// those camera rays into the next queue behind the surviving rays.
+void launch_stream_plan(ull* counters, StreamState* st, int64_t capacity, int64_t* log, int iter, cudaStream_t s);
+void launch_camera_refill(const WaveChunk* chunks, const StreamState* st, const DeviceJob* jobs, RayQueueDev rq,
+                          LaunchCfg cfg, cudaStream_t s);
+// dst[i] += src[i] (a finished frame's sums into its job's sums).
+void launch_add_floats(float* dst, const float* src, int64_t n, cudaStream_t s);
 
 // RayQueue::sortKey over the queue (each ray's scene bounds), (key, index)
 // pairs for the radix sort.

@@ -90,55 +90,97 @@ __device__ __forceinline__ int tile_pixel(int q, int W, int H)
     return y * W + x;
 }
 
+// The camera ray of path g of a chunk list (chunks ordered by path_offset,
+// g >= chunks[0].path_offset), written at queue position q.
+__device__ __forceinline__ void camera_path(const WaveChunk* __restrict__ chunks, int nchunks,
+                                            const DeviceJob* __restrict__ jobs, int64_t g, int64_t q,
+                                            const RayQueueDev& rq)
+{
+    int lo = 0, hi = nchunks - 1;  // last chunk with path_offset <= g
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (chunks[mid].path_offset <= g) lo = mid; else hi = mid - 1;
+    }
+    const WaveChunk ch = chunks[lo];
+    const DeviceJob& J = jobs[ch.job];
+    const int64_t local = g - ch.path_offset;
+    const int64_t pi = local / ch.nspp;
+    const int s = (int)(local - pi * ch.nspp);
+    int p = (int)pi;
+    if (ch.active_count > 0)
+        p = J.active[p];  // generatePrimaryRays' activePixels mask
+    else
+        p = tile_pixel(p, J.width, J.height);
+    const int x = p % J.width, y = p / J.width;
+    const int sample = ch.first_sample + s;
+    const wf_camera& cam = J.camera;
+    const V3 org = {cam.origin[0], cam.origin[1], cam.origin[2]};
+    const V3 tl = {cam.top_left[0], cam.top_left[1], cam.top_left[2]};
+    const V3 hz = {cam.horizontal[0], cam.horizontal[1], cam.horizontal[2]};
+    const V3 vt = {cam.vertical[0], cam.vertical[1], cam.vertical[2]};
+    Stream rng(J.seed_lo, J.seed_hi, kPurposeCamera, 0, (uint32_t)p, (uint32_t)sample);
+    float u = ((float)x + rng.next()) / (float)(J.width - 1);
+    float v = 1.0f - ((float)y + rng.next()) / (float)(J.height - 1);
+    V3 d = normalized(tl + hz * u + vt * v - org);
+    stq(&rq.ox[q], org.x);
+    stq(&rq.oy[q], org.y);
+    stq(&rq.oz[q], org.z);
+    stq(&rq.dx[q], d.x);
+    stq(&rq.dy[q], d.y);
+    stq(&rq.dz[q], d.z);
+    stq(&rq.tr[q], 1.0f);
+    stq(&rq.tg[q], 1.0f);
+    stq(&rq.tb[q], 1.0f);
+    stq(&rq.pdf[q], -1.0f);
+    stq(&rq.pixel[q], p);
+    stq(&rq.depth[q], 0);
+    stq(&rq.sample[q], sample);
+    stq(&rq.job[q], ch.job);
+}
+
 __global__ void k_camera_chunks(const WaveChunk* __restrict__ chunks, const long long* __restrict__ header,
                                 const DeviceJob* __restrict__ jobs, RayQueueDev rq)
 {
     const int64_t total = header[0];
     const int nchunks = (int)header[1];
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
-         i += (int64_t)gridDim.x * blockDim.x) {
-        int lo = 0, hi = nchunks - 1;  // last chunk with path_offset <= i
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (chunks[mid].path_offset <= i) lo = mid; else hi = mid - 1;
-        }
-        const WaveChunk ch = chunks[lo];
-        const DeviceJob& J = jobs[ch.job];
-        const int64_t np = ch.active_count > 0 ? ch.active_count : (int64_t)J.width * J.height;
-        const int64_t local = i - ch.path_offset;
-        const int64_t pi = local / ch.nspp;
-        const int s = (int)(local - pi * ch.nspp);
-        int p = (int)pi;
-        if (ch.active_count > 0)
-            p = J.active[p];  // generatePrimaryRays' activePixels mask
-        else
-            p = tile_pixel(p, J.width, J.height);
-        const int x = p % J.width, y = p / J.width;
-        const int sample = ch.first_sample + s;
-        const wf_camera& cam = J.camera;
-        const V3 org = {cam.origin[0], cam.origin[1], cam.origin[2]};
-        const V3 tl = {cam.top_left[0], cam.top_left[1], cam.top_left[2]};
-        const V3 hz = {cam.horizontal[0], cam.horizontal[1], cam.horizontal[2]};
-        const V3 vt = {cam.vertical[0], cam.vertical[1], cam.vertical[2]};
-        Stream rng(J.seed_lo, J.seed_hi, kPurposeCamera, 0, (uint32_t)p, (uint32_t)sample);
-        float u = ((float)x + rng.next()) / (float)(J.width - 1);
-        float v = 1.0f - ((float)y + rng.next()) / (float)(J.height - 1);
-        V3 d = normalized(tl + hz * u + vt * v - org);
-        stq(&rq.ox[i], org.x);
-        stq(&rq.oy[i], org.y);
-        stq(&rq.oz[i], org.z);
-        stq(&rq.dx[i], d.x);
-        stq(&rq.dy[i], d.y);
-        stq(&rq.dz[i], d.z);
-        stq(&rq.tr[i], 1.0f);
-        stq(&rq.tg[i], 1.0f);
-        stq(&rq.tb[i], 1.0f);
-        stq(&rq.pdf[i], -1.0f);
-        stq(&rq.pixel[i], p);
-        stq(&rq.depth[i], 0);
-        stq(&rq.sample[i], sample);
-        stq(&rq.job[i], ch.job);
-    }
+         i += (int64_t)gridDim.x * blockDim.x)
+        camera_path(chunks, nchunks, jobs, i, i, rq);
+}
+
+// Streaming waves (path regeneration): one thread plans the refill of the
+// next queue after a bounce's shading.  Every live path advances one bounce
+// per iteration, so paths generated here are finished (depth limit) after
+// max_depth more iterations; the cursor log lets the host tell when.
+__global__ void k_stream_plan(ull* __restrict__ counters, StreamState* __restrict__ st, int64_t capacity,
+                              int64_t* __restrict__ log, int iter)
+{
+    const int64_t live = (int64_t)counters[3];
+    int64_t k = capacity - live;
+    const int64_t left = st->total - st->cursor;
+    if (k > left) k = left;
+    if (k < 0) k = 0;
+    st->refill_first = st->cursor;
+    st->refill_base = live;
+    st->refill_count = k;
+    st->cursor += k;
+    counters[3] = (ull)(live + k);
+    log[iter] = st->cursor;
+}
+
+__global__ void k_camera_refill(const WaveChunk* __restrict__ chunks, const StreamState* __restrict__ st,
+                                const DeviceJob* __restrict__ jobs, RayQueueDev rq)
+{
+    const int64_t n = st->refill_count, first = st->refill_first, base = st->refill_base;
+    const int nchunks = st->nchunks;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        camera_path(chunks, nchunks, jobs, first + i, base + i, rq);
+}
+
+__global__ void k_add_floats(float* __restrict__ dst, const float* __restrict__ src, int64_t n)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        dst[i] += src[i];
 }
 
 // End of a bounce in a device-counted chain (no host round trip, or a
@@ -1494,6 +1536,21 @@ static bool misses_in_compaction(const WaveTables& t, bool ray_order)
     return ray_order && !t.multi && t.scene0.env_rgb != nullptr;
 }
 
+// Multi-job waves: the binary traversal kernels hold 68 (closest hit) and 60
+// (shadow rays) registers, 7 and 8 resident blocks per SM.  Where one of the
+// resident scenes is dense (its tree and triangles from kDenseSceneBytes on)
+// variant 0 runs them at 9 blocks (56 registers), which hides more of the
+// dense scene's memory latency: the served mix of the Cornell box, the dense
+// mesh and Cornell variants +3.7%, while the batched
+// Cornell variants alone keep 7 (9 blocks: -3.6%; 8 blocks: -3.7%).
+constexpr int64_t kDenseSceneBytes = int64_t(16) << 20;
+static LaunchCfg multi_job_occupancy(const WaveTables& t, LaunchCfg cfg)
+{
+    if (cfg.variant == 0 && t.multi && t.tree == kTreeBinary && cfg.max_scene_bytes >= kDenseSceneBytes)
+        cfg.variant = 1;
+    return cfg;
+}
+
 void launch_trace_render(const WaveTables& t, RayQueueDev rq, const ull* d_n, HitQueueDev hq, ull* hq_n,
                          float* accum, ull* work, int* err, LaunchCfg cfg, cudaStream_t s)
 {
@@ -1505,6 +1562,7 @@ void launch_trace_render(const WaveTables& t, RayQueueDev rq, const ull* d_n, Hi
     if (cfg.variant == 0 && !t.multi && t.tree == kTreeBinary && cfg.l2_bytes > 0 &&
         (int64_t)t.scene0.num_nodes * (int64_t)sizeof(BvhNode) + (int64_t)t.scene0.num_tris * 48 > cfg.l2_bytes)
         cfg.variant = 1;
+    cfg = multi_job_occupancy(t, cfg);
 #define WF_TRACE(M, B, T, K)                                                                                  \
     k_trace_render<M, B, T, K><<<cfg.grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, d_n, hq, hq_n, \
                                                         accum, work, err, cfg.speculative, cfg.ray_order)
@@ -1532,6 +1590,22 @@ void launch_camera_chunks(const WaveChunk* chunks, const long long* header, cons
 }
 
 void launch_bounce_end(ull* counters, ull* tally, cudaStream_t s) { k_bounce_end<<<1, 1, 0, s>>>(counters, tally); }
+
+void launch_stream_plan(ull* counters, StreamState* st, int64_t capacity, int64_t* log, int iter, cudaStream_t s)
+{
+    k_stream_plan<<<1, 1, 0, s>>>(counters, st, capacity, log, iter);
+}
+
+void launch_camera_refill(const WaveChunk* chunks, const StreamState* st, const DeviceJob* jobs, RayQueueDev rq,
+                          LaunchCfg cfg, cudaStream_t s)
+{
+    k_camera_refill<<<cfg.grid, 256, 0, s>>>(chunks, st, jobs, rq);
+}
+
+void launch_add_floats(float* dst, const float* src, int64_t n, cudaStream_t s)
+{
+    k_add_floats<<<grid_for(n, 256, 65535), 256, 0, s>>>(dst, src, n);
+}
 
 int shade_blocks_per_sm(bool plain)
 {
@@ -1594,6 +1668,7 @@ void launch_occluded_render(const WaveTables& t, ShadowQueueDev sh, const ull* s
                             int* err, LaunchCfg cfg, cudaStream_t s)
 {
     const bool far_first = !t.multi && t.scene0.num_tris >= kFarFirstTriangles;
+    cfg = multi_job_occupancy(t, cfg);
 #define WF_OCC(M, B, T, K)                                                                                       \
     k_occluded_render<M, B, T, K><<<cfg.grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, sh, sh_n, accum, work, \
                                                            err, cfg.speculative)
