@@ -167,6 +167,37 @@ def test_server_streams_frames_larger_than_its_queue(wf, ctx, scene_small):
     assert _same(final, alone) >= 0.999
 
 
+def test_server_mixes_textured_and_plain_scenes(wf, ctx, scene_c2small):
+    """A job on a scene with textures and an environment map arrives while
+    jobs on plain scenes run: the server's captured step is redone with the
+    full shading instance (the lean one, used while no queued scene needs
+    them, compiles texture and environment lookups out), and every job equals
+    its render alone."""
+    jobs, hosts = _jobs(wf, ctx, 3, seed0=1300)
+    sid = ctx.add_scene(scene_c2small.desc)
+    cam = scene_c2small.camera(40, 32)
+    tex_job = wf.make_job(sid, 40, 32, 8, 8, cam, seed=515)
+    srv = wf.Server(ctx, hbm_budget_bytes=64 << 20, frame_spp=4, max_paths_per_wave=1 << 14)
+    ids = [srv.submit(j) for j in jobs]
+    srv.step()
+    tid = srv.submit(tex_job)
+    for _ in range(200):
+        info = srv.step()
+        if info["running"] == 0 and info["queued"] == 0:
+            break
+    assert all(srv.status(i)["state"] == wf.JOB_DONE for i in ids + [tid])
+    imgs = [srv.image(i, j.width, j.height) for i, j in zip(ids + [tid], jobs + [tex_job])]
+    srv.close()
+    for j, hs, img in zip(jobs, hosts, imgs):
+        ctx.upload(hs.desc)
+        alone, _ = ctx.render(wf.render_params(j.width, j.height, j.samples_per_pixel, j.max_depth, j.camera,
+                                               seed=j.seed_lo))
+        assert _same(img, alone) >= 0.999
+    ctx.upload(scene_c2small.desc)
+    alone, _ = ctx.render(wf.render_params(40, 32, 8, 8, cam, seed=515))
+    assert _same(imgs[-1], alone) >= 0.999
+
+
 def test_server_cancel(wf, ctx):
     jobs, hosts = _jobs(wf, ctx, 3, seed0=900)
     srv = wf.Server(ctx, hbm_budget_bytes=64 << 20, frame_spp=2, max_paths_per_wave=1 << 14)

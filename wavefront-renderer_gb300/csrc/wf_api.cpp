@@ -36,6 +36,23 @@ void free_all(std::vector<void*>& v)
     v.clear();
 }
 
+// The largest tree + triangles among the scenes `ids` (all resident scenes
+// when ids is null) and whether none of them has an environment map,
+// textures or a directional light (the lean shading instance).
+void wave_scene_traits(const wf_ctx* c, const int32_t* ids, int n, int64_t& max_bytes, int& lean)
+{
+    max_bytes = 0;
+    lean = 1;
+    const int count = ids ? n : (int)c->scenes.size();
+    for (int k = 0; k < count; ++k) {
+        const int i = ids ? ids[k] : k;
+        if (i < 0 || i >= (int)c->scenes.size() || !c->scenes[i].live) continue;
+        const ResidentScene& r = c->scenes[i];
+        max_bytes = std::max<int64_t>(max_bytes, (int64_t)r.tree_bytes);
+        if (r.S.env_alias_prob || r.S.num_textures > 0 || r.S.directional.intensity > 0.0f) lean = 0;
+    }
+}
+
 LaunchCfg persist_cfg(const wf_ctx* c)
 {
     int per_sm = c->tuning.persistent_blocks_per_sm > 0 ? c->tuning.persistent_blocks_per_sm : 16;
@@ -43,8 +60,12 @@ LaunchCfg persist_cfg(const wf_ctx* c)
     cfg.variant = c->tuning.trace_variant;
     cfg.speculative = c->tuning.speculative_traversal;
     cfg.l2_bytes = c->l2_bytes;
-    for (const auto& r : c->scenes)
-        if (r.live) cfg.max_scene_bytes = std::max<int64_t>(cfg.max_scene_bytes, (int64_t)r.tree_bytes);
+    if (c->wave_scene_bytes >= 0 && c->wave_lean >= 0) {
+        cfg.max_scene_bytes = c->wave_scene_bytes;
+        cfg.lean_multi = c->wave_lean;
+    } else {
+        wave_scene_traits(c, nullptr, 0, cfg.max_scene_bytes, cfg.lean_multi);
+    }
     cfg.shade_grid = c->num_sms * c->shade_per_sm;
     cfg.shade_grid_other = c->num_sms * c->shade_per_sm_other;
     return cfg;

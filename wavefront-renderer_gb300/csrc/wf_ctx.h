@@ -43,6 +43,8 @@ struct CapturedWave {
     int64_t key_cap = 0;
     int tree = kTreeBinary;         // tree format (TreeFormat) of the traversal
     int kernels = 0;                // kernels per replay
+    int lean = 0;                   // LaunchCfg::lean_multi of the capture
+    bool dense = false;             // LaunchCfg::max_scene_bytes >= kDenseSceneBytes at the capture
 };
 
 }  // namespace wf
@@ -56,6 +58,11 @@ struct wf_ctx {
     int shade_per_sm_other = 0;  // the same for its multi-job and cost-timed forms
     std::string last_error;
     int64_t paths_per_wave = wf::kDefaultPathsPerWave;
+    // The scenes of the multi-job wave about to be launched (render_batch and
+    // the server set them from their jobs; -1 = every resident scene): the
+    // largest tree + triangles and whether all fit the lean shading instance.
+    int64_t wave_scene_bytes = -1;
+    int wave_lean = -1;
 
     // Resident scenes; slot 0 is the scene of wf_scene_upload (the "current"
     // scene of the single-scene entry points).
@@ -143,6 +150,7 @@ namespace wf {
 
 int set_err(wf_ctx* c, int code, const std::string& msg);
 void free_all(std::vector<void*>& v);
+void wave_scene_traits(const wf_ctx* c, const int32_t* ids, int n, int64_t& max_bytes, int& lean);
 LaunchCfg persist_cfg(const wf_ctx* c);
 LaunchCfg wide_cfg(const wf_ctx* c);
 int ensure_render_buffers(wf_ctx* c, int64_t paths);

@@ -20,12 +20,17 @@ struct ShadeParams {
 };
 
 // Build it as LaunchCfg{grid, block} and assign the other members by name.
+// Multi-job waves over a scene whose tree + triangles reach this size run
+// the traversal kernels at 9 blocks per SM under variant 0 (wf_render.cu).
+constexpr int64_t kDenseSceneBytes = int64_t(16) << 20;
+
 struct LaunchCfg {
     int grid;
     int block;
     int variant = 0;   // kernel variant (traversal occupancy hint / stack placement)
     int64_t l2_bytes = 0;  // the device's L2 size (variant 0 of a larger scene runs at 9 blocks per SM)
     int64_t max_scene_bytes = 0;  // largest resident tree + triangles (variant 0 of multi-job waves)
+    int lean_multi = 0;  // no resident scene has an environment map, textures or a directional light
     int speculative = 0;  // 1 = speculative while-while traversal
     int ray_order = 0;    // 1 = hit records at their rays' indices, listed by k_compact_hits
     int shade_grid = 0;        // k_shade's grid (one full wave of resident blocks); 0 = grid

@@ -308,10 +308,13 @@ int wave_graph(wf_ctx* c, int max_depth, bool ray_sort, wf_render_stats& stats)
     int tree = kTreeBinary;
     int rc = table_tree(c, tree);
     if (rc) return rc;
+    const LaunchCfg pc = persist_cfg(c);
+    const bool dense = pc.max_scene_bytes >= kDenseSceneBytes;
     CapturedWave* g = nullptr;
     for (auto& x : c->graphs)
         if (x.max_depth == max_depth && x.ray_sort == ray_sort && x.variant == c->tuning.trace_variant &&
-            x.key_ptr == c->arena && x.key_cap == c->cap && x.tree == tree)
+            x.key_ptr == c->arena && x.key_cap == c->cap && x.tree == tree && x.lean == pc.lean_multi &&
+            x.dense == dense)
             g = &x;
     if (!g) {
         cudaGraph_t graph = nullptr;
@@ -330,6 +333,8 @@ int wave_graph(wf_ctx* c, int max_depth, bool ray_sort, wf_render_stats& stats)
         w.key_cap = c->cap;
         w.tree = tree;
         w.kernels = k;
+        w.lean = pc.lean_multi;
+        w.dense = dense;
         c->graphs.push_back(w);
         g = &c->graphs.back();
     }
@@ -424,6 +429,21 @@ int wave_chain(wf_ctx* c, int max_depth, bool ray_sort, const DeviceJob& job, wf
     stats.kernel_launches += kernels;
     return WF_OK;
 }
+
+// Scene traits (wave_scene_traits) of the jobs of the multi-job waves about
+// to be launched, for the launch configuration while the scope lasts.
+struct WaveSceneScope {
+    wf_ctx* c;
+    WaveSceneScope(wf_ctx* ctx, const std::vector<int32_t>& scene_ids) : c(ctx)
+    {
+        wave_scene_traits(c, scene_ids.data(), (int)scene_ids.size(), c->wave_scene_bytes, c->wave_lean);
+    }
+    ~WaveSceneScope()
+    {
+        c->wave_scene_bytes = -1;
+        c->wave_lean = -1;
+    }
+};
 
 int read_tally(wf_ctx* c, wf_render_stats& stats)
 {
@@ -718,8 +738,16 @@ struct wf_server {
     RangeAllocator frames;   // frame sums
     int64_t wave_paths = 0;  // streaming queue capacity
     int64_t wave_bytes = 0;
-    float* tmp = nullptr;  // averaged image staging (largest job)
+    float* tmp = nullptr;  // averaged image staging (device)
     int64_t tmp_floats = 0;
+    float* host_stage = nullptr;  // finished images (page-locked)
+    int64_t host_stage_floats = 0;
+    std::vector<int64_t> finishing;  // jobs whose last frame finished this step
+    // page-locked sources of the step's uploads (read by the device after the
+    // call returns; rewritten only after the step's final wait)
+    DeviceJob* job_stage = nullptr;    // one per table entry
+    WaveChunk* chunk_stage = nullptr;  // the chunk list
+    int64_t* state_stage = nullptr;    // [0] total, [1] nchunks
     // Streaming wave, owned by the server (its queues hold paths between steps)
     std::vector<void*> allocs;
     RayQueueDev rq[2]{};
@@ -739,7 +767,8 @@ struct wf_server {
     cudaEvent_t ev[2]{};
     cudaGraphExec_t exec = nullptr;
     const void* exec_table = nullptr;  // scene table, variant and tree the capture used
-    int exec_variant = -1, exec_tree = -1;
+    int exec_variant = -1, exec_tree = -1, exec_lean = -1;
+    bool exec_dense = false;
     int64_t cursor = 0;       // paths generated (device cursor after the last step)
     int64_t appended = 0;     // paths appended (the list's end)
     int64_t live = 0;         // rays queued for the next iteration
@@ -765,6 +794,12 @@ void server_free(wf_server* sv)
         if (e) cudaEventDestroy(e);
     if (sv->rb) cudaFreeHost(sv->rb);
     sv->rb = nullptr;
+    for (void* p : {(void*)sv->host_stage, (void*)sv->job_stage, (void*)sv->chunk_stage, (void*)sv->state_stage})
+        if (p) cudaFreeHost(p);
+    sv->host_stage = nullptr;
+    sv->job_stage = nullptr;
+    sv->chunk_stage = nullptr;
+    sv->state_stage = nullptr;
     free_all(sv->allocs);
     cudaFree(sv->tmp);
     sv->tmp = nullptr;
@@ -807,6 +842,9 @@ int server_alloc(wf_server* sv, int64_t arena_floats)
     WF_CK(c, wf_dalloc(A, &sv->d_state, 1));
     WF_CK(c, wf_dalloc(A, &sv->d_log, (size_t)kGroupIters));
     WF_CK(c, cudaMallocHost(&sv->rb, sizeof(StepReadback)));
+    WF_CK(c, cudaMallocHost(&sv->job_stage, sizeof(DeviceJob) * (size_t)kServerSlots));
+    WF_CK(c, cudaMallocHost(&sv->chunk_stage, sizeof(WaveChunk) * (size_t)sv->chunks_cap));
+    WF_CK(c, cudaMallocHost(&sv->state_stage, sizeof(int64_t) * 2));
     for (auto& e : sv->ev) WF_CK(c, cudaEventCreate(&e));
     cudaStream_t s = c->stream;
     WF_CK(c, cudaMemsetAsync(sv->counters, 0, sizeof(ull) * 8, s));
@@ -852,8 +890,10 @@ int ensure_stream_graph(wf_server* sv)
     int tree = kTreeBinary;
     int rc = table_tree(c, tree);
     if (rc) return rc;
+    const LaunchCfg pc = persist_cfg(c);
+    const bool dense = pc.max_scene_bytes >= kDenseSceneBytes;
     if (sv->exec && sv->exec_table == c->d_scene_table && sv->exec_variant == c->tuning.trace_variant &&
-        sv->exec_tree == tree)
+        sv->exec_tree == tree && sv->exec_lean == pc.lean_multi && sv->exec_dense == dense)
         return WF_OK;
     if (sv->exec) cudaGraphExecDestroy(sv->exec);
     sv->exec = nullptr;
@@ -869,27 +909,54 @@ int ensure_stream_graph(wf_server* sv)
     sv->exec_table = c->d_scene_table;
     sv->exec_variant = c->tuning.trace_variant;
     sv->exec_tree = tree;
+    sv->exec_lean = pc.lean_multi;
+    sv->exec_dense = dense;
     return WF_OK;
 }
 
-int finish_job(wf_server* sv, int64_t id, ServedJob& j)
+// Jobs whose last frame finished this step: their averaged images are made
+// together at the end of the step (one copy, one wait), then their sums go.
+int flush_finished(wf_server* sv, wf_server_step_info& si)
 {
+    if (sv->finishing.empty()) return WF_OK;
     wf_ctx* c = sv->c;
-    const int64_t nf = j.accum_floats;
-    if (nf > sv->tmp_floats) {
+    int64_t total = 0;
+    for (int64_t id : sv->finishing) total += sv->jobs[id].accum_floats;
+    if (total > sv->tmp_floats) {
         cudaFree(sv->tmp);
         sv->tmp = nullptr;
         sv->tmp_floats = 0;
-        WF_CK(c, cudaMalloc(&sv->tmp, sizeof(float) * nf));
-        sv->tmp_floats = nf;
+        WF_CK(c, cudaMalloc(&sv->tmp, sizeof(float) * total));
+        sv->tmp_floats = total;
     }
-    launch_finalize(sv->arena + j.accum_off, nf, (float)j.samples_done, sv->tmp, c->stream);
-    j.final_image.resize(nf);
-    WF_CK(c, cudaMemcpyAsync(j.final_image.data(), sv->tmp, sizeof(float) * nf, cudaMemcpyDeviceToHost, c->stream));
+    if (total > sv->host_stage_floats) {
+        cudaFreeHost(sv->host_stage);
+        sv->host_stage = nullptr;
+        sv->host_stage_floats = 0;
+        WF_CK(c, cudaMallocHost(&sv->host_stage, sizeof(float) * total));
+        sv->host_stage_floats = total;
+    }
+    int64_t o = 0;
+    for (int64_t id : sv->finishing) {
+        const ServedJob& j = sv->jobs[id];
+        launch_finalize(sv->arena + j.accum_off, j.accum_floats, (float)j.samples_done, sv->tmp + o, c->stream);
+        o += j.accum_floats;
+    }
+    WF_CK(c, cudaMemcpyAsync(sv->host_stage, sv->tmp, sizeof(float) * total, cudaMemcpyDeviceToHost, c->stream));
     WF_CK(c, cudaStreamSynchronize(c->stream));
-    sv->alloc.release(j.accum_off, j.accum_floats);
-    j.accum_off = -1;
-    (void)id;
+    const double now = seconds_since(sv->t0);
+    o = 0;
+    for (int64_t id : sv->finishing) {
+        ServedJob& j = sv->jobs[id];
+        j.final_image.assign(sv->host_stage + o, sv->host_stage + o + j.accum_floats);
+        o += j.accum_floats;
+        sv->alloc.release(j.accum_off, j.accum_floats);
+        j.accum_off = -1;
+        j.state = WF_JOB_DONE;
+        j.t_done = now;
+        si.completed_this_step++;
+    }
+    sv->finishing.clear();
     return WF_OK;
 }
 
@@ -920,7 +987,7 @@ int append_frame(wf_server* sv, int64_t id, ServedJob& j, bool& room)
     k.floats = j.accum_floats;
     k.len = (int64_t)j.spec.width * j.spec.height * k.nspp;
     k.path_offset = sv->appended;
-    DeviceJob dj;
+    DeviceJob& dj = sv->job_stage[k.slot];
     int rc = make_device_job(c, j.spec, foff, dj);
     if (rc) return rc;
     WF_CK(c, cudaMemcpyAsync(sv->d_jobs + k.slot, &dj, sizeof(dj), cudaMemcpyHostToDevice, c->stream));
@@ -947,13 +1014,7 @@ int retire_chunk(wf_server* sv, const ServerChunk& k, double now, wf_server_step
         j.samples_done += k.nspp;
         j.frames++;
         if (j.t_first < 0) j.t_first = now;
-        if (j.samples_done >= j.spec.samples_per_pixel) {
-            int rc = finish_job(sv, k.job, j);
-            if (rc) return rc;
-            j.state = WF_JOB_DONE;
-            j.t_done = seconds_since(sv->t0);
-            si.completed_this_step++;
-        }
+        if (j.samples_done >= j.spec.samples_per_pixel) sv->finishing.push_back(k.job);
     } else if (j.chunks_out == 0 && j.accum_off >= 0) {  // cancelled: its sums go once no frame runs
         sv->alloc.release(j.accum_off, j.accum_floats);
         j.accum_off = -1;
@@ -1198,6 +1259,9 @@ int wf_render_batch(wf_ctx* c, const wf_job* jobs, int32_t njobs, float* const* 
         if ((rc = make_device_job(c, jobs[j], offs[j], table[j]))) return rc;
     if ((rc = upload_jobs(c, table))) return rc;
     WF_CK(c, cudaMemsetAsync(c->arena, 0, sizeof(float) * (size_t)floats, s));
+    std::vector<int32_t> scene_ids(njobs);
+    for (int j = 0; j < njobs; ++j) scene_ids[j] = jobs[j].scene_id;
+    const WaveSceneScope scene_scope(c, scene_ids);
     const bool graph = use_graph(c, true, WF_POLICY_NONE);
     wf_render_stats stats{};
     if (graph && (rc = zero_tally(c))) return rc;
@@ -1366,10 +1430,7 @@ int wf_server_step(wf_server* sv, wf_server_step_info* info)
             j.samples_done = j.scheduled = j.spec.samples_per_pixel;
             j.frames = 1;
             j.t_first = seconds_since(sv->t0);
-            if ((rc = finish_job(sv, id, j))) return rc;
-            j.state = WF_JOB_DONE;
-            j.t_done = seconds_since(sv->t0);
-            si.completed_this_step++;
+            sv->finishing.push_back(id);
             continue;
         }
         sv->running.push_back(id);
@@ -1406,21 +1467,30 @@ int wf_server_step(wf_server* sv, wf_server_step_info* info)
             off += it->len;
         }
         sv->appended = sv->pending.empty() ? sv->cursor : off;
-        std::vector<WaveChunk> hc;
-        hc.reserve(sv->pending.size());
-        for (const auto& k : sv->pending) hc.push_back(WaveChunk{k.slot, k.first_sample, k.nspp, 0, k.path_offset});
-        if (!hc.empty())
-            WF_CK(c, cudaMemcpyAsync(sv->d_chunks, hc.data(), sizeof(WaveChunk) * hc.size(), cudaMemcpyHostToDevice, s));
-        const int64_t total = sv->appended;
-        const int32_t nchunks = (int32_t)hc.size();
-        WF_CK(c, cudaMemcpyAsync(reinterpret_cast<char*>(sv->d_state) + offsetof(StreamState, total), &total,
-                                 sizeof(total), cudaMemcpyHostToDevice, s));
-        WF_CK(c, cudaMemcpyAsync(reinterpret_cast<char*>(sv->d_state) + offsetof(StreamState, nchunks), &nchunks,
-                                 sizeof(nchunks), cudaMemcpyHostToDevice, s));
+        int nchunks = 0;
+        for (const auto& k : sv->pending)
+            sv->chunk_stage[nchunks++] = WaveChunk{k.slot, k.first_sample, k.nspp, 0, k.path_offset};
+        if (nchunks > 0)
+            WF_CK(c, cudaMemcpyAsync(sv->d_chunks, sv->chunk_stage, sizeof(WaveChunk) * nchunks, cudaMemcpyHostToDevice, s));
+        sv->state_stage[0] = sv->appended;
+        sv->state_stage[1] = nchunks;
+        WF_CK(c, cudaMemcpyAsync(reinterpret_cast<char*>(sv->d_state) + offsetof(StreamState, total), sv->state_stage,
+                                 sizeof(int64_t), cudaMemcpyHostToDevice, s));
+        int32_t* nc32 = reinterpret_cast<int32_t*>(sv->state_stage + 1);
+        *nc32 = nchunks;
+        WF_CK(c, cudaMemcpyAsync(reinterpret_cast<char*>(sv->d_state) + offsetof(StreamState, nchunks), nc32,
+                                 sizeof(int32_t), cudaMemcpyHostToDevice, s));
     }
     // 4. run the step's iterations, unless nothing is queued or left to generate
     if (sv->live > 0 || sv->appended > sv->cursor) {
-        if ((rc = ensure_stream_graph(sv))) return rc;
+        // the scenes whose rays the queue can hold during the step
+        std::vector<int32_t> scene_ids;
+        for (const auto& k : sv->inflight) scene_ids.push_back(sv->jobs[k.job].spec.scene_id);
+        for (const auto& k : sv->pending) scene_ids.push_back(sv->jobs[k.job].spec.scene_id);
+        {
+            const WaveSceneScope scene_scope(c, scene_ids);
+            if ((rc = ensure_stream_graph(sv))) return rc;
+        }
         WF_CK(c, cudaEventRecord(sv->ev[0], s));
         WF_CK(c, cudaGraphLaunch(sv->exec, s));
         WF_CK(c, cudaEventRecord(sv->ev[1], s));
@@ -1477,6 +1547,7 @@ int wf_server_step(wf_server* sv, wf_server_step_info* info)
         }
     }
     sv->inflight.swap(keep);
+    if ((rc = flush_finished(sv, si))) return rc;
     sv->running.erase(std::remove_if(sv->running.begin(), sv->running.end(),
                                      [&](int64_t id) { return sv->jobs[id].state != WF_JOB_RUNNING; }),
                       sv->running.end());

@@ -1543,7 +1543,6 @@ static bool misses_in_compaction(const WaveTables& t, bool ray_order)
 // dense scene's memory latency: the served mix of the Cornell box, the dense
 // mesh and Cornell variants +3.7%, while the batched
 // Cornell variants alone keep 7 (9 blocks: -3.6%; 8 blocks: -3.7%).
-constexpr int64_t kDenseSceneBytes = int64_t(16) << 20;
 static LaunchCfg multi_job_occupancy(const WaveTables& t, LaunchCfg cfg)
 {
     if (cfg.variant == 0 && t.multi && t.tree == kTreeBinary && cfg.max_scene_bytes >= kDenseSceneBytes)
@@ -1635,7 +1634,10 @@ void launch_shade(const WaveTables& t, RayQueueDev rq, HitQueueDev hq, const ull
 {
     const int plain_grid = cfg.shade_grid > 0 ? cfg.shade_grid : cfg.grid;
     const int grid = cfg.shade_grid_other > 0 ? cfg.shade_grid_other : cfg.grid;
-    if (t.multi)
+    if (t.multi && cfg.lean_multi)  // every resident scene fits the lean instance
+        k_shade<true, false, true><<<grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, hq, hq_n,
+                                                        cfg.ray_order, sh, sh_n, next, next_n, accum, err);
+    else if (t.multi)
         k_shade<true, false><<<grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, hq, hq_n, cfg.ray_order,
                                                   sh, sh_n, next, next_n, accum, err);
     else if (t.job0.cost_sum_mat)
