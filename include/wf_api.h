@@ -297,9 +297,11 @@ typedef struct wf_tuning {
                             binary tree (Karras radix tree), 2 = the PLOC tree
                             collapsed into compressed 8-wide nodes, 3 = the
                             PLOC tree collapsed into 4-wide nodes (full-
-                            precision boxes, 128 bytes each); a PLOC tree
-                            deeper than its traversal stack falls back to
-                            LBVH */
+                            precision boxes, 128 bytes each), 4 = the PLOC
+                            binary tree with leaves chosen by the surface
+                            area heuristic (large triangles get leaves of
+                            their own); a PLOC tree deeper than its traversal
+                            stack falls back to LBVH */
     int32_t sort_min_queue; /* sort-or-skip: the ray sort and the shading
                             policies run on a bounce only when its queue holds
                             at least this many entries (0 = always, as the

@@ -316,9 +316,9 @@ def test_render_is_order_independent(wf, ctx, scene_small, scene_c2small, which)
         ctx.set_tuning()
 
 
-@pytest.mark.parametrize("builder", [2, 3])
+@pytest.mark.parametrize("builder", [2, 3, 4])
 def test_tree_formats_render_the_same_image(wf, ctx, scene_c2small, builder):
-    """The 8-wide and 4-wide trees return the binary tree's hits, so a render
+    """The 8-wide, 4-wide and surface-area-leaf trees return the binary tree's hits, so a render
     over them (plain launches, graph replay, every launch variant) gives the
     binary tree's image up to float-add order (1e-4 relative, 99.9% of
     pixels).  A context of its own: the resident scenes of one context share
@@ -610,8 +610,9 @@ def test_gpu_live_costs_only_reorder_shading(wf, ctx, scene_c2small, policy):
 @pytest.mark.parametrize("which", ["c0", "small", "c2small"])
 def test_bvh_builders_give_identical_hits(wf, orc, ctx, scene0, scene_small, scene_c2small, which):
     """The binary PLOC tree, the LBVH, the compressed 8-wide and the 4-wide
-    PLOC trees return the same closest hits and occlusion bit for bit (and the
-    port's), and each passes the build's structural check."""
+    PLOC trees and the PLOC tree with surface-area leaves return the same
+    closest hits and occlusion bit for bit (and the port's), and each passes
+    the build's structural check."""
     scene = {"c0": scene0, "small": scene_small, "c2small": scene_c2small}[which]
     rng = np.random.default_rng(21)
     lo, hi = ([0.0, 0.01, 0.0], [16.0, 0.9, 16.0]) if which == "c2small" else \
@@ -623,7 +624,7 @@ def test_bvh_builders_give_identical_hits(wf, orc, ctx, scene0, scene_small, sce
     want_occ = port.trace_occluded(o, d, maxd)
     infos = []
     try:
-        for builder in (0, 1, 2, 3):
+        for builder in (0, 1, 2, 3, 4):
             ctx.set_tuning(bvh_builder=builder)
             infos.append(ctx.upload(scene.desc))
             got = ctx.trace_closest(o, d)
@@ -632,7 +633,7 @@ def test_bvh_builders_give_identical_hits(wf, orc, ctx, scene0, scene_small, sce
             assert np.array_equal(ctx.trace_occluded(o, d, maxd), want_occ), builder
     finally:
         ctx.set_tuning()
-    assert [i.bvh_builder for i in infos] == [0, 1, 2, 3]
+    assert [i.bvh_builder for i in infos] == [0, 1, 2, 3, 4]
     assert infos[2].bvh_nodes < infos[0].bvh_nodes  # the 8-wide tree has fewer nodes
     assert infos[3].bvh_nodes < infos[0].bvh_nodes  # so has the 4-wide one
     assert infos[3].bvh_depth < infos[0].bvh_depth
@@ -663,7 +664,7 @@ def test_bvh_builders_on_tiny_scenes(wf, orc, ntri):
     want = port.trace_closest(o, d)
     want_occ = port.trace_occluded(o, d, maxd)
     assert (want["prim_id"] >= 0).mean() > 0.3
-    for builder in (0, 1, 2, 3):
+    for builder in (0, 1, 2, 3, 4):
         c2 = wf.Context(0)
         try:
             c2.set_tuning(bvh_builder=builder)

@@ -609,6 +609,9 @@ int build_scene(wf_ctx* c, const wf_scene_desc* D, ResidentScene& R)
         } else if (c->tuning.bvh_builder == 3) {
             brc = build_ploc4(bi, bo, c->num_sms, s, err);
             R.info.bvh_builder = 3;
+        } else if (c->tuning.bvh_builder == 4) {
+            brc = build_ploc(bi, bo, c->num_sms, s, err, true);
+            R.info.bvh_builder = 4;
         }
         if (brc) {  // LBVH on request, or when a PLOC tree is too deep for its stack
             brc = build_lbvh(bi, bo, c->num_sms, s, err);
@@ -1228,7 +1231,7 @@ int wf_set_tuning(wf_ctx* c, const wf_tuning* t)
 {
     if (!c || !t) return WF_ERR_INVALID_ARGUMENT;
     if (t->trace_variant < 0 || t->trace_variant > 3 || t->persistent_blocks_per_sm < 0 ||
-        t->persistent_blocks_per_sm > 32 || t->bvh_builder < 0 || t->bvh_builder > 3)
+        t->persistent_blocks_per_sm > 32 || t->bvh_builder < 0 || t->bvh_builder > 4)
         return set_err(c, WF_ERR_INVALID_ARGUMENT, "tuning out of range");
     c->tuning = *t;
     return WF_OK;

@@ -363,23 +363,31 @@ __global__ void k_ploc_root(int root, int* offset, int* depth)
     depth[root] = 0;
 }
 
-// Kept interior nodes (more than kLeafMax triangles below them) are
+// Kept interior nodes (interior[], from k_bin_leaves / k_bin_interior) are
 // numbered in reverse creation order, q = (last id) - id: the root gets 0 and
 // the nodes of one clustering pass — one band of the tree's levels — stay
 // together, so the top levels every ray visits share cache lines.  (A
 // depth-first order measured ~10% slower on the dense-mesh and lattice
-// workloads.)  A child with kLeafMax triangles or fewer becomes a leaf over
-// its depth-first triangle range.
-__global__ void k_ploc_keep(int num_tris, int last_id, const int* __restrict__ cnt, int* __restrict__ keep)
+// workloads.)  A child that is not kept becomes a leaf over its depth-first
+// triangle range.
+__global__ void k_ploc_keep(int num_tris, int last_id, const uint8_t* __restrict__ interior, int* __restrict__ keep)
+{
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q <= last_id - num_tris; q += gridDim.x * blockDim.x)
+        keep[q] = interior[last_id - q - num_tris];
+}
+
+// Interior nodes with more than kLeafMax triangles below them (the 4-wide
+// builder's bound on its node count), in the same numbering.
+__global__ void k_ploc_big(int num_tris, int last_id, const int* __restrict__ cnt, int* __restrict__ keep)
 {
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q <= last_id - num_tris; q += gridDim.x * blockDim.x)
         keep[q] = cnt[last_id - q] > kLeafMax ? 1 : 0;
 }
 
 __device__ __forceinline__ uint32_t ploc_child(int c, int num_tris, int last_id, const int* cnt, const int* offset,
-                                               const int* newid)
+                                               const int* newid, const uint8_t* interior)
 {
-    if (c < num_tris || cnt[c] <= kLeafMax)
+    if (c < num_tris || !interior[c - num_tris])
         return kLeafFlag | ((uint32_t)offset[c] << 3) | (uint32_t)(cnt[c] - 1);
     return (uint32_t)newid[last_id - c];
 }
@@ -387,10 +395,11 @@ __device__ __forceinline__ uint32_t ploc_child(int c, int num_tris, int last_id,
 __global__ void k_ploc_emit(int num_tris, int last_id, const int* __restrict__ left, const int* __restrict__ right,
                             const int* __restrict__ cnt, const int* __restrict__ offset,
                             const int* __restrict__ depth, const int* __restrict__ newid,
-                            const float* __restrict__ nbox, BvhNode* __restrict__ nodes, int* __restrict__ max_depth)
+                            const uint8_t* __restrict__ interior, const float* __restrict__ nbox,
+                            BvhNode* __restrict__ nodes, int* __restrict__ max_depth)
 {
     for (int id = num_tris + blockIdx.x * blockDim.x + threadIdx.x; id <= last_id; id += gridDim.x * blockDim.x) {
-        if (cnt[id] <= kLeafMax) continue;
+        if (!interior[id - num_tris]) continue;
         const int l = left[id - num_tris], r = right[id - num_tris];
         float a[6], b[6];
 #pragma unroll
@@ -404,8 +413,8 @@ __global__ void k_ploc_emit(int num_tris, int last_id, const int* __restrict__ l
         nd.c0xy = make_float4(a[0], a[3], a[1], a[4]);
         nd.c1xy = make_float4(b[0], b[3], b[1], b[4]);
         nd.cz = make_float4(a[2], a[5], b[2], b[5]);
-        nd.kids = make_int4((int)ploc_child(l, num_tris, last_id, cnt, offset, newid),
-                            (int)ploc_child(r, num_tris, last_id, cnt, offset, newid), 0, 0);
+        nd.kids = make_int4((int)ploc_child(l, num_tris, last_id, cnt, offset, newid, interior),
+                            (int)ploc_child(r, num_tris, last_id, cnt, offset, newid, interior), 0, 0);
         nodes[newid[last_id - id]] = nd;
         atomicMax(max_depth, depth[id]);
     }
@@ -524,6 +533,62 @@ __device__ __forceinline__ float box_area(const float* x)
 {
     const float dx = x[3] - x[0], dy = x[4] - x[1], dz = x[5] - x[2];
     return dx * dy + dy * dz + dz * dx;
+}
+
+// Leaves of the binary tree: a subtree of at most kLeafMax triangles is one
+// leaf; with sah (wf_tuning::bvh_builder 4) only where testing its triangles
+// is expected to cost no more than descending it (surface area heuristic: a
+// node test and a triangle test cost 1 each, weighted by the area of the box
+// that leads to them).  Measured against the fixed rule: Cornell box +4.6%
+// (its wall triangles get leaves of their own), lattice +0.7%, batched
+// Cornell variants +0.3%, dense mesh -1.4% (twice the nodes: its small
+// leaves were cheaper to test than to split).  One launch per clustering
+// pass in creation order (children first).
+constexpr float kBinSahPrim = 1.0f;
+
+__global__ void k_bin_leaves(int first_id, int count, int num_tris, const int* __restrict__ left,
+                             const int* __restrict__ right, const int* __restrict__ cnt,
+                             const float* __restrict__ nbox, int sah, float* __restrict__ cost,
+                             uint8_t* __restrict__ leaf)
+{
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
+        const int id = first_id + k;
+        const int64_t in = id - num_tris;
+        const int N = cnt[id];
+        if (!sah) {
+            leaf[in] = N <= kLeafMax ? 1 : 0;
+            continue;
+        }
+        float below = 0.0f;
+        for (int h = 0; h < 2; ++h) {
+            const int c = h ? right[in] : left[in];
+            below += c < num_tris ? box_area(nbox + 6 * (int64_t)c) * kBinSahPrim : cost[c - num_tris];
+        }
+        const float A = box_area(nbox + 6 * (int64_t)id);
+        const float split = A + below;
+        const float as_leaf = N <= kLeafMax ? A * kBinSahPrim * (float)N : INFINITY;
+        const bool lf = as_leaf <= split;
+        leaf[in] = lf ? 1 : 0;
+        cost[in] = lf ? as_leaf : split;
+    }
+}
+
+// Interior nodes top down (one launch per pass, the root's first): the root
+// is interior; a child node is interior when its parent is and it is no leaf.
+__global__ void k_bin_root(int root, int num_tris, uint8_t* interior) { interior[root - num_tris] = 1; }
+
+__global__ void k_bin_interior(int first_id, int count, int num_tris, const int* __restrict__ left,
+                               const int* __restrict__ right, const uint8_t* __restrict__ leaf,
+                               uint8_t* __restrict__ interior)
+{
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
+        const int64_t in = first_id + k - num_tris;
+        if (!interior[in]) continue;
+        for (int h = 0; h < 2; ++h) {
+            const int c = h ? right[in] : left[in];
+            if (c >= num_tris) interior[c - num_tris] = leaf[c - num_tris] ? 0 : 1;
+        }
+    }
 }
 
 template <int kWidth, int kLeafCnt>
@@ -1168,7 +1233,8 @@ fail:
 
 }  // namespace
 
-int build_ploc(const BvhBuildInput& in, BvhBuildOutput& out, int num_sms, cudaStream_t s, std::string& err)
+int build_ploc(const BvhBuildInput& in, BvhBuildOutput& out, int num_sms, cudaStream_t s, std::string& err,
+               bool sah_leaves)
 {
     const int n = in.num_tris;
     out.tris = nullptr;
@@ -1180,27 +1246,40 @@ int build_ploc(const BvhBuildInput& in, BvhBuildOutput& out, int num_sms, cudaSt
     BuildScratch B;
     PlocTree T;
     int *keep, *newid, *d_depth;
+    float* bin_cost;
+    uint8_t *leaf, *interior;
     const int grid = num_sms * 8;
     int h_depth = 0;
     if (ploc_tree(in, num_sms, s, err, B, T)) goto fail;
     WF_TRY(B.alloc(&keep, (size_t)n));
     WF_TRY(B.alloc(&newid, (size_t)n));
     WF_TRY(B.alloc(&d_depth, 1));
+    WF_TRY(B.alloc(&bin_cost, (size_t)n));
+    WF_TRY(B.alloc(&leaf, (size_t)n));
+    WF_TRY(B.alloc(&interior, (size_t)n));
     WF_TRY(cudaMemsetAsync(d_depth, 0, sizeof(int), s));
+    WF_TRY(cudaMemsetAsync(interior, 0, (size_t)n, s));
     if (n <= kLeafMax) {
         WF_TRY(cudaMalloc(&out.nodes, sizeof(BvhNode)));
         k_ploc_single<<<1, 1, 0, s>>>(n, T.root, T.nbox, out.nodes);
         out.num_nodes = 1;
     } else {
         const int ninternal = T.root - n + 1;
-        k_ploc_keep<<<grid, 256, 0, s>>>(n, T.root, T.cnt, keep);
+        for (const auto& it : T.iters)
+            k_bin_leaves<<<std::max(1, std::min(grid, (it.second + 255) / 256)), 256, 0, s>>>(
+                it.first, it.second, n, T.left, T.right, T.cnt, T.nbox, sah_leaves ? 1 : 0, bin_cost, leaf);
+        k_bin_root<<<1, 1, 0, s>>>(T.root, n, interior);
+        for (auto it = T.iters.rbegin(); it != T.iters.rend(); ++it)
+            k_bin_interior<<<std::max(1, std::min(grid, (it->second + 255) / 256)), 256, 0, s>>>(
+                it->first, it->second, n, T.left, T.right, leaf, interior);
+        k_ploc_keep<<<grid, 256, 0, s>>>(n, T.root, interior, keep);
         exclusive_scan_i32(keep, ninternal, newid, T.block_sums, T.d_total, s);
         int kept = 0;
         WF_TRY(cudaMemcpyAsync(&kept, T.d_total, sizeof(int), cudaMemcpyDeviceToHost, s));
         WF_TRY(cudaStreamSynchronize(s));
         WF_TRY(cudaMalloc(&out.nodes, sizeof(BvhNode) * (size_t)std::max(kept, 1)));
-        k_ploc_emit<<<grid, 256, 0, s>>>(n, T.root, T.left, T.right, T.cnt, T.offset, T.depth, newid, T.nbox,
-                                        out.nodes, d_depth);
+        k_ploc_emit<<<grid, 256, 0, s>>>(n, T.root, T.left, T.right, T.cnt, T.offset, T.depth, newid, interior,
+                                        T.nbox, out.nodes, d_depth);
         out.num_nodes = kept;
         WF_TRY(cudaMemcpyAsync(&h_depth, d_depth, sizeof(int), cudaMemcpyDeviceToHost, s));
     }
@@ -1353,7 +1432,7 @@ int build_ploc4(const BvhBuildInput& in, BvhBuildOutput& out, int num_sms, cudaS
     WF_TRY(B.alloc(&keep_off, (size_t)n));
     if (n > 1) {
         const int ninternal = T.root - n + 1;
-        k_ploc_keep<<<grid, 256, 0, s>>>(n, T.root, T.cnt, keep);
+        k_ploc_big<<<grid, 256, 0, s>>>(n, T.root, T.cnt, keep);
         exclusive_scan_i32(keep, ninternal, keep_off, T.block_sums, T.d_total, s);
         WF_TRY(cudaMemcpyAsync(&cap, T.d_total, sizeof(int), cudaMemcpyDeviceToHost, s));
         WF_TRY(cudaStreamSynchronize(s));

@@ -33,9 +33,11 @@ int build_lbvh(const BvhBuildInput& in, BvhBuildOutput& out, int num_sms, cudaSt
                std::string& err);
 
 // PLOC (Meister & Bittner 2018) over the same Morton order: higher-quality
-// trees (smaller surface-area cost) for the same traversal layout.
+// trees (smaller surface-area cost) for the same traversal layout.  Leaves:
+// every subtree of <= kLeafMax triangles, or with sah_leaves only those the
+// surface area heuristic prefers to splitting.
 int build_ploc(const BvhBuildInput& in, BvhBuildOutput& out, int num_sms, cudaStream_t s,
-               std::string& err);
+               std::string& err, bool sah_leaves = false);
 
 // PLOC tree collapsed top-down into compressed 8-wide nodes (WideNode):
 // each wide node opens the binary subtree greedily (largest surface area

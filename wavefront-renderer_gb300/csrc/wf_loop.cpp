@@ -706,6 +706,19 @@ struct ServerChunk {
     int64_t done_iter = -1;   // iterations after which all its paths have finished
 };
 
+// Served jobs by id: ids are 1, 2, 3, ... in submission order, so the table
+// is a deque (stable references as it grows, constant-time lookup).
+struct JobTable {
+    std::deque<ServedJob> v;
+    ServedJob& operator[](int64_t id) { return v[(size_t)(id - 1)]; }
+    ServedJob* find(int64_t id) { return id >= 1 && id <= (int64_t)v.size() ? &v[(size_t)(id - 1)] : nullptr; }
+    int64_t add(ServedJob&& j)
+    {
+        v.push_back(std::move(j));
+        return (int64_t)v.size();
+    }
+};
+
 double seconds_since(std::chrono::steady_clock::time_point t0)
 {
     return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
@@ -729,10 +742,11 @@ struct StepReadback {
 struct wf_server {
     wf_ctx* c = nullptr;
     wf_server_config cfg{};
-    std::map<int64_t, ServedJob> jobs;
-    std::deque<int64_t> queue;
-    std::vector<int64_t> running;
-    int64_t next_id = 1;
+    JobTable jobs;
+    std::deque<int64_t> queue;       // submitted, not admitted yet
+    std::deque<int64_t> fresh;       // admitted, no frame appended yet
+    std::deque<int64_t> to_schedule; // admitted, frames left to append (admission order)
+    int64_t running = 0;             // admitted jobs not finished or cancelled
     std::chrono::steady_clock::time_point t0;
     RangeAllocator alloc;    // job sums
     RangeAllocator frames;   // frame sums
@@ -955,6 +969,7 @@ int flush_finished(wf_server* sv, wf_server_step_info& si)
         j.state = WF_JOB_DONE;
         j.t_done = now;
         si.completed_this_step++;
+        sv->running--;
     }
     sv->finishing.clear();
     return WF_OK;
@@ -1388,13 +1403,10 @@ int wf_server_submit(wf_server* sv, const wf_job* job, int64_t* out_id)
     j.spec.enable_cost_aware_rr = 0;
     j.t_submit = seconds_since(sv->t0);
     j.accum_floats = 3 * (int64_t)job->width * job->height;
-    const int64_t id = sv->next_id++;
-    if (j.accum_floats > sv->alloc.total || (int64_t)job->width * job->height > sv->wave_paths) {
-        j.state = WF_JOB_REJECTED;
-    } else {
-        sv->queue.push_back(id);
-    }
-    sv->jobs.emplace(id, std::move(j));
+    const bool reject = j.accum_floats > sv->alloc.total || (int64_t)job->width * job->height > sv->wave_paths;
+    if (reject) j.state = WF_JOB_REJECTED;
+    const int64_t id = sv->jobs.add(std::move(j));
+    if (!reject) sv->queue.push_back(id);
     *out_id = id;
     return WF_OK;
 }
@@ -1426,6 +1438,7 @@ int wf_server_step(wf_server* sv, wf_server_step_info* info)
         WF_CK(c, cudaMemsetAsync(sv->arena + off, 0, sizeof(float) * (size_t)j.accum_floats, s));
         const int64_t id = sv->queue.front();
         sv->queue.pop_front();
+        sv->running++;
         if (j.spec.max_depth == 0) {  // renderScene traces depths 0 .. maxDepth-1: nothing
             j.samples_done = j.scheduled = j.spec.samples_per_pixel;
             j.frames = 1;
@@ -1433,7 +1446,8 @@ int wf_server_step(wf_server* sv, wf_server_step_info* info)
             sv->finishing.push_back(id);
             continue;
         }
-        sv->running.push_back(id);
+        sv->fresh.push_back(id);
+        sv->to_schedule.push_back(id);
     }
     // 2. append frames until the list holds what one step can generate at most
     // (kGroupIters full queues): first the first frame of every job that has
@@ -1442,17 +1456,22 @@ int wf_server_step(wf_server* sv, wf_server_step_info* info)
     // came while a new one shows a frame a few bounces after it starts.
     const int64_t target = (int64_t)kGroupIters * sv->wave_paths;
     bool room = true;
-    for (auto it = sv->running.begin(); room && it != sv->running.end(); ++it) {
-        ServedJob& j = sv->jobs[*it];
-        if (j.scheduled == 0 && sv->appended - sv->cursor < 2 * target) {
-            if ((rc = append_frame(sv, *it, j, room))) return rc;
+    while (room && !sv->fresh.empty() && sv->appended - sv->cursor < 2 * target) {
+        ServedJob& j = sv->jobs[sv->fresh.front()];
+        if (j.state == WF_JOB_RUNNING && j.scheduled == 0) {
+            if ((rc = append_frame(sv, sv->fresh.front(), j, room))) return rc;
+            if (!room) break;
         }
+        sv->fresh.pop_front();
     }
-    for (auto it = sv->running.begin(); room && it != sv->running.end() && sv->appended - sv->cursor < target; ++it) {
-        ServedJob& j = sv->jobs[*it];
+    while (room && !sv->to_schedule.empty() && sv->appended - sv->cursor < target) {
+        const int64_t id = sv->to_schedule.front();
+        ServedJob& j = sv->jobs[id];
         while (room && j.state == WF_JOB_RUNNING && j.scheduled < j.spec.samples_per_pixel &&
                sv->appended - sv->cursor < target)
-            if ((rc = append_frame(sv, *it, j, room))) return rc;
+            if ((rc = append_frame(sv, id, j, room))) return rc;
+        if (j.state != WF_JOB_RUNNING || j.scheduled >= j.spec.samples_per_pixel) sv->to_schedule.pop_front();
+        else break;
     }
     // 3. lay the unstarted frames out again, first frames of jobs ahead (the
     // front frame may be partly generated and keeps its place)
@@ -1548,11 +1567,8 @@ int wf_server_step(wf_server* sv, wf_server_step_info* info)
     }
     sv->inflight.swap(keep);
     if ((rc = flush_finished(sv, si))) return rc;
-    sv->running.erase(std::remove_if(sv->running.begin(), sv->running.end(),
-                                     [&](int64_t id) { return sv->jobs[id].state != WF_JOB_RUNNING; }),
-                      sv->running.end());
     si.queued = (int32_t)sv->queue.size();
-    si.running = (int32_t)sv->running.size();
+    si.running = (int32_t)sv->running;
     si.budget_used_bytes = sv->wave_bytes + 4 * (sv->alloc.used + sv->frames.used);
     if (info) *info = si;
     return WF_OK;
@@ -1561,9 +1577,9 @@ int wf_server_step(wf_server* sv, wf_server_step_info* info)
 int wf_server_status(wf_server* sv, int64_t id, wf_job_status* out)
 {
     if (!sv || !out) return WF_ERR_INVALID_ARGUMENT;
-    auto it = sv->jobs.find(id);
-    if (it == sv->jobs.end()) return set_err(sv->c, WF_ERR_INVALID_ARGUMENT, "no such job");
-    const ServedJob& j = it->second;
+    const ServedJob* jp = sv->jobs.find(id);
+    if (!jp) return set_err(sv->c, WF_ERR_INVALID_ARGUMENT, "no such job");
+    const ServedJob& j = *jp;
     out->state = j.state;
     out->samples_done = j.samples_done;
     out->frames = j.frames;
@@ -1578,9 +1594,9 @@ int wf_server_status(wf_server* sv, int64_t id, wf_job_status* out)
 int wf_server_image(wf_server* sv, int64_t id, float* image, int64_t nf)
 {
     if (!sv || !image) return WF_ERR_INVALID_ARGUMENT;
-    auto it = sv->jobs.find(id);
-    if (it == sv->jobs.end()) return set_err(sv->c, WF_ERR_INVALID_ARGUMENT, "no such job");
-    ServedJob& j = it->second;
+    ServedJob* jp = sv->jobs.find(id);
+    if (!jp) return set_err(sv->c, WF_ERR_INVALID_ARGUMENT, "no such job");
+    ServedJob& j = *jp;
     if (nf < j.accum_floats) return set_err(sv->c, WF_ERR_CAPACITY, "image buffer too small");
     if (j.state == WF_JOB_DONE) {
         std::memcpy(image, j.final_image.data(), sizeof(float) * j.accum_floats);
@@ -1604,9 +1620,9 @@ int wf_server_image(wf_server* sv, int64_t id, float* image, int64_t nf)
 int wf_server_cancel(wf_server* sv, int64_t id)
 {
     if (!sv) return WF_ERR_INVALID_ARGUMENT;
-    auto it = sv->jobs.find(id);
-    if (it == sv->jobs.end()) return set_err(sv->c, WF_ERR_INVALID_ARGUMENT, "no such job");
-    ServedJob& j = it->second;
+    ServedJob* jp = sv->jobs.find(id);
+    if (!jp) return set_err(sv->c, WF_ERR_INVALID_ARGUMENT, "no such job");
+    ServedJob& j = *jp;
     if (j.state == WF_JOB_RUNNING) {
         // frames not started yet are dropped; frames already generating run
         // to their end and are discarded (their paths are in the queue)
@@ -1626,7 +1642,7 @@ int wf_server_cancel(wf_server* sv, int64_t id)
         int64_t end = cursor;
         for (const auto& k : sv->pending) end = std::max(end, k.path_offset + k.len);
         sv->appended = end;
-        sv->running.erase(std::remove(sv->running.begin(), sv->running.end(), id), sv->running.end());
+        sv->running--;
         if (j.chunks_out == 0) {
             sv->alloc.release(j.accum_off, j.accum_floats);
             j.accum_off = -1;
