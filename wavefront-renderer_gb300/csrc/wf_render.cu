@@ -1170,28 +1170,41 @@ __global__ void k_cb_reduce(ShadeColumnsDev c, const ull* __restrict__ d_n, doub
     if (staged)
         for (int m = threadIdx.x; m < num_materials; m += blockDim.x) s_benefit[m] = 0.0;
     __syncthreads();
+    __shared__ float s_lum[8][32];  // 256-thread blocks: one row per warp
     const int64_t n = (int64_t)*d_n;
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     unsigned mn[3] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu}, mx[3] = {0u, 0u, 0u};
     for (int64_t b = blockIdx.x * (int64_t)blockDim.x; b < n; b += (int64_t)gridDim.x * blockDim.x) {
         const int64_t i = b + threadIdx.x;
         const bool ok = i < n;
         const int m = ok ? c.mat[i] : -1;
         // luminance, include/render/AdaptiveSampler.h:21-27 (float), summed in double
-        const double l = ok ? (double)(0.2126f * c.tr[i] + 0.7152f * c.tg[i] + 0.0722f * c.tb[i]) : 0.0;
+        s_lum[warp][lane] = ok ? 0.2126f * c.tr[i] + 0.7152f * c.tg[i] + 0.0722f * c.tb[i] : 0.0f;
         const unsigned peers = __match_any_sync(0xFFFFFFFFu, m);
-        double sum = 0.0;
-        for (int k = 0; k < 32; ++k) {
-            const double v = __shfl_sync(0xFFFFFFFFu, l, k);
-            if ((peers >> k) & 1u) sum += v;
-        }
+        __syncwarp();
+        // The leader of each material's lanes sums their luminances in
+        // float-float (two-sum, then renormalised: ~2^-48 relative), one FP64
+        // add per group: a 32-step double loop per warp made this kernel wait
+        // on the FP64 pipe, which takes 16 cycles per warp-wide add here.
         if (ok && lane == __ffs(peers) - 1) {
+            float hi = 0.0f, lo = 0.0f;
+            for (unsigned rest = peers; rest; rest &= rest - 1) {
+                const float v = s_lum[warp][__ffs(rest) - 1];
+                const float s = hi + v;
+                const float bv = s - hi;
+                float e = (hi - (s - bv)) + (v - bv);
+                e += lo;
+                hi = s + e;
+                lo = e - (hi - s);
+            }
+            const double sum = (double)hi + (double)lo;
             if (staged)
                 atomicAdd(&s_benefit[m], sum);
             else
                 atomicAdd(&benefit[m], sum);
             present[m] = 1;
         }
+        __syncwarp();
         if (ok) {
             const float p3[3] = {c.px[i], c.py[i], c.pz[i]};
 #pragma unroll

@@ -47,8 +47,19 @@ __global__ void __launch_bounds__(kTile) k_hist(const uint64_t* __restrict__ key
     __syncthreads();
     int64_t start, end;
     chunk_of((int64_t)*d_n, nb, blockIdx.x, start, end);
-    for (int64_t i = start + threadIdx.x; i < end; i += kTile)
-        atomicAdd(&h[(uint32_t)(__ldg(keys + i) >> shift) & 0xFFu], 1u);
+    // one shared atomic per distinct digit of a warp: policy keys use a few
+    // digits, and lanes adding to one counter would queue behind each other
+    const unsigned lt = (1u << (threadIdx.x & 31)) - 1u;
+    for (int64_t b = start; b < end; b += kTile) {
+        const int64_t i = b + threadIdx.x;
+        const bool valid = i < end;
+        const unsigned vmask = __ballot_sync(0xFFFFFFFFu, valid);
+        if (valid) {
+            const uint32_t d = (uint32_t)(__ldg(keys + i) >> shift) & 0xFFu;
+            const unsigned peers = __match_any_sync(vmask, d);
+            if ((peers & lt) == 0u) atomicAdd(&h[d], (uint32_t)__popc(peers));
+        }
+    }
     __syncthreads();
     hist[(int64_t)threadIdx.x * nb + blockIdx.x] = h[threadIdx.x];
 }
@@ -74,12 +85,19 @@ __device__ __forceinline__ uint32_t block_exclusive_scan256(uint32_t v, uint32_t
     return before + x - v;
 }
 
-// Scatter of one digit pass.  A tile of 2048 keys is ranked in input order
-// (rounds of 256; within a round by warp, within a warp by __match_any_sync),
-// placed digit-sorted in shared memory, and written out in that order: the
-// keys of one digit leave a tile as one contiguous run, so the global writes
-// coalesce.  Stable: a key's position among equal digits follows its index.
-__global__ void __launch_bounds__(kTile) k_scatter(const uint64_t* __restrict__ kin,
+// Scatter of one digit pass.  A tile of 2048 keys: warp w ranks the 256 keys
+// [base + 256 w, base + 256 w + 256) in 8 rounds of 32 (coalesced loads); a
+// key's rank among its warp's equal digits comes from __match_any_sync and a
+// per-warp digit count in shared memory, updated warp-synchronously (no block
+// barrier per round).  Then per digit an exclusive scan over the 8 warps and
+// one over the 256 digits place every key in the tile, staged digit-sorted in
+// shared memory and written out as one contiguous run per digit, so the
+// global writes coalesce.  Stable: within a digit, keys keep their input
+// order (warp, round, lane).  Six block barriers per tile; ranking every
+// round across the block took thirty-seven.  Six resident blocks per SM (40
+// registers; at 64 only four fit, and the grid of six per SM ran in 1.5
+// waves).
+__global__ void __launch_bounds__(kTile, 6) k_scatter(const uint64_t* __restrict__ kin,
                                                    const uint32_t* __restrict__ vin,
                                                    uint64_t* __restrict__ kout,
                                                    uint32_t* __restrict__ vout,
@@ -87,11 +105,11 @@ __global__ void __launch_bounds__(kTile) k_scatter(const uint64_t* __restrict__ 
                                                    int shift, const uint32_t* __restrict__ offs,
                                                    int nb)
 {
+    constexpr int kWarps = kTile / 32;
     __shared__ uint32_t running[kDigits];
-    __shared__ uint32_t tile_cnt[kDigits];
     __shared__ uint32_t tile_start[kDigits];
-    __shared__ uint32_t wcnt[kTile / 32][kDigits];
-    __shared__ uint32_t warp_sums[kTile / 32];
+    __shared__ uint32_t wcnt[kWarps][kDigits];  // per-warp digit counts, then the warp's offsets
+    __shared__ uint32_t warp_sums[kWarps];
     __shared__ uint64_t skey[kTileKeys];
     __shared__ uint32_t sval[kTileKeys];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -100,57 +118,54 @@ __global__ void __launch_bounds__(kTile) k_scatter(const uint64_t* __restrict__ 
     int64_t start, end;
     chunk_of((int64_t)*d_n, nb, blockIdx.x, start, end);
     for (int64_t base = start; base < end; base += kTileKeys) {
-        tile_cnt[tid] = 0;
-#pragma unroll
-        for (int w = 0; w < kTile / 32; ++w) wcnt[w][tid] = 0;
-        __syncthreads();
+        for (int d = lane; d < kDigits; d += 32) wcnt[warp][d] = 0;  // this warp's row
+        __syncwarp();
         uint64_t key[kItems];
         uint32_t val[kItems], rank[kItems];
+        const int64_t wbase = base + (int64_t)warp * 32 * kItems;
 #pragma unroll
         for (int r = 0; r < kItems; ++r) {
-            const int64_t i = base + (int64_t)r * kTile + tid;
+            const int64_t i = wbase + (int64_t)r * 32 + lane;
             const bool valid = i < end;
             const unsigned vmask = __ballot_sync(0xFFFFFFFFu, valid);
-            uint32_t digit = 0;
-            int wrank = 0;
             key[r] = 0;
             val[r] = 0;
+            rank[r] = 0;
             if (valid) {
                 key[r] = kin[i];
                 val[r] = vin[i];
-                digit = (uint32_t)(key[r] >> shift) & 0xFFu;
+                const uint32_t digit = (uint32_t)(key[r] >> shift) & 0xFFu;
                 const unsigned peers = __match_any_sync(vmask, digit);
-                wrank = __popc(peers & lt);
-                if (wrank == 0) wcnt[warp][digit] = __popc(peers);
+                const uint32_t before = wcnt[warp][digit];
+                rank[r] = before + (uint32_t)__popc(peers & lt);
+                __syncwarp(vmask);  // every peer has read the count
+                if ((peers & lt) == 0u) wcnt[warp][digit] = before + (uint32_t)__popc(peers);
             }
-            __syncthreads();
-            uint32_t round_total = 0;
-#pragma unroll
-            for (int w = 0; w < kTile / 32; ++w) {
-                const uint32_t c = wcnt[w][tid];
-                wcnt[w][tid] = round_total;
-                round_total += c;
-            }
-            __syncthreads();
-            rank[r] = valid ? tile_cnt[digit] + wcnt[warp][digit] + (uint32_t)wrank : 0u;
-            __syncthreads();
-            tile_cnt[tid] += round_total;
-#pragma unroll
-            for (int w = 0; w < kTile / 32; ++w) wcnt[w][tid] = 0;
-            __syncthreads();
+            __syncwarp();
         }
-        tile_start[tid] = block_exclusive_scan256(tile_cnt[tid], warp_sums);
         __syncthreads();
-        const int tile_n = (int)min((int64_t)kTileKeys, end - base);
+        // thread = digit: the warps' offsets within the digit, the digit's total
+        uint32_t tot = 0;
+#pragma unroll
+        for (int w = 0; w < kWarps; ++w) {
+            const uint32_t c = wcnt[w][tid];
+            wcnt[w][tid] = tot;
+            tot += c;
+        }
+        const uint32_t first = block_exclusive_scan256(tot, warp_sums);
+        tile_start[tid] = first;
+        __syncthreads();
 #pragma unroll
         for (int r = 0; r < kItems; ++r) {
-            if (base + (int64_t)r * kTile + tid < end) {
-                const uint32_t pos = tile_start[(uint32_t)(key[r] >> shift) & 0xFFu] + rank[r];
+            if (wbase + (int64_t)r * 32 + lane < end) {
+                const uint32_t d = (uint32_t)(key[r] >> shift) & 0xFFu;
+                const uint32_t pos = tile_start[d] + wcnt[warp][d] + rank[r];
                 skey[pos] = key[r];
                 sval[pos] = val[r];
             }
         }
         __syncthreads();
+        const int tile_n = (int)min((int64_t)kTileKeys, end - base);
         for (int idx = tid; idx < tile_n; idx += kTile) {
             const uint64_t k = skey[idx];
             const uint32_t d = (uint32_t)(k >> shift) & 0xFFu;
@@ -159,8 +174,7 @@ __global__ void __launch_bounds__(kTile) k_scatter(const uint64_t* __restrict__ 
             vout[gpos] = sval[idx];
         }
         __syncthreads();
-        running[tid] += tile_cnt[tid];
-        __syncthreads();
+        running[tid] += tot;
     }
 }
 
