@@ -171,6 +171,9 @@ struct HitQueueDev {
     float* bu;      // barycentrics from Moller-Trumbore
     float* bv;
     int64_t capacity;
+    // Shading order (a policy's permutation): k_shade reads entry order[k]
+    // for its k-th hit; null = list order.
+    const uint32_t* order = nullptr;
 };
 
 // Queue columns of the bounce loop are written once and read once per bounce,

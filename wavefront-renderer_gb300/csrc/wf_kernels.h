@@ -143,8 +143,11 @@ struct ShadeColumnsMut {
     int32_t* tex;
     float *tr, *tg, *tb, *px, *py, *pz;
 };
-void launch_hit_columns(const DeviceScene* scenes, const DeviceJob* jobs, RayQueueDev rq, HitQueueDev hq,
-                        const ull* d_n, ShadeColumnsMut out, LaunchCfg cfg, cudaStream_t s);
+// full: the throughput and hit point columns too (costBenefit); scene: the
+// scene of every hit when the wave has one job (device pointer), else null.
+void launch_hit_columns(const DeviceScene* scenes, const DeviceJob* jobs, const DeviceScene* scene, bool full,
+                        RayQueueDev rq, HitQueueDev hq, const ull* d_n, ShadeColumnsMut out, LaunchCfg cfg,
+                        cudaStream_t s);
 void launch_permute_hits(HitQueueDev in, const uint32_t* perm, const ull* d_n, HitQueueDev out,
                          LaunchCfg cfg, cudaStream_t s);
 

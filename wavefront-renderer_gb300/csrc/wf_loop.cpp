@@ -203,7 +203,9 @@ int wave_host(wf_ctx* c, int64_t total, int max_depth, int policy, bool ray_sort
         }
         if (policy != WF_POLICY_NONE && hits >= (ull)c->tuning.sort_min_queue) {
             ShadeColumnsMut cm{c->col_mat, c->col_tex, c->col_tr, c->col_tg, c->col_tb, c->col_px, c->col_py, c->col_pz};
-            launch_hit_columns(c->d_scene_table, c->d_jobs, c->rq[cur], c->hq[0], c->counters + 1, cm, WC, s);
+            launch_hit_columns(c->d_scene_table, c->d_jobs, single_job ? c->d_scene_table + single_job->scene : nullptr,
+                               policy == WF_POLICY_COST_BENEFIT_AWARE, c->rq[cur], c->hq[0], c->counters + 1, cm, WC,
+                               s);
             ShadeColumnsDev cd{c->col_mat, c->col_tex, c->col_tr, c->col_tg, c->col_tb, c->col_px, c->col_py, c->col_pz};
             const ResidentScene& R = c->scenes[policy_scene];
             if (track_costs) {  // the trackers' state after the previous bounce
@@ -221,9 +223,20 @@ int wave_host(wf_ctx* c, int64_t total, int max_depth, int policy, bool ray_sort
             int rc = schedule_columns(c, policy, c->counters + 1, (int64_t)hits, cd, R.S.materials, R.S.num_materials,
                                       R.mats, R.S.num_textures, R.d_tex_bytes, R.tex_bytes, rc_mat, rc_tex, &perm);
             if (rc) return rc;
-            launch_permute_hits(c->hq[0], perm, c->counters + 1, c->hq[1], WC, s);
-            stats.kernel_launches += c->last_schedule_launches + 2;
-            hq_use = c->hq[1];
+            // ShadingQueue::materialize's gather.  A material or texture order
+            // keeps long runs of the list order (a stable sort by a few type and
+            // cost ranks), so k_shade reads the hits through the permutation
+            // (C2 material +5.8%, dense mesh material +8.7%); costBenefit's
+            // Morton sub-order scatters them, and a separate gather is faster
+            // there (shading through it measured 12 ms slower per C2 step).
+            if (policy == WF_POLICY_COST_BENEFIT_AWARE) {
+                launch_permute_hits(c->hq[0], perm, c->counters + 1, c->hq[1], WC, s);
+                stats.kernel_launches += c->last_schedule_launches + 2;
+                hq_use = c->hq[1];
+            } else {
+                stats.kernel_launches += c->last_schedule_launches + 1;
+                hq_use.order = perm;
+            }
             stats.sorted_elements += hits;
         }
         WF_CK(c, cudaEventRecord(ev[6], s));

@@ -659,8 +659,9 @@ __global__ void __launch_bounds__(128, (kMulti || kTimed) ? WF_SHADE_MIN_BLOCKS 
         int cost_mat = -1, cost_tex = -1;
         unsigned cyc_mat = 0, cyc_tex = 0;
         if (active) {
-            const int ri = ldq(&hq.ray[k]);
-            const int64_t hk = ray_order ? (int64_t)ri : k;
+            const int64_t pk = hq.order ? (int64_t)hq.order[k] : k;
+            const int ri = ldq(&hq.ray[pk]);
+            const int64_t hk = ray_order ? (int64_t)ri : pk;
             job = kMulti ? ldq(&rq.job[ri]) : 0;
             const DeviceJob& J = kMulti ? jobs[job] : job0;
             const DeviceScene& S = kMulti ? scenes[J.scene] : scene0;
@@ -1267,19 +1268,25 @@ __global__ void k_cb_keys(ShadeColumnsDev c, const ull* __restrict__ d_n,
     }
 }
 
+// kFull: also the throughput and hit point (costBenefit's benefit and Morton
+// keys); the material and texture policies read only the ids (C2 material
+// schedule: the full columns took 8.5 of its 17.6 ms per step).  scene:
+// every hit's scene when the wave has one job, else null (looked up per ray).
+template <bool kFull>
 __global__ void k_hit_columns(const DeviceScene* __restrict__ scenes, const DeviceJob* __restrict__ jobs,
-                              RayQueueDev rq, HitQueueDev hq, const ull* __restrict__ d_n,
-                              ShadeColumnsMut out)
+                              const DeviceScene* __restrict__ scene, RayQueueDev rq, HitQueueDev hq,
+                              const ull* __restrict__ d_n, ShadeColumnsMut out)
 {
     const int64_t n = (int64_t)*d_n;
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
          k += (int64_t)gridDim.x * blockDim.x) {
-        const int ri = hq.ray[k];
-        const DeviceScene& S = scenes[jobs[rq.job[ri]].scene];
+        const int ri = (kFull || !scene) ? hq.ray[k] : 0;
+        const DeviceScene& S = scene ? *scene : scenes[jobs[rq.job[ri]].scene];
         const float4 b = __ldg(S.tris + 3 * (int64_t)hq.tri[k] + 1);
         const int m = S.mesh_material[__float_as_int(b.w)];
         out.mat[k] = m;
         out.tex[k] = S.materials[m].texture_id;
+        if (!kFull) continue;
         out.tr[k] = rq.tr[ri];
         out.tg[k] = rq.tg[ri];
         out.tb[k] = rq.tb[ri];
@@ -1764,10 +1771,14 @@ void launch_cb_keys(ShadeColumnsDev c, const ull* d_n, const wf_material* mats,
     k_cb_keys<<<cfg.grid, 256, 0, s>>>(c, d_n, mats, prio_rank, prio_bits, bounds6, keys, vals);
 }
 
-void launch_hit_columns(const DeviceScene* scenes, const DeviceJob* jobs, RayQueueDev rq, HitQueueDev hq,
-                        const ull* d_n, ShadeColumnsMut out, LaunchCfg cfg, cudaStream_t s)
+void launch_hit_columns(const DeviceScene* scenes, const DeviceJob* jobs, const DeviceScene* scene, bool full,
+                        RayQueueDev rq, HitQueueDev hq, const ull* d_n, ShadeColumnsMut out, LaunchCfg cfg,
+                        cudaStream_t s)
 {
-    k_hit_columns<<<cfg.grid, 256, 0, s>>>(scenes, jobs, rq, hq, d_n, out);
+    if (full)
+        k_hit_columns<true><<<cfg.grid, 256, 0, s>>>(scenes, jobs, scene, rq, hq, d_n, out);
+    else
+        k_hit_columns<false><<<cfg.grid, 256, 0, s>>>(scenes, jobs, scene, rq, hq, d_n, out);
 }
 
 void launch_permute_hits(HitQueueDev in, const uint32_t* perm, const ull* d_n, HitQueueDev out,

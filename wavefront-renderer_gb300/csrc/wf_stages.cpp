@@ -524,7 +524,8 @@ int wf_shading_queue_schedule(wf_shading_queue* q, int32_t policy, const double*
         q->at_ray = false;
     }
     ShadeColumnsMut cm{c->col_mat, c->col_tex, c->col_tr, c->col_tg, c->col_tb, c->col_px, c->col_py, c->col_pz};
-    launch_hit_columns(c->d_scene_table, c->d_jobs, q->rays, q->h[q->cur], q->counts, cm, WC, s);
+    launch_hit_columns(c->d_scene_table, c->d_jobs, nullptr, policy == WF_POLICY_COST_BENEFIT_AWARE, q->rays,
+                       q->h[q->cur], q->counts, cm, WC, s);
     ShadeColumnsDev cd{c->col_mat, c->col_tex, c->col_tr, c->col_tg, c->col_tb, c->col_px, c->col_py, c->col_pz};
     const ResidentScene& R = c->scenes[0];
     uint32_t* perm = nullptr;
