@@ -565,9 +565,8 @@ def main() -> int:
     ap.add_argument("--blocks-per-sm", type=int, default=0)
     ap.add_argument("--ref-rows", type=int, default=REF_ROWS, help="CPU legs: rows of the timed band")
     ap.add_argument("--ref-spp", type=int, default=REF_SPP, help="CPU legs: samples per pixel of the timed band")
-    ap.add_argument("--bvh", default="ploc", choices=["ploc", "lbvh", "wide", "ploc4", "ploc_sah"])
+    ap.add_argument("--bvh", default="ploc", choices=["ploc", "lbvh", "ploc4", "ploc_sah"])
     ap.add_argument("--autotune", type=int, default=0, help="run wf_autotune on the workload before timing")
-    ap.add_argument("--speculative", type=int, default=0, help="1 = speculative while-while traversal")
     ap.add_argument("--adaptive", type=int, default=0, help="the reference's adaptive sampling (threshold 0.05)")
     ap.add_argument("--ray-sort-bits", type=int, default=0, help="key bits of the loop's ray sort (0 = 33)")
     ap.add_argument("--cost-rr", type=int, default=0, help="cost-aware RR fed by the live device CostTracker")
@@ -601,8 +600,7 @@ def main() -> int:
     ctx = pkg.Context(local)
     scene = pkg.HostScene(wl["config"])
     ctx.set_tuning(max(args.trace_variant, 0), args.blocks_per_sm,
-                   bvh_builder={"ploc": 0, "lbvh": 1, "wide": 2, "ploc4": 3, "ploc_sah": 4}[args.bvh],
-                   speculative_traversal=args.speculative,
+                   bvh_builder={"ploc": 0, "lbvh": 1, "ploc4": 3, "ploc_sah": 4}[args.bvh],
                    ray_sort_bits=args.ray_sort_bits)
     info = ctx.upload(scene.desc)
     W, H = wl["width"], wl["height"]
@@ -709,7 +707,7 @@ def main() -> int:
         "clocks": clocks,
         "gpu_launches": int(sum(s["kernel_launches"] for s in stats)),
         "bvh_build_ms": info.bvh_build_ms,
-        "bvh": {"builder": ["ploc", "lbvh", "ploc_wide8", "ploc4", "ploc_sah_leaves"][info.bvh_builder],
+        "bvh": {"builder": {0: "ploc", 1: "lbvh", 3: "ploc4", 4: "ploc_sah_leaves"}[info.bvh_builder],
                 "nodes": info.bvh_nodes,
                 "depth": info.bvh_depth},
         "tuning": dict(ctx.get_tuning(), autotuned=bool(args.autotune), autotune_wave_ms=tune_ms),

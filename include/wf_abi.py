@@ -112,7 +112,7 @@ class WfSceneInfo(C.Structure):
 
 class WfTuning(C.Structure):
     _fields_ = [("trace_variant", C.c_int32), ("persistent_blocks_per_sm", C.c_int32), ("graph_mode", C.c_int32),
-                ("bvh_builder", C.c_int32), ("sort_min_queue", C.c_int32), ("speculative_traversal", C.c_int32),
+                ("bvh_builder", C.c_int32), ("sort_min_queue", C.c_int32), ("reserved2", C.c_int32),
                 ("reserved", C.c_int32), ("ray_sort_bits", C.c_int32)]
 
 

@@ -275,12 +275,9 @@ int wf_scene_get_info(wf_ctx* ctx, wf_scene_info* out_info);
 
 /* Launch tuning of a context (the autotuner's knobs).  trace_variant: 0 = no
  * occupancy hint on the traversal kernels (the closest-hit kernel of a
- * single-job render whose binary tree and triangles exceed L2 runs as 1),
- * 1 = 9 blocks of 128 threads per SM (56 registers, no spills), 2 = the
- * traversal stack's bottom 6 entries in shared memory and the rest in local
- * memory (stack placement; binary trees, 3 KB per block), 3 = the binary
- * tree's top 31 nodes staged in shared memory once per block (node staging;
- * single-scene renders, else 0).  Variants 2 and 3 run 8 blocks per SM.
+ * single-job render whose binary tree and triangles exceed L2, and multi-job
+ * waves over a dense scene, run as 1), 1 = 9 blocks of 128 threads per SM
+ * (56 registers, no spills).
  * persistent_blocks_per_sm: resident blocks launched per
  * SM by the persistent traversal kernels (0 = 16).  graph_mode: whether a
  * wave's bounce chain is captured once as a CUDA graph and replayed. */
@@ -293,23 +290,21 @@ typedef struct wf_tuning {
                             bounces with device-side counts, as a single
                             render does */
     int32_t bvh_builder; /* scenes uploaded afterwards: 0 = PLOC binary tree
-                            (locally-ordered clustering, default), 1 = LBVH
-                            binary tree (Karras radix tree), 2 = the PLOC tree
-                            collapsed into compressed 8-wide nodes, 3 = the
-                            PLOC tree collapsed into 4-wide nodes (full-
-                            precision boxes, 128 bytes each), 4 = the PLOC
-                            binary tree with leaves chosen by the surface
-                            area heuristic (large triangles get leaves of
-                            their own); a PLOC tree deeper than its traversal
-                            stack falls back to LBVH */
+                            (locally-ordered clustering, default; leaves by
+                            the surface area heuristic below 4096 triangles,
+                            else every subtree of <= 4 triangles), 1 = LBVH
+                            binary tree (Karras radix tree), 3 = the PLOC tree
+                            collapsed into 4-wide nodes (full-precision boxes,
+                            128 bytes each), 4 = the PLOC binary tree with
+                            surface-area leaves at any size (2, a compressed
+                            8-wide tree, was taken out); a PLOC tree deeper
+                            than its traversal stack falls back to LBVH */
     int32_t sort_min_queue; /* sort-or-skip: the ray sort and the shading
                             policies run on a bounce only when its queue holds
                             at least this many entries (0 = always, as the
                             reference does); skipping reorders nothing that
                             changes the image */
-    int32_t speculative_traversal; /* 0 = while-while traversal (default);
-                            1 = speculative while-while (lanes postpone their
-                            first leaf until every lane of the warp has one) */
+    int32_t reserved2;   /* must be 0 */
     int32_t reserved;    /* must be 0 */
     int32_t ray_sort_bits; /* the render loop's ray sort uses the top bits of
                             RayQueue::sortKey's 33 (0 = all 33; fewer bits =
@@ -321,10 +316,9 @@ int wf_get_tuning(const wf_ctx* ctx, wf_tuning* out_tuning);
 
 /* Autotuner (no reference counterpart): renders one wave of `params` on the
  * current scene (samples capped at one wave, adaptive sampling and cost
- * tracking off) under every combination of trace_variant {0, 1, 2, 3}
- * (block occupancy, stack placement, node staging), persistent_blocks_per_sm
- * {4, 8, 12, 16, 24}, graph_mode {2, 1} and speculative_traversal {0, 1}, each
- * once untimed and twice
+ * tracking off) under every combination of trace_variant {0, 1} (block
+ * occupancy), persistent_blocks_per_sm {4, 8, 12, 16, 24} and graph_mode
+ * {2, 1}, each once untimed and twice
  * timed on the device; then, when params sort rays or shading, the
  * sort-or-skip threshold sort_min_queue over {0, 2^18, 2^20, 2^22, never}
  * and, with the ray sort on, its key width ray_sort_bits over {24, 16}, with

@@ -35,10 +35,9 @@ def _same(a, b):
     return np.isclose(a, b, rtol=1e-4, atol=1e-6).all(axis=2).mean()
 
 
-@pytest.mark.parametrize("variant", [0, 2])
+@pytest.mark.parametrize("variant", [0, 1])
 def test_batch_job_equals_job_alone(wf, ctx, variant):
-    """Variant 2 runs the multi-job traversal with its stack's bottom entries
-    in shared memory."""
+    """Variant 1 runs the multi-job traversal at 9 resident blocks per SM."""
     ctx.set_tuning(trace_variant=variant)
     try:
         jobs, hosts = _jobs(wf, ctx, 12)

@@ -295,15 +295,13 @@ def test_render_is_order_independent(wf, ctx, scene_small, scene_c2small, which)
         img, _ = ctx.render(wf.render_params(W, H, 8, 12, cam, seed=5, **kw))
         agree = np.isclose(img, base, rtol=1e-4, atol=1e-6).all(axis=2).mean()
         assert agree >= 0.999, (kw, agree)
-    # launch tuning: occupancy variant, stack placement in shared memory, top
-    # nodes staged in shared memory, speculative traversal, grid size, graph
-    # replay and the sort-or-skip threshold change no pixel beyond that.
+    # launch tuning: occupancy variant, grid size, graph replay and the
+    # sort-or-skip threshold change no pixel beyond that.
     # The base render issues its bounces back to back with device-side counts;
     # a sort-or-skip threshold sends policy none through the loop that waits
     # for each bounce's counts on the host, graph_mode=1 through graph replay.
     try:
-        for tune, kw in [(dict(trace_variant=1), {}), (dict(trace_variant=2), {}), (dict(trace_variant=3), {}),
-                         (dict(trace_variant=2, speculative_traversal=1), {}), (dict(speculative_traversal=1), {}),
+        for tune, kw in [(dict(trace_variant=1), {}),
                          (dict(ray_sort_bits=16), dict(ray_sort=True)),
                          (dict(persistent_blocks_per_sm=4), {}), (dict(graph_mode=1), {}),
                          (dict(sort_min_queue=6000), dict(policy=1, ray_sort=True)),
@@ -316,9 +314,9 @@ def test_render_is_order_independent(wf, ctx, scene_small, scene_c2small, which)
         ctx.set_tuning()
 
 
-@pytest.mark.parametrize("builder", [2, 3, 4])
+@pytest.mark.parametrize("builder", [3, 4])
 def test_tree_formats_render_the_same_image(wf, ctx, scene_c2small, builder):
-    """The 8-wide, 4-wide and surface-area-leaf trees return the binary tree's hits, so a render
+    """The 4-wide and surface-area-leaf trees return the binary tree's hits, so a render
     over them (plain launches, graph replay, every launch variant) gives the
     binary tree's image up to float-add order (1e-4 relative, 99.9% of
     pixels).  A context of its own: the resident scenes of one context share
@@ -332,7 +330,7 @@ def test_tree_formats_render_the_same_image(wf, ctx, scene_c2small, builder):
         other.set_tuning(bvh_builder=builder)
         info = other.upload(scene_c2small.desc)
         assert info.bvh_builder == builder
-        for tune in [{}, dict(graph_mode=1), dict(trace_variant=1), dict(speculative_traversal=1)]:
+        for tune in [{}, dict(graph_mode=1), dict(trace_variant=1)]:
             other.set_tuning(bvh_builder=builder, **tune)
             img, st = other.render(wf.render_params(W, H, 8, 8, cam, seed=13))
             agree = np.isclose(img, base, rtol=1e-4, atol=1e-6).all(axis=2).mean()
@@ -349,7 +347,7 @@ def test_autotune_picks_a_valid_tuning(wf, ctx, scene_small):
     try:
         tuning, ms = ctx.autotune(p)
         assert ms > 0
-        assert tuning["trace_variant"] in (0, 1, 2, 3) and tuning["persistent_blocks_per_sm"] in (4, 8, 12, 16, 24)
+        assert tuning["trace_variant"] in (0, 1) and tuning["persistent_blocks_per_sm"] in (4, 8, 12, 16, 24)
         assert tuning["sort_min_queue"] in (0, 1 << 18, 1 << 20, 1 << 22, 2**31 - 1)
         assert ctx.get_tuning() == tuning
         img, _ = ctx.render(p)
@@ -609,10 +607,10 @@ def test_gpu_live_costs_only_reorder_shading(wf, ctx, scene_c2small, policy):
 
 @pytest.mark.parametrize("which", ["c0", "small", "c2small"])
 def test_bvh_builders_give_identical_hits(wf, orc, ctx, scene0, scene_small, scene_c2small, which):
-    """The binary PLOC tree, the LBVH, the compressed 8-wide and the 4-wide
-    PLOC trees and the PLOC tree with surface-area leaves return the same
-    closest hits and occlusion bit for bit (and the port's), and each passes
-    the build's structural check."""
+    """The binary PLOC tree (default leaves), the LBVH, the 4-wide PLOC tree
+    and the PLOC tree with surface-area leaves return the same closest hits
+    and occlusion bit for bit (and the port's), and each passes the build's
+    structural check."""
     scene = {"c0": scene0, "small": scene_small, "c2small": scene_c2small}[which]
     rng = np.random.default_rng(21)
     lo, hi = ([0.0, 0.01, 0.0], [16.0, 0.9, 16.0]) if which == "c2small" else \
@@ -624,7 +622,7 @@ def test_bvh_builders_give_identical_hits(wf, orc, ctx, scene0, scene_small, sce
     want_occ = port.trace_occluded(o, d, maxd)
     infos = []
     try:
-        for builder in (0, 1, 2, 3, 4):
+        for builder in (0, 1, 3, 4):
             ctx.set_tuning(bvh_builder=builder)
             infos.append(ctx.upload(scene.desc))
             got = ctx.trace_closest(o, d)
@@ -633,10 +631,9 @@ def test_bvh_builders_give_identical_hits(wf, orc, ctx, scene0, scene_small, sce
             assert np.array_equal(ctx.trace_occluded(o, d, maxd), want_occ), builder
     finally:
         ctx.set_tuning()
-    assert [i.bvh_builder for i in infos] == [0, 1, 2, 3, 4]
-    assert infos[2].bvh_nodes < infos[0].bvh_nodes  # the 8-wide tree has fewer nodes
-    assert infos[3].bvh_nodes < infos[0].bvh_nodes  # so has the 4-wide one
-    assert infos[3].bvh_depth < infos[0].bvh_depth
+    assert [i.bvh_builder for i in infos] == [0, 1, 3, 4]
+    assert infos[2].bvh_nodes < infos[0].bvh_nodes  # the 4-wide tree has fewer nodes
+    assert infos[2].bvh_depth < infos[0].bvh_depth
 
 
 @pytest.mark.parametrize("ntri", [1, 2, 4, 5, 9, 33])
@@ -664,7 +661,7 @@ def test_bvh_builders_on_tiny_scenes(wf, orc, ntri):
     want = port.trace_closest(o, d)
     want_occ = port.trace_occluded(o, d, maxd)
     assert (want["prim_id"] >= 0).mean() > 0.3
-    for builder in (0, 1, 2, 3, 4):
+    for builder in (0, 1, 3, 4):
         c2 = wf.Context(0)
         try:
             c2.set_tuning(bvh_builder=builder)

@@ -534,10 +534,9 @@ class Context:
         return out
 
     def set_tuning(self, trace_variant: int = 0, persistent_blocks_per_sm: int = 0, graph_mode: int = 0,
-                   bvh_builder: int = 0, sort_min_queue: int = 0, speculative_traversal: int = 0,
-                   ray_sort_bits: int = 0) -> None:
-        t = WfTuning(trace_variant, persistent_blocks_per_sm, graph_mode, bvh_builder, sort_min_queue,
-                     speculative_traversal, 0, ray_sort_bits)
+                   bvh_builder: int = 0, sort_min_queue: int = 0, ray_sort_bits: int = 0) -> None:
+        t = WfTuning(trace_variant, persistent_blocks_per_sm, graph_mode, bvh_builder, sort_min_queue, 0, 0,
+                     ray_sort_bits)
         _check(load_library().wf_set_tuning(self._h, C.byref(t)), "wf_set_tuning", self)
 
     def autotune(self, params: WfRenderParams) -> tuple[dict, float]:
@@ -553,7 +552,7 @@ class Context:
         _check(load_library().wf_get_tuning(self._h, C.byref(t)), "wf_get_tuning", self)
         return {"trace_variant": t.trace_variant, "persistent_blocks_per_sm": t.persistent_blocks_per_sm,
                 "graph_mode": t.graph_mode, "bvh_builder": t.bvh_builder, "sort_min_queue": t.sort_min_queue,
-                "speculative_traversal": t.speculative_traversal, "ray_sort_bits": t.ray_sort_bits}
+                "ray_sort_bits": t.ray_sort_bits}
 
     def add_scene(self, desc: WfSceneDesc) -> int:
         sid = C.c_int32()

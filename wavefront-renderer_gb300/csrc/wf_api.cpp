@@ -58,7 +58,6 @@ LaunchCfg persist_cfg(const wf_ctx* c)
     int per_sm = c->tuning.persistent_blocks_per_sm > 0 ? c->tuning.persistent_blocks_per_sm : 16;
     LaunchCfg cfg{c->num_sms * per_sm, 128};
     cfg.variant = c->tuning.trace_variant;
-    cfg.speculative = c->tuning.speculative_traversal;
     cfg.l2_bytes = c->l2_bytes;
     if (c->wave_scene_bytes >= 0 && c->wave_lean >= 0) {
         cfg.max_scene_bytes = c->wave_scene_bytes;
@@ -424,10 +423,13 @@ int check_device_flag(wf_ctx* c)
 
 namespace {
 
+// Default builder: scenes below this many triangles get surface-area leaves.
+constexpr int kSahLeafTriangles = 4096;
+
 // Bytes per node of a built tree's format.
 size_t tree_node_bytes(const BvhBuildOutput& b)
 {
-    return b.wnodes ? sizeof(WideNode) : (b.nodes4 ? sizeof(Bvh4Node) : sizeof(BvhNode));
+    return b.nodes4 ? sizeof(Bvh4Node) : sizeof(BvhNode);
 }
 
 // srgbToLinear, reference src/shading/Texture.cpp:20-27.
@@ -601,11 +603,12 @@ int build_scene(wf_ctx* c, const wf_scene_desc* D, ResidentScene& R)
         auto b0 = std::chrono::steady_clock::now();
         int brc = -1;
         if (c->tuning.bvh_builder == 0) {
-            brc = build_ploc(bi, bo, c->num_sms, s, err);
+            // Scenes of few triangles (the Cornell-box workloads, whose wall
+            // triangles dwarf the rest) get leaves by the surface area
+            // heuristic (Cornell box +4.6%); dense scenes keep leaves of up to
+            // four triangles (dense mesh with SAH leaves: -1.4%).
+            brc = build_ploc(bi, bo, c->num_sms, s, err, ntri < kSahLeafTriangles);
             R.info.bvh_builder = 0;
-        } else if (c->tuning.bvh_builder == 2) {
-            brc = build_ploc_wide(bi, bo, c->num_sms, s, err);
-            R.info.bvh_builder = 2;
         } else if (c->tuning.bvh_builder == 3) {
             brc = build_ploc4(bi, bo, c->num_sms, s, err);
             R.info.bvh_builder = 3;
@@ -629,25 +632,19 @@ int build_scene(wf_ctx* c, const wf_scene_desc* D, ResidentScene& R)
             if (cudaMalloc(&pool, node_bytes + tri_bytes) != cudaSuccess) {
                 cudaFree(bo.tris);
                 cudaFree(bo.nodes);
-                cudaFree(bo.wnodes);
                 cudaFree(bo.nodes4);
                 free_scene_res(R);
                 return set_err(c, WF_ERR_OUT_OF_MEMORY, "BVH pool allocation failed");
             }
-            const void* src_nodes = bo.wnodes   ? (const void*)bo.wnodes
-                                    : bo.nodes4 ? (const void*)bo.nodes4
-                                                : (const void*)bo.nodes;
+            const void* src_nodes = bo.nodes4 ? (const void*)bo.nodes4 : (const void*)bo.nodes;
             cudaMemcpyAsync(pool, src_nodes, node_bytes, cudaMemcpyDeviceToDevice, s);
             cudaMemcpyAsync(pool + node_bytes, bo.tris, tri_bytes, cudaMemcpyDeviceToDevice, s);
             cudaStreamSynchronize(s);
             cudaFree(bo.tris);
             cudaFree(bo.nodes);
-            cudaFree(bo.wnodes);
             cudaFree(bo.nodes4);
             bo.tris = reinterpret_cast<float4*>(pool + node_bytes);
-            if (bo.wnodes)
-                bo.wnodes = reinterpret_cast<WideNode*>(pool);
-            else if (bo.nodes4)
+            if (bo.nodes4)
                 bo.nodes4 = reinterpret_cast<Bvh4Node*>(pool);
             else
                 bo.nodes = reinterpret_cast<BvhNode*>(pool);
@@ -660,7 +657,6 @@ int build_scene(wf_ctx* c, const wf_scene_desc* D, ResidentScene& R)
     }
     S.tris = bo.tris;
     S.nodes = bo.nodes;
-    S.wnodes = bo.wnodes;
     S.nodes4 = bo.nodes4;
     S.num_tris = ntri;
     S.num_nodes = bo.num_nodes;
@@ -1230,8 +1226,9 @@ int wf_get_stream(wf_ctx* c, void** out)
 int wf_set_tuning(wf_ctx* c, const wf_tuning* t)
 {
     if (!c || !t) return WF_ERR_INVALID_ARGUMENT;
-    if (t->trace_variant < 0 || t->trace_variant > 3 || t->persistent_blocks_per_sm < 0 ||
-        t->persistent_blocks_per_sm > 32 || t->bvh_builder < 0 || t->bvh_builder > 4)
+    if (t->trace_variant < 0 || t->trace_variant > 1 || t->persistent_blocks_per_sm < 0 ||
+        t->persistent_blocks_per_sm > 32 || t->bvh_builder < 0 || t->bvh_builder > 4 || t->bvh_builder == 2 ||
+        t->reserved2 != 0 || t->reserved != 0)
         return set_err(c, WF_ERR_INVALID_ARGUMENT, "tuning out of range");
     c->tuning = *t;
     return WF_OK;

@@ -714,107 +714,6 @@ __global__ void k_wide_gather_sah(const int* __restrict__ items, int count, int 
     }
 }
 
-// Smallest power-of-two step 2^e (e in [-126, 127]) with lo + 255 * 2^e >= hi.
-__device__ __forceinline__ int wide_exponent(float lo, float hi)
-{
-    const double ext = (double)hi - (double)lo;
-    int e = -126;
-    if (ext > 0.0) e = max(-126, min(127, (int)ceil(log2(ext / 255.0))));
-    while (e < 127 && (double)lo + 255.0 * ldexp(1.0, e) < (double)hi) ++e;
-    return e;
-}
-
-__global__ void k_wide_emit(const int* __restrict__ items, int count, int level_base, int next_base, int tri_base0,
-                            const int* __restrict__ kids, const int* __restrict__ int_off,
-                            const int* __restrict__ tri_off, int num_tris, const int* __restrict__ cnt,
-                            const float* __restrict__ nbox, const int* __restrict__ offset,
-                            const uint32_t* __restrict__ final_ids, WideNode* __restrict__ wn,
-                            int* __restrict__ next_items, uint32_t* __restrict__ wide_ids)
-{
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
-        int ch[8];
-        int m = 0;
-        for (int i = 0; i < 8; ++i) {
-            const int c = kids[8 * (int64_t)k + i];
-            if (c >= 0) ch[m++] = c;
-        }
-        // padded child boxes and the node box
-        float bx[8][6];
-        float lo[3] = {3.0e38f, 3.0e38f, 3.0e38f}, hi[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
-        for (int i = 0; i < m; ++i) {
-            for (int a = 0; a < 6; ++a) bx[i][a] = nbox[6 * (int64_t)ch[i] + a];
-            pad_box(bx[i]);
-            for (int a = 0; a < 3; ++a) {
-                lo[a] = fminf(lo[a], bx[i][a]);
-                hi[a] = fmaxf(hi[a], bx[i][a + 3]);
-            }
-        }
-        // slot q takes the child nearest for rays of direction octant q
-        // (greedy on dot(child centre - node centre, octant direction))
-        int slot_child[8];
-        for (int q = 0; q < 8; ++q) slot_child[q] = -1;
-        bool placed[8] = {false, false, false, false, false, false, false, false};
-        for (int round = 0; round < m; ++round) {
-            float best = 3.0e38f;
-            int bi = -1, bs = -1;
-            for (int i = 0; i < m; ++i) {
-                if (placed[i]) continue;
-                const float cx = 0.5f * (bx[i][0] + bx[i][3]) - 0.5f * (lo[0] + hi[0]);
-                const float cy = 0.5f * (bx[i][1] + bx[i][4]) - 0.5f * (lo[1] + hi[1]);
-                const float cz = 0.5f * (bx[i][2] + bx[i][5]) - 0.5f * (lo[2] + hi[2]);
-                for (int q = 0; q < 8; ++q) {
-                    if (slot_child[q] >= 0) continue;
-                    const float cost = ((q & 1) ? -cx : cx) + ((q & 2) ? -cy : cy) + ((q & 4) ? -cz : cz);
-                    if (bi < 0 || cost < best) {
-                        best = cost;
-                        bi = i;
-                        bs = q;
-                    }
-                }
-            }
-            placed[bi] = true;
-            slot_child[bs] = bi;
-        }
-        WideNode nd;
-        uint8_t* raw = reinterpret_cast<uint8_t*>(&nd);
-        for (int a = 0; a < (int)sizeof(WideNode); ++a) raw[a] = 0;
-        double scale[3];
-        for (int a = 0; a < 3; ++a) {
-            const int e = wide_exponent(lo[a], hi[a]);
-            nd.p[a] = lo[a];
-            nd.e[a] = (uint8_t)(e + 127);
-            scale[a] = ldexp(1.0, e);
-        }
-        const uint32_t child_base = (uint32_t)(next_base + int_off[k]);
-        const uint32_t tri_base = (uint32_t)(tri_base0 + tri_off[k]);
-        nd.child_base = child_base;
-        nd.tri_base = tri_base;
-        int irank = 0, toff = 0;
-        for (int q = 0; q < 8; ++q) {
-            const int i = slot_child[q];
-            if (i < 0) continue;
-            const int c = ch[i];
-            if (cnt[c] > kWideLeafMax) {
-                nd.meta[q] = (uint8_t)(0x20 | (24 + q));
-                nd.imask |= (uint8_t)(1u << q);
-                next_items[child_base - next_base + irank] = c;
-                ++irank;
-            } else {
-                const int nc = cnt[c];
-                nd.meta[q] = (uint8_t)((((1u << nc) - 1u) << 5) | (uint32_t)toff);
-                for (int j = 0; j < nc; ++j) wide_ids[tri_base + toff + j] = final_ids[offset[c] + j];
-                toff += nc;
-            }
-            for (int a = 0; a < 3; ++a) {
-                const double ql = floor(((double)bx[i][a] - (double)lo[a]) / scale[a]);
-                const double qh = ceil(((double)bx[i][a + 3] - (double)lo[a]) / scale[a]);
-                nd.qlo[a][q] = (uint8_t)fmin(255.0, fmax(0.0, ql));
-                nd.qhi[a][q] = (uint8_t)fmin(255.0, fmax(0.0, qh));
-            }
-        }
-        wn[level_base + k] = nd;
-    }
-}
 
 // One level of 4-wide nodes: padded child boxes at full precision, interior
 // children numbered from next_base in the order of the level's items, leaf
@@ -871,33 +770,6 @@ __global__ void k_four_emit(const int* __restrict__ items, int count, int level_
 // and triangle range must lie inside the arrays (a failed check rejects the
 // tree; the traversal kernels then never see it).
 // ---------------------------------------------------------------------------
-__global__ void k_validate_wide(const WideNode* __restrict__ wn, int num_nodes, int num_tris, int* __restrict__ bad)
-{
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < num_nodes; i += gridDim.x * blockDim.x) {
-        const WideNode& nd = wn[i];
-        const int ni = __popc((unsigned)nd.imask);
-        bool ok = true;
-        if (ni > 0) ok = ok && nd.child_base > (uint32_t)i && (int64_t)nd.child_base + ni <= (int64_t)num_nodes;
-        for (int a = 0; a < 3; ++a) ok = ok && nd.e[a] >= 1 && nd.e[a] <= 254;
-        for (int q = 0; q < 8; ++q) {
-            const uint32_t m = nd.meta[q];
-            const bool interior = ((nd.imask >> q) & 1u) != 0;
-            if (m == 0) {
-                ok = ok && !interior;
-                continue;
-            }
-            if ((m & 0x1Fu) >= 24u) {
-                ok = ok && interior && (m & 0x1Fu) == 24u + (uint32_t)q && (m >> 5) == 1u;
-            } else {
-                const uint32_t u = m >> 5, off = m & 0x1Fu;
-                const int c = u == 1u ? 1 : (u == 3u ? 2 : (u == 7u ? 3 : 0));
-                ok = ok && !interior && c > 0 && off + (uint32_t)c <= 24u &&
-                     (int64_t)nd.tri_base + off + c <= (int64_t)num_tris;
-            }
-        }
-        if (!ok) atomicOr(bad, 1);
-    }
-}
 
 __global__ void k_validate_binary(const BvhNode* __restrict__ nodes, int num_nodes, int num_tris, int* __restrict__ bad)
 {
@@ -951,9 +823,7 @@ int validate_tree(const BvhBuildOutput& out, int num_tris, int num_sms, cudaStre
         return -1;
     }
     cudaMemsetAsync(d_bad, 0, sizeof(int), s);
-    if (out.wnodes)
-        k_validate_wide<<<num_sms * 8, 256, 0, s>>>(out.wnodes, out.num_nodes, num_tris, d_bad);
-    else if (out.nodes4)
+    if (out.nodes4)
         k_validate_four<<<num_sms * 8, 256, 0, s>>>(out.nodes4, out.num_nodes, num_tris, d_bad);
     else if (out.nodes)
         k_validate_binary<<<num_sms * 8, 256, 0, s>>>(out.nodes, out.num_nodes, num_tris, d_bad);
@@ -1239,7 +1109,6 @@ int build_ploc(const BvhBuildInput& in, BvhBuildOutput& out, int num_sms, cudaSt
     const int n = in.num_tris;
     out.tris = nullptr;
     out.nodes = nullptr;
-    out.wnodes = nullptr;
     out.num_nodes = 0;
     out.max_depth = 0;
     if (n <= 0) return 0;
@@ -1303,110 +1172,11 @@ fail:
     return -1;
 }
 
-int build_ploc_wide(const BvhBuildInput& in, BvhBuildOutput& out, int num_sms, cudaStream_t s, std::string& err)
-{
-    const int n = in.num_tris;
-    out.tris = nullptr;
-    out.nodes = nullptr;
-    out.wnodes = nullptr;
-    out.num_nodes = 0;
-    out.max_depth = 0;
-    if (n <= 0) return 0;
-    BuildScratch B;
-    PlocTree T;
-    const int grid = num_sms * 8;
-    int *items, *next_items, *kids, *n_int, *n_tri, *int_off, *tri_off;
-    uint32_t* wide_ids;
-    float* sah_cost = nullptr;
-    uint8_t* sah_choice = nullptr;
-    int64_t cap_items = std::max(16, n / 2 + 16);
-    int64_t cap_nodes = std::max<int64_t>(16, n / 4 + 16);
-    int level_base = 0, count = 1, next_base = 1, tri_base = 0, levels = 0;
-    if (ploc_tree(in, num_sms, s, err, B, T)) goto fail;
-    WF_TRY(B.alloc(&items, (size_t)cap_items));
-    WF_TRY(B.alloc(&next_items, (size_t)cap_items));
-    WF_TRY(B.alloc(&kids, 8 * (size_t)cap_items));
-    WF_TRY(B.alloc(&n_int, (size_t)cap_items));
-    WF_TRY(B.alloc(&n_tri, (size_t)cap_items));
-    WF_TRY(B.alloc(&int_off, (size_t)cap_items));
-    WF_TRY(B.alloc(&tri_off, (size_t)cap_items));
-    WF_TRY(B.alloc(&wide_ids, (size_t)n));
-    WF_TRY(cudaMalloc(&out.wnodes, sizeof(WideNode) * (size_t)cap_nodes));
-    if (n > 1) {  // SAH costs and choices of every interior binary node, pass by pass
-        WF_TRY(B.alloc(&sah_cost, 7 * (size_t)(n - 1)));
-        WF_TRY(B.alloc(&sah_choice, 8 * (size_t)(n - 1)));
-        for (const auto& it : T.iters)
-            k_wide_sah<8, kWideLeafMax><<<std::max(1, std::min(grid, (it.second + 127) / 128)), 128, 0, s>>>(
-                it.first, it.second, n, T.left, T.right, T.cnt, T.nbox, sah_cost, sah_choice);
-    }
-    WF_TRY(cudaMemcpyAsync(items, &T.root, sizeof(int), cudaMemcpyHostToDevice, s));
-    while (count > 0) {
-        if (++levels > kWideStack) {
-            err = "wide BVH deeper than the traversal stack";
-            goto fail;
-        }
-        const int g = std::max(1, std::min(grid, (count + 127) / 128));
-        if (n > 1)
-            k_wide_gather_sah<8, kWideLeafMax><<<g, 128, 0, s>>>(items, count, n, T.left, T.right, T.cnt, sah_choice,
-                                                                 kids, n_int, n_tri);
-        else
-            k_wide_gather<8, kWideLeafMax><<<g, 128, 0, s>>>(items, count, n, T.left, T.right, T.cnt, T.nbox, kids,
-                                                             n_int, n_tri);
-        exclusive_scan_i32(n_int, count, int_off, T.block_sums, T.d_total, s);
-        exclusive_scan_i32(n_tri, count, tri_off, T.block_sums, T.d_total + 1, s);
-        int tot[2] = {0, 0};
-        WF_TRY(cudaMemcpyAsync(tot, T.d_total, sizeof(tot), cudaMemcpyDeviceToHost, s));
-        WF_TRY(cudaStreamSynchronize(s));
-        if (tot[0] > cap_items) {  // a level holds disjoint subtrees of > 3 triangles: at most n/4
-            err = "wide BVH level larger than its buffers";
-            goto fail;
-        }
-        if ((int64_t)next_base + tot[0] > cap_nodes) {
-            // grow the node array (and the level buffers) and carry on
-            const int64_t need_nodes = std::max<int64_t>(2 * cap_nodes, (int64_t)next_base + tot[0]);
-            WideNode* bigger = nullptr;
-            WF_TRY(cudaMalloc(&bigger, sizeof(WideNode) * (size_t)need_nodes));
-            WF_TRY(cudaMemcpyAsync(bigger, out.wnodes, sizeof(WideNode) * (size_t)level_base, cudaMemcpyDeviceToDevice,
-                                   s));
-            WF_TRY(cudaStreamSynchronize(s));
-            cudaFree(out.wnodes);
-            out.wnodes = bigger;
-            cap_nodes = need_nodes;
-        }
-        k_wide_emit<<<g, 128, 0, s>>>(items, count, level_base, next_base, tri_base, kids, int_off, tri_off, n,
-                                      T.cnt, T.nbox, T.offset, T.final_ids, out.wnodes, next_items, wide_ids);
-        std::swap(items, next_items);
-        level_base = next_base;
-        next_base += tot[0];
-        tri_base += tot[1];
-        count = tot[0];
-    }
-    if (tri_base != n) {
-        err = "wide BVH lost triangles";
-        goto fail;
-    }
-    WF_TRY(cudaMalloc(&out.tris, 3 * sizeof(float4) * (size_t)n));
-    k_emit_tris<<<grid, 256, 0, s>>>(in.px, in.py, in.pz, in.idx, in.tri_geom, in.tri_prim, wide_ids, n, out.tris);
-    WF_TRY(cudaGetLastError());
-    WF_TRY(cudaStreamSynchronize(s));
-    out.num_nodes = level_base;  // every level written: total nodes
-    out.max_depth = levels;
-    if (validate_tree(out, n, num_sms, s, err)) goto fail;
-    return 0;
-fail:
-    cudaFree(out.tris);
-    cudaFree(out.wnodes);
-    out.tris = nullptr;
-    out.wnodes = nullptr;
-    return -1;
-}
-
 int build_ploc4(const BvhBuildInput& in, BvhBuildOutput& out, int num_sms, cudaStream_t s, std::string& err)
 {
     const int n = in.num_tris;
     out.tris = nullptr;
     out.nodes = nullptr;
-    out.wnodes = nullptr;
     out.nodes4 = nullptr;
     out.num_nodes = 0;
     out.max_depth = 0;

@@ -24,7 +24,6 @@ struct BvhBuildOutput {
     BvhNode* nodes;    // num_nodes (cudaMalloc'd; caller frees), binary trees
     int num_nodes;
     int max_depth;
-    WideNode* wnodes = nullptr;  // compressed 8-wide tree instead of nodes
     Bvh4Node* nodes4 = nullptr;  // 4-wide tree instead of nodes
 };
 
@@ -39,16 +38,9 @@ int build_lbvh(const BvhBuildInput& in, BvhBuildOutput& out, int num_sms, cudaSt
 int build_ploc(const BvhBuildInput& in, BvhBuildOutput& out, int num_sms, cudaStream_t s,
                std::string& err, bool sah_leaves = false);
 
-// PLOC tree collapsed top-down into compressed 8-wide nodes (WideNode):
-// each wide node opens the binary subtree greedily (largest surface area
-// first) up to eight children; subtrees of <= kWideLeafMax triangles become
-// leaf children.  out.wnodes / out.num_nodes / out.max_depth (wide levels).
-int build_ploc_wide(const BvhBuildInput& in, BvhBuildOutput& out, int num_sms, cudaStream_t s,
-                    std::string& err);
-
 // PLOC tree collapsed top-down into 4-wide nodes (Bvh4Node), level by
 // level, with the SAH-optimal choice of each node's (up to four) children
-// (the 8-wide build's dynamic programming); subtrees of <= kLeafMax triangles stay leaves
+// (dynamic programming over each binary subtree, Ylitie et al. 2017); subtrees of <= kLeafMax triangles stay leaves
 // over the same triangle order as build_ploc.  out.nodes4 / out.num_nodes /
 // out.max_depth (levels).
 int build_ploc4(const BvhBuildInput& in, BvhBuildOutput& out, int num_sms, cudaStream_t s, std::string& err);

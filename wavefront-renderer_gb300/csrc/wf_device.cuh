@@ -53,31 +53,6 @@ struct EmissiveMesh {
     int32_t pad;
 };
 
-// Compressed 8-wide BVH node (Ylitie, Karras & Laine, "Efficient Incoherent
-// Ray Traversal on GPUs Through Compressed Wide BVHs", HPG 2017): the child
-// boxes are quantized to 8 bits per plane on a power-of-two grid anchored
-// at p, conservatively (floor for lower planes, ceil for upper planes, boxes
-// padded before quantizing).  Interior children are stored contiguously
-// from child_base in slot order; leaf children (1-3 triangles) contiguously
-// from tri_base.  meta[s]: 0 = empty slot; interior 0x20 | (24 + s); leaf
-// (unary triangle count << 5) | offset from tri_base.  Slot s holds the child
-// nearest for rays whose direction octant (bit set = negative component) is
-// s, so popping hit slots by descending (s ^ octant ^ 7) visits near
-// children first.
-struct alignas(16) WideNode {
-    float p[3];
-    uint8_t e[3];         // per-axis scale 2^(e - 127)
-    uint8_t imask;        // bit s: slot s holds an interior child
-    uint32_t child_base;
-    uint32_t tri_base;
-    uint8_t meta[8];
-    uint8_t qlo[3][8];
-    uint8_t qhi[3][8];
-};
-static_assert(sizeof(WideNode) == 80, "WideNode is five 16-byte words");
-constexpr int kWideLeafMax = 3;   // triangles per leaf child
-constexpr int kWideStack = 32;    // node-group stack entries (checked at build)
-
 // 4-wide node: the four child boxes at full precision, one 128-byte line.
 // Planes are stored per axis and side for the four children (lox.x = child
 // 0's lower x plane, ...); kids holds the child words of BvhNode's encoding,
@@ -94,7 +69,7 @@ constexpr uint32_t kEmptyChild4 = 0xFFFFFFFFu;  // never a leaf word: scenes hol
 constexpr int kStack4 = 96;  // 4-wide traversal stack entries (checked at build: 1 + 3 x levels)
 
 // Tree format of a resident scene; the kernels of one wave use one traversal.
-enum TreeFormat : int { kTreeBinary = 0, kTreeWide8 = 1, kTreeFour = 2 };
+enum TreeFormat : int { kTreeBinary = 0, kTreeFour = 2 };
 
 struct DeviceScene {
     // Triangles in BVH leaf order: 3 float4 each.
@@ -102,8 +77,7 @@ struct DeviceScene {
     //   [1] = (v1 - v0).xyz, w = geomID (mesh index)
     //   [2] = (v2 - v0).xyz, w = primID (index within the mesh)
     const float4* tris;
-    const BvhNode* nodes;      // binary tree, or null when wnodes / nodes4 is set
-    const WideNode* wnodes;    // compressed 8-wide tree, or null
+    const BvhNode* nodes;      // binary tree, or null when nodes4 is set
     const Bvh4Node* nodes4;    // 4-wide tree, or null
     int32_t num_tris;
     int32_t num_nodes;
@@ -144,7 +118,7 @@ struct DeviceScene {
 
 __host__ __device__ __forceinline__ int tree_format(const DeviceScene& S)
 {
-    return S.wnodes ? kTreeWide8 : (S.nodes4 ? kTreeFour : kTreeBinary);
+    return S.nodes4 ? kTreeFour : kTreeBinary;
 }
 
 // ---------------------------------------------------------------------------

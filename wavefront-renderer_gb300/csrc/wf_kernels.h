@@ -31,7 +31,6 @@ struct LaunchCfg {
     int64_t l2_bytes = 0;  // the device's L2 size (variant 0 of a larger scene runs at 9 blocks per SM)
     int64_t max_scene_bytes = 0;  // largest resident tree + triangles (variant 0 of multi-job waves)
     int lean_multi = 0;  // no resident scene has an environment map, textures or a directional light
-    int speculative = 0;  // 1 = speculative while-while traversal
     int ray_order = 0;    // 1 = hit records at their rays' indices, listed by k_compact_hits
     int shade_grid = 0;        // k_shade's grid (one full wave of resident blocks); 0 = grid
     int shade_grid_other = 0;  // the same for its multi-job and cost-timed forms

@@ -1112,19 +1112,16 @@ int wf_autotune(wf_ctx* c, const wf_render_params* P, wf_tuning* out, double* ou
     const wf_tuning base = c->tuning;
     wf_tuning best = base;
     double best_ms = -1.0;
-    const int variants[4] = {0, 1, 2, 3};
+    const int variants[2] = {0, 1};
     const int blocks[5] = {4, 8, 12, 16, 24};
     const int graphs[2] = {2, 1};
-    const int specs[2] = {0, 1};
     for (int v : variants)
         for (int b : blocks)
-            for (int g : graphs)
-                for (int sp : specs) {
+            for (int g : graphs) {
                 wf_tuning t = base;
                 t.trace_variant = v;
                 t.persistent_blocks_per_sm = b;
                 t.graph_mode = g;
-                t.speculative_traversal = sp;
                 c->tuning = t;
                 double ms = 0.0;
                 for (int rep = 0; rep < 3; ++rep) {

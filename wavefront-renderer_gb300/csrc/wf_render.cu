@@ -260,59 +260,6 @@ __global__ void __launch_bounds__(128) k_occluded_api(DeviceScene S, int64_t n, 
     }
 }
 
-// Binary traversals that read the tree's top nodes from shared memory.
-using TraversalStaged = Traversal<false, false, true>;
-using TraversalAnyStaged = Traversal<true, false, true>;
-using TraversalFarStaged = Traversal<true, true, true>;
-
-// Speculation switch of the binary traversal (the wide one has none).
-template <class Tr>
-__device__ __forceinline__ void set_speculative(Tr& tr, bool on)
-{
-    if constexpr (std::is_same<Tr, Traversal<false>>::value || std::is_same<Tr, Traversal<true>>::value ||
-                  std::is_same<Tr, Traversal<true, true>>::value || std::is_same<Tr, TraversalStaged>::value ||
-                  std::is_same<Tr, TraversalAnyStaged>::value || std::is_same<Tr, TraversalFarStaged>::value)
-        tr.speculative = on;
-}
-
-// Where a persistent traversal kernel keeps its stack and its top nodes
-// (kStage): 0 = stack in local memory; 1 = the stack's bottom kSharedStack
-// entries in shared memory (SplitStack); 2 = local stack, the tree's first
-// kTopNodes nodes staged in shared memory (binary traversal with kStagedTop,
-// single-scene waves).  The stack object a kernel passes to the traversal:
-template <int kStage, class Entry>
-struct StackSel {
-    __device__ __forceinline__ static Entry* make(Entry* loc) { return loc; }
-};
-template <>
-struct StackSel<1, uint32_t> {
-    __device__ __forceinline__ static SplitStack make(uint32_t* loc)
-    {
-        __shared__ uint32_t sh[kSharedStack * 128];
-        return SplitStack{sh + threadIdx.x, loc};
-    }
-};
-
-// kStage 2: the block copies the first kTopNodes nodes of scene S (64-byte
-// nodes, four float4 each) into shared memory and points the traversal at
-// them; called by every thread of the block before its first round.
-template <int kStage, class Tr>
-__device__ __forceinline__ void stage_top_nodes(Tr& tr, const DeviceScene& S)
-{
-    if constexpr (kStage == 2) {
-        if constexpr (Tr::kStaged) {
-            __shared__ BvhNode top[kTopNodes];
-            const uint32_t cnt = S.nodes ? (uint32_t)min(kTopNodes, max(S.num_nodes, 0)) : 0u;
-            const float4* src = reinterpret_cast<const float4*>(S.nodes);
-            float4* dst = reinterpret_cast<float4*>(top);
-            for (uint32_t i = threadIdx.x; i < 4 * cnt; i += blockDim.x) dst[i] = __ldg(src + i);
-            __syncthreads();
-            tr.staged = top;
-            tr.num_staged = cnt;
-        }
-    }
-}
-
 // Child order of the binary any-hit traversal: the farther child first
 // measured faster on dense scenes (dense mesh +1.4%, lattice with environment
 // NEE +0.8%) and slower on the Cornell-box scenes of 36 triangles, whose
@@ -353,24 +300,20 @@ __device__ __forceinline__ void accum_add(float* accum, int32_t slot, V3 c)
 // ---------------------------------------------------------------------------
 // kMulti = false: every ray belongs to job0 on scene0 (passed by value, read
 // from the constant bank); true: each ray looks its job and scene up.
-template <bool kMulti, int kMinBlocks, class Tr, int kStage = 0>
+template <bool kMulti, int kMinBlocks, class Tr>
 __global__ void __launch_bounds__(128, kMinBlocks) k_trace_render(DeviceScene scene0, DeviceJob job0,
                                                                   const DeviceScene* __restrict__ scenes,
                                                                   const DeviceJob* __restrict__ jobs,
                                                                   RayQueueDev rq, const ull* __restrict__ d_n,
                                                                   HitQueueDev hq, ull* hq_n, float* accum,
-                                                                  ull* work, int* err, int speculative,
-                                                                  int ray_order)
+                                                                  ull* work, int* err, int ray_order)
 {
     const int64_t n = (int64_t)*d_n;
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     Tr tr;
-    typename Tr::Entry lstack[Tr::kStack];
-    const auto stack = StackSel<kStage, typename Tr::Entry>::make(lstack);
+    typename Tr::Entry stack[Tr::kStack];
     const DeviceScene* S = kMulti ? scenes : &scene0;
-    stage_top_nodes<kStage>(tr, scene0);
-    set_speculative(tr, speculative != 0);
     int job = 0;
     int64_t ray = -1;
     bool exhausted = false;
@@ -931,24 +874,20 @@ __global__ void __launch_bounds__(128, (kMulti || kTimed) ? WF_SHADE_MIN_BLOCKS 
 // Shadow rays (EmbreeAccelerator::occluded): unblocked contributions are
 // added to their pixel.  Same persistent, dynamic-fetch structure as
 // k_trace_render.
-template <bool kMulti, int kMinBlocks, class Tr, int kStage = 0>
+template <bool kMulti, int kMinBlocks, class Tr>
 __global__ void __launch_bounds__(128, kMinBlocks) k_occluded_render(DeviceScene scene0, DeviceJob job0,
                                                                      const DeviceScene* __restrict__ scenes,
                                                                      const DeviceJob* __restrict__ jobs,
                                                                      ShadowQueueDev sh,
                                                                      const ull* __restrict__ d_n,
-                                                                     float* accum, ull* work, int* err,
-                                                                     int speculative)
+                                                                     float* accum, ull* work, int* err)
 {
     const int64_t n = (int64_t)*d_n;
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     Tr tr;
-    typename Tr::Entry lstack[Tr::kStack];
-    const auto stack = StackSel<kStage, typename Tr::Entry>::make(lstack);
+    typename Tr::Entry stack[Tr::kStack];
     const DeviceScene* S = kMulti ? scenes : &scene0;
-    stage_top_nodes<kStage>(tr, scene0);
-    set_speculative(tr, speculative != 0);
     int job = 0;
     int64_t ray = -1;
     bool exhausted = false;
@@ -1535,15 +1474,12 @@ void launch_occluded_api(const DeviceScene& S, int64_t n, const float* ox, const
                                                              out, err);
 }
 
-// variant: 0 = no occupancy hint, 1 = 9 blocks of 128 per SM, 2 = the binary
-// traversal's stack with its bottom entries in shared memory (SplitStack),
-// 3 = the binary tree's top nodes staged in shared memory (single-scene
-// waves; else variant 0); the traversal follows the scene's tree (binary,
-// 4-wide or compressed 8-wide; variants 2 and 3 apply to binary trees, at 8
-// resident blocks).  The autotuner picks among them.  (A whole 64-entry stack in shared memory, 32 KB
-// per block, -10%, the top 256 nodes staged, -8% / -10%, and an L2
-// persistence window over the tree, -4%, measured slower on both workloads
-// and were taken out.)
+// variant: 0 = no occupancy hint, 1 = 9 blocks of 128 per SM; the traversal
+// follows the scene's tree (binary or 4-wide).  (The stack in shared memory,
+// whole or its bottom six entries, the tree's top nodes staged in shared
+// memory, speculative while-while, a compressed 8-wide tree and an L2
+// persistence window over the tree all measured slower on every workload and
+// were taken out.)
 // Where a ray-order bounce shades its misses: an environment-map lookup
 // (atan2, asin, a texel fetch) evaluated by finished lanes inside the
 // traversal loop stalls their warp, so for a single-job render of a scene
@@ -1582,19 +1518,13 @@ void launch_trace_render(const WaveTables& t, RayQueueDev rq, const ull* d_n, Hi
         (int64_t)t.scene0.num_nodes * (int64_t)sizeof(BvhNode) + (int64_t)t.scene0.num_tris * 48 > cfg.l2_bytes)
         cfg.variant = 1;
     cfg = multi_job_occupancy(t, cfg);
-#define WF_TRACE(M, B, T, K)                                                                                  \
-    k_trace_render<M, B, T, K><<<cfg.grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, d_n, hq, hq_n, \
-                                                        accum, work, err, cfg.speculative, cfg.ray_order)
+#define WF_TRACE(M, B, T)                                                                                   \
+    k_trace_render<M, B, T><<<cfg.grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, d_n, hq, hq_n, \
+                                                     accum, work, err, cfg.ray_order)
 #define WF_TRACE2(M, T) \
-    if (cfg.variant == 1) WF_TRACE(M, 9, T, 0); else WF_TRACE(M, 1, T, 0)
-    if (t.tree == kTreeWide8) {
-        if (t.multi) { WF_TRACE2(true, WideTraversal<false>); } else { WF_TRACE2(false, WideTraversal<false>); }
-    } else if (t.tree == kTreeFour) {
+    if (cfg.variant == 1) WF_TRACE(M, 9, T); else WF_TRACE(M, 1, T)
+    if (t.tree == kTreeFour) {
         if (t.multi) { WF_TRACE2(true, Traversal4<false>); } else { WF_TRACE2(false, Traversal4<false>); }
-    } else if (cfg.variant == 2) {
-        if (t.multi) { WF_TRACE(true, 8, Traversal<false>, 1); } else { WF_TRACE(false, 8, Traversal<false>, 1); }
-    } else if (cfg.variant == 3 && !t.multi) {
-        WF_TRACE(false, 8, TraversalStaged, 2);
     } else {
         if (t.multi) { WF_TRACE2(true, Traversal<false>); } else { WF_TRACE2(false, Traversal<false>); }
     }
@@ -1691,21 +1621,13 @@ void launch_occluded_render(const WaveTables& t, ShadowQueueDev sh, const ull* s
 {
     const bool far_first = !t.multi && t.scene0.num_tris >= kFarFirstTriangles;
     cfg = multi_job_occupancy(t, cfg);
-#define WF_OCC(M, B, T, K)                                                                                       \
-    k_occluded_render<M, B, T, K><<<cfg.grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, sh, sh_n, accum, work, \
-                                                           err, cfg.speculative)
+#define WF_OCC(M, B, T)                                                                                       \
+    k_occluded_render<M, B, T><<<cfg.grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, sh, sh_n, accum, work, \
+                                                        err)
 #define WF_OCC2(M, T) \
-    if (cfg.variant == 1) WF_OCC(M, 9, T, 0); else WF_OCC(M, 1, T, 0)
-    if (t.tree == kTreeWide8) {
-        if (t.multi) { WF_OCC2(true, WideTraversal<true>); } else { WF_OCC2(false, WideTraversal<true>); }
-    } else if (t.tree == kTreeFour) {
+    if (cfg.variant == 1) WF_OCC(M, 9, T); else WF_OCC(M, 1, T)
+    if (t.tree == kTreeFour) {
         if (t.multi) { WF_OCC2(true, Traversal4<true>); } else { WF_OCC2(false, Traversal4<true>); }
-    } else if (cfg.variant == 2) {
-        if (t.multi) { WF_OCC(true, 8, Traversal<true>, 1); }
-        else if (far_first) { WF_OCC(false, 8, TraversalFar, 1); }
-        else { WF_OCC(false, 8, Traversal<true>, 1); }
-    } else if (cfg.variant == 3 && !t.multi) {
-        if (far_first) { WF_OCC(false, 8, TraversalFarStaged, 2); } else { WF_OCC(false, 8, TraversalAnyStaged, 2); }
     } else if (far_first) {
         WF_OCC2(false, TraversalFar);
     } else {

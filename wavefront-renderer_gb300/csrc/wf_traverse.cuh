@@ -1,5 +1,5 @@
-// wf_traverse.cuh — BVH traversal (closest hit and any hit) over the binary,
-// 4-wide and compressed 8-wide trees.
+// wf_traverse.cuh — BVH traversal (closest hit and any hit) over the binary
+// and 4-wide trees.
 //
 // Closest hit follows the brute-force semantics of the reference's
 // Scene::hit / Mesh::hit (src/core/Scene.cpp:120-160, src/geometry/Mesh.cpp
@@ -71,51 +71,15 @@ __device__ __forceinline__ BvhNode load_node(const BvhNode* nodes, uint32_t i)
 
 constexpr uint32_t kSentinel = 0xFFFFFFFFu;
 
-// Traversal-stack placement in shared memory (the binary traversal's
-// stack-placement choice, wf_tuning::trace_variant 2): entries
-// [0, kSharedStack) of thread t live in shared memory at sh[i * 128] (one
-// 128-thread block; the lanes of a warp hit 32 distinct banks), deeper
-// entries in the thread's local array.  Six entries are 3 KB per block, which
-// eight resident blocks fit into the shared-memory share the driver already
-// sets aside for kernels that declare none.
-constexpr int kSharedStack = 6;
-struct SplitStack {
-    uint32_t* sh;   // shared array + threadIdx.x
-    uint32_t* loc;  // local array of kStackSize entries (the first kSharedStack unused)
-    struct Ref {
-        const SplitStack& s;
-        int i;
-        __device__ __forceinline__ operator uint32_t() const { return i < kSharedStack ? s.sh[i * 128] : s.loc[i]; }
-        __device__ __forceinline__ Ref& operator=(uint32_t v)
-        {
-            if (i < kSharedStack)
-                s.sh[i * 128] = v;
-            else
-                s.loc[i] = v;
-            return *this;
-        }
-    };
-    __device__ __forceinline__ Ref operator[](int i) const { return Ref{*this, i}; }
-};
-
-// Top-of-tree staging (wf_tuning::trace_variant 3): the first kTopNodes
-// nodes of a binary tree — numbered in reverse creation order, so the root
-// and the last clustering passes' nodes — are copied into shared memory once
-// per block and read from there (31 x 64 B per block).
-constexpr int kTopNodes = 31;
-
 // Resumable while-while traversal (Aila & Laine, "Understanding the
 // efficiency of ray traversal on GPUs", HPG 2009).  One call of round() walks
 // interior nodes down to a leaf, then leaves until it pops an interior node or
 // the stack's sentinel, so the lanes of a warp reconverge after every round
 // and a persistent kernel can hand a finished lane a new ray between rounds.
-template <bool kAnyHit, bool kFarFirst = false, bool kStagedTop = false>
+template <bool kAnyHit, bool kFarFirst = false>
 struct Traversal {
     using Entry = uint32_t;
     static constexpr int kStack = kStackSize;
-    static constexpr bool kStaged = kStagedTop;
-    const BvhNode* staged = nullptr;  // kStagedTop: nodes [0, num_staged) in shared memory
-    uint32_t num_staged = 0;
     V3 o, d, inv, oi;
     float tmin, best_t;
     int best_g;
@@ -123,7 +87,6 @@ struct Traversal {
     uint32_t top;  // the entry the next pop returns (binary traversal)
     int sp;
     bool overflow;
-    bool speculative = false;
     TraceResult res;
 
     // The stack lives outside the struct (a dynamically indexed array would
@@ -147,14 +110,6 @@ struct Traversal {
     }
     __device__ __forceinline__ bool done() const { return cur == kSentinel; }
     __device__ __forceinline__ void idle() { cur = kSentinel; }
-
-    __device__ __forceinline__ BvhNode fetch(const BvhNode* nodes, uint32_t i) const
-    {
-        if constexpr (kStagedTop) {
-            if (i < num_staged) return staged[i];
-        }
-        return load_node(nodes, i);
-    }
 
     // Binary-traversal stack with its top entry in a register: entries
     // 0 .. sp-2 are in memory, entry sp-1 is `top`.  A pop returns the
@@ -191,70 +146,24 @@ struct Traversal {
     __device__ __forceinline__ void round(const BvhNode* __restrict__ nodes, const float4* __restrict__ tris,
                                           Stk stack)
     {
-        if (!speculative) {
-            // While-while: walk interior nodes down to a leaf, then test
-            // leaves until an interior node or the sentinel comes off the
-            // stack.
-            while (!(cur & kLeafFlag)) {
-                const BvhNode nd = fetch(nodes, cur);
-                float tn0, tn1;
-                bool h0, h1;
-                slab2(nd, inv, oi, tmin, best_t, tn0, tn1, h0, h1);
-                const uint32_t c0 = (uint32_t)nd.kids.x, c1 = (uint32_t)nd.kids.y;
-                if (h0 && h1) {
-                    const bool swap = child_order_swap(nd, tn0, tn1);
-                    const uint32_t farc = swap ? c0 : c1;
-                    cur = swap ? c1 : c0;
-                    push(stack, farc);
-                } else if (h0 || h1) {
-                    cur = h0 ? c0 : c1;
-                } else {
-                    cur = pop(stack);
-                }
-            }
-            while (cur != kSentinel && (cur & kLeafFlag)) {
-                const uint32_t leaf = cur;
-                cur = pop(stack);
-                if (test_leaf(tris, leaf)) {
-                    cur = kSentinel;
-                    return;
-                }
-            }
-            return;
-        }
-        // Speculative while-while (Aila & Laine 2009): a lane that reaches a
-        // leaf postpones it and keeps descending while another lane of the
-        // warp is still looking for its first leaf; then all lanes test
-        // their leaves together.
-        const unsigned active = __activemask();
-        uint32_t postponed = 0u;  // leaf words always carry kLeafFlag, so 0 = none
-        for (;;) {
-            if (cur != kSentinel && !(cur & kLeafFlag)) {
-                const BvhNode nd = fetch(nodes, cur);
-                float tn0, tn1;
-                bool h0, h1;
-                slab2(nd, inv, oi, tmin, best_t, tn0, tn1, h0, h1);
-                const uint32_t c0 = (uint32_t)nd.kids.x, c1 = (uint32_t)nd.kids.y;
-                if (h0 && h1) {
-                    const bool swap = child_order_swap(nd, tn0, tn1);
-                    const uint32_t farc = swap ? c0 : c1;
-                    cur = swap ? c1 : c0;
-                    push(stack, farc);
-                } else if (h0 || h1) {
-                    cur = h0 ? c0 : c1;
-                } else {
-                    cur = pop(stack);
-                }
-            }
-            if (postponed == 0u && cur != kSentinel && (cur & kLeafFlag)) {
-                postponed = cur;
+        // While-while: walk interior nodes down to a leaf, then test leaves
+        // until an interior node or the sentinel comes off the stack.
+        while (!(cur & kLeafFlag)) {
+            const BvhNode nd = load_node(nodes, cur);
+            float tn0, tn1;
+            bool h0, h1;
+            slab2(nd, inv, oi, tmin, best_t, tn0, tn1, h0, h1);
+            const uint32_t c0 = (uint32_t)nd.kids.x, c1 = (uint32_t)nd.kids.y;
+            if (h0 && h1) {
+                const bool swap = child_order_swap(tn0, tn1);
+                const uint32_t farc = swap ? c0 : c1;
+                cur = swap ? c1 : c0;
+                push(stack, farc);
+            } else if (h0 || h1) {
+                cur = h0 ? c0 : c1;
+            } else {
                 cur = pop(stack);
             }
-            if (!__any_sync(active, postponed == 0u && cur != kSentinel)) break;
-        }
-        if (postponed != 0u && test_leaf(tris, postponed)) {
-            cur = kSentinel;  // any hit: done
-            return;
         }
         while (cur != kSentinel && (cur & kLeafFlag)) {
             const uint32_t leaf = cur;
@@ -270,23 +179,10 @@ struct Traversal {
     // any hit (shadow rays) the nearer one, or with kFarFirst the farther
     // one, which reaches the occluders between the surface and the light
     // before the geometry around the ray's own origin, where a shadow ray
-    // leaving its surface finds nothing.  WF_ANYHIT_ORDER selects other
-    // orders for shadow rays (1 = the first child, 2 = the child with the
-    // larger box).
-    __device__ __forceinline__ static bool child_order_swap(const BvhNode& nd, float tn0, float tn1)
+    // leaving its surface finds nothing.  (Visiting the first child or the
+    // larger box first measured 0.5-3% slower on the dense mesh.)
+    __device__ __forceinline__ static bool child_order_swap(float tn0, float tn1)
     {
-#if defined(WF_ANYHIT_ORDER) && WF_ANYHIT_ORDER == 1
-        if (kAnyHit) return false;
-#elif defined(WF_ANYHIT_ORDER) && WF_ANYHIT_ORDER == 2
-        if (kAnyHit) {
-            const float a0 = (nd.c0xy.y - nd.c0xy.x) * (nd.c0xy.w - nd.c0xy.z) +
-                             (nd.c0xy.w - nd.c0xy.z) * (nd.cz.y - nd.cz.x) + (nd.cz.y - nd.cz.x) * (nd.c0xy.y - nd.c0xy.x);
-            const float a1 = (nd.c1xy.y - nd.c1xy.x) * (nd.c1xy.w - nd.c1xy.z) +
-                             (nd.c1xy.w - nd.c1xy.z) * (nd.cz.w - nd.cz.z) + (nd.cz.w - nd.cz.z) * (nd.c1xy.y - nd.c1xy.x);
-            return a1 > a0;
-        }
-#endif
-        (void)nd;
         if (kAnyHit && kFarFirst) return !(tn1 < tn0);
         return tn1 < tn0;
     }
@@ -413,162 +309,6 @@ struct Traversal4 : Traversal<kAnyHit> {
     }
 };
 
-// Traversal of the compressed 8-wide BVH (WideNode), after Ylitie, Karras &
-// Laine (HPG 2017): the stack holds node groups (x = first interior child,
-// y = hit keys << 24 | interior mask); one round descends into the nearest
-// remaining hit child — pushing the rest of its group — intersects that
-// node's eight child boxes, and tests the triangles of the leaf children it
-// hit, or pops a group when nothing is left.  Same acceptance rule as the
-// binary traversal (smallest t, ties to the larger global index), so the
-// result does not depend on the tree.
-template <bool kAnyHit>
-struct WideTraversal {
-    using Entry = uint2;
-    static constexpr int kStack = kWideStack;
-    V3 o, d, inv, oi;
-    float tmin, best_t;
-    int best_g;
-    uint32_t octinv;
-    uint2 ng;  // node group
-    int sp;
-    bool fin;
-    bool overflow;
-    TraceResult res;
-
-    __device__ __forceinline__ void init(const DeviceScene& S, uint2* stack, V3 o_, V3 d_, float tmin_,
-                                         float tmax_)
-    {
-        (void)stack;
-        o = o_;
-        d = d_;
-        inv = v3(safe_inv(d.x), safe_inv(d.y), safe_inv(d.z));
-        oi = v3(o.x * inv.x, o.y * inv.y, o.z * inv.z);
-        tmin = tmin_;
-        best_t = tmax_;
-        best_g = -1;
-        res.leafpos = -1;
-        octinv = 7u ^ ((d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u));
-        // the root as the only interior child (slot 0) of a virtual group
-        ng = make_uint2(0u, (1u << (24u + octinv)) | 1u);
-        sp = 0;
-        fin = S.root_is_empty != 0;
-        overflow = false;
-    }
-    __device__ __forceinline__ bool done() const { return fin; }
-    __device__ __forceinline__ void idle() { fin = true; }
-
-    // One round walks interior nodes (the nearest remaining hit child of the
-    // current group, popping groups as they empty) until a node hits leaf
-    // children, then tests those triangles: like the binary while-while
-    // round, it ends at a leaf, so the persistent kernel's per-round work
-    // (result ballots, refills) is paid once per leaf visit, not per node.
-    __device__ __forceinline__ void round(const DeviceScene& S, uint2* stack)
-    {
-        uint32_t tri_base = 0, tri_hits = 0;
-        for (;;) {
-            if (ng.y > 0x00FFFFFFu) {
-                const uint32_t b = 31u - (uint32_t)__clz(ng.y);
-                ng.y &= ~(1u << b);
-                const uint32_t slot = (b - 24u) ^ octinv;
-                const uint32_t node = ng.x + (uint32_t)__popc(ng.y & ((1u << slot) - 1u) & 0xFFu);
-                if (ng.y > 0x00FFFFFFu) {
-                    if (sp < kStack)
-                        stack[sp++] = ng;
-                    else
-                        overflow = true;
-                }
-                intersect_node(S.wnodes + node, tri_base, tri_hits);
-                if (tri_hits) break;
-            } else if (sp > 0) {
-                ng = stack[--sp];
-            } else {
-                fin = true;
-                return;
-            }
-        }
-        while (tri_hits) {
-            const int lp = (int)tri_base + __ffs(tri_hits) - 1;
-            tri_hits &= tri_hits - 1u;
-            const float4 a = __ldg(S.tris + 3 * lp + 0);
-            const float4 bq = __ldg(S.tris + 3 * lp + 1);
-            const float4 c = __ldg(S.tris + 3 * lp + 2);
-            float th, uh, vh;
-            if (intersect_triangle(o, d, v3(a.x, a.y, a.z), v3(bq.x, bq.y, bq.z), v3(c.x, c.y, c.z), tmin, best_t,
-                                   th, uh, vh)) {
-                const int g = __float_as_int(a.w);
-                if (kAnyHit || th < best_t || res.leafpos < 0 || g > best_g) {
-                    res.leafpos = lp;
-                    res.t = th;
-                    res.bu = uh;
-                    res.bv = vh;
-                    best_t = th;
-                    best_g = g;
-                    if (kAnyHit) {
-                        fin = true;
-                        return;
-                    }
-                }
-            }
-        }
-    }
-
-    // Eight quantized child boxes, decoded as p + q * 2^e (q made a float
-    // exactly from its byte, one rounding in the fma) and slab-tested like
-    // the binary nodes; empty slots are masked out.
-    __device__ __forceinline__ static float byte_float(uint32_t word, uint32_t shift)
-    {
-        return __uint_as_float(0x4B000000u | ((word >> shift) & 0xFFu)) - 8388608.0f;
-    }
-    __device__ __forceinline__ void intersect_node(const WideNode* nodep, uint32_t& tri_base, uint32_t& tri_hits)
-    {
-        const float4* q = reinterpret_cast<const float4*>(nodep);
-        const float4 w0 = __ldg(q), w1 = __ldg(q + 1), w2 = __ldg(q + 2), w3 = __ldg(q + 3), w4 = __ldg(q + 4);
-        const uint32_t hdr = __float_as_uint(w0.w);
-        const float sx = __uint_as_float((hdr & 0xFFu) << 23);
-        const float sy = __uint_as_float(((hdr >> 8) & 0xFFu) << 23);
-        const float sz = __uint_as_float(((hdr >> 16) & 0xFFu) << 23);
-        const uint32_t imask = hdr >> 24;
-        const uint32_t meta0 = __float_as_uint(w1.z), meta1 = __float_as_uint(w1.w);
-        const uint32_t lox[2] = {__float_as_uint(w2.x), __float_as_uint(w2.y)};
-        const uint32_t loy[2] = {__float_as_uint(w2.z), __float_as_uint(w2.w)};
-        const uint32_t loz[2] = {__float_as_uint(w3.x), __float_as_uint(w3.y)};
-        const uint32_t hix[2] = {__float_as_uint(w3.z), __float_as_uint(w3.w)};
-        const uint32_t hiy[2] = {__float_as_uint(w4.x), __float_as_uint(w4.y)};
-        const uint32_t hiz[2] = {__float_as_uint(w4.z), __float_as_uint(w4.w)};
-        const uint32_t meta[2] = {meta0, meta1};
-        uint32_t hits_i = 0, hits_t = 0;
-        // all eight slots unrolled (96 registers, 5 resident blocks): two per
-        // step (64 registers, 8 blocks) measured 15% slower on the dense mesh
-        // and the lattice
-#pragma unroll
-        for (int s = 0; s < 8; ++s) {
-            const int wd = s >> 2;
-            const uint32_t sh = 8u * (uint32_t)(s & 3);
-            const uint32_t m = (meta[wd] >> sh) & 0xFFu;
-            const float lx = __fmaf_rn(byte_float(lox[wd], sh), sx, w0.x);
-            const float hx = __fmaf_rn(byte_float(hix[wd], sh), sx, w0.x);
-            const float ly = __fmaf_rn(byte_float(loy[wd], sh), sy, w0.y);
-            const float hy = __fmaf_rn(byte_float(hiy[wd], sh), sy, w0.y);
-            const float lz = __fmaf_rn(byte_float(loz[wd], sh), sz, w0.z);
-            const float hz = __fmaf_rn(byte_float(hiz[wd], sh), sz, w0.z);
-            const float tlx = __fmaf_rn(lx, inv.x, -oi.x), thx = __fmaf_rn(hx, inv.x, -oi.x);
-            const float tly = __fmaf_rn(ly, inv.y, -oi.y), thy = __fmaf_rn(hy, inv.y, -oi.y);
-            const float tlz = __fmaf_rn(lz, inv.z, -oi.z), thz = __fmaf_rn(hz, inv.z, -oi.z);
-            const float tn = fmax3(fminf(tlx, thx), fminf(tly, thy), fmaxf(fminf(tlz, thz), tmin));
-            const float tf = fmin3(fmaxf(tlx, thx), fmaxf(tly, thy), fminf(fmaxf(tlz, thz), best_t));
-            if (m != 0u && tn <= tf) {
-                if ((m & 0x1Fu) >= 24u)
-                    hits_i |= 1u << (24u + ((uint32_t)s ^ octinv));
-                else
-                    hits_t |= (m >> 5) << (m & 0x1Fu);
-            }
-        }
-        ng = make_uint2(__float_as_uint(w1.x), hits_i | imask);
-        tri_base = __float_as_uint(w1.y);
-        tri_hits = hits_t;
-    }
-};
-
 // Whole traversal of one ray (host-API kernels).  Returns false (and sets
 // *err_flag) only if the stack would overflow, which the build rules out by
 // checking the tree depth.
@@ -589,7 +329,6 @@ template <bool kAnyHit>
 __device__ __forceinline__ bool traverse(const DeviceScene& S, V3 o, V3 d, float tmin, float tmax,
                                          TraceResult& res, int* err_flag)
 {
-    if (S.wnodes) return traverse_with<WideTraversal<kAnyHit>>(S, o, d, tmin, tmax, res, err_flag);
     if (S.nodes4) return traverse_with<Traversal4<kAnyHit>>(S, o, d, tmin, tmax, res, err_flag);
     return traverse_with<Traversal<kAnyHit>>(S, o, d, tmin, tmax, res, err_flag);
 }
