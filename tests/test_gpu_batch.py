@@ -53,13 +53,19 @@ def test_batch_job_equals_job_alone(wf, ctx, variant):
 
 
 def test_batch_job_matches_oracle(wf, orc, ctx):
+    """Jobs of a batch against the port rendering each alone (same random
+    streams); the agreement is reported before it is asserted."""
+    from conftest import report
+
     jobs, hosts = _jobs(wf, ctx, 3, seed0=300)
     imgs, _ = ctx.render_batch(jobs)
-    for j, hs, img in zip(jobs, hosts, imgs):
+    for k, (j, hs, img) in enumerate(zip(jobs, hosts, imgs)):
         port = orc.Port(hs.desc)
         p = wf.render_params(j.width, j.height, j.samples_per_pixel, j.max_depth, j.camera, seed=j.seed_lo)
         acc, _ = port.render_window(p, 0, 0, j.width, j.height)
-        agree = np.isclose(img, acc / j.samples_per_pixel, rtol=1e-3, atol=1e-4).all(axis=2).mean()
+        close = np.isclose(img, acc / j.samples_per_pixel, rtol=1e-3, atol=1e-4).all(axis=2)
+        agree = float(close.mean())
+        report(f"batch_job{k}_paths", agree=agree, disagreeing_pixels=int((~close).sum()), pixels=int(close.size))
         assert agree >= 0.97
 
 
