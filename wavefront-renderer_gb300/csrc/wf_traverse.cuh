@@ -271,9 +271,12 @@ struct Traversal4 : Traversal<kAnyHit> {
                                            Stk stack)
     {
         while (!(this->cur & kLeafFlag)) {
+            // one 128-byte node in three 256-bit loads and one 128-bit load
             const float4* p = reinterpret_cast<const float4*>(nodes + this->cur);
-            const float4 lx = __ldg(p + 0), hx = __ldg(p + 1), ly = __ldg(p + 2), hy = __ldg(p + 3);
-            const float4 lz = __ldg(p + 4), hz = __ldg(p + 5);
+            float4 lx, hx, ly, hy, lz, hz;
+            ldg_v8(p + 0, lx, hx);
+            ldg_v8(p + 2, ly, hy);
+            ldg_v8(p + 4, lz, hz);
             const int4 k = __ldg(reinterpret_cast<const int4*>(p + 6));
             uint32_t k0 = slab_key(lx.x, hx.x, ly.x, hy.x, lz.x, hz.x, k.x, 0u);
             uint32_t k1 = slab_key(lx.y, hx.y, ly.y, hy.y, lz.y, hz.y, k.y, 1u);
