@@ -269,6 +269,7 @@ __global__ void __launch_bounds__(128) k_occluded_api(DeviceScene S, int64_t n, 
 // its own: as a launch argument the choice cost the dense mesh 0.7%).
 constexpr int kFarFirstTriangles = 4096;
 using TraversalFar = Traversal<true, true>;
+using Traversal4Far = Traversal4<true, true>;
 
 __device__ __forceinline__ void accum_add(float* accum, int32_t slot, V3 c)
 {
@@ -1627,7 +1628,9 @@ void launch_occluded_render(const WaveTables& t, ShadowQueueDev sh, const ull* s
 #define WF_OCC2(M, T) \
     if (cfg.variant == 1) WF_OCC(M, 9, T); else WF_OCC(M, 1, T)
     if (t.tree == kTreeFour) {
-        if (t.multi) { WF_OCC2(true, Traversal4<true>); } else { WF_OCC2(false, Traversal4<true>); }
+        if (t.multi) { WF_OCC2(true, Traversal4<true>); }
+        else if (far_first) { WF_OCC2(false, Traversal4Far); }
+        else { WF_OCC2(false, Traversal4<true>); }
     } else if (far_first) {
         WF_OCC2(false, TraversalFar);
     } else {

@@ -222,7 +222,7 @@ struct Traversal {
 // the low two bits, misses all ones), the nearest is visited next and the
 // others are pushed farthest first.  Same state, leaf test and acceptance
 // rule as the binary traversal, so the result does not depend on the tree.
-template <bool kAnyHit>
+template <bool kAnyHit, bool kFarFirst = false>
 struct Traversal4 : Traversal<kAnyHit> {
     static constexpr int kStack = kStack4;
 
@@ -241,8 +241,11 @@ struct Traversal4 : Traversal<kAnyHit> {
         const float tn = fmax3(fminf(tlx, thx), fminf(tly, thy), fmaxf(fminf(tlz, thz), this->tmin));
         const float tf = fmin3(fmaxf(tlx, thx), fmaxf(tly, thy), fminf(fmaxf(tlz, thz), this->best_t));
         // tn >= tmin: for tmin >= 0 the bits order like the distances (the
-        // order only steers the walk, never the result)
-        return (tn <= tf && (uint32_t)kid != kEmptyChild4) ? ((__float_as_uint(tn) & ~3u) | slot) : 0xFFFFFFFFu;
+        // order only steers the walk, never the result); kFarFirst (shadow
+        // rays of dense scenes) inverts them, so the farthest hit child
+        // comes first (its keys keep the top bit, a miss stays all ones)
+        const uint32_t bits = kAnyHit && kFarFirst ? ~__float_as_uint(tn) : __float_as_uint(tn);
+        return (tn <= tf && (uint32_t)kid != kEmptyChild4) ? ((bits & ~3u) | slot) : 0xFFFFFFFFu;
     }
     __device__ __forceinline__ static void sort2(uint32_t& a, uint32_t& b)
     {
