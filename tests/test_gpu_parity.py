@@ -356,6 +356,22 @@ def test_tree_formats_render_the_same_image(wf, ctx, scene_c2small, builder):
         other.close()
 
 
+def test_tuning_rejects_removed_options(wf, ctx):
+    """The options taken out after measuring slower everywhere are refused,
+    not silently ignored: trace variants beyond 1, the compressed 8-wide tree
+    (bvh_builder 2) and non-zero reserved fields."""
+    try:
+        for bad in [dict(trace_variant=2), dict(trace_variant=3), dict(bvh_builder=2), dict(bvh_builder=5)]:
+            with pytest.raises(wf.WfError):
+                ctx.set_tuning(**bad)
+        for t in (wf.WfTuning(0, 0, 0, 0, 0, 1, 0, 0), wf.WfTuning(0, 0, 0, 0, 0, 0, 1, 0)):  # reserved2, reserved
+            rc = wf.load_library().wf_set_tuning(ctx._h, wf.C.byref(t))
+            assert wf.ERRORS.get(rc) == "WF_ERR_INVALID_ARGUMENT", rc
+        ctx.set_tuning(bvh_builder=4)  # still valid
+    finally:
+        ctx.set_tuning()
+
+
 def test_autotune_picks_a_valid_tuning(wf, ctx, scene_small):
     ctx.upload(scene_small.desc)
     cam = scene_small.camera(64, 64)
