@@ -456,7 +456,7 @@ __global__ void k_ploc_init(int n, const float* __restrict__ leaf_box, float* __
 }
 
 // ---------------------------------------------------------------------------
-// Compressed 8-wide collapse of the PLOC tree, one level of wide nodes per
+// Collapse of the PLOC tree into 4-wide nodes, one level of wide nodes per
 // pass (items = binary node ids of the level's wide nodes).
 // ---------------------------------------------------------------------------
 

@@ -577,7 +577,7 @@ constexpr int kShadeWarps = 4;  // k_shade runs 128-thread blocks
 // map lookups), the texture lookups and the directional NEE — a smaller
 // kernel that waits less on the instruction cache (dense mesh +0.9%,
 // Cornell box +1.7% for the environment block alone).
-template <bool kMulti, bool kTimed, bool kLean = false>
+template <bool kMulti, bool kTimed, bool kLean = false, bool kGroup = false>
 __global__ void __launch_bounds__(128, (kMulti || kTimed) ? WF_SHADE_MIN_BLOCKS : WF_SHADE_MIN_BLOCKS_PLAIN)
     k_shade(DeviceScene scene0, DeviceJob job0,
                                                const DeviceScene* __restrict__ scenes,
@@ -589,7 +589,9 @@ __global__ void __launch_bounds__(128, (kMulti || kTimed) ? WF_SHADE_MIN_BLOCKS 
     // hq.ray lists the rays that hit; their records (tri, t, u, v) sit at the
     // list position, or with ray_order at the ray's own index.
     __shared__ unsigned blk_sh[kShadeWarps], blk_nx[kShadeWarps];
+    __shared__ unsigned blk_oct[8 * kShadeWarps];  // next rays per (octant, warp), octant-major
     __shared__ ull blk_first[2];
+    static_assert(8 * kShadeWarps == 32, "one scan lane per (octant, warp)");
     const int64_t n = (int64_t)*hq_n;
     WF_BLOCK_LOOP(base, n)
     {
@@ -793,32 +795,77 @@ __global__ void __launch_bounds__(128, (kMulti || kTimed) ? WF_SHADE_MIN_BLOCKS 
         const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
         const unsigned lt = (1u << lane) - 1u;
         const unsigned ma = __ballot_sync(0xFFFFFFFFu, want_area), md = __ballot_sync(0xFFFFFFFFu, want_dir);
-        const unsigned me = __ballot_sync(0xFFFFFFFFu, want_env), mn = __ballot_sync(0xFFFFFFFFu, want_next);
-        if (lane == 0) {
-            blk_sh[warp] = (unsigned)(__popc(ma) + __popc(md) + __popc(me));
-            blk_nx[warp] = (unsigned)__popc(mn);
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            unsigned ts = 0, tn = 0;
-            for (int w = 0; w < kShadeWarps; ++w) {
-                const unsigned a = blk_sh[w], b = blk_nx[w];
-                blk_sh[w] = ts;
-                blk_nx[w] = tn;
-                ts += a;
-                tn += b;
+        const unsigned me = __ballot_sync(0xFFFFFFFFu, want_env);
+        int64_t sh0, pn;
+        if constexpr (kGroup) {
+            // The block's next rays are written grouped by the octant of their
+            // direction (octant-major, then warp, then lane), so the warps that
+            // fetch them get rays whose traversals take the same child order.
+            const unsigned oct = (__float_as_uint(nd.x) >> 31) | (__float_as_uint(nd.y) >> 31) << 1 |
+                                 (__float_as_uint(nd.z) >> 31) << 2;
+            // Lanes of octant o among those with a next ray: mn with every bit
+            // of o matched against the ballot of that bit.
+            const unsigned mn = __ballot_sync(0xFFFFFFFFu, want_next);
+            const unsigned b0 = __ballot_sync(0xFFFFFFFFu, oct & 1u), b1 = __ballot_sync(0xFFFFFFFFu, oct & 2u),
+                           b2 = __ballot_sync(0xFFFFFFFFu, oct & 4u);
+            const auto peers = [&](unsigned o) {
+                return mn & ~((b0 ^ (0u - (o & 1u))) | (b1 ^ (0u - ((o >> 1) & 1u))) | (b2 ^ (0u - ((o >> 2) & 1u))));
+            };
+            const unsigned oct_rank = (unsigned)__popc(peers(oct) & lt);
+            if (lane < 8) blk_oct[lane * kShadeWarps + warp] = (unsigned)__popc(peers((unsigned)lane));
+            if (lane == 0) blk_sh[warp] = (unsigned)(__popc(ma) + __popc(md) + __popc(me));
+            __syncthreads();
+            if (warp == 0) {
+                const unsigned v = blk_oct[lane];
+                unsigned x = v;
+#pragma unroll
+                for (int dd = 1; dd < 32; dd <<= 1) {
+                    const unsigned y = __shfl_up_sync(0xFFFFFFFFu, x, dd);
+                    if (lane >= dd) x += y;
+                }
+                blk_oct[lane] = x - v;
+                const unsigned tn = __shfl_sync(0xFFFFFFFFu, x, 31);
+                if (lane == 0) {
+                    unsigned ts = 0;
+                    for (int w = 0; w < kShadeWarps; ++w) {
+                        const unsigned a = blk_sh[w];
+                        blk_sh[w] = ts;
+                        ts += a;
+                    }
+                    blk_first[0] = ts ? atomicAdd(sh_n, (ull)ts) : 0ull;
+                    blk_first[1] = tn ? atomicAdd(nx_n, (ull)tn) : 0ull;
+                }
             }
-            blk_first[0] = ts ? atomicAdd(sh_n, (ull)ts) : 0ull;
-            blk_first[1] = tn ? atomicAdd(nx_n, (ull)tn) : 0ull;
+            __syncthreads();
+            sh0 = (int64_t)blk_first[0] + blk_sh[warp];
+            pn = (int64_t)blk_first[1] + blk_oct[(want_next ? oct : 0u) * kShadeWarps + warp] + oct_rank;
+        } else {
+            const unsigned mn = __ballot_sync(0xFFFFFFFFu, want_next);
+            if (lane == 0) {
+                blk_sh[warp] = (unsigned)(__popc(ma) + __popc(md) + __popc(me));
+                blk_nx[warp] = (unsigned)__popc(mn);
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                unsigned ts = 0, tn = 0;
+                for (int w = 0; w < kShadeWarps; ++w) {
+                    const unsigned a = blk_sh[w], b = blk_nx[w];
+                    blk_sh[w] = ts;
+                    blk_nx[w] = tn;
+                    ts += a;
+                    tn += b;
+                }
+                blk_first[0] = ts ? atomicAdd(sh_n, (ull)ts) : 0ull;
+                blk_first[1] = tn ? atomicAdd(nx_n, (ull)tn) : 0ull;
+            }
+            __syncthreads();
+            sh0 = (int64_t)blk_first[0] + blk_sh[warp];
+            pn = (int64_t)blk_first[1] + blk_nx[warp] + __popc(mn & lt);
         }
-        __syncthreads();
-        const int64_t sh0 = (int64_t)blk_first[0] + blk_sh[warp];
-        const int64_t nx0 = (int64_t)blk_first[1] + blk_nx[warp];
         __syncthreads();  // the block's words are rewritten by the next iteration
         const int64_t pa = sh0 + __popc(ma & lt);
         const int64_t pd = sh0 + __popc(ma) + __popc(md & lt);
         const int64_t pe = sh0 + __popc(ma) + __popc(md) + __popc(me & lt);
-        const int64_t pn = nx0 + __popc(mn & lt);
         if (want_area) {
             if (pa < sh.capacity) {
                 stq(&sh.ox[pa], p.x); stq(&sh.oy[pa], p.y); stq(&sh.oz[pa], p.z);
@@ -1585,21 +1632,30 @@ void launch_shade(const WaveTables& t, RayQueueDev rq, HitQueueDev hq, const ull
 {
     const int plain_grid = cfg.shade_grid > 0 ? cfg.shade_grid : cfg.grid;
     const int grid = cfg.shade_grid_other > 0 ? cfg.shade_grid_other : cfg.grid;
+    // Next rays grouped by octant where the traversal gains more than the
+    // grouping costs k_shade: single scenes from kFarFirstTriangles on, waves
+    // over a dense scene.
+    const bool group = t.multi ? cfg.max_scene_bytes >= kDenseSceneBytes : t.scene0.num_tris >= kFarFirstTriangles;
+#define WF_SHADE(M, T, L, GRID)                                                                                   \
+    do {                                                                                                          \
+        if (group)                                                                                                \
+            k_shade<M, T, L, true><<<GRID, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, hq, hq_n,         \
+                                                        cfg.ray_order, sh, sh_n, next, next_n, accum, err);       \
+        else                                                                                                      \
+            k_shade<M, T, L, false><<<GRID, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, hq, hq_n,        \
+                                                         cfg.ray_order, sh, sh_n, next, next_n, accum, err);      \
+    } while (0)
     if (t.multi && cfg.lean_multi)  // every resident scene fits the lean instance
-        k_shade<true, false, true><<<grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, hq, hq_n,
-                                                        cfg.ray_order, sh, sh_n, next, next_n, accum, err);
+        WF_SHADE(true, false, true, grid);
     else if (t.multi)
-        k_shade<true, false><<<grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, hq, hq_n, cfg.ray_order,
-                                                  sh, sh_n, next, next_n, accum, err);
+        WF_SHADE(true, false, false, grid);
     else if (t.job0.cost_sum_mat)
-        k_shade<false, true><<<grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, hq, hq_n, cfg.ray_order,
-                                                  sh, sh_n, next, next_n, accum, err);
+        WF_SHADE(false, true, false, grid);
     else if (!t.scene0.env_alias_prob && t.scene0.num_textures == 0 && !(t.scene0.directional.intensity > 0.0f))
-        k_shade<false, false, true><<<plain_grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, hq, hq_n,
-                                                                cfg.ray_order, sh, sh_n, next, next_n, accum, err);
+        WF_SHADE(false, false, true, plain_grid);
     else
-        k_shade<false, false><<<plain_grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, hq, hq_n, cfg.ray_order,
-                                                   sh, sh_n, next, next_n, accum, err);
+        WF_SHADE(false, false, false, plain_grid);
+#undef WF_SHADE
 }
 
 void launch_compact_hits(const WaveTables& t, RayQueueDev rq, const ull* d_n, HitQueueDev hq, ull* hq_n,
