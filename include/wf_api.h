@@ -239,6 +239,8 @@ int wf_version(void);
  * construction of WavefrontRenderer (include/render/WavefrontRenderer.h:36-39)
  * and EmbreeAccelerator (src/accelerator/Embree.cpp:9-14). */
 int wf_create(const wf_config* config, wf_ctx** out_ctx);
+/* Destroys a context.  Its servers and device queues must be destroyed
+ * before it (the Python binding's Context.close does so). */
 int wf_destroy(wf_ctx* ctx);
 /* Message of the last failing call on ctx ("" when none). */
 const char* wf_last_error(const wf_ctx* ctx);
@@ -690,8 +692,11 @@ int wf_render_batch(wf_ctx* ctx, const wf_job* jobs, int32_t njobs, float* const
  * of whole frames.  Budget = the queue (276 B per path) + the jobs' sums + a
  * share for frame sums (an eighth of the rest, at least 6 floats per queued
  * path).  The queue keeps paths between steps: the server's buffers are its
- * own, apart from the context's.  Times are seconds on the server's monotonic
- * clock.  No counterpart in the reference
+ * own, apart from the context's.  A job whose last frame ends in a step has
+ * its sums freed at the end of that step and its image copied out while the
+ * next step runs; it turns WF_JOB_DONE (and leaves `running`) in that next
+ * step, or at once when wf_server_image or wf_server_cancel asks for it.
+ * Times are seconds on the server's monotonic clock.  No counterpart in the reference
  * (it renders one image per process; its GUI polls a preview file). */
 typedef struct wf_server wf_server;
 typedef struct wf_server_config {

@@ -15,6 +15,7 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+import weakref
 from pathlib import Path
 
 import numpy as np
@@ -259,6 +260,7 @@ class Server:
         self._h = C.c_void_p()
         cfg = WfServerConfig(hbm_budget_bytes, max_paths_per_wave, frame_spp)
         _check(load_library().wf_server_create(ctx._h, C.byref(cfg), C.byref(self._h)), "wf_server_create", ctx)
+        ctx._children.add(self)
 
     def close(self):
         if self._h:
@@ -309,6 +311,7 @@ class _DeviceQueue:
         self._h = C.c_void_p()
         _check(getattr(load_library(), f"wf_{self._kind}_queue_alloc")(ctx._h, self.capacity, C.byref(self._h)),
                f"wf_{self._kind}_queue_alloc", ctx)
+        ctx._children.add(self)
 
     def close(self):
         if self._h:
@@ -404,12 +407,17 @@ class Context:
     def __init__(self, device: int = 0, max_paths_per_wave: int = 0):
         lib = load_library()
         self._h = C.c_void_p()
+        # servers and device queues made on this context: closed before it,
+        # whatever still refers to them (the C API wants them destroyed first)
+        self._children = weakref.WeakSet()
         cfg = WfConfig(device, max_paths_per_wave)
         rc = lib.wf_create(C.byref(cfg), C.byref(self._h))
         _check(rc, "wf_create")
 
     def close(self):
         if self._h:
+            for child in list(self._children):
+                child.close()
             load_library().wf_destroy(self._h)
             self._h = C.c_void_p()
 

@@ -697,6 +697,7 @@ struct ServedJob {
     int chunks_out = 0;     // frames appended and not yet finished
     int64_t accum_off = -1;
     int64_t accum_floats = 0;
+    bool flushing = false;  // image copy in flight (its sums released), done at the next flush_complete
     double t_submit = 0, t_admit = -1, t_first = -1, t_done = -1;
     std::vector<float> final_image;
 };
@@ -770,6 +771,7 @@ struct wf_server {
     float* host_stage = nullptr;  // finished images (page-locked)
     int64_t host_stage_floats = 0;
     std::vector<int64_t> finishing;  // jobs whose last frame finished this step
+    std::vector<int64_t> flushing;   // jobs whose averaged images are being copied into host_stage
     // page-locked sources of the step's uploads (read by the device after the
     // call returns; rewritten only after the step's final wait)
     DeviceJob* job_stage = nullptr;    // one per table entry
@@ -791,7 +793,7 @@ struct wf_server {
     StreamState* d_state = nullptr;
     int64_t* d_log = nullptr;
     StepReadback* rb = nullptr;  // page-locked
-    cudaEvent_t ev[2]{};
+    cudaEvent_t ev[3]{};  // [0], [1] around the step's graph, [2] after the finished images' copy
     cudaGraphExec_t exec = nullptr;
     const void* exec_table = nullptr;  // scene table, variant and tree the capture used
     int exec_variant = -1, exec_tree = -1, exec_lean = -1;
@@ -942,8 +944,11 @@ int ensure_stream_graph(wf_server* sv)
 }
 
 // Jobs whose last frame finished this step: their averaged images are made
-// together at the end of the step (one copy, one wait), then their sums go.
-int flush_finished(wf_server* sv, wf_server_step_info& si)
+// together at the end of the step and copied into page-locked memory with no
+// wait (their sums are released at once: later work on the stream runs after
+// the copy).  flush_complete hands the images over while the next step's
+// iterations run, so the host copies overlap the device.
+int flush_begin(wf_server* sv)
 {
     if (sv->finishing.empty()) return WF_OK;
     wf_ctx* c = sv->c;
@@ -956,7 +961,7 @@ int flush_finished(wf_server* sv, wf_server_step_info& si)
         WF_CK(c, cudaMalloc(&sv->tmp, sizeof(float) * total));
         sv->tmp_floats = total;
     }
-    if (total > sv->host_stage_floats) {
+    if (total > sv->host_stage_floats) {  // no copy into it is in flight (flush_complete ran first)
         cudaFreeHost(sv->host_stage);
         sv->host_stage = nullptr;
         sv->host_stage_floats = 0;
@@ -965,26 +970,38 @@ int flush_finished(wf_server* sv, wf_server_step_info& si)
     }
     int64_t o = 0;
     for (int64_t id : sv->finishing) {
-        const ServedJob& j = sv->jobs[id];
-        launch_finalize(sv->arena + j.accum_off, j.accum_floats, (float)j.samples_done, sv->tmp + o, c->stream);
-        o += j.accum_floats;
-    }
-    WF_CK(c, cudaMemcpyAsync(sv->host_stage, sv->tmp, sizeof(float) * total, cudaMemcpyDeviceToHost, c->stream));
-    WF_CK(c, cudaStreamSynchronize(c->stream));
-    const double now = seconds_since(sv->t0);
-    o = 0;
-    for (int64_t id : sv->finishing) {
         ServedJob& j = sv->jobs[id];
-        j.final_image.assign(sv->host_stage + o, sv->host_stage + o + j.accum_floats);
+        launch_finalize(sv->arena + j.accum_off, j.accum_floats, (float)j.samples_done, sv->tmp + o, c->stream);
         o += j.accum_floats;
         sv->alloc.release(j.accum_off, j.accum_floats);
         j.accum_off = -1;
+        j.flushing = true;
+    }
+    WF_CK(c, cudaMemcpyAsync(sv->host_stage, sv->tmp, sizeof(float) * total, cudaMemcpyDeviceToHost, c->stream));
+    WF_CK(c, cudaEventRecord(sv->ev[2], c->stream));
+    sv->flushing.swap(sv->finishing);
+    sv->finishing.clear();
+    return WF_OK;
+}
+
+int flush_complete(wf_server* sv, wf_server_step_info& si)
+{
+    if (sv->flushing.empty()) return WF_OK;
+    wf_ctx* c = sv->c;
+    WF_CK(c, cudaEventSynchronize(sv->ev[2]));
+    const double now = seconds_since(sv->t0);
+    int64_t o = 0;
+    for (int64_t id : sv->flushing) {
+        ServedJob& j = sv->jobs[id];
+        j.final_image.assign(sv->host_stage + o, sv->host_stage + o + j.accum_floats);
+        o += j.accum_floats;
+        j.flushing = false;
         j.state = WF_JOB_DONE;
         j.t_done = now;
         si.completed_this_step++;
         sv->running--;
     }
-    sv->finishing.clear();
+    sv->flushing.clear();
     return WF_OK;
 }
 
@@ -1528,6 +1545,7 @@ int wf_server_step(wf_server* sv, wf_server_step_info* info)
         WF_CK(c, cudaMemcpyAsync(&rb->live, sv->counters, sizeof(ull), cudaMemcpyDeviceToHost, s));
         WF_CK(c, cudaMemcpyAsync(&rb->st, sv->d_state, sizeof(StreamState), cudaMemcpyDeviceToHost, s));
         WF_CK(c, cudaMemcpyAsync(rb->log, sv->d_log, sizeof(rb->log), cudaMemcpyDeviceToHost, s));
+        if ((rc = flush_complete(sv, si))) return rc;  // the last step's finished jobs, while this one runs
         WF_CK(c, cudaStreamSynchronize(s));
         int flag = 0;
         WF_CK(c, cudaMemcpy(&flag, sv->err, sizeof(int), cudaMemcpyDeviceToHost));
@@ -1556,6 +1574,7 @@ int wf_server_step(wf_server* sv, wf_server_step_info* info)
         sv->cursor = rb->st.cursor;
         sv->live = (int64_t)rb->live;
     }
+    if ((rc = flush_complete(sv, si))) return rc;  // no iterations this step
     // 5. retire finished frames, in the order they were generated
     if (sv->live == 0 && sv->pending.empty())  // every generated path has ended
         for (auto& k : sv->inflight) k.done_iter = std::min<int64_t>(k.done_iter, sv->iters);
@@ -1576,7 +1595,7 @@ int wf_server_step(wf_server* sv, wf_server_step_info* info)
         }
     }
     sv->inflight.swap(keep);
-    if ((rc = flush_finished(sv, si))) return rc;
+    if ((rc = flush_begin(sv))) return rc;
     si.queued = (int32_t)sv->queue.size();
     si.running = (int32_t)sv->running;
     si.budget_used_bytes = sv->wave_bytes + 4 * (sv->alloc.used + sv->frames.used);
@@ -1608,6 +1627,11 @@ int wf_server_image(wf_server* sv, int64_t id, float* image, int64_t nf)
     if (!jp) return set_err(sv->c, WF_ERR_INVALID_ARGUMENT, "no such job");
     ServedJob& j = *jp;
     if (nf < j.accum_floats) return set_err(sv->c, WF_ERR_CAPACITY, "image buffer too small");
+    if (j.flushing) {
+        wf_server_step_info si{};
+        const int rc = flush_complete(sv, si);
+        if (rc) return rc;
+    }
     if (j.state == WF_JOB_DONE) {
         std::memcpy(image, j.final_image.data(), sizeof(float) * j.accum_floats);
         return WF_OK;
@@ -1633,6 +1657,10 @@ int wf_server_cancel(wf_server* sv, int64_t id)
     ServedJob* jp = sv->jobs.find(id);
     if (!jp) return set_err(sv->c, WF_ERR_INVALID_ARGUMENT, "no such job");
     ServedJob& j = *jp;
+    if (j.flushing) {  // every frame has finished: the job completes
+        wf_server_step_info si{};
+        return flush_complete(sv, si);
+    }
     if (j.state == WF_JOB_RUNNING) {
         // frames not started yet are dropped; frames already generating run
         // to their end and are discarded (their paths are in the queue)
