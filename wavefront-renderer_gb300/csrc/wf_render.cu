@@ -266,7 +266,9 @@ __global__ void __launch_bounds__(128) k_occluded_api(DeviceScene S, int64_t n, 
 // occluders are the two boxes standing on the surfaces that cast the shadow
 // rays (Cornell box -1.1%, batched Cornell variants -2.8%); single-job
 // renders of scenes from kFarFirstTriangles on use it (a kernel instance of
-// its own: as a launch argument the choice cost the dense mesh 0.7%).
+// its own: as a launch argument the choice cost the dense mesh 0.7%), and so
+// do multi-job waves over a dense scene (served stream with dense-mesh jobs
+// among Cornell-box ones: +1.7% device rate).
 constexpr int kFarFirstTriangles = 4096;
 using TraversalFar = Traversal<true, true>;
 using Traversal4Far = Traversal4<true, true>;
@@ -1676,7 +1678,9 @@ void launch_compact_hits(const WaveTables& t, RayQueueDev rq, const ull* d_n, Hi
 void launch_occluded_render(const WaveTables& t, ShadowQueueDev sh, const ull* sh_n, float* accum, ull* work,
                             int* err, LaunchCfg cfg, cudaStream_t s)
 {
-    const bool far_first = !t.multi && t.scene0.num_tris >= kFarFirstTriangles;
+    // farther child first where a dense scene's rays are in the queue: single
+    // scenes from kFarFirstTriangles on, multi-job waves over a dense scene
+    const bool far_first = t.multi ? cfg.max_scene_bytes >= kDenseSceneBytes : t.scene0.num_tris >= kFarFirstTriangles;
     cfg = multi_job_occupancy(t, cfg);
 #define WF_OCC(M, B, T)                                                                                       \
     k_occluded_render<M, B, T><<<cfg.grid, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, sh, sh_n, accum, work, \
@@ -1684,13 +1688,16 @@ void launch_occluded_render(const WaveTables& t, ShadowQueueDev sh, const ull* s
 #define WF_OCC2(M, T) \
     if (cfg.variant == 1) WF_OCC(M, 9, T); else WF_OCC(M, 1, T)
     if (t.tree == kTreeFour) {
-        if (t.multi) { WF_OCC2(true, Traversal4<true>); }
-        else if (far_first) { WF_OCC2(false, Traversal4Far); }
+        if (t.multi) {
+            if (far_first) { WF_OCC2(true, Traversal4Far); } else { WF_OCC2(true, Traversal4<true>); }
+        } else if (far_first) { WF_OCC2(false, Traversal4Far); }
         else { WF_OCC2(false, Traversal4<true>); }
+    } else if (t.multi) {
+        if (far_first) { WF_OCC2(true, TraversalFar); } else { WF_OCC2(true, Traversal<true>); }
     } else if (far_first) {
         WF_OCC2(false, TraversalFar);
     } else {
-        if (t.multi) { WF_OCC2(true, Traversal<true>); } else { WF_OCC2(false, Traversal<true>); }
+        WF_OCC2(false, Traversal<true>);
     }
 #undef WF_OCC2
 #undef WF_OCC
