@@ -232,6 +232,37 @@ def test_server_mixes_textured_and_plain_scenes(wf, ctx, scene_c2small):
     assert _same(imgs[-1], alone) >= 0.999
 
 
+@pytest.mark.parametrize("ask", ["image", "cancel"])
+def test_server_hands_over_a_finished_job_on_request(wf, ctx, ask):
+    """After the step in which a job's last frame ends, the job still counts as
+    running (its image is being copied out); wf_server_image hands it over at
+    once, and wf_server_cancel finds it complete, not cancelled."""
+    jobs, hosts = _jobs(wf, ctx, 1, seed0=950)
+    j, hs = jobs[0], hosts[0]
+    j.samples_per_pixel = 8
+    srv = wf.Server(ctx, hbm_budget_bytes=64 << 20, frame_spp=4, max_paths_per_wave=1 << 16)
+    try:
+        jid = srv.submit(j)
+        img = None
+        for _ in range(100):
+            info = srv.step()
+            st = srv.status(jid)
+            if st["state"] == wf.JOB_RUNNING and st["samples_done"] == 8:
+                if ask == "cancel":
+                    srv.cancel(jid)
+                img = srv.image(jid, j.width, j.height)
+                assert srv.status(jid)["state"] == wf.JOB_DONE
+                break
+            if info["running"] == 0 and info["queued"] == 0:
+                break
+        assert img is not None  # the job was seen between its last frame and its hand-over
+        ctx.upload(hs.desc)
+        alone, _ = ctx.render(wf.render_params(j.width, j.height, 8, j.max_depth, j.camera, seed=j.seed_lo))
+        assert _same(img, alone) >= 0.999
+    finally:
+        srv.close()
+
+
 def test_server_cancel(wf, ctx):
     jobs, hosts = _jobs(wf, ctx, 3, seed0=900)
     srv = wf.Server(ctx, hbm_budget_bytes=64 << 20, frame_spp=2, max_paths_per_wave=1 << 14)
