@@ -1627,7 +1627,7 @@ int wf_server_image(wf_server* sv, int64_t id, float* image, int64_t nf)
     if (!jp) return set_err(sv->c, WF_ERR_INVALID_ARGUMENT, "no such job");
     ServedJob& j = *jp;
     if (nf < j.accum_floats) return set_err(sv->c, WF_ERR_CAPACITY, "image buffer too small");
-    if (j.flushing) {
+    if (!sv->flushing.empty()) {  // this job's image, or a copy out of tmp that must end before tmp is reused
         wf_server_step_info si{};
         const int rc = flush_complete(sv, si);
         if (rc) return rc;
