@@ -562,7 +562,7 @@ __global__ void k_cost_update(CostTrackerDev mat, CostTrackerDev tex, int repeat
 // roulette and the next ray.  Random streams per (purpose, depth, pixel,
 // sample) — the oracle uses the same ones.
 // ---------------------------------------------------------------------------
-constexpr int kShadeWarps = 4;  // k_shade runs 128-thread blocks
+constexpr int kShadeWarps = 4;  // k_shade's grid is sized in 128-thread blocks
 // Resident blocks of k_shade per SM: the multi-job and cost-timed instances,
 // and the plain single-job instance, each bounded where it still compiles
 // without spills.
@@ -572,6 +572,35 @@ constexpr int kShadeWarps = 4;  // k_shade runs 128-thread blocks
 #ifndef WF_SHADE_MIN_BLOCKS_PLAIN
 #define WF_SHADE_MIN_BLOCKS_PLAIN 8
 #endif
+// Warps per block of each k_shade form.  The octant grouping of the next rays
+// spans a block, and the single-job forms that group run 512-thread blocks
+// (against 128: dense mesh +1.3%, lattice +3.4%; 256: dense mesh the same,
+// lattice -1.3%).  The multi-job grouped forms stay at 128 (256 threads at 3
+// resident blocks: served stream -12%), and so do the plain forms (256:
+// Cornell box -1%).
+#ifndef WF_GROUP_WARPS
+#define WF_GROUP_WARPS 16
+#endif
+#ifndef WF_GROUP_WARPS_MULTI
+#define WF_GROUP_WARPS_MULTI 4
+#endif
+#ifndef WF_PLAIN_WARPS
+#define WF_PLAIN_WARPS 4
+#endif
+template <bool kMulti, bool kTimed, bool kGroup>
+__host__ __device__ constexpr int shade_warps()
+{
+    return (kMulti || kTimed) ? (kGroup ? WF_GROUP_WARPS_MULTI : kShadeWarps) : (kGroup ? WF_GROUP_WARPS : WF_PLAIN_WARPS);
+}
+template <bool kMulti, bool kTimed, bool kGroup>
+__host__ __device__ constexpr int shade_min_blocks()
+{
+    return ((kMulti || kTimed) ? WF_SHADE_MIN_BLOCKS : WF_SHADE_MIN_BLOCKS_PLAIN) * kShadeWarps /
+                       shade_warps<kMulti, kTimed, kGroup>() > 0
+               ? ((kMulti || kTimed) ? WF_SHADE_MIN_BLOCKS : WF_SHADE_MIN_BLOCKS_PLAIN) * kShadeWarps /
+                     shade_warps<kMulti, kTimed, kGroup>()
+               : 1;
+}
 // kTimed: the live CostTracker times a quarter of the hits (single-job
 // renders only); the other instances carry no clock reads.  kLean: a
 // single-job render of a scene without an environment map, textures or a
@@ -580,7 +609,8 @@ constexpr int kShadeWarps = 4;  // k_shade runs 128-thread blocks
 // kernel that waits less on the instruction cache (dense mesh +0.9%,
 // Cornell box +1.7% for the environment block alone).
 template <bool kMulti, bool kTimed, bool kLean = false, bool kGroup = false>
-__global__ void __launch_bounds__(128, (kMulti || kTimed) ? WF_SHADE_MIN_BLOCKS : WF_SHADE_MIN_BLOCKS_PLAIN)
+__global__ void __launch_bounds__(32 * shade_warps<kMulti, kTimed, kGroup>(),
+                                  shade_min_blocks<kMulti, kTimed, kGroup>())
     k_shade(DeviceScene scene0, DeviceJob job0,
                                                const DeviceScene* __restrict__ scenes,
                                                const DeviceJob* __restrict__ jobs, RayQueueDev rq,
@@ -590,10 +620,11 @@ __global__ void __launch_bounds__(128, (kMulti || kTimed) ? WF_SHADE_MIN_BLOCKS 
 {
     // hq.ray lists the rays that hit; their records (tri, t, u, v) sit at the
     // list position, or with ray_order at the ray's own index.
-    __shared__ unsigned blk_sh[kShadeWarps], blk_nx[kShadeWarps];
-    __shared__ unsigned blk_oct[8 * kShadeWarps];  // next rays per (octant, warp), octant-major
+    constexpr int kW = shade_warps<kMulti, kTimed, kGroup>();
+    __shared__ unsigned blk_sh[kW], blk_nx[kW];
+    __shared__ unsigned blk_oct[8 * kW];  // next rays per (octant, warp), octant-major
     __shared__ ull blk_first[2];
-    static_assert(8 * kShadeWarps == 32, "one scan lane per (octant, warp)");
+    static_assert(8 * kW == 32 || 8 * kW == 64 || 8 * kW == 128, "one, two or four scan entries per lane");
     const int64_t n = (int64_t)*hq_n;
     WF_BLOCK_LOOP(base, n)
     {
@@ -814,22 +845,33 @@ __global__ void __launch_bounds__(128, (kMulti || kTimed) ? WF_SHADE_MIN_BLOCKS 
                 return mn & ~((b0 ^ (0u - (o & 1u))) | (b1 ^ (0u - ((o >> 1) & 1u))) | (b2 ^ (0u - ((o >> 2) & 1u))));
             };
             const unsigned oct_rank = (unsigned)__popc(peers(oct) & lt);
-            if (lane < 8) blk_oct[lane * kShadeWarps + warp] = (unsigned)__popc(peers((unsigned)lane));
+            if (lane < 8) blk_oct[lane * kW + warp] = (unsigned)__popc(peers((unsigned)lane));
             if (lane == 0) blk_sh[warp] = (unsigned)(__popc(ma) + __popc(md) + __popc(me));
             __syncthreads();
             if (warp == 0) {
-                const unsigned v = blk_oct[lane];
+                constexpr int kPer = 8 * kW / 32;  // entries per lane
+                unsigned e[kPer], v = 0;
+#pragma unroll
+                for (int q = 0; q < kPer; ++q) {
+                    e[q] = blk_oct[kPer * lane + q];
+                    v += e[q];
+                }
                 unsigned x = v;
 #pragma unroll
                 for (int dd = 1; dd < 32; dd <<= 1) {
                     const unsigned y = __shfl_up_sync(0xFFFFFFFFu, x, dd);
                     if (lane >= dd) x += y;
                 }
-                blk_oct[lane] = x - v;
+                unsigned ex = x - v;
+#pragma unroll
+                for (int q = 0; q < kPer; ++q) {
+                    blk_oct[kPer * lane + q] = ex;
+                    ex += e[q];
+                }
                 const unsigned tn = __shfl_sync(0xFFFFFFFFu, x, 31);
                 if (lane == 0) {
                     unsigned ts = 0;
-                    for (int w = 0; w < kShadeWarps; ++w) {
+                    for (int w = 0; w < kW; ++w) {
                         const unsigned a = blk_sh[w];
                         blk_sh[w] = ts;
                         ts += a;
@@ -840,7 +882,7 @@ __global__ void __launch_bounds__(128, (kMulti || kTimed) ? WF_SHADE_MIN_BLOCKS 
             }
             __syncthreads();
             sh0 = (int64_t)blk_first[0] + blk_sh[warp];
-            pn = (int64_t)blk_first[1] + blk_oct[(want_next ? oct : 0u) * kShadeWarps + warp] + oct_rank;
+            pn = (int64_t)blk_first[1] + blk_oct[(want_next ? oct : 0u) * kW + warp] + oct_rank;
         } else {
             const unsigned mn = __ballot_sync(0xFFFFFFFFu, want_next);
             if (lane == 0) {
@@ -850,7 +892,7 @@ __global__ void __launch_bounds__(128, (kMulti || kTimed) ? WF_SHADE_MIN_BLOCKS 
             __syncthreads();
             if (threadIdx.x == 0) {
                 unsigned ts = 0, tn = 0;
-                for (int w = 0; w < kShadeWarps; ++w) {
+                for (int w = 0; w < kW; ++w) {
                     const unsigned a = blk_sh[w], b = blk_nx[w];
                     blk_sh[w] = ts;
                     blk_nx[w] = tn;
@@ -1641,11 +1683,15 @@ void launch_shade(const WaveTables& t, RayQueueDev rq, HitQueueDev hq, const ull
 #define WF_SHADE(M, T, L, GRID)                                                                                   \
     do {                                                                                                          \
         if (group)                                                                                                \
-            k_shade<M, T, L, true><<<GRID, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, hq, hq_n,         \
-                                                        cfg.ray_order, sh, sh_n, next, next_n, accum, err);       \
+            k_shade<M, T, L, true><<<std::max(1, (GRID) * kShadeWarps / shade_warps<M, T, true>()),             \
+                                     32 * shade_warps<M, T, true>(), 0, s>>>(                                     \
+                t.scene0, t.job0, t.scenes, t.jobs, rq, hq, hq_n, cfg.ray_order, sh, sh_n, next, next_n, accum,   \
+                err);                                                                                             \
         else                                                                                                      \
-            k_shade<M, T, L, false><<<GRID, 128, 0, s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, hq, hq_n,        \
-                                                         cfg.ray_order, sh, sh_n, next, next_n, accum, err);      \
+            k_shade<M, T, L, false><<<std::max(1, (GRID) * kShadeWarps / shade_warps<M, T, false>()),            \
+                                      32 * shade_warps<M, T, false>(), 0, s>>>(                                   \
+                t.scene0, t.job0, t.scenes, t.jobs, rq, hq, hq_n, cfg.ray_order, sh, sh_n, next, next_n, accum,   \
+                err);                                                                                             \
     } while (0)
     if (t.multi && cfg.lean_multi)  // every resident scene fits the lean instance
         WF_SHADE(true, false, true, grid);
