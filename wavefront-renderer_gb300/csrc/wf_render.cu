@@ -624,7 +624,7 @@ __global__ void __launch_bounds__(32 * shade_warps<kMulti, kTimed, kGroup>(),
     __shared__ unsigned blk_sh[kW], blk_nx[kW];
     __shared__ unsigned blk_oct[8 * kW];  // next rays per (octant, warp), octant-major
     __shared__ ull blk_first[2];
-    static_assert(8 * kW == 32 || 8 * kW == 64 || 8 * kW == 128, "one, two or four scan entries per lane");
+    static_assert(8 * kW == 32 || 8 * kW == 64 || 8 * kW == 128 || 8 * kW == 256, "1, 2, 4 or 8 scan entries per lane");
     const int64_t n = (int64_t)*hq_n;
     WF_BLOCK_LOOP(base, n)
     {
