@@ -573,33 +573,24 @@ constexpr int kShadeWarps = 4;  // k_shade's grid is sized in 128-thread blocks
 #define WF_SHADE_MIN_BLOCKS_PLAIN 8
 #endif
 // Warps per block of each k_shade form.  The octant grouping of the next rays
-// spans a block, and the single-job forms that group run 512-thread blocks
-// (against 128: dense mesh +1.3%, lattice +3.4%; 256: dense mesh the same,
-// lattice -1.3%).  The multi-job grouped forms stay at 128 (256 threads at 3
-// resident blocks: served stream -12%), and so do the plain forms (256:
-// Cornell box -1%).
-#ifndef WF_GROUP_WARPS
-#define WF_GROUP_WARPS 16
-#endif
-#ifndef WF_GROUP_WARPS_MULTI
-#define WF_GROUP_WARPS_MULTI 4
-#endif
-#ifndef WF_PLAIN_WARPS
-#define WF_PLAIN_WARPS 4
-#endif
-template <bool kMulti, bool kTimed, bool kGroup>
+// spans a block, so the forms that group run larger blocks (the same threads
+// per SM): the single-job ones 512 threads (against 128: dense mesh +1.3%,
+// lattice +3.4%; 256: dense mesh the same, lattice -1.3%; 1024: dense mesh
+// -0.3%), the lean multi-job one 256 threads at 4 blocks per SM, where it
+// still needs no spills (served stream +0.7%).  The other multi-job and the
+// cost-timed grouped forms need more than 64 registers and stay at 128, and
+// so do the plain forms (256: Cornell box -1%).
+template <bool kMulti, bool kTimed, bool kLean, bool kGroup>
 __host__ __device__ constexpr int shade_warps()
 {
-    return (kMulti || kTimed) ? (kGroup ? WF_GROUP_WARPS_MULTI : kShadeWarps) : (kGroup ? WF_GROUP_WARPS : WF_PLAIN_WARPS);
+    return !kGroup ? kShadeWarps : kTimed ? kShadeWarps : !kMulti ? 16 : kLean ? 8 : kShadeWarps;
 }
-template <bool kMulti, bool kTimed, bool kGroup>
+template <bool kMulti, bool kTimed, bool kLean, bool kGroup>
 __host__ __device__ constexpr int shade_min_blocks()
 {
-    return ((kMulti || kTimed) ? WF_SHADE_MIN_BLOCKS : WF_SHADE_MIN_BLOCKS_PLAIN) * kShadeWarps /
-                       shade_warps<kMulti, kTimed, kGroup>() > 0
-               ? ((kMulti || kTimed) ? WF_SHADE_MIN_BLOCKS : WF_SHADE_MIN_BLOCKS_PLAIN) * kShadeWarps /
-                     shade_warps<kMulti, kTimed, kGroup>()
-               : 1;
+    return shade_warps<kMulti, kTimed, kLean, kGroup>() == kShadeWarps
+               ? ((kMulti || kTimed) ? WF_SHADE_MIN_BLOCKS : WF_SHADE_MIN_BLOCKS_PLAIN)
+               : 2048 / (32 * shade_warps<kMulti, kTimed, kLean, kGroup>()) / 2;  // 64 registers a thread
 }
 // kTimed: the live CostTracker times a quarter of the hits (single-job
 // renders only); the other instances carry no clock reads.  kLean: a
@@ -609,8 +600,8 @@ __host__ __device__ constexpr int shade_min_blocks()
 // kernel that waits less on the instruction cache (dense mesh +0.9%,
 // Cornell box +1.7% for the environment block alone).
 template <bool kMulti, bool kTimed, bool kLean = false, bool kGroup = false>
-__global__ void __launch_bounds__(32 * shade_warps<kMulti, kTimed, kGroup>(),
-                                  shade_min_blocks<kMulti, kTimed, kGroup>())
+__global__ void __launch_bounds__(32 * shade_warps<kMulti, kTimed, kLean, kGroup>(),
+                                  shade_min_blocks<kMulti, kTimed, kLean, kGroup>())
     k_shade(DeviceScene scene0, DeviceJob job0,
                                                const DeviceScene* __restrict__ scenes,
                                                const DeviceJob* __restrict__ jobs, RayQueueDev rq,
@@ -620,7 +611,7 @@ __global__ void __launch_bounds__(32 * shade_warps<kMulti, kTimed, kGroup>(),
 {
     // hq.ray lists the rays that hit; their records (tri, t, u, v) sit at the
     // list position, or with ray_order at the ray's own index.
-    constexpr int kW = shade_warps<kMulti, kTimed, kGroup>();
+    constexpr int kW = shade_warps<kMulti, kTimed, kLean, kGroup>();
     __shared__ unsigned blk_sh[kW], blk_nx[kW];
     __shared__ unsigned blk_oct[8 * kW];  // next rays per (octant, warp), octant-major
     __shared__ ull blk_first[2];
@@ -1671,6 +1662,28 @@ int shade_blocks_per_sm(bool plain)
 // equal share; its grid is therefore one full wave of resident blocks.  A grid
 // that is not a multiple of them (16 blocks per SM against 6 resident: 2.67
 // waves) leaves a partial last wave whose blocks start late and end late.
+// One full wave of resident blocks of a grouped k_shade form (its block
+// size differs from the 128 threads the context's shade grids count), from
+// the occupancy calculator; fallback: the 128-thread grid scaled to the block.
+template <bool M, bool T, bool L>
+static int grouped_shade_grid(int grid128)
+{
+    static int grid = 0;
+    if (grid == 0) {
+        int dev = 0, sms = 0, occ = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_shade<M, T, L, true>, 32 * shade_warps<M, T, L, true>(),
+                                                          0) != cudaSuccess ||
+            occ <= 0 || sms <= 0) {
+            cudaGetLastError();
+            return std::max(1, grid128 * kShadeWarps / shade_warps<M, T, L, true>());
+        }
+        grid = occ * sms;
+    }
+    return grid;
+}
+
 void launch_shade(const WaveTables& t, RayQueueDev rq, HitQueueDev hq, const ull* hq_n, ShadowQueueDev sh,
                   ull* sh_n, RayQueueDev next, ull* next_n, float* accum, int* err, LaunchCfg cfg, cudaStream_t s)
 {
@@ -1683,13 +1696,11 @@ void launch_shade(const WaveTables& t, RayQueueDev rq, HitQueueDev hq, const ull
 #define WF_SHADE(M, T, L, GRID)                                                                                   \
     do {                                                                                                          \
         if (group)                                                                                                \
-            k_shade<M, T, L, true><<<std::max(1, (GRID) * kShadeWarps / shade_warps<M, T, true>()),             \
-                                     32 * shade_warps<M, T, true>(), 0, s>>>(                                     \
+            k_shade<M, T, L, true><<<grouped_shade_grid<M, T, L>(GRID), 32 * shade_warps<M, T, L, true>(), 0, s>>>( \
                 t.scene0, t.job0, t.scenes, t.jobs, rq, hq, hq_n, cfg.ray_order, sh, sh_n, next, next_n, accum,   \
                 err);                                                                                             \
         else                                                                                                      \
-            k_shade<M, T, L, false><<<std::max(1, (GRID) * kShadeWarps / shade_warps<M, T, false>()),            \
-                                      32 * shade_warps<M, T, false>(), 0, s>>>(                                   \
+            k_shade<M, T, L, false><<<GRID, 32 * kShadeWarps, 0, s>>>(                                           \
                 t.scene0, t.job0, t.scenes, t.jobs, rq, hq, hq_n, cfg.ray_order, sh, sh_n, next, next_n, accum,   \
                 err);                                                                                             \
     } while (0)
