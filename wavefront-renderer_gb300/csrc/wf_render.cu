@@ -572,18 +572,21 @@ constexpr int kShadeWarps = 4;  // k_shade's grid is sized in 128-thread blocks
 #ifndef WF_SHADE_MIN_BLOCKS_PLAIN
 #define WF_SHADE_MIN_BLOCKS_PLAIN 8
 #endif
-// Warps per block of each k_shade form.  The octant grouping of the next rays
-// spans a block, so the forms that group run larger blocks (the same threads
-// per SM): the single-job ones 512 threads (against 128: dense mesh +1.3%,
+// Warps per block of each k_shade form (the same threads per SM whatever the
+// block).  The octant grouping of the next rays spans a block, and the warps
+// of a larger block walk the large kernel together, sharing its instruction
+// cache lines (no_instruction stalls 3.1 -> 0.5 per issue at 512 threads).
+// The single-job grouped forms run 512 threads (against 128: dense mesh +1.3%,
 // lattice +3.4%; 256: dense mesh the same, lattice -1.3%; 1024: dense mesh
-// -0.3%), the lean multi-job one 256 threads at 4 blocks per SM, where it
-// still needs no spills (served stream +0.7%).  The other multi-job and the
-// cost-timed grouped forms need more than 64 registers and stay at 128, and
-// so do the plain forms (256: Cornell box -1%).
+// -0.3%); the lean multi-job forms 256 threads at 4 blocks per SM, where they
+// still need no spills (served stream +0.7%, batched Cornell jobs +1.9%).
+// The other multi-job and the cost-timed forms need more than 64 registers
+// and stay at 128, and so does the plain single-job form, whose barrier waits
+// cost more than its cache gains (256: Cornell box -1%, 512: -3%).
 template <bool kMulti, bool kTimed, bool kLean, bool kGroup>
 __host__ __device__ constexpr int shade_warps()
 {
-    return !kGroup ? kShadeWarps : kTimed ? kShadeWarps : !kMulti ? 16 : kLean ? 8 : kShadeWarps;
+    return kTimed ? kShadeWarps : !kMulti ? (kGroup ? 16 : kShadeWarps) : kLean ? 8 : kShadeWarps;
 }
 template <bool kMulti, bool kTimed, bool kLean, bool kGroup>
 __host__ __device__ constexpr int shade_min_blocks()
@@ -1662,22 +1665,23 @@ int shade_blocks_per_sm(bool plain)
 // equal share; its grid is therefore one full wave of resident blocks.  A grid
 // that is not a multiple of them (16 blocks per SM against 6 resident: 2.67
 // waves) leaves a partial last wave whose blocks start late and end late.
-// One full wave of resident blocks of a grouped k_shade form (its block
-// size differs from the 128 threads the context's shade grids count), from
-// the occupancy calculator; fallback: the 128-thread grid scaled to the block.
-template <bool M, bool T, bool L>
-static int grouped_shade_grid(int grid128)
+// One full wave of resident blocks of a k_shade form: the context's grid
+// counts 128-thread blocks; a form with other blocks takes its own from the
+// occupancy calculator (fallback: the 128-thread grid scaled to its block).
+template <bool M, bool T, bool L, bool G>
+static int shade_grid(int grid128)
 {
+    if (shade_warps<M, T, L, G>() == kShadeWarps) return grid128;
     static int grid = 0;
     if (grid == 0) {
         int dev = 0, sms = 0, occ = 0;
         if (cudaGetDevice(&dev) != cudaSuccess ||
             cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_shade<M, T, L, true>, 32 * shade_warps<M, T, L, true>(),
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_shade<M, T, L, G>, 32 * shade_warps<M, T, L, G>(),
                                                           0) != cudaSuccess ||
             occ <= 0 || sms <= 0) {
             cudaGetLastError();
-            return std::max(1, grid128 * kShadeWarps / shade_warps<M, T, L, true>());
+            return std::max(1, grid128 * kShadeWarps / shade_warps<M, T, L, G>());
         }
         grid = occ * sms;
     }
@@ -1696,13 +1700,13 @@ void launch_shade(const WaveTables& t, RayQueueDev rq, HitQueueDev hq, const ull
 #define WF_SHADE(M, T, L, GRID)                                                                                   \
     do {                                                                                                          \
         if (group)                                                                                                \
-            k_shade<M, T, L, true><<<grouped_shade_grid<M, T, L>(GRID), 32 * shade_warps<M, T, L, true>(), 0, s>>>( \
+            k_shade<M, T, L, true><<<shade_grid<M, T, L, true>(GRID), 32 * shade_warps<M, T, L, true>(), 0, s>>>( \
                 t.scene0, t.job0, t.scenes, t.jobs, rq, hq, hq_n, cfg.ray_order, sh, sh_n, next, next_n, accum,   \
                 err);                                                                                             \
         else                                                                                                      \
-            k_shade<M, T, L, false><<<GRID, 32 * kShadeWarps, 0, s>>>(                                           \
-                t.scene0, t.job0, t.scenes, t.jobs, rq, hq, hq_n, cfg.ray_order, sh, sh_n, next, next_n, accum,   \
-                err);                                                                                             \
+            k_shade<M, T, L, false><<<shade_grid<M, T, L, false>(GRID), 32 * shade_warps<M, T, L, false>(), 0,    \
+                                      s>>>(t.scene0, t.job0, t.scenes, t.jobs, rq, hq, hq_n, cfg.ray_order, sh,   \
+                                           sh_n, next, next_n, accum, err);                                       \
     } while (0)
     if (t.multi && cfg.lean_multi)  // every resident scene fits the lean instance
         WF_SHADE(true, false, true, grid);
