@@ -578,15 +578,17 @@ constexpr int kShadeWarps = 4;  // k_shade's grid is sized in 128-thread blocks
 // cache lines (no_instruction stalls 3.1 -> 0.5 per issue at 512 threads).
 // The single-job grouped forms run 512 threads (against 128: dense mesh +1.3%,
 // lattice +3.4%; 256: dense mesh the same, lattice -1.3%; 1024: dense mesh
-// -0.3%); the lean multi-job forms 256 threads at 4 blocks per SM, where they
-// still need no spills (served stream +0.7%, batched Cornell jobs +1.9%).
-// The other multi-job and the cost-timed forms need more than 64 registers
-// and stay at 128, and so does the plain single-job form, whose barrier waits
-// cost more than its cache gains (256: Cornell box -1%, 512: -3%).
+// -0.3%), the cost-timed one too although its 72 registers then spill (dense
+// mesh with live cost-aware RR +4.0%); the lean multi-job forms 256 threads at
+// 4 blocks per SM, where they still need no spills (served stream +0.7%,
+// batched Cornell jobs +1.9%; 512: batched -2%).  The other multi-job forms
+// need 72 registers and stay at 128, and so does the plain single-job form,
+// whose barrier waits cost more than its cache gains (256: Cornell box -1%,
+// 512: -3%).
 template <bool kMulti, bool kTimed, bool kLean, bool kGroup>
 __host__ __device__ constexpr int shade_warps()
 {
-    return kTimed ? kShadeWarps : !kMulti ? (kGroup ? 16 : kShadeWarps) : kLean ? 8 : kShadeWarps;
+    return !kMulti ? (kGroup ? 16 : kShadeWarps) : kLean ? 8 : kShadeWarps;
 }
 template <bool kMulti, bool kTimed, bool kLean, bool kGroup>
 __host__ __device__ constexpr int shade_min_blocks()
