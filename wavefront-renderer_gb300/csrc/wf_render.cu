@@ -1669,7 +1669,8 @@ int shade_blocks_per_sm(bool plain)
 // waves) leaves a partial last wave whose blocks start late and end late.
 // One full wave of resident blocks of a k_shade form: the context's grid
 // counts 128-thread blocks; a form with other blocks takes its own from the
-// occupancy calculator (fallback: the 128-thread grid scaled to its block).
+// occupancy calculator (fallback: the 128-thread grid scaled to its block),
+// computed once per process (the devices of one process are one GPU model).
 template <bool M, bool T, bool L, bool G>
 static int shade_grid(int grid128)
 {
